@@ -1,0 +1,156 @@
+"""ctypes front end of the oracle (oracle/xmd_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
+CPU-baseline leg of bench.py, never by the product.  ``OrcSim`` wraps numpy
+arrays in the reference's own bead-major order; see xmd_oracle.h.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = None
+
+TRAP_HARMONIC, TRAP_HARMONIC_2, TRAP_NEG_HARMONIC = 1, 2, 3
+PAIR_GAUSSIAN, PAIR_PERIODIC_GAUSSIAN, PAIR_COULOMB, PAIR_PERIODIC_COULOMB, PAIR_EWALD = 1, 2, 3, 4, 5
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+
+
+class _Sim(C.Structure):
+    _fields_ = [("D", C.c_int), ("L", C.c_int), ("nb", C.c_int), ("m", _dp), ("x", _dp),
+                ("v", _dp), ("f", _dp), ("nf", C.c_int), ("cf", _ip), ("theta", _dp),
+                ("vtheta", _dp), ("Q", _dp), ("T", C.c_double), ("box", C.c_double * 3)]
+
+
+class Params(C.Structure):
+    _fields_ = [("trap_w", C.c_double), ("trap_w2", C.c_double * 3), ("trap_c", C.c_double * 3),
+                ("gauss_g", C.c_double), ("gauss_s", C.c_double), ("coul_s", C.c_double),
+                ("coul_alpha", C.c_double), ("coul_nsum", C.c_int)]
+
+
+class StepCfg(C.Structure):
+    _fields_ = [("N", C.c_int), ("P", C.c_int), ("beta", C.c_double), ("vi", C.c_double),
+                ("omegaP", C.c_double), ("image", C.c_int), ("trap_kind", C.c_int),
+                ("pair_kind", C.c_int), ("pbc", C.c_int), ("prm", Params)]
+
+
+def build():
+    """Compile liborc.so with oracle/Makefile (gcc only)."""
+    subprocess.run(["make", "-s", "-C", HERE, "liborc.so"], check=True)
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        path = os.path.join(HERE, "liborc.so")
+        src = os.path.join(HERE, "xmd_oracle.c")
+        if not os.path.exists(path) or os.path.getmtime(path) < os.path.getmtime(src):
+            build()
+        L = C.CDLL(path)
+        d, i, vp = C.c_double, C.c_int, C.c_void_p
+        sig = {
+            "orc_minimum_image": (d, [d, d]),
+            "orc_reset_force": (None, [vp]),
+            "orc_nhc_vv3_1": (i, [vp, d]),
+            "orc_nhc_vv3_2": (i, [vp, d]),
+            "orc_periodic_boundary": (None, [vp]),
+            "orc_fast_fill_ENk": (i, [vp, i, i, d, i, _dp, _dp]),
+            "orc_fill_ENk_cubic": (i, [vp, i, i, d, i, _dp]),
+            "orc_fill_VB": (i, [i, d, d, _dp, _dp]),
+            "orc_fast_force_VB": (i, [vp, i, i, d, d, d, i, _dp, _dp, _dp, _dp]),
+            "orc_force_VB_cubic": (i, [vp, i, i, d, d, d, i, _dp, _dp]),
+            "orc_trap_force": (i, [vp, i, i, i, vp]),
+            "orc_pair_force": (i, [vp, i, i, i, vp]),
+            "orc_pair_force_one": (None, [i, vp, i, _dp, _dp, _dp, _dp, d]),
+            "orc_vbn_energy": (d, [i, i, i, d, d, _dp, _dp]),
+            "orc_fast_fill_ENk2": (i, [vp, i, i, d, i, _dp]),
+            "orc_fill_ENk2_cubic": (i, [vp, i, i, d, i, _dp]),
+            "orc_vi_virial_energy": (d, [vp, i, i, d, d, i, _dp, _dp, _dp]),
+            "orc_trap_energy": (d, [vp, i, i, i, vp]),
+            "orc_pair_energy": (d, [vp, i, i, i, vp]),
+            "orc_pair_energy_one": (d, [i, vp, i, _dp, _dp, _dp]),
+            "orc_madelung": (d, [_dp, vp]),
+            "orc_vi_sign": (d, [i, d, d, d, _dp, _dp]),
+            "orc_step": (i, [vp, vp, d, _dp, _dp, _dp]),
+            "orc_set_seed": (None, [C.c_uint]),
+            "orc_random_uniform": (d, [d, d]),
+            "orc_random_gaussian": (d, []),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _LIB = L
+    return _LIB
+
+
+def ptr(a, ct=C.c_double):
+    return a.ctypes.data_as(C.POINTER(ct))
+
+
+def ntri(n):
+    return n * (n + 1) // 2
+
+
+class OrcSim:
+    """Simulation state held in numpy arrays, shared with the C oracle."""
+
+    def __init__(self, D, L, nb, m, x, v, f, cf, theta, vtheta, Q, T, box):
+        self.D, self.L, self.nb = D, L, nb
+        self.m = np.ascontiguousarray(m, dtype=np.float64).copy()
+        self.x = np.ascontiguousarray(x, dtype=np.float64).copy()
+        self.v = np.ascontiguousarray(v, dtype=np.float64).copy()
+        self.f = np.ascontiguousarray(f, dtype=np.float64).copy()
+        self.cf = np.ascontiguousarray(cf, dtype=np.int32).copy()
+        self.theta = np.ascontiguousarray(theta, dtype=np.float64).copy()
+        self.vtheta = np.ascontiguousarray(vtheta, dtype=np.float64).copy()
+        self.Q = np.ascontiguousarray(Q, dtype=np.float64).copy()
+        self.s = _Sim(D, L, nb, ptr(self.m), ptr(self.x), ptr(self.v), ptr(self.f),
+                      len(self.cf), ptr(self.cf, C.c_int), ptr(self.theta), ptr(self.vtheta),
+                      ptr(self.Q), float(T), (C.c_double * 3)(*(list(box) + [0.0] * 3)[:3]))
+
+    @property
+    def ref(self):
+        return C.byref(self.s)
+
+    @classmethod
+    def from_fixture(cls, fx, prefix="init/"):
+        from_h = fx["hdr"]
+        D, L, N, P = int(from_h[0]), int(from_h[1]), int(from_h[2]), int(from_h[3])
+        T, box = from_h[9], from_h[10]
+        return cls(D, L, N * P, fx["m"], fx[prefix + "x"], fx[prefix + "v"], fx[prefix + "f"],
+                   fx[prefix + "cf"], fx[prefix + "theta"], fx[prefix + "vtheta"], fx[prefix + "Q"],
+                   T, [box] * 3)
+
+
+def params(trap_w=1.0, trap_c=(0, 0, 0), trap_w2=(1, 1, 1), gauss_g=0.0, gauss_s=1.0,
+           coul_s=1.0, coul_alpha=1.0, coul_nsum=1):
+    return Params(trap_w, (C.c_double * 3)(*trap_w2), (C.c_double * 3)(*trap_c), gauss_g,
+                  gauss_s, coul_s, coul_alpha, coul_nsum)
+
+
+def fast_fill_ENk(sim, N, P, omegaP, image):
+    ENk = np.zeros(ntri(N))
+    Eint = np.zeros(N)
+    lib().orc_fast_fill_ENk(sim.ref, N, P, omegaP, image, ptr(ENk), ptr(Eint))
+    return ENk, Eint
+
+
+def fill_VB(N, beta, vi, ENk):
+    VBN = np.zeros(N + 1)
+    lib().orc_fill_VB(N, beta, vi, ptr(np.ascontiguousarray(ENk)), ptr(VBN))
+    return VBN
+
+
+def fast_force_VB(sim, N, P, beta, vi, omegaP, image, ENk, VBN):
+    G = np.zeros(N * N)
+    tmpV = np.zeros(N + 1)
+    rc = lib().orc_fast_force_VB(sim.ref, N, P, beta, vi, omegaP, image,
+                                 ptr(np.ascontiguousarray(ENk)), ptr(np.ascontiguousarray(VBN)),
+                                 ptr(G), ptr(tmpV))
+    assert rc == 0
+    return G.reshape(N, N), tmpV

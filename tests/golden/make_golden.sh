@@ -1,0 +1,41 @@
+#!/bin/sh
+# Regenerates the golden fixtures in tests/golden/ from MD-Lab's own _nocl
+# build.  Needs the MD-Lab source tree (REF_DIR, default /root/reference);
+# the fixtures it writes are committed, so the tests themselves never need it.
+set -e
+HERE=$(cd "$(dirname "$0")" && pwd)
+ROOT=$(cd "$HERE/../.." && pwd)
+REF_DIR=${REF_DIR:-/root/reference}
+make -s -C "$ROOT/oracle" ref REF_DIR="$REF_DIR"
+OUT=$ROOT/oracle/_ref
+for v in d3l8 d3l4 d2l4; do
+  gcc -O2 -ffp-contract=off -w -I "$OUT/src_$v" -o "$OUT/make_golden_$v" "$HERE/make_golden.c" \
+      -L "$OUT" -lxmd_x_$v -Wl,-rpath,"$OUT" -lm
+done
+G3="$OUT/make_golden_d3l4"
+G38="$OUT/make_golden_d3l8"
+G2="$OUT/make_golden_d2l4"
+cd "$HERE"
+# 2D harmonic trap, N=4 bosons, P=32, beta=2, V=2 exp(-r^2/0.25), dt=0.01
+$G2 pimd d2l4_cfg1.bin N=4 P=32 vi=1 beta=2 g=1.5707963267948966 s=0.5 dt=0.01 seed=2024 steps=1000 every=100
+# 3D trap, V=3 exp(-r^2/0.25), beta=4, dt=0.005, three statistics
+$G3 pimd d3l4_trap_vi1.bin N=8 P=8 vi=1 beta=4 seed=11 steps=1000 every=100
+$G3 pimd d3l4_trap_vi05.bin N=8 P=8 vi=0.5 beta=4 seed=12 steps=200 every=50
+$G3 pimd d3l4_trap_vi0.bin N=8 P=8 vi=0 beta=4 seed=13 steps=200 every=50
+# ragged sizes, P=2 (no interior beads), N=1, grouped chains (f=3, fc=3)
+$G3 pimd d3l4_trap_n37p6.bin N=37 P=6 vi=0.75 beta=3 seed=14 steps=20 every=10
+$G3 pimd d3l4_trap_p2.bin N=5 P=2 vi=1 beta=2 seed=15 steps=50 every=25
+$G3 pimd d3l4_trap_n1.bin N=1 P=8 vi=1 beta=4 seed=16 steps=50 every=25
+$G3 pimd d3l4_trap_chain3.bin N=6 P=4 vi=0.25 beta=4 f=3 fc=3 seed=17 steps=50 every=25
+# periodic electron gas with Ewald (alpha = 5.6/L), minimum-image springs, wrap
+$G3 pimd d3l4_ueg.bin N=8 P=4 vi=0.6 rs=2 theta=0.5 ueg=1 image=1 pbc=1 nsum=3 dt=0.05 seed=18 steps=20 every=10
+# the reference's default chain length
+$G38 pimd d3l8_trap.bin N=6 P=8 vi=1 beta=4 seed=19 steps=100 every=50
+# cubic vs quadratic exchange paths
+$G3 cubic d3l4_cubic.bin N=7 P=5 vi=0.5 beta=2 seed=21 image=0
+$G3 cubic d3l4_cubic_img.bin N=6 P=4 vi=1 beta=3 seed=22 image=1 box=2.5
+# random numbers and isolated pair callbacks
+$G3 rng rng.bin
+$G3 pairs d3_pairs.bin
+$G2 pairs d2_pairs.bin
+ls -la "$HERE"/*.bin
