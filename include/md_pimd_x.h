@@ -1,0 +1,111 @@
+/*
+ * md_pimd_x.h -- the path-integral (PIMD) step for fictitious identical
+ * particles: exchange recursion, bead forces and estimators.  MD-Lab C ABI
+ * as implemented by the GB300 library libxmd_x.
+ *
+ * Replaces MD-Lab md_pimd_x.h:1-233 for the force-and-integrate step.
+ * Every compute entry point below is asynchronous on the library's CUDA
+ * stream, exactly like the reference's OpenCL queue: results become visible
+ * on the host through md_pimd_sync_host_x / md_simulation_sync_host_x /
+ * md_stats_sync_host_x.  Functions return 0 on success and a negative
+ * MD_GB_ERR_* code (md_gb300_x.h) on failure; nothing falls back to the CPU.
+ */
+#ifndef MD_PIMD_X_H
+#define MD_PIMD_X_H
+
+#include <stdio.h>
+
+#include "md_particle_x.h"
+#include "md_simulation_x.h"
+#include "md_statistics_x.h"
+#include "md_util_x.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* bead (l, j) of a ring polymer, both 1-based: md_pimd_x.h:10 */
+#define MD_PIMD_INDEX_X(l, j, P) (((l)-1) * (P) + (j)-1)
+
+/* md_pimd_x.h:12-106 without the OpenCL members */
+typedef struct {
+  md_simulation_t_x *sim;
+  int N, P;
+  int ENk_count;       /* N(N+1)/2 */
+  md_num_t_x **ENk;    /* ENk[l-1][k-1]: spring energy of the cycle over l-k+1..l */
+  md_num_t_x **ENk2;   /* virial cross terms, same shape */
+  md_num_t_x **ENk3;
+  md_num_t_x *VBN;     /* [N+1] exchange potentials V_B^(n) */
+  md_num_t_x vi;       /* statistics parameter xi */
+  md_num_t_x omegaP;   /* sqrt(P)/(beta hbar) */
+  md_num_t_x beta;
+  int pcount_in, pcount_ex;
+  md_index_pair_t_x *pair_in;
+  md_index_pair_t_x *pair_ex;
+  int *Eindices;
+  md_num_t_x *minE;
+  int cut_Pj;
+  md_num_t_x *Eint;
+  md_num_t_x *Evir;
+  int mc_par;
+  int pbc;
+  int *pbW;
+  int worm_index;
+  md_num_t_x worm_pos[MD_DIMENSION_X];
+  int old_worm_index;
+  md_num_t_x old_worm_pos[MD_DIMENSION_X];
+} md_pimd_t_x;
+
+/* md_pimd_x.h:114-120 */
+md_pimd_t_x *md_pimd_sync_host_x(md_pimd_t_x *pimd, int read_only);
+md_pimd_t_x *md_alloc_pimd_x(md_simulation_t_x *sim, int N, int P, md_num_t_x vi, md_num_t_x T);
+void md_pimd_change_temperature_x(md_pimd_t_x *pimd, md_num_t_x T);
+int md_pimd_next_index_x(int l, int j, int N2, int k, int P);
+int md_pimd_prev_index_x(int l, int j, int N2, int k, int P);
+int md_pimd_init_particle_uniform_pos_x(md_pimd_t_x *pimd, md_num_t_x *center, md_num_t_x *L, md_num_t_x fluc);
+
+/* exchange: md_pimd_x.h:121-140.  The cubic-scaling entry points
+   (md_pimd_fill_ENk_x, md_pimd_fill_force_VB_x) run the quadratic kernels,
+   which compute the same quantities (they agree with the reference's cubic
+   output to rounding). */
+md_num_t_x md_pimd_ENk_x(md_pimd_t_x *pimd, int N2, int k, int image);
+int md_pimd_fill_ENk_x(md_pimd_t_x *pimd, int image);
+int md_pimd_fprint_ENk_x(FILE *out, md_pimd_t_x *pimd);
+md_num_t_x md_pimd_xexp_x(md_num_t_x k, md_num_t_x E, md_num_t_x EE, md_num_t_x beta, md_num_t_x vi);
+md_num_t_x md_pimd_xminE_x(md_pimd_t_x *pimd, int N2);
+int md_pimd_fill_VB_x(md_pimd_t_x *pimd);
+int md_pimd_fprint_VBN_x(FILE *out, md_pimd_t_x *pimd);
+int md_pimd_fill_force_VB_x(md_pimd_t_x *pimd, int image);
+int md_pimd_fast_fill_ENk_x(md_pimd_t_x *pimd, int image);
+md_num_t_x md_pimd_fast_xminE_x(md_pimd_t_x *pimd, int u, md_num_t_x *V);
+md_num_t_x md_pimd_fast_xexp_x(md_num_t_x l, md_num_t_x k, md_num_t_x E, md_num_t_x EE, md_num_t_x beta, md_num_t_x vi);
+int md_pimd_fast_fill_force_VB_x(md_pimd_t_x *pimd, int image);
+
+/* external bead forces and energies: md_pimd_x.h:130-134 */
+int md_pimd_calc_VBN_energy_x(md_pimd_t_x *pimd, md_stats_t_x *stats);
+int md_pimd_calc_trap_force_x(md_pimd_t_x *pimd, md_trap_force_t_x tf);
+int md_pimd_calc_trap_energy_x(md_pimd_t_x *pimd, md_trap_energy_t_x te, md_stats_t_x *stats);
+int md_pimd_calc_pair_force_x(md_pimd_t_x *pimd, md_pair_force_t_x pf);
+int md_pimd_calc_pair_energy_x(md_pimd_t_x *pimd, md_pair_energy_t_x pe, md_stats_t_x *stats);
+
+/* virial estimator: md_pimd_x.h:157-162 */
+int md_pimd_fill_ENk2_x(md_pimd_t_x *pimd, int image);
+int md_pimd_fprint_ENk2_x(FILE *out, md_pimd_t_x *pimd);
+int md_pimd_calc_vi_virial_energy_x(md_pimd_t_x *pimd, md_stats_t_x *stats, int image);
+int md_pimd_fast_fill_ENk2_x(md_pimd_t_x *pimd, int image);
+
+/* accumulator arithmetic: md_pimd_x.h:163-169 */
+int md_reset_stats_x(md_stats_t_x *stats, md_num_t_x e);
+int md_stats_add_to_x(md_stats_t_x *stats, md_stats_t_x *stats2);
+int md_stats_copy_to_x(md_stats_t_x *stats, md_stats_t_x *stats2);
+int md_stats_mult_to_x(md_stats_t_x *stats, md_stats_t_x *stats2);
+
+/* xi -> xi' reweighting with sign, e.g. bosons to fermions:
+   md_pimd_x.h:171-172 (host side, on the synced ENk/VBN) */
+md_num_t_x md_pimd_xminE2_x(md_pimd_t_x *pimd, int N2, md_num_t_x *VBN2, md_num_t_x vi2);
+int md_pimd_calc_vi_sign_x(md_pimd_t_x *pimd, md_stats_t_x *e_s, md_stats_t_x *s_s, md_num_t_x vi2);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

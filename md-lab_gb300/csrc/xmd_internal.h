@@ -1,0 +1,101 @@
+// xmd_internal.h -- device state behind the MD-Lab structs.
+//
+// The public structs keep the reference's exact layout, so device state is
+// held in side tables keyed by the struct's address.  Ownership follows the
+// reference's OpenCL back end (md_util_x.c:359-551, md_pimd_x.c:9-326): a
+// device copy is created on the first device call and is authoritative until
+// a *_sync_host_x(..., 0) hands authority back to the host; the next device
+// call then uploads again.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+
+#include "md_gb300_x.h"
+#include "xmd_kernels.cuh"
+
+namespace xmd {
+
+// ---- errors ----
+int fail(int code, const char *fmt, ...);
+int cuda_fail(cudaError_t e, const char *what);
+#define XMD_CUDA(call)                                   \
+  do {                                                   \
+    cudaError_t xmd_e_ = (call);                         \
+    if (xmd_e_ != cudaSuccess) return ::xmd::cuda_fail(xmd_e_, #call); \
+  } while (0)
+#define XMD_TRY(call)                \
+  do {                               \
+    int xmd_r_ = (call);             \
+    if (xmd_r_ != 0) return xmd_r_;  \
+  } while (0)
+
+// ---- runtime ----
+int ensure_device();       // MD_GB_ERR_NO_DEVICE when CUDA has no device
+bool device_present();     // without setting an error
+cudaStream_t stream();
+bool capturing();
+
+struct DevBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+  template <class T>
+  T *as() const { return (T *)p; }
+};
+int reserve(DevBuf &b, size_t bytes);  // grows, never shrinks
+void release(DevBuf &b);
+
+// pinned host allocations made by md_alloc_* (freed with cudaFreeHost)
+void *host_alloc(size_t bytes);
+void host_free(void *p);
+
+struct SimDev {
+  bool valid = false;  // device copy authoritative
+  xk::Geo geo{};
+  int nf = 0, L = 0;
+  bool fast_chains = true;
+  bool uniform_mass = true;
+  double mass0 = 1.0;
+  DevBuf x, v, f, m;
+  DevBuf th, vt, Q;
+  DevBuf cf, c0, c2;
+  DevBuf stage;    // AoS records on the device
+  DevBuf scratch;  // partial sums of pair / exchange / reduction kernels
+};
+
+struct PimdDev {
+  bool valid = false;  // ENk / ENk2 / VBN / Eint on the device authoritative
+  DevBuf ENk, ENk2, Eint, VBN, tmpV, G;
+  // Ewald reciprocal tables, rebuilt when the parameters change
+  DevBuf rc_coef, rc_cols, rc_phase, rc_S;
+  int rc_nsum = -1;
+  double rc_alpha = 0, rc_qs = 0, rc_box[3] = {0, 0, 0};
+  int rc_nk = 0;
+};
+
+struct StatsDev {
+  bool valid = false;
+  DevBuf acc;
+};
+
+// layout of a simulation: N particles x P beads (set by md_alloc_pimd_x)
+void layout_hint(md_simulation_t_x *sim, int N, int P);
+void forget(const void *key);
+
+// device copies, created on demand
+int sim_device(md_simulation_t_x *sim, SimDev **out);
+int sim_to_host(md_simulation_t_x *sim, bool keep);
+int pimd_device(md_pimd_t_x *pimd, SimDev **sd, PimdDev **pd);
+int pimd_to_host(md_pimd_t_x *pimd, bool keep);
+int stats_device(md_stats_t_x *st, double **acc);
+int stats_to_host(md_stats_t_x *st);
+int scratch(SimDev *sd, size_t doubles, double **out);
+
+// read the current potential parameter globals
+xk::TrapPrm trap_params(int kind);
+int pair_kind_of(const void *fn, bool energy);
+int trap_kind_of(const void *fn, bool energy);
+
+}  // namespace xmd

@@ -1,0 +1,1699 @@
+// xmd_kernels.cu -- sm_103a kernels of the PIMD force-and-integrate step.
+//
+// FP64 throughout (the "plain" form that reproduces MD-Lab's _nocl build to
+// 1e-10).  On GB300 the FP64 pipe runs at 1/58 of the FP32 rate (measured:
+// 1.2 TFLOP/s DFMA), so every kernel is organised to spend as few FP64
+// instructions as the reference's arithmetic allows: pair forces use
+// Newton's third law with warp-rotation tiles (one evaluation per pair, no
+// atomics), the Ewald reciprocal sum goes through per-slice structure factors
+// with per-axis phase factors (O(N K) instead of O(N^2 K)), and reductions
+// are warp shuffles with a fixed summation order (results are bitwise
+// reproducible run to run).
+//
+// Reference counterparts (MD-Lab file:line) are cited at each kernel.
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "xmd_kernels.cuh"
+
+namespace xk {
+
+static std::atomic<uint64_t> g_launches{0};
+uint64_t launch_count() { return g_launches.load(); }
+
+// ---- live per-kernel timing (CUDA events on the launching stream) ----
+static bool g_prof = false;
+struct ProfRec {
+  const char *name;
+  cudaEvent_t a, b;
+};
+static std::vector<ProfRec> g_prof_recs;
+
+void profile_enable(bool on) { g_prof = on; }
+
+// sums the recorded launches per kernel name: returns "name ms launches;..."
+std::string profile_report() {
+  std::vector<std::pair<std::string, std::pair<double, int>>> acc;
+  for (auto &r : g_prof_recs) {
+    cudaEventSynchronize(r.b);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, r.a, r.b);
+    bool found = false;
+    for (auto &e : acc)
+      if (e.first == r.name) {
+        e.second.first += ms;
+        e.second.second += 1;
+        found = true;
+      }
+    if (!found) acc.push_back({r.name, {ms, 1}});
+    cudaEventDestroy(r.a);
+    cudaEventDestroy(r.b);
+  }
+  g_prof_recs.clear();
+  std::string out;
+  char buf[256];
+  for (auto &e : acc) {
+    snprintf(buf, sizeof buf, "%s %.6f %d;", e.first.c_str(), e.second.first, e.second.second);
+    out += buf;
+  }
+  return out;
+}
+
+// RAII bracket around one launch; inert unless profiling is on and the
+// stream is not being captured into a graph
+struct Prof {
+  const char *name;
+  cudaStream_t st;
+  cudaEvent_t a = nullptr;
+  Prof(const char *n, cudaStream_t s) : name(n), st(s) {
+    if (!g_prof) return;
+    cudaStreamCaptureStatus cs;
+    if (cudaStreamIsCapturing(st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return;
+    cudaEventCreate(&a);
+    cudaEventRecord(a, st);
+  }
+  ~Prof() {
+    if (!a) return;
+    cudaEvent_t b;
+    cudaEventCreate(&b);
+    cudaEventRecord(b, st);
+    g_prof_recs.push_back({name, a, b});
+  }
+};
+#define XK_PROF(name) Prof xk_prof_(name, st)
+
+#define XK_LAUNCHED() (g_launches.fetch_add(1), cudaGetLastError())
+#define FULL 0xffffffffu
+
+__host__ __device__ inline size_t sidx(int j, int d, int l, int D, int Ns) {
+  return ((size_t)j * D + d) * Ns + l;
+}
+__device__ inline size_t dtri(int n) { return (size_t)n * (n - 1) / 2; }
+
+// md_simulation_x.c:70-81 with md_periodic_image_count_x (:858-865): shift
+// a + L/2 into [0, L] by whole boxes, then subtract L/2 again.
+__device__ inline double min_image(double a, double L, double invL) {
+  a += L / 2;
+  int c = (int)(fabs(a) * invL);
+  if (a > L)
+    a += L * (double)(-c);
+  else if (a < 0)
+    a += L * (double)(c + 1);
+  return a - L / 2;
+}
+
+__device__ inline double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
+  return v;
+}
+__device__ inline double warp_min(double v) {
+#pragma unroll
+  for (int o = 16; o; o >>= 1) {
+    double t = __shfl_xor_sync(FULL, v, o);
+    v = t < v ? t : v;
+  }
+  return v;
+}
+
+// block-wide reductions; buf needs 33 doubles and must not be reused by the
+// caller until one more __syncthreads() has passed.
+__device__ inline double block_sum(double v, double *buf) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  v = warp_sum(v);
+  if (lane == 0) buf[w] = v;
+  __syncthreads();
+  if (w == 0) {
+    double t = lane < nw ? buf[lane] : 0.0;
+    t = warp_sum(t);
+    if (lane == 0) buf[32] = t;
+  }
+  __syncthreads();
+  return buf[32];
+}
+__device__ inline double block_min(double v, double init, double *buf) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  v = warp_min(v);
+  if (lane == 0) buf[w] = v;
+  __syncthreads();
+  if (w == 0) {
+    double t = lane < nw ? buf[lane] : init;
+    t = warp_min(t);
+    if (lane == 0) buf[32] = t < init ? t : init;
+  }
+  __syncthreads();
+  return buf[32];
+}
+
+static inline int cdiv(size_t a, int b) { return (int)((a + b - 1) / b); }
+
+#define DISPATCH_D(Dv, ...)                 \
+  switch (Dv) {                             \
+    case 1: {                               \
+      constexpr int D = 1;                  \
+      __VA_ARGS__;                          \
+    } break;                                \
+    case 2: {                               \
+      constexpr int D = 2;                  \
+      __VA_ARGS__;                          \
+    } break;                                \
+    case 3: {                               \
+      constexpr int D = 3;                  \
+      __VA_ARGS__;                          \
+    } break;                                \
+    default:                                \
+      return cudaErrorInvalidValue;         \
+  }
+
+// ===================================================================
+// layout conversion
+// ===================================================================
+
+template <int D>
+__global__ void k_aos_to_soa(Geo g, const double *__restrict__ aos, double *x, double *v,
+                             double *f, double *m) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= g.N * g.P) return;
+  const int l = b / g.P, j = b % g.P;
+  const double *r = aos + (size_t)b * (1 + 3 * D);
+  m[(size_t)j * g.Ns + l] = r[0];
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    const size_t s = sidx(j, d, l, D, g.Ns);
+    x[s] = r[1 + d];
+    v[s] = r[1 + D + d];
+    f[s] = r[1 + 2 * D + d];
+  }
+}
+
+template <int D>
+__global__ void k_soa_to_aos(Geo g, double *__restrict__ aos, const double *x, const double *v,
+                             const double *f, const double *m) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= g.N * g.P) return;
+  const int l = b / g.P, j = b % g.P;
+  double *r = aos + (size_t)b * (1 + 3 * D);
+  r[0] = m[(size_t)j * g.Ns + l];
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    const size_t s = sidx(j, d, l, D, g.Ns);
+    r[1 + d] = x[s];
+    r[1 + D + d] = v[s];
+    r[1 + 2 * D + d] = f[s];
+  }
+}
+
+cudaError_t aos_to_soa(const Geo &g, const double *aos, double *x, double *v, double *f,
+                       double *m, cudaStream_t st) {
+  const int n = g.N * g.P;
+  {
+    XK_PROF("aos_to_soa");
+    DISPATCH_D(g.D, k_aos_to_soa<D><<<cdiv(n, 256), 256, 0, st>>>(g, aos, x, v, f, m));
+  }
+  return XK_LAUNCHED();
+}
+
+cudaError_t soa_to_aos(const Geo &g, double *aos, const double *x, const double *v,
+                       const double *f, const double *m, cudaStream_t st) {
+  const int n = g.N * g.P;
+  {
+    XK_PROF("soa_to_aos");
+    DISPATCH_D(g.D, k_soa_to_aos<D><<<cdiv(n, 256), 256, 0, st>>>(g, aos, x, v, f, m));
+  }
+  return XK_LAUNCHED();
+}
+
+// chain record: int f at offset 0, then theta[L], vtheta[L], Q[L] (doubles)
+// starting at offset 8.  Fast chains go to slot order, grouped chains keep
+// the chain order.
+template <int D>
+__global__ void k_chains(Geo g, int L, int nf, bool fast, bool to_dev, unsigned char *rec,
+                         size_t rb, double *th, double *vt, double *Q) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nf) return;
+  size_t slot, stride;
+  if (fast) {
+    const int b = c / D, d = c % D;
+    const int l = b / g.P, j = b % g.P;
+    slot = sidx(j, d, l, D, g.Ns);
+    stride = g.slots();
+  } else {
+    slot = c;
+    stride = nf;
+  }
+  double *r = (double *)(rec + (size_t)c * rb + 8);
+  for (int i = 0; i < L; ++i) {
+    if (to_dev) {
+      th[i * stride + slot] = r[i];
+      vt[i * stride + slot] = r[L + i];
+      Q[i * stride + slot] = r[2 * L + i];
+    } else {
+      r[i] = th[i * stride + slot];
+      r[L + i] = vt[i * stride + slot];
+      r[2 * L + i] = Q[i * stride + slot];
+    }
+  }
+}
+
+cudaError_t chains_to_dev(const Geo &g, int L, int nf, bool fast, const unsigned char *rec,
+                          size_t rb, double *th, double *vt, double *Q, cudaStream_t st) {
+  {
+    XK_PROF("chains");
+    DISPATCH_D(g.D, k_chains<D><<<cdiv(nf, 256), 256, 0, st>>>(g, L, nf, fast, true,
+                                                              (unsigned char *)rec, rb, th, vt, Q));
+  }
+  return XK_LAUNCHED();
+}
+
+cudaError_t chains_to_host(const Geo &g, int L, int nf, bool fast, unsigned char *rec, size_t rb,
+                           const double *th, const double *vt, const double *Q,
+                           cudaStream_t st) {
+  {
+    XK_PROF("chains");
+    DISPATCH_D(g.D, k_chains<D><<<cdiv(nf, 256), 256, 0, st>>>(
+                        g, L, nf, fast, false, rec, rb, (double *)th, (double *)vt, (double *)Q));
+  }
+  return XK_LAUNCHED();
+}
+
+// ===================================================================
+// Nose-Hoover chains, "VV3" splitting: md_simulation_x.c:599-792
+// ===================================================================
+
+// Thermostat update of one chain.  v[], F[], mass[] are the chain's DOFs
+// (ndof of them, counted as cfv DOFs in the kinetic term); half = 1 is
+// md_update_nhc_VV3_1_x (kick, chain, drift, chain), half = 2 is
+// md_update_nhc_VV3_2_x (kick, chain).
+template <int L>
+struct ChainState {
+  double th[L], vt[L], Q[L];
+};
+
+template <int L>
+__device__ inline void chain_forces(const ChainState<L> &c, double kin, double cfv, double kT,
+                                    double *nhf) {
+  // md_simulation_x.c:599-613
+  nhf[0] = (kin - cfv * kT) / c.Q[0];
+#pragma unroll
+  for (int j = 1; j < L; ++j) nhf[j] = (c.Q[j - 1] * c.vt[j - 1] * c.vt[j - 1] - kT) / c.Q[j];
+}
+
+template <int L>
+__device__ inline void chain_odd(ChainState<L> &c, double h, const double *nhf) {
+  constexpr int M2 = L / 2;
+#pragma unroll
+  for (int j = 1; j <= M2; ++j) {
+    const double nxt = (j == M2) ? 0.0 : c.vt[2 * j];
+    c.vt[2 * j - 1] = c.vt[2 * j - 1] * exp(-0.5 * h * nxt) + 0.5 * h * nhf[2 * j - 1] * exp(-0.25 * h * nxt);
+  }
+}
+
+template <int D, int L>
+__global__ void __launch_bounds__(256) k_nhc_fast(Geo g, int half, double *__restrict__ x,
+                                                  double *__restrict__ v,
+                                                  const double *__restrict__ f,
+                                                  const double *__restrict__ m,
+                                                  double *__restrict__ th, double *__restrict__ vt,
+                                                  const double *__restrict__ Q, double kT,
+                                                  double h) {
+  const size_t S = g.slots();
+  const size_t s = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= S) return;
+  const int l = (int)(s % g.Ns);
+  if (l >= g.N) return;
+  const int j = (int)(s / ((size_t)D * g.Ns));
+  constexpr int M2 = L / 2;
+  ChainState<L> c;
+#pragma unroll
+  for (int i = 0; i < L; ++i) {
+    c.th[i] = th[i * S + s];
+    c.vt[i] = vt[i * S + s];
+    c.Q[i] = Q[i * S + s];
+  }
+  const double mass = m[(size_t)j * g.Ns + l];
+  double vv = v[s];
+  const double F = f[s];
+  double nhf[L];
+  if (half == 1) chain_forces<L>(c, mass * vv * vv, 1.0, kT, nhf);
+  // thermostatted half kick: md_simulation_x.c:674-678
+  vv = vv * exp(-0.5 * h * c.vt[0]) + 0.5 * h * F * exp(-0.25 * h * c.vt[0]);
+#pragma unroll
+  for (int k = 1; k <= M2; ++k) c.th[2 * k - 2] = c.th[2 * k - 2] + h * c.vt[2 * k - 2] / 2;
+  if (half == 2) chain_forces<L>(c, mass * vv * vv, 1.0, kT, nhf);
+  chain_odd<L>(c, h, nhf);
+  if (half == 1) {
+    x[s] = x[s] + h * vv;  // drift: md_simulation_x.c:684-689
+#pragma unroll
+    for (int k = 1; k <= M2; ++k) c.th[2 * k - 1] = c.th[2 * k - 1] + h * c.vt[2 * k - 1];
+    chain_forces<L>(c, mass * vv * vv, 1.0, kT, nhf);
+#pragma unroll
+    for (int k = 1; k <= M2; ++k)
+      c.vt[2 * k - 2] = c.vt[2 * k - 2] * exp(-h * c.vt[2 * k - 1]) +
+                        h * nhf[2 * k - 2] * exp(-0.5 * h * c.vt[2 * k - 1]);
+  }
+  v[s] = vv;
+#pragma unroll
+  for (int i = 0; i < L; ++i) {
+    th[i * S + s] = c.th[i];
+    vt[i * S + s] = c.vt[i];
+  }
+}
+
+// chains over several DOFs (reference numbering dof = bead*D + d,
+// bead = l*P + j); one thread per chain, DOFs in the reference's order.
+template <int D, int L>
+__global__ void k_nhc_grouped(Geo g, int half, int nf, const int *__restrict__ cf,
+                              const int *__restrict__ c0, const int *__restrict__ c2,
+                              double *__restrict__ x, double *__restrict__ v,
+                              const double *__restrict__ f, const double *__restrict__ m,
+                              double *__restrict__ th, double *__restrict__ vt,
+                              const double *__restrict__ Q, double kT, double h) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nf) return;
+  constexpr int M2 = L / 2;
+  ChainState<L> c;
+#pragma unroll
+  for (int k = 0; k < L; ++k) {
+    c.th[k] = th[(size_t)k * nf + i];
+    c.vt[k] = vt[(size_t)k * nf + i];
+    c.Q[k] = Q[(size_t)k * nf + i];
+  }
+  const int f0 = c0[i], f2 = c2[i];
+  const double cfv = cf[i];
+  auto slot = [&](int dof) {
+    const int b = dof / D, d = dof % D;
+    return sidx(b % g.P, d, b / g.P, D, g.Ns);
+  };
+  auto mass = [&](int dof) {
+    const int b = dof / D;
+    return m[(size_t)(b % g.P) * g.Ns + b / g.P];
+  };
+  auto kinetic = [&]() {
+    double sum = 0;
+    for (int q = 0; q < f2; ++q) {
+      const size_t s = slot(f0 + q);
+      sum += mass(f0 + q) * v[s] * v[s];
+    }
+    return sum;
+  };
+  double nhf[L];
+  if (half == 1) chain_forces<L>(c, kinetic(), cfv, kT, nhf);
+  const double e1 = exp(-0.5 * h * c.vt[0]), e2 = exp(-0.25 * h * c.vt[0]);
+  for (int q = 0; q < f2; ++q) {
+    const size_t s = slot(f0 + q);
+    v[s] = v[s] * e1 + 0.5 * h * f[s] * e2;
+  }
+#pragma unroll
+  for (int k = 1; k <= M2; ++k) c.th[2 * k - 2] = c.th[2 * k - 2] + h * c.vt[2 * k - 2] / 2;
+  if (half == 2) chain_forces<L>(c, kinetic(), cfv, kT, nhf);
+  chain_odd<L>(c, h, nhf);
+  if (half == 1) {
+    for (int q = 0; q < f2; ++q) {
+      const size_t s = slot(f0 + q);
+      x[s] = x[s] + h * v[s];
+    }
+#pragma unroll
+    for (int k = 1; k <= M2; ++k) c.th[2 * k - 1] = c.th[2 * k - 1] + h * c.vt[2 * k - 1];
+    chain_forces<L>(c, kinetic(), cfv, kT, nhf);
+#pragma unroll
+    for (int k = 1; k <= M2; ++k)
+      c.vt[2 * k - 2] = c.vt[2 * k - 2] * exp(-h * c.vt[2 * k - 1]) +
+                        h * nhf[2 * k - 2] * exp(-0.5 * h * c.vt[2 * k - 1]);
+  }
+#pragma unroll
+  for (int k = 0; k < L; ++k) {
+    th[(size_t)k * nf + i] = c.th[k];
+    vt[(size_t)k * nf + i] = c.vt[k];
+  }
+}
+
+#define DISPATCH_L(Lv, ...)           \
+  switch (Lv) {                       \
+    case 2: {                         \
+      constexpr int LL = 2;           \
+      __VA_ARGS__;                    \
+    } break;                          \
+    case 4: {                         \
+      constexpr int LL = 4;           \
+      __VA_ARGS__;                    \
+    } break;                          \
+    case 6: {                         \
+      constexpr int LL = 6;           \
+      __VA_ARGS__;                    \
+    } break;                          \
+    case 8: {                         \
+      constexpr int LL = 8;           \
+      __VA_ARGS__;                    \
+    } break;                          \
+    default:                          \
+      return cudaErrorInvalidValue;   \
+  }
+
+cudaError_t nhc_vv3(const Geo &g, int half, const Chains &c, double *x, double *v,
+                    const double *f, const double *m, double kT, double h, cudaStream_t st) {
+  if (c.fast) {
+    const size_t S = g.slots();
+    {
+      XK_PROF("nhc_fast");
+      DISPATCH_D(g.D, DISPATCH_L(c.L, k_nhc_fast<D, LL><<<cdiv(S, 256), 256, 0, st>>>(
+                                          g, half, x, v, f, m, c.th, c.vt, c.Q, kT, h)));
+    }
+  } else {
+    {
+      XK_PROF("nhc_grouped");
+      DISPATCH_D(g.D, DISPATCH_L(c.L, k_nhc_grouped<D, LL><<<cdiv(c.nf, 128), 128, 0, st>>>(
+                                          g, half, c.nf, c.cf, c.c0, c.c2, x, v, f, m, c.th,
+                                          c.vt, c.Q, kT, h)));
+    }
+  }
+  return XK_LAUNCHED();
+}
+
+// md_simulation_x.c:846-853
+__global__ void k_wrap(Geo g, double *x) {
+  const size_t s = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= g.slots()) return;
+  if ((int)(s % g.Ns) >= g.N) return;
+  const int d = (int)((s / g.Ns) % g.D);
+  const double L = g.box[d];
+  double a = x[s];
+  if (a < 0)
+    a += L;
+  else if (a > L)
+    a -= L;
+  x[s] = a;
+}
+
+cudaError_t wrap_box(const Geo &g, double *x, cudaStream_t st) {
+  {
+    XK_PROF("wrap");
+    k_wrap<<<cdiv(g.slots(), 256), 256, 0, st>>>(g, x);
+  }
+  return XK_LAUNCHED();
+}
+
+cudaError_t zero(double *p, size_t n, cudaStream_t st) {
+  return cudaMemsetAsync(p, 0, n * sizeof(double), st);
+}
+
+// ===================================================================
+// cycle spring energies E_l^(k): md_pimd_x.c:1969-2210 (CPU :2086-2207)
+// ===================================================================
+
+template <int D>
+__device__ inline double spring2(Geo g, const double *x, int ja, int la, int jb, int lb,
+                                 int image) {
+  double s = 0;
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    double t = x[sidx(ja, d, la, D, g.Ns)] - x[sidx(jb, d, lb, D, g.Ns)];
+    if (image) t = min_image(t, g.box[d], g.inv_box[d]);
+    s += t * t;
+  }
+  return s;
+}
+
+// interior ring springs of particle l and the closing spring P -> 1
+template <int D>
+__global__ void k_eint(Geo g, const double *__restrict__ x, const double *__restrict__ m,
+                       double w2, int image, double *Eint, double *ENk) {
+  const int l = blockIdx.x * blockDim.x + threadIdx.x;
+  if (l >= g.N) return;
+  double res = 0;
+  for (int j = 0; j + 1 < g.P; ++j)
+    res += 0.5 * m[(size_t)j * g.Ns + l] * w2 * spring2<D>(g, x, j, l, j + 1, l, image);
+  Eint[l] = res;
+  const int jP = g.P - 1;
+  ENk[dtri(l + 1)] = res + 0.5 * m[(size_t)jP * g.Ns + l] * w2 * spring2<D>(g, x, jP, l, 0, l, image);
+}
+
+// spring between bead P of particle a and bead 1 of particle b (0-based),
+// weighted by the mass of the bead-P end as in the reference.
+template <int D>
+__device__ inline double link(Geo g, const double *x, const double *m, double w2, int a, int b,
+                              int image) {
+  const int jP = g.P - 1;
+  return 0.5 * m[(size_t)jP * g.Ns + a] * w2 * spring2<D>(g, x, jP, a, 0, b, image);
+}
+
+// one warp per particle l (1-based row l >= 2): E_l^(k) for k = 2..l as an
+// inclusive scan of the increments
+//   Eint[l-k+1] - link(l, l-k+2) + link(l-k+1, l-k+2) + link(l, l-k+1)
+template <int D>
+__global__ void k_enk_rows(Geo g, const double *__restrict__ x, const double *__restrict__ m,
+                           double w2, int image, const double *__restrict__ Eint,
+                           double *__restrict__ ENk) {
+  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  const int l = w + 2;  // 1-based
+  if (l > g.N) return;
+  double carry = ENk[dtri(l)];
+  for (int k0 = 2; k0 <= l; k0 += 32) {
+    const int k = k0 + lane;
+    double inc = 0;
+    if (k <= l) {
+      const int c = l - k + 1, b = l - k + 2;  // 1-based
+      inc = Eint[c - 1] - link<D>(g, x, m, w2, l - 1, b - 1, image) +
+            link<D>(g, x, m, w2, c - 1, b - 1, image) + link<D>(g, x, m, w2, l - 1, c - 1, image);
+    }
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const double t = __shfl_up_sync(FULL, inc, o);
+      if (lane >= o) inc += t;
+    }
+    const double e = carry + inc;
+    if (k <= l) ENk[dtri(l) + k - 1] = e;
+    carry = __shfl_sync(FULL, e, 31);
+  }
+}
+
+cudaError_t fill_enk(const Geo &g, const double *x, const double *m, double w2, int image,
+                     double *Eint, double *ENk, cudaStream_t st) {
+  {
+    XK_PROF("eint");
+    DISPATCH_D(g.D, k_eint<D><<<cdiv(g.N, 128), 128, 0, st>>>(g, x, m, w2, image, Eint, ENk));
+  }
+  cudaError_t e = XK_LAUNCHED();
+  if (e != cudaSuccess || g.N < 2) return e;
+  const size_t thr = (size_t)(g.N - 1) * 32;
+  {
+    XK_PROF("enk_rows");
+    DISPATCH_D(g.D, k_enk_rows<D><<<cdiv(thr, 256), 256, 0, st>>>(g, x, m, w2, image, Eint, ENk));
+  }
+  return XK_LAUNCHED();
+}
+
+// virial cross term 1/2 m w2 (x_a - x_b).(x_a - x_c) for beads a, b, c:
+// md_pimd_x.c:4376-4421
+template <int D>
+__device__ inline double cross(Geo g, const double *x, const double *m, double w2, int ja, int la,
+                               int jb, int lb, int jc, int lc, int image) {
+  double r = 0;
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    const double xa = x[sidx(ja, d, la, D, g.Ns)];
+    double t = xa - x[sidx(jb, d, lb, D, g.Ns)];
+    double u = xa - x[sidx(jc, d, lc, D, g.Ns)];
+    if (image) {
+      t = min_image(t, g.box[d], g.inv_box[d]);
+      u = min_image(u, g.box[d], g.inv_box[d]);
+    }
+    r += 0.5 * m[(size_t)ja * g.Ns + la] * w2 * t * u;
+  }
+  return r;
+}
+
+// md_pimd_x.c:4423-4556 (CPU :4521-4553): row l, k = 1..l
+template <int D>
+__global__ void k_enk2_rows(Geo g, const double *__restrict__ x, const double *__restrict__ m,
+                            double w2, int image, double *__restrict__ ENk2) {
+  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  const int l = w + 1;  // 1-based
+  if (l > g.N) return;
+  const int jP = g.P - 1;
+  double carry = 0;
+  for (int k0 = 1; k0 <= l; k0 += 32) {
+    const int k = k0 + lane;
+    double inc = 0;
+    if (k == 1) {
+      inc = cross<D>(g, x, m, w2, 0, l - 1, jP, l - 1, 0, l - 1, image);
+    } else if (k <= l) {
+      const int b = l - k + 2, c = l - k + 1;  // 1-based
+      inc = -cross<D>(g, x, m, w2, 0, l - 1, jP, b - 1, 0, b - 1, image);
+      inc += cross<D>(g, x, m, w2, 0, c - 1, jP, b - 1, 0, b - 1, image);
+      inc += cross<D>(g, x, m, w2, 0, l - 1, jP, c - 1, 0, c - 1, image);
+    }
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const double t = __shfl_up_sync(FULL, inc, o);
+      if (lane >= o) inc += t;
+    }
+    const double e = carry + inc;
+    if (k <= l) ENk2[dtri(l) + k - 1] = e;
+    carry = __shfl_sync(FULL, e, 31);
+  }
+}
+
+cudaError_t fill_enk2(const Geo &g, const double *x, const double *m, double w2, int image,
+                      double *ENk2, cudaStream_t st) {
+  const size_t thr = (size_t)g.N * 32;
+  {
+    XK_PROF("enk2_rows");
+    DISPATCH_D(g.D, k_enk2_rows<D><<<cdiv(thr, 256), 256, 0, st>>>(g, x, m, w2, image, ENk2));
+  }
+  return XK_LAUNCHED();
+}
+
+// ===================================================================
+// exchange recursions (single persistent block each)
+// ===================================================================
+
+static int rec_threads(int N) {
+  int t = ((N + 31) / 32) * 32;
+  if (t < 64) t = 64;
+  if (t > 1024) t = 1024;
+  return t;
+}
+
+// forward V_B: md_pimd_x.c:814-953 (CPU :934-950) with md_pimd_xminE_x
+// (:796-806) and md_pimd_xexp_x (:681-686)
+__global__ void k_fill_vb(int N, double beta, double vi, const double *__restrict__ ENk,
+                          double *__restrict__ VBN) {
+  extern __shared__ double sh[];
+  double *V = sh;               // N+1
+  double *bmin = sh + N + 1;    // 33
+  double *bsum = bmin + 33;     // 33
+  const double lnvi = vi != 0.0 ? log(vi) : 0.0;
+  if (threadIdx.x == 0) V[0] = 0.0;
+  __syncthreads();
+  for (int n = 1; n <= N; ++n) {
+    const double *row = ENk + dtri(n);
+    double mloc = 1e10;
+    if (vi == 0.0) {
+      mloc = beta * (row[0] + V[n - 1]);
+    } else {
+      for (int k = threadIdx.x + 1; k <= n; k += blockDim.x) {
+        const double t = -(k - 1) * lnvi + beta * (row[k - 1] + V[n - k]);
+        if (t < mloc) mloc = t;
+      }
+      mloc = block_min(mloc, 1e10, bmin);
+    }
+    double s = 0;
+    for (int k = threadIdx.x + 1; k <= n; k += blockDim.x) {
+      if (vi == 0.0 && k != 1) continue;
+      const double E = row[k - 1] + V[n - k];
+      s += (vi == 0.0) ? exp(-beta * E + mloc) : exp((k - 1) * lnvi - beta * E + mloc);
+    }
+    s = block_sum(s, bsum);
+    if (threadIdx.x == 0) V[n] = (mloc - log(s) + log((double)n)) / beta;
+    __syncthreads();
+  }
+  for (int i = threadIdx.x; i <= N; i += blockDim.x) VBN[i] = V[i];
+}
+
+cudaError_t fill_vb(int N, double beta, double vi, const double *ENk, double *VBN,
+                    cudaStream_t st) {
+  const size_t smem = sizeof(double) * (N + 1 + 66);
+  {
+    XK_PROF("fill_vb");
+    k_fill_vb<<<1, rec_threads(N), smem, st>>>(N, beta, vi, ENk, VBN);
+  }
+  return XK_LAUNCHED();
+}
+
+// backward recursion tmpV: md_pimd_x.c:2648-2659 with md_pimd_fast_xminE_x
+// (:2321-2333) and md_pimd_fast_xexp_x (:2337-2342)
+__global__ void k_back_vb(int N, double beta, double vi, const double *__restrict__ ENk,
+                          double *__restrict__ tmpV) {
+  extern __shared__ double sh[];
+  double *V = sh;              // N+1
+  double *lg = sh + N + 1;     // N+1, lg[l] = log(l)
+  double *bmin = lg + N + 1;   // 33
+  double *bsum = bmin + 33;    // 33
+  const double lnvi = vi != 0.0 ? log(vi) : 0.0;
+  for (int i = threadIdx.x + 1; i <= N; i += blockDim.x) lg[i] = log((double)i);
+  if (threadIdx.x == 0) V[N] = 0.0;
+  __syncthreads();
+  for (int u = N; u >= 1; --u) {
+    double mloc = 1e10;
+    if (vi == 0.0) {
+      mloc = lg[u] + beta * (ENk[dtri(u)] + V[u]);
+    } else {
+      for (int l = u + threadIdx.x; l <= N; l += blockDim.x) {
+        const int k = l - u + 1;
+        const double t = -(k - 1) * lnvi + lg[l] + beta * (ENk[dtri(l) + k - 1] + V[l]);
+        if (t < mloc) mloc = t;
+      }
+      mloc = block_min(mloc, 1e10, bmin);
+    }
+    double s = 0;
+    for (int l = u + threadIdx.x; l <= N; l += blockDim.x) {
+      const int k = l - u + 1;
+      if (vi == 0.0 && k != 1) continue;
+      const double E = ENk[dtri(l) + k - 1] + V[l];
+      s += (vi == 0.0) ? exp(-beta * E + mloc - lg[l]) : exp((k - 1) * lnvi - beta * E + mloc - lg[l]);
+    }
+    s = block_sum(s, bsum);
+    if (threadIdx.x == 0) V[u - 1] = (mloc - log(s)) / beta;
+    __syncthreads();
+  }
+  for (int i = threadIdx.x; i <= N; i += blockDim.x) tmpV[i] = V[i];
+}
+
+cudaError_t back_vb(int N, double beta, double vi, const double *ENk, double *tmpV,
+                    cudaStream_t st) {
+  const size_t smem = sizeof(double) * (2 * (N + 1) + 66);
+  {
+    XK_PROF("back_vb");
+    k_back_vb<<<1, rec_threads(N), smem, st>>>(N, beta, vi, ENk, tmpV);
+  }
+  return XK_LAUNCHED();
+}
+
+// connection probabilities G[l][j]: md_pimd_x.c:2660-2673
+__global__ void k_fill_g(int N, double beta, double vi, const double *__restrict__ ENk,
+                         const double *__restrict__ VBN, const double *__restrict__ tmpV,
+                         double *__restrict__ G) {
+  const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (size_t)N * N) return;
+  const int l = (int)(t / N) + 1, j = (int)(t % N) + 1;  // 1-based
+  double gv;
+  if (j > l + 1)
+    gv = 0;
+  else if (j == l + 1)
+    gv = 1 - exp(-beta * (VBN[l] + tmpV[l] - VBN[N]));
+  else if (vi == 0.0 && l - j != 0)
+    gv = 0;
+  else if (vi == 0.0)
+    gv = exp(-beta * (VBN[j - 1] + ENk[dtri(l) + l - j] + tmpV[l] - VBN[N])) / l;
+  else
+    gv = exp(-beta * (VBN[j - 1] + ENk[dtri(l) + l - j] + tmpV[l] - VBN[N]) + (l - j) * log(vi)) / l;
+  G[t] = gv;
+}
+
+cudaError_t fill_g(int N, double beta, double vi, const double *ENk, const double *VBN,
+                   const double *tmpV, double *G, cudaStream_t st) {
+  {
+    XK_PROF("fill_g");
+    k_fill_g<<<cdiv((size_t)N * N, 256), 256, 0, st>>>(N, beta, vi, ENk, VBN, tmpV, G);
+  }
+  return XK_LAUNCHED();
+}
+
+// ===================================================================
+// exchange-weighted spring forces: md_pimd_x.c:2674-2717
+// ===================================================================
+
+// gradient of the two springs at bead (ja, la) towards (jn, ln) and (jp, lp):
+// m w2 (x - x_n) + m w2 (x - x_p), md_pimd_x.c:2344-2367
+template <int D>
+__device__ inline void grad2(Geo g, const double *x, double mw2, int ja, int la, int jn, int ln,
+                             int jp, int lp, int image, double *gr) {
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    const double xa = x[sidx(ja, d, la, D, g.Ns)];
+    double a = xa - x[sidx(jn, d, ln, D, g.Ns)];
+    double c = xa - x[sidx(jp, d, lp, D, g.Ns)];
+    if (image) {
+      a = min_image(a, g.box[d], g.inv_box[d]);
+      c = min_image(c, g.box[d], g.inv_box[d]);
+    }
+    gr[d] = mw2 * a + mw2 * c;
+  }
+}
+
+// interior beads j = 2..P-1 (1-based): plain springs
+template <int D>
+__global__ void k_spring_interior(Geo g, const double *__restrict__ x,
+                                  const double *__restrict__ m, double w2, int image,
+                                  double *__restrict__ f) {
+  const int P2 = g.P - 2;
+  const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (P2 <= 0 || t >= (size_t)P2 * g.Ns) return;
+  const int l = (int)(t % g.Ns), j = (int)(t / g.Ns) + 1;  // 0-based bead index 1..P-2
+  if (l >= g.N) return;
+  const double mm = m[(size_t)j * g.Ns + l];
+  double gr[D];
+  grad2<D>(g, x, mm * w2, j, l, j + 1, l, j - 1, l, image, gr);
+#pragma unroll
+  for (int d = 0; d < D; ++d) f[sidx(j, d, l, D, g.Ns)] += -gr[d] / mm;
+}
+
+// bead 1 and bead P of every particle, weighted by G.  Block (32 x 8)
+// covers 32 particles and one slice of the partner index range; partial
+// sums go to scratch[js][side][d][l] and are added to f by k_exch_finish.
+constexpr int EX_TY = 8;
+
+template <int D>
+__global__ void k_exch_ends(Geo g, const double *__restrict__ x, const double *__restrict__ m,
+                            double w2, int image, const double *__restrict__ G,
+                            double *__restrict__ scratch, int nsplit) {
+  __shared__ double red[EX_TY][2 * D][32];
+  const int l = blockIdx.x * 32 + threadIdx.x;
+  const int js = blockIdx.y;
+  const int N = g.N, jP = g.P - 1;
+  double a1[D], aP[D];
+#pragma unroll
+  for (int d = 0; d < D; ++d) a1[d] = aP[d] = 0;
+  if (l < N) {
+    const double m1 = m[l], mP = m[(size_t)jP * g.Ns + l];
+    // partner q runs over this block's part of 0..N-1
+    for (int q = js * EX_TY + threadIdx.y; q < N; q += nsplit * EX_TY) {
+      double gr[D];
+      // bead 1 of l, previous bead = bead P of q, weight G[q][l]
+      const double g1 = G[(size_t)q * N + l];
+      if (g1 != 0.0) {
+        grad2<D>(g, x, m1 * w2, 0, l, 1, l, jP, q, image, gr);
+#pragma unroll
+        for (int d = 0; d < D; ++d) a1[d] += g1 * gr[d];
+      }
+      // bead P of l, next bead = bead 1 of q, weight G[l][q]
+      const double gP = G[(size_t)l * N + q];
+      if (gP != 0.0) {
+        grad2<D>(g, x, mP * w2, jP, l, jP - 1, l, 0, q, image, gr);
+#pragma unroll
+        for (int d = 0; d < D; ++d) aP[d] += gP * gr[d];
+      }
+    }
+  }
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    red[threadIdx.y][d][threadIdx.x] = a1[d];
+    red[threadIdx.y][D + d][threadIdx.x] = aP[d];
+  }
+  __syncthreads();
+  if (threadIdx.y == 0 && l < N) {
+#pragma unroll
+    for (int q = 0; q < 2 * D; ++q) {
+      double s = 0;
+      for (int y = 0; y < EX_TY; ++y) s += red[y][q][threadIdx.x];
+      scratch[((size_t)js * 2 * D + q) * g.Ns + l] = s;
+    }
+  }
+}
+
+template <int D>
+__global__ void k_exch_finish(Geo g, const double *__restrict__ m,
+                              const double *__restrict__ scratch, int nsplit,
+                              double *__restrict__ f) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= 2 * D * g.Ns) return;
+  const int l = t % g.Ns, q = t / g.Ns;  // q = side*D + d
+  if (l >= g.N) return;
+  const int side = q / D, d = q % D;
+  const int j = side ? g.P - 1 : 0;
+  double s = 0;
+  for (int js = 0; js < nsplit; ++js) s += scratch[((size_t)js * 2 * D + q) * g.Ns + l];
+  f[sidx(j, d, l, D, g.Ns)] += -s / m[(size_t)j * g.Ns + l];
+}
+
+static int exch_split(const Geo &g) {
+  const int tiles = (g.N + 31) / 32;
+  int ns = (2 * 152 + tiles - 1) / tiles;
+  const int maxs = (g.N + EX_TY - 1) / EX_TY;
+  if (ns > maxs) ns = maxs;
+  if (ns < 1) ns = 1;
+  return ns;
+}
+
+size_t exch_scratch_doubles(const Geo &g) { return (size_t)exch_split(g) * 2 * g.D * g.Ns; }
+
+cudaError_t exch_force(const Geo &g, const double *x, const double *m, double w2, int image,
+                       const double *G, double *f, double *scratch, cudaStream_t st) {
+  if (g.P > 2) {
+    const size_t n = (size_t)(g.P - 2) * g.Ns;
+    {
+      XK_PROF("spring_interior");
+      DISPATCH_D(g.D, k_spring_interior<D><<<cdiv(n, 256), 256, 0, st>>>(g, x, m, w2, image, f));
+    }
+    cudaError_t e = XK_LAUNCHED();
+    if (e != cudaSuccess) return e;
+  }
+  const int ns = exch_split(g);
+  dim3 grid((g.N + 31) / 32, ns), blk(32, EX_TY);
+  {
+    XK_PROF("exch_ends");
+    DISPATCH_D(g.D, k_exch_ends<D><<<grid, blk, 0, st>>>(g, x, m, w2, image, G, scratch, ns));
+  }
+  cudaError_t e = XK_LAUNCHED();
+  if (e != cudaSuccess) return e;
+  {
+    XK_PROF("exch_finish");
+    DISPATCH_D(g.D, k_exch_finish<D><<<cdiv(2 * g.D * g.Ns, 256), 256, 0, st>>>(g, m, scratch, ns, f));
+  }
+  return XK_LAUNCHED();
+}
+
+// ===================================================================
+// trap: md_pimd_x.c:1297-1391 (CPU :1370-1389), md_simulation_x.c:127-159
+// ===================================================================
+
+__device__ inline double trap_f(const TrapPrm &p, int d, double xv) {
+  if (p.kind == TRAP_HARMONIC) return -p.w * p.w * (xv - p.c[d]);
+  if (p.kind == TRAP_NEG_HARMONIC) return -(-p.w * p.w * (xv - p.c[d]));
+  return -p.w2[d] * p.w2[d] * (xv - p.c[d]);
+}
+
+__global__ void k_trap_force(Geo g, TrapPrm p, const double *__restrict__ x,
+                             double *__restrict__ f) {
+  const size_t s = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= g.slots() || (int)(s % g.Ns) >= g.N) return;
+  const int d = (int)((s / g.Ns) % g.D);
+  f[s] += trap_f(p, d, x[s]) / g.P;
+}
+
+cudaError_t trap_force(const Geo &g, const TrapPrm &p, const double *x, double *f,
+                       cudaStream_t st) {
+  {
+    XK_PROF("trap_force");
+    k_trap_force<<<cdiv(g.slots(), 256), 256, 0, st>>>(g, p, x, f);
+  }
+  return XK_LAUNCHED();
+}
+
+// deterministic final reduction of per-block partial sums into *acc
+__global__ void k_reduce_into(const double *__restrict__ part, int n, double scale, double add,
+                              double *acc) {
+  __shared__ double buf[33];
+  double s = 0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s += part[i];
+  s = block_sum(s, buf);
+  if (threadIdx.x == 0) *acc += s * scale + add;
+}
+
+static cudaError_t reduce_into(const double *part, int n, double scale, double add, double *acc,
+                               cudaStream_t st) {
+  {
+    XK_PROF("reduce_into");
+    k_reduce_into<<<1, 256, 0, st>>>(part, n, scale, add, acc);
+  }
+  return XK_LAUNCHED();
+}
+
+// md_statistics_x.c:322-338 energies
+template <int D>
+__global__ void k_trap_energy(Geo g, TrapPrm p, const double *__restrict__ x,
+                              const double *__restrict__ m, double *part) {
+  __shared__ double buf[33];
+  double e = 0;
+  for (size_t b = (size_t)blockIdx.x * blockDim.x + threadIdx.x; b < (size_t)g.N * g.P;
+       b += (size_t)gridDim.x * blockDim.x) {
+    const int l = (int)(b % g.N), j = (int)(b / g.N);
+    const double mm = m[(size_t)j * g.Ns + l];
+    if (p.kind == TRAP_HARMONIC_2) {
+      double r = 0;
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        const double t = x[sidx(j, d, l, D, g.Ns)] - p.c[d];
+        r += 0.5 * mm * p.w2[d] * p.w2[d] * t * t;
+      }
+      e += r;
+    } else {
+      double r2 = 0;
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        const double t = x[sidx(j, d, l, D, g.Ns)] - p.c[d];
+        r2 += t * t;
+      }
+      const double v = 0.5 * mm * p.w * p.w * r2;
+      e += p.kind == TRAP_HARMONIC ? v : -v;
+    }
+  }
+  e = block_sum(e, buf);
+  if (threadIdx.x == 0) part[blockIdx.x] = e;
+}
+
+cudaError_t trap_energy(const Geo &g, const TrapPrm &p, const double *x, const double *m,
+                        double *acc, double *scratch, cudaStream_t st) {
+  int nb = cdiv((size_t)g.N * g.P, 256);
+  if (nb > 304) nb = 304;
+  {
+    XK_PROF("trap_energy");
+    DISPATCH_D(g.D, k_trap_energy<D><<<nb, 256, 0, st>>>(g, p, x, m, scratch));
+  }
+  cudaError_t e = XK_LAUNCHED();
+  if (e != cudaSuccess) return e;
+  return reduce_into(scratch, nb, 1.0 / g.P, 0.0, acc, st);
+}
+
+// ===================================================================
+// pair forces and energies per bead slice: md_pimd_x.c:1527-1677
+// (CPU :1650-1675) and :1679-1824, potentials md_simulation_x.c:166-293,
+// md_statistics_x.c:340-396.
+//
+// One warp evaluates a 32 x 32 tile (I, J), I <= J, of one slice: lane i
+// keeps particle a = 32I + i; the partner data (position, mass, reaction
+// force) rotates through the lanes, so every unordered pair is evaluated
+// once and both forces are kept in registers.  Each particle's force from
+// the tiles of partner block t lands in scratch slot t exactly once; the
+// finishing kernel sums the slots in a fixed order and adds (sum)/P.
+// ===================================================================
+
+constexpr double SQRT_PI = 1.7724538509055160273;
+
+template <int D, int KIND>
+__device__ inline void pair_eval(const PairPrm &p, const Geo &g, const double *dx, double *F,
+                                 double &E, bool want_e) {
+  if (KIND == PAIR_GAUSSIAN || KIND == PAIR_PERIODIC_GAUSSIAN) {
+    double t[D], r2 = 0;
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      t[d] = dx[d];
+      if (KIND == PAIR_PERIODIC_GAUSSIAN) t[d] = min_image(t[d], g.box[d], g.inv_box[d]);
+      r2 += t[d] * t[d];
+    }
+    const double s2 = p.s * p.s;
+    const double mult = (p.g / (M_PI * s2)) * exp(-r2 / s2);
+#pragma unroll
+    for (int d = 0; d < D; ++d) F[d] = mult * (2 * t[d]) / s2;
+    if (want_e) E = mult;
+  } else if (KIND == PAIR_COULOMB || KIND == PAIR_PERIODIC_COULOMB) {
+    double t[D], r2 = 0;
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      t[d] = dx[d];
+      if (KIND == PAIR_PERIODIC_COULOMB) t[d] = min_image(t[d], g.box[d], g.inv_box[d]);
+      r2 += t[d] * t[d];
+    }
+    const double r = sqrt(r2);
+    const double mult = p.qs / (r2 * r);
+#pragma unroll
+    for (int d = 0; d < D; ++d) F[d] = mult * t[d];
+    if (want_e) E = p.qs / r;
+  } else if (KIND == PAIR_EWALD_REAL) {
+    // real-space images inside the reference's cube |n_i| <= nsum whose
+    // distance is below rcut (erfc(alpha rcut) < 1e-15)
+    int lo[3], hi[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      lo[d] = (int)ceil((dx[d] - p.rcut) * g.inv_box[d]);
+      hi[d] = (int)floor((dx[d] + p.rcut) * g.inv_box[d]);
+      lo[d] = lo[d] < -p.nsum ? -p.nsum : lo[d];
+      hi[d] = hi[d] > p.nsum ? p.nsum : hi[d];
+    }
+    const double rc2 = p.rcut * p.rcut, a = p.alpha, a2 = a * a;
+    double F0 = 0, F1 = 0, F2 = 0, e = 0;
+    for (int n0 = lo[0]; n0 <= hi[0]; ++n0) {
+      const double t0 = dx[0] - n0 * g.box[0];
+      for (int n1 = lo[1]; n1 <= hi[1]; ++n1) {
+        const double t1 = dx[1] - n1 * g.box[1];
+        for (int n2 = lo[2]; n2 <= hi[2]; ++n2) {
+          const double t2 = dx[2] - n2 * g.box[2];
+          const double R2 = t0 * t0 + t1 * t1 + t2 * t2;
+          if (R2 >= rc2) continue;
+          const double R = sqrt(R2);
+          const double ec = erfc(a * R);
+          const double mult = p.qs * 2 * a * exp(-a2 * R2) / (SQRT_PI * R2) + p.qs * ec / (R2 * R);
+          F0 += t0 * mult;
+          F1 += t1 * mult;
+          F2 += t2 * mult;
+          if (want_e) e += ec / R;
+        }
+      }
+    }
+    F[0] = F0;
+    if (D > 1) F[1] = F1;
+    if (D > 2) F[2] = F2;
+    if (want_e) E = p.qs * e;
+  }
+}
+
+template <int D, int KIND, bool ENERGY>
+__global__ void __launch_bounds__(256) k_pair_tiles(Geo g, PairPrm p,
+                                                    const double *__restrict__ x,
+                                                    const double *__restrict__ m,
+                                                    double *__restrict__ out, int T, int jobs) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= jobs * g.P) return;
+  const int j = warp / jobs;
+  int job = warp % jobs, I = 0;
+  while (job >= T - I) {
+    job -= T - I;
+    ++I;
+  }
+  const int J = I + job;
+  const int a = I * 32 + lane, b0 = J * 32 + lane;
+  const bool va = a < g.N, vb = b0 < g.N;
+  double xa[D], xb[D], fa[D], fb[D];
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    xa[d] = va ? x[sidx(j, d, a, D, g.Ns)] : 0.0;
+    xb[d] = vb ? x[sidx(j, d, b0, D, g.Ns)] : 0.0;
+    fa[d] = fb[d] = 0.0;
+  }
+  const double ma = va ? m[(size_t)j * g.Ns + a] : 1.0;
+  double mb = vb ? m[(size_t)j * g.Ns + b0] : 1.0;
+  double ea = 0;
+  for (int s = 0; s < 32; ++s) {
+    const int bi = J * 32 + ((lane + s) & 31);
+    const bool act = va && bi < g.N && (I != J || a > bi);
+    if (act) {
+      double dx[D], F[D], E = 0;
+#pragma unroll
+      for (int d = 0; d < D; ++d) dx[d] = xa[d] - xb[d];
+      pair_eval<D, KIND>(p, g, dx, F, E, ENERGY);
+      if (ENERGY) {
+        ea += E;
+      } else {
+        // the reference divides by the mass of the higher-index particle
+        const double inv = 1.0 / (a > bi ? ma : mb);
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+          fa[d] += F[d] * inv;
+          fb[d] -= F[d] * inv;
+        }
+      }
+    }
+    const int src = (lane + 1) & 31;
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      xb[d] = __shfl_sync(FULL, xb[d], src);
+      if (!ENERGY) fb[d] = __shfl_sync(FULL, fb[d], src);
+    }
+    mb = __shfl_sync(FULL, mb, src);
+  }
+  if (ENERGY) {
+    ea = warp_sum(ea);
+    if (lane == 0) out[warp] = ea;
+    return;
+  }
+  // slot layout: out[((t*P + j)*D + d)*Ns + l]
+  if (I == J) {
+    if (va) {
+#pragma unroll
+      for (int d = 0; d < D; ++d) out[(((size_t)I * g.P + j) * D + d) * g.Ns + a] = fa[d] + fb[d];
+    }
+  } else {
+    if (va) {
+#pragma unroll
+      for (int d = 0; d < D; ++d) out[(((size_t)J * g.P + j) * D + d) * g.Ns + a] = fa[d];
+    }
+    if (vb) {
+#pragma unroll
+      for (int d = 0; d < D; ++d) out[(((size_t)I * g.P + j) * D + d) * g.Ns + b0] = fb[d];
+    }
+  }
+}
+
+__global__ void k_pair_finish(Geo g, const double *__restrict__ part, int T, double scale,
+                              double *__restrict__ f) {
+  const size_t s = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const size_t S = g.slots();
+  if (s >= S || (int)(s % g.Ns) >= g.N) return;
+  double acc = 0;
+  for (int t = 0; t < T; ++t) acc += part[(size_t)t * S + s];
+  f[s] += acc * scale;
+}
+
+size_t pair_scratch_doubles(const Geo &g) {
+  const int T = (g.N + 31) / 32;
+  const size_t jobs = (size_t)T * (T + 1) / 2;
+  size_t a = (size_t)T * g.slots();
+  size_t b = jobs * g.P;
+  return a > b ? a : b;
+}
+
+template <int D, bool ENERGY>
+static cudaError_t pair_launch(const Geo &g, const PairPrm &p, const double *x, const double *m,
+                               double *out, int T, int jobs, cudaStream_t st) {
+  const size_t thr = (size_t)jobs * g.P * 32;
+  const int nb = cdiv(thr, 256);
+  switch (p.kind) {
+    case PAIR_GAUSSIAN:
+      {
+        XK_PROF("pair_tiles_gauss");
+        k_pair_tiles<D, PAIR_GAUSSIAN, ENERGY><<<nb, 256, 0, st>>>(g, p, x, m, out, T, jobs);
+      }
+      break;
+    case PAIR_PERIODIC_GAUSSIAN:
+      {
+        XK_PROF("pair_tiles_pgauss");
+        k_pair_tiles<D, PAIR_PERIODIC_GAUSSIAN, ENERGY><<<nb, 256, 0, st>>>(g, p, x, m, out, T, jobs);
+      }
+      break;
+    case PAIR_COULOMB:
+      {
+        XK_PROF("pair_tiles_coul");
+        k_pair_tiles<D, PAIR_COULOMB, ENERGY><<<nb, 256, 0, st>>>(g, p, x, m, out, T, jobs);
+      }
+      break;
+    case PAIR_PERIODIC_COULOMB:
+      {
+        XK_PROF("pair_tiles_pcoul");
+        k_pair_tiles<D, PAIR_PERIODIC_COULOMB, ENERGY><<<nb, 256, 0, st>>>(g, p, x, m, out, T, jobs);
+      }
+      break;
+    case PAIR_EWALD_REAL:
+      if (D != 3) return cudaErrorInvalidValue;
+      {
+        XK_PROF("pair_tiles_ewald_real");
+        k_pair_tiles<D, PAIR_EWALD_REAL, ENERGY><<<nb, 256, 0, st>>>(g, p, x, m, out, T, jobs);
+      }
+      break;
+    default:
+      return cudaErrorInvalidValue;
+  }
+  return XK_LAUNCHED();
+}
+
+cudaError_t pair_force(const Geo &g, const PairPrm &p, const double *x, const double *m,
+                       double *f, double *scratch, cudaStream_t st) {
+  const int T = (g.N + 31) / 32;
+  const int jobs = T * (T + 1) / 2;
+  cudaError_t e;
+  DISPATCH_D(g.D, e = (pair_launch<D, false>(g, p, x, m, scratch, T, jobs, st)));
+  if (e != cudaSuccess) return e;
+  {
+    XK_PROF("pair_finish");
+    k_pair_finish<<<cdiv(g.slots(), 256), 256, 0, st>>>(g, scratch, T, 1.0 / g.P, f);
+  }
+  return XK_LAUNCHED();
+}
+
+cudaError_t pair_energy(const Geo &g, const PairPrm &p, const double *x, double *acc,
+                        double *scratch, cudaStream_t st) {
+  const int T = (g.N + 31) / 32;
+  const int jobs = T * (T + 1) / 2;
+  cudaError_t e;
+  DISPATCH_D(g.D, e = (pair_launch<D, true>(g, p, x, nullptr, scratch, T, jobs, st)));
+  if (e != cudaSuccess) return e;
+  // the Ewald energy carries -pi/(alpha^2 V) per pair (md_statistics_x.c:385)
+  double add = 0;
+  if (p.kind == PAIR_EWALD_REAL) {
+    const double V = g.box[0] * g.box[1] * g.box[2];
+    add = -p.qs * M_PI / (p.alpha * p.alpha * V) * ((double)g.N * (g.N - 1) / 2);
+  }
+  return reduce_into(scratch, jobs * g.P, 1.0 / g.P, add, acc, st);
+}
+
+// ===================================================================
+// Ewald reciprocal space through structure factors (md_simulation_x.c:
+// 259-280 force, md_statistics_x.c:364-385 energy).  For every wave vector
+// n of the half cube H (|n_i| <= nsum, first non-zero component positive)
+//   S_j(n) = sum_l exp(i 2 pi n.x_l / L)            (bead slice j)
+//   F_a    = 4 pi/(m P) sum_{n in H} (n/L) c(n) Im(exp(i theta_a) S_j(n)*)
+//   E_j    = sum_{n in H} c(n) (|S_j(n)|^2 - N)
+// with c(n) = s exp(-pi^2 G^2/alpha^2)/(pi V G^2): the same sums as the
+// reference's per-pair loops, regrouped (the l = l2 term of sin vanishes).
+// Wave vectors are grouped in columns (nx, ny) with nz contiguous, so the
+// phase exp(i(theta_x + theta_y)) is formed once per column.
+// ===================================================================
+
+struct Col {
+  int nx, ny, nz0, off;
+};
+
+static std::vector<Col> columns(int ns) {
+  std::vector<Col> c;
+  int off = 0;
+  for (int nx = 0; nx <= ns; ++nx)
+    for (int ny = -ns; ny <= ns; ++ny) {
+      if (nx == 0 && ny < 0) continue;
+      const int nz0 = (nx == 0 && ny == 0) ? 1 : -ns;
+      c.push_back({nx, ny, nz0, off});
+      off += ns - nz0 + 1;
+    }
+  return c;
+}
+
+int recip_count(int ns) { return ((2 * ns + 1) * (2 * ns + 1) * (2 * ns + 1) - 1) / 2; }
+
+size_t recip_phase_doubles(const Geo &g, int ns) { return (size_t)g.P * 3 * (ns + 1) * g.Ns * 2; }
+
+// phase[((j*3 + d)*(ns+1) + n)*Ns + l] = exp(i 2 pi n x / L) as (re, im)
+__global__ void k_phase(Geo g, int ns, const double *__restrict__ x, double2 *__restrict__ ph) {
+  const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (size_t)g.P * 3 * g.Ns) return;
+  const int l = (int)(t % g.Ns);
+  const int jd = (int)(t / g.Ns);  // j*3 + d
+  const int d = jd % 3;
+  double s1 = 0, c1 = 1;
+  if (l < g.N) sincospi(2.0 * x[t] * g.inv_box[d], &s1, &c1);
+  double re = 1, im = 0;
+  double2 *o = ph + (size_t)jd * (ns + 1) * g.Ns + l;
+  o[0] = make_double2(1.0, 0.0);
+  for (int n = 1; n <= ns; ++n) {
+    const double r2 = re * c1 - im * s1, i2 = re * s1 + im * c1;
+    re = r2;
+    im = i2;
+    o[(size_t)n * g.Ns] = make_double2(re, im);
+  }
+}
+
+__device__ inline double2 cmul(double2 a, double2 b) {
+  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ inline double2 phase_at(const double2 *ph, const Geo &g, int ns, int j, int d, int n,
+                                   int l) {
+  const double2 v = ph[(((size_t)j * 3 + d) * (ns + 1) + (n < 0 ? -n : n)) * g.Ns + l];
+  return n < 0 ? make_double2(v.x, -v.y) : v;
+}
+
+// S_j(n) for one column (nx, ny) and all its nz: block per (slice, column)
+template <int NS>
+__global__ void __launch_bounds__(256) k_sk(Geo g, const double2 *__restrict__ ph,
+                                            const int4 *__restrict__ cols,
+                                            double2 *__restrict__ S, int nk) {
+  constexpr int NZ = 2 * NS + 1;
+  __shared__ double red[8][2 * NZ];
+  const int j = blockIdx.y;
+  const int4 c = cols[blockIdx.x];  // nx, ny, nz0, off
+  double2 acc[NZ];
+#pragma unroll
+  for (int q = 0; q < NZ; ++q) acc[q] = make_double2(0, 0);
+  for (int l = threadIdx.x; l < g.N; l += blockDim.x) {
+    const double2 exy = cmul(phase_at(ph, g, NS, j, 0, c.x, l), phase_at(ph, g, NS, j, 1, c.y, l));
+    const double2 *pz = ph + (((size_t)j * 3 + 2) * (NS + 1)) * g.Ns + l;
+    double2 ez[NS + 1];
+#pragma unroll
+    for (int n = 0; n <= NS; ++n) ez[n] = pz[(size_t)n * g.Ns];
+#pragma unroll
+    for (int q = 0; q < NZ; ++q) {
+      const int nz = q - NS;
+      const double2 e = nz < 0 ? make_double2(ez[-nz].x, -ez[-nz].y) : ez[nz];
+      const double2 v = cmul(exy, e);
+      acc[q].x += v.x;
+      acc[q].y += v.y;
+    }
+  }
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int q = 0; q < NZ; ++q) {
+    const double re = warp_sum(acc[q].x), im = warp_sum(acc[q].y);
+    if (lane == 0) {
+      red[w][2 * q] = re;
+      red[w][2 * q + 1] = im;
+    }
+  }
+  __syncthreads();
+  const int nw = blockDim.x >> 5;
+  for (int q = threadIdx.x; q < 2 * NZ; q += blockDim.x) {
+    const int nz = q / 2 - NS;
+    if (nz < c.z) continue;
+    double s = 0;
+    for (int y = 0; y < nw; ++y) s += red[y][q];
+    double *o = (double *)&S[(size_t)j * nk + c.w + (nz - c.z)];
+    o[q & 1] = s;
+  }
+}
+
+// forces: block per (slice, 128 particles); S and c(n) of the slice staged
+// in shared memory
+template <int NS>
+__global__ void __launch_bounds__(128) k_recip_force(Geo g, const double2 *__restrict__ ph,
+                                                     const int4 *__restrict__ cols, int ncol,
+                                                     const double2 *__restrict__ S,
+                                                     const double *__restrict__ coef, int nk,
+                                                     double scale, double *__restrict__ f) {
+  extern __shared__ double sm[];
+  double2 *sS = (double2 *)sm;
+  double *sc = sm + 2 * nk;
+  const int j = blockIdx.y;
+  for (int k = threadIdx.x; k < nk; k += blockDim.x) {
+    sS[k] = S[(size_t)j * nk + k];
+    sc[k] = coef[k];
+  }
+  __syncthreads();
+  const int l = blockIdx.x * blockDim.x + threadIdx.x;
+  if (l >= g.N) return;
+  double2 ez[NS + 1];
+  const double2 *pz = ph + (((size_t)j * 3 + 2) * (NS + 1)) * g.Ns + l;
+#pragma unroll
+  for (int n = 0; n <= NS; ++n) ez[n] = pz[(size_t)n * g.Ns];
+  double Fx = 0, Fy = 0, Fz = 0;
+  for (int ci = 0; ci < ncol; ++ci) {
+    const int4 c = cols[ci];
+    const double2 exy = cmul(phase_at(ph, g, NS, j, 0, c.x, l), phase_at(ph, g, NS, j, 1, c.y, l));
+    double Tsum = 0, Zsum = 0;
+#pragma unroll
+    for (int q = 0; q < 2 * NS + 1; ++q) {
+      const int nz = q - NS;
+      if (nz < c.z) continue;
+      const double2 e = cmul(exy, nz < 0 ? make_double2(ez[-nz].x, -ez[-nz].y) : ez[nz]);
+      const int k = c.w + (nz - c.z);
+      const double2 s = sS[k];
+      const double wv = sc[k] * (e.y * s.x - e.x * s.y);
+      Tsum += wv;
+      Zsum += nz * wv;
+    }
+    Fx += c.x * Tsum;
+    Fy += c.y * Tsum;
+    Fz += Zsum;
+  }
+  f[sidx(j, 0, l, 3, g.Ns)] += scale * Fx * g.inv_box[0];
+  f[sidx(j, 1, l, 3, g.Ns)] += scale * Fy * g.inv_box[1];
+  f[sidx(j, 2, l, 3, g.Ns)] += scale * Fz * g.inv_box[2];
+}
+
+__global__ void k_recip_energy(Geo g, const double2 *__restrict__ S, const double *__restrict__ coef,
+                               int nk, double *part) {
+  __shared__ double buf[33];
+  const int j = blockIdx.x;
+  double e = 0;
+  for (int k = threadIdx.x; k < nk; k += blockDim.x) {
+    const double2 s = S[(size_t)j * nk + k];
+    e += coef[k] * (s.x * s.x + s.y * s.y - g.N);
+  }
+  e = block_sum(e, buf);
+  if (threadIdx.x == 0) part[j] = e;
+}
+
+cudaError_t recip_setup(const Geo &g, int ns, double alpha, double qs, Recip &r,
+                        cudaStream_t st) {
+  // host-side tables: column descriptors then c(n) in column order
+  std::vector<Col> cols = columns(ns);
+  const int nk = recip_count(ns);
+  std::vector<double> coef(nk);
+  std::vector<int4> cd(cols.size());
+  const double V = g.box[0] * g.box[1] * g.box[2];
+  for (size_t i = 0; i < cols.size(); ++i) {
+    const Col &c = cols[i];
+    cd[i] = make_int4(c.nx, c.ny, c.nz0, c.off);
+    for (int nz = c.nz0; nz <= ns; ++nz) {
+      const double gx = c.nx / g.box[0], gy = c.ny / g.box[1], gz = nz / g.box[2];
+      const double G = sqrt(gx * gx + gy * gy + gz * gz);
+      coef[c.off + nz - c.nz0] = qs * pow(G, -2) * exp(-M_PI * M_PI * G * G / (alpha * alpha)) / (V * M_PI);
+    }
+  }
+  r.nsum = ns;
+  r.nk = nk;
+  cudaError_t e = cudaMemcpyAsync(r.coef, coef.data(), sizeof(double) * nk, cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return e;
+  e = cudaMemcpyAsync(r.kvec, cd.data(), sizeof(int4) * cd.size(), cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return e;
+  return cudaStreamSynchronize(st);
+}
+
+static int ncols(int ns) { return ns * (2 * ns + 1) + ns + 1; }
+
+#define DISPATCH_NS(nsv, ...)                                         \
+  switch (nsv) {                                                      \
+    case 1: { constexpr int NS = 1; __VA_ARGS__; } break;             \
+    case 2: { constexpr int NS = 2; __VA_ARGS__; } break;             \
+    case 3: { constexpr int NS = 3; __VA_ARGS__; } break;             \
+    case 4: { constexpr int NS = 4; __VA_ARGS__; } break;             \
+    case 5: { constexpr int NS = 5; __VA_ARGS__; } break;             \
+    case 6: { constexpr int NS = 6; __VA_ARGS__; } break;             \
+    case 7: { constexpr int NS = 7; __VA_ARGS__; } break;             \
+    case 8: { constexpr int NS = 8; __VA_ARGS__; } break;             \
+    case 9: { constexpr int NS = 9; __VA_ARGS__; } break;             \
+    case 10: { constexpr int NS = 10; __VA_ARGS__; } break;           \
+    case 11: { constexpr int NS = 11; __VA_ARGS__; } break;           \
+    case 12: { constexpr int NS = 12; __VA_ARGS__; } break;           \
+    default: return cudaErrorInvalidValue;                            \
+  }
+
+static cudaError_t structure_factors(const Geo &g, const Recip &r, const double *x,
+                                     cudaStream_t st) {
+  const size_t n = (size_t)g.P * 3 * g.Ns;
+  {
+    XK_PROF("phase");
+    k_phase<<<cdiv(n, 256), 256, 0, st>>>(g, r.nsum, x, (double2 *)r.phase);
+  }
+  cudaError_t e = XK_LAUNCHED();
+  if (e != cudaSuccess) return e;
+  dim3 grid(ncols(r.nsum), g.P);
+  int thr = ((g.N + 31) / 32) * 32;
+  if (thr > 256) thr = 256;
+  {
+    XK_PROF("sk");
+    DISPATCH_NS(r.nsum, k_sk<NS><<<grid, thr, 0, st>>>(g, (const double2 *)r.phase,
+                                                       (const int4 *)r.kvec, (double2 *)r.S, r.nk));
+  }
+  return XK_LAUNCHED();
+}
+
+cudaError_t recip_force(const Geo &g, const Recip &r, const double *x, double inv_mP, double *f,
+                        cudaStream_t st) {
+  if (g.D != 3) return cudaErrorInvalidValue;
+  cudaError_t e = structure_factors(g, r, x, st);
+  if (e != cudaSuccess) return e;
+  const size_t smem = sizeof(double) * 3 * r.nk;
+  dim3 grid((g.N + 127) / 128, g.P);
+  DISPATCH_NS(r.nsum, {
+    auto kf = k_recip_force<NS>;
+    // opt in to the largest dynamic shared memory once per instantiation
+    static bool opted = false;
+    if (!opted) {
+      cudaError_t ea = cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+      if (ea != cudaSuccess) return ea;
+      opted = true;
+    }
+    {
+      XK_PROF("recip_force");
+      kf<<<grid, 128, smem, st>>>(g, (const double2 *)r.phase, (const int4 *)r.kvec, ncols(r.nsum),
+                                  (const double2 *)r.S, r.coef, r.nk, 4 * M_PI * inv_mP, f);
+    }
+  });
+  return XK_LAUNCHED();
+}
+
+cudaError_t recip_energy(const Geo &g, const Recip &r, const double *x, double *acc,
+                         double *scratch, cudaStream_t st) {
+  if (g.D != 3) return cudaErrorInvalidValue;
+  cudaError_t e = structure_factors(g, r, x, st);
+  if (e != cudaSuccess) return e;
+  {
+    XK_PROF("recip_energy");
+    k_recip_energy<<<g.P, 256, 0, st>>>(g, (const double2 *)r.S, r.coef, r.nk, scratch);
+  }
+  e = XK_LAUNCHED();
+  if (e != cudaSuccess) return e;
+  return reduce_into(scratch, g.P, 1.0 / g.P, 0.0, acc, st);
+}
+
+// ===================================================================
+// estimators
+// ===================================================================
+
+// primitive (md_pimd_x.c:1267-1293) and, with ENk2, virial
+// (md_pimd_x.c:4288-4322) exchange recursions; adds res[N] + add to *acc
+__global__ void k_vbn_energy(int N, double beta, double vi, double add,
+                             const double *__restrict__ ENk, const double *__restrict__ VBN,
+                             const double *__restrict__ ENk2, double *acc) {
+  extern __shared__ double sh[];
+  double *res = sh;            // N+1
+  double *bmin = sh + N + 1;   // 33
+  double *bs1 = bmin + 33;     // 33
+  double *bs2 = bs1 + 33;      // 33
+  const double lnvi = vi != 0.0 ? log(vi) : 0.0;
+  const double *E2 = ENk2 ? ENk2 : ENk;
+  if (threadIdx.x == 0) res[0] = 0;
+  __syncthreads();
+  for (int n = 1; n <= N; ++n) {
+    const double *row = ENk + dtri(n), *row2 = E2 + dtri(n);
+    double mloc = 1e10;
+    if (vi == 0.0) {
+      mloc = beta * (row[0] + VBN[n - 1]);
+    } else {
+      for (int k = threadIdx.x + 1; k <= n; k += blockDim.x) {
+        const double t = -(k - 1) * lnvi + beta * (row[k - 1] + VBN[n - k]);
+        if (t < mloc) mloc = t;
+      }
+      mloc = block_min(mloc, 1e10, bmin);
+    }
+    double s1 = 0, s2 = 0;
+    for (int k = threadIdx.x + 1; k <= n; k += blockDim.x) {
+      if (vi == 0.0 && k != 1) continue;
+      const double E = row[k - 1] + VBN[n - k];
+      const double w = (vi == 0.0) ? exp(-beta * E + mloc) : exp((k - 1) * lnvi - beta * E + mloc);
+      s1 += w;
+      s2 += (res[n - k] - row2[k - 1]) * w;
+    }
+    s1 = block_sum(s1, bs1);
+    s2 = block_sum(s2, bs2);
+    if (threadIdx.x == 0) res[n] = s2 / s1;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *acc += res[N] + add;
+}
+
+cudaError_t vbn_energy(int N, double beta, double vi, double add, const double *ENk,
+                       const double *VBN, const double *ENk2, double *acc, cudaStream_t st) {
+  const size_t smem = sizeof(double) * (N + 1 + 99);
+  {
+    XK_PROF("vbn_energy");
+    k_vbn_energy<<<1, rec_threads(N), smem, st>>>(N, beta, vi, add, ENk, VBN, ENk2, acc);
+  }
+  return XK_LAUNCHED();
+}
+
+// sum over beads j >= 2 of -(x_j - x_1).F m: md_pimd_x.c:4323-4345
+template <int D>
+__global__ void k_force_virial(Geo g, const double *__restrict__ x, const double *__restrict__ f,
+                               const double *__restrict__ m, int image, double *part) {
+  __shared__ double buf[33];
+  double e = 0;
+  const size_t nb = (size_t)(g.P - 1) * g.N;
+  for (size_t b = (size_t)blockIdx.x * blockDim.x + threadIdx.x; b < nb;
+       b += (size_t)gridDim.x * blockDim.x) {
+    const int l = (int)(b % g.N), j = (int)(b / g.N) + 1;
+    const double mm = m[(size_t)j * g.Ns + l];
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      double t = x[sidx(j, d, l, D, g.Ns)] - x[sidx(0, d, l, D, g.Ns)];
+      if (image) t = min_image(t, g.box[d], g.inv_box[d]);
+      e += -t * f[sidx(j, d, l, D, g.Ns)] * mm;
+    }
+  }
+  e = block_sum(e, buf);
+  if (threadIdx.x == 0) part[blockIdx.x] = e;
+}
+
+cudaError_t force_virial(const Geo &g, const double *x, const double *f, const double *m,
+                         int image, double *acc, double *scratch, cudaStream_t st) {
+  int nb = cdiv((size_t)g.N * (g.P > 1 ? g.P - 1 : 1), 256);
+  if (nb > 304) nb = 304;
+  {
+    XK_PROF("force_virial");
+    DISPATCH_D(g.D, k_force_virial<D><<<nb, 256, 0, st>>>(g, x, f, m, image, scratch));
+  }
+  cudaError_t e = XK_LAUNCHED();
+  if (e != cudaSuccess) return e;
+  return reduce_into(scratch, nb, 0.5, 0.0, acc, st);
+}
+
+__global__ void k_add_scalar(double *acc, double v) { *acc += v; }
+
+cudaError_t add_scalar(double *acc, double v, cudaStream_t st) {
+  {
+    XK_PROF("add_scalar");
+    k_add_scalar<<<1, 1, 0, st>>>(acc, v);
+  }
+  return XK_LAUNCHED();
+}
+
+}  // namespace xk
+
+namespace xk {
+
+// ===================================================================
+// FP64 pipe probe: eight independent FMA chains per thread, enough warps to
+// fill every SM.  Gives the FP64 roofline denominator of this GPU.
+// ===================================================================
+__global__ void k_dfma_probe(double *out, int iters, double a, double b) {
+  double x0 = threadIdx.x * 1e-3, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3;
+  double x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+  for (int i = 0; i < iters; ++i) {
+    x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
+    x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
+  }
+  out[(size_t)blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+}
+
+double fp64_peak_tflops(cudaStream_t st) {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int blocks = sms * 8, threads = 256, iters = 2048;
+  double *out = nullptr;
+  if (cudaMallocAsync(&out, sizeof(double) * blocks * threads, st) != cudaSuccess) return -1;
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  double best = 0;
+  for (int rep = 0; rep < 3; ++rep) {
+    cudaEventRecord(a, st);
+    k_dfma_probe<<<blocks, threads, 0, st>>>(out, iters, 0.999999, 1e-7);
+    cudaEventRecord(b, st);
+    cudaEventSynchronize(b);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, a, b);
+    const double tf = 2.0 * 8 * iters * (double)blocks * threads / (ms * 1e-3) / 1e12;
+    if (tf > best) best = tf;
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaFreeAsync(out, st);
+  cudaStreamSynchronize(st);
+  return cudaGetLastError() == cudaSuccess ? best : -1;
+}
+
+}  // namespace xk

@@ -1,0 +1,149 @@
+// xmd_kernels.cuh -- launch interface of the sm_103a kernels behind libxmd_x.
+//
+// Every function enqueues work on `st` and returns the launch status.  All
+// pointers are device pointers.  Bead data is kept slice-major ("SoA"):
+//     x[(j*D + d)*Ns + l]   particle l = 0..N-1, bead j = 0..P-1, dim d
+// with Ns = N rounded up to a multiple of 4, so that every bead slice starts
+// on a 32-byte boundary and a slice's coordinates are contiguous.  Masses
+// are m[j*Ns + l].  Thermostat chains with one DOF each ("fast" chains) are
+// stored in the same slot order, member i of the chain at slot s being
+// th[i*S + s] with S = P*D*Ns.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+#include <string>
+
+#ifdef __CUDACC__
+#define XK_HD __host__ __device__
+#else
+#define XK_HD
+#endif
+
+namespace xk {
+
+struct Geo {
+  int D, N, P, Ns;
+  double box[3];
+  double inv_box[3];
+  XK_HD size_t slots() const { return (size_t)P * D * Ns; }
+};
+
+inline int pad_n(int N) { return (N + 3) & ~3; }
+inline size_t tri(int n) { return (size_t)n * (n - 1) / 2; }  // row start, 1-based n
+inline size_t ntri(int n) { return (size_t)n * (n + 1) / 2; }
+
+// count of kernels launched by this library (for launch accounting)
+uint64_t launch_count();
+
+// live per-kernel timing with CUDA events; report is "name total_ms launches;..."
+void profile_enable(bool on);
+std::string profile_report();
+// measured FP64 FMA throughput of this GPU in TFLOP/s (-1 on failure)
+double fp64_peak_tflops(cudaStream_t st);
+
+// ---- layout conversion (host AoS records <-> device SoA) ----
+cudaError_t aos_to_soa(const Geo &g, const double *aos, double *x, double *v, double *f,
+                       double *m, cudaStream_t st);
+cudaError_t soa_to_aos(const Geo &g, double *aos, const double *x, const double *v,
+                       const double *f, const double *m, cudaStream_t st);
+// chains: host records {int f; double theta[L], vtheta[L], Q[L]} of rec_bytes each
+cudaError_t chains_to_dev(const Geo &g, int L, int nf, bool fast, const unsigned char *rec,
+                          size_t rec_bytes, double *th, double *vt, double *Q, cudaStream_t st);
+cudaError_t chains_to_host(const Geo &g, int L, int nf, bool fast, unsigned char *rec,
+                           size_t rec_bytes, const double *th, const double *vt,
+                           const double *Q, cudaStream_t st);
+
+// ---- integrator ----
+struct Chains {
+  bool fast;            // one DOF per chain, chains in slot order
+  int L, nf;            // chain length, number of chains
+  double *th, *vt, *Q;  // [L][S] (fast) or [L][nf] (grouped)
+  const int *cf;        // grouped: nhcs[i].f
+  const int *c0;        // grouped: first DOF (reference numbering)
+  const int *c2;        // grouped: number of DOFs updated
+  int ndof;             // D * beads
+};
+cudaError_t nhc_vv3(const Geo &g, int half, const Chains &c, double *x, double *v,
+                    const double *f, const double *m, double kT, double h, cudaStream_t st);
+cudaError_t wrap_box(const Geo &g, double *x, cudaStream_t st);
+cudaError_t zero(double *p, size_t n, cudaStream_t st);
+
+// ---- exchange ----
+cudaError_t fill_enk(const Geo &g, const double *x, const double *m, double w2, int image,
+                     double *Eint, double *ENk, cudaStream_t st);
+cudaError_t fill_enk2(const Geo &g, const double *x, const double *m, double w2, int image,
+                      double *ENk2, cudaStream_t st);
+cudaError_t fill_vb(int N, double beta, double vi, const double *ENk, double *VBN,
+                    cudaStream_t st);
+cudaError_t back_vb(int N, double beta, double vi, const double *ENk, double *tmpV,
+                    cudaStream_t st);
+cudaError_t fill_g(int N, double beta, double vi, const double *ENk, const double *VBN,
+                   const double *tmpV, double *G, cudaStream_t st);
+// scratch: at least exch_scratch_doubles(g) doubles
+size_t exch_scratch_doubles(const Geo &g);
+cudaError_t exch_force(const Geo &g, const double *x, const double *m, double w2, int image,
+                       const double *G, double *f, double *scratch, cudaStream_t st);
+
+// ---- external forces ----
+enum TrapKind { TRAP_HARMONIC = 1, TRAP_HARMONIC_2 = 2, TRAP_NEG_HARMONIC = 3 };
+struct TrapPrm {
+  int kind;
+  double w;
+  double w2[3];
+  double c[3];
+};
+cudaError_t trap_force(const Geo &g, const TrapPrm &p, const double *x, double *f,
+                       cudaStream_t st);
+// energy sum over beads of V(x)/P, added to *acc
+cudaError_t trap_energy(const Geo &g, const TrapPrm &p, const double *x, const double *m,
+                        double *acc, double *scratch, cudaStream_t st);
+
+enum PairKind {
+  PAIR_GAUSSIAN = 1,
+  PAIR_PERIODIC_GAUSSIAN = 2,
+  PAIR_COULOMB = 3,
+  PAIR_PERIODIC_COULOMB = 4,
+  PAIR_EWALD_REAL = 5
+};
+struct PairPrm {
+  int kind;
+  double g, s;          // Gaussian strength / range
+  double qs;            // Coulomb strength
+  double alpha;         // Ewald splitting
+  int nsum;             // Ewald image cube
+  double rcut;          // Ewald real-space cut-off radius
+};
+size_t pair_scratch_doubles(const Geo &g);
+cudaError_t pair_force(const Geo &g, const PairPrm &p, const double *x, const double *m,
+                       double *f, double *scratch, cudaStream_t st);
+cudaError_t pair_energy(const Geo &g, const PairPrm &p, const double *x, double *acc,
+                        double *scratch, cudaStream_t st);
+
+// Ewald reciprocal space through structure factors (D = 3)
+struct Recip {
+  int nsum;
+  int nk;              // half-space wave vectors
+  double *coef;        // [nk] s * exp(-pi^2 G^2/alpha^2) / (pi V G^2)
+  int *kvec;           // column table: int4 (nx, ny, first nz, offset of its first k)
+  double *phase;       // [P][3][nsum+1][Ns] complex
+  double *S;           // [P][nk] complex
+};
+size_t recip_phase_doubles(const Geo &g, int nsum);
+int recip_count(int nsum);
+cudaError_t recip_setup(const Geo &g, int nsum, double alpha, double qs, Recip &r,
+                        cudaStream_t st);
+cudaError_t recip_force(const Geo &g, const Recip &r, const double *x, double inv_mP,
+                        double *f, cudaStream_t st);
+cudaError_t recip_energy(const Geo &g, const Recip &r, const double *x, double *acc,
+                         double *scratch, cudaStream_t st);
+
+// ---- estimators ----
+cudaError_t vbn_energy(int N, double beta, double vi, double add, const double *ENk,
+                       const double *VBN, const double *ENk2, double *acc, cudaStream_t st);
+cudaError_t force_virial(const Geo &g, const double *x, const double *f, const double *m,
+                         int image, double *acc, double *scratch, cudaStream_t st);
+cudaError_t add_scalar(double *acc, double v, cudaStream_t st);
+
+}  // namespace xk

@@ -1,0 +1,577 @@
+// xmd_runtime.cpp -- CUDA runtime layer of libxmd_x: errors, the stream,
+// graph capture, and the device copies behind the MD-Lab structs.
+//
+// Replaces the reference's OpenCL glue (md_util_x.c:18-83 queue handling,
+// :359-551 context transfer and host sync; md_pimd_x.c:9-326;
+// md_statistics_x.c:72-201).  One CUDA stream orders all work, as the one
+// OpenCL queue does; host <-> device copies use page-locked host memory.
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <unordered_map>
+#include <unordered_set>
+#include <vector>
+
+#include "xmd_internal.h"
+
+namespace xmd {
+
+static thread_local std::string t_err;
+static std::mutex g_mu;
+
+int fail(int code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  t_err = buf;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char *what) {
+  return fail(MD_GB_ERR_CUDA, "%s: %s (%s)", what, cudaGetErrorName(e), cudaGetErrorString(e));
+}
+
+// ------------------------------------------------------------------
+// device and stream
+// ------------------------------------------------------------------
+static int g_dev_state = 0;  // 0 unknown, 1 present, -1 absent
+static cudaStream_t g_own = nullptr, g_user = nullptr;
+static bool g_user_set = false;
+
+bool device_present() {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (g_dev_state == 0) {
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    g_dev_state = (e == cudaSuccess && n > 0) ? 1 : -1;
+    if (g_dev_state < 0) cudaGetLastError();
+  }
+  return g_dev_state > 0;
+}
+
+int ensure_device() {
+  if (!device_present()) return fail(MD_GB_ERR_NO_DEVICE, "no CUDA device is available");
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!g_own) {
+    cudaError_t e = cudaStreamCreateWithFlags(&g_own, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamCreateWithFlags");
+  }
+  return 0;
+}
+
+cudaStream_t stream() { return g_user_set ? g_user : g_own; }
+
+bool capturing() {
+  cudaStreamCaptureStatus s = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(stream(), &s) != cudaSuccess) return false;
+  return s != cudaStreamCaptureStatusNone;
+}
+
+int reserve(DevBuf &b, size_t bytes) {
+  if (bytes <= b.bytes && b.p) return 0;
+  if (capturing()) return fail(MD_GB_ERR_CAPTURE, "device allocation requested while capturing a graph");
+  if (b.p) {
+    cudaFreeAsync(b.p, stream());
+    b.p = nullptr;
+    b.bytes = 0;
+  }
+  if (bytes == 0) bytes = 8;
+  cudaError_t e = cudaMallocAsync(&b.p, bytes, stream());
+  if (e != cudaSuccess) {
+    b.p = nullptr;
+    return fail(MD_GB_ERR_ALLOC, "cudaMallocAsync(%zu bytes): %s", bytes, cudaGetErrorString(e));
+  }
+  b.bytes = bytes;
+  return 0;
+}
+
+void release(DevBuf &b) {
+  if (b.p) cudaFreeAsync(b.p, stream());
+  b.p = nullptr;
+  b.bytes = 0;
+}
+
+static std::unordered_set<void *> g_pinned;
+
+void *host_alloc(size_t bytes) {
+  if (bytes == 0) bytes = 1;
+  void *p = nullptr;
+  if (device_present() && cudaMallocHost(&p, bytes) == cudaSuccess) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    g_pinned.insert(p);
+    memset(p, 0, bytes);
+    return p;
+  }
+  cudaGetLastError();
+  p = calloc(1, bytes);
+  return p;
+}
+
+void host_free(void *p) {
+  if (!p) return;
+  {
+    std::lock_guard<std::mutex> lk(g_mu);
+    auto it = g_pinned.find(p);
+    if (it != g_pinned.end()) {
+      g_pinned.erase(it);
+      cudaFreeHost(p);
+      return;
+    }
+  }
+  free(p);
+}
+
+// ------------------------------------------------------------------
+// side tables
+// ------------------------------------------------------------------
+struct Layout {
+  int N, P;
+};
+static std::unordered_map<const void *, Layout> g_layout;
+static std::unordered_map<const void *, SimDev *> g_sim;
+static std::unordered_map<const void *, PimdDev *> g_pimd;
+static std::unordered_map<const void *, StatsDev *> g_stats;
+
+template <class T>
+static T *lookup(std::unordered_map<const void *, T *> &m, const void *k, bool create) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  auto it = m.find(k);
+  if (it != m.end()) return it->second;
+  if (!create) return nullptr;
+  T *t = new T();
+  m[k] = t;
+  return t;
+}
+
+static void free_sim(SimDev *d) {
+  for (DevBuf *b : {&d->x, &d->v, &d->f, &d->m, &d->th, &d->vt, &d->Q, &d->cf, &d->c0, &d->c2,
+                    &d->stage, &d->scratch})
+    release(*b);
+}
+
+static void free_pimd(PimdDev *d) {
+  for (DevBuf *b : {&d->ENk, &d->ENk2, &d->Eint, &d->VBN, &d->tmpV, &d->G, &d->rc_coef,
+                    &d->rc_cols, &d->rc_phase, &d->rc_S})
+    release(*b);
+}
+
+void forget(const void *key) {
+  SimDev *s = nullptr;
+  PimdDev *p = nullptr;
+  StatsDev *t = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(g_mu);
+    g_layout.erase(key);
+    auto a = g_sim.find(key);
+    if (a != g_sim.end()) {
+      s = a->second;
+      g_sim.erase(a);
+    }
+    auto b = g_pimd.find(key);
+    if (b != g_pimd.end()) {
+      p = b->second;
+      g_pimd.erase(b);
+    }
+    auto c = g_stats.find(key);
+    if (c != g_stats.end()) {
+      t = c->second;
+      g_stats.erase(c);
+    }
+  }
+  if (s) {
+    free_sim(s);
+    delete s;
+  }
+  if (p) {
+    free_pimd(p);
+    delete p;
+  }
+  if (t) {
+    release(t->acc);
+    delete t;
+  }
+}
+
+void layout_hint(md_simulation_t_x *sim, int N, int P) {
+  SimDev *d = lookup(g_sim, sim, false);
+  if (d && d->valid && (d->geo.N != N || d->geo.P != P)) sim_to_host(sim, false);
+  std::lock_guard<std::mutex> lk(g_mu);
+  g_layout[sim] = {N, P};
+}
+
+static xk::Geo make_geo(md_simulation_t_x *sim) {
+  xk::Geo g{};
+  g.D = MD_DIMENSION_X;
+  Layout lay{sim->N, 1};
+  {
+    std::lock_guard<std::mutex> lk(g_mu);
+    auto it = g_layout.find(sim);
+    if (it != g_layout.end() && it->second.N * it->second.P == sim->N) lay = it->second;
+  }
+  g.N = lay.N;
+  g.P = lay.P;
+  g.Ns = xk::pad_n(lay.N);
+  for (int d = 0; d < 3; ++d) {
+    g.box[d] = 0;
+    g.inv_box[d] = 0;
+  }
+  if (sim->box && sim->box->type == MD_ND_RECT_BOX_X && sim->box->box) {
+    const nd_rect_t_x *r = (const nd_rect_t_x *)sim->box->box;
+    for (int d = 0; d < MD_DIMENSION_X; ++d) {
+      g.box[d] = r->L[d];
+      g.inv_box[d] = r->L[d] != 0 ? 1.0 / r->L[d] : 0.0;
+    }
+  }
+  return g;
+}
+
+// ------------------------------------------------------------------
+// simulation
+// ------------------------------------------------------------------
+int sim_device(md_simulation_t_x *sim, SimDev **out) {
+  if (!sim || !sim->particles || sim->N < 1) return fail(MD_GB_ERR_ARG, "invalid simulation");
+  XMD_TRY(ensure_device());
+  SimDev *d = lookup(g_sim, sim, true);
+  *out = d;
+  // the box may change between calls (md_init_nd_rect_box_x)
+  if (d->valid) {
+    xk::Geo g = make_geo(sim);
+    for (int q = 0; q < 3; ++q) {
+      d->geo.box[q] = g.box[q];
+      d->geo.inv_box[q] = g.inv_box[q];
+    }
+    return 0;
+  }
+  if (capturing()) return fail(MD_GB_ERR_CAPTURE, "simulation state is not on the device yet");
+  cudaStream_t st = stream();
+  d->geo = make_geo(sim);
+  const xk::Geo &g = d->geo;
+  const size_t S = g.slots();
+  const int D = MD_DIMENSION_X, L = MD_NHC_LENGTH_X;
+  XMD_TRY(reserve(d->x, S * 8));
+  XMD_TRY(reserve(d->v, S * 8));
+  XMD_TRY(reserve(d->f, S * 8));
+  XMD_TRY(reserve(d->m, (size_t)g.P * g.Ns * 8));
+  // padding lanes stay zero so that slice-wide kernels read defined values
+  XMD_CUDA(cudaMemsetAsync(d->x.p, 0, S * 8, st));
+  XMD_CUDA(cudaMemsetAsync(d->v.p, 0, S * 8, st));
+  XMD_CUDA(cudaMemsetAsync(d->f.p, 0, S * 8, st));
+  XMD_CUDA(cudaMemsetAsync(d->m.p, 0, (size_t)g.P * g.Ns * 8, st));
+  // chains: one DOF each in the reference's order -> slot order
+  d->nf = sim->Nf;
+  d->L = L;
+  bool fast = sim->nhcs != nullptr && sim->Nf == D * sim->N;
+  for (int i = 0; fast && i < sim->Nf; ++i) fast = sim->nhcs[i].f == 1;
+  d->fast_chains = fast;
+  const size_t pbytes = sizeof(md_particle_t_x) * (size_t)sim->N;
+  const size_t cbytes = sizeof(md_nhc_t_x) * (size_t)(sim->nhcs ? sim->Nf : 0);
+  XMD_TRY(reserve(d->stage, pbytes > cbytes ? pbytes : cbytes));
+  d->uniform_mass = true;
+  d->mass0 = sim->particles[0].m;
+  for (int b = 1; b < sim->N; ++b)
+    if (sim->particles[b].m != d->mass0) {
+      d->uniform_mass = false;
+      break;
+    }
+  XMD_CUDA(cudaMemcpyAsync(d->stage.p, sim->particles, pbytes, cudaMemcpyHostToDevice, st));
+  XMD_CUDA(xk::aos_to_soa(g, d->stage.as<double>(), d->x.as<double>(), d->v.as<double>(),
+                          d->f.as<double>(), d->m.as<double>(), st));
+  if (sim->nhcs && sim->Nf > 0) {
+    const size_t cs = fast ? S : (size_t)sim->Nf;
+    XMD_TRY(reserve(d->th, cs * L * 8));
+    XMD_TRY(reserve(d->vt, cs * L * 8));
+    XMD_TRY(reserve(d->Q, cs * L * 8));
+    if (fast) {
+      // padding slots: Q = 1 so that no kernel ever divides by zero there
+      XMD_CUDA(cudaMemsetAsync(d->th.p, 0, cs * L * 8, st));
+      XMD_CUDA(cudaMemsetAsync(d->vt.p, 0, cs * L * 8, st));
+      XMD_CUDA(cudaMemsetAsync(d->Q.p, 0, cs * L * 8, st));
+    } else {
+      // grouped chains: first DOF and DOF count as the reference's loop
+      // (md_simulation_x.c:664-668) computes them
+      std::vector<int> cf(sim->Nf), c0(sim->Nf), c2(sim->Nf);
+      int f0 = 0;
+      for (int i = 0; i < sim->Nf; ++i) {
+        cf[i] = sim->nhcs[i].f;
+        c0[i] = f0;
+        c2[i] = (i == sim->Nf - 1) ? D * sim->N - f0 : cf[i];
+        if (f0 < 0 || c2[i] < 0 || f0 + c2[i] > D * sim->N)
+          return fail(MD_GB_ERR_ARG, "chain %d covers DOFs outside the simulation", i);
+        f0 += cf[i];
+      }
+      XMD_TRY(reserve(d->cf, sizeof(int) * sim->Nf));
+      XMD_TRY(reserve(d->c0, sizeof(int) * sim->Nf));
+      XMD_TRY(reserve(d->c2, sizeof(int) * sim->Nf));
+      XMD_CUDA(cudaMemcpyAsync(d->cf.p, cf.data(), sizeof(int) * sim->Nf, cudaMemcpyHostToDevice, st));
+      XMD_CUDA(cudaMemcpyAsync(d->c0.p, c0.data(), sizeof(int) * sim->Nf, cudaMemcpyHostToDevice, st));
+      XMD_CUDA(cudaMemcpyAsync(d->c2.p, c2.data(), sizeof(int) * sim->Nf, cudaMemcpyHostToDevice, st));
+      XMD_CUDA(cudaStreamSynchronize(st));  // the vectors above go out of scope
+    }
+    XMD_CUDA(cudaMemcpyAsync(d->stage.p, sim->nhcs, cbytes, cudaMemcpyHostToDevice, st));
+    XMD_CUDA(xk::chains_to_dev(g, L, sim->Nf, fast, d->stage.as<unsigned char>(), sizeof(md_nhc_t_x),
+                               d->th.as<double>(), d->vt.as<double>(), d->Q.as<double>(), st));
+  }
+  d->valid = true;
+  return 0;
+}
+
+int sim_to_host(md_simulation_t_x *sim, bool keep) {
+  if (!sim) return fail(MD_GB_ERR_ARG, "NULL simulation");
+  SimDev *d = lookup(g_sim, sim, false);
+  if (!d || !d->valid) return 0;
+  if (capturing()) return fail(MD_GB_ERR_CAPTURE, "host synchronisation while capturing a graph");
+  cudaStream_t st = stream();
+  const xk::Geo &g = d->geo;
+  const size_t pbytes = sizeof(md_particle_t_x) * (size_t)sim->N;
+  XMD_CUDA(xk::soa_to_aos(g, d->stage.as<double>(), d->x.as<double>(), d->v.as<double>(),
+                          d->f.as<double>(), d->m.as<double>(), st));
+  XMD_CUDA(cudaMemcpyAsync(sim->particles, d->stage.p, pbytes, cudaMemcpyDeviceToHost, st));
+  if (sim->nhcs && sim->Nf > 0) {
+    // the particle copy must leave the stage before the chains reuse it
+    XMD_CUDA(cudaStreamSynchronize(st));
+    const size_t cbytes = sizeof(md_nhc_t_x) * (size_t)sim->Nf;
+    XMD_CUDA(xk::chains_to_host(g, d->L, sim->Nf, d->fast_chains, d->stage.as<unsigned char>(),
+                                sizeof(md_nhc_t_x), d->th.as<double>(), d->vt.as<double>(),
+                                d->Q.as<double>(), st));
+    // f of each chain is not changed on the device: copy everything but f
+    XMD_CUDA(cudaStreamSynchronize(st));
+    std::vector<unsigned char> tmp(cbytes);
+    XMD_CUDA(cudaMemcpy(tmp.data(), d->stage.p, cbytes, cudaMemcpyDeviceToHost));
+    for (int i = 0; i < sim->Nf; ++i) {
+      const md_nhc_t_x *src = (const md_nhc_t_x *)(tmp.data() + (size_t)i * sizeof(md_nhc_t_x));
+      memcpy(sim->nhcs[i].theta, src->theta, sizeof(src->theta));
+      memcpy(sim->nhcs[i].vtheta, src->vtheta, sizeof(src->vtheta));
+      memcpy(sim->nhcs[i].Q, src->Q, sizeof(src->Q));
+    }
+  }
+  XMD_CUDA(cudaStreamSynchronize(st));
+  if (!keep) d->valid = false;
+  return 0;
+}
+
+int scratch(SimDev *sd, size_t doubles, double **out) {
+  XMD_TRY(reserve(sd->scratch, doubles * 8));
+  *out = sd->scratch.as<double>();
+  return 0;
+}
+
+// ------------------------------------------------------------------
+// path-integral state
+// ------------------------------------------------------------------
+int pimd_device(md_pimd_t_x *pimd, SimDev **sd, PimdDev **pd) {
+  if (!pimd || !pimd->sim) return fail(MD_GB_ERR_ARG, "invalid path-integral state");
+  if (pimd->N < 1 || pimd->P < 1 || pimd->N * pimd->P != pimd->sim->N)
+    return fail(MD_GB_ERR_ARG, "N*P (%d*%d) does not match the simulation's %d beads", pimd->N,
+                pimd->P, pimd->sim->N);
+  layout_hint(pimd->sim, pimd->N, pimd->P);
+  XMD_TRY(sim_device(pimd->sim, sd));
+  PimdDev *d = lookup(g_pimd, pimd, true);
+  *pd = d;
+  if (d->valid) return 0;
+  if (capturing()) return fail(MD_GB_ERR_CAPTURE, "exchange state is not on the device yet");
+  const int N = pimd->N;
+  const size_t nt = xk::ntri(N);
+  XMD_TRY(reserve(d->ENk, nt * 8));
+  XMD_TRY(reserve(d->ENk2, nt * 8));
+  XMD_TRY(reserve(d->Eint, (size_t)N * 8));
+  XMD_TRY(reserve(d->VBN, (size_t)(N + 1) * 8));
+  XMD_TRY(reserve(d->tmpV, (size_t)(N + 1) * 8));
+  XMD_TRY(reserve(d->G, (size_t)N * N * 8));
+  cudaStream_t st = stream();
+  XMD_CUDA(cudaMemcpyAsync(d->ENk.p, pimd->ENk[0], nt * 8, cudaMemcpyHostToDevice, st));
+  XMD_CUDA(cudaMemcpyAsync(d->ENk2.p, pimd->ENk2[0], nt * 8, cudaMemcpyHostToDevice, st));
+  XMD_CUDA(cudaMemcpyAsync(d->Eint.p, pimd->Eint, (size_t)N * 8, cudaMemcpyHostToDevice, st));
+  XMD_CUDA(cudaMemcpyAsync(d->VBN.p, pimd->VBN, (size_t)(N + 1) * 8, cudaMemcpyHostToDevice, st));
+  d->valid = true;
+  return 0;
+}
+
+int pimd_to_host(md_pimd_t_x *pimd, bool keep) {
+  if (!pimd) return fail(MD_GB_ERR_ARG, "NULL path-integral state");
+  PimdDev *d = lookup(g_pimd, pimd, false);
+  if (!d || !d->valid) return 0;
+  if (capturing()) return fail(MD_GB_ERR_CAPTURE, "host synchronisation while capturing a graph");
+  cudaStream_t st = stream();
+  const int N = pimd->N;
+  const size_t nt = xk::ntri(N);
+  XMD_CUDA(cudaMemcpyAsync(pimd->ENk[0], d->ENk.p, nt * 8, cudaMemcpyDeviceToHost, st));
+  XMD_CUDA(cudaMemcpyAsync(pimd->ENk2[0], d->ENk2.p, nt * 8, cudaMemcpyDeviceToHost, st));
+  XMD_CUDA(cudaMemcpyAsync(pimd->Eint, d->Eint.p, (size_t)N * 8, cudaMemcpyDeviceToHost, st));
+  XMD_CUDA(cudaMemcpyAsync(pimd->VBN, d->VBN.p, (size_t)(N + 1) * 8, cudaMemcpyDeviceToHost, st));
+  XMD_CUDA(cudaStreamSynchronize(st));
+  if (!keep) d->valid = false;
+  return 0;
+}
+
+// ------------------------------------------------------------------
+// accumulators
+// ------------------------------------------------------------------
+int stats_device(md_stats_t_x *s, double **acc) {
+  if (!s || !s->es || s->N < 1) return fail(MD_GB_ERR_ARG, "invalid statistics accumulator");
+  XMD_TRY(ensure_device());
+  StatsDev *d = lookup(g_stats, s, true);
+  if (!d->valid) {
+    if (capturing()) return fail(MD_GB_ERR_CAPTURE, "accumulator is not on the device yet");
+    XMD_TRY(reserve(d->acc, 8));
+    XMD_CUDA(cudaMemcpyAsync(d->acc.p, &s->es[s->N - 1], 8, cudaMemcpyHostToDevice, stream()));
+    XMD_CUDA(cudaStreamSynchronize(stream()));
+    d->valid = true;
+  }
+  *acc = d->acc.as<double>();
+  return 0;
+}
+
+int stats_to_host(md_stats_t_x *s) {
+  if (!s) return fail(MD_GB_ERR_ARG, "NULL accumulator");
+  StatsDev *d = lookup(g_stats, s, false);
+  if (!d || !d->valid) return 0;
+  if (capturing()) return fail(MD_GB_ERR_CAPTURE, "host synchronisation while capturing a graph");
+  XMD_CUDA(cudaMemcpyAsync(&s->es[s->N - 1], d->acc.p, 8, cudaMemcpyDeviceToHost, stream()));
+  XMD_CUDA(cudaStreamSynchronize(stream()));
+  d->valid = false;
+  return 0;
+}
+
+}  // namespace xmd
+
+// ------------------------------------------------------------------
+// public additions (md_gb300_x.h)
+// ------------------------------------------------------------------
+using namespace xmd;
+
+struct md_gb300_graph {
+  cudaGraph_t g = nullptr;
+  cudaGraphExec_t e = nullptr;
+};
+
+extern "C" {
+
+const char *md_gb300_last_error_x(void) { return t_err.c_str(); }
+
+void md_gb300_variant_x(int *dimension, int *nhc_length) {
+  if (dimension) *dimension = MD_DIMENSION_X;
+  if (nhc_length) *nhc_length = MD_NHC_LENGTH_X;
+}
+
+int md_gb300_device_count_x(void) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n;
+}
+
+unsigned long long md_gb300_launch_count_x(void) { return xk::launch_count(); }
+
+int md_gb300_set_device_x(int dev) {
+  if (!device_present()) return fail(MD_GB_ERR_NO_DEVICE, "no CUDA device is available");
+  if (g_own) return fail(MD_GB_ERR_ARG, "the device must be chosen before the first device call");
+  XMD_CUDA(cudaSetDevice(dev));
+  return 0;
+}
+
+int md_gb300_set_stream_x(void *s) {
+  XMD_TRY(ensure_device());
+  g_user = (cudaStream_t)s;
+  g_user_set = s != nullptr;
+  return 0;
+}
+
+void *md_gb300_get_stream_x(void) {
+  if (ensure_device() != 0) return nullptr;
+  return (void *)stream();
+}
+
+int md_gb300_synchronize_x(void) {
+  XMD_TRY(ensure_device());
+  XMD_CUDA(cudaStreamSynchronize(stream()));
+  return 0;
+}
+
+int md_gb300_capture_begin_x(void) {
+  XMD_TRY(ensure_device());
+  if (capturing()) return fail(MD_GB_ERR_CAPTURE, "already capturing");
+  XMD_CUDA(cudaStreamBeginCapture(stream(), cudaStreamCaptureModeThreadLocal));
+  return 0;
+}
+
+int md_gb300_capture_end_x(md_gb300_graph_t_x **out) {
+  if (!out) return fail(MD_GB_ERR_ARG, "NULL graph pointer");
+  XMD_TRY(ensure_device());
+  md_gb300_graph *gr = new md_gb300_graph();
+  cudaError_t e = cudaStreamEndCapture(stream(), &gr->g);
+  if (e != cudaSuccess) {
+    delete gr;
+    return cuda_fail(e, "cudaStreamEndCapture");
+  }
+  e = cudaGraphInstantiate(&gr->e, gr->g, 0);
+  if (e != cudaSuccess) {
+    cudaGraphDestroy(gr->g);
+    delete gr;
+    return cuda_fail(e, "cudaGraphInstantiate");
+  }
+  *out = gr;
+  return 0;
+}
+
+int md_gb300_graph_launch_x(md_gb300_graph_t_x *gr, int count) {
+  if (!gr || count < 0) return fail(MD_GB_ERR_ARG, "invalid graph launch");
+  for (int i = 0; i < count; ++i) XMD_CUDA(cudaGraphLaunch(gr->e, stream()));
+  return 0;
+}
+
+int md_gb300_graph_kernel_count_x(md_gb300_graph_t_x *gr) {
+  if (!gr) return fail(MD_GB_ERR_ARG, "NULL graph");
+  size_t n = 0;
+  XMD_CUDA(cudaGraphGetNodes(gr->g, nullptr, &n));
+  std::vector<cudaGraphNode_t> nodes(n);
+  XMD_CUDA(cudaGraphGetNodes(gr->g, nodes.data(), &n));
+  int k = 0;
+  for (size_t i = 0; i < n; ++i) {
+    cudaGraphNodeType t;
+    if (cudaGraphNodeGetType(nodes[i], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++k;
+  }
+  return k;
+}
+
+void md_gb300_graph_free_x(md_gb300_graph_t_x *gr) {
+  if (!gr) return;
+  if (gr->e) cudaGraphExecDestroy(gr->e);
+  if (gr->g) cudaGraphDestroy(gr->g);
+  delete gr;
+}
+
+int md_gb300_profile_x(int on) {
+  XMD_TRY(ensure_device());
+  xk::profile_enable(on != 0);
+  return 0;
+}
+
+int md_gb300_profile_report_x(char *buf, int len) {
+  if (!buf || len < 1) return fail(MD_GB_ERR_ARG, "invalid report buffer");
+  const std::string r = xk::profile_report();
+  snprintf(buf, (size_t)len, "%s", r.c_str());
+  return (int)r.size();
+}
+
+double md_gb300_fp64_peak_x(void) {
+  if (ensure_device() != 0) return -1;
+  return xk::fp64_peak_tflops(stream());
+}
+
+int md_gb300_release_simulation_x(md_simulation_t_x *sim) {
+  if (!sim) return fail(MD_GB_ERR_ARG, "NULL simulation");
+  XMD_TRY(sim_to_host(sim, false));
+  forget(sim);
+  return 0;
+}
+
+}  // extern "C"

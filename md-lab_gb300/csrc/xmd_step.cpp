@@ -1,0 +1,598 @@
+// xmd_step.cpp -- device entry points of the MD-Lab C ABI in libxmd_x: the
+// integrator, the exchange recursion, bead forces and estimators.
+//
+// Each function validates its arguments, makes sure the state is on the
+// device (xmd_runtime.cpp) and enqueues the kernels of xmd_kernels.cu on
+// the library stream.  Reference counterparts are cited per function
+// (MD-Lab file:line); the OpenCL branch of each is what these replace.
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+
+#include "xmd_internal.h"
+
+using namespace xmd;
+
+static const int D = MD_DIMENSION_X;
+
+// Ewald real-space images are summed while alpha*R < EWALD_XCUT.  Beyond it
+// both terms of the pair force, erfc(aR)/R^3 and 2a exp(-a^2R^2)/(sqrt(pi)R^2),
+// are below 2e-14 of their value at contact, far under the 1e-10 parity bar;
+// the reference sums the same images over its whole cube.
+static const double EWALD_XCUT = 5.8;
+
+namespace xmd {
+
+xk::TrapPrm trap_params(int kind) {
+  xk::TrapPrm p{};
+  p.kind = kind;
+  p.w = md_trap_frequency_x;
+  for (int d = 0; d < 3; ++d) {
+    p.w2[d] = d < D ? md_trap_frequency_2_x[d] : 0;
+    p.c[d] = d < D ? md_trap_center_x[d] : 0;
+  }
+  return p;
+}
+
+int trap_kind_of(const void *fn, bool energy) {
+  if (!energy) {
+    if (fn == (const void *)&md_harmonic_trap_force_x) return xk::TRAP_HARMONIC;
+    if (fn == (const void *)&md_harmonic_trap_force_2_x) return xk::TRAP_HARMONIC_2;
+    if (fn == (const void *)&md_neg_harmonic_trap_force_x) return xk::TRAP_NEG_HARMONIC;
+  } else {
+    if (fn == (const void *)&md_harmonic_trap_energy_x) return xk::TRAP_HARMONIC;
+    if (fn == (const void *)&md_harmonic_trap_energy_2_x) return xk::TRAP_HARMONIC_2;
+    if (fn == (const void *)&md_neg_harmonic_trap_energy_x) return xk::TRAP_NEG_HARMONIC;
+  }
+  return 0;
+}
+
+int pair_kind_of(const void *fn, bool energy) {
+  if (!energy) {
+    if (fn == (const void *)&md_gaussian_force_x) return xk::PAIR_GAUSSIAN;
+    if (fn == (const void *)&md_periodic_gaussian_force_x) return xk::PAIR_PERIODIC_GAUSSIAN;
+    if (fn == (const void *)&md_coulomb_force_x) return xk::PAIR_COULOMB;
+    if (fn == (const void *)&md_coulomb_periodic_force_x) return xk::PAIR_PERIODIC_COULOMB;
+    if (fn == (const void *)&md_coulomb_3d_ewald_force_x) return xk::PAIR_EWALD_REAL;
+  } else {
+    if (fn == (const void *)&md_gaussian_energy_x) return xk::PAIR_GAUSSIAN;
+    if (fn == (const void *)&md_periodic_gaussian_energy_x) return xk::PAIR_PERIODIC_GAUSSIAN;
+    if (fn == (const void *)&md_coulomb_energy_x) return xk::PAIR_COULOMB;
+    if (fn == (const void *)&md_coulomb_periodic_energy_x) return xk::PAIR_PERIODIC_COULOMB;
+    if (fn == (const void *)&md_coulomb_3d_ewald_energy_x) return xk::PAIR_EWALD_REAL;
+  }
+  return 0;
+}
+
+}  // namespace xmd
+
+static xk::Chains chains_of(SimDev *sd) {
+  xk::Chains c{};
+  c.fast = sd->fast_chains;
+  c.L = sd->L;
+  c.nf = sd->nf;
+  c.th = sd->th.as<double>();
+  c.vt = sd->vt.as<double>();
+  c.Q = sd->Q.as<double>();
+  c.cf = sd->cf.as<int>();
+  c.c0 = sd->c0.as<int>();
+  c.c2 = sd->c2.as<int>();
+  return c;
+}
+
+// features of the reference's PIMC / worm code paths that this step does not
+// implement: refuse rather than compute something else
+static int check_plain(md_pimd_t_x *p) {
+  if (p->worm_index > 0 || p->cut_Pj != -1 || p->pbc)
+    return fail(MD_GB_ERR_UNSUPPORTED, "worm, cut-bead and winding bookkeeping are not supported");
+  return 0;
+}
+
+static int check_image(const SimDev *sd, int image) {
+  if (image && (sd->geo.box[0] <= 0 || (D > 1 && sd->geo.box[1] <= 0) || (D > 2 && sd->geo.box[2] <= 0)))
+    return fail(MD_GB_ERR_ARG, "minimum image requested without a positive box");
+  return 0;
+}
+
+static double *scratch_for(SimDev *sd, size_t doubles, int *rc) {
+  double *p = nullptr;
+  *rc = scratch(sd, doubles, &p);
+  return p;
+}
+
+static size_t general_scratch(const xk::Geo &g) {
+  size_t n = xk::pair_scratch_doubles(g);
+  const size_t e = xk::exch_scratch_doubles(g);
+  if (e > n) n = e;
+  if (n < 4096) n = 4096;
+  if (n < (size_t)g.P) n = g.P;
+  return n;
+}
+
+extern "C" {
+
+// ------------------------------------------------------------------
+// integrator: md_simulation_x.c:421-472, :615-792, :794-856
+// ------------------------------------------------------------------
+int md_reset_force_x(md_simulation_t_x *sim) {
+  SimDev *sd;
+  XMD_TRY(sim_device(sim, &sd));
+  XMD_CUDA(xk::zero(sd->f.as<double>(), sd->geo.slots(), stream()));
+  return 0;
+}
+
+static int nhc(md_simulation_t_x *sim, md_num_t_x h, int half) {
+  SimDev *sd;
+  XMD_TRY(sim_device(sim, &sd));
+  if (sd->nf < 1) return 0;
+  if (sd->L % 2 || sd->L > 8) return fail(MD_GB_ERR_UNSUPPORTED, "chain length %d (even, <= 8 supported)", sd->L);
+  XMD_CUDA(xk::nhc_vv3(sd->geo, half, chains_of(sd), sd->x.as<double>(), sd->v.as<double>(),
+                       sd->f.as<double>(), sd->m.as<double>(), MD_kB_X * sim->T, h, stream()));
+  return 0;
+}
+
+int md_update_nhc_VV3_1_x(md_simulation_t_x *sim, md_num_t_x h) { return nhc(sim, h, 1); }
+int md_update_nhc_VV3_2_x(md_simulation_t_x *sim, md_num_t_x h) { return nhc(sim, h, 2); }
+
+int md_periodic_boundary_x(md_simulation_t_x *sim) {
+  if (!sim || !sim->box || sim->box->type != MD_ND_RECT_BOX_X) return 0;
+  SimDev *sd;
+  XMD_TRY(sim_device(sim, &sd));
+  XMD_CUDA(xk::wrap_box(sd->geo, sd->x.as<double>(), stream()));
+  return 0;
+}
+
+// ------------------------------------------------------------------
+// path-integral state: md_pimd_x.c:330-567
+// ------------------------------------------------------------------
+md_pimd_t_x *md_alloc_pimd_x(md_simulation_t_x *sim, int N, int P, md_num_t_x vi, md_num_t_x T) {
+  if (!sim || N < 1 || P < 1) return NULL;
+  md_pimd_t_x *p = (md_pimd_t_x *)calloc(1, sizeof(md_pimd_t_x));
+  if (!p) return NULL;
+  p->sim = sim;
+  p->N = N;
+  p->P = P;
+  p->vi = vi;
+  sim->T = T;
+  p->beta = 1.0 / (MD_kB_X * T);
+  p->omegaP = sqrt((double)P) / (p->beta * MD_hBar_X);
+  const size_t nt = xk::ntri(N);
+  p->ENk_count = (int)nt;
+  p->VBN = (md_num_t_x *)calloc(N + 1, sizeof(md_num_t_x));
+  p->minE = (md_num_t_x *)calloc(N + 1, sizeof(md_num_t_x));
+  p->Eint = (md_num_t_x *)calloc(N, sizeof(md_num_t_x));
+  p->Evir = (md_num_t_x *)calloc(N + 1, sizeof(md_num_t_x));
+  md_num_t_x ***tabs[3] = {&p->ENk, &p->ENk2, &p->ENk3};
+  for (int t = 0; t < 3; ++t) {
+    *tabs[t] = (md_num_t_x **)malloc(sizeof(md_num_t_x *) * N);
+    if (!*tabs[t]) {
+      md_gb300_free_pimd_x(p);
+      return NULL;
+    }
+    (*tabs[t])[0] = (md_num_t_x *)calloc(nt, sizeof(md_num_t_x));
+    if (!(*tabs[t])[0]) {
+      md_gb300_free_pimd_x(p);
+      return NULL;
+    }
+    for (int l = 2; l <= N; ++l) (*tabs[t])[l - 1] = (*tabs[t])[0] + xk::tri(l);
+  }
+  p->pcount_in = (int)nt;
+  p->pcount_ex = N * (N - 1) / 2;
+  p->pair_in = (md_index_pair_t_x *)malloc(sizeof(md_index_pair_t_x) * nt);
+  p->pair_ex = (md_index_pair_t_x *)malloc(sizeof(md_index_pair_t_x) * (p->pcount_ex > 0 ? p->pcount_ex : 1));
+  p->Eindices = (int *)malloc(sizeof(int) * (size_t)N * N);
+  p->pbW = (int *)calloc((size_t)N * P * D, sizeof(int));
+  if (!p->VBN || !p->minE || !p->Eint || !p->Evir || !p->pair_in || !p->pair_ex || !p->Eindices || !p->pbW) {
+    md_gb300_free_pimd_x(p);
+    return NULL;
+  }
+  int a = 0, b = 0;
+  for (int i = 0; i < N; ++i)
+    for (int j = 0; j <= i; ++j) {
+      p->pair_in[a] = {i, j};
+      p->Eindices[i * N + j] = a++;
+      if (j < i) p->pair_ex[b++] = {i, j};
+    }
+  p->cut_Pj = -1;
+  p->mc_par = -1;
+  p->pbc = 0;
+  p->worm_index = -1;
+  p->old_worm_index = -1;
+  layout_hint(sim, N, P);
+  return p;
+}
+
+void md_gb300_free_pimd_x(md_pimd_t_x *p) {
+  if (!p) return;
+  forget(p);
+  md_num_t_x **tabs[3] = {p->ENk, p->ENk2, p->ENk3};
+  for (int t = 0; t < 3; ++t)
+    if (tabs[t]) {
+      free(tabs[t][0]);
+      free(tabs[t]);
+    }
+  free(p->VBN);
+  free(p->minE);
+  free(p->Eint);
+  free(p->Evir);
+  free(p->pair_in);
+  free(p->pair_ex);
+  free(p->Eindices);
+  free(p->pbW);
+  free(p);
+}
+
+md_pimd_t_x *md_pimd_sync_host_x(md_pimd_t_x *pimd, int read_only) {
+  return pimd_to_host(pimd, read_only != 0) == 0 ? pimd : NULL;
+}
+
+void md_pimd_change_temperature_x(md_pimd_t_x *p, md_num_t_x T) {
+  p->sim->T = T;
+  p->beta = 1.0 / (MD_kB_X * T);
+  p->omegaP = sqrt((double)p->P) / (p->beta * MD_hBar_X);
+}
+
+// neighbours on the cycle closing particles N2-k+1..N2: md_pimd_x.c:521-549
+int md_pimd_next_index_x(int l, int j, int N2, int k, int P) {
+  if (j != P) return MD_PIMD_INDEX_X(l, j + 1, P);
+  return MD_PIMD_INDEX_X(l == N2 ? N2 - k + 1 : l + 1, 1, P);
+}
+
+int md_pimd_prev_index_x(int l, int j, int N2, int k, int P) {
+  if (j != 1) return MD_PIMD_INDEX_X(l, j - 1, P);
+  return MD_PIMD_INDEX_X(l == N2 - k + 1 ? N2 : l - 1, P, P);
+}
+
+// md_pimd_x.c:551-567
+int md_pimd_init_particle_uniform_pos_x(md_pimd_t_x *p, md_num_t_x *center, md_num_t_x *L, md_num_t_x fluc) {
+  if (!md_simulation_sync_host_x(p->sim, 0)) return -1;
+  for (int l = 0; l < p->N; ++l) {
+    double c[MD_DIMENSION_X];
+    for (int d = 0; d < D; ++d) c[d] = md_random_uniform_x(center[d] - L[d] / 2, center[d] + L[d] / 2);
+    for (int j = 0; j < p->P; ++j)
+      for (int d = 0; d < D; ++d)
+        p->sim->particles[MD_PIMD_INDEX_X(l + 1, j + 1, p->P)].x[d] = c[d] + fluc * (md_random_uniform_x(0, 2) - 1);
+  }
+  return 0;
+}
+
+// ------------------------------------------------------------------
+// exchange: md_pimd_x.c:593-665, :814-953, :997-1109, :1969-2210, :2369-2721
+// ------------------------------------------------------------------
+int md_pimd_fast_fill_ENk_x(md_pimd_t_x *pimd, int image) {
+  SimDev *sd;
+  PimdDev *pd;
+  XMD_TRY(pimd_device(pimd, &sd, &pd));
+  XMD_TRY(check_plain(pimd));
+  XMD_TRY(check_image(sd, image));
+  XMD_CUDA(xk::fill_enk(sd->geo, sd->x.as<double>(), sd->m.as<double>(), pimd->omegaP * pimd->omegaP, image,
+                        pd->Eint.as<double>(), pd->ENk.as<double>(), stream()));
+  return 0;
+}
+
+int md_pimd_fill_ENk_x(md_pimd_t_x *pimd, int image) { return md_pimd_fast_fill_ENk_x(pimd, image); }
+
+int md_pimd_fill_VB_x(md_pimd_t_x *pimd) {
+  SimDev *sd;
+  PimdDev *pd;
+  XMD_TRY(pimd_device(pimd, &sd, &pd));
+  XMD_TRY(check_plain(pimd));
+  XMD_CUDA(xk::fill_vb(pimd->N, pimd->beta, pimd->vi, pd->ENk.as<double>(), pd->VBN.as<double>(), stream()));
+  return 0;
+}
+
+int md_pimd_fast_fill_force_VB_x(md_pimd_t_x *pimd, int image) {
+  SimDev *sd;
+  PimdDev *pd;
+  XMD_TRY(pimd_device(pimd, &sd, &pd));
+  XMD_TRY(check_plain(pimd));
+  XMD_TRY(check_image(sd, image));
+  if (pimd->P < 2) return fail(MD_GB_ERR_ARG, "the exchange spring force needs P >= 2 beads");
+  int rc;
+  double *scr = scratch_for(sd, general_scratch(sd->geo), &rc);
+  if (rc) return rc;
+  cudaStream_t st = stream();
+  const int N = pimd->N;
+  XMD_CUDA(xk::back_vb(N, pimd->beta, pimd->vi, pd->ENk.as<double>(), pd->tmpV.as<double>(), st));
+  XMD_CUDA(xk::fill_g(N, pimd->beta, pimd->vi, pd->ENk.as<double>(), pd->VBN.as<double>(), pd->tmpV.as<double>(),
+                      pd->G.as<double>(), st));
+  XMD_CUDA(xk::exch_force(sd->geo, sd->x.as<double>(), sd->m.as<double>(), pimd->omegaP * pimd->omegaP, image,
+                          pd->G.as<double>(), sd->f.as<double>(), scr, st));
+  return 0;
+}
+
+int md_pimd_fill_force_VB_x(md_pimd_t_x *pimd, int image) { return md_pimd_fast_fill_force_VB_x(pimd, image); }
+
+// ------------------------------------------------------------------
+// external forces: md_pimd_x.c:1297-1391, :1527-1677
+// ------------------------------------------------------------------
+int md_pimd_calc_trap_force_x(md_pimd_t_x *pimd, md_trap_force_t_x tf) {
+  const int kind = trap_kind_of((const void *)tf, false);
+  if (!kind) return fail(MD_GB_ERR_UNSUPPORTED, "trap force function has no device kernel");
+  SimDev *sd;
+  PimdDev *pd;
+  XMD_TRY(pimd_device(pimd, &sd, &pd));
+  XMD_CUDA(xk::trap_force(sd->geo, trap_params(kind), sd->x.as<double>(), sd->f.as<double>(), stream()));
+  return 0;
+}
+
+static int ewald_tables(md_pimd_t_x *pimd, SimDev *sd, PimdDev *pd) {
+  const int ns = md_coulomb_n_sum_x;
+  const double a = md_coulomb_truc_x, qs = md_coulomb_strength_x;
+  if (ns < 1 || ns > 12) return fail(MD_GB_ERR_UNSUPPORTED, "Ewald n_sum %d (1..12 supported)", ns);
+  if (!(a > 0)) return fail(MD_GB_ERR_ARG, "Ewald alpha must be positive");
+  const xk::Geo &g = sd->geo;
+  if (pd->rc_nsum == ns && pd->rc_alpha == a && pd->rc_qs == qs && pd->rc_box[0] == g.box[0] &&
+      pd->rc_box[1] == g.box[1] && pd->rc_box[2] == g.box[2] && pd->rc_phase.p)
+    return 0;
+  if (capturing()) return fail(MD_GB_ERR_CAPTURE, "Ewald tables change while capturing a graph");
+  const int nk = xk::recip_count(ns);
+  XMD_TRY(reserve(pd->rc_coef, sizeof(double) * nk));
+  XMD_TRY(reserve(pd->rc_cols, sizeof(int) * 4 * (ns * (2 * ns + 1) + ns + 1)));
+  XMD_TRY(reserve(pd->rc_phase, sizeof(double) * xk::recip_phase_doubles(g, ns)));
+  XMD_TRY(reserve(pd->rc_S, sizeof(double) * 2 * (size_t)nk * g.P));
+  xk::Recip r{};
+  r.coef = pd->rc_coef.as<double>();
+  r.kvec = pd->rc_cols.as<int>();
+  XMD_CUDA(xk::recip_setup(g, ns, a, qs, r, stream()));
+  pd->rc_nsum = ns;
+  pd->rc_alpha = a;
+  pd->rc_qs = qs;
+  pd->rc_nk = nk;
+  for (int d = 0; d < 3; ++d) pd->rc_box[d] = g.box[d];
+  (void)pimd;
+  return 0;
+}
+
+static xk::Recip recip_of(PimdDev *pd) {
+  xk::Recip r{};
+  r.nsum = pd->rc_nsum;
+  r.nk = pd->rc_nk;
+  r.coef = pd->rc_coef.as<double>();
+  r.kvec = pd->rc_cols.as<int>();
+  r.phase = pd->rc_phase.as<double>();
+  r.S = pd->rc_S.as<double>();
+  return r;
+}
+
+static xk::PairPrm pair_params(int kind) {
+  xk::PairPrm p{};
+  p.kind = kind;
+  p.g = md_gaussian_strength_x;
+  p.s = md_gaussian_range_x;
+  p.qs = md_coulomb_strength_x;
+  p.alpha = md_coulomb_truc_x;
+  p.nsum = md_coulomb_n_sum_x;
+  p.rcut = p.alpha > 0 ? EWALD_XCUT / p.alpha : 0;
+  return p;
+}
+
+int md_pimd_calc_pair_force_x(md_pimd_t_x *pimd, md_pair_force_t_x pf) {
+  const int kind = pair_kind_of((const void *)pf, false);
+  if (!kind) return fail(MD_GB_ERR_UNSUPPORTED, "pair force function has no device kernel");
+  SimDev *sd;
+  PimdDev *pd;
+  XMD_TRY(pimd_device(pimd, &sd, &pd));
+  if (kind == xk::PAIR_EWALD_REAL && D != 3) return 0;  // the reference's Ewald is 3D only
+  if (kind == xk::PAIR_PERIODIC_GAUSSIAN || kind == xk::PAIR_PERIODIC_COULOMB || kind == xk::PAIR_EWALD_REAL)
+    XMD_TRY(check_image(sd, 1));
+  int rc;
+  double *scr = scratch_for(sd, general_scratch(sd->geo), &rc);
+  if (rc) return rc;
+  cudaStream_t st = stream();
+  const xk::PairPrm prm = pair_params(kind);
+  if (kind == xk::PAIR_EWALD_REAL) {
+    if (!sd->uniform_mass) return fail(MD_GB_ERR_UNSUPPORTED, "structure-factor Ewald needs equal bead masses");
+    XMD_TRY(ewald_tables(pimd, sd, pd));
+    XMD_CUDA(xk::recip_force(sd->geo, recip_of(pd), sd->x.as<double>(), 1.0 / (sd->mass0 * pimd->P),
+                             sd->f.as<double>(), st));
+  }
+  XMD_CUDA(xk::pair_force(sd->geo, prm, sd->x.as<double>(), sd->m.as<double>(), sd->f.as<double>(), scr, st));
+  return 0;
+}
+
+// ------------------------------------------------------------------
+// estimators: md_pimd_x.c:1111-1295, :1393-1525, :1679-1824,
+// :3989-4056, :4072-4348, :4423-4556
+// ------------------------------------------------------------------
+int md_pimd_calc_VBN_energy_x(md_pimd_t_x *pimd, md_stats_t_x *stats) {
+  SimDev *sd;
+  PimdDev *pd;
+  double *acc;
+  XMD_TRY(pimd_device(pimd, &sd, &pd));
+  XMD_TRY(check_plain(pimd));
+  XMD_TRY(stats_device(stats, &acc));
+  const double add = D * pimd->N * pimd->P / (2 * pimd->beta);
+  XMD_CUDA(xk::vbn_energy(pimd->N, pimd->beta, pimd->vi, add, pd->ENk.as<double>(), pd->VBN.as<double>(), nullptr,
+                          acc, stream()));
+  return 0;
+}
+
+int md_pimd_fast_fill_ENk2_x(md_pimd_t_x *pimd, int image) {
+  SimDev *sd;
+  PimdDev *pd;
+  XMD_TRY(pimd_device(pimd, &sd, &pd));
+  XMD_TRY(check_plain(pimd));
+  XMD_TRY(check_image(sd, image));
+  XMD_CUDA(xk::fill_enk2(sd->geo, sd->x.as<double>(), sd->m.as<double>(), pimd->omegaP * pimd->omegaP, image,
+                         pd->ENk2.as<double>(), stream()));
+  return 0;
+}
+
+int md_pimd_fill_ENk2_x(md_pimd_t_x *pimd, int image) { return md_pimd_fast_fill_ENk2_x(pimd, image); }
+
+int md_pimd_calc_vi_virial_energy_x(md_pimd_t_x *pimd, md_stats_t_x *stats, int image) {
+  SimDev *sd;
+  PimdDev *pd;
+  double *acc;
+  XMD_TRY(pimd_device(pimd, &sd, &pd));
+  XMD_TRY(check_plain(pimd));
+  XMD_TRY(check_image(sd, image));
+  XMD_TRY(stats_device(stats, &acc));
+  int rc;
+  double *scr = scratch_for(sd, general_scratch(sd->geo), &rc);
+  if (rc) return rc;
+  cudaStream_t st = stream();
+  const double add = D * pimd->N / (2 * pimd->beta);
+  XMD_CUDA(xk::vbn_energy(pimd->N, pimd->beta, pimd->vi, add, pd->ENk.as<double>(), pd->VBN.as<double>(),
+                          pd->ENk2.as<double>(), acc, st));
+  XMD_CUDA(xk::force_virial(sd->geo, sd->x.as<double>(), sd->f.as<double>(), sd->m.as<double>(), image, acc, scr, st));
+  return 0;
+}
+
+int md_pimd_calc_trap_energy_x(md_pimd_t_x *pimd, md_trap_energy_t_x te, md_stats_t_x *stats) {
+  const int kind = trap_kind_of((const void *)te, true);
+  if (!kind) return fail(MD_GB_ERR_UNSUPPORTED, "trap energy function has no device kernel");
+  SimDev *sd;
+  PimdDev *pd;
+  double *acc;
+  XMD_TRY(pimd_device(pimd, &sd, &pd));
+  XMD_TRY(stats_device(stats, &acc));
+  int rc;
+  double *scr = scratch_for(sd, general_scratch(sd->geo), &rc);
+  if (rc) return rc;
+  XMD_CUDA(xk::trap_energy(sd->geo, trap_params(kind), sd->x.as<double>(), sd->m.as<double>(), acc, scr, stream()));
+  return 0;
+}
+
+int md_pimd_calc_pair_energy_x(md_pimd_t_x *pimd, md_pair_energy_t_x pe, md_stats_t_x *stats) {
+  const int kind = pair_kind_of((const void *)pe, true);
+  if (!kind) return fail(MD_GB_ERR_UNSUPPORTED, "pair energy function has no device kernel");
+  SimDev *sd;
+  PimdDev *pd;
+  double *acc;
+  XMD_TRY(pimd_device(pimd, &sd, &pd));
+  if (kind == xk::PAIR_EWALD_REAL && D != 3) return 0;
+  if (kind == xk::PAIR_PERIODIC_GAUSSIAN || kind == xk::PAIR_PERIODIC_COULOMB || kind == xk::PAIR_EWALD_REAL)
+    XMD_TRY(check_image(sd, 1));
+  XMD_TRY(stats_device(stats, &acc));
+  int rc;
+  double *scr = scratch_for(sd, general_scratch(sd->geo), &rc);
+  if (rc) return rc;
+  cudaStream_t st = stream();
+  if (kind == xk::PAIR_EWALD_REAL) {
+    XMD_TRY(ewald_tables(pimd, sd, pd));
+    XMD_CUDA(xk::recip_energy(sd->geo, recip_of(pd), sd->x.as<double>(), acc, scr, st));
+  }
+  XMD_CUDA(xk::pair_energy(sd->geo, pair_params(kind), sd->x.as<double>(), acc, scr, st));
+  return 0;
+}
+
+// ------------------------------------------------------------------
+// host-side helpers on synchronised data (md_pimd_x.c:569-591, :667-812,
+// :955-965, :2213-2342, :4058-4070, :4652-4706)
+// ------------------------------------------------------------------
+md_num_t_x md_pimd_ENk_x(md_pimd_t_x *pimd, int N2, int k, int image) {
+  md_simulation_t_x *sim = md_simulation_sync_host_x(pimd->sim, 1);
+  if (!sim) return NAN;
+  const double *L = sim->box && sim->box->box ? ((nd_rect_t_x *)sim->box->box)->L : nullptr;
+  double e = 0;
+  for (int l = N2 - k + 1; l <= N2; ++l)
+    for (int j = 1; j <= pimd->P; ++j) {
+      const md_particle_t_x *a = &sim->particles[MD_PIMD_INDEX_X(l, j, pimd->P)];
+      const md_particle_t_x *b = &sim->particles[md_pimd_next_index_x(l, j, N2, k, pimd->P)];
+      const double r = image ? md_minimum_image_distance_x((double *)a->x, (double *)b->x, (double *)L)
+                             : md_distance_x((double *)a->x, (double *)b->x);
+      e += 0.5 * a->m * pimd->omegaP * pimd->omegaP * r * r;
+    }
+  return e;
+}
+
+static int print_tri(FILE *out, const char *tag, md_pimd_t_x *pimd, md_num_t_x **tab) {
+  if (!md_pimd_sync_host_x(pimd, 1)) return -1;
+  fprintf(out, "%s %d\n", tag, pimd->N);
+  for (int l = 1; l <= pimd->N; ++l) {
+    for (int k = 1; k <= l; ++k) fprintf(out, "%f ", tab[l - 1][k - 1]);
+    fprintf(out, "\n");
+  }
+  return ferror(out);
+}
+
+int md_pimd_fprint_ENk_x(FILE *out, md_pimd_t_x *pimd) { return print_tri(out, "ENk", pimd, pimd->ENk); }
+int md_pimd_fprint_ENk2_x(FILE *out, md_pimd_t_x *pimd) { return print_tri(out, "ENk2", pimd, pimd->ENk2); }
+
+int md_pimd_fprint_VBN_x(FILE *out, md_pimd_t_x *pimd) {
+  if (!md_pimd_sync_host_x(pimd, 1)) return -1;
+  fprintf(out, "VBN %d\n", pimd->N);
+  for (int i = 0; i <= pimd->N; ++i) fprintf(out, "%f ", pimd->VBN[i]);
+  fprintf(out, "\n");
+  return ferror(out);
+}
+
+md_num_t_x md_pimd_xexp_x(md_num_t_x k, md_num_t_x E, md_num_t_x EE, md_num_t_x beta, md_num_t_x vi) {
+  return vi == 0.0 ? exp(-beta * E + EE) : exp((k - 1) * log(vi) - beta * E + EE);
+}
+
+md_num_t_x md_pimd_fast_xexp_x(md_num_t_x l, md_num_t_x k, md_num_t_x E, md_num_t_x EE, md_num_t_x beta,
+                               md_num_t_x vi) {
+  return vi == 0.0 ? exp(-beta * E + EE - log(l)) : exp((k - 1) * log(vi) - beta * E + EE - log(l));
+}
+
+// log-sum-exp shift over the cycles ending at particle N2 for a given
+// xi and V_B table (also used for the xi' reweighting)
+static double min_shift(md_pimd_t_x *p, int N2, const double *V, double vi) {
+  if (vi == 0.0) return p->beta * (p->ENk[N2 - 1][0] + V[N2 - 1]);
+  double m = 1e10;
+  for (int k = 1; k <= N2; ++k) {
+    const double t = -(k - 1) * log(vi) + p->beta * (p->ENk[N2 - 1][k - 1] + V[N2 - k]);
+    if (t < m) m = t;
+  }
+  return m;
+}
+
+md_num_t_x md_pimd_xminE_x(md_pimd_t_x *pimd, int N2) {
+  if (!md_pimd_sync_host_x(pimd, 1)) return NAN;
+  return min_shift(pimd, N2, pimd->VBN, pimd->vi);
+}
+
+md_num_t_x md_pimd_xminE2_x(md_pimd_t_x *pimd, int N2, md_num_t_x *VBN2, md_num_t_x vi2) {
+  if (!md_pimd_sync_host_x(pimd, 1)) return NAN;
+  return min_shift(pimd, N2, VBN2, vi2);
+}
+
+md_num_t_x md_pimd_fast_xminE_x(md_pimd_t_x *pimd, int u, md_num_t_x *V) {
+  if (!md_pimd_sync_host_x(pimd, 1)) return NAN;
+  if (pimd->vi == 0.0) return log(u) + pimd->beta * (pimd->ENk[u - 1][0] + V[u]);
+  double m = 1e10;
+  for (int l = u; l <= pimd->N; ++l) {
+    const int k = l - u + 1;
+    const double t = -(k - 1) * log(pimd->vi) + log(l) + pimd->beta * (pimd->ENk[l - 1][k - 1] + V[l]);
+    if (t < m) m = t;
+  }
+  return m;
+}
+
+// signed V_B for xi' (possibly negative) on the current ENk; multiplies both
+// accumulators' es[0] by sign * exp(-beta (V'_N - V_N))
+int md_pimd_calc_vi_sign_x(md_pimd_t_x *pimd, md_stats_t_x *e_s, md_stats_t_x *s_s, md_num_t_x vi2) {
+  if (!md_pimd_sync_host_x(pimd, 1) || !md_stats_sync_host_x(e_s) || !md_stats_sync_host_x(s_s)) return -1;
+  const int N = pimd->N;
+  double *V2 = (double *)malloc(sizeof(double) * (N + 1));
+  double *sg = (double *)malloc(sizeof(double) * (N + 1));
+  if (!V2 || !sg) {
+    free(V2);
+    free(sg);
+    return -1;
+  }
+  V2[0] = 0;
+  sg[0] = 1;
+  const double sv = vi2 < 0 ? -1 : 1, av = fabs(vi2);
+  for (int n = 1; n <= N; ++n) {
+    const double m = min_shift(pimd, n, V2, av);
+    double sum = 0;
+    for (int k = 1; k <= n; ++k) {
+      if (vi2 == 0 && k != 1) continue;
+      sum += sg[n - k] * pow(sv, k - 1) * md_pimd_xexp_x(k, pimd->ENk[n - 1][k - 1] + V2[n - k], m, pimd->beta, av);
+    }
+    sg[n] = sum >= 0 ? 1 : -1;
+    V2[n] = (m - log(fabs(sum)) + log(n)) / pimd->beta;
+  }
+  const double s = sg[N] * exp(-pimd->beta * V2[N] + pimd->beta * pimd->VBN[N]);
+  e_s->es[0] *= s;
+  s_s->es[0] *= s;
+  free(V2);
+  free(sg);
+  return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,126 @@
+"""Parity of the CUDA library with MD-Lab's _nocl build.
+
+Every fixture in tests/golden/ was produced by the reference library itself;
+this test drives libxmd_x through the same C entry points in the same order
+and compares every stage at 1e-10 relative (the FP64 parity bar), then
+follows the trajectory to the end of the recorded run.
+"""
+import numpy as np
+import pytest
+
+import fixtures
+import xmd_x
+from gpu_common import PARITY
+from helpers import assert_close, relerr
+
+pytestmark = pytest.mark.gpu
+
+
+def _setup(name):
+    fx = fixtures.load(name)
+    h = fixtures.header(fx)
+    lib = xmd_x.load(h["D"], h["L"])
+    s = xmd_x.PimdSystem(lib, h["N"], h["P"], h["vi"], h["T"], box=h["box"], f=h["f"], fc=h["fc"])
+    xmd_x.set_potentials(lib, trap_w=1.0, gauss_g=h["g"], gauss_s=h["s"], coul_s=1.0,
+                         alpha=h["alpha"], nsum=h["nsum"])
+    s.set_state(m=fx["m"], x=fx["init/x"], v=fx["init/v"], f=fx["init/f"], theta=fx["init/theta"],
+                vtheta=fx["init/vtheta"], Q=fx["init/Q"], cf=fx["init/cf"])
+    trap = None if h["ueg"] else lib.fn("md_harmonic_trap_force_x")
+    pair = lib.fn("md_coulomb_3d_ewald_force_x" if h["ueg"] else "md_gaussian_force_x")
+    return fx, h, lib, s, trap, pair
+
+
+@pytest.mark.parametrize("name", fixtures.PIMD_FIXTURES)
+def test_step_stages_match_reference(name):
+    fx, h, lib, s, trap, pair = _setup(name)
+    ck, img = lib.check, h["image"]
+    ck(lib.md_update_nhc_VV3_1_x(s.sim, h["dt"]), "VV3_1")
+    st = s.state()
+    for k in ("x", "v", "theta", "vtheta"):
+        assert_close(st[k], fx["s1/" + k], PARITY, f"VV3_1 {k}")
+    ck(lib.md_reset_force_x(s.sim))
+    ck(lib.md_pimd_fast_fill_ENk_x(s.pimd, img))
+    ex = s.exchange()
+    assert_close(ex["ENk"], fx["ENk"], PARITY, "ENk")
+    assert_close(ex["Eint"], fx["Eint"], PARITY, "Eint")
+    ck(lib.md_pimd_fill_VB_x(s.pimd))
+    assert_close(s.exchange()["VBN"], fx["VBN"], PARITY, "VBN")
+    ck(lib.md_pimd_fast_fill_force_VB_x(s.pimd, img))
+    assert_close(s.state()["f"], fx["f_exch/f"], PARITY, "exchange spring force")
+    if trap:
+        ck(lib.md_pimd_calc_trap_force_x(s.pimd, trap))
+        assert_close(s.state()["f"], fx["f_trap/f"], PARITY, "trap force")
+    ck(lib.md_pimd_calc_pair_force_x(s.pimd, pair))
+    assert_close(s.state()["f"], fx["f_pair/f"], PARITY, "pair force")
+    # estimators at these positions
+    ck(lib.md_pimd_calc_VBN_energy_x(s.pimd, s.stats))
+    assert_close([s.take_energy()], fx["s1/e_prim_exch"], PARITY, "primitive estimator")
+    ck(lib.md_pimd_fast_fill_ENk2_x(s.pimd, img))
+    assert_close(s.exchange()["ENk2"], fx["s1/ENk2"], PARITY, "ENk2")
+    ck(lib.md_pimd_calc_vi_virial_energy_x(s.pimd, s.stats, img))
+    assert_close([s.take_energy()], fx["s1/e_vir_exch"], PARITY, "virial estimator")
+    if trap:
+        ck(lib.md_pimd_calc_trap_energy_x(s.pimd, lib.fn("md_harmonic_trap_energy_x"), s.stats))
+        assert_close([s.take_energy()], fx["s1/e_trap"], PARITY, "trap energy")
+    pe = lib.fn("md_coulomb_3d_ewald_energy_x" if h["ueg"] else "md_gaussian_energy_x")
+    ck(lib.md_pimd_calc_pair_energy_x(s.pimd, pe, s.stats))
+    assert_close([s.take_energy()], fx["s1/e_pair"], PARITY, "pair energy")
+    es, ss = lib.md_alloc_stats_x(1), lib.md_alloc_stats_x(1)
+    es.contents.es[0] = 1.0
+    ss.contents.es[0] = 1.0
+    ck(lib.md_pimd_calc_vi_sign_x(s.pimd, es, ss, -1.0))
+    assert_close([es.contents.es[0]], fx["s1/sign_m1"], 1e-9, "xi=-1 reweighting")
+    ck(lib.md_update_nhc_VV3_2_x(s.sim, h["dt"]))
+    st = s.state()
+    for k in ("x", "v", "theta", "vtheta"):
+        assert_close(st[k], fx["s2/" + k], PARITY, f"VV3_2 {k}")
+    if h["pbc"]:
+        ck(lib.md_periodic_boundary_x(s.sim))
+        assert_close(s.state()["x"], fx["s3/x"], PARITY, "wrapped positions")
+    s.free()
+
+
+@pytest.mark.parametrize("name", [n for n in fixtures.PIMD_FIXTURES])
+def test_trajectory_tracks_reference(name):
+    """Whole steps, device-resident between samples, against the reference's
+    recorded estimators and final state.  The bar widens with the number of
+    steps because the dynamics amplify rounding differences."""
+    fx, h, lib, s, trap, pair = _setup(name)
+    if h["steps"] < 2:
+        pytest.skip("single-step fixture")
+    worst = 0.0
+    for st in range(1, h["steps"] + 1):
+        xmd_x.md_step(lib, s, h["dt"], image=h["image"], trap=trap, pair=pair, pbc=bool(h["pbc"]))
+        key = f"t{st}/e_prim_exch"
+        if key in fx:
+            lib.check(lib.md_pimd_calc_VBN_energy_x(s.pimd, s.stats))
+            e = s.take_energy()
+            worst = max(worst, relerr([e], fx[key]))
+    tol = 1e-10 if h["steps"] <= 50 else 1e-8
+    assert worst <= tol, f"{name}: estimator drift {worst:.2e}"
+    fin = s.state()
+    for k in ("x", "v", "theta", "vtheta"):
+        assert_close(fin[k], fx["final/" + k], tol, f"{name} final {k} after {h['steps']} steps")
+    s.free()
+
+
+@pytest.mark.parametrize("name", fixtures.CUBIC_FIXTURES)
+def test_cubic_entry_points(name):
+    """md_pimd_fill_ENk_x / md_pimd_fill_force_VB_x reproduce the reference's
+    cubic-scaling outputs."""
+    fx = fixtures.load(name)
+    h = fixtures.header(fx, "cubic")
+    lib = xmd_x.load(h["D"], h["L"])
+    s = xmd_x.PimdSystem(lib, h["N"], h["P"], h["vi"], 1.0 / h["beta"], box=h["box"])
+    nb = h["N"] * h["P"]
+    s.set_state(m=np.ones(nb), x=fx["init/x"], v=np.zeros(nb * h["D"]), f=np.zeros(nb * h["D"]))
+    ck = lib.check
+    ck(lib.md_pimd_fill_ENk_x(s.pimd, h["image"]))
+    assert_close(s.exchange()["ENk"], fx["ENk_cubic"], PARITY, "ENk")
+    ck(lib.md_pimd_fill_VB_x(s.pimd))
+    assert_close(s.exchange()["VBN"], fx["VBN_cubic"], PARITY, "VBN")
+    ck(lib.md_pimd_fill_force_VB_x(s.pimd, h["image"]))
+    assert_close(s.state()["f"], fx["f_cubic/f"], 1e-10, "cubic exchange force")
+    ck(lib.md_pimd_fill_ENk2_x(s.pimd, h["image"]))
+    assert_close(s.exchange()["ENk2"], fx["ENk2_cubic"], PARITY, "ENk2")
+    s.free()
