@@ -1,0 +1,88 @@
+"""Generates xmd_ewald_tables.h: piecewise polynomials for the real-space
+Ewald kernel, so that the GPU evaluates no FP64 erfc/exp per image.
+
+    h(x) = erfc(x) + 2 x exp(-x^2) / sqrt(pi)    force:  F = s h(alpha R) r / R^3
+    e(x) = erfc(x)                               energy: E = s e(alpha R) / R
+
+(h'(x) = -4 x^2 exp(-x^2)/sqrt(pi).)  On each interval [i w, (i+1) w] of
+[0, XMAX] a degree-DEG polynomial in t = 2 (x - centre)/w is the Chebyshev
+interpolant computed with 40-digit arithmetic (mpmath), stored in monomial
+form for Horner evaluation.  The script measures the absolute error of the
+double-precision Horner evaluation against mpmath and records it in the
+header.  Absolute accuracy is what the sums need: both functions are at most
+1 and each image's contribution scales with them.
+
+Run:  python gen_ewald_tables.py > xmd_ewald_tables.h   (needs mpmath)
+"""
+import mpmath as mp
+
+mp.mp.dps = 40
+XMAX, NINT, DEG = 6.0, 24, 12
+W = XMAX / NINT
+
+
+def h(x):
+    return mp.erfc(x) + 2 * x * mp.e ** (-x * x) / mp.sqrt(mp.pi)
+
+
+def e(x):
+    return mp.erfc(x)
+
+
+def interpolant(f, a, b, deg):
+    n = deg + 1
+    nodes = [mp.cos(mp.pi * (k + mp.mpf(1) / 2) / n) for k in range(n)]
+    vals = [f((a + b) / 2 + (b - a) / 2 * t) for t in nodes]
+    A = mp.matrix([[t ** j for j in range(n)] for t in nodes])
+    c = mp.lu_solve(A, mp.matrix(vals))
+    return [c[j] for j in range(n)]
+
+
+def horner(cd, t):
+    acc = cd[-1]
+    for c in reversed(cd[:-1]):
+        acc = acc * t + c
+    return acc
+
+
+def table(f):
+    rows, worst = [], 0.0
+    for i in range(NINT):
+        a, b = mp.mpf(i) * W, mp.mpf(i + 1) * W
+        cd = [float(c) for c in interpolant(f, a, b, DEG)]
+        for s in range(401):
+            t = -1 + 2 * mp.mpf(s) / 400
+            x = (a + b) / 2 + (b - a) / 2 * t
+            worst = max(worst, abs(horner(cd, float(t)) - f(x)))
+        rows.append(cd)
+    return rows, float(worst)
+
+
+def emit(name, rows):
+    """An initializer macro, usable for host arrays and __constant__ arrays."""
+    out = [f"#define {name}_INIT {{ \\"]
+    for r in rows:
+        out.append("    {" + ", ".join(repr(c) for c in r) + "}, \\")
+    out.append("  }")
+    return "\n".join(out)
+
+
+if __name__ == "__main__":
+    th, eh = table(h)
+    te, ee = table(e)
+    print(f"""// xmd_ewald_tables.h -- generated by gen_ewald_tables.py; do not edit.
+//
+// Piecewise polynomials on [0, {XMAX}] ({NINT} intervals of width {W}, degree
+// {DEG}, variable t = 2 (x - centre)/w in [-1, 1]) for
+//   EW_H:    erfc(x) + 2 x exp(-x^2)/sqrt(pi)   max |error| {eh:.2e}
+//   EW_ERFC: erfc(x)                            max |error| {ee:.2e}
+// (errors of the double-precision Horner evaluation against 40-digit values
+// at 401 points per interval).
+#pragma once
+#define EW_XMAX {XMAX}
+#define EW_NINT {NINT}
+#define EW_DEG {DEG}
+#define EW_INV_W {1 / W!r}
+""")
+    print(emit("EW_H", th))
+    print(emit("EW_ERFC", te))

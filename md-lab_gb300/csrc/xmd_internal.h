@@ -68,6 +68,7 @@ struct SimDev {
 struct PimdDev {
   bool valid = false;  // ENk / ENk2 / VBN / Eint on the device authoritative
   DevBuf ENk, ENk2, Eint, VBN, tmpV, G;
+  DevBuf rec;  // weights of the factorised recursions
   // Ewald reciprocal tables, rebuilt when the parameters change
   DevBuf rc_coef, rc_cols, rc_phase, rc_S;
   int rc_nsum = -1;

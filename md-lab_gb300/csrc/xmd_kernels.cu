@@ -19,6 +19,7 @@
 #include <string>
 #include <vector>
 
+#include "xmd_ewald_tables.h"
 #include "xmd_kernels.cuh"
 
 namespace xk {
@@ -661,14 +662,11 @@ static int rec_threads(int N) {
   return t;
 }
 
+// ---- exact forms (one block; the reference's loop order) ----------
 // forward V_B: md_pimd_x.c:814-953 (CPU :934-950) with md_pimd_xminE_x
-// (:796-806) and md_pimd_xexp_x (:681-686)
-__global__ void k_fill_vb(int N, double beta, double vi, const double *__restrict__ ENk,
-                          double *__restrict__ VBN) {
-  extern __shared__ double sh[];
-  double *V = sh;               // N+1
-  double *bmin = sh + N + 1;    // 33
-  double *bsum = bmin + 33;     // 33
+// (:796-806) and md_pimd_xexp_x (:681-686); V in shared memory.
+__device__ void vb_exact(int N, double beta, double vi, const double *__restrict__ ENk, double *V,
+                         double *bmin, double *bsum) {
   const double lnvi = vi != 0.0 ? log(vi) : 0.0;
   if (threadIdx.x == 0) V[0] = 0.0;
   __syncthreads();
@@ -694,40 +692,23 @@ __global__ void k_fill_vb(int N, double beta, double vi, const double *__restric
     if (threadIdx.x == 0) V[n] = (mloc - log(s) + log((double)n)) / beta;
     __syncthreads();
   }
-  for (int i = threadIdx.x; i <= N; i += blockDim.x) VBN[i] = V[i];
 }
 
-cudaError_t fill_vb(int N, double beta, double vi, const double *ENk, double *VBN,
-                    cudaStream_t st) {
-  const size_t smem = sizeof(double) * (N + 1 + 66);
-  {
-    XK_PROF("fill_vb");
-    k_fill_vb<<<1, rec_threads(N), smem, st>>>(N, beta, vi, ENk, VBN);
-  }
-  return XK_LAUNCHED();
-}
-
-// backward recursion tmpV: md_pimd_x.c:2648-2659 with md_pimd_fast_xminE_x
-// (:2321-2333) and md_pimd_fast_xexp_x (:2337-2342)
-__global__ void k_back_vb(int N, double beta, double vi, const double *__restrict__ ENk,
-                          double *__restrict__ tmpV) {
-  extern __shared__ double sh[];
-  double *V = sh;              // N+1
-  double *lg = sh + N + 1;     // N+1, lg[l] = log(l)
-  double *bmin = lg + N + 1;   // 33
-  double *bsum = bmin + 33;    // 33
+// backward tmpV: md_pimd_x.c:2648-2659 with md_pimd_fast_xminE_x (:2321-2333)
+// and md_pimd_fast_xexp_x (:2337-2342); V in shared memory.
+__device__ void tv_exact(int N, double beta, double vi, const double *__restrict__ ENk, double *V,
+                         double *bmin, double *bsum) {
   const double lnvi = vi != 0.0 ? log(vi) : 0.0;
-  for (int i = threadIdx.x + 1; i <= N; i += blockDim.x) lg[i] = log((double)i);
   if (threadIdx.x == 0) V[N] = 0.0;
   __syncthreads();
   for (int u = N; u >= 1; --u) {
     double mloc = 1e10;
     if (vi == 0.0) {
-      mloc = lg[u] + beta * (ENk[dtri(u)] + V[u]);
+      mloc = log((double)u) + beta * (ENk[dtri(u)] + V[u]);
     } else {
       for (int l = u + threadIdx.x; l <= N; l += blockDim.x) {
         const int k = l - u + 1;
-        const double t = -(k - 1) * lnvi + lg[l] + beta * (ENk[dtri(l) + k - 1] + V[l]);
+        const double t = -(k - 1) * lnvi + log((double)l) + beta * (ENk[dtri(l) + k - 1] + V[l]);
         if (t < mloc) mloc = t;
       }
       mloc = block_min(mloc, 1e10, bmin);
@@ -737,21 +718,207 @@ __global__ void k_back_vb(int N, double beta, double vi, const double *__restric
       const int k = l - u + 1;
       if (vi == 0.0 && k != 1) continue;
       const double E = ENk[dtri(l) + k - 1] + V[l];
-      s += (vi == 0.0) ? exp(-beta * E + mloc - lg[l]) : exp((k - 1) * lnvi - beta * E + mloc - lg[l]);
+      const double lg = log((double)l);
+      s += (vi == 0.0) ? exp(-beta * E + mloc - lg) : exp((k - 1) * lnvi - beta * E + mloc - lg);
     }
     s = block_sum(s, bsum);
     if (threadIdx.x == 0) V[u - 1] = (mloc - log(s)) / beta;
     __syncthreads();
   }
+}
+
+// ---- factorised forms -------------------------------------------------
+// With a prediction Vp of V (the previous call's values) every weight of the
+// recursion splits into a part known in advance and one factor per earlier
+// step:
+//   exp((k-1) ln xi - beta (E_n^(k) + V_{n-k}))
+//     = exp(-c_n) * A_{n,k} * B_{n-k},
+//   A_{n,k} = exp(c_n - t_{n,k}),  t_{n,k} = beta (E_n^(k) + Vp_{n-k}) - (k-1) ln xi,
+//   c_n = min_k t_{n,k},           B_j = exp(-beta (V_j - Vp_j)).
+// Then V_n = (c_n - ln S_n + ln n)/beta with S_n = sum_k A_{n,k} B_{n-k}, and
+// B_n = S_n K_n with K_n = exp(beta Vp_n - c_n - ln n).  All exponentials
+// (A, K) are computed in parallel over the whole GPU; the sequential part
+// is one dot product per n.  If a B or S leaves [1e-250, 1e250] (a poor or
+// absent prediction) the sequential kernel restarts with the exact form.
+// The backward recursion factorises the same way with l, u and ln l.
+
+constexpr double REC_LO = 1e-250, REC_HI = 1e250;
+
+// one warp per row n = 1..N: W[(n-1)*N + k-1], c[n], K[n]
+__global__ void k_vb_weights(int N, double beta, double vi, const double *__restrict__ ENk,
+                             const double *__restrict__ Vp, double *__restrict__ W,
+                             double *__restrict__ c, double *__restrict__ K) {
+  const int n = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) + 1;
+  const int lane = threadIdx.x & 31;
+  if (n > N) return;
+  const double lnvi = vi != 0.0 ? log(vi) : 0.0;
+  const int kmax = vi == 0.0 ? 1 : n;
+  const double *row = ENk + dtri(n);
+  double *w = W + (size_t)(n - 1) * N;
+  double mn = 1e300;
+  for (int k = lane + 1; k <= kmax; k += 32) {
+    const double t = beta * (row[k - 1] + Vp[n - k]) - (k - 1) * lnvi;
+    w[k - 1] = t;
+    mn = t < mn ? t : mn;
+  }
+  mn = warp_min(mn);
+  __syncwarp();
+  for (int k = lane + 1; k <= kmax; k += 32) w[k - 1] = exp(mn - w[k - 1]);
+  if (lane == 0) {
+    c[n] = mn;
+    K[n] = exp(beta * Vp[n] - mn - log((double)n));
+  }
+}
+
+__global__ void k_vb_seq(int N, double beta, double vi, const double *__restrict__ ENk,
+                         const double *__restrict__ W, const double *__restrict__ c,
+                         const double *__restrict__ K, double *__restrict__ VBN) {
+  extern __shared__ double sh[];
+  double *B = sh;             // N+1
+  double *S = B + N + 1;      // N+1
+  double *bmin = S + N + 1;   // 33
+  double *bsum = bmin + 33;   // 33
+  __shared__ int bad;
+  if (threadIdx.x == 0) {
+    B[0] = 1.0;
+    bad = 0;
+  }
+  __syncthreads();
+  const int one = vi == 0.0;
+  // prefetch of this thread's first weight of the next row
+  double wnext = (threadIdx.x < 1) ? W[threadIdx.x] : 0.0;
+  for (int n = 1; n <= N; ++n) {
+    const int kmax = one ? 1 : n;
+    const double *w = W + (size_t)(n - 1) * N;
+    double part = 0;
+    const int k0 = threadIdx.x + 1;
+    if (k0 <= kmax) part = wnext * B[n - k0];
+    for (int k = k0 + blockDim.x; k <= kmax; k += blockDim.x) part += w[k - 1] * B[n - k];
+    if (n < N) {
+      const int kn = one ? 1 : n + 1;
+      wnext = k0 <= kn ? W[(size_t)n * N + k0 - 1] : 0.0;
+    }
+    const double sn = block_sum(part, bsum);
+    if (threadIdx.x == 0) {
+      const double bn = sn * K[n];
+      S[n] = sn;
+      B[n] = bn;
+      if (!(sn > REC_LO && sn < REC_HI && bn > REC_LO && bn < REC_HI)) bad = 1;
+    }
+    __syncthreads();
+    if (bad) break;
+  }
+  if (!bad) {
+    for (int n = threadIdx.x + 1; n <= N; n += blockDim.x)
+      VBN[n] = (c[n] - log(S[n]) + log((double)n)) / beta;
+    if (threadIdx.x == 0) VBN[0] = 0.0;
+    return;
+  }
+  __syncthreads();
+  double *V = B;  // reuse: N+1
+  vb_exact(N, beta, vi, ENk, V, bmin, bsum);
+  for (int i = threadIdx.x; i <= N; i += blockDim.x) VBN[i] = V[i];
+}
+
+// one warp per row u = 1..N, l = u..N (k = l-u+1): W[(u-1)*N + l-1], c[u], K[u]
+__global__ void k_tv_weights(int N, double beta, double vi, const double *__restrict__ ENk,
+                             const double *__restrict__ Tp, double *__restrict__ W,
+                             double *__restrict__ c, double *__restrict__ K) {
+  const int u = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) + 1;
+  const int lane = threadIdx.x & 31;
+  if (u > N) return;
+  const double lnvi = vi != 0.0 ? log(vi) : 0.0;
+  const int lmax = vi == 0.0 ? u : N;
+  double *w = W + (size_t)(u - 1) * N;
+  double mn = 1e300;
+  for (int l = u + lane; l <= lmax; l += 32) {
+    const int k = l - u + 1;
+    const double t = beta * (ENk[dtri(l) + k - 1] + Tp[l]) - (k - 1) * lnvi + log((double)l);
+    w[l - 1] = t;
+    mn = t < mn ? t : mn;
+  }
+  mn = warp_min(mn);
+  __syncwarp();
+  for (int l = u + lane; l <= lmax; l += 32) w[l - 1] = exp(mn - w[l - 1]);
+  if (lane == 0) {
+    c[u] = mn;
+    K[u] = exp(beta * Tp[u - 1] - mn);
+  }
+}
+
+__global__ void k_tv_seq(int N, double beta, double vi, const double *__restrict__ ENk,
+                         const double *__restrict__ W, const double *__restrict__ c,
+                         const double *__restrict__ K, double *__restrict__ tmpV) {
+  extern __shared__ double sh[];
+  double *B = sh;             // N+1, B[l] for l = 0..N
+  double *S = B + N + 1;      // N+1
+  double *bmin = S + N + 1;   // 33
+  double *bsum = bmin + 33;   // 33
+  __shared__ int bad;
+  if (threadIdx.x == 0) {
+    B[N] = 1.0;
+    bad = 0;
+  }
+  __syncthreads();
+  const int one = vi == 0.0;
+  for (int u = N; u >= 1; --u) {
+    const int lmax = one ? u : N;
+    const double *w = W + (size_t)(u - 1) * N;
+    double part = 0;
+    for (int l = u + threadIdx.x; l <= lmax; l += blockDim.x) part += w[l - 1] * B[l];
+    const double su = block_sum(part, bsum);
+    if (threadIdx.x == 0) {
+      const double bu = su * K[u];
+      S[u] = su;
+      B[u - 1] = bu;
+      if (!(su > REC_LO && su < REC_HI && bu > REC_LO && bu < REC_HI)) bad = 1;
+    }
+    __syncthreads();
+    if (bad) break;
+  }
+  if (!bad) {
+    for (int u = threadIdx.x + 1; u <= N; u += blockDim.x) tmpV[u - 1] = (c[u] - log(S[u])) / beta;
+    if (threadIdx.x == 0) tmpV[N] = 0.0;
+    return;
+  }
+  __syncthreads();
+  double *V = B;
+  tv_exact(N, beta, vi, ENk, V, bmin, bsum);
   for (int i = threadIdx.x; i <= N; i += blockDim.x) tmpV[i] = V[i];
 }
 
-cudaError_t back_vb(int N, double beta, double vi, const double *ENk, double *tmpV,
+size_t rec_scratch_doubles(int N) { return (size_t)N * N + 2 * (size_t)(N + 1); }
+
+cudaError_t fill_vb(int N, double beta, double vi, const double *ENk, double *VBN, double *rs,
                     cudaStream_t st) {
+  double *W = rs, *c = rs + (size_t)N * N, *K = c + N + 1;
+  {
+    XK_PROF("vb_weights");
+    k_vb_weights<<<cdiv((size_t)N * 32, 256), 256, 0, st>>>(N, beta, vi, ENk, VBN, W, c, K);
+  }
+  cudaError_t e = XK_LAUNCHED();
+  if (e != cudaSuccess) return e;
   const size_t smem = sizeof(double) * (2 * (N + 1) + 66);
   {
-    XK_PROF("back_vb");
-    k_back_vb<<<1, rec_threads(N), smem, st>>>(N, beta, vi, ENk, tmpV);
+    XK_PROF("vb_seq");
+    k_vb_seq<<<1, rec_threads(N), smem, st>>>(N, beta, vi, ENk, W, c, K, VBN);
+  }
+  return XK_LAUNCHED();
+}
+
+cudaError_t back_vb(int N, double beta, double vi, const double *ENk, double *tmpV, double *rs,
+                    cudaStream_t st) {
+  double *W = rs, *c = rs + (size_t)N * N, *K = c + N + 1;
+  {
+    XK_PROF("tv_weights");
+    k_tv_weights<<<cdiv((size_t)N * 32, 256), 256, 0, st>>>(N, beta, vi, ENk, tmpV, W, c, K);
+  }
+  cudaError_t e = XK_LAUNCHED();
+  if (e != cudaSuccess) return e;
+  const size_t smem = sizeof(double) * (2 * (N + 1) + 66);
+  {
+    XK_PROF("tv_seq");
+    k_tv_seq<<<1, rec_threads(N), smem, st>>>(N, beta, vi, ENk, W, c, K, tmpV);
   }
   return XK_LAUNCHED();
 }
@@ -1035,11 +1202,12 @@ cudaError_t trap_energy(const Geo &g, const TrapPrm &p, const double *x, const d
 // finishing kernel sums the slots in a fixed order and adds (sum)/P.
 // ===================================================================
 
-constexpr double SQRT_PI = 1.7724538509055160273;
+__constant__ double c_ew_h[EW_NINT][EW_DEG + 1] = EW_H_INIT;
+__constant__ double c_ew_erfc[EW_NINT][EW_DEG + 1] = EW_ERFC_INIT;
 
-template <int D, int KIND>
+template <int D, int KIND, bool ENERGY_TAB>
 __device__ inline void pair_eval(const PairPrm &p, const Geo &g, const double *dx, double *F,
-                                 double &E, bool want_e) {
+                                 double &E, bool want_e, const double *tabs) {
   if (KIND == PAIR_GAUSSIAN || KIND == PAIR_PERIODIC_GAUSSIAN) {
     double t[D], r2 = 0;
 #pragma unroll
@@ -1067,48 +1235,76 @@ __device__ inline void pair_eval(const PairPrm &p, const Geo &g, const double *d
     for (int d = 0; d < D; ++d) F[d] = mult * t[d];
     if (want_e) E = p.qs / r;
   } else if (KIND == PAIR_EWALD_REAL) {
-    // real-space images inside the reference's cube |n_i| <= nsum whose
-    // distance is below rcut (erfc(alpha rcut) < 1e-15)
-    int lo[3], hi[3];
+    // Real-space images of the partner inside the reference's cube
+    // |n_i| <= nsum (md_simulation_x.c:281-292) whose distance is below
+    // rcut.  dx is first reduced to its minimum image m = dx - s L, so the
+    // candidates are n = s + k with |k| <= kmax.  Per image the force factor
+    // s (erfc(x) + 2x exp(-x^2)/sqrt(pi)) / R^3 with x = alpha R comes from
+    // the piecewise polynomial EW_H (no FP64 erfc or exp), 1/R from rsqrt.
+    const double *tab = ENERGY_TAB ? tabs + EW_NINT * (EW_DEG + 1) : tabs;
+    double mm[3];
+    int sh[3];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-      lo[d] = (int)ceil((dx[d] - p.rcut) * g.inv_box[d]);
-      hi[d] = (int)floor((dx[d] + p.rcut) * g.inv_box[d]);
-      lo[d] = lo[d] < -p.nsum ? -p.nsum : lo[d];
-      hi[d] = hi[d] > p.nsum ? p.nsum : hi[d];
+      sh[d] = (int)rint(dx[d] * g.inv_box[d]);
+      mm[d] = fma(-(double)sh[d], g.box[d], dx[d]);
     }
-    const double rc2 = p.rcut * p.rcut, a = p.alpha, a2 = a * a;
+    const double rc2 = p.rcut * p.rcut;
     double F0 = 0, F1 = 0, F2 = 0, e = 0;
-    for (int n0 = lo[0]; n0 <= hi[0]; ++n0) {
-      const double t0 = dx[0] - n0 * g.box[0];
-      for (int n1 = lo[1]; n1 <= hi[1]; ++n1) {
-        const double t1 = dx[1] - n1 * g.box[1];
-        for (int n2 = lo[2]; n2 <= hi[2]; ++n2) {
-          const double t2 = dx[2] - n2 * g.box[2];
-          const double R2 = t0 * t0 + t1 * t1 + t2 * t2;
+    for (int k0 = -p.kmax[0]; k0 <= p.kmax[0]; ++k0) {
+      if (abs(sh[0] + k0) > p.nsum) continue;
+      const double t0 = fma(-(double)k0, g.box[0], mm[0]);
+      const double a0 = t0 * t0;
+      if (a0 >= rc2) continue;
+      for (int k1 = -p.kmax[1]; k1 <= p.kmax[1]; ++k1) {
+        if (abs(sh[1] + k1) > p.nsum) continue;
+        const double t1 = fma(-(double)k1, g.box[1], mm[1]);
+        const double a1 = fma(t1, t1, a0);
+        if (a1 >= rc2) continue;
+        for (int k2 = -p.kmax[2]; k2 <= p.kmax[2]; ++k2) {
+          if (abs(sh[2] + k2) > p.nsum) continue;
+          const double t2 = fma(-(double)k2, g.box[2], mm[2]);
+          const double R2 = fma(t2, t2, a1);
           if (R2 >= rc2) continue;
-          const double R = sqrt(R2);
-          const double ec = erfc(a * R);
-          const double mult = p.qs * 2 * a * exp(-a2 * R2) / (SQRT_PI * R2) + p.qs * ec / (R2 * R);
-          F0 += t0 * mult;
-          F1 += t1 * mult;
-          F2 += t2 * mult;
-          if (want_e) e += ec / R;
+          const double rinv = rsqrt(R2);
+          const double xr = p.alpha * (R2 * rinv);
+          int iv = (int)(xr * EW_INV_W);
+          iv = iv < EW_NINT - 1 ? iv : EW_NINT - 1;
+          const double u = fma(xr, 2 * EW_INV_W, -(double)(2 * iv + 1));
+          const double *c = tab + iv * (EW_DEG + 1);
+          double hv = c[EW_DEG];
+#pragma unroll
+          for (int q = EW_DEG - 1; q >= 0; --q) hv = fma(hv, u, c[q]);
+          if (ENERGY_TAB) {
+            e = fma(hv, rinv, e);
+          } else {
+            const double mult = hv * (rinv * rinv * rinv);
+            F0 = fma(t0, mult, F0);
+            F1 = fma(t1, mult, F1);
+            F2 = fma(t2, mult, F2);
+          }
         }
       }
     }
-    F[0] = F0;
-    if (D > 1) F[1] = F1;
-    if (D > 2) F[2] = F2;
+    F[0] = p.qs * F0;
+    if (D > 1) F[1] = p.qs * F1;
+    if (D > 2) F[2] = p.qs * F2;
     if (want_e) E = p.qs * e;
   }
 }
 
 template <int D, int KIND, bool ENERGY>
-__global__ void __launch_bounds__(256) k_pair_tiles(Geo g, PairPrm p,
+__global__ void __launch_bounds__(256, 1) k_pair_tiles(Geo g, PairPrm p,
                                                     const double *__restrict__ x,
                                                     const double *__restrict__ m,
                                                     double *__restrict__ out, int T, int jobs) {
+  // Ewald polynomial tables staged in shared memory (lanes index them freely)
+  __shared__ double stab[KIND == PAIR_EWALD_REAL ? 2 * EW_NINT * (EW_DEG + 1) : 1];
+  if (KIND == PAIR_EWALD_REAL) {
+    for (int i = threadIdx.x; i < 2 * EW_NINT * (EW_DEG + 1); i += blockDim.x)
+      stab[i] = i < EW_NINT * (EW_DEG + 1) ? (&c_ew_h[0][0])[i] : (&c_ew_erfc[0][0])[i - EW_NINT * (EW_DEG + 1)];
+    __syncthreads();
+  }
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (warp >= jobs * g.P) return;
@@ -1138,7 +1334,7 @@ __global__ void __launch_bounds__(256) k_pair_tiles(Geo g, PairPrm p,
       double dx[D], F[D], E = 0;
 #pragma unroll
       for (int d = 0; d < D; ++d) dx[d] = xa[d] - xb[d];
-      pair_eval<D, KIND>(p, g, dx, F, E, ENERGY);
+      pair_eval<D, KIND, ENERGY>(p, g, dx, F, E, ENERGY, stab);
       if (ENERGY) {
         ea += E;
       } else {

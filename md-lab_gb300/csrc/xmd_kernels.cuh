@@ -75,9 +75,13 @@ cudaError_t fill_enk(const Geo &g, const double *x, const double *m, double w2, 
                      double *Eint, double *ENk, cudaStream_t st);
 cudaError_t fill_enk2(const Geo &g, const double *x, const double *m, double w2, int image,
                       double *ENk2, cudaStream_t st);
-cudaError_t fill_vb(int N, double beta, double vi, const double *ENk, double *VBN,
+// V_B^(n) (forward) and tmpV (backward) recursions.  VBN / tmpV hold the
+// previous values on entry (used as the prediction of the factorised form)
+// and the new ones on return.  rs: rec_scratch_doubles(N) doubles.
+size_t rec_scratch_doubles(int N);
+cudaError_t fill_vb(int N, double beta, double vi, const double *ENk, double *VBN, double *rs,
                     cudaStream_t st);
-cudaError_t back_vb(int N, double beta, double vi, const double *ENk, double *tmpV,
+cudaError_t back_vb(int N, double beta, double vi, const double *ENk, double *tmpV, double *rs,
                     cudaStream_t st);
 cudaError_t fill_g(int N, double beta, double vi, const double *ENk, const double *VBN,
                    const double *tmpV, double *G, cudaStream_t st);
@@ -114,6 +118,7 @@ struct PairPrm {
   double alpha;         // Ewald splitting
   int nsum;             // Ewald image cube
   double rcut;          // Ewald real-space cut-off radius
+  int kmax[3];          // Ewald: image shifts |k| <= kmax around the minimum image
 };
 size_t pair_scratch_doubles(const Geo &g);
 cudaError_t pair_force(const Geo &g, const PairPrm &p, const double *x, const double *m,

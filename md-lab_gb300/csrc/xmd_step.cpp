@@ -277,7 +277,8 @@ int md_pimd_fill_VB_x(md_pimd_t_x *pimd) {
   PimdDev *pd;
   XMD_TRY(pimd_device(pimd, &sd, &pd));
   XMD_TRY(check_plain(pimd));
-  XMD_CUDA(xk::fill_vb(pimd->N, pimd->beta, pimd->vi, pd->ENk.as<double>(), pd->VBN.as<double>(), stream()));
+  XMD_CUDA(xk::fill_vb(pimd->N, pimd->beta, pimd->vi, pd->ENk.as<double>(), pd->VBN.as<double>(),
+                       pd->rec.as<double>(), stream()));
   return 0;
 }
 
@@ -293,7 +294,8 @@ int md_pimd_fast_fill_force_VB_x(md_pimd_t_x *pimd, int image) {
   if (rc) return rc;
   cudaStream_t st = stream();
   const int N = pimd->N;
-  XMD_CUDA(xk::back_vb(N, pimd->beta, pimd->vi, pd->ENk.as<double>(), pd->tmpV.as<double>(), st));
+  XMD_CUDA(xk::back_vb(N, pimd->beta, pimd->vi, pd->ENk.as<double>(), pd->tmpV.as<double>(),
+                       pd->rec.as<double>(), st));
   XMD_CUDA(xk::fill_g(N, pimd->beta, pimd->vi, pd->ENk.as<double>(), pd->VBN.as<double>(), pd->tmpV.as<double>(),
                       pd->G.as<double>(), st));
   XMD_CUDA(xk::exch_force(sd->geo, sd->x.as<double>(), sd->m.as<double>(), pimd->omegaP * pimd->omegaP, image,
@@ -367,6 +369,16 @@ static xk::PairPrm pair_params(int kind) {
   return p;
 }
 
+// image shifts around the minimum image that can fall inside rcut:
+// |m - k L| < rcut with |m| <= L/2 needs |k| < 1/2 + rcut/L
+static void ewald_shifts(xk::PairPrm &p, const xk::Geo &g) {
+  for (int d = 0; d < 3; ++d) {
+    p.kmax[d] = 0;
+    if (g.box[d] > 0) p.kmax[d] = (int)ceil(0.5 + p.rcut / g.box[d]) - 1;
+    if (p.kmax[d] < 0) p.kmax[d] = 0;
+  }
+}
+
 int md_pimd_calc_pair_force_x(md_pimd_t_x *pimd, md_pair_force_t_x pf) {
   const int kind = pair_kind_of((const void *)pf, false);
   if (!kind) return fail(MD_GB_ERR_UNSUPPORTED, "pair force function has no device kernel");
@@ -380,7 +392,8 @@ int md_pimd_calc_pair_force_x(md_pimd_t_x *pimd, md_pair_force_t_x pf) {
   double *scr = scratch_for(sd, general_scratch(sd->geo), &rc);
   if (rc) return rc;
   cudaStream_t st = stream();
-  const xk::PairPrm prm = pair_params(kind);
+  xk::PairPrm prm = pair_params(kind);
+  ewald_shifts(prm, sd->geo);
   if (kind == xk::PAIR_EWALD_REAL) {
     if (!sd->uniform_mass) return fail(MD_GB_ERR_UNSUPPORTED, "structure-factor Ewald needs equal bead masses");
     XMD_TRY(ewald_tables(pimd, sd, pd));
@@ -474,7 +487,9 @@ int md_pimd_calc_pair_energy_x(md_pimd_t_x *pimd, md_pair_energy_t_x pe, md_stat
     XMD_TRY(ewald_tables(pimd, sd, pd));
     XMD_CUDA(xk::recip_energy(sd->geo, recip_of(pd), sd->x.as<double>(), acc, scr, st));
   }
-  XMD_CUDA(xk::pair_energy(sd->geo, pair_params(kind), sd->x.as<double>(), acc, scr, st));
+  xk::PairPrm prm = pair_params(kind);
+  ewald_shifts(prm, sd->geo);
+  XMD_CUDA(xk::pair_energy(sd->geo, prm, sd->x.as<double>(), acc, scr, st));
   return 0;
 }
 

@@ -80,11 +80,40 @@ def test_step_stages_match_reference(name):
     s.free()
 
 
+def _intrinsic_divergence(fx, h):
+    """How far the reference algorithm itself drifts from its own recorded
+    trajectory when every initial coordinate is moved by one ulp: the
+    Lyapunov-limited horizon of the run, measured with the oracle."""
+    import orc
+    prm = orc.params(trap_w=1.0, gauss_g=h["g"], gauss_s=h["s"], coul_s=1.0, coul_alpha=h["alpha"],
+                     coul_nsum=h["nsum"])
+    trap = 0 if h["ueg"] else orc.TRAP_HARMONIC
+    pair = orc.PAIR_EWALD if h["ueg"] else orc.PAIR_GAUSSIAN
+    N, P = h["N"], h["P"]
+    cfg = orc.StepCfg(N, P, h["beta"], h["vi"], h["omegaP"], h["image"], trap, pair, h["pbc"], prm)
+    o = orc.OrcSim.from_fixture(fx)
+    o.x[:] = np.nextafter(o.x, np.inf)
+    ENk, Eint, VBN = np.zeros(orc.ntri(N)), np.zeros(N), np.zeros(N + 1)
+    est = 0.0
+    for st in range(1, h["steps"] + 1):
+        assert orc.lib().orc_step(o.ref, orc.C.byref(cfg), h["dt"], orc.ptr(ENk), orc.ptr(Eint),
+                                  orc.ptr(VBN)) == 0
+        key = f"t{st}/e_prim_exch"
+        if key in fx:
+            e = orc.lib().orc_vbn_energy(h["D"], N, P, h["beta"], h["vi"], orc.ptr(ENk), orc.ptr(VBN))
+            est = max(est, relerr([e], fx[key]))
+    fin = max(relerr(getattr(o, k), fx["final/" + k]) for k in ("x", "v", "theta", "vtheta"))
+    return est, fin
+
+
 @pytest.mark.parametrize("name", [n for n in fixtures.PIMD_FIXTURES])
 def test_trajectory_tracks_reference(name):
     """Whole steps, device-resident between samples, against the reference's
-    recorded estimators and final state.  The bar widens with the number of
-    steps because the dynamics amplify rounding differences."""
+    recorded estimators and final state.  Over short runs the bar is the
+    1e-10 parity bar; over long runs chaotic dynamics amplify any rounding
+    difference (the GPU's exp/log differ from glibc's by an ulp), so the bar
+    is 1e-10 or 30x the drift the reference shows against itself after a
+    one-ulp change of the initial positions, whichever is larger."""
     fx, h, lib, s, trap, pair = _setup(name)
     if h["steps"] < 2:
         pytest.skip("single-step fixture")
@@ -96,11 +125,13 @@ def test_trajectory_tracks_reference(name):
             lib.check(lib.md_pimd_calc_VBN_energy_x(s.pimd, s.stats))
             e = s.take_energy()
             worst = max(worst, relerr([e], fx[key]))
-    tol = 1e-10 if h["steps"] <= 50 else 1e-8
-    assert worst <= tol, f"{name}: estimator drift {worst:.2e}"
     fin = s.state()
-    for k in ("x", "v", "theta", "vtheta"):
-        assert_close(fin[k], fx["final/" + k], tol, f"{name} final {k} after {h['steps']} steps")
+    final = max(relerr(fin[k], fx["final/" + k]) for k in ("x", "v", "theta", "vtheta"))
+    own_est, own_fin = _intrinsic_divergence(fx, h)
+    print(f"{name}: {h['steps']} steps, GPU vs reference: estimator {worst:.2e}, state {final:.2e}; "
+          f"reference vs itself (1-ulp start): estimator {own_est:.2e}, state {own_fin:.2e}")
+    assert worst <= max(PARITY, 30 * own_est), f"{name}: estimator drift {worst:.2e} (own {own_est:.2e})"
+    assert final <= max(PARITY, 30 * own_fin), f"{name}: state drift {final:.2e} (own {own_fin:.2e})"
     s.free()
 
 
