@@ -641,6 +641,53 @@ __global__ void k_enk2_rows(Geo g, const double *__restrict__ x, const double *_
   }
 }
 
+// cubic-path table of md_pimd_fill_ENk2_x (md_pimd_x.c:3959-3987, CPU
+// :4049-4054): for the cycle over particles l = N2-k+1..N2, each bead P is
+// followed by bead 1 of the next particle in the cycle (b) and
+//   ENk2[N2][k] = sum_l 1/2 m_b w2 (x_b - x_{l,P}).(x_b - x_{l,1}).
+// For l < N2 the term depends on l alone (b = l+1), so a row is a scan over
+// k of those terms plus the closing term of l = N2 (b = N2-k+1).
+template <int D>
+__global__ void k_enk2_cubic_rows(Geo g, const double *__restrict__ x, const double *__restrict__ m,
+                                  double w2, int image, double *__restrict__ ENk2) {
+  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  const int n = w + 1;  // 1-based N2
+  if (n > g.N) return;
+  const int jP = g.P - 1;
+  double carry = 0;
+  for (int k0 = 1; k0 <= n; k0 += 32) {
+    const int k = k0 + lane;
+    double inc = 0, close = 0;
+    if (k <= n) {
+      if (k >= 2) {
+        const int l = n - k + 1;  // 1-based, l < n: b = l+1
+        inc = cross<D>(g, x, m, w2, 0, l, jP, l - 1, 0, l - 1, image);
+      }
+      const int b = n - k + 1;  // closing bead of l = n
+      close = cross<D>(g, x, m, w2, 0, b - 1, jP, n - 1, 0, n - 1, image);
+    }
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const double t = __shfl_up_sync(FULL, inc, o);
+      if (lane >= o) inc += t;
+    }
+    const double e = carry + inc;
+    if (k <= n) ENk2[dtri(n) + k - 1] = e + close;
+    carry = __shfl_sync(FULL, e, 31);
+  }
+}
+
+cudaError_t fill_enk2_cubic(const Geo &g, const double *x, const double *m, double w2, int image,
+                            double *ENk2, cudaStream_t st) {
+  const size_t thr = (size_t)g.N * 32;
+  {
+    XK_PROF("enk2_cubic_rows");
+    DISPATCH_D(g.D, k_enk2_cubic_rows<D><<<cdiv(thr, 256), 256, 0, st>>>(g, x, m, w2, image, ENk2));
+  }
+  return XK_LAUNCHED();
+}
+
 cudaError_t fill_enk2(const Geo &g, const double *x, const double *m, double w2, int image,
                       double *ENk2, cudaStream_t st) {
   const size_t thr = (size_t)g.N * 32;
@@ -662,265 +709,231 @@ static int rec_threads(int N) {
   return t;
 }
 
-// ---- exact forms (one block; the reference's loop order) ----------
-// forward V_B: md_pimd_x.c:814-953 (CPU :934-950) with md_pimd_xminE_x
-// (:796-806) and md_pimd_xexp_x (:681-686); V in shared memory.
-__device__ void vb_exact(int N, double beta, double vi, const double *__restrict__ ENk, double *V,
-                         double *bmin, double *bsum) {
-  const double lnvi = vi != 0.0 ? log(vi) : 0.0;
-  if (threadIdx.x == 0) V[0] = 0.0;
-  __syncthreads();
-  for (int n = 1; n <= N; ++n) {
-    const double *row = ENk + dtri(n);
-    double mloc = 1e10;
-    if (vi == 0.0) {
-      mloc = beta * (row[0] + V[n - 1]);
-    } else {
-      for (int k = threadIdx.x + 1; k <= n; k += blockDim.x) {
-        const double t = -(k - 1) * lnvi + beta * (row[k - 1] + V[n - k]);
-        if (t < mloc) mloc = t;
-      }
-      mloc = block_min(mloc, 1e10, bmin);
-    }
-    double s = 0;
-    for (int k = threadIdx.x + 1; k <= n; k += blockDim.x) {
-      if (vi == 0.0 && k != 1) continue;
-      const double E = row[k - 1] + V[n - k];
-      s += (vi == 0.0) ? exp(-beta * E + mloc) : exp((k - 1) * lnvi - beta * E + mloc);
-    }
-    s = block_sum(s, bsum);
-    if (threadIdx.x == 0) V[n] = (mloc - log(s) + log((double)n)) / beta;
-    __syncthreads();
+// ---- linear-solve form ----------------------------------------------
+// With Z_n = exp(-beta V_n) the forward recursion is linear:
+//   Z_0 = 1,  Z_n = sum_{k=1..n} M_{n,n-k} Z_{n-k},
+//   M_{n,j} = xi^(k-1) exp(-beta E_n^(k)) / n            (k = n - j),
+// and V_n = -ln(Z_n)/beta; this is the reference's log-sum-exp recursion
+// without the shift.  The backward recursion is the same system after the
+// index map i = N-u+1 (X_i = exp(-beta tmpV_{u-1})), j = N-l, k = i-j:
+//   M'_{i,j} = xi^(k-1) exp(-beta E_l^(k)) / l.
+// Z spans far more than the FP64 exponent range (beta V_n ~ 100 n), so every
+// weight and unknown is kept in extended range: an FP64 mantissa and an int
+// power of two.  All weights (N^2/2 exponentials) are computed in parallel
+// over the GPU; one block then solves the unit lower-triangular system in
+// chunks of 32 rows: the contribution of the already known unknowns to the
+// chunk is a parallel extended-range dot product per row, and the chunk
+// itself is a 32-step warp-synchronous substitution.  No exponential or
+// logarithm sits on the sequential chain, which matters because a dependent
+// FP64 operation costs ~64 cycles on this GPU.
+//
+// For xi = 0 only k = 1 enters (M_{i,i-1}), as in the reference's branch.
+
+// ln 2 split so that e * LN2_HI is exact for |e| < 2^21 (32 significant bits)
+constexpr double LN2_HI = 0.6931471803691238, LN2_LO = 1.9082149292705877e-10;
+constexpr double LOG2E = 1.4426950408889634;
+
+struct Ext {
+  double m;  // mantissa (0 or a normal number of moderate size)
+  int e;     // value = m * 2^e
+};
+
+// exp(x) in extended range for any finite x: 2^e * exp(r), |r| <= ln2/2
+__device__ inline Ext ext_exp(double x) {
+  const double q = rint(x * LOG2E);
+  double r = fma(-q, LN2_HI, x);
+  r = fma(-q, LN2_LO, r);
+  return {exp(r), (int)q};
+}
+
+// m * 2^d for d <= 0 (0 once the result would drop below the subnormals)
+__device__ inline double scale_down(double m, int d) {
+  if (d >= -1022) return m * __longlong_as_double((long long)(d + 1023) << 52);
+  if (d < -1100) return 0.0;
+  return m * 0x1p-1022 * __longlong_as_double((long long)(d + 1022 + 1023) << 52);
+}
+
+// acc += t in extended range
+__device__ inline void ext_add(double &am, int &ae, double tm, int te) {
+  if (tm == 0.0) return;
+  if (am == 0.0) {
+    am = tm;
+    ae = te;
+  } else if (te > ae) {
+    am = scale_down(am, ae - te) + tm;
+    ae = te;
+  } else {
+    am += scale_down(tm, te - ae);
   }
 }
 
-// backward tmpV: md_pimd_x.c:2648-2659 with md_pimd_fast_xminE_x (:2321-2333)
-// and md_pimd_fast_xexp_x (:2337-2342); V in shared memory.
-__device__ void tv_exact(int N, double beta, double vi, const double *__restrict__ ENk, double *V,
-                         double *bmin, double *bsum) {
-  const double lnvi = vi != 0.0 ? log(vi) : 0.0;
-  if (threadIdx.x == 0) V[N] = 0.0;
-  __syncthreads();
-  for (int u = N; u >= 1; --u) {
-    double mloc = 1e10;
-    if (vi == 0.0) {
-      mloc = log((double)u) + beta * (ENk[dtri(u)] + V[u]);
-    } else {
-      for (int l = u + threadIdx.x; l <= N; l += blockDim.x) {
-        const int k = l - u + 1;
-        const double t = -(k - 1) * lnvi + log((double)l) + beta * (ENk[dtri(l) + k - 1] + V[l]);
-        if (t < mloc) mloc = t;
-      }
-      mloc = block_min(mloc, 1e10, bmin);
-    }
-    double s = 0;
-    for (int l = u + threadIdx.x; l <= N; l += blockDim.x) {
-      const int k = l - u + 1;
-      if (vi == 0.0 && k != 1) continue;
-      const double E = ENk[dtri(l) + k - 1] + V[l];
-      const double lg = log((double)l);
-      s += (vi == 0.0) ? exp(-beta * E + mloc - lg) : exp((k - 1) * lnvi - beta * E + mloc - lg);
-    }
-    s = block_sum(s, bsum);
-    if (threadIdx.x == 0) V[u - 1] = (mloc - log(s)) / beta;
-    __syncthreads();
-  }
+__device__ inline void ext_norm(double &m, int &e) {
+  if (m == 0.0) return;
+  int k;
+  m = frexp(m, &k);
+  e += k;
 }
 
-// ---- factorised forms -------------------------------------------------
-// With a prediction Vp of V (the previous call's values) every weight of the
-// recursion splits into a part known in advance and one factor per earlier
-// step:
-//   exp((k-1) ln xi - beta (E_n^(k) + V_{n-k}))
-//     = exp(-c_n) * A_{n,k} * B_{n-k},
-//   A_{n,k} = exp(c_n - t_{n,k}),  t_{n,k} = beta (E_n^(k) + Vp_{n-k}) - (k-1) ln xi,
-//   c_n = min_k t_{n,k},           B_j = exp(-beta (V_j - Vp_j)).
-// Then V_n = (c_n - ln S_n + ln n)/beta with S_n = sum_k A_{n,k} B_{n-k}, and
-// B_n = S_n K_n with K_n = exp(beta Vp_n - c_n - ln n).  All exponentials
-// (A, K) are computed in parallel over the whole GPU; the sequential part
-// is one dot product per n.  If a B or S leaves [1e-250, 1e250] (a poor or
-// absent prediction) the sequential kernel restarts with the exact form.
-// The backward recursion factorises the same way with l, u and ln l.
+// packed lower triangle: row i (1..N), column j (0..i-1) at tri(i) + j
+__device__ inline size_t moff(int i, int j) { return (size_t)i * (i - 1) / 2 + j; }
 
-constexpr double REC_LO = 1e-250, REC_HI = 1e250;
-
-// one warp per row n = 1..N: W[(n-1)*N + k-1], c[n], K[n]
+// forward weights M_{n,j}, one warp per row n
 __global__ void k_vb_weights(int N, double beta, double vi, const double *__restrict__ ENk,
-                             const double *__restrict__ Vp, double *__restrict__ W,
-                             double *__restrict__ c, double *__restrict__ K) {
+                             double *__restrict__ Mm, int *__restrict__ Me) {
   const int n = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) + 1;
   const int lane = threadIdx.x & 31;
   if (n > N) return;
   const double lnvi = vi != 0.0 ? log(vi) : 0.0;
-  const int kmax = vi == 0.0 ? 1 : n;
-  const double *row = ENk + dtri(n);
-  double *w = W + (size_t)(n - 1) * N;
-  double mn = 1e300;
-  for (int k = lane + 1; k <= kmax; k += 32) {
-    const double t = beta * (row[k - 1] + Vp[n - k]) - (k - 1) * lnvi;
-    w[k - 1] = t;
-    mn = t < mn ? t : mn;
-  }
-  mn = warp_min(mn);
-  __syncwarp();
-  for (int k = lane + 1; k <= kmax; k += 32) w[k - 1] = exp(mn - w[k - 1]);
-  if (lane == 0) {
-    c[n] = mn;
-    K[n] = exp(beta * Vp[n] - mn - log((double)n));
+  const double lnn = log((double)n);
+  for (int j = lane; j < n; j += 32) {
+    const int k = n - j;
+    Ext w{0.0, 0};
+    if (vi != 0.0 || k == 1) w = ext_exp(-beta * ENk[dtri(n) + k - 1] + (k - 1) * lnvi - lnn);
+    Mm[moff(n, j)] = w.m;
+    Me[moff(n, j)] = w.e;
   }
 }
 
-__global__ void k_vb_seq(int N, double beta, double vi, const double *__restrict__ ENk,
-                         const double *__restrict__ W, const double *__restrict__ c,
-                         const double *__restrict__ K, double *__restrict__ VBN) {
-  extern __shared__ double sh[];
-  double *B = sh;             // N+1
-  double *S = B + N + 1;      // N+1
-  double *bmin = S + N + 1;   // 33
-  double *bsum = bmin + 33;   // 33
-  __shared__ int bad;
-  if (threadIdx.x == 0) {
-    B[0] = 1.0;
-    bad = 0;
-  }
-  __syncthreads();
-  const int one = vi == 0.0;
-  // prefetch of this thread's first weight of the next row
-  double wnext = (threadIdx.x < 1) ? W[threadIdx.x] : 0.0;
-  for (int n = 1; n <= N; ++n) {
-    const int kmax = one ? 1 : n;
-    const double *w = W + (size_t)(n - 1) * N;
-    double part = 0;
-    const int k0 = threadIdx.x + 1;
-    if (k0 <= kmax) part = wnext * B[n - k0];
-    for (int k = k0 + blockDim.x; k <= kmax; k += blockDim.x) part += w[k - 1] * B[n - k];
-    if (n < N) {
-      const int kn = one ? 1 : n + 1;
-      wnext = k0 <= kn ? W[(size_t)n * N + k0 - 1] : 0.0;
-    }
-    const double sn = block_sum(part, bsum);
-    if (threadIdx.x == 0) {
-      const double bn = sn * K[n];
-      S[n] = sn;
-      B[n] = bn;
-      if (!(sn > REC_LO && sn < REC_HI && bn > REC_LO && bn < REC_HI)) bad = 1;
-    }
-    __syncthreads();
-    if (bad) break;
-  }
-  if (!bad) {
-    for (int n = threadIdx.x + 1; n <= N; n += blockDim.x)
-      VBN[n] = (c[n] - log(S[n]) + log((double)n)) / beta;
-    if (threadIdx.x == 0) VBN[0] = 0.0;
-    return;
-  }
-  __syncthreads();
-  double *V = B;  // reuse: N+1
-  vb_exact(N, beta, vi, ENk, V, bmin, bsum);
-  for (int i = threadIdx.x; i <= N; i += blockDim.x) VBN[i] = V[i];
-}
-
-// one warp per row u = 1..N, l = u..N (k = l-u+1): W[(u-1)*N + l-1], c[u], K[u]
+// backward weights M'_{i,j}, row i <-> u = N-i+1, column j <-> l = N-j
 __global__ void k_tv_weights(int N, double beta, double vi, const double *__restrict__ ENk,
-                             const double *__restrict__ Tp, double *__restrict__ W,
-                             double *__restrict__ c, double *__restrict__ K) {
-  const int u = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) + 1;
+                             double *__restrict__ Mm, int *__restrict__ Me) {
+  const int i = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) + 1;
   const int lane = threadIdx.x & 31;
-  if (u > N) return;
+  if (i > N) return;
   const double lnvi = vi != 0.0 ? log(vi) : 0.0;
-  const int lmax = vi == 0.0 ? u : N;
-  double *w = W + (size_t)(u - 1) * N;
-  double mn = 1e300;
-  for (int l = u + lane; l <= lmax; l += 32) {
-    const int k = l - u + 1;
-    const double t = beta * (ENk[dtri(l) + k - 1] + Tp[l]) - (k - 1) * lnvi + log((double)l);
-    w[l - 1] = t;
-    mn = t < mn ? t : mn;
-  }
-  mn = warp_min(mn);
-  __syncwarp();
-  for (int l = u + lane; l <= lmax; l += 32) w[l - 1] = exp(mn - w[l - 1]);
-  if (lane == 0) {
-    c[u] = mn;
-    K[u] = exp(beta * Tp[u - 1] - mn);
+  for (int j = lane; j < i; j += 32) {
+    const int k = i - j, l = N - j;
+    Ext w{0.0, 0};
+    if (vi != 0.0 || k == 1) w = ext_exp(-beta * ENk[dtri(l) + k - 1] + (k - 1) * lnvi - log((double)l));
+    Mm[moff(i, j)] = w.m;
+    Me[moff(i, j)] = w.e;
   }
 }
 
-__global__ void k_tv_seq(int N, double beta, double vi, const double *__restrict__ ENk,
-                         const double *__restrict__ W, const double *__restrict__ c,
-                         const double *__restrict__ K, double *__restrict__ tmpV) {
+// X_0 = 1, X_i = sum_{j<i} M_{i,j} X_j (i = 1..N); out_i = -ln(X_i)/beta written
+// to out[i] (forward) or out[N-i] (backward).  One block, 16 warps.
+constexpr int TS_WARPS = 16, TS_CHUNK = 32;
+
+__global__ void __launch_bounds__(TS_WARPS * 32) k_tri_solve(int N, double beta,
+                                                             const double *__restrict__ Mm,
+                                                             const int *__restrict__ Me,
+                                                             double *__restrict__ out,
+                                                             int backward) {
   extern __shared__ double sh[];
-  double *B = sh;             // N+1, B[l] for l = 0..N
-  double *S = B + N + 1;      // N+1
-  double *bmin = S + N + 1;   // 33
-  double *bsum = bmin + 33;   // 33
-  __shared__ int bad;
+  double *Xm = sh;                      // N+1
+  double *Pm = Xm + N + 1;              // TS_CHUNK
+  int *Xe = (int *)(Pm + TS_CHUNK);     // N+1
+  int *Pe = Xe + N + 1;                 // TS_CHUNK
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   if (threadIdx.x == 0) {
-    B[N] = 1.0;
-    bad = 0;
+    Xm[0] = 0.5;
+    Xe[0] = 1;
   }
   __syncthreads();
-  const int one = vi == 0.0;
-  for (int u = N; u >= 1; --u) {
-    const int lmax = one ? u : N;
-    const double *w = W + (size_t)(u - 1) * N;
-    double part = 0;
-    for (int l = u + threadIdx.x; l <= lmax; l += blockDim.x) part += w[l - 1] * B[l];
-    const double su = block_sum(part, bsum);
-    if (threadIdx.x == 0) {
-      const double bu = su * K[u];
-      S[u] = su;
-      B[u - 1] = bu;
-      if (!(su > REC_LO && su < REC_HI && bu > REC_LO && bu < REC_HI)) bad = 1;
+  for (int i0 = 1; i0 <= N; i0 += TS_CHUNK) {
+    // known part: rows i0..i0+31 against columns 0..i0-1, two rows per warp
+    for (int r = w; r < TS_CHUNK; r += TS_WARPS) {
+      const int i = i0 + r;
+      double am = 0.0;
+      int ae = 0;
+      if (i <= N) {
+        const double *mr = Mm + moff(i, 0);
+        const int *er = Me + moff(i, 0);
+        for (int j = lane; j < i0; j += 32) ext_add(am, ae, mr[j] * Xm[j], er[j] + Xe[j]);
+      }
+#pragma unroll
+      for (int o = 16; o; o >>= 1) {
+        const double om = __shfl_xor_sync(FULL, am, o);
+        const int oe = __shfl_xor_sync(FULL, ae, o);
+        ext_add(am, ae, om, oe);
+      }
+      if (lane == 0) {
+        ext_norm(am, ae);
+        Pm[r] = am;
+        Pe[r] = ae;
+      }
     }
     __syncthreads();
-    if (bad) break;
+    // the chunk itself: lane r owns row i0+r
+    if (w == 0) {
+      const int i = i0 + lane;
+      const bool own = i <= N;
+      double am = own ? Pm[lane] : 0.0;
+      int ae = own ? Pe[lane] : 0;
+      double mm[TS_CHUNK];
+      int me[TS_CHUNK];
+#pragma unroll
+      for (int s = 0; s < TS_CHUNK; ++s) {
+        const bool in = own && s < lane;
+        mm[s] = in ? Mm[moff(i, i0 + s)] : 0.0;
+        me[s] = in ? Me[moff(i, i0 + s)] : 0;
+      }
+#pragma unroll
+      for (int s = 0; s < TS_CHUNK; ++s) {
+        if (lane == s) {
+          ext_norm(am, ae);
+          if (own) {
+            Xm[i] = am;
+            Xe[i] = ae;
+          }
+        }
+        const double xm = __shfl_sync(FULL, am, s);
+        const int xe = __shfl_sync(FULL, ae, s);
+        if (lane > s) ext_add(am, ae, mm[s] * xm, me[s] + xe);
+      }
+    }
+    __syncthreads();
   }
-  if (!bad) {
-    for (int u = threadIdx.x + 1; u <= N; u += blockDim.x) tmpV[u - 1] = (c[u] - log(S[u])) / beta;
-    if (threadIdx.x == 0) tmpV[N] = 0.0;
-    return;
+  for (int i = threadIdx.x + 1; i <= N; i += blockDim.x) {
+    const double lnx = log(Xm[i]) + Xe[i] * LN2_HI + Xe[i] * LN2_LO;
+    out[backward ? N - i : i] = -lnx / beta;
   }
-  __syncthreads();
-  double *V = B;
-  tv_exact(N, beta, vi, ENk, V, bmin, bsum);
-  for (int i = threadIdx.x; i <= N; i += blockDim.x) tmpV[i] = V[i];
+  if (threadIdx.x == 0) out[backward ? N : 0] = 0.0;
 }
 
-size_t rec_scratch_doubles(int N) { return (size_t)N * N + 2 * (size_t)(N + 1); }
+// scratch: mantissas (ntri(N) doubles) then exponents (ntri(N) ints)
+size_t rec_scratch_doubles(int N) { return ntri(N) + (ntri(N) + 1) / 2 + 1; }
+
+static cudaError_t tri_solve(int N, double beta, const double *Mm, const int *Me, double *out,
+                             int backward, cudaStream_t st) {
+  const size_t smem = (sizeof(double) + sizeof(int)) * (N + 1 + TS_CHUNK) + 16;
+  static bool opted = false;
+  if (!opted) {
+    cudaError_t ea = cudaFuncSetAttribute(k_tri_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    if (ea != cudaSuccess) return ea;
+    opted = true;
+  }
+  {
+    XK_PROF(backward ? "tv_solve" : "vb_solve");
+    k_tri_solve<<<1, TS_WARPS * 32, smem, st>>>(N, beta, Mm, Me, out, backward);
+  }
+  return XK_LAUNCHED();
+}
 
 cudaError_t fill_vb(int N, double beta, double vi, const double *ENk, double *VBN, double *rs,
                     cudaStream_t st) {
-  double *W = rs, *c = rs + (size_t)N * N, *K = c + N + 1;
+  double *Mm = rs;
+  int *Me = (int *)(rs + ntri(N));
   {
     XK_PROF("vb_weights");
-    k_vb_weights<<<cdiv((size_t)N * 32, 256), 256, 0, st>>>(N, beta, vi, ENk, VBN, W, c, K);
+    k_vb_weights<<<cdiv((size_t)N * 32, 256), 256, 0, st>>>(N, beta, vi, ENk, Mm, Me);
   }
   cudaError_t e = XK_LAUNCHED();
   if (e != cudaSuccess) return e;
-  const size_t smem = sizeof(double) * (2 * (N + 1) + 66);
-  {
-    XK_PROF("vb_seq");
-    k_vb_seq<<<1, rec_threads(N), smem, st>>>(N, beta, vi, ENk, W, c, K, VBN);
-  }
-  return XK_LAUNCHED();
+  return tri_solve(N, beta, Mm, Me, VBN, 0, st);
 }
 
 cudaError_t back_vb(int N, double beta, double vi, const double *ENk, double *tmpV, double *rs,
                     cudaStream_t st) {
-  double *W = rs, *c = rs + (size_t)N * N, *K = c + N + 1;
+  double *Mm = rs;
+  int *Me = (int *)(rs + ntri(N));
   {
     XK_PROF("tv_weights");
-    k_tv_weights<<<cdiv((size_t)N * 32, 256), 256, 0, st>>>(N, beta, vi, ENk, tmpV, W, c, K);
+    k_tv_weights<<<cdiv((size_t)N * 32, 256), 256, 0, st>>>(N, beta, vi, ENk, Mm, Me);
   }
   cudaError_t e = XK_LAUNCHED();
   if (e != cudaSuccess) return e;
-  const size_t smem = sizeof(double) * (2 * (N + 1) + 66);
-  {
-    XK_PROF("tv_seq");
-    k_tv_seq<<<1, rec_threads(N), smem, st>>>(N, beta, vi, ENk, W, c, K, tmpV);
-  }
-  return XK_LAUNCHED();
+  return tri_solve(N, beta, Mm, Me, tmpV, 1, st);
 }
 
 // connection probabilities G[l][j]: md_pimd_x.c:2660-2673
@@ -1205,9 +1218,12 @@ cudaError_t trap_energy(const Geo &g, const TrapPrm &p, const double *x, const d
 __constant__ double c_ew_h[EW_NINT][EW_DEG + 1] = EW_H_INIT;
 __constant__ double c_ew_erfc[EW_NINT][EW_DEG + 1] = EW_ERFC_INIT;
 
+// Force F(dx) (times the pair's strength, before the 1/m and 1/P factors)
+// and, with want_e, the pair energy.  The Ewald kind is warp-collective: all
+// lanes call it, `active` says whether the lane's pair counts.
 template <int D, int KIND, bool ENERGY_TAB>
 __device__ inline void pair_eval(const PairPrm &p, const Geo &g, const double *dx, double *F,
-                                 double &E, bool want_e, const double *tabs) {
+                                 double &E, bool want_e, const double *tabs, bool active) {
   if (KIND == PAIR_GAUSSIAN || KIND == PAIR_PERIODIC_GAUSSIAN) {
     double t[D], r2 = 0;
 #pragma unroll
@@ -1238,43 +1254,56 @@ __device__ inline void pair_eval(const PairPrm &p, const Geo &g, const double *d
     // Real-space images of the partner inside the reference's cube
     // |n_i| <= nsum (md_simulation_x.c:281-292) whose distance is below
     // rcut.  dx is first reduced to its minimum image m = dx - s L, so the
-    // candidates are n = s + k with |k| <= kmax.  Per image the force factor
-    // s (erfc(x) + 2x exp(-x^2)/sqrt(pi)) / R^3 with x = alpha R comes from
-    // the piecewise polynomial EW_H (no FP64 erfc or exp), 1/R from rsqrt.
+    // candidates are n = s + k with |k_d| <= kmax.  The candidates are culled
+    // on the FP32 pipe into a bit mask (with a 1e-4 margin; the FP64 test
+    // below decides), then evaluated in warp-wide rounds, one accepted image
+    // per lane per round, so that the FP64 pipe runs with full warps.  Per
+    // image the factor (erfc(x) + 2x exp(-x^2)/sqrt(pi)) / R^3, x = alpha R,
+    // comes from the piecewise polynomial EW_H (no FP64 erfc or exp), 1/R
+    // from rsqrt.
     const double *tab = ENERGY_TAB ? tabs + EW_NINT * (EW_DEG + 1) : tabs;
+    const double rc2 = p.rcut * p.rcut;
     double mm[3];
     int sh[3];
+    unsigned mask = 0u;
+    if (active) {
 #pragma unroll
-    for (int d = 0; d < 3; ++d) {
-      sh[d] = (int)rint(dx[d] * g.inv_box[d]);
-      mm[d] = fma(-(double)sh[d], g.box[d], dx[d]);
+      for (int d = 0; d < 3; ++d) {
+        sh[d] = (int)rint(dx[d] * g.inv_box[d]);
+        mm[d] = fma(-(double)sh[d], g.box[d], dx[d]);
+      }
+      const float rc2f = (float)(rc2 * 1.0001);
+      const float m0 = (float)mm[0], m1 = (float)mm[1], m2 = (float)mm[2];
+      const float L0 = (float)g.box[0], L1 = (float)g.box[1], L2 = (float)g.box[2];
+#pragma unroll
+      for (int c = 0; c < 27; ++c) {
+        const int k0 = c / 9 - 1, k1 = (c / 3) % 3 - 1, k2 = c % 3 - 1;
+        const float t0 = fmaf(-(float)k0, L0, m0), t1 = fmaf(-(float)k1, L1, m1), t2 = fmaf(-(float)k2, L2, m2);
+        const float r2 = fmaf(t2, t2, fmaf(t1, t1, t0 * t0));
+        const bool in_cube = abs(sh[0] + k0) <= p.nsum && abs(sh[1] + k1) <= p.nsum && abs(sh[2] + k2) <= p.nsum;
+        if (r2 < rc2f && in_cube) mask |= 1u << c;
+      }
     }
-    const double rc2 = p.rcut * p.rcut;
     double F0 = 0, F1 = 0, F2 = 0, e = 0;
-    for (int k0 = -p.kmax[0]; k0 <= p.kmax[0]; ++k0) {
-      if (abs(sh[0] + k0) > p.nsum) continue;
-      const double t0 = fma(-(double)k0, g.box[0], mm[0]);
-      const double a0 = t0 * t0;
-      if (a0 >= rc2) continue;
-      for (int k1 = -p.kmax[1]; k1 <= p.kmax[1]; ++k1) {
-        if (abs(sh[1] + k1) > p.nsum) continue;
+    while (__any_sync(FULL, mask != 0u)) {
+      if (mask) {
+        const int c = __ffs(mask) - 1;
+        mask &= mask - 1;
+        const int k0 = c / 9 - 1, k1 = (c / 3) % 3 - 1, k2 = c % 3 - 1;
+        const double t0 = fma(-(double)k0, g.box[0], mm[0]);
         const double t1 = fma(-(double)k1, g.box[1], mm[1]);
-        const double a1 = fma(t1, t1, a0);
-        if (a1 >= rc2) continue;
-        for (int k2 = -p.kmax[2]; k2 <= p.kmax[2]; ++k2) {
-          if (abs(sh[2] + k2) > p.nsum) continue;
-          const double t2 = fma(-(double)k2, g.box[2], mm[2]);
-          const double R2 = fma(t2, t2, a1);
-          if (R2 >= rc2) continue;
+        const double t2 = fma(-(double)k2, g.box[2], mm[2]);
+        const double R2 = fma(t2, t2, fma(t1, t1, t0 * t0));
+        if (R2 < rc2) {
           const double rinv = rsqrt(R2);
           const double xr = p.alpha * (R2 * rinv);
           int iv = (int)(xr * EW_INV_W);
           iv = iv < EW_NINT - 1 ? iv : EW_NINT - 1;
           const double u = fma(xr, 2 * EW_INV_W, -(double)(2 * iv + 1));
-          const double *c = tab + iv * (EW_DEG + 1);
-          double hv = c[EW_DEG];
+          const double *cf = tab + iv * (EW_DEG + 1);
+          double hv = cf[EW_DEG];
 #pragma unroll
-          for (int q = EW_DEG - 1; q >= 0; --q) hv = fma(hv, u, c[q]);
+          for (int q = EW_DEG - 1; q >= 0; --q) hv = fma(hv, u, cf[q]);
           if (ENERGY_TAB) {
             e = fma(hv, rinv, e);
           } else {
@@ -1330,11 +1359,15 @@ __global__ void __launch_bounds__(256, 1) k_pair_tiles(Geo g, PairPrm p,
   for (int s = 0; s < 32; ++s) {
     const int bi = J * 32 + ((lane + s) & 31);
     const bool act = va && bi < g.N && (I != J || a > bi);
-    if (act) {
-      double dx[D], F[D], E = 0;
+    double dx[D], F[D], E = 0;
 #pragma unroll
-      for (int d = 0; d < D; ++d) dx[d] = xa[d] - xb[d];
-      pair_eval<D, KIND, ENERGY>(p, g, dx, F, E, ENERGY, stab);
+    for (int d = 0; d < D; ++d) {
+      dx[d] = xa[d] - xb[d];
+      F[d] = 0;
+    }
+    if (KIND == PAIR_EWALD_REAL) pair_eval<D, KIND, ENERGY>(p, g, dx, F, E, ENERGY, stab, act);
+    if (act) {
+      if (KIND != PAIR_EWALD_REAL) pair_eval<D, KIND, ENERGY>(p, g, dx, F, E, ENERGY, stab, true);
       if (ENERGY) {
         ea += E;
       } else {

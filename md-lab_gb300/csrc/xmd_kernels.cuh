@@ -75,9 +75,11 @@ cudaError_t fill_enk(const Geo &g, const double *x, const double *m, double w2, 
                      double *Eint, double *ENk, cudaStream_t st);
 cudaError_t fill_enk2(const Geo &g, const double *x, const double *m, double w2, int image,
                       double *ENk2, cudaStream_t st);
-// V_B^(n) (forward) and tmpV (backward) recursions.  VBN / tmpV hold the
-// previous values on entry (used as the prediction of the factorised form)
-// and the new ones on return.  rs: rec_scratch_doubles(N) doubles.
+// the cubic path's table (md_pimd_fill_ENk2_x), a different quantity
+cudaError_t fill_enk2_cubic(const Geo &g, const double *x, const double *m, double w2, int image,
+                            double *ENk2, cudaStream_t st);
+// V_B^(n) (forward) and tmpV (backward) recursions, solved as extended-
+// range triangular systems.  rs: rec_scratch_doubles(N) doubles of scratch.
 size_t rec_scratch_doubles(int N);
 cudaError_t fill_vb(int N, double beta, double vi, const double *ENk, double *VBN, double *rs,
                     cudaStream_t st);

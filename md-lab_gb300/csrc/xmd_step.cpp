@@ -395,6 +395,9 @@ int md_pimd_calc_pair_force_x(md_pimd_t_x *pimd, md_pair_force_t_x pf) {
   xk::PairPrm prm = pair_params(kind);
   ewald_shifts(prm, sd->geo);
   if (kind == xk::PAIR_EWALD_REAL) {
+    if (prm.kmax[0] > 1 || prm.kmax[1] > 1 || prm.kmax[2] > 1)
+      return fail(MD_GB_ERR_UNSUPPORTED, "Ewald alpha*L below %.1f (images beyond the neighbouring boxes)",
+                  2 * EWALD_XCUT / 3);
     if (!sd->uniform_mass) return fail(MD_GB_ERR_UNSUPPORTED, "structure-factor Ewald needs equal bead masses");
     XMD_TRY(ewald_tables(pimd, sd, pd));
     XMD_CUDA(xk::recip_force(sd->geo, recip_of(pd), sd->x.as<double>(), 1.0 / (sd->mass0 * pimd->P),
@@ -432,7 +435,18 @@ int md_pimd_fast_fill_ENk2_x(md_pimd_t_x *pimd, int image) {
   return 0;
 }
 
-int md_pimd_fill_ENk2_x(md_pimd_t_x *pimd, int image) { return md_pimd_fast_fill_ENk2_x(pimd, image); }
+// the cubic entry point fills a different table than the fast one (only
+// the virial estimator built on either agrees): md_pimd_x.c:3959-4056
+int md_pimd_fill_ENk2_x(md_pimd_t_x *pimd, int image) {
+  SimDev *sd;
+  PimdDev *pd;
+  XMD_TRY(pimd_device(pimd, &sd, &pd));
+  XMD_TRY(check_plain(pimd));
+  XMD_TRY(check_image(sd, image));
+  XMD_CUDA(xk::fill_enk2_cubic(sd->geo, sd->x.as<double>(), sd->m.as<double>(), pimd->omegaP * pimd->omegaP,
+                               image, pd->ENk2.as<double>(), stream()));
+  return 0;
+}
 
 int md_pimd_calc_vi_virial_energy_x(md_pimd_t_x *pimd, md_stats_t_x *stats, int image) {
   SimDev *sd;
@@ -489,6 +503,9 @@ int md_pimd_calc_pair_energy_x(md_pimd_t_x *pimd, md_pair_energy_t_x pe, md_stat
   }
   xk::PairPrm prm = pair_params(kind);
   ewald_shifts(prm, sd->geo);
+  if (kind == xk::PAIR_EWALD_REAL && (prm.kmax[0] > 1 || prm.kmax[1] > 1 || prm.kmax[2] > 1))
+    return fail(MD_GB_ERR_UNSUPPORTED, "Ewald alpha*L below %.1f (images beyond the neighbouring boxes)",
+                2 * EWALD_XCUT / 3);
   XMD_CUDA(xk::pair_energy(sd->geo, prm, sd->x.as<double>(), acc, scr, st));
   return 0;
 }
