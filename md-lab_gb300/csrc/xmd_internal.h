@@ -70,7 +70,7 @@ struct PimdDev {
   DevBuf ENk, ENk2, Eint, VBN, tmpV, G;
   DevBuf rec;  // weights of the factorised recursions
   // Ewald reciprocal tables, rebuilt when the parameters change
-  DevBuf rc_coef, rc_cols, rc_phase, rc_S;
+  DevBuf rc_coef, rc_cols, rc_phase, rc_S, rc_T;
   int rc_nsum = -1;
   double rc_alpha = 0, rc_qs = 0, rc_box[3] = {0, 0, 0};
   int rc_nk = 0;

@@ -1285,14 +1285,21 @@ __device__ inline void pair_eval(const PairPrm &p, const Geo &g, const double *d
       }
     }
     double F0 = 0, F1 = 0, F2 = 0, e = 0;
+    // the three candidate components per axis, m - k L for k = -1, 0, 1
+    double c0[3], c1[3], c2[3];
+    if (mask) {
+      c0[0] = mm[0] + g.box[0], c0[1] = mm[0], c0[2] = mm[0] - g.box[0];
+      c1[0] = mm[1] + g.box[1], c1[1] = mm[1], c1[2] = mm[1] - g.box[1];
+      c2[0] = mm[2] + g.box[2], c2[1] = mm[2], c2[2] = mm[2] - g.box[2];
+    }
     while (__any_sync(FULL, mask != 0u)) {
       if (mask) {
         const int c = __ffs(mask) - 1;
         mask &= mask - 1;
-        const int k0 = c / 9 - 1, k1 = (c / 3) % 3 - 1, k2 = c % 3 - 1;
-        const double t0 = fma(-(double)k0, g.box[0], mm[0]);
-        const double t1 = fma(-(double)k1, g.box[1], mm[1]);
-        const double t2 = fma(-(double)k2, g.box[2], mm[2]);
+        const int q0 = c / 9, q1 = (c / 3) % 3, q2 = c % 3;
+        const double t0 = q0 == 0 ? c0[0] : (q0 == 1 ? c0[1] : c0[2]);
+        const double t1 = q1 == 0 ? c1[0] : (q1 == 1 ? c1[1] : c1[2]);
+        const double t2 = q2 == 0 ? c2[0] : (q2 == 1 ? c2[1] : c2[2]);
         const double R2 = fma(t2, t2, fma(t1, t1, t0 * t0));
         if (R2 < rc2) {
           const double rinv = rsqrt(R2);
@@ -1565,96 +1572,143 @@ __device__ inline double2 phase_at(const double2 *ph, const Geo &g, int ns, int 
   return n < 0 ? make_double2(v.x, -v.y) : v;
 }
 
-// S_j(n) for one column (nx, ny) and all its nz: block per (slice, column)
+// Within a column the wave vectors +nz and -nz share cos(nz theta_z) and
+// sin(nz theta_z): exp(i(theta_xy +- nz theta_z)) = e_xy (c +- i s).  Both
+// kernels below work on such pairs, which roughly halves their FP64 work.
+
+// S_j(n) for one column (nx, ny) and all its nz.  One thread per (slice,
+// column) sums over the slice's particles, whose phase factors are staged in
+// shared memory in chunks, so no cross-thread reduction is needed.  With
+// P = sum e_xy c and Q = sum e_xy s:  S(+nz) = P + iQ,  S(-nz) = P - iQ.
+constexpr int SK_THREADS = 64, SK_CHUNK = 64;
+
 template <int NS>
-__global__ void __launch_bounds__(256) k_sk(Geo g, const double2 *__restrict__ ph,
-                                            const int4 *__restrict__ cols,
-                                            double2 *__restrict__ S, int nk) {
-  constexpr int NZ = 2 * NS + 1;
-  __shared__ double red[8][2 * NZ];
+__global__ void __launch_bounds__(SK_THREADS) k_sk(Geo g, const double2 *__restrict__ ph,
+                                                   const int4 *__restrict__ cols, int ncol,
+                                                   double2 *__restrict__ S, int nk) {
+  // staged phases of SK_CHUNK particles: x, y, z factors for n = 0..NS
+  __shared__ double2 sp[3][NS + 1][SK_CHUNK];
   const int j = blockIdx.y;
-  const int4 c = cols[blockIdx.x];  // nx, ny, nz0, off
-  double2 acc[NZ];
+  const int ci = blockIdx.x * SK_THREADS + threadIdx.x;
+  const bool live = ci < ncol;
+  const int4 c = live ? cols[ci] : make_int4(0, 0, 1, 0);
+  const int ax = c.x, ay = c.y < 0 ? -c.y : c.y;
+  const bool cy = c.y < 0;  // conjugate the y factor
+  double s0r = 0, s0i = 0, P[NS][2], Q[NS][2];
 #pragma unroll
-  for (int q = 0; q < NZ; ++q) acc[q] = make_double2(0, 0);
-  for (int l = threadIdx.x; l < g.N; l += blockDim.x) {
-    const double2 exy = cmul(phase_at(ph, g, NS, j, 0, c.x, l), phase_at(ph, g, NS, j, 1, c.y, l));
-    const double2 *pz = ph + (((size_t)j * 3 + 2) * (NS + 1)) * g.Ns + l;
-    double2 ez[NS + 1];
+  for (int n = 0; n < NS; ++n) P[n][0] = P[n][1] = Q[n][0] = Q[n][1] = 0.0;
+  const double2 *base = ph + (size_t)j * 3 * (NS + 1) * g.Ns;
+  for (int l0 = 0; l0 < g.N; l0 += SK_CHUNK) {
+    const int cnt = g.N - l0 < SK_CHUNK ? g.N - l0 : SK_CHUNK;
+    __syncthreads();
+    for (int q = threadIdx.x; q < 3 * (NS + 1) * SK_CHUNK; q += SK_THREADS) {
+      const int l = q % SK_CHUNK, row = q / SK_CHUNK;  // row = d*(NS+1) + n
+      (&sp[0][0][0])[q] = l < cnt ? base[(size_t)row * g.Ns + l0 + l] : make_double2(0.0, 0.0);
+    }
+    __syncthreads();
+    if (!live) continue;
+    for (int l = 0; l < cnt; ++l) {
+      const double2 ex = sp[0][ax][l];
+      double2 ey = sp[1][ay][l];
+      if (cy) ey.y = -ey.y;
+      const double2 exy = cmul(ex, ey);
+      s0r += exy.x;
+      s0i += exy.y;
 #pragma unroll
-    for (int n = 0; n <= NS; ++n) ez[n] = pz[(size_t)n * g.Ns];
-#pragma unroll
-    for (int q = 0; q < NZ; ++q) {
-      const int nz = q - NS;
-      const double2 e = nz < 0 ? make_double2(ez[-nz].x, -ez[-nz].y) : ez[nz];
-      const double2 v = cmul(exy, e);
-      acc[q].x += v.x;
-      acc[q].y += v.y;
+      for (int n = 1; n <= NS; ++n) {
+        const double2 ez = sp[2][n][l];
+        P[n - 1][0] = fma(exy.x, ez.x, P[n - 1][0]);
+        P[n - 1][1] = fma(exy.y, ez.x, P[n - 1][1]);
+        Q[n - 1][0] = fma(exy.x, ez.y, Q[n - 1][0]);
+        Q[n - 1][1] = fma(exy.y, ez.y, Q[n - 1][1]);
+      }
     }
   }
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (!live) return;
+  double2 *o = S + (size_t)j * nk + c.w - c.z;  // o[nz] for nz = c.z..NS
+  if (c.z <= 0) o[0] = make_double2(s0r, s0i);
 #pragma unroll
-  for (int q = 0; q < NZ; ++q) {
-    const double re = warp_sum(acc[q].x), im = warp_sum(acc[q].y);
-    if (lane == 0) {
-      red[w][2 * q] = re;
-      red[w][2 * q + 1] = im;
-    }
-  }
-  __syncthreads();
-  const int nw = blockDim.x >> 5;
-  for (int q = threadIdx.x; q < 2 * NZ; q += blockDim.x) {
-    const int nz = q / 2 - NS;
-    if (nz < c.z) continue;
-    double s = 0;
-    for (int y = 0; y < nw; ++y) s += red[y][q];
-    double *o = (double *)&S[(size_t)j * nk + c.w + (nz - c.z)];
-    o[q & 1] = s;
+  for (int n = 1; n <= NS; ++n) {
+    const double Pr = P[n - 1][0], Pi = P[n - 1][1], Qr = Q[n - 1][0], Qi = Q[n - 1][1];
+    o[n] = make_double2(Pr - Qi, Pi + Qr);
+    if (c.z < 0) o[-n] = make_double2(Pr + Qi, Pi - Qr);
   }
 }
 
-// forces: block per (slice, 128 particles); S and c(n) of the slice staged
-// in shared memory
+// force tables per (slice, column): W(nz) = c(n) conj(S(n)); slot 0 holds
+// W(0), slots 4n-3 .. 4n hold A = W(+n) + W(-n), B = W(+n) - W(-n), n A
+// and n B (W(-n) = 0 where -n is not in the half space: column (0, 0))
+template <int NS>
+__global__ void k_recip_tables(const int4 *__restrict__ cols, int ncol, const double2 *__restrict__ S,
+                               const double *__restrict__ coef, int nk, double2 *__restrict__ T) {
+  constexpr int NT = 4 * NS + 1;
+  const int j = blockIdx.y;
+  const int ci = blockIdx.x * blockDim.y + threadIdx.y;
+  const int n = threadIdx.x;  // 0..NS
+  if (ci >= ncol || n > NS) return;
+  const int4 c = cols[ci];
+  auto W = [&](int nz) {
+    if (nz < c.z) return make_double2(0.0, 0.0);
+    const int k = c.w + (nz - c.z);
+    const double2 s = S[(size_t)j * nk + k];
+    return make_double2(coef[k] * s.x, -coef[k] * s.y);
+  };
+  double2 *o = T + ((size_t)j * ncol + ci) * NT;
+  if (n == 0) {
+    o[0] = W(0);
+  } else {
+    const double2 wp = W(n), wm = W(-n);
+    const double2 A = make_double2(wp.x + wm.x, wp.y + wm.y), B = make_double2(wp.x - wm.x, wp.y - wm.y);
+    o[4 * n - 3] = A;
+    o[4 * n - 2] = B;
+    o[4 * n - 1] = make_double2(n * A.x, n * A.y);
+    o[4 * n] = make_double2(n * B.x, n * B.y);
+  }
+}
+
+// forces: block per (slice, 128 particles), the slice's tables in shared
+// memory.  Per column, with U = sum_nz e_z(nz) W(nz) and V = sum_nz nz e_z W:
+//   sum_nz c(n) Im(e^{i theta} conj S(n)) = Im(e_xy U),   z part Im(e_xy V),
+// where for each pair +-nz:  e_z(+)W(+) + e_z(-)W(-) = c A + i s B  and
+// nz (e_z(+)W(+) - e_z(-)W(-)) = nz (c B + i s A).
 template <int NS>
 __global__ void __launch_bounds__(128) k_recip_force(Geo g, const double2 *__restrict__ ph,
                                                      const int4 *__restrict__ cols, int ncol,
-                                                     const double2 *__restrict__ S,
-                                                     const double *__restrict__ coef, int nk,
-                                                     double scale, double *__restrict__ f) {
+                                                     const double2 *__restrict__ T, double scale,
+                                                     double *__restrict__ f) {
+  constexpr int NT = 4 * NS + 1;
   extern __shared__ double sm[];
-  double2 *sS = (double2 *)sm;
-  double *sc = sm + 2 * nk;
+  double2 *sT = (double2 *)sm;
   const int j = blockIdx.y;
-  for (int k = threadIdx.x; k < nk; k += blockDim.x) {
-    sS[k] = S[(size_t)j * nk + k];
-    sc[k] = coef[k];
-  }
+  const double2 *Tj = T + (size_t)j * ncol * NT;
+  for (int q = threadIdx.x; q < ncol * NT; q += blockDim.x) sT[q] = Tj[q];
   __syncthreads();
   const int l = blockIdx.x * blockDim.x + threadIdx.x;
   if (l >= g.N) return;
   double2 ez[NS + 1];
   const double2 *pz = ph + (((size_t)j * 3 + 2) * (NS + 1)) * g.Ns + l;
 #pragma unroll
-  for (int n = 0; n <= NS; ++n) ez[n] = pz[(size_t)n * g.Ns];
+  for (int n = 1; n <= NS; ++n) ez[n] = pz[(size_t)n * g.Ns];
   double Fx = 0, Fy = 0, Fz = 0;
   for (int ci = 0; ci < ncol; ++ci) {
     const int4 c = cols[ci];
     const double2 exy = cmul(phase_at(ph, g, NS, j, 0, c.x, l), phase_at(ph, g, NS, j, 1, c.y, l));
-    double Tsum = 0, Zsum = 0;
+    const double2 *t = sT + ci * NT;
+    double Ur = t[0].x, Ui = t[0].y, Vr = 0, Vi = 0;
 #pragma unroll
-    for (int q = 0; q < 2 * NS + 1; ++q) {
-      const int nz = q - NS;
-      if (nz < c.z) continue;
-      const double2 e = cmul(exy, nz < 0 ? make_double2(ez[-nz].x, -ez[-nz].y) : ez[nz]);
-      const int k = c.w + (nz - c.z);
-      const double2 s = sS[k];
-      const double wv = sc[k] * (e.y * s.x - e.x * s.y);
-      Tsum += wv;
-      Zsum += nz * wv;
+    for (int n = 1; n <= NS; ++n) {
+      const double2 A = t[4 * n - 3], B = t[4 * n - 2], nA = t[4 * n - 1], nB = t[4 * n];
+      const double cz = ez[n].x, sz = ez[n].y;
+      Ur = fma(cz, A.x, fma(-sz, B.y, Ur));
+      Ui = fma(cz, A.y, fma(sz, B.x, Ui));
+      Vr = fma(cz, nB.x, fma(-sz, nA.y, Vr));
+      Vi = fma(cz, nB.y, fma(sz, nA.x, Vi));
     }
-    Fx += c.x * Tsum;
-    Fy += c.y * Tsum;
-    Fz += Zsum;
+    const double Tm = fma(exy.x, Ui, exy.y * Ur);  // Im(e_xy U)
+    const double Zm = fma(exy.x, Vi, exy.y * Vr);  // Im(e_xy V)
+    Fx = fma((double)c.x, Tm, Fx);
+    Fy = fma((double)c.y, Tm, Fy);
+    Fz += Zm;
   }
   f[sidx(j, 0, l, 3, g.Ns)] += scale * Fx * g.inv_box[0];
   f[sidx(j, 1, l, 3, g.Ns)] += scale * Fy * g.inv_box[1];
@@ -1728,25 +1782,33 @@ static cudaError_t structure_factors(const Geo &g, const Recip &r, const double 
   }
   cudaError_t e = XK_LAUNCHED();
   if (e != cudaSuccess) return e;
-  dim3 grid(ncols(r.nsum), g.P);
-  int thr = ((g.N + 31) / 32) * 32;
-  if (thr > 256) thr = 256;
+  const int nc = ncols(r.nsum);
+  dim3 grid((nc + SK_THREADS - 1) / SK_THREADS, g.P);
   {
     XK_PROF("sk");
-    DISPATCH_NS(r.nsum, k_sk<NS><<<grid, thr, 0, st>>>(g, (const double2 *)r.phase,
-                                                       (const int4 *)r.kvec, (double2 *)r.S, r.nk));
+    DISPATCH_NS(r.nsum, k_sk<NS><<<grid, SK_THREADS, 0, st>>>(g, (const double2 *)r.phase,
+                                                             (const int4 *)r.kvec, nc, (double2 *)r.S, r.nk));
   }
   return XK_LAUNCHED();
 }
+
+size_t recip_table_doubles(const Geo &g, int ns) { return (size_t)g.P * ncols(ns) * (4 * ns + 1) * 2; }
 
 cudaError_t recip_force(const Geo &g, const Recip &r, const double *x, double inv_mP, double *f,
                         cudaStream_t st) {
   if (g.D != 3) return cudaErrorInvalidValue;
   cudaError_t e = structure_factors(g, r, x, st);
   if (e != cudaSuccess) return e;
-  const size_t smem = sizeof(double) * 3 * r.nk;
+  const int nc = ncols(r.nsum);
+  const size_t smem = sizeof(double2) * nc * (4 * r.nsum + 1);
+  dim3 tgrid((nc + 7) / 8, g.P), tblk(r.nsum + 1, 8);
   dim3 grid((g.N + 127) / 128, g.P);
   DISPATCH_NS(r.nsum, {
+    {
+      XK_PROF("recip_tables");
+      k_recip_tables<NS><<<tgrid, tblk, 0, st>>>((const int4 *)r.kvec, nc, (const double2 *)r.S, r.coef,
+                                                 r.nk, (double2 *)r.T);
+    }
     auto kf = k_recip_force<NS>;
     // opt in to the largest dynamic shared memory once per instantiation
     static bool opted = false;
@@ -1757,8 +1819,8 @@ cudaError_t recip_force(const Geo &g, const Recip &r, const double *x, double in
     }
     {
       XK_PROF("recip_force");
-      kf<<<grid, 128, smem, st>>>(g, (const double2 *)r.phase, (const int4 *)r.kvec, ncols(r.nsum),
-                                  (const double2 *)r.S, r.coef, r.nk, 4 * M_PI * inv_mP, f);
+      kf<<<grid, 128, smem, st>>>(g, (const double2 *)r.phase, (const int4 *)r.kvec, nc,
+                                  (const double2 *)r.T, 4 * M_PI * inv_mP, f);
     }
   });
   return XK_LAUNCHED();

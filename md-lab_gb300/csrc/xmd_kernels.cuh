@@ -136,9 +136,11 @@ struct Recip {
   int *kvec;           // column table: int4 (nx, ny, first nz, offset of its first k)
   double *phase;       // [P][3][nsum+1][Ns] complex
   double *S;           // [P][nk] complex
+  double *T;           // [P][columns][2 nsum + 1] complex force tables
 };
 size_t recip_phase_doubles(const Geo &g, int nsum);
 int recip_count(int nsum);
+size_t recip_table_doubles(const Geo &g, int nsum);
 cudaError_t recip_setup(const Geo &g, int nsum, double alpha, double qs, Recip &r,
                         cudaStream_t st);
 cudaError_t recip_force(const Geo &g, const Recip &r, const double *x, double inv_mP,

@@ -321,7 +321,7 @@ int md_pimd_calc_trap_force_x(md_pimd_t_x *pimd, md_trap_force_t_x tf) {
 static int ewald_tables(md_pimd_t_x *pimd, SimDev *sd, PimdDev *pd) {
   const int ns = md_coulomb_n_sum_x;
   const double a = md_coulomb_truc_x, qs = md_coulomb_strength_x;
-  if (ns < 1 || ns > 12) return fail(MD_GB_ERR_UNSUPPORTED, "Ewald n_sum %d (1..12 supported)", ns);
+  if (ns < 1 || ns > 11) return fail(MD_GB_ERR_UNSUPPORTED, "Ewald n_sum %d (1..11 supported)", ns);
   if (!(a > 0)) return fail(MD_GB_ERR_ARG, "Ewald alpha must be positive");
   const xk::Geo &g = sd->geo;
   if (pd->rc_nsum == ns && pd->rc_alpha == a && pd->rc_qs == qs && pd->rc_box[0] == g.box[0] &&
@@ -333,6 +333,7 @@ static int ewald_tables(md_pimd_t_x *pimd, SimDev *sd, PimdDev *pd) {
   XMD_TRY(reserve(pd->rc_cols, sizeof(int) * 4 * (ns * (2 * ns + 1) + ns + 1)));
   XMD_TRY(reserve(pd->rc_phase, sizeof(double) * xk::recip_phase_doubles(g, ns)));
   XMD_TRY(reserve(pd->rc_S, sizeof(double) * 2 * (size_t)nk * g.P));
+  XMD_TRY(reserve(pd->rc_T, sizeof(double) * xk::recip_table_doubles(g, ns)));
   xk::Recip r{};
   r.coef = pd->rc_coef.as<double>();
   r.kvec = pd->rc_cols.as<int>();
@@ -354,6 +355,7 @@ static xk::Recip recip_of(PimdDev *pd) {
   r.kvec = pd->rc_cols.as<int>();
   r.phase = pd->rc_phase.as<double>();
   r.S = pd->rc_S.as<double>();
+  r.T = pd->rc_T.as<double>();
   return r;
 }
 
