@@ -69,6 +69,37 @@ int md_gb300_profile_report_x(char *buf, int len);
    the roofline denominator of the FP64 kernels (-1 on failure) */
 double md_gb300_fp64_peak_x(void);
 
+/* Pair forces for callers that cannot allocate device memory.  No
+   counterpart in MD-Lab.  Every other compute call here allocates its device
+   copies and scratch on first use; some callers cannot allow that: a host
+   application whose own allocator has reserved the GPU's memory up front
+   (a framework's caching allocator, a fixed-footprint service), or a plugin
+   that must not change the process's device-memory footprint.  This call
+   takes the caller's device buffers and stream and allocates nothing: the
+   per-tile partial sums use a fixed 4 MiB array inside the library, which
+   every GPU that loads the library keeps until the process exits.
+
+   pf     md_gaussian_force_x, md_periodic_gaussian_force_x,
+          md_coulomb_force_x or md_coulomb_periodic_force_x (parameters from
+          the usual globals); Ewald is not available here
+   x, m   device arrays, bead slices major: x[(j*D + d)*ld + l], m[j*ld + l]
+          for particle l < N, bead j < P, dimension d < D
+   f      device array laid out like x; receives += the pair forces of each
+          bead slice with the reference's convention (F/(m P), m of the
+          higher-index particle; md_pimd_x.c:1650-1675)
+   ld     leading dimension, ld >= N
+   L      host array of D box lengths (needed by the periodic kinds)
+   stream cudaStream_t to run on (NULL: the legacy default stream)
+
+   Limit: ceil(N/32) * P * D * ld <= 524288 doubles (for example N = 256,
+   P = 64 in 3D); larger configurations are refused with MD_GB_ERR_ARG.
+   The first call on each device looks up the array's device address with
+   that device current.  All calls share the array, so calls that overlap
+   on the GPU (different streams, or several host threads) race; nothing in
+   the array needs clearing between calls. */
+int md_gb300_pair_force_noalloc_x(md_pair_force_t_x pf, const double *x, const double *m, double *f, int N, int P,
+                                  int ld, const double *L, void *stream);
+
 /* release the device copies (and, for *_free_*, the host structs) */
 int md_gb300_release_simulation_x(md_simulation_t_x *sim);
 void md_gb300_free_simulation_x(md_simulation_t_x *sim);

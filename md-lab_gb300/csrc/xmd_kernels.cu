@@ -16,6 +16,7 @@
 #include <atomic>
 #include <cmath>
 #include <cstdio>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -1985,6 +1986,82 @@ double fp64_peak_tflops(cudaStream_t st) {
   cudaFreeAsync(out, st);
   cudaStreamSynchronize(st);
   return cudaGetLastError() == cudaSuccess ? best : -1;
+}
+
+}  // namespace xk
+
+namespace xk {
+
+// ===================================================================
+// Pair forces without any allocation (md_gb300_pair_force_noalloc_x).
+//
+// For callers that may not allocate device memory, the per-tile partial
+// forces of k_pair_tiles go to this fixed array instead of a buffer from
+// the allocator.  It lives in every GPU that loads the library, until the
+// process exits.  k_pair_tiles writes every element that k_pair_finish reads,
+// so nothing in it has to start at zero; concurrent calls share it and
+// therefore must not overlap on the GPU.
+// ===================================================================
+static __device__ __align__(256) double g_noalloc_scratch[NOALLOC_SCRATCH_DOUBLES];
+
+constexpr int NOALLOC_MAX_DEVICES = 64;
+static double *g_noalloc_addr[NOALLOC_MAX_DEVICES];
+static std::mutex g_noalloc_mu;
+
+size_t pair_force_noalloc_need(const Geo &g) {
+  const int T = (g.N + 31) / 32;
+  return (size_t)T * g.slots();
+}
+
+cudaError_t pair_force_noalloc(const Geo &g, const PairPrm &p, const double *x, const double *m,
+                               double *f, cudaStream_t st) {
+  if (p.kind == PAIR_EWALD_REAL) return cudaErrorNotSupported;
+  if (pair_force_noalloc_need(g) > NOALLOC_SCRATCH_DOUBLES) return cudaErrorInvalidValue;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) return cudaErrorInvalidDevice;
+  double *scratch;
+  {
+    // set-up, once per device, with that device current: the array's
+    // device address (its host-side name is not a device pointer)
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+      void *a = nullptr;
+      e = cudaGetSymbolAddress(&a, g_noalloc_scratch);
+      if (e != cudaSuccess) return e;
+      g_noalloc_addr[dev] = (double *)a;
+    }
+    scratch = g_noalloc_addr[dev];
+  }
+  const int T = (g.N + 31) / 32;
+  const int jobs = T * (T + 1) / 2;
+  const int nb = cdiv((size_t)jobs * g.P * 32, 256);
+  switch (g.D * 16 + p.kind) {
+#define XK_NOALLOC_CASE(DV, K)                                                                   \
+  case DV * 16 + K:                                                                              \
+    k_pair_tiles<DV, K, false><<<nb, 256, 0, st>>>(g, p, x, m, scratch, T, jobs);                \
+    break;
+    XK_NOALLOC_CASE(1, PAIR_GAUSSIAN)
+    XK_NOALLOC_CASE(1, PAIR_PERIODIC_GAUSSIAN)
+    XK_NOALLOC_CASE(1, PAIR_COULOMB)
+    XK_NOALLOC_CASE(1, PAIR_PERIODIC_COULOMB)
+    XK_NOALLOC_CASE(2, PAIR_GAUSSIAN)
+    XK_NOALLOC_CASE(2, PAIR_PERIODIC_GAUSSIAN)
+    XK_NOALLOC_CASE(2, PAIR_COULOMB)
+    XK_NOALLOC_CASE(2, PAIR_PERIODIC_COULOMB)
+    XK_NOALLOC_CASE(3, PAIR_GAUSSIAN)
+    XK_NOALLOC_CASE(3, PAIR_PERIODIC_GAUSSIAN)
+    XK_NOALLOC_CASE(3, PAIR_COULOMB)
+    XK_NOALLOC_CASE(3, PAIR_PERIODIC_COULOMB)
+#undef XK_NOALLOC_CASE
+    default:
+      return cudaErrorNotSupported;
+  }
+  e = XK_LAUNCHED();
+  if (e != cudaSuccess) return e;
+  k_pair_finish<<<cdiv(g.slots(), 256), 256, 0, st>>>(g, scratch, T, 1.0 / g.P, f);
+  return XK_LAUNCHED();
 }
 
 }  // namespace xk

@@ -128,6 +128,15 @@ cudaError_t pair_force(const Geo &g, const PairPrm &p, const double *x, const do
 cudaError_t pair_energy(const Geo &g, const PairPrm &p, const double *x, double *acc,
                         double *scratch, cudaStream_t st);
 
+// Pair forces (not Ewald) with the per-tile partials in a fixed array of
+// NOALLOC_SCRATCH_DOUBLES doubles inside the library (4 MiB): no allocation.
+// Returns cudaErrorInvalidValue when the configuration needs more than that
+// (pair_force_noalloc_need), cudaErrorNotSupported for Ewald.
+constexpr size_t NOALLOC_SCRATCH_DOUBLES = (size_t)1 << 19;
+size_t pair_force_noalloc_need(const Geo &g);
+cudaError_t pair_force_noalloc(const Geo &g, const PairPrm &p, const double *x, const double *m,
+                               double *f, cudaStream_t st);
+
 // Ewald reciprocal space through structure factors (D = 3)
 struct Recip {
   int nsum;

@@ -409,6 +409,43 @@ int md_pimd_calc_pair_force_x(md_pimd_t_x *pimd, md_pair_force_t_x pf) {
   return 0;
 }
 
+// Pair forces for callers that cannot allocate device memory (md_gb300_x.h).
+// Everything here works on the caller's device pointers and stream; the
+// per-tile partial sums go to a fixed array inside the library.  This
+// function calls no allocator: not cudaMalloc, not the stream-ordered
+// allocator, and it creates no stream or event.
+int md_gb300_pair_force_noalloc_x(md_pair_force_t_x pf, const double *x, const double *m, double *f, int N, int P,
+                                  int ld, const double *L, void *stream) {
+  const int kind = pair_kind_of((const void *)pf, false);
+  if (!kind || kind == xk::PAIR_EWALD_REAL)
+    return fail(MD_GB_ERR_UNSUPPORTED, "no-allocation pair forces: Gaussian and Coulomb kinds only");
+  if (!x || !m || !f || N < 1 || P < 1 || ld < N)
+    return fail(MD_GB_ERR_ARG, "no-allocation pair forces: invalid pointers or sizes (N=%d P=%d ld=%d)", N, P, ld);
+  const bool periodic = kind == xk::PAIR_PERIODIC_GAUSSIAN || kind == xk::PAIR_PERIODIC_COULOMB;
+  if (periodic && !L) return fail(MD_GB_ERR_ARG, "no-allocation pair forces: periodic kind needs the box");
+  if (!device_present()) return fail(MD_GB_ERR_NO_DEVICE, "no CUDA device is available");
+  xk::Geo g{};
+  g.D = D;
+  g.N = N;
+  g.P = P;
+  g.Ns = ld;
+  for (int d = 0; d < 3; ++d) {
+    g.box[d] = (L && d < D) ? L[d] : 0.0;
+    g.inv_box[d] = g.box[d] > 0 ? 1.0 / g.box[d] : 0.0;
+  }
+  if (periodic)
+    for (int d = 0; d < D; ++d)
+      if (!(g.box[d] > 0)) return fail(MD_GB_ERR_ARG, "no-allocation pair forces: box lengths must be positive");
+  const size_t need = xk::pair_force_noalloc_need(g);
+  if (need > xk::NOALLOC_SCRATCH_DOUBLES)
+    return fail(MD_GB_ERR_ARG,
+                "no-allocation pair forces: N=%d, P=%d, ld=%d needs %zu doubles of scratch, more than the fixed %zu "
+                "(ceil(N/32) * P * D * ld must not exceed it)",
+                N, P, ld, need, (size_t)xk::NOALLOC_SCRATCH_DOUBLES);
+  XMD_CUDA(xk::pair_force_noalloc(g, pair_params(kind), x, m, f, (cudaStream_t)stream));
+  return 0;
+}
+
 // ------------------------------------------------------------------
 // estimators: md_pimd_x.c:1111-1295, :1393-1525, :1679-1824,
 // :3989-4056, :4072-4348, :4423-4556
