@@ -191,18 +191,21 @@ def cpu_step_estimate(cores, budget_s):
 # ---------------------------------------------------------------------
 # GB300 arm
 # ---------------------------------------------------------------------
-# algorithmic FP64 work per launch of each kernel
+# algorithmic FP64 work per launch of each kernel, FMA = 2 flops (the design doc
+# section 4 derives each count from the kernel's arithmetic)
 def kernel_flops(name, launches_per_step):
-    nk = ((2 * NSUM + 1) ** 3 - 1) // 2
+    ncol = NSUM * (2 * NSUM + 1) + NSUM + 1  # wave-vector columns (nx, ny)
     if name == "recip_force":
-        return 11.0 * nk * N * P
+        return 177.0 * ncol * N * P
     if name == "sk":
-        return 8.0 * nk * N * P
+        return 88.0 * ncol * N * P
     if name == "pair_tiles_ewald_real":
         box, _ = workload()
         rc = 5.8 / (ALPHA_L / box)
+        # expected images inside the cut-off per pair: (4/3) pi rc^3 / V
         n_img = 4 / 3 * math.pi * rc ** 3 / box ** 3
-        return 24.0 * n_img * P * N * (N - 1) / 2
+        pairs = P * N * (N - 1) / 2
+        return pairs * (47.0 * n_img + 39.0)
     return None
 
 

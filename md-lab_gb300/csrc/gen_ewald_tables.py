@@ -4,10 +4,11 @@ Ewald kernel, so that the GPU evaluates no FP64 erfc/exp per image.
     h(x) = erfc(x) + 2 x exp(-x^2) / sqrt(pi)    force:  F = s h(alpha R) r / R^3
     e(x) = erfc(x)                               energy: E = s e(alpha R) / R
 
-(h'(x) = -4 x^2 exp(-x^2)/sqrt(pi).)  On each interval [i w, (i+1) w] of
-[0, XMAX] a degree-DEG polynomial in t = 2 (x - centre)/w is the Chebyshev
-interpolant computed with 40-digit arithmetic (mpmath), stored in monomial
-form for Horner evaluation.  The script measures the absolute error of the
+(h'(x) = -4 x^2 exp(-x^2)/sqrt(pi).)  Interval i = 0..NINT-1 is centred at
+i w, [(i - 1/2) w, (i + 1/2) w], so that the kernel finds it by rounding x/w
+to the nearest integer; on it a degree-DEG polynomial in t = 2 (x - i w)/w is
+the Chebyshev interpolant computed with 40-digit arithmetic (mpmath), stored
+in monomial form for Horner evaluation.  The script measures the absolute error of the
 double-precision Horner evaluation against mpmath and records it in the
 header.  Absolute accuracy is what the sums need: both functions are at most
 1 and each image's contribution scales with them.
@@ -17,8 +18,8 @@ Run:  python gen_ewald_tables.py > xmd_ewald_tables.h   (needs mpmath)
 import mpmath as mp
 
 mp.mp.dps = 40
-XMAX, NINT, DEG = 6.0, 24, 12
-W = XMAX / NINT
+W, NINT, DEG = 0.25, 25, 12
+XMAX = (NINT - 0.5) * W
 
 
 def h(x):
@@ -48,7 +49,7 @@ def horner(cd, t):
 def table(f):
     rows, worst = [], 0.0
     for i in range(NINT):
-        a, b = mp.mpf(i) * W, mp.mpf(i + 1) * W
+        a, b = (mp.mpf(i) - mp.mpf(1) / 2) * W, (mp.mpf(i) + mp.mpf(1) / 2) * W
         cd = [float(c) for c in interpolant(f, a, b, DEG)]
         for s in range(401):
             t = -1 + 2 * mp.mpf(s) / 400
@@ -72,8 +73,8 @@ if __name__ == "__main__":
     te, ee = table(e)
     print(f"""// xmd_ewald_tables.h -- generated by gen_ewald_tables.py; do not edit.
 //
-// Piecewise polynomials on [0, {XMAX}] ({NINT} intervals of width {W}, degree
-// {DEG}, variable t = 2 (x - centre)/w in [-1, 1]) for
+// Piecewise polynomials on [0, {XMAX}] ({NINT} intervals of width {W} centred
+// at i w, degree {DEG}, variable t = 2 (x - i w)/w in [-1, 1]) for
 //   EW_H:    erfc(x) + 2 x exp(-x^2)/sqrt(pi)   max |error| {eh:.2e}
 //   EW_ERFC: erfc(x)                            max |error| {ee:.2e}
 // (errors of the double-precision Horner evaluation against 40-digit values

@@ -1222,9 +1222,19 @@ __constant__ double c_ew_erfc[EW_NINT][EW_DEG + 1] = EW_ERFC_INIT;
 // Force F(dx) (times the pair's strength, before the 1/m and 1/P factors)
 // and, with want_e, the pair energy.  The Ewald kind is warp-collective: all
 // lanes call it, `active` says whether the lane's pair counts.
+// per-warp queue of accepted Ewald images (shared memory)
+constexpr int EW_TAKE = 4;  // images per lane per batch
+struct EwWarp {
+  double cm[32][9];          // each lane's candidate components m_d - k L_d
+  double val[32 * EW_TAKE];  // evaluated factor per queue item
+  unsigned take[32];         // each lane's images in this batch (bit = k code)
+  int base[32];              // first queue item of each lane
+};
+
 template <int D, int KIND, bool ENERGY_TAB>
-__device__ inline void pair_eval(const PairPrm &p, const Geo &g, const double *dx, double *F,
-                                 double &E, bool want_e, const double *tabs, bool active) {
+__device__ inline void pair_eval(const PairPrm &p, const Geo &g, const double *dx, const float *dxf,
+                                 double *F, double &E, bool want_e, const double *tabs, bool active,
+                                 EwWarp *ws, int lane) {
   if (KIND == PAIR_GAUSSIAN || KIND == PAIR_PERIODIC_GAUSSIAN) {
     double t[D], r2 = 0;
 #pragma unroll
@@ -1255,27 +1265,34 @@ __device__ inline void pair_eval(const PairPrm &p, const Geo &g, const double *d
     // Real-space images of the partner inside the reference's cube
     // |n_i| <= nsum (md_simulation_x.c:281-292) whose distance is below
     // rcut.  dx is first reduced to its minimum image m = dx - s L, so the
-    // candidates are n = s + k with |k_d| <= kmax.  The candidates are culled
+    // candidates are n = s + k with |k_d| <= 1.  The candidates are culled
     // on the FP32 pipe into a bit mask (with a 1e-4 margin; the FP64 test
     // below decides), then evaluated in warp-wide rounds, one accepted image
     // per lane per round, so that the FP64 pipe runs with full warps.  Per
     // image the factor (erfc(x) + 2x exp(-x^2)/sqrt(pi)) / R^3, x = alpha R,
     // comes from the piecewise polynomial EW_H (no FP64 erfc or exp), 1/R
-    // from rsqrt.
+    // from rsqrt.  On this GPU FP64 comparisons and int <-> double
+    // conversions share the slow FP64 pipe, so rounding to integers uses
+    // the 1.5 * 2^52 addition and the cut-off test compares bit patterns.
+    constexpr double MAGIC = 6755399441055744.0;  // 1.5 * 2^52
     const double *tab = ENERGY_TAB ? tabs + EW_NINT * (EW_DEG + 1) : tabs;
     const double rc2 = p.rcut * p.rcut;
+    const long long rc2_bits = __double_as_longlong(rc2);
     double mm[3];
     int sh[3];
     unsigned mask = 0u;
     if (active) {
 #pragma unroll
       for (int d = 0; d < 3; ++d) {
-        sh[d] = (int)rint(dx[d] * g.inv_box[d]);
-        mm[d] = fma(-(double)sh[d], g.box[d], dx[d]);
+        const double tq = fma(dx[d], g.inv_box[d], MAGIC);  // MAGIC + rint(dx/L)
+        sh[d] = __double2loint(tq);
+        mm[d] = fma(-(tq - MAGIC), g.box[d], dx[d]);
       }
       const float rc2f = (float)(rc2 * 1.0001);
-      const float m0 = (float)mm[0], m1 = (float)mm[1], m2 = (float)mm[2];
       const float L0 = (float)g.box[0], L1 = (float)g.box[1], L2 = (float)g.box[2];
+      const float m0 = fmaf(-(float)sh[0], L0, dxf[0]);
+      const float m1 = fmaf(-(float)sh[1], L1, dxf[1]);
+      const float m2 = fmaf(-(float)sh[2], L2, dxf[2]);
 #pragma unroll
       for (int c = 0; c < 27; ++c) {
         const int k0 = c / 9 - 1, k1 = (c / 3) % 3 - 1, k2 = c % 3 - 1;
@@ -1287,41 +1304,87 @@ __device__ inline void pair_eval(const PairPrm &p, const Geo &g, const double *d
     }
     double F0 = 0, F1 = 0, F2 = 0, e = 0;
     // the three candidate components per axis, m - k L for k = -1, 0, 1
-    double c0[3], c1[3], c2[3];
+    double cm[9];
     if (mask) {
-      c0[0] = mm[0] + g.box[0], c0[1] = mm[0], c0[2] = mm[0] - g.box[0];
-      c1[0] = mm[1] + g.box[1], c1[1] = mm[1], c1[2] = mm[1] - g.box[1];
-      c2[0] = mm[2] + g.box[2], c2[1] = mm[2], c2[2] = mm[2] - g.box[2];
+      cm[0] = mm[0] + g.box[0], cm[1] = mm[0], cm[2] = mm[0] - g.box[0];
+      cm[3] = mm[1] + g.box[1], cm[4] = mm[1], cm[5] = mm[1] - g.box[1];
+      cm[6] = mm[2] + g.box[2], cm[7] = mm[2], cm[8] = mm[2] - g.box[2];
+#pragma unroll
+      for (int q = 0; q < 9; ++q) ws->cm[lane][q] = cm[q];
     }
-    while (__any_sync(FULL, mask != 0u)) {
-      if (mask) {
-        const int c = __ffs(mask) - 1;
-        mask &= mask - 1;
+    // Accepted images are evaluated as one queue per warp: batches of up to
+    // four images per lane, every lane evaluating consecutive queue items, so
+    // that the FP64 pipe runs with (nearly) full warps whatever the number of
+    // images of each lane's pair.  The owner lane then accumulates its own.
+    unsigned rem = mask;
+    while (__any_sync(FULL, rem != 0u)) {
+      unsigned take = 0u, t = rem;
+#pragma unroll
+      for (int i = 0; i < EW_TAKE; ++i) {
+        const unsigned b = t & (0u - t);
+        take |= b;
+        t ^= b;
+      }
+      rem ^= take;
+      const int cnt = __popc(take);
+      int incl = cnt;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(FULL, incl, o);
+        if (lane >= o) incl += v;
+      }
+      const int base = incl - cnt, total = __shfl_sync(FULL, incl, 31);
+      ws->take[lane] = take;
+      ws->base[lane] = base;
+      __syncwarp();
+      for (int round = 0; round < total; round += 32) {
+        const int q = round + lane;
+        if (q >= total) continue;
+        int o = 0;
+#pragma unroll
+        for (int st = 16; st; st >>= 1)
+          if (ws->base[o + st] <= q) o += st;
+        unsigned b = ws->take[o];
+        for (int r = q - ws->base[o]; r > 0; --r) b &= b - 1;
+        const int c = __ffs(b) - 1;
         const int q0 = c / 9, q1 = (c / 3) % 3, q2 = c % 3;
-        const double t0 = q0 == 0 ? c0[0] : (q0 == 1 ? c0[1] : c0[2]);
-        const double t1 = q1 == 0 ? c1[0] : (q1 == 1 ? c1[1] : c1[2]);
-        const double t2 = q2 == 0 ? c2[0] : (q2 == 1 ? c2[1] : c2[2]);
+        const double t0 = ws->cm[o][q0], t1 = ws->cm[o][3 + q1], t2 = ws->cm[o][6 + q2];
         const double R2 = fma(t2, t2, fma(t1, t1, t0 * t0));
-        if (R2 < rc2) {
+        double val = 0.0;
+        if (__double_as_longlong(R2) < rc2_bits) {
           const double rinv = rsqrt(R2);
           const double xr = p.alpha * (R2 * rinv);
-          int iv = (int)(xr * EW_INV_W);
+          const double tq = fma(xr, EW_INV_W, MAGIC);  // MAGIC + rint(x/w): interval index
+          int iv = __double2loint(tq);
           iv = iv < EW_NINT - 1 ? iv : EW_NINT - 1;
-          const double u = fma(xr, 2 * EW_INV_W, -(double)(2 * iv + 1));
+          const double u = fma(xr, 2 * EW_INV_W, fma(-2.0, tq, 2 * MAGIC));  // 2 (x/w - iv)
           const double *cf = tab + iv * (EW_DEG + 1);
           double hv = cf[EW_DEG];
 #pragma unroll
-          for (int q = EW_DEG - 1; q >= 0; --q) hv = fma(hv, u, cf[q]);
-          if (ENERGY_TAB) {
-            e = fma(hv, rinv, e);
-          } else {
-            const double mult = hv * (rinv * rinv * rinv);
-            F0 = fma(t0, mult, F0);
-            F1 = fma(t1, mult, F1);
-            F2 = fma(t2, mult, F2);
-          }
+          for (int qq = EW_DEG - 1; qq >= 0; --qq) hv = fma(hv, u, cf[qq]);
+          val = ENERGY_TAB ? hv * rinv : hv * (rinv * rinv * rinv);
+        }
+        ws->val[q] = val;
+      }
+      __syncwarp();
+      unsigned b = take;
+      for (int i = 0; i < cnt; ++i) {
+        const int c = __ffs(b) - 1;
+        b &= b - 1;
+        const double val = ws->val[base + i];
+        if (ENERGY_TAB) {
+          e += val;
+        } else {
+          const int q0 = c / 9, q1 = (c / 3) % 3, q2 = c % 3;
+          const double t0 = q0 == 0 ? cm[0] : (q0 == 1 ? cm[1] : cm[2]);
+          const double t1 = q1 == 0 ? cm[3] : (q1 == 1 ? cm[4] : cm[5]);
+          const double t2 = q2 == 0 ? cm[6] : (q2 == 1 ? cm[7] : cm[8]);
+          F0 = fma(t0, val, F0);
+          F1 = fma(t1, val, F1);
+          F2 = fma(t2, val, F2);
         }
       }
+      __syncwarp();
     }
     F[0] = p.qs * F0;
     if (D > 1) F[1] = p.qs * F1;
@@ -1342,6 +1405,8 @@ __global__ void __launch_bounds__(256, 1) k_pair_tiles(Geo g, PairPrm p,
       stab[i] = i < EW_NINT * (EW_DEG + 1) ? (&c_ew_h[0][0])[i] : (&c_ew_erfc[0][0])[i - EW_NINT * (EW_DEG + 1)];
     __syncthreads();
   }
+  __shared__ EwWarp ewq[KIND == PAIR_EWALD_REAL ? 8 : 1];
+  EwWarp *ews = &ewq[KIND == PAIR_EWALD_REAL ? (threadIdx.x >> 5) : 0];
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (warp >= jobs * g.P) return;
@@ -1355,32 +1420,39 @@ __global__ void __launch_bounds__(256, 1) k_pair_tiles(Geo g, PairPrm p,
   const int a = I * 32 + lane, b0 = J * 32 + lane;
   const bool va = a < g.N, vb = b0 < g.N;
   double xa[D], xb[D], fa[D], fb[D];
+  float xaf[D], xbf[D];  // FP32 copies for the Ewald image culling
 #pragma unroll
   for (int d = 0; d < D; ++d) {
     xa[d] = va ? x[sidx(j, d, a, D, g.Ns)] : 0.0;
     xb[d] = vb ? x[sidx(j, d, b0, D, g.Ns)] : 0.0;
+    xaf[d] = (float)xa[d];
+    xbf[d] = (float)xb[d];
     fa[d] = fb[d] = 0.0;
   }
-  const double ma = va ? m[(size_t)j * g.Ns + a] : 1.0;
-  double mb = vb ? m[(size_t)j * g.Ns + b0] : 1.0;
+  // inverse masses, so that each pair multiplies instead of dividing
+  const double ima = (!ENERGY && va) ? 1.0 / m[(size_t)j * g.Ns + a] : 1.0;
+  double imb = (!ENERGY && vb) ? 1.0 / m[(size_t)j * g.Ns + b0] : 1.0;
   double ea = 0;
   for (int s = 0; s < 32; ++s) {
     const int bi = J * 32 + ((lane + s) & 31);
     const bool act = va && bi < g.N && (I != J || a > bi);
     double dx[D], F[D], E = 0;
+    float dxf[D];
 #pragma unroll
     for (int d = 0; d < D; ++d) {
       dx[d] = xa[d] - xb[d];
+      dxf[d] = xaf[d] - xbf[d];
       F[d] = 0;
     }
-    if (KIND == PAIR_EWALD_REAL) pair_eval<D, KIND, ENERGY>(p, g, dx, F, E, ENERGY, stab, act);
+    if (KIND == PAIR_EWALD_REAL) pair_eval<D, KIND, ENERGY>(p, g, dx, dxf, F, E, ENERGY, stab, act, ews, lane);
     if (act) {
-      if (KIND != PAIR_EWALD_REAL) pair_eval<D, KIND, ENERGY>(p, g, dx, F, E, ENERGY, stab, true);
+      if (KIND != PAIR_EWALD_REAL)
+        pair_eval<D, KIND, ENERGY>(p, g, dx, dxf, F, E, ENERGY, stab, true, nullptr, lane);
       if (ENERGY) {
         ea += E;
       } else {
         // the reference divides by the mass of the higher-index particle
-        const double inv = 1.0 / (a > bi ? ma : mb);
+        const double inv = a > bi ? ima : imb;
 #pragma unroll
         for (int d = 0; d < D; ++d) {
           fa[d] += F[d] * inv;
@@ -1392,9 +1464,10 @@ __global__ void __launch_bounds__(256, 1) k_pair_tiles(Geo g, PairPrm p,
 #pragma unroll
     for (int d = 0; d < D; ++d) {
       xb[d] = __shfl_sync(FULL, xb[d], src);
+      if (KIND == PAIR_EWALD_REAL) xbf[d] = __shfl_sync(FULL, xbf[d], src);
       if (!ENERGY) fb[d] = __shfl_sync(FULL, fb[d], src);
     }
-    mb = __shfl_sync(FULL, mb, src);
+    if (!ENERGY) imb = __shfl_sync(FULL, imb, src);
   }
   if (ENERGY) {
     ea = warp_sum(ea);
