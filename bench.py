@@ -238,36 +238,56 @@ def run_gb300(args, dist, rank, ws):
     for _ in range(args.warmup):
         step()
     lib.check(lib.md_gb300_synchronize_x(), "sync")
-    # one step as a CUDA graph
-    g = C.c_void_p()
-    lib.check(lib.md_gb300_capture_begin_x(), "capture begin")
-    step()
-    lib.check(lib.md_gb300_capture_end_x(C.byref(g)), "capture end")
-    kernels_per_step = lib.md_gb300_graph_kernel_count_x(g)
     stream = torch.cuda.ExternalStream(lib.md_gb300_get_stream_x())
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
-    for _ in range(max(3, args.warmup)):
-        lib.check(lib.md_gb300_graph_launch_x(g, 1))
-    lib.check(lib.md_gb300_synchronize_x())
-    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-           for _ in range(args.steps)]
-    barrier(dist)
-    torch.cuda.synchronize()
-    with Clocks(dev) as clk:
-        t0 = time.perf_counter()
-        with torch.cuda.stream(stream):
-            for e0, e1 in evs:
-                flush.zero_()
-                e0.record(stream)
-                lib.check(lib.md_gb300_graph_launch_x(g, 1))
-                e1.record(stream)
+
+    def timed_graph(nsteps):
+        """capture one step, replay it; per-step CUDA events, L2 flushed in between"""
+        g = C.c_void_p()
+        lib.check(lib.md_gb300_capture_begin_x(), "capture begin")
+        step()
+        lib.check(lib.md_gb300_capture_end_x(C.byref(g)), "capture end")
+        kps = lib.md_gb300_graph_kernel_count_x(g)
+        for _ in range(max(3, args.warmup)):
+            lib.check(lib.md_gb300_graph_launch_x(g, 1))
         lib.check(lib.md_gb300_synchronize_x())
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(nsteps)]
+        barrier(dist)
         torch.cuda.synchronize()
-        wall = time.perf_counter() - t0
-    barrier(dist)
-    step_ms = sum(a.elapsed_time(b) for a, b in evs) / args.steps
-    step_ms = max_over_ranks(dist, step_ms)
+        with Clocks(dev) as clk:
+            t0 = time.perf_counter()
+            with torch.cuda.stream(stream):
+                for e0, e1 in evs:
+                    flush.zero_()
+                    e0.record(stream)
+                    lib.check(lib.md_gb300_graph_launch_x(g, 1))
+                    e1.record(stream)
+            lib.check(lib.md_gb300_synchronize_x())
+            torch.cuda.synchronize()
+            wall = time.perf_counter() - t0
+        barrier(dist)
+        lib.md_gb300_graph_free_x(g)
+        ms = sum(a.elapsed_time(b) for a, b in evs) / nsteps
+        return max_over_ranks(dist, ms), kps, wall, clk.summary()
+
+    step_ms, kernels_per_step, wall, clocks = timed_graph(args.steps)
     value = ws * N * P / (step_ms * 1e-3)
+    # the mixed-precision form on the same state: time and force error
+    forms = {"plain_fp64": {"value": value, "ms_per_step": step_ms}}
+    if not args.no_mixed:
+        def forces(mode):
+            lib.check(lib.md_gb300_set_precision_x(mode))
+            lib.check(lib.md_reset_force_x(s.sim))
+            lib.check(lib.md_pimd_calc_pair_force_x(s.pimd, pair))
+            return s.state()["f"]
+        import numpy as np
+        f64, f32 = forces(0), forces(1)
+        ferr = float(np.max(np.abs(f32 - f64)) / np.max(np.abs(f64)))
+        mixed_ms, _, _, mixed_clocks = timed_graph(args.steps)
+        lib.check(lib.md_gb300_set_precision_x(0))
+        forms["mixed_fp32_forces"] = {"value": ws * N * P / (mixed_ms * 1e-3), "ms_per_step": mixed_ms,
+                                      "force_error_vs_fp64": ferr, "clocks": mixed_clocks}
     # live per-kernel timing of two plain steps (outside the timed region)
     lib.check(lib.md_gb300_profile_x(1))
     for _ in range(2):
@@ -311,17 +331,16 @@ def run_gb300(args, dist, rank, ws):
               "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
               "data": "synthetic (seeded uniform electron-gas configuration from the library's own "
                       "initial-condition routines)",
-              "config": config("plain FP64"), "gpu_launches": launches,
+              "config": config("plain FP64"), "gpu_launches": launches, "forms": forms,
               "kernels_per_step": kernels_per_step, "wall_s_timed": wall,
               "e2e": {"value": ws * N * P / e2e_s, "unit": "bead-steps/s", "h2d_bytes_per_step": h2d,
                       "d2h_bytes_per_step": h2d + 8, "steps": ke},
               "roofline": roof, "kernel_ms_per_step": {k: v[0] / 2 for k, v in prof.items()},
-              "clocks": clk.summary()}
+              "clocks": clocks}
     if rank == 0 and ws == 1 and not args.no_cpu:
         st, sample = cpu_step_estimate(1, args.cpu_budget)
         result["cpu_baseline"] = {"value": N * P / st, "unit": "bead-steps/s", "cores": 1,
                                   "kind": "port", "sample": sample}
-    lib.md_gb300_graph_free_x(g)
     s.free()
     return result
 
@@ -354,6 +373,7 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--cpu-budget", type=float, default=8.0, help="seconds of CPU sample")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision form")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":

@@ -100,6 +100,18 @@ double md_gb300_fp64_peak_x(void);
 int md_gb300_pair_force_noalloc_x(md_pair_force_t_x pf, const double *x, const double *m, double *f, int N, int P,
                                   int ld, const double *L, void *stream);
 
+/* Arithmetic of the pair forces (md_pimd_calc_pair_force_x), including
+   both Ewald parts.  MD_GB_PRECISION_FP64 (default) reproduces MD-Lab to
+   1e-10.  MD_GB_PRECISION_MIXED evaluates pair and real-space Ewald forces in
+   FP32 with compensated (Kahan) accumulation and the reciprocal sum with FP32
+   phase products accumulated in double-float; positions, the exchange
+   recursion, springs, the thermostat and every estimator stay FP64.  The
+   force error against the FP64 form is about 1e-6 of the force scale. */
+#define MD_GB_PRECISION_FP64 0
+#define MD_GB_PRECISION_MIXED 1
+int md_gb300_set_precision_x(int mode);
+int md_gb300_get_precision_x(void);
+
 /* release the device copies (and, for *_free_*, the host structs) */
 int md_gb300_release_simulation_x(md_simulation_t_x *sim);
 void md_gb300_free_simulation_x(md_simulation_t_x *sim);

@@ -2138,3 +2138,423 @@ cudaError_t pair_force_noalloc(const Geo &g, const PairPrm &p, const double *x, 
 }
 
 }  // namespace xk
+
+namespace xk {
+
+// ===================================================================
+// Mixed-precision form: pair and real-space Ewald forces in FP32 with
+// compensated (Kahan) accumulation of every force sum; reciprocal space
+// with FP32 phase products accumulated in double-float (an unevaluated sum
+// of two FP32 numbers, ~48 significant bits).  Positions, the phases
+// themselves and every estimator stay FP64; partial sums leave the FP32
+// kernels as doubles.
+// ===================================================================
+
+struct Kahan {
+  float s = 0.f, c = 0.f;
+  __device__ inline void add(float v) {
+    const float y = v - c;
+    const float t = s + y;
+    c = (t - s) - y;
+    s = t;
+  }
+  __device__ inline double value() const { return (double)s - (double)c; }
+};
+
+// double-float accumulator: hi + lo with error-free TwoSum per addition
+struct DF {
+  float hi = 0.f, lo = 0.f;
+  __device__ inline void add(float v) {
+    const float s = hi + v;
+    const float bp = s - hi;
+    const float e = (hi - (s - bp)) + (v - bp);
+    hi = s;
+    lo += e;
+  }
+  __device__ inline double value() const { return (double)hi + (double)lo; }
+};
+
+template <int D, int KIND>
+__device__ inline void pair_eval32(const PairPrm &p, const float *Lf, const float *iLf, const float *dx,
+                                   float *F, const float *tab, float alpha, float rc2, int kmax) {
+  if (KIND == PAIR_GAUSSIAN || KIND == PAIR_PERIODIC_GAUSSIAN) {
+    float t[D], r2 = 0.f;
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      t[d] = dx[d];
+      if (KIND == PAIR_PERIODIC_GAUSSIAN) t[d] = t[d] - Lf[d] * rintf(t[d] * iLf[d]);
+      r2 = fmaf(t[d], t[d], r2);
+    }
+    const float s2 = (float)(p.s * p.s);
+    const float mult = (float)(p.g / (M_PI * p.s * p.s)) * expf(-r2 / s2) * (2.f / s2);
+#pragma unroll
+    for (int d = 0; d < D; ++d) F[d] = mult * t[d];
+  } else if (KIND == PAIR_COULOMB || KIND == PAIR_PERIODIC_COULOMB) {
+    float t[D], r2 = 0.f;
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      t[d] = dx[d];
+      if (KIND == PAIR_PERIODIC_COULOMB) t[d] = t[d] - Lf[d] * rintf(t[d] * iLf[d]);
+      r2 = fmaf(t[d], t[d], r2);
+    }
+    const float ri = rsqrtf(r2);
+    const float mult = (float)p.qs * ri * ri * ri;
+#pragma unroll
+    for (int d = 0; d < D; ++d) F[d] = mult * t[d];
+  } else if (KIND == PAIR_EWALD_REAL) {
+    float m[3];
+    int sh[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const float r = rintf(dx[d] * iLf[d]);
+      sh[d] = (int)r;
+      m[d] = fmaf(-r, Lf[d], dx[d]);
+    }
+    float F0 = 0.f, F1 = 0.f, F2 = 0.f;
+    for (int k0 = -kmax; k0 <= kmax; ++k0) {
+      if (abs(sh[0] + k0) > p.nsum) continue;
+      const float t0 = fmaf(-(float)k0, Lf[0], m[0]);
+      for (int k1 = -kmax; k1 <= kmax; ++k1) {
+        if (abs(sh[1] + k1) > p.nsum) continue;
+        const float t1 = fmaf(-(float)k1, Lf[1], m[1]);
+        for (int k2 = -kmax; k2 <= kmax; ++k2) {
+          if (abs(sh[2] + k2) > p.nsum) continue;
+          const float t2 = fmaf(-(float)k2, Lf[2], m[2]);
+          const float R2 = fmaf(t2, t2, fmaf(t1, t1, t0 * t0));
+          if (R2 >= rc2) continue;
+          const float ri = rsqrtf(R2);
+          const float xr = alpha * R2 * ri;
+          int iv = __float2int_rn(xr * (float)EW_INV_W);
+          iv = iv < EW_NINT - 1 ? iv : EW_NINT - 1;
+          const float u = fmaf(xr, 2.f * (float)EW_INV_W, -2.f * (float)iv);
+          const float *cf = tab + iv * (EW_DEG + 1);
+          float hv = cf[EW_DEG];
+#pragma unroll
+          for (int q = EW_DEG - 1; q >= 0; --q) hv = fmaf(hv, u, cf[q]);
+          const float mult = hv * ri * ri * ri;
+          F0 = fmaf(t0, mult, F0);
+          F1 = fmaf(t1, mult, F1);
+          F2 = fmaf(t2, mult, F2);
+        }
+      }
+    }
+    const float qs = (float)p.qs;
+    F[0] = qs * F0;
+    if (D > 1) F[1] = qs * F1;
+    if (D > 2) F[2] = qs * F2;
+  }
+}
+
+// same tile/rotation scheme and scratch layout as k_pair_tiles, FP32 with
+// Kahan-compensated per-particle sums
+template <int D, int KIND>
+__global__ void __launch_bounds__(256) k_pair_tiles32(Geo g, PairPrm p, const double *__restrict__ x,
+                                                      const double *__restrict__ m,
+                                                      double *__restrict__ out, int T, int jobs) {
+  __shared__ float stab[KIND == PAIR_EWALD_REAL ? EW_NINT * (EW_DEG + 1) : 1];
+  if (KIND == PAIR_EWALD_REAL) {
+    for (int i = threadIdx.x; i < EW_NINT * (EW_DEG + 1); i += blockDim.x) stab[i] = (float)(&c_ew_h[0][0])[i];
+    __syncthreads();
+  }
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= jobs * g.P) return;
+  const int j = warp / jobs;
+  int job = warp % jobs, I = 0;
+  while (job >= T - I) {
+    job -= T - I;
+    ++I;
+  }
+  const int J = I + job;
+  const int a = I * 32 + lane, b0 = J * 32 + lane;
+  const bool va = a < g.N, vb = b0 < g.N;
+  float Lf[3], iLf[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    Lf[d] = (float)g.box[d];
+    iLf[d] = (float)g.inv_box[d];
+  }
+  const float alpha = (float)p.alpha, rc2 = (float)(p.rcut * p.rcut);
+  const int kmax = p.kmax[0] > p.kmax[1] ? (p.kmax[0] > p.kmax[2] ? p.kmax[0] : p.kmax[2])
+                                         : (p.kmax[1] > p.kmax[2] ? p.kmax[1] : p.kmax[2]);
+  float xa[D], xb[D];
+  Kahan fa[D], fb[D];
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    xa[d] = va ? (float)x[sidx(j, d, a, D, g.Ns)] : 0.f;
+    xb[d] = vb ? (float)x[sidx(j, d, b0, D, g.Ns)] : 0.f;
+  }
+  const float ima = va ? (float)(1.0 / m[(size_t)j * g.Ns + a]) : 1.f;
+  float imb = vb ? (float)(1.0 / m[(size_t)j * g.Ns + b0]) : 1.f;
+  for (int s = 0; s < 32; ++s) {
+    const int bi = J * 32 + ((lane + s) & 31);
+    const bool act = va && bi < g.N && (I != J || a > bi);
+    if (act) {
+      float dx[D], F[D];
+#pragma unroll
+      for (int d = 0; d < D; ++d) dx[d] = xa[d] - xb[d];
+      pair_eval32<D, KIND>(p, Lf, iLf, dx, F, stab, alpha, rc2, kmax);
+      const float inv = a > bi ? ima : imb;
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        fa[d].add(F[d] * inv);
+        fb[d].add(-F[d] * inv);
+      }
+    }
+    const int src = (lane + 1) & 31;
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      xb[d] = __shfl_sync(FULL, xb[d], src);
+      fb[d].s = __shfl_sync(FULL, fb[d].s, src);
+      fb[d].c = __shfl_sync(FULL, fb[d].c, src);
+    }
+    imb = __shfl_sync(FULL, imb, src);
+  }
+  if (I == J) {
+    if (va) {
+#pragma unroll
+      for (int d = 0; d < D; ++d)
+        out[(((size_t)I * g.P + j) * D + d) * g.Ns + a] = fa[d].value() + fb[d].value();
+    }
+  } else {
+    if (va) {
+#pragma unroll
+      for (int d = 0; d < D; ++d) out[(((size_t)J * g.P + j) * D + d) * g.Ns + a] = fa[d].value();
+    }
+    if (vb) {
+#pragma unroll
+      for (int d = 0; d < D; ++d) out[(((size_t)I * g.P + j) * D + d) * g.Ns + b0] = fb[d].value();
+    }
+  }
+}
+
+cudaError_t pair_force32(const Geo &g, const PairPrm &p, const double *x, const double *m, double *f,
+                         double *scratch, cudaStream_t st) {
+  const int T = (g.N + 31) / 32;
+  const int jobs = T * (T + 1) / 2;
+  const int nb = cdiv((size_t)jobs * g.P * 32, 256);
+  {
+    XK_PROF(p.kind == PAIR_EWALD_REAL ? "pair_tiles32_ewald_real" : "pair_tiles32");
+    switch (g.D * 16 + p.kind) {
+#define XK_P32_CASE(DV, K) \
+  case DV * 16 + K:        \
+    k_pair_tiles32<DV, K><<<nb, 256, 0, st>>>(g, p, x, m, scratch, T, jobs); \
+    break;
+      XK_P32_CASE(1, PAIR_GAUSSIAN)
+      XK_P32_CASE(1, PAIR_PERIODIC_GAUSSIAN)
+      XK_P32_CASE(1, PAIR_COULOMB)
+      XK_P32_CASE(1, PAIR_PERIODIC_COULOMB)
+      XK_P32_CASE(2, PAIR_GAUSSIAN)
+      XK_P32_CASE(2, PAIR_PERIODIC_GAUSSIAN)
+      XK_P32_CASE(2, PAIR_COULOMB)
+      XK_P32_CASE(2, PAIR_PERIODIC_COULOMB)
+      XK_P32_CASE(3, PAIR_GAUSSIAN)
+      XK_P32_CASE(3, PAIR_PERIODIC_GAUSSIAN)
+      XK_P32_CASE(3, PAIR_COULOMB)
+      XK_P32_CASE(3, PAIR_PERIODIC_COULOMB)
+      XK_P32_CASE(3, PAIR_EWALD_REAL)
+#undef XK_P32_CASE
+      default:
+        return cudaErrorInvalidValue;
+    }
+  }
+  cudaError_t e = XK_LAUNCHED();
+  if (e != cudaSuccess) return e;
+  {
+    XK_PROF("pair_finish");
+    k_pair_finish<<<cdiv(g.slots(), 256), 256, 0, st>>>(g, scratch, T, 1.0 / g.P, f);
+  }
+  return XK_LAUNCHED();
+}
+
+// ---- reciprocal space, mixed ----------------------------------------
+// FP32 copies of the FP64 phase factors: ph32[((j*3 + d)*(NS+1) + n)*Ns + l]
+__global__ void k_phase_to32(Geo g, int ns, const double2 *__restrict__ ph, float2 *__restrict__ ph32) {
+  const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const size_t n = (size_t)g.P * 3 * (ns + 1) * g.Ns;
+  if (t >= n) return;
+  const double2 v = ph[t];
+  ph32[t] = make_float2((float)v.x, (float)v.y);
+}
+
+__device__ inline float2 cmulf(float2 a, float2 b) {
+  return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+}
+
+// structure factors as k_sk, FP32 products accumulated in double-float
+template <int NS>
+__global__ void __launch_bounds__(SK_THREADS) k_sk32(Geo g, const float2 *__restrict__ ph,
+                                                     const int4 *__restrict__ cols, int ncol,
+                                                     double2 *__restrict__ S, int nk) {
+  __shared__ float2 sp[3][NS + 1][SK_CHUNK];
+  const int j = blockIdx.y;
+  const int ci = blockIdx.x * SK_THREADS + threadIdx.x;
+  const bool live = ci < ncol;
+  const int4 c = live ? cols[ci] : make_int4(0, 0, 1, 0);
+  const int ax = c.x, ay = c.y < 0 ? -c.y : c.y;
+  const bool cy = c.y < 0;
+  DF s0r, s0i, P[NS][2], Q[NS][2];
+  const float2 *base = ph + (size_t)j * 3 * (NS + 1) * g.Ns;
+  for (int l0 = 0; l0 < g.N; l0 += SK_CHUNK) {
+    const int cnt = g.N - l0 < SK_CHUNK ? g.N - l0 : SK_CHUNK;
+    __syncthreads();
+    for (int q = threadIdx.x; q < 3 * (NS + 1) * SK_CHUNK; q += SK_THREADS) {
+      const int l = q % SK_CHUNK, row = q / SK_CHUNK;
+      (&sp[0][0][0])[q] = l < cnt ? base[(size_t)row * g.Ns + l0 + l] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    if (!live) continue;
+    for (int l = 0; l < cnt; ++l) {
+      float2 ey = sp[1][ay][l];
+      if (cy) ey.y = -ey.y;
+      const float2 exy = cmulf(sp[0][ax][l], ey);
+      s0r.add(exy.x);
+      s0i.add(exy.y);
+#pragma unroll
+      for (int n = 1; n <= NS; ++n) {
+        const float2 ez = sp[2][n][l];
+        P[n - 1][0].add(exy.x * ez.x);
+        P[n - 1][1].add(exy.y * ez.x);
+        Q[n - 1][0].add(exy.x * ez.y);
+        Q[n - 1][1].add(exy.y * ez.y);
+      }
+    }
+  }
+  if (!live) return;
+  double2 *o = S + (size_t)j * nk + c.w - c.z;
+  if (c.z <= 0) o[0] = make_double2(s0r.value(), s0i.value());
+#pragma unroll
+  for (int n = 1; n <= NS; ++n) {
+    const double Pr = P[n - 1][0].value(), Pi = P[n - 1][1].value();
+    const double Qr = Q[n - 1][0].value(), Qi = Q[n - 1][1].value();
+    o[n] = make_double2(Pr - Qi, Pi + Qr);
+    if (c.z < 0) o[-n] = make_double2(Pr + Qi, Pi - Qr);
+  }
+}
+
+// force tables as k_recip_tables, stored in FP32
+template <int NS>
+__global__ void k_recip_tables32(const int4 *__restrict__ cols, int ncol, const double2 *__restrict__ S,
+                                 const double *__restrict__ coef, int nk, float2 *__restrict__ T) {
+  constexpr int NT = 4 * NS + 1;
+  const int j = blockIdx.y;
+  const int ci = blockIdx.x * blockDim.y + threadIdx.y;
+  const int n = threadIdx.x;
+  if (ci >= ncol || n > NS) return;
+  const int4 c = cols[ci];
+  auto W = [&](int nz) {
+    if (nz < c.z) return make_double2(0.0, 0.0);
+    const int k = c.w + (nz - c.z);
+    const double2 s = S[(size_t)j * nk + k];
+    return make_double2(coef[k] * s.x, -coef[k] * s.y);
+  };
+  float2 *o = T + ((size_t)j * ncol + ci) * NT;
+  if (n == 0) {
+    const double2 w = W(0);
+    o[0] = make_float2((float)w.x, (float)w.y);
+  } else {
+    const double2 wp = W(n), wm = W(-n);
+    const double Ar = wp.x + wm.x, Ai = wp.y + wm.y, Br = wp.x - wm.x, Bi = wp.y - wm.y;
+    o[4 * n - 3] = make_float2((float)Ar, (float)Ai);
+    o[4 * n - 2] = make_float2((float)Br, (float)Bi);
+    o[4 * n - 1] = make_float2((float)(n * Ar), (float)(n * Ai));
+    o[4 * n] = make_float2((float)(n * Br), (float)(n * Bi));
+  }
+}
+
+template <int NS>
+__global__ void __launch_bounds__(128) k_recip_force32(Geo g, const float2 *__restrict__ ph,
+                                                       const int4 *__restrict__ cols, int ncol,
+                                                       const float2 *__restrict__ T, double scale,
+                                                       double *__restrict__ f) {
+  constexpr int NT = 4 * NS + 1;
+  extern __shared__ float smf[];
+  float2 *sT = (float2 *)smf;
+  const int j = blockIdx.y;
+  const float2 *Tj = T + (size_t)j * ncol * NT;
+  for (int q = threadIdx.x; q < ncol * NT; q += blockDim.x) sT[q] = Tj[q];
+  __syncthreads();
+  const int l = blockIdx.x * blockDim.x + threadIdx.x;
+  if (l >= g.N) return;
+  const float2 *pj = ph + (size_t)j * 3 * (NS + 1) * g.Ns + l;
+  float2 ez[NS + 1];
+#pragma unroll
+  for (int n = 1; n <= NS; ++n) ez[n] = pj[((size_t)2 * (NS + 1) + n) * g.Ns];
+  Kahan Fx, Fy, Fz;
+  for (int ci = 0; ci < ncol; ++ci) {
+    const int4 c = cols[ci];
+    float2 ey = pj[((size_t)(NS + 1) + (c.y < 0 ? -c.y : c.y)) * g.Ns];
+    if (c.y < 0) ey.y = -ey.y;
+    const float2 exy = cmulf(pj[(size_t)c.x * g.Ns], ey);
+    const float2 *t = sT + ci * NT;
+    float Ur = t[0].x, Ui = t[0].y, Vr = 0.f, Vi = 0.f;
+#pragma unroll
+    for (int n = 1; n <= NS; ++n) {
+      const float2 A = t[4 * n - 3], B = t[4 * n - 2], nA = t[4 * n - 1], nB = t[4 * n];
+      const float cz = ez[n].x, sz = ez[n].y;
+      Ur = fmaf(cz, A.x, fmaf(-sz, B.y, Ur));
+      Ui = fmaf(cz, A.y, fmaf(sz, B.x, Ui));
+      Vr = fmaf(cz, nB.x, fmaf(-sz, nA.y, Vr));
+      Vi = fmaf(cz, nB.y, fmaf(sz, nA.x, Vi));
+    }
+    const float Tm = fmaf(exy.x, Ui, exy.y * Ur);
+    const float Zm = fmaf(exy.x, Vi, exy.y * Vr);
+    Fx.add((float)c.x * Tm);
+    Fy.add((float)c.y * Tm);
+    Fz.add(Zm);
+  }
+  f[sidx(j, 0, l, 3, g.Ns)] += scale * Fx.value() * g.inv_box[0];
+  f[sidx(j, 1, l, 3, g.Ns)] += scale * Fy.value() * g.inv_box[1];
+  f[sidx(j, 2, l, 3, g.Ns)] += scale * Fz.value() * g.inv_box[2];
+}
+
+cudaError_t recip_force32(const Geo &g, const Recip &r, const double *x, double inv_mP, double *f,
+                          cudaStream_t st) {
+  if (g.D != 3) return cudaErrorInvalidValue;
+  const size_t n = (size_t)g.P * 3 * g.Ns;
+  {
+    XK_PROF("phase");
+    k_phase<<<cdiv(n, 256), 256, 0, st>>>(g, r.nsum, x, (double2 *)r.phase);
+  }
+  cudaError_t e = XK_LAUNCHED();
+  if (e != cudaSuccess) return e;
+  // FP32 phases live behind the FP64 ones in the same buffer
+  float2 *ph32 = (float2 *)(r.phase + recip_phase_doubles(g, r.nsum));
+  const size_t np = (size_t)g.P * 3 * (r.nsum + 1) * g.Ns;
+  {
+    XK_PROF("phase_to32");
+    k_phase_to32<<<cdiv(np, 256), 256, 0, st>>>(g, r.nsum, (const double2 *)r.phase, ph32);
+  }
+  e = XK_LAUNCHED();
+  if (e != cudaSuccess) return e;
+  const int nc = ncols(r.nsum);
+  dim3 sgrid((nc + SK_THREADS - 1) / SK_THREADS, g.P);
+  dim3 tgrid((nc + 7) / 8, g.P), tblk(r.nsum + 1, 8);
+  dim3 grid((g.N + 127) / 128, g.P);
+  const size_t smem = sizeof(float2) * nc * (4 * r.nsum + 1);
+  float2 *T32 = (float2 *)r.T;
+  DISPATCH_NS(r.nsum, {
+    {
+      XK_PROF("sk32");
+      k_sk32<NS><<<sgrid, SK_THREADS, 0, st>>>(g, ph32, (const int4 *)r.kvec, nc, (double2 *)r.S, r.nk);
+    }
+    {
+      XK_PROF("recip_tables32");
+      k_recip_tables32<NS><<<tgrid, tblk, 0, st>>>((const int4 *)r.kvec, nc, (const double2 *)r.S, r.coef, r.nk, T32);
+    }
+    auto kf = k_recip_force32<NS>;
+    static bool opted = false;
+    if (!opted) {
+      cudaError_t ea = cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+      if (ea != cudaSuccess) return ea;
+      opted = true;
+    }
+    {
+      XK_PROF("recip_force32");
+      kf<<<grid, 128, smem, st>>>(g, ph32, (const int4 *)r.kvec, nc, T32, 4 * M_PI * inv_mP, f);
+    }
+  });
+  return XK_LAUNCHED();
+}
+
+}  // namespace xk

@@ -157,6 +157,13 @@ cudaError_t recip_force(const Geo &g, const Recip &r, const double *x, double in
 cudaError_t recip_energy(const Geo &g, const Recip &r, const double *x, double *acc,
                          double *scratch, cudaStream_t st);
 
+// ---- mixed-precision form: FP32 arithmetic, compensated accumulation ----
+cudaError_t pair_force32(const Geo &g, const PairPrm &p, const double *x, const double *m,
+                         double *f, double *scratch, cudaStream_t st);
+// needs r.phase sized recip_phase_doubles(g, nsum) * 3 / 2 (FP32 copy behind)
+cudaError_t recip_force32(const Geo &g, const Recip &r, const double *x, double inv_mP, double *f,
+                          cudaStream_t st);
+
 // ---- estimators ----
 cudaError_t vbn_energy(int N, double beta, double vi, double add, const double *ENk,
                        const double *VBN, const double *ENk2, double *acc, cudaStream_t st);

@@ -331,7 +331,8 @@ static int ewald_tables(md_pimd_t_x *pimd, SimDev *sd, PimdDev *pd) {
   const int nk = xk::recip_count(ns);
   XMD_TRY(reserve(pd->rc_coef, sizeof(double) * nk));
   XMD_TRY(reserve(pd->rc_cols, sizeof(int) * 4 * (ns * (2 * ns + 1) + ns + 1)));
-  XMD_TRY(reserve(pd->rc_phase, sizeof(double) * xk::recip_phase_doubles(g, ns)));
+  // FP64 phases, then their FP32 copy for the mixed form
+  XMD_TRY(reserve(pd->rc_phase, sizeof(double) * xk::recip_phase_doubles(g, ns) * 3 / 2));
   XMD_TRY(reserve(pd->rc_S, sizeof(double) * 2 * (size_t)nk * g.P));
   XMD_TRY(reserve(pd->rc_T, sizeof(double) * xk::recip_table_doubles(g, ns)));
   xk::Recip r{};
@@ -346,6 +347,9 @@ static int ewald_tables(md_pimd_t_x *pimd, SimDev *sd, PimdDev *pd) {
   (void)pimd;
   return 0;
 }
+
+// library-wide arithmetic of the pair and Ewald forces (md_gb300_x.h)
+static int g_precision = MD_GB_PRECISION_FP64;
 
 static xk::Recip recip_of(PimdDev *pd) {
   xk::Recip r{};
@@ -396,18 +400,34 @@ int md_pimd_calc_pair_force_x(md_pimd_t_x *pimd, md_pair_force_t_x pf) {
   cudaStream_t st = stream();
   xk::PairPrm prm = pair_params(kind);
   ewald_shifts(prm, sd->geo);
+  const bool mixed = g_precision == MD_GB_PRECISION_MIXED;
   if (kind == xk::PAIR_EWALD_REAL) {
     if (prm.kmax[0] > 1 || prm.kmax[1] > 1 || prm.kmax[2] > 1)
       return fail(MD_GB_ERR_UNSUPPORTED, "Ewald alpha*L below %.1f (images beyond the neighbouring boxes)",
                   2 * EWALD_XCUT / 3);
     if (!sd->uniform_mass) return fail(MD_GB_ERR_UNSUPPORTED, "structure-factor Ewald needs equal bead masses");
     XMD_TRY(ewald_tables(pimd, sd, pd));
-    XMD_CUDA(xk::recip_force(sd->geo, recip_of(pd), sd->x.as<double>(), 1.0 / (sd->mass0 * pimd->P),
-                             sd->f.as<double>(), st));
+    const double inv_mP = 1.0 / (sd->mass0 * pimd->P);
+    if (mixed)
+      XMD_CUDA(xk::recip_force32(sd->geo, recip_of(pd), sd->x.as<double>(), inv_mP, sd->f.as<double>(), st));
+    else
+      XMD_CUDA(xk::recip_force(sd->geo, recip_of(pd), sd->x.as<double>(), inv_mP, sd->f.as<double>(), st));
   }
-  XMD_CUDA(xk::pair_force(sd->geo, prm, sd->x.as<double>(), sd->m.as<double>(), sd->f.as<double>(), scr, st));
+  if (mixed)
+    XMD_CUDA(xk::pair_force32(sd->geo, prm, sd->x.as<double>(), sd->m.as<double>(), sd->f.as<double>(), scr, st));
+  else
+    XMD_CUDA(xk::pair_force(sd->geo, prm, sd->x.as<double>(), sd->m.as<double>(), sd->f.as<double>(), scr, st));
   return 0;
 }
+
+int md_gb300_set_precision_x(int mode) {
+  if (mode != MD_GB_PRECISION_FP64 && mode != MD_GB_PRECISION_MIXED)
+    return fail(MD_GB_ERR_ARG, "unknown precision mode %d", mode);
+  g_precision = mode;
+  return 0;
+}
+
+int md_gb300_get_precision_x(void) { return g_precision; }
 
 // Pair forces for callers that cannot allocate device memory (md_gb300_x.h).
 // Everything here works on the caller's device pointers and stream; the

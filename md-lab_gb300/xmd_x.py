@@ -147,6 +147,8 @@ class XLib:
                 "md_gb300_profile_report_x": (_i, [C.c_char_p, _i]),
                 "md_gb300_fp64_peak_x": (_d, []),
                 "md_gb300_set_device_x": (_i, [_i]),
+                "md_gb300_set_precision_x": (_i, [_i]),
+                "md_gb300_get_precision_x": (_i, []),
                 "md_gb300_pair_force_noalloc_x": (_i, [_vp, _vp, _vp, _vp, _i, _i, _i, _dp, _vp]),
             })
         for name, (res, args) in sig.items():
