@@ -815,6 +815,29 @@ __global__ void k_tv_weights(int N, double beta, double vi, const double *__rest
 // to out[i] (forward) or out[N-i] (backward).  One block, 16 warps.
 constexpr int TS_WARPS = 16, TS_CHUNK = 32;
 
+// v * 2^d for a non-negative double v and d <= 0, by integer arithmetic on
+// the exponent field (the FP64 pipe is the scarce resource); results below
+// the normal range are flushed to 0 (they are below 2^-1021 of the sum
+// they enter)
+__device__ inline double scale2(double v, int d) {
+  const long long b = __double_as_longlong(v);
+  const int ex = (int)((b >> 52) & 0x7ff);
+  if (ex == 0 || ex + d <= 0) return 0.0;
+  return __longlong_as_double(b + ((long long)d << 52));
+}
+
+// normalise a non-negative extended value to a mantissa in [0.5, 1)
+__device__ inline void norm2(double &m, int &e) {
+  const long long b = __double_as_longlong(m);
+  const int ex = (int)((b >> 52) & 0x7ff);
+  if (ex == 0) {  // zero (values here are never subnormal)
+    m = 0.0;
+    return;
+  }
+  e += ex - 1022;
+  m = __longlong_as_double((b & ~(0x7ffLL << 52)) | (1022LL << 52));
+}
+
 __global__ void __launch_bounds__(TS_WARPS * 32) k_tri_solve(int N, double beta,
                                                              const double *__restrict__ Mm,
                                                              const int *__restrict__ Me,
@@ -832,30 +855,39 @@ __global__ void __launch_bounds__(TS_WARPS * 32) k_tri_solve(int N, double beta,
   }
   __syncthreads();
   for (int i0 = 1; i0 <= N; i0 += TS_CHUNK) {
-    // known part: rows i0..i0+31 against columns 0..i0-1, two rows per warp
+    // known part: rows i0..i0+31 against columns 0..i0-1, two rows per warp.
+    // An integer pass finds the row's largest term exponent E; the terms are
+    // then scaled to 2^E by exponent arithmetic and summed with one FMA each.
     for (int r = w; r < TS_CHUNK; r += TS_WARPS) {
       const int i = i0 + r;
       double am = 0.0;
-      int ae = 0;
+      int E = -2147483647;
       if (i <= N) {
         const double *mr = Mm + moff(i, 0);
         const int *er = Me + moff(i, 0);
-        for (int j = lane; j < i0; j += 32) ext_add(am, ae, mr[j] * Xm[j], er[j] + Xe[j]);
-      }
+        for (int j = lane; j < i0; j += 32) {
+          const int te = er[j] + Xe[j];
+          E = te > E ? te : E;
+        }
 #pragma unroll
-      for (int o = 16; o; o >>= 1) {
-        const double om = __shfl_xor_sync(FULL, am, o);
-        const int oe = __shfl_xor_sync(FULL, ae, o);
-        ext_add(am, ae, om, oe);
+        for (int o = 16; o; o >>= 1) {
+          const int oe = __shfl_xor_sync(FULL, E, o);
+          E = oe > E ? oe : E;
+        }
+        for (int j = lane; j < i0; j += 32) am = fma(mr[j], scale2(Xm[j], er[j] + Xe[j] - E), am);
       }
+      am = warp_sum(am);
       if (lane == 0) {
-        ext_norm(am, ae);
+        int ae = E;
+        norm2(am, ae);
         Pm[r] = am;
         Pe[r] = ae;
       }
     }
     __syncthreads();
-    // the chunk itself: lane r owns row i0+r
+    // the chunk itself: lane r owns row i0+r; each step publishes one
+    // unknown and every later row adds its term (exponent arithmetic and
+    // one FMA on the sequential chain)
     if (w == 0) {
       const int i = i0 + lane;
       const bool own = i <= N;
@@ -872,7 +904,7 @@ __global__ void __launch_bounds__(TS_WARPS * 32) k_tri_solve(int N, double beta,
 #pragma unroll
       for (int s = 0; s < TS_CHUNK; ++s) {
         if (lane == s) {
-          ext_norm(am, ae);
+          norm2(am, ae);
           if (own) {
             Xm[i] = am;
             Xe[i] = ae;
@@ -880,7 +912,14 @@ __global__ void __launch_bounds__(TS_WARPS * 32) k_tri_solve(int N, double beta,
         }
         const double xm = __shfl_sync(FULL, am, s);
         const int xe = __shfl_sync(FULL, ae, s);
-        if (lane > s) ext_add(am, ae, mm[s] * xm, me[s] + xe);
+        if (lane > s && mm[s] != 0.0) {
+          const int te = me[s] + xe;
+          if (te > ae) {  // the new term sets the scale
+            am = scale2(am, ae - te);
+            ae = te;
+          }
+          am = fma(mm[s], scale2(xm, te - ae), am);
+        }
       }
     }
     __syncthreads();
