@@ -35,6 +35,7 @@ sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
 N, P, RS, THETA, XI, NSUM, DT = 512, 64, 1.0, 0.5, 0.5, 10, 0.01
 ALPHA_L = 5.6
+NSUM_CHEAP, JUDGE_EVERY = 3, 50
 METRIC = "bead-steps/s UEG N=512 P=64: learned+FP32 vs plain FP64 on 1 GB300, at stated ΔE/N"
 
 
@@ -191,21 +192,24 @@ def cpu_step_estimate(cores, budget_s):
 # ---------------------------------------------------------------------
 # GB300 arm
 # ---------------------------------------------------------------------
-# algorithmic FP64 work per launch of each kernel, FMA = 2 flops (the design doc
-# section 4 derives each count from the kernel's arithmetic)
-def kernel_flops(name, launches_per_step):
-    ncol = NSUM * (2 * NSUM + 1) + NSUM + 1  # wave-vector columns (nx, ny)
-    if name == "recip_force":
-        return 177.0 * ncol * N * P
-    if name == "sk":
-        return 88.0 * ncol * N * P
-    if name == "pair_tiles_ewald_real":
-        box, _ = workload()
-        rc = 5.8 / (ALPHA_L / box)
-        # expected images inside the cut-off per pair: (4/3) pi rc^3 / V
-        n_img = 4 / 3 * math.pi * rc ** 3 / box ** 3
+def n_images():
+    box, _ = workload()
+    rc = 5.8 / (ALPHA_L / box)
+    return 4 / 3 * math.pi * rc ** 3 / box ** 3  # expected images inside the cut-off per pair
+
+
+# algorithmic work per launch of each kernel (FMA = 2 flops); the same count
+# for the FP64 and FP32 versions of a kernel (the design doc section 4 derives
+# each from the kernel's arithmetic)
+def kernel_flops(name, nsum=NSUM):
+    ncol = nsum * (2 * nsum + 1) + nsum + 1  # wave-vector columns (nx, ny)
+    if name in ("recip_force", "recip_force32"):
+        return 177.0 * ncol * N * P * nsum / NSUM
+    if name in ("sk", "sk32"):
+        return 88.0 * ncol * N * P * nsum / NSUM
+    if name in ("pair_tiles_ewald_real", "pair_tiles32_ewald_real"):
         pairs = P * N * (N - 1) / 2
-        return pairs * (47.0 * n_img + 39.0)
+        return pairs * (47.0 * n_images() + 39.0)
     return None
 
 
@@ -225,6 +229,146 @@ def make_system(lib):
     return s
 
 
+class Runner:
+    """Graph capture and per-step CUDA-event timing on the library's stream."""
+
+    def __init__(self, lib, dist, dev, args):
+        import torch
+        self.torch, self.lib, self.dist, self.dev, self.args = torch, lib, dist, dev, args
+        self.stream = torch.cuda.ExternalStream(lib.md_gb300_get_stream_x())
+        self.flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def capture(self, step):
+        lib = self.lib
+        g = C.c_void_p()
+        lib.check(lib.md_gb300_capture_begin_x(), "capture begin")
+        step()
+        lib.check(lib.md_gb300_capture_end_x(C.byref(g)), "capture end")
+        return g, lib.md_gb300_graph_kernel_count_x(g)
+
+    def launcher(self, g):
+        lib = self.lib
+        return lambda: lib.check(lib.md_gb300_graph_launch_x(g, 1))
+
+    def time(self, actions, warm):
+        """Per-step CUDA events around each action (one step each); the L2 is
+        flushed (256 MB write) before every step, outside the events."""
+        torch, lib = self.torch, self.lib
+        for a in warm:
+            a()
+        lib.check(lib.md_gb300_synchronize_x())
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in actions]
+        barrier(self.dist)
+        torch.cuda.synchronize()
+        with Clocks(self.dev) as clk:
+            t0 = time.perf_counter()
+            with torch.cuda.stream(self.stream):
+                for (e0, e1), act in zip(evs, actions):
+                    self.flush.zero_()
+                    e0.record(self.stream)
+                    act()
+                    e1.record(self.stream)
+            lib.check(lib.md_gb300_synchronize_x())
+            torch.cuda.synchronize()
+            wall = time.perf_counter() - t0
+        barrier(self.dist)
+        ms = sum(a.elapsed_time(b) for a, b in evs) / len(evs)
+        return max_over_ranks(self.dist, ms), wall, clk.summary()
+
+    def profile(self, step, n=2):
+        """live per-kernel times of n un-captured steps: {kernel: ms per step}"""
+        lib = self.lib
+        lib.check(lib.md_gb300_synchronize_x())
+        lib.check(lib.md_gb300_profile_x(1))
+        for _ in range(n):
+            step()
+        lib.check(lib.md_gb300_synchronize_x())
+        prof = lib.profile_report()
+        lib.check(lib.md_gb300_profile_x(0))
+        return {k: (v[0] / n, v[1] // n) for k, v in prof.items()}
+
+
+def roofline(prof, peak, peak_name, unit_nsum=NSUM):
+    """FLOP roofline of the step's dominant kernel from its live per-launch time"""
+    total = sum(v[0] for v in prof.values())
+    name, (ms, launches) = max(prof.items(), key=lambda kv: kv[1][0])
+    per_launch_ms = ms / max(launches, 1)
+    roof = {"kernel": name, "bound": "fp64" if peak_name == "fp64" else "fp32", "unit": "TFLOP/s",
+            "share": ms / total if total else None, "launch_ms": per_launch_ms, "peak": peak,
+            "peak_source": f"live {peak_name.upper()} FMA probe on this GPU (md_gb300_{peak_name}_peak_x)",
+            "traffic": None}
+    flops = kernel_flops(name, unit_nsum)
+    if flops:
+        roof["algorithmic_flop_per_launch"] = flops
+        roof["achieved"] = flops / (per_launch_ms * 1e-3) / 1e12
+        roof["frac"] = roof["achieved"] / peak if peak > 0 else None
+    return roof
+
+
+def learned_form(lib, R, s, pair, step, args, ws):
+    """Truncated Ewald (|n| <= NSUM_CHEAP) + the residual network, FP32 forces.
+    Data from plain runs of this system (converged Ewald, mixed forces),
+    training on the GPU, then the timed run with the converged sum as judge
+    every JUDGE_EVERY steps (the judge's converged step and its FP64
+    judgement are inside the timed region)."""
+    import xmd_x
+    lib.check(lib.md_gb300_set_precision_x(1))
+    m = xmd_x.EwaldModel(lib, s, nsum_cheap=NSUM_CHEAP, capacity=args.learn_configs, seed=7)
+    t0 = time.perf_counter()
+    for _ in range(args.learn_configs):
+        step()
+        m.collect(s)
+    lib.check(lib.md_gb300_synchronize_x())
+    t_collect = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    loss = m.train(args.learn_steps, args.learn_batch, args.learn_lr)
+    t_train = time.perf_counter() - t0
+    for _ in range(5):
+        step()
+    first = m.judge(s)
+    # graphs: the learned step, and the converged (judge) step
+    g_conv, _ = R.capture(step)
+    m.attach(s, judge_every=0)
+    g_learn, kps = R.capture(step)
+    state = {"reverted": False}
+    judges = []
+
+    def judge_step():
+        lib.check(lib.md_gb300_graph_launch_x(g_conv, 1))
+        j = m.judge(s)
+        judges.append(j)
+        if j["force_err"] > args.force_tol or j["energy_err"] > args.energy_tol:
+            state["reverted"] = True
+
+    def learned_step():
+        lib.check(lib.md_gb300_graph_launch_x(g_conv if state["reverted"] else g_learn, 1))
+
+    nsteps = max(args.steps, JUDGE_EVERY)
+    actions = [judge_step if i % JUDGE_EVERY == 0 else learned_step for i in range(nsteps)]
+    ms, wall, clocks = R.time(actions, [R.launcher(g_learn)] * 3)
+    prof = R.profile(step)
+    value = ws * N * P / (ms * 1e-3)
+    lib.md_gb300_graph_free_x(g_learn)
+    lib.md_gb300_graph_free_x(g_conv)
+    keys = ("force_err", "energy_err", "force_err_truncated", "energy_err_truncated")
+    all_j = [first] + judges
+    form = {"value": value, "ms_per_step": ms, "steps_timed": nsteps, "kernels_per_learned_step": kps,
+            "clocks": clocks, "wall_s_timed": wall, "reverted": state["reverted"],
+            "nsum_truncated": NSUM_CHEAP, "nsum_converged": NSUM, "judge_every": JUDGE_EVERY,
+            "training": {"configurations": args.learn_configs, "bead_slice_configurations": args.learn_configs * P,
+                         "rows": args.learn_configs * N * P, "adam_steps": args.learn_steps,
+                         "batch_rows": args.learn_batch * 128, "lr": args.learn_lr, "final_loss": loss,
+                         "collect_s": t_collect, "train_s": t_train},
+            "judged": {k: [j[k] for j in all_j] for k in keys},
+            "delta_E_per_particle_Ha": max(j["energy_err"] for j in all_j),
+            "delta_E_per_particle_truncated_only_Ha": max(j["energy_err_truncated"] for j in all_j),
+            "force_err_rms_rel": max(j["force_err"] for j in all_j),
+            "force_err_rms_rel_truncated_only": max(j["force_err_truncated"] for j in all_j),
+            "tolerances": {"force": args.force_tol, "energy_per_particle_Ha": args.energy_tol},
+            "kernel_ms_per_step": {k: v[0] for k, v in prof.items()}}
+    return m, form, prof, kps
+
+
 def run_gb300(args, dist, rank, ws):
     import torch
     import xmd_x
@@ -238,79 +382,56 @@ def run_gb300(args, dist, rank, ws):
     for _ in range(args.warmup):
         step()
     lib.check(lib.md_gb300_synchronize_x(), "sync")
-    stream = torch.cuda.ExternalStream(lib.md_gb300_get_stream_x())
-    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    R = Runner(lib, dist, dev, args)
 
-    def timed_graph(nsteps):
-        """capture one step, replay it; per-step CUDA events, L2 flushed in between"""
-        g = C.c_void_p()
-        lib.check(lib.md_gb300_capture_begin_x(), "capture begin")
-        step()
-        lib.check(lib.md_gb300_capture_end_x(C.byref(g)), "capture end")
-        kps = lib.md_gb300_graph_kernel_count_x(g)
-        for _ in range(max(3, args.warmup)):
-            lib.check(lib.md_gb300_graph_launch_x(g, 1))
-        lib.check(lib.md_gb300_synchronize_x())
-        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-               for _ in range(nsteps)]
-        barrier(dist)
-        torch.cuda.synchronize()
-        with Clocks(dev) as clk:
-            t0 = time.perf_counter()
-            with torch.cuda.stream(stream):
-                for e0, e1 in evs:
-                    flush.zero_()
-                    e0.record(stream)
-                    lib.check(lib.md_gb300_graph_launch_x(g, 1))
-                    e1.record(stream)
-            lib.check(lib.md_gb300_synchronize_x())
-            torch.cuda.synchronize()
-            wall = time.perf_counter() - t0
-        barrier(dist)
+    def graph_form():
+        g, kps = R.capture(step)
+        ms, wall, clocks = R.time([R.launcher(g)] * args.steps, [R.launcher(g)] * max(3, args.warmup))
         lib.md_gb300_graph_free_x(g)
-        ms = sum(a.elapsed_time(b) for a, b in evs) / nsteps
-        return max_over_ranks(dist, ms), kps, wall, clk.summary()
+        return ms, kps, wall, clocks
 
-    step_ms, kernels_per_step, wall, clocks = timed_graph(args.steps)
-    value = ws * N * P / (step_ms * 1e-3)
-    # the mixed-precision form on the same state: time and force error
-    forms = {"plain_fp64": {"value": value, "ms_per_step": step_ms}}
-    if not args.no_mixed:
-        def forces(mode):
-            lib.check(lib.md_gb300_set_precision_x(mode))
-            lib.check(lib.md_reset_force_x(s.sim))
-            lib.check(lib.md_pimd_calc_pair_force_x(s.pimd, pair))
-            return s.state()["f"]
-        import numpy as np
-        f64, f32 = forces(0), forces(1)
-        ferr = float(np.max(np.abs(f32 - f64)) / np.max(np.abs(f64)))
-        mixed_ms, _, _, mixed_clocks = timed_graph(args.steps)
-        lib.check(lib.md_gb300_set_precision_x(0))
-        forms["mixed_fp32_forces"] = {"value": ws * N * P / (mixed_ms * 1e-3), "ms_per_step": mixed_ms,
-                                      "force_error_vs_fp64": ferr, "clocks": mixed_clocks}
-    # live per-kernel timing of two plain steps (outside the timed region)
-    lib.check(lib.md_gb300_profile_x(1))
-    for _ in range(2):
-        step()
-    lib.check(lib.md_gb300_synchronize_x())
-    prof = lib.profile_report()
-    lib.check(lib.md_gb300_profile_x(0))
-    total = sum(v[0] for v in prof.values())
-    top = max(prof.items(), key=lambda kv: kv[1][0])
+    # plain FP64: the form that reproduces MD-Lab to 1e-10
+    lib.check(lib.md_gb300_set_precision_x(0))
+    plain_ms, plain_kps, plain_wall, plain_clocks = graph_form()
+    plain_prof = R.profile(step)
     fp64_peak = lib.md_gb300_fp64_peak_x()
-    per_launch_ms = top[1][0] / top[1][1]
-    flops = kernel_flops(top[0], top[1][1] / 2)
-    roof = {"kernel": top[0], "bound": "fp64", "unit": "TFLOP/s",
-            "share": top[1][0] / total if total else None,
-            "launch_ms": per_launch_ms,
-            "peak": fp64_peak, "peak_source": "live DFMA probe on this GPU (md_gb300_fp64_peak_x)",
-            "traffic": None}
-    if flops:
-        roof["achieved"] = flops / (per_launch_ms * 1e-3) / 1e12
-        roof["frac"] = roof["achieved"] / fp64_peak if fp64_peak > 0 else None
-    # e2e: host structs authoritative every step
+    forms = {"plain_fp64": {"value": ws * N * P / (plain_ms * 1e-3), "ms_per_step": plain_ms,
+                            "kernels_per_step": plain_kps, "clocks": plain_clocks,
+                            "kernel_ms_per_step": {k: v[0] for k, v in plain_prof.items()},
+                            "roofline": roofline(plain_prof, fp64_peak, "fp64")}}
+    # mixed precision, converged Ewald
+    import numpy as np
+
+    def forces(mode):
+        lib.check(lib.md_gb300_set_precision_x(mode))
+        lib.check(lib.md_reset_force_x(s.sim))
+        lib.check(lib.md_pimd_calc_pair_force_x(s.pimd, pair))
+        return s.state()["f"]
+
+    f64, f32 = forces(0), forces(1)
+    ferr = float(np.max(np.abs(f32 - f64)) / np.max(np.abs(f64)))
+    mixed_ms, mixed_kps, _, mixed_clocks = graph_form()
+    mixed_prof = R.profile(step)
+    fp32_peak = lib.md_gb300_fp32_peak_x()
+    forms["mixed_fp32_forces"] = {"value": ws * N * P / (mixed_ms * 1e-3), "ms_per_step": mixed_ms,
+                                  "kernels_per_step": mixed_kps, "force_error_vs_fp64": ferr,
+                                  "clocks": mixed_clocks,
+                                  "kernel_ms_per_step": {k: v[0] for k, v in mixed_prof.items()}}
+    headline = "plain_fp64"
+    model = None
+    if not args.no_learned:
+        model, lform, lprof, lkps = learned_form(lib, R, s, pair, step, args, ws)
+        lform["roofline"] = roofline(lprof, fp32_peak, "fp32")
+        lform["speedup_vs_plain_fp64"] = lform["value"] / forms["plain_fp64"]["value"]
+        forms["learned_fp32"] = lform
+        headline = "learned_fp32"
+    H = forms[headline]
+    # e2e through the C ABI, host structs authoritative every step: the state
+    # is uploaded from page-locked host memory and read back, plus the
+    # estimator, every step (the headline form, model attached and judging)
+    if model is not None:
+        model.attach(s, judge_every=JUDGE_EVERY, force_tol=args.force_tol, energy_tol=args.energy_tol)
     ke = min(args.steps, args.e2e_steps)
-    pe = lib.fn("md_coulomb_3d_ewald_energy_x")
     h2d = C.sizeof(lib.Particle) * N * P + C.sizeof(lib.Nhc) * s.sim.contents.Nf
     lib.check(lib.md_gb300_synchronize_x())
     barrier(dist)
@@ -323,24 +444,30 @@ def run_gb300(args, dist, rank, ws):
         s.take_energy()  # estimator read
     if not lib.md_simulation_sync_host_x(s.sim, 1):
         raise RuntimeError(lib.err())
-    e2e_s = (time.perf_counter() - t0) / ke
-    e2e_s = max_over_ranks(dist, e2e_s)
-    launches = kernels_per_step * args.steps
-    result = {"metric": METRIC, "value": value, "unit": "bead-steps/s", "n_gpus": ws,
-              "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms,
-              "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+    e2e_s = max_over_ranks(dist, (time.perf_counter() - t0) / ke)
+    kps = H.get("kernels_per_learned_step", H.get("kernels_per_step"))
+    result = {"metric": METRIC, "value": H["value"], "unit": "bead-steps/s", "n_gpus": ws,
+              "steps": H.get("steps_timed", args.steps), "warmup": args.warmup, "ms_per_step": H["ms_per_step"],
+              "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+              "dtype": "fp32 forces + bf16/fp32 network (fp64 recursion, NHC, estimators)"
+                       if headline == "learned_fp32" else "f64",
               "data": "synthetic (seeded uniform electron-gas configuration from the library's own "
-                      "initial-condition routines)",
-              "config": config("plain FP64"), "gpu_launches": launches, "forms": forms,
-              "kernels_per_step": kernels_per_step, "wall_s_timed": wall,
+                      "initial-condition routines; training data from plain runs of the same system)",
+              "config": config("learned+FP32" if headline == "learned_fp32" else "plain FP64"),
+              "gpu_launches": kps * H.get("steps_timed", args.steps), "forms": forms,
               "e2e": {"value": ws * N * P / e2e_s, "unit": "bead-steps/s", "h2d_bytes_per_step": h2d,
-                      "d2h_bytes_per_step": h2d + 8, "steps": ke},
-              "roofline": roof, "kernel_ms_per_step": {k: v[0] / 2 for k, v in prof.items()},
-              "clocks": clocks}
+                      "d2h_bytes_per_step": h2d + 8, "steps": ke, "form": headline},
+              "roofline": H.get("roofline", forms["plain_fp64"]["roofline"]),
+              "clocks": H["clocks"]}
+    if headline == "learned_fp32":
+        result["delta_E_per_particle_Ha"] = H["delta_E_per_particle_Ha"]
+        result["speedup_vs_plain_fp64"] = H["speedup_vs_plain_fp64"]
     if rank == 0 and ws == 1 and not args.no_cpu:
         st, sample = cpu_step_estimate(1, args.cpu_budget)
         result["cpu_baseline"] = {"value": N * P / st, "unit": "bead-steps/s", "cores": 1,
-                                  "kind": "port", "sample": sample}
+                                  "kind": "port", "sample": sample, "form": "plain FP64 (converged Ewald)"}
+    if model is not None:
+        model.free()
     s.free()
     return result
 
@@ -373,7 +500,14 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--cpu-budget", type=float, default=8.0, help="seconds of CPU sample")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision form")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned form")
+    ap.add_argument("--learn-configs", type=int, default=3125,
+                    help="configurations collected for training (x P bead slices)")
+    ap.add_argument("--learn-steps", type=int, default=3000)
+    ap.add_argument("--learn-batch", type=int, default=128, help="tiles of 128 rows per Adam step")
+    ap.add_argument("--learn-lr", type=float, default=1e-3)
+    ap.add_argument("--force-tol", type=float, default=0.05)
+    ap.add_argument("--energy-tol", type=float, default=1e-4)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":

@@ -68,6 +68,8 @@ int md_gb300_profile_report_x(char *buf, int len);
 /* measured FP64 fused-multiply-add throughput of the current GPU, TFLOP/s:
    the roofline denominator of the FP64 kernels (-1 on failure) */
 double md_gb300_fp64_peak_x(void);
+/* the same for FP32 fused multiply-add (the FP32 kernels' denominator) */
+double md_gb300_fp32_peak_x(void);
 
 /* Pair forces for callers that cannot allocate device memory.  No
    counterpart in MD-Lab.  Every other compute call here allocates its device
@@ -111,6 +113,64 @@ int md_gb300_pair_force_noalloc_x(md_pair_force_t_x pf, const double *x, const d
 #define MD_GB_PRECISION_MIXED 1
 int md_gb300_set_precision_x(int mode);
 int md_gb300_get_precision_x(void);
+
+/* ---- learned Ewald residual (no counterpart in MD-Lab) ----
+   A network of 64 -> 128 -> 128 -> 4 units (tanh, BF16 weights and
+   activations, FP32 accumulation on the tcgen05 tensor cores) predicts, per
+   bead slice and particle, the difference between the converged Ewald
+   reciprocal sum (n_sum from md_set_coulomb_*) and a truncated one
+   (n_sum_cheap): an energy and the coefficients of three vector features
+   that give the force.  Inputs are 64 descriptors per particle: 32 Gaussian
+   radial functions and the spherical averages sin(kr)/(kr) of the 32 lowest
+   reciprocal-lattice shells, both summed over minimum-image neighbours
+   within half the box.  A model belongs to one system shape (N, P, box,
+   Ewald alpha and strength) and lives on the GPU. */
+typedef struct md_gb300_ewald_model md_gb300_ewald_model_t_x;
+int md_gb300_ewald_model_nparam_x(void);
+/* capacity: configurations (all bead slices of the system) kept for training */
+int md_gb300_ewald_model_create_x(md_gb300_ewald_model_t_x **model, md_pimd_t_x *pimd, int nsum_cheap,
+                                  long capacity, unsigned seed);
+void md_gb300_ewald_model_free_x(md_gb300_ewald_model_t_x *model);
+/* add pimd's current configuration to the training set (descriptors and the
+   FP64 converged-minus-truncated forces and per-particle energies); the first
+   call also fixes the normalisation of inputs and outputs */
+int md_gb300_ewald_model_collect_x(md_gb300_ewald_model_t_x *model, md_pimd_t_x *pimd);
+/* steps Adam steps on random batches of batch_tiles x 128 rows; *loss: the
+   last batch's loss (may be NULL) */
+int md_gb300_ewald_model_train_x(md_gb300_ewald_model_t_x *model, int steps, int batch_tiles, double lr,
+                                 double *loss);
+/* From now on md_pimd_calc_pair_force_x / md_pimd_calc_pair_energy_x with
+   md_coulomb_3d_ewald_* on pimd use the truncated sum plus the network.
+   Every judge_every-th force call outside graph capture (0: never) computes
+   the converged sum instead and judges the network on that configuration;
+   when the force error (rms |dF| / rms |F_reciprocal|) is above force_tol or
+   the energy error per particle above energy_tol, the network is dropped
+   and later calls use the converged sum.  model NULL detaches. */
+int md_gb300_ewald_model_attach_x(md_pimd_t_x *pimd, md_gb300_ewald_model_t_x *model, int judge_every,
+                                  double force_tol, double energy_tol);
+/* errors on pimd's current configuration: out[0] force error and out[1]
+   energy error per particle (Ha) of truncated sum + network, out[2], out[3]
+   the same for the truncated sum alone */
+int md_gb300_ewald_model_judge_x(md_gb300_ewald_model_t_x *model, md_pimd_t_x *pimd, double out[4]);
+int md_gb300_ewald_model_status_x(md_gb300_ewald_model_t_x *model, long *configurations, int *judged,
+                                  int *reverted, double last[4]);
+/* FP32 master parameters (md_gb300_ewald_model_nparam_x floats: W1[128][64],
+   b1, W2[128][128], b2, W3[4][128], b3); set != 0 uploads */
+int md_gb300_ewald_model_params_x(md_gb300_ewald_model_t_x *model, float *params, int set);
+/* the tensor-core kernels on host data: outputs Y[rows][4] of inputs
+   X[rows][64] (rounded to BF16); gradient of the training loss for rows
+   with vector features and weight V[rows][12] and targets T[rows][4] */
+int md_gb300_mlp_forward_x(md_gb300_ewald_model_t_x *model, const float *X, int rows, float *Y);
+int md_gb300_mlp_grad_x(md_gb300_ewald_model_t_x *model, const float *X, const float *V, const float *T, int rows,
+                        double we, double wf, float *grad, float *loss);
+/* raw descriptors F[N*P][64] and vector features V[N*P][12] of pimd's
+   current configuration (row j*N + l), and the descriptor definition */
+int md_gb300_ewald_model_features_x(md_gb300_ewald_model_t_x *model, md_pimd_t_x *pimd, float *F, float *V);
+int md_gb300_ewald_model_desc_info_x(md_gb300_ewald_model_t_x *model, double *rc, float *basis, double vmu[3],
+                                     double vsig[3]);
+/* tensor-core layout self-test: max errors of a 128 x 128 product for
+   K-major operands and the two readings of MN-major descriptors */
+int md_gb300_tc_selftest_x(double err[5]);
 
 /* release the device copies (and, for *_free_*, the host structs) */
 int md_gb300_release_simulation_x(md_simulation_t_x *sim);

@@ -74,6 +74,7 @@ struct PimdDev {
   int rc_nsum = -1;
   double rc_alpha = 0, rc_qs = 0, rc_box[3] = {0, 0, 0};
   int rc_nk = 0;
+  double rc_csum = 0;
 };
 
 struct StatsDev {
@@ -93,6 +94,24 @@ int pimd_to_host(md_pimd_t_x *pimd, bool keep);
 int stats_device(md_stats_t_x *st, double **acc);
 int stats_to_host(md_stats_t_x *st);
 int scratch(SimDev *sd, size_t doubles, double **out);
+
+// shared by the step and the learned residual (xmd_step.cpp)
+int check_image(const SimDev *sd, int image);
+double *scratch_for(SimDev *sd, size_t doubles, int *rc);
+size_t general_scratch(const xk::Geo &g);
+int ewald_tables(md_pimd_t_x *pimd, SimDev *sd, PimdDev *pd);
+xk::Recip recip_of(PimdDev *pd);
+xk::PairPrm pair_params(int kind);
+void ewald_shifts(xk::PairPrm &p, const xk::Geo &g);
+
+// learned Ewald residual (xmd_learned_api.cpp).  learned_mode: 0 = plain
+// Ewald, 1 = truncated sum + network, 2 = plain Ewald then judge the network
+// (force calls count towards the judging interval when count_call is set)
+int learned_mode(md_pimd_t_x *pimd, bool count_call);
+int learned_pair_force(md_pimd_t_x *pimd, SimDev *sd, PimdDev *pd, const xk::PairPrm &prm, double *scr);
+int learned_judge_step(md_pimd_t_x *pimd, SimDev *sd, PimdDev *pd);
+// reciprocal part of the energy in learned mode (truncated sum + network), added to *acc
+int learned_recip_energy(md_pimd_t_x *pimd, SimDev *sd, double *acc, double *scr);
 
 // read the current potential parameter globals
 xk::TrapPrm trap_params(int kind);

@@ -66,35 +66,28 @@ std::string profile_report() {
   return out;
 }
 
-// RAII bracket around one launch; inert unless profiling is on and the
-// stream is not being captured into a graph
-struct Prof {
-  const char *name;
-  cudaStream_t st;
-  cudaEvent_t a = nullptr;
-  Prof(const char *n, cudaStream_t s) : name(n), st(s) {
-    if (!g_prof) return;
-    cudaStreamCaptureStatus cs;
-    if (cudaStreamIsCapturing(st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return;
-    cudaEventCreate(&a);
-    cudaEventRecord(a, st);
-  }
-  ~Prof() {
-    if (!a) return;
-    cudaEvent_t b;
-    cudaEventCreate(&b);
-    cudaEventRecord(b, st);
-    g_prof_recs.push_back({name, a, b});
-  }
-};
-#define XK_PROF(name) Prof xk_prof_(name, st)
+Prof::Prof(const char *n, cudaStream_t s) : name(n), st(s) {
+  if (!g_prof) return;
+  cudaStreamCaptureStatus cs;
+  if (cudaStreamIsCapturing(st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return;
+  cudaEventCreate(&a);
+  cudaEventRecord(a, st);
+}
+Prof::~Prof() {
+  if (!a) return;
+  cudaEvent_t b;
+  cudaEventCreate(&b);
+  cudaEventRecord(b, st);
+  g_prof_recs.push_back({name, a, b});
+}
 
-#define XK_LAUNCHED() (g_launches.fetch_add(1), cudaGetLastError())
+cudaError_t launched() {
+  g_launches.fetch_add(1);
+  return cudaGetLastError();
+}
+
 #define FULL 0xffffffffu
 
-__host__ __device__ inline size_t sidx(int j, int d, int l, int D, int Ns) {
-  return ((size_t)j * D + d) * Ns + l;
-}
 __device__ inline size_t dtri(int n) { return (size_t)n * (n - 1) / 2; }
 
 // md_simulation_x.c:70-81 with md_periodic_image_count_x (:858-865): shift
@@ -1784,11 +1777,16 @@ __global__ void k_recip_tables(const int4 *__restrict__ cols, int ncol, const do
 //   sum_nz c(n) Im(e^{i theta} conj S(n)) = Im(e_xy U),   z part Im(e_xy V),
 // where for each pair +-nz:  e_z(+)W(+) + e_z(-)W(-) = c A + i s B  and
 // nz (e_z(+)W(+) - e_z(-)W(-)) = nz (c B + i s A).
-template <int NS>
+//
+// WITH_E also writes the particle's share of the slice energy,
+//   e[j*Ns + l] = sum_n c(n) Re(e^{i theta} conj S(n)) - e0 = Re(sum_col e_xy U) - e0,
+// with e0 = sum_n c(n), so that sum_l e = sum_n c(n) (|S(n)|^2 - N).
+template <int NS, bool WITH_E = false>
 __global__ void __launch_bounds__(128) k_recip_force(Geo g, const double2 *__restrict__ ph,
                                                      const int4 *__restrict__ cols, int ncol,
                                                      const double2 *__restrict__ T, double scale,
-                                                     double *__restrict__ f) {
+                                                     double *__restrict__ f, double *__restrict__ e = nullptr,
+                                                     double e0 = 0.0) {
   constexpr int NT = 4 * NS + 1;
   extern __shared__ double sm[];
   double2 *sT = (double2 *)sm;
@@ -1802,7 +1800,7 @@ __global__ void __launch_bounds__(128) k_recip_force(Geo g, const double2 *__res
   const double2 *pz = ph + (((size_t)j * 3 + 2) * (NS + 1)) * g.Ns + l;
 #pragma unroll
   for (int n = 1; n <= NS; ++n) ez[n] = pz[(size_t)n * g.Ns];
-  double Fx = 0, Fy = 0, Fz = 0;
+  double Fx = 0, Fy = 0, Fz = 0, Er = 0;
   for (int ci = 0; ci < ncol; ++ci) {
     const int4 c = cols[ci];
     const double2 exy = cmul(phase_at(ph, g, NS, j, 0, c.x, l), phase_at(ph, g, NS, j, 1, c.y, l));
@@ -1822,7 +1820,9 @@ __global__ void __launch_bounds__(128) k_recip_force(Geo g, const double2 *__res
     Fx = fma((double)c.x, Tm, Fx);
     Fy = fma((double)c.y, Tm, Fy);
     Fz += Zm;
+    if (WITH_E) Er += fma(exy.x, Ur, -exy.y * Ui);  // Re(e_xy U)
   }
+  if (WITH_E) e[(size_t)j * g.Ns + l] = Er - e0;
   f[sidx(j, 0, l, 3, g.Ns)] += scale * Fx * g.inv_box[0];
   f[sidx(j, 1, l, 3, g.Ns)] += scale * Fy * g.inv_box[1];
   f[sidx(j, 2, l, 3, g.Ns)] += scale * Fz * g.inv_box[2];
@@ -1860,6 +1860,8 @@ cudaError_t recip_setup(const Geo &g, int ns, double alpha, double qs, Recip &r,
   }
   r.nsum = ns;
   r.nk = nk;
+  r.csum = 0;
+  for (double c : coef) r.csum += c;
   cudaError_t e = cudaMemcpyAsync(r.coef, coef.data(), sizeof(double) * nk, cudaMemcpyHostToDevice, st);
   if (e != cudaSuccess) return e;
   e = cudaMemcpyAsync(r.kvec, cd.data(), sizeof(int4) * cd.size(), cudaMemcpyHostToDevice, st);
@@ -1933,7 +1935,39 @@ cudaError_t recip_force(const Geo &g, const Recip &r, const double *x, double in
     {
       XK_PROF("recip_force");
       kf<<<grid, 128, smem, st>>>(g, (const double2 *)r.phase, (const int4 *)r.kvec, nc,
-                                  (const double2 *)r.T, 4 * M_PI * inv_mP, f);
+                                  (const double2 *)r.T, 4 * M_PI * inv_mP, f, nullptr, 0.0);
+    }
+  });
+  return XK_LAUNCHED();
+}
+
+cudaError_t recip_force_energy(const Geo &g, const Recip &r, const double *x, double scale, double *f,
+                               double *e, cudaStream_t st) {
+  if (g.D != 3) return cudaErrorInvalidValue;
+  cudaError_t err = structure_factors(g, r, x, st);
+  if (err != cudaSuccess) return err;
+  const int nc = ncols(r.nsum);
+  const double e0 = r.csum;
+  const size_t smem = sizeof(double2) * nc * (4 * r.nsum + 1);
+  dim3 tgrid((nc + 7) / 8, g.P), tblk(r.nsum + 1, 8);
+  dim3 grid((g.N + 127) / 128, g.P);
+  DISPATCH_NS(r.nsum, {
+    {
+      XK_PROF("recip_tables");
+      k_recip_tables<NS><<<tgrid, tblk, 0, st>>>((const int4 *)r.kvec, nc, (const double2 *)r.S, r.coef,
+                                                 r.nk, (double2 *)r.T);
+    }
+    auto kf = k_recip_force<NS, true>;
+    static bool opted = false;
+    if (!opted) {
+      cudaError_t ea = cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+      if (ea != cudaSuccess) return ea;
+      opted = true;
+    }
+    {
+      XK_PROF("recip_force_energy");
+      kf<<<grid, 128, smem, st>>>(g, (const double2 *)r.phase, (const int4 *)r.kvec, nc, (const double2 *)r.T,
+                                  4 * M_PI * scale, f, e, e0);
     }
   });
   return XK_LAUNCHED();
@@ -2086,6 +2120,46 @@ double fp64_peak_tflops(cudaStream_t st) {
   for (int rep = 0; rep < 3; ++rep) {
     cudaEventRecord(a, st);
     k_dfma_probe<<<blocks, threads, 0, st>>>(out, iters, 0.999999, 1e-7);
+    cudaEventRecord(b, st);
+    cudaEventSynchronize(b);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, a, b);
+    const double tf = 2.0 * 8 * iters * (double)blocks * threads / (ms * 1e-3) / 1e12;
+    if (tf > best) best = tf;
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaFreeAsync(out, st);
+  cudaStreamSynchronize(st);
+  return cudaGetLastError() == cudaSuccess ? best : -1;
+}
+
+// FP32 pipe probe, the same shape: the roofline denominator of the FP32
+// kernels of the mixed and learned forms
+__global__ void k_ffma_probe(float *out, int iters, float a, float b) {
+  float x0 = threadIdx.x * 1e-3f, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3;
+  float x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+  for (int i = 0; i < iters; ++i) {
+    x0 = fmaf(x0, a, b); x1 = fmaf(x1, a, b); x2 = fmaf(x2, a, b); x3 = fmaf(x3, a, b);
+    x4 = fmaf(x4, a, b); x5 = fmaf(x5, a, b); x6 = fmaf(x6, a, b); x7 = fmaf(x7, a, b);
+  }
+  out[(size_t)blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+}
+
+double fp32_peak_tflops(cudaStream_t st) {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int blocks = sms * 8, threads = 256, iters = 65536;
+  float *out = nullptr;
+  if (cudaMallocAsync(&out, sizeof(float) * blocks * threads, st) != cudaSuccess) return -1;
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  double best = 0;
+  for (int rep = 0; rep < 3; ++rep) {
+    cudaEventRecord(a, st);
+    k_ffma_probe<<<blocks, threads, 0, st>>>(out, iters, 0.999999f, 1e-7f);
     cudaEventRecord(b, st);
     cudaEventSynchronize(b);
     float ms = 0;

@@ -29,6 +29,8 @@ struct Geo {
   double inv_box[3];
   XK_HD size_t slots() const { return (size_t)P * D * Ns; }
 };
+// slot of coordinate d of particle l in bead slice j
+XK_HD inline size_t sidx(int j, int d, int l, int D, int Ns) { return ((size_t)j * D + d) * Ns + l; }
 
 inline int pad_n(int N) { return (N + 3) & ~3; }
 inline size_t tri(int n) { return (size_t)n * (n - 1) / 2; }  // row start, 1-based n
@@ -36,12 +38,26 @@ inline size_t ntri(int n) { return (size_t)n * (n + 1) / 2; }
 
 // count of kernels launched by this library (for launch accounting)
 uint64_t launch_count();
+// counts one launch and returns cudaGetLastError()
+cudaError_t launched();
+#define XK_LAUNCHED() ::xk::launched()
+// RAII bracket around one launch for the live per-kernel timing; inert
+// unless profiling is on and the stream is not being captured into a graph
+struct Prof {
+  const char *name;
+  cudaStream_t st;
+  cudaEvent_t a = nullptr;
+  Prof(const char *n, cudaStream_t s);
+  ~Prof();
+};
+#define XK_PROF(name) ::xk::Prof xk_prof_(name, st)
 
 // live per-kernel timing with CUDA events; report is "name total_ms launches;..."
 void profile_enable(bool on);
 std::string profile_report();
 // measured FP64 FMA throughput of this GPU in TFLOP/s (-1 on failure)
 double fp64_peak_tflops(cudaStream_t st);
+double fp32_peak_tflops(cudaStream_t st);
 
 // ---- layout conversion (host AoS records <-> device SoA) ----
 cudaError_t aos_to_soa(const Geo &g, const double *aos, double *x, double *v, double *f,
@@ -146,6 +162,7 @@ struct Recip {
   double *phase;       // [P][3][nsum+1][Ns] complex
   double *S;           // [P][nk] complex
   double *T;           // [P][columns][2 nsum + 1] complex force tables
+  double csum;         // sum of coef (host value, set by recip_setup)
 };
 size_t recip_phase_doubles(const Geo &g, int nsum);
 int recip_count(int nsum);
@@ -156,6 +173,12 @@ cudaError_t recip_force(const Geo &g, const Recip &r, const double *x, double in
                         double *f, cudaStream_t st);
 cudaError_t recip_energy(const Geo &g, const Recip &r, const double *x, double *acc,
                          double *scratch, cudaStream_t st);
+
+// reciprocal-space forces plus per-particle energies
+//   e[j*Ns + l] = sum_k c(k) (Re(e^{i k x_l} conj S_j(k)) - 1)  (half space)
+// so that sum_l e = the slice's reciprocal energy; forces scaled as recip_force
+cudaError_t recip_force_energy(const Geo &g, const Recip &r, const double *x, double scale, double *f,
+                               double *e, cudaStream_t st);
 
 // ---- mixed-precision form: FP32 arithmetic, compensated accumulation ----
 cudaError_t pair_force32(const Geo &g, const PairPrm &p, const double *x, const double *m,

@@ -570,6 +570,11 @@ double md_gb300_fp64_peak_x(void) {
   return xk::fp64_peak_tflops(stream());
 }
 
+double md_gb300_fp32_peak_x(void) {
+  if (ensure_device() != 0) return -1;
+  return xk::fp32_peak_tflops(stream());
+}
+
 int md_gb300_release_simulation_x(md_simulation_t_x *sim) {
   if (!sim) return fail(MD_GB_ERR_ARG, "NULL simulation");
   XMD_TRY(sim_to_host(sim, false));

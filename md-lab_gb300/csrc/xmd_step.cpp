@@ -88,19 +88,19 @@ static int check_plain(md_pimd_t_x *p) {
   return 0;
 }
 
-static int check_image(const SimDev *sd, int image) {
+int xmd::check_image(const SimDev *sd, int image) {
   if (image && (sd->geo.box[0] <= 0 || (D > 1 && sd->geo.box[1] <= 0) || (D > 2 && sd->geo.box[2] <= 0)))
     return fail(MD_GB_ERR_ARG, "minimum image requested without a positive box");
   return 0;
 }
 
-static double *scratch_for(SimDev *sd, size_t doubles, int *rc) {
+double *xmd::scratch_for(SimDev *sd, size_t doubles, int *rc) {
   double *p = nullptr;
   *rc = scratch(sd, doubles, &p);
   return p;
 }
 
-static size_t general_scratch(const xk::Geo &g) {
+size_t xmd::general_scratch(const xk::Geo &g) {
   size_t n = xk::pair_scratch_doubles(g);
   const size_t e = xk::exch_scratch_doubles(g);
   if (e > n) n = e;
@@ -318,7 +318,9 @@ int md_pimd_calc_trap_force_x(md_pimd_t_x *pimd, md_trap_force_t_x tf) {
   return 0;
 }
 
-static int ewald_tables(md_pimd_t_x *pimd, SimDev *sd, PimdDev *pd) {
+}  // extern "C"
+
+int xmd::ewald_tables(md_pimd_t_x *pimd, SimDev *sd, PimdDev *pd) {
   const int ns = md_coulomb_n_sum_x;
   const double a = md_coulomb_truc_x, qs = md_coulomb_strength_x;
   if (ns < 1 || ns > 11) return fail(MD_GB_ERR_UNSUPPORTED, "Ewald n_sum %d (1..11 supported)", ns);
@@ -343,6 +345,7 @@ static int ewald_tables(md_pimd_t_x *pimd, SimDev *sd, PimdDev *pd) {
   pd->rc_alpha = a;
   pd->rc_qs = qs;
   pd->rc_nk = nk;
+  pd->rc_csum = r.csum;
   for (int d = 0; d < 3; ++d) pd->rc_box[d] = g.box[d];
   (void)pimd;
   return 0;
@@ -351,7 +354,7 @@ static int ewald_tables(md_pimd_t_x *pimd, SimDev *sd, PimdDev *pd) {
 // library-wide arithmetic of the pair and Ewald forces (md_gb300_x.h)
 static int g_precision = MD_GB_PRECISION_FP64;
 
-static xk::Recip recip_of(PimdDev *pd) {
+xk::Recip xmd::recip_of(PimdDev *pd) {
   xk::Recip r{};
   r.nsum = pd->rc_nsum;
   r.nk = pd->rc_nk;
@@ -360,10 +363,11 @@ static xk::Recip recip_of(PimdDev *pd) {
   r.phase = pd->rc_phase.as<double>();
   r.S = pd->rc_S.as<double>();
   r.T = pd->rc_T.as<double>();
+  r.csum = pd->rc_csum;
   return r;
 }
 
-static xk::PairPrm pair_params(int kind) {
+xk::PairPrm xmd::pair_params(int kind) {
   xk::PairPrm p{};
   p.kind = kind;
   p.g = md_gaussian_strength_x;
@@ -377,13 +381,15 @@ static xk::PairPrm pair_params(int kind) {
 
 // image shifts around the minimum image that can fall inside rcut:
 // |m - k L| < rcut with |m| <= L/2 needs |k| < 1/2 + rcut/L
-static void ewald_shifts(xk::PairPrm &p, const xk::Geo &g) {
+void xmd::ewald_shifts(xk::PairPrm &p, const xk::Geo &g) {
   for (int d = 0; d < 3; ++d) {
     p.kmax[d] = 0;
     if (g.box[d] > 0) p.kmax[d] = (int)ceil(0.5 + p.rcut / g.box[d]) - 1;
     if (p.kmax[d] < 0) p.kmax[d] = 0;
   }
 }
+
+extern "C" {
 
 int md_pimd_calc_pair_force_x(md_pimd_t_x *pimd, md_pair_force_t_x pf) {
   const int kind = pair_kind_of((const void *)pf, false);
@@ -401,12 +407,15 @@ int md_pimd_calc_pair_force_x(md_pimd_t_x *pimd, md_pair_force_t_x pf) {
   xk::PairPrm prm = pair_params(kind);
   ewald_shifts(prm, sd->geo);
   const bool mixed = g_precision == MD_GB_PRECISION_MIXED;
+  int learned = 0;
   if (kind == xk::PAIR_EWALD_REAL) {
     if (prm.kmax[0] > 1 || prm.kmax[1] > 1 || prm.kmax[2] > 1)
       return fail(MD_GB_ERR_UNSUPPORTED, "Ewald alpha*L below %.1f (images beyond the neighbouring boxes)",
                   2 * EWALD_XCUT / 3);
     if (!sd->uniform_mass) return fail(MD_GB_ERR_UNSUPPORTED, "structure-factor Ewald needs equal bead masses");
     XMD_TRY(ewald_tables(pimd, sd, pd));
+    learned = learned_mode(pimd, true);
+    if (learned == 1) return learned_pair_force(pimd, sd, pd, prm, scr);
     const double inv_mP = 1.0 / (sd->mass0 * pimd->P);
     if (mixed)
       XMD_CUDA(xk::recip_force32(sd->geo, recip_of(pd), sd->x.as<double>(), inv_mP, sd->f.as<double>(), st));
@@ -417,6 +426,7 @@ int md_pimd_calc_pair_force_x(md_pimd_t_x *pimd, md_pair_force_t_x pf) {
     XMD_CUDA(xk::pair_force32(sd->geo, prm, sd->x.as<double>(), sd->m.as<double>(), sd->f.as<double>(), scr, st));
   else
     XMD_CUDA(xk::pair_force(sd->geo, prm, sd->x.as<double>(), sd->m.as<double>(), sd->f.as<double>(), scr, st));
+  if (learned == 2) XMD_TRY(learned_judge_step(pimd, sd, pd));
   return 0;
 }
 
@@ -558,7 +568,11 @@ int md_pimd_calc_pair_energy_x(md_pimd_t_x *pimd, md_pair_energy_t_x pe, md_stat
   cudaStream_t st = stream();
   if (kind == xk::PAIR_EWALD_REAL) {
     XMD_TRY(ewald_tables(pimd, sd, pd));
-    XMD_CUDA(xk::recip_energy(sd->geo, recip_of(pd), sd->x.as<double>(), acc, scr, st));
+    if (learned_mode(pimd, false) == 1) {
+      XMD_TRY(learned_recip_energy(pimd, sd, acc, scr));
+    } else {
+      XMD_CUDA(xk::recip_energy(sd->geo, recip_of(pd), sd->x.as<double>(), acc, scr, st));
+    }
   }
   xk::PairPrm prm = pair_params(kind);
   ewald_shifts(prm, sd->geo);

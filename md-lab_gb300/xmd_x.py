@@ -26,6 +26,7 @@ LIBDIR = os.path.join(HERE, "lib")
 
 _d, _i, _vp = C.c_double, C.c_int, C.c_void_p
 _dp = C.POINTER(C.c_double)
+_fp = C.POINTER(C.c_float)
 
 
 def lib_path(D, L):
@@ -146,10 +147,25 @@ class XLib:
                 "md_gb300_profile_x": (_i, [_i]),
                 "md_gb300_profile_report_x": (_i, [C.c_char_p, _i]),
                 "md_gb300_fp64_peak_x": (_d, []),
+                "md_gb300_fp32_peak_x": (_d, []),
                 "md_gb300_set_device_x": (_i, [_i]),
                 "md_gb300_set_precision_x": (_i, [_i]),
                 "md_gb300_get_precision_x": (_i, []),
                 "md_gb300_pair_force_noalloc_x": (_i, [_vp, _vp, _vp, _vp, _i, _i, _i, _dp, _vp]),
+                "md_gb300_tc_selftest_x": (_i, [_dp]),
+                "md_gb300_ewald_model_nparam_x": (_i, []),
+                "md_gb300_ewald_model_create_x": (_i, [C.POINTER(_vp), pp, _i, C.c_long, C.c_uint]),
+                "md_gb300_ewald_model_free_x": (None, [_vp]),
+                "md_gb300_ewald_model_collect_x": (_i, [_vp, pp]),
+                "md_gb300_ewald_model_train_x": (_i, [_vp, _i, _i, _d, _dp]),
+                "md_gb300_ewald_model_attach_x": (_i, [pp, _vp, _i, _d, _d]),
+                "md_gb300_ewald_model_judge_x": (_i, [_vp, pp, _dp]),
+                "md_gb300_ewald_model_status_x": (_i, [_vp, C.POINTER(C.c_long), C.POINTER(_i), C.POINTER(_i), _dp]),
+                "md_gb300_ewald_model_params_x": (_i, [_vp, _fp, _i]),
+                "md_gb300_mlp_forward_x": (_i, [_vp, _fp, _i, _fp]),
+                "md_gb300_mlp_grad_x": (_i, [_vp, _fp, _fp, _fp, _i, _d, _d, _fp, _fp]),
+                "md_gb300_ewald_model_features_x": (_i, [_vp, pp, _fp, _fp]),
+                "md_gb300_ewald_model_desc_info_x": (_i, [_vp, _dp, _fp, _dp, _dp]),
             })
         for name, (res, args) in sig.items():
             fn = getattr(self.h, name)
@@ -323,3 +339,90 @@ def md_step(lib, s, dt, image=0, trap=None, pair=None, pbc=False):
     if pbc:
         ck(lib.md_periodic_boundary_x(s.sim), "periodic boundary")
     return 0
+
+
+class EwaldModel:
+    """The learned Ewald residual of one system (md_gb300_ewald_model_*_x)."""
+
+    def __init__(self, lib, system, nsum_cheap=3, capacity=16, seed=1):
+        self.lib, self.h = lib, C.c_void_p()
+        lib.check(lib.md_gb300_ewald_model_create_x(C.byref(self.h), system.pimd, nsum_cheap, capacity, seed),
+                  "model create")
+        self.N, self.P = system.N, system.P
+
+    def collect(self, system):
+        self.lib.check(self.lib.md_gb300_ewald_model_collect_x(self.h, system.pimd), "collect")
+
+    def train(self, steps, batch_tiles, lr):
+        loss = C.c_double()
+        self.lib.check(self.lib.md_gb300_ewald_model_train_x(self.h, steps, batch_tiles, lr, C.byref(loss)), "train")
+        return loss.value
+
+    def attach(self, system, judge_every=50, force_tol=1e-2, energy_tol=1e-4):
+        self.lib.check(self.lib.md_gb300_ewald_model_attach_x(system.pimd, self.h, judge_every, force_tol,
+                                                              energy_tol), "attach")
+
+    def detach(self, system):
+        self.lib.check(self.lib.md_gb300_ewald_model_attach_x(system.pimd, None, 0, 0.0, 0.0), "detach")
+
+    def judge(self, system):
+        out = (C.c_double * 4)()
+        self.lib.check(self.lib.md_gb300_ewald_model_judge_x(self.h, system.pimd, out), "judge")
+        return {"force_err": out[0], "energy_err": out[1], "force_err_truncated": out[2],
+                "energy_err_truncated": out[3]}
+
+    def status(self):
+        n, j, r = C.c_long(), C.c_int(), C.c_int()
+        last = (C.c_double * 4)()
+        self.lib.check(self.lib.md_gb300_ewald_model_status_x(self.h, C.byref(n), C.byref(j), C.byref(r), last))
+        return {"configurations": n.value, "judged": j.value, "reverted": bool(r.value), "last": list(last)}
+
+    def params(self, p=None):
+        import numpy as np
+        n = self.lib.md_gb300_ewald_model_nparam_x()
+        if p is None:
+            out = np.zeros(n, np.float32)
+            self.lib.check(self.lib.md_gb300_ewald_model_params_x(self.h, out.ctypes.data_as(_fp), 0))
+            return out
+        q = np.ascontiguousarray(p, np.float32)
+        assert q.size == n
+        self.lib.check(self.lib.md_gb300_ewald_model_params_x(self.h, q.ctypes.data_as(_fp), 1))
+
+    def forward(self, X):
+        import numpy as np
+        X = np.ascontiguousarray(X, np.float32)
+        Y = np.zeros((X.shape[0], 4), np.float32)
+        self.lib.check(self.lib.md_gb300_mlp_forward_x(self.h, X.ctypes.data_as(_fp), X.shape[0],
+                                                       Y.ctypes.data_as(_fp)), "forward")
+        return Y
+
+    def grad(self, X, V, T, we=1.0, wf=1.0):
+        import numpy as np
+        X, V, T = (np.ascontiguousarray(a, np.float32) for a in (X, V, T))
+        g = np.zeros(self.lib.md_gb300_ewald_model_nparam_x(), np.float32)
+        loss = np.zeros(2, np.float32)
+        self.lib.check(self.lib.md_gb300_mlp_grad_x(self.h, X.ctypes.data_as(_fp), V.ctypes.data_as(_fp),
+                                                    T.ctypes.data_as(_fp), X.shape[0], we, wf,
+                                                    g.ctypes.data_as(_fp), loss.ctypes.data_as(_fp)), "grad")
+        return g, loss
+
+    def features(self, system):
+        import numpy as np
+        F = np.zeros((self.N * self.P, 64), np.float32)
+        V = np.zeros((self.N * self.P, 12), np.float32)
+        self.lib.check(self.lib.md_gb300_ewald_model_features_x(self.h, system.pimd, F.ctypes.data_as(_fp),
+                                                                V.ctypes.data_as(_fp)), "features")
+        return F, V
+
+    def desc_info(self):
+        import numpy as np
+        rc = C.c_double()
+        B = np.zeros((128, 64), np.float32)
+        mu, sg = (C.c_double * 3)(), (C.c_double * 3)()
+        self.lib.check(self.lib.md_gb300_ewald_model_desc_info_x(self.h, C.byref(rc), B.ctypes.data_as(_fp), mu, sg))
+        return rc.value, B, list(mu), list(sg)
+
+    def free(self):
+        if self.h:
+            self.lib.md_gb300_ewald_model_free_x(self.h)
+            self.h = C.c_void_p()

@@ -47,8 +47,8 @@ def lib():
     global _LIB
     if _LIB is None:
         path = os.path.join(HERE, "liborc.so")
-        src = os.path.join(HERE, "xmd_oracle.c")
-        if not os.path.exists(path) or os.path.getmtime(path) < os.path.getmtime(src):
+        srcs = [os.path.join(HERE, f) for f in ("xmd_oracle.c", "xmd_oracle.h", "orc_learned.c")]
+        if not os.path.exists(path) or any(os.path.getmtime(path) < os.path.getmtime(f) for f in srcs):
             build()
         L = C.CDLL(path)
         d, i, vp = C.c_double, C.c_int, C.c_void_p
@@ -79,6 +79,12 @@ def lib():
             "orc_set_seed": (None, [C.c_uint]),
             "orc_random_uniform": (d, [d, d]),
             "orc_random_gaussian": (d, []),
+            "orc_mlp_nparam": (i, []),
+            "orc_bf16": (d, [d]),
+            "orc_desc_features": (None, [i, _dp, _dp, d, i, _dp, _dp, _dp, _dp, _dp]),
+            "orc_mlp_forward": (None, [i, _dp, _dp, i, _dp, _dp, _dp]),
+            "orc_mlp_loss": (d, [i, _dp, _dp, _dp, _dp, d, d, d, i]),
+            "orc_mlp_grad": (None, [i, _dp, _dp, _dp, _dp, d, d, d, i, _dp, _dp]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -154,3 +160,41 @@ def fast_force_VB(sim, N, P, beta, vi, omegaP, image, ENk, VBN):
                                  ptr(G), ptr(tmpV))
     assert rc == 0
     return G.reshape(N, N), tmpV
+
+
+# ---- learned residual (orc_learned.c) ----
+def mlp_forward(X, p, bf=1):
+    X = np.ascontiguousarray(X, np.float64)
+    p = np.ascontiguousarray(p, np.float64)
+    Y = np.zeros((X.shape[0], 4))
+    lib().orc_mlp_forward(X.shape[0], ptr(X), ptr(p), bf, ptr(Y), None, None)
+    return Y
+
+
+def mlp_loss(X, V, T, p, we=1.0, wf=1.0, inv_rows=None, bf=0):
+    X, V, T, p = (np.ascontiguousarray(a, np.float64) for a in (X, V, T, p))
+    inv = 1.0 / X.shape[0] if inv_rows is None else inv_rows
+    return lib().orc_mlp_loss(X.shape[0], ptr(X), ptr(V), ptr(T), ptr(p), we, wf, inv, bf)
+
+
+def mlp_grad(X, V, T, p, we=1.0, wf=1.0, inv_rows=None, bf=0):
+    X, V, T, p = (np.ascontiguousarray(a, np.float64) for a in (X, V, T, p))
+    inv = 1.0 / X.shape[0] if inv_rows is None else inv_rows
+    g = np.zeros(lib().orc_mlp_nparam())
+    loss = np.zeros(2)
+    lib().orc_mlp_grad(X.shape[0], ptr(X), ptr(V), ptr(T), ptr(p), we, wf, inv, bf, ptr(g), ptr(loss))
+    return g, loss
+
+
+def desc_features(x, box, rc, basis, vmu, vsig, nb=128):
+    """x: positions [N][3] of one bead slice"""
+    x = np.ascontiguousarray(x, np.float64)
+    N = x.shape[0]
+    L = np.ascontiguousarray(box, np.float64)
+    B = np.ascontiguousarray(basis, np.float64)
+    mu = np.ascontiguousarray(vmu, np.float64)
+    sg = np.ascontiguousarray(vsig, np.float64)
+    F = np.zeros((N, 64))
+    V = np.zeros((N, 9))
+    lib().orc_desc_features(N, ptr(x), ptr(L), rc, nb, ptr(B), ptr(mu), ptr(sg), ptr(F), ptr(V))
+    return F, V
