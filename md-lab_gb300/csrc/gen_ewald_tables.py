@@ -13,9 +13,15 @@ double-precision Horner evaluation against mpmath and records it in the
 header.  Absolute accuracy is what the sums need: both functions are at most
 1 and each image's contribution scales with them.
 
-Run:  python gen_ewald_tables.py > xmd_ewald_tables.h   (needs mpmath)
+The FP32 kernels use one global approximation instead (no table lookups):
+h(x) = exp(-x^2) (2x/sqrt(pi) + erfcx(x)) with erfcx(x) = exp(x^2) erfc(x)
+~ t P(t), t = 1/(1 + x/2), P of degree EW32_DEG, fitted here by least
+squares in relative error on Chebyshev nodes of [0, EW32_XFIT].
+
+Run:  python gen_ewald_tables.py > xmd_ewald_tables.h   (needs mpmath, numpy)
 """
 import mpmath as mp
+import numpy as np
 
 mp.mp.dps = 40
 W, NINT, DEG = 0.25, 25, 12
@@ -59,6 +65,27 @@ def table(f):
     return rows, float(worst)
 
 
+EW32_C, EW32_DEG, EW32_XFIT = 0.5, 8, 4.7
+
+
+def erfcx(x):
+    return mp.erfc(x) * mp.e ** (x * x)
+
+
+def erfcx_fit():
+    """coefficients c_k of erfcx(x) ~ t sum_k c_k t^k, t = 1/(1 + C x)"""
+    x = EW32_XFIT * (1 - np.cos(np.linspace(0, np.pi, 3000))) / 2
+    t = 1 / (1 + EW32_C * x)
+    y = np.array([float(erfcx(mp.mpf(float(v)))) for v in x])
+    A = np.vstack([t ** (k + 1) for k in range(EW32_DEG + 1)]).T
+    c, *_ = np.linalg.lstsq(A / y[:, None], np.ones_like(y), rcond=None)
+    xe = np.linspace(0, EW32_XFIT, 2001)
+    te = 1 / (1 + EW32_C * xe)
+    ye = np.array([float(erfcx(mp.mpf(float(v)))) for v in xe])
+    fit = np.vstack([te ** (k + 1) for k in range(EW32_DEG + 1)]).T @ c
+    return [float(v) for v in c], float(np.max(np.abs(fit - ye) / ye))
+
+
 def emit(name, rows):
     """An initializer macro, usable for host arrays and __constant__ arrays."""
     out = [f"#define {name}_INIT {{ \\"]
@@ -87,3 +114,12 @@ if __name__ == "__main__":
 """)
     print(emit("EW_H", th))
     print(emit("EW_ERFC", te))
+    c32, e32 = erfcx_fit()
+    print(f"""
+// FP32 form: erfcx(x) = exp(x^2) erfc(x) ~ t (c0 + c1 t + ... + c{EW32_DEG} t^{EW32_DEG}),
+// t = 1/(1 + {EW32_C} x), least squares in relative error on [0, {EW32_XFIT}]:
+// max relative error {e32:.2e} (double evaluation)
+#define EW32_C {EW32_C!r}
+#define EW32_DEG {EW32_DEG}
+#define EW32_XFIT {EW32_XFIT!r}
+#define EW32_ERFCX_INIT {{ {", ".join(repr(v) for v in c32)} }}""")

@@ -68,7 +68,12 @@ struct SimDev {
 struct PimdDev {
   bool valid = false;  // ENk / ENk2 / VBN / Eint on the device authoritative
   DevBuf ENk, ENk2, Eint, VBN, tmpV, G;
-  DevBuf rec;  // weights of the factorised recursions
+  DevBuf linkt;  // N x N bead-P -> bead-1 springs (scratch of the ENk fill)
+  DevBuf rec;  // weights of the forward and backward recursions (two halves)
+  // tmpV (backward recursion) computed by the last md_pimd_fill_VB_x from
+  // the current ENk with these beta and vi
+  bool tmpv_fresh = false;
+  double tmpv_beta = 0, tmpv_vi = 0;
   // Ewald reciprocal tables, rebuilt when the parameters change
   DevBuf rc_coef, rc_cols, rc_phase, rc_S, rc_T;
   int rc_nsum = -1;

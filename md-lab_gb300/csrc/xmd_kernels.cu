@@ -513,18 +513,23 @@ __device__ inline double spring2(Geo g, const double *x, int ja, int la, int jb,
   return s;
 }
 
-// interior ring springs of particle l and the closing spring P -> 1
+// interior ring springs of particle l and the closing spring P -> 1: one
+// warp per particle, lanes over the beads, fixed-order warp sum
 template <int D>
 __global__ void k_eint(Geo g, const double *__restrict__ x, const double *__restrict__ m,
                        double w2, int image, double *Eint, double *ENk) {
-  const int l = blockIdx.x * blockDim.x + threadIdx.x;
+  const int l = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
   if (l >= g.N) return;
   double res = 0;
-  for (int j = 0; j + 1 < g.P; ++j)
+  for (int j = lane; j + 1 < g.P; j += 32)
     res += 0.5 * m[(size_t)j * g.Ns + l] * w2 * spring2<D>(g, x, j, l, j + 1, l, image);
-  Eint[l] = res;
-  const int jP = g.P - 1;
-  ENk[dtri(l + 1)] = res + 0.5 * m[(size_t)jP * g.Ns + l] * w2 * spring2<D>(g, x, jP, l, 0, l, image);
+  res = warp_sum(res);
+  if (lane == 0) {
+    Eint[l] = res;
+    const int jP = g.P - 1;
+    ENk[dtri(l + 1)] = res + 0.5 * m[(size_t)jP * g.Ns + l] * w2 * spring2<D>(g, x, jP, l, 0, l, image);
+  }
 }
 
 // spring between bead P of particle a and bead 1 of particle b (0-based),
@@ -536,25 +541,34 @@ __device__ inline double link(Geo g, const double *x, const double *m, double w2
   return 0.5 * m[(size_t)jP * g.Ns + a] * w2 * spring2<D>(g, x, jP, a, 0, b, image);
 }
 
+// every such spring: lt[a*N + b] = link(a, b), one thread per (a, b)
+template <int D>
+__global__ void k_link_table(Geo g, const double *__restrict__ x, const double *__restrict__ m, double w2,
+                             int image, double *__restrict__ lt) {
+  const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (size_t)g.N * g.N) return;
+  const int a = (int)(t / g.N), b = (int)(t % g.N);
+  lt[t] = link<D>(g, x, m, w2, a, b, image);
+}
+
 // one warp per particle l (1-based row l >= 2): E_l^(k) for k = 2..l as an
 // inclusive scan of the increments
 //   Eint[l-k+1] - link(l, l-k+2) + link(l-k+1, l-k+2) + link(l, l-k+1)
-template <int D>
-__global__ void k_enk_rows(Geo g, const double *__restrict__ x, const double *__restrict__ m,
-                           double w2, int image, const double *__restrict__ Eint,
+// (links read from the table lt)
+__global__ void k_enk_rows(int N, const double *__restrict__ lt, const double *__restrict__ Eint,
                            double *__restrict__ ENk) {
   const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   const int l = w + 2;  // 1-based
-  if (l > g.N) return;
+  if (l > N) return;
   double carry = ENk[dtri(l)];
+  const double *rl = lt + (size_t)(l - 1) * N;
   for (int k0 = 2; k0 <= l; k0 += 32) {
     const int k = k0 + lane;
     double inc = 0;
     if (k <= l) {
       const int c = l - k + 1, b = l - k + 2;  // 1-based
-      inc = Eint[c - 1] - link<D>(g, x, m, w2, l - 1, b - 1, image) +
-            link<D>(g, x, m, w2, c - 1, b - 1, image) + link<D>(g, x, m, w2, l - 1, c - 1, image);
+      inc = Eint[c - 1] - rl[b - 1] + lt[(size_t)(c - 1) * N + (b - 1)] + rl[c - 1];
     }
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -568,17 +582,23 @@ __global__ void k_enk_rows(Geo g, const double *__restrict__ x, const double *__
 }
 
 cudaError_t fill_enk(const Geo &g, const double *x, const double *m, double w2, int image,
-                     double *Eint, double *ENk, cudaStream_t st) {
+                     double *Eint, double *ENk, double *lt, cudaStream_t st) {
   {
     XK_PROF("eint");
-    DISPATCH_D(g.D, k_eint<D><<<cdiv(g.N, 128), 128, 0, st>>>(g, x, m, w2, image, Eint, ENk));
+    DISPATCH_D(g.D, k_eint<D><<<cdiv((size_t)g.N * 32, 256), 256, 0, st>>>(g, x, m, w2, image, Eint, ENk));
   }
   cudaError_t e = XK_LAUNCHED();
   if (e != cudaSuccess || g.N < 2) return e;
+  {
+    XK_PROF("link_table");
+    DISPATCH_D(g.D, k_link_table<D><<<cdiv((size_t)g.N * g.N, 256), 256, 0, st>>>(g, x, m, w2, image, lt));
+  }
+  e = XK_LAUNCHED();
+  if (e != cudaSuccess) return e;
   const size_t thr = (size_t)(g.N - 1) * 32;
   {
     XK_PROF("enk_rows");
-    DISPATCH_D(g.D, k_enk_rows<D><<<cdiv(thr, 256), 256, 0, st>>>(g, x, m, w2, image, Eint, ENk));
+    k_enk_rows<<<cdiv(thr, 256), 256, 0, st>>>(g.N, lt, Eint, ENk);
   }
   return XK_LAUNCHED();
 }
@@ -831,61 +851,121 @@ __device__ inline void norm2(double &m, int &e) {
   m = __longlong_as_double((b & ~(0x7ffLL << 52)) | (1022LL << 52));
 }
 
-__global__ void __launch_bounds__(TS_WARPS * 32) k_tri_solve(int N, double beta,
-                                                             const double *__restrict__ Mm,
-                                                             const int *__restrict__ Me,
-                                                             double *__restrict__ out,
-                                                             int backward) {
+// Block b solves direction first + b (0 forward, 1 backward) with the
+// weights (Mm[dir], Me[dir]) into out[dir]: launched with two blocks, the
+// forward and backward recursions run side by side on two SMs.
+struct TriJob {
+  const double *Mm[2];
+  const int *Me[2];
+  double *out[2];
+};
+
+// Extended-range dot product of row i of the weights with the unknowns over
+// columns [j0, j1), reduced over the warp: (am, E) with value am 2^E.  An
+// integer pass finds the largest term exponent E; the terms are then scaled
+// to 2^E by exponent arithmetic and summed with one FMA each.  Zero weights
+// (xi = 0 beyond k = 1) are skipped by their bit pattern.
+__device__ inline void ext_dot(const double *__restrict__ mr, const int *__restrict__ er, const double *Xm,
+                               const int *Xe, int j0, int j1, int lane, double &am, int &E) {
+  E = -2147483647;
+  for (int j = j0 + lane; j < j1; j += 32)
+    if (__double_as_longlong(mr[j]) != 0) {
+      const int te = er[j] + Xe[j];
+      E = te > E ? te : E;
+    }
+#pragma unroll
+  for (int o = 16; o; o >>= 1) {
+    const int oe = __shfl_xor_sync(FULL, E, o);
+    E = oe > E ? oe : E;
+  }
+  am = 0.0;
+  if (E != -2147483647)
+    for (int j = j0 + lane; j < j1; j += 32)
+      if (__double_as_longlong(mr[j]) != 0) am = fma(mr[j], scale2(Xm[j], er[j] + Xe[j] - E), am);
+  am = warp_sum(am);
+}
+
+// (pm, pe) += (am, E), both non-negative extended-range values; normalised
+__device__ inline void ext_acc(double &pm, int &pe, double am, int E) {
+  if (__double_as_longlong(am) != 0) {
+    if (__double_as_longlong(pm) == 0) {
+      pm = am;
+      pe = E;
+    } else {
+      const int mx = pe > E ? pe : E;
+      pm = scale2(pm, pe - mx) + scale2(am, E - mx);
+      pe = mx;
+    }
+  }
+  norm2(pm, pe);
+}
+
+// The chunks of TS_CHUNK rows are solved in order by warp 0.  Row i's sum
+// over the unknowns of earlier chunks is split: the part over all but the
+// previous chunk is computed by warps 1.. while warp 0 is still solving that
+// previous chunk (so it costs no time on the sequential path); the previous
+// chunk's 32 columns are added by all warps between the two solves.
+__global__ void __launch_bounds__(TS_WARPS * 32) k_tri_solve(int N, double beta, TriJob job, int first) {
+  const int backward = first + blockIdx.x;
+  const double *__restrict__ Mm = job.Mm[backward];
+  const int *__restrict__ Me = job.Me[backward];
+  double *__restrict__ out = job.out[backward];
   extern __shared__ double sh[];
-  double *Xm = sh;                      // N+1
-  double *Pm = Xm + N + 1;              // TS_CHUNK
-  int *Xe = (int *)(Pm + TS_CHUNK);     // N+1
-  int *Pe = Xe + N + 1;                 // TS_CHUNK
+  double *Xm = sh;                        // N+1
+  double *Pm = Xm + N + 1;                // 2 x TS_CHUNK (double buffer)
+  int *Xe = (int *)(Pm + 2 * TS_CHUNK);   // N+1
+  int *Pe = Xe + N + 1;                   // 2 x TS_CHUNK
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   if (threadIdx.x == 0) {
     Xm[0] = 0.5;
     Xe[0] = 1;
   }
   __syncthreads();
-  for (int i0 = 1; i0 <= N; i0 += TS_CHUNK) {
-    // known part: rows i0..i0+31 against columns 0..i0-1, two rows per warp.
-    // An integer pass finds the row's largest term exponent E; the terms are
-    // then scaled to 2^E by exponent arithmetic and summed with one FMA each.
-    for (int r = w; r < TS_CHUNK; r += TS_WARPS) {
-      const int i = i0 + r;
-      double am = 0.0;
-      int E = -2147483647;
-      if (i <= N) {
-        const double *mr = Mm + moff(i, 0);
-        const int *er = Me + moff(i, 0);
-        for (int j = lane; j < i0; j += 32) {
-          const int te = er[j] + Xe[j];
-          E = te > E ? te : E;
-        }
-#pragma unroll
-        for (int o = 16; o; o >>= 1) {
-          const int oe = __shfl_xor_sync(FULL, E, o);
-          E = oe > E ? oe : E;
-        }
-        for (int j = lane; j < i0; j += 32) am = fma(mr[j], scale2(Xm[j], er[j] + Xe[j] - E), am);
-      }
-      am = warp_sum(am);
-      if (lane == 0) {
-        int ae = E;
-        norm2(am, ae);
-        Pm[r] = am;
-        Pe[r] = ae;
-      }
+  // chunk 0: its rows against column 0
+  for (int r = w; r < TS_CHUNK; r += TS_WARPS) {
+    const int i = 1 + r;
+    double am = 0.0;
+    int E = 0;
+    if (i <= N) ext_dot(Mm + moff(i, 0), Me + moff(i, 0), Xm, Xe, 0, 1, lane, am, E);
+    if (lane == 0) {
+      double pm = 0.0;
+      int pe = 0;
+      if (i <= N) ext_acc(pm, pe, am, E);
+      Pm[r] = pm;
+      Pe[r] = pe;
     }
-    __syncthreads();
-    // the chunk itself: lane r owns row i0+r; each step publishes one
-    // unknown and every later row adds its term (exponent arithmetic and
-    // one FMA on the sequential chain)
+  }
+  __syncthreads();
+  for (int i0 = 1, c = 0; i0 <= N; i0 += TS_CHUNK, ++c) {
+    const int buf = c & 1;
+    double *Pmc = Pm + buf * TS_CHUNK;
+    int *Pec = Pe + buf * TS_CHUNK;
+    // the previous chunk's columns [i0 - 32, i0)
+    if (c > 0) {
+      for (int r = w; r < TS_CHUNK; r += TS_WARPS) {
+        const int i = i0 + r;
+        if (i > N) continue;  // warp-uniform
+        double am;
+        int E;
+        ext_dot(Mm + moff(i, 0), Me + moff(i, 0), Xm, Xe, i0 - TS_CHUNK, i0, lane, am, E);
+        if (lane == 0) {
+          double pm = Pmc[r];
+          int pe = Pec[r];
+          ext_acc(pm, pe, am, E);
+          Pmc[r] = pm;
+          Pec[r] = pe;
+        }
+      }
+      __syncthreads();
+    }
     if (w == 0) {
+      // lane r owns row i0+r; each step publishes one unknown and every
+      // later row adds its term (exponent arithmetic and one FMA on the
+      // sequential chain)
       const int i = i0 + lane;
       const bool own = i <= N;
-      double am = own ? Pm[lane] : 0.0;
-      int ae = own ? Pe[lane] : 0;
+      double am = own ? Pmc[lane] : 0.0;
+      int ae = own ? Pec[lane] : 0;
       double mm[TS_CHUNK];
       int me[TS_CHUNK];
 #pragma unroll
@@ -914,6 +994,23 @@ __global__ void __launch_bounds__(TS_WARPS * 32) k_tri_solve(int N, double beta,
           am = fma(mm[s], scale2(xm, te - ae), am);
         }
       }
+    } else {
+      // next chunk's rows against the columns solved before this chunk
+      const int n0 = i0 + TS_CHUNK;
+      for (int r = w - 1; r < TS_CHUNK; r += TS_WARPS - 1) {
+        const int i = n0 + r;
+        if (i > N) break;  // warp-uniform; later rows are out of range too
+        double am;
+        int E;
+        ext_dot(Mm + moff(i, 0), Me + moff(i, 0), Xm, Xe, 0, i0, lane, am, E);
+        if (lane == 0) {
+          double pm = 0.0;
+          int pe = 0;
+          ext_acc(pm, pe, am, E);
+          Pm[(buf ^ 1) * TS_CHUNK + r] = pm;
+          Pe[(buf ^ 1) * TS_CHUNK + r] = pe;
+        }
+      }
     }
     __syncthreads();
   }
@@ -927,9 +1024,9 @@ __global__ void __launch_bounds__(TS_WARPS * 32) k_tri_solve(int N, double beta,
 // scratch: mantissas (ntri(N) doubles) then exponents (ntri(N) ints)
 size_t rec_scratch_doubles(int N) { return ntri(N) + (ntri(N) + 1) / 2 + 1; }
 
-static cudaError_t tri_solve(int N, double beta, const double *Mm, const int *Me, double *out,
-                             int backward, cudaStream_t st) {
-  const size_t smem = (sizeof(double) + sizeof(int)) * (N + 1 + TS_CHUNK) + 16;
+// directions first .. first + count - 1 of job
+static cudaError_t tri_solve(int N, double beta, const TriJob &job, int first, int count, cudaStream_t st) {
+  const size_t smem = (sizeof(double) + sizeof(int)) * (N + 1 + 2 * TS_CHUNK) + 16;
   static bool opted = false;
   if (!opted) {
     cudaError_t ea = cudaFuncSetAttribute(k_tri_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
@@ -937,10 +1034,21 @@ static cudaError_t tri_solve(int N, double beta, const double *Mm, const int *Me
     opted = true;
   }
   {
-    XK_PROF(backward ? "tv_solve" : "vb_solve");
-    k_tri_solve<<<1, TS_WARPS * 32, smem, st>>>(N, beta, Mm, Me, out, backward);
+    XK_PROF(count == 2 ? "vb_tv_solve" : (first ? "tv_solve" : "vb_solve"));
+    k_tri_solve<<<count, TS_WARPS * 32, smem, st>>>(N, beta, job, first);
   }
   return XK_LAUNCHED();
+}
+
+static TriJob tri_job(int N, double *rs_f, double *rs_b, double *VBN, double *tmpV) {
+  TriJob j{};
+  j.Mm[0] = rs_f;
+  j.Me[0] = (const int *)(rs_f + ntri(N));
+  j.out[0] = VBN;
+  j.Mm[1] = rs_b;
+  j.Me[1] = (const int *)(rs_b + ntri(N));
+  j.out[1] = tmpV;
+  return j;
 }
 
 cudaError_t fill_vb(int N, double beta, double vi, const double *ENk, double *VBN, double *rs,
@@ -953,7 +1061,7 @@ cudaError_t fill_vb(int N, double beta, double vi, const double *ENk, double *VB
   }
   cudaError_t e = XK_LAUNCHED();
   if (e != cudaSuccess) return e;
-  return tri_solve(N, beta, Mm, Me, VBN, 0, st);
+  return tri_solve(N, beta, tri_job(N, rs, nullptr, VBN, nullptr), 0, 1, st);
 }
 
 cudaError_t back_vb(int N, double beta, double vi, const double *ENk, double *tmpV, double *rs,
@@ -966,7 +1074,24 @@ cudaError_t back_vb(int N, double beta, double vi, const double *ENk, double *tm
   }
   cudaError_t e = XK_LAUNCHED();
   if (e != cudaSuccess) return e;
-  return tri_solve(N, beta, Mm, Me, tmpV, 1, st);
+  return tri_solve(N, beta, tri_job(N, nullptr, rs, nullptr, tmpV), 1, 1, st);
+}
+
+cudaError_t fill_vb_tv(int N, double beta, double vi, const double *ENk, double *VBN, double *tmpV, double *rs_f,
+                       double *rs_b, cudaStream_t st) {
+  {
+    XK_PROF("vb_weights");
+    k_vb_weights<<<cdiv((size_t)N * 32, 256), 256, 0, st>>>(N, beta, vi, ENk, rs_f, (int *)(rs_f + ntri(N)));
+  }
+  cudaError_t e = XK_LAUNCHED();
+  if (e != cudaSuccess) return e;
+  {
+    XK_PROF("tv_weights");
+    k_tv_weights<<<cdiv((size_t)N * 32, 256), 256, 0, st>>>(N, beta, vi, ENk, rs_b, (int *)(rs_b + ntri(N)));
+  }
+  e = XK_LAUNCHED();
+  if (e != cudaSuccess) return e;
+  return tri_solve(N, beta, tri_job(N, rs_f, rs_b, VBN, tmpV), 0, 2, st);
 }
 
 // connection probabilities G[l][j]: md_pimd_x.c:2660-2673
@@ -2287,9 +2412,29 @@ struct DF {
   __device__ inline double value() const { return (double)hi + (double)lo; }
 };
 
+// Real-space images farther than EW32_XCUT / alpha are left out of the FP32
+// form: there h(x) = erfc(x) + 2x exp(-x^2)/sqrt(pi) < 4e-9, far below the
+// resolution of the FP32 force sums.
+constexpr float EW32_XCUT = 4.6f;
+
+// h(alpha R) / R^3 in FP32 without tables: h(x) = exp(-x^2) (2x/sqrt(pi) +
+// erfcx(x)), erfcx(x) ~ t P(t), t = 1/(1 + x/2) (fit in xmd_ewald_tables.h,
+// relative error 2e-8 on [0, 4.7]); 1/R from rsqrt, exp from ex2
+__device__ __forceinline__ float ew_h32(float R2, float alpha) {
+  const float cc[EW32_DEG + 1] = EW32_ERFCX_INIT;
+  const float ri = rsqrtf(R2);
+  const float x = alpha * (R2 * ri);
+  const float t = __fdividef(1.f, fmaf((float)EW32_C, x, 1.f));
+  float q = cc[EW32_DEG];
+#pragma unroll
+  for (int k = EW32_DEG - 1; k >= 0; --k) q = fmaf(q, t, cc[k]);
+  const float e = __expf(-x * x);
+  return e * fmaf(x, 1.1283791670955126f, q * t) * (ri * ri * ri);
+}
+
 template <int D, int KIND>
 __device__ inline void pair_eval32(const PairPrm &p, const float *Lf, const float *iLf, const float *dx,
-                                   float *F, const float *tab, float alpha, float rc2, int kmax) {
+                                   float *F, float alpha, float rc2, int kmax) {
   if (KIND == PAIR_GAUSSIAN || KIND == PAIR_PERIODIC_GAUSSIAN) {
     float t[D], r2 = 0.f;
 #pragma unroll
@@ -2315,39 +2460,57 @@ __device__ inline void pair_eval32(const PairPrm &p, const float *Lf, const floa
 #pragma unroll
     for (int d = 0; d < D; ++d) F[d] = mult * t[d];
   } else if (KIND == PAIR_EWALD_REAL) {
-    float m[3];
+    // Minimum image m = dx - sh L; images t = m - k L.  Images beyond rc32
+    // (alpha rc32 <= EW32_XCUT) are left out.  When rc32 is at most the
+    // smallest box length only the 8 images with k_d in {0, sign(m_d)} can
+    // lie inside it (any other has a component of length >= L); otherwise
+    // all 27 with |k_d| <= 1 are tried.
+    float m[3], sg[3];
     int sh[3];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
       const float r = rintf(dx[d] * iLf[d]);
       sh[d] = (int)r;
       m[d] = fmaf(-r, Lf[d], dx[d]);
+      sg[d] = m[d] < 0.f ? -1.f : 1.f;
     }
     float F0 = 0.f, F1 = 0.f, F2 = 0.f;
-    for (int k0 = -kmax; k0 <= kmax; ++k0) {
-      if (abs(sh[0] + k0) > p.nsum) continue;
-      const float t0 = fmaf(-(float)k0, Lf[0], m[0]);
-      for (int k1 = -kmax; k1 <= kmax; ++k1) {
-        if (abs(sh[1] + k1) > p.nsum) continue;
-        const float t1 = fmaf(-(float)k1, Lf[1], m[1]);
-        for (int k2 = -kmax; k2 <= kmax; ++k2) {
-          if (abs(sh[2] + k2) > p.nsum) continue;
-          const float t2 = fmaf(-(float)k2, Lf[2], m[2]);
-          const float R2 = fmaf(t2, t2, fmaf(t1, t1, t0 * t0));
-          if (R2 >= rc2) continue;
-          const float ri = rsqrtf(R2);
-          const float xr = alpha * R2 * ri;
-          int iv = __float2int_rn(xr * (float)EW_INV_W);
-          iv = iv < EW_NINT - 1 ? iv : EW_NINT - 1;
-          const float u = fmaf(xr, 2.f * (float)EW_INV_W, -2.f * (float)iv);
-          const float *cf = tab + iv * (EW_DEG + 1);
-          float hv = cf[EW_DEG];
+    if (kmax == 0) {
 #pragma unroll
-          for (int q = EW_DEG - 1; q >= 0; --q) hv = fmaf(hv, u, cf[q]);
-          const float mult = hv * ri * ri * ri;
+      for (int c = 0; c < 8; ++c) {
+        const int k0 = c & 1, k1 = (c >> 1) & 1, k2 = c >> 2;
+        const float t0 = k0 ? fmaf(-sg[0], Lf[0], m[0]) : m[0];
+        const float t1 = k1 ? fmaf(-sg[1], Lf[1], m[1]) : m[1];
+        const float t2 = k2 ? fmaf(-sg[2], Lf[2], m[2]) : m[2];
+        const float R2 = fmaf(t2, t2, fmaf(t1, t1, t0 * t0));
+        bool ok = R2 < rc2;
+        if (p.nsum < 2)
+          ok = ok && abs(sh[0] + k0 * (int)sg[0]) <= p.nsum && abs(sh[1] + k1 * (int)sg[1]) <= p.nsum &&
+               abs(sh[2] + k2 * (int)sg[2]) <= p.nsum;
+        if (ok) {
+          const float mult = ew_h32(R2, alpha);
           F0 = fmaf(t0, mult, F0);
           F1 = fmaf(t1, mult, F1);
           F2 = fmaf(t2, mult, F2);
+        }
+      }
+    } else {
+      for (int k0 = -kmax; k0 <= kmax; ++k0) {
+        if (abs(sh[0] + k0) > p.nsum) continue;
+        const float t0 = fmaf(-(float)k0, Lf[0], m[0]);
+        for (int k1 = -kmax; k1 <= kmax; ++k1) {
+          if (abs(sh[1] + k1) > p.nsum) continue;
+          const float t1 = fmaf(-(float)k1, Lf[1], m[1]);
+          for (int k2 = -kmax; k2 <= kmax; ++k2) {
+            if (abs(sh[2] + k2) > p.nsum) continue;
+            const float t2 = fmaf(-(float)k2, Lf[2], m[2]);
+            const float R2 = fmaf(t2, t2, fmaf(t1, t1, t0 * t0));
+            if (R2 >= rc2) continue;
+            const float mult = ew_h32(R2, alpha);
+            F0 = fmaf(t0, mult, F0);
+            F1 = fmaf(t1, mult, F1);
+            F2 = fmaf(t2, mult, F2);
+          }
         }
       }
     }
@@ -2361,91 +2524,106 @@ __device__ inline void pair_eval32(const PairPrm &p, const float *Lf, const floa
 // same tile/rotation scheme and scratch layout as k_pair_tiles, FP32 with
 // Kahan-compensated per-particle sums
 template <int D, int KIND>
-__global__ void __launch_bounds__(256) k_pair_tiles32(Geo g, PairPrm p, const double *__restrict__ x,
+__global__ void __launch_bounds__(256, 3) k_pair_tiles32(Geo g, PairPrm p, const double *__restrict__ x,
                                                       const double *__restrict__ m,
                                                       double *__restrict__ out, int T, int jobs) {
-  __shared__ float stab[KIND == PAIR_EWALD_REAL ? EW_NINT * (EW_DEG + 1) : 1];
-  if (KIND == PAIR_EWALD_REAL) {
-    for (int i = threadIdx.x; i < EW_NINT * (EW_DEG + 1); i += blockDim.x) stab[i] = (float)(&c_ew_h[0][0])[i];
-    __syncthreads();
-  }
-  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
-  if (warp >= jobs * g.P) return;
-  const int j = warp / jobs;
-  int job = warp % jobs, I = 0;
-  while (job >= T - I) {
-    job -= T - I;
-    ++I;
-  }
-  const int J = I + job;
-  const int a = I * 32 + lane, b0 = J * 32 + lane;
-  const bool va = a < g.N, vb = b0 < g.N;
-  float Lf[3], iLf[3];
-#pragma unroll
-  for (int d = 0; d < 3; ++d) {
-    Lf[d] = (float)g.box[d];
-    iLf[d] = (float)g.inv_box[d];
-  }
-  const float alpha = (float)p.alpha, rc2 = (float)(p.rcut * p.rcut);
-  const int kmax = p.kmax[0] > p.kmax[1] ? (p.kmax[0] > p.kmax[2] ? p.kmax[0] : p.kmax[2])
-                                         : (p.kmax[1] > p.kmax[2] ? p.kmax[1] : p.kmax[2]);
-  float xa[D], xb[D];
-  Kahan fa[D], fb[D];
-#pragma unroll
-  for (int d = 0; d < D; ++d) {
-    xa[d] = va ? (float)x[sidx(j, d, a, D, g.Ns)] : 0.f;
-    xb[d] = vb ? (float)x[sidx(j, d, b0, D, g.Ns)] : 0.f;
-  }
-  const float ima = va ? (float)(1.0 / m[(size_t)j * g.Ns + a]) : 1.f;
-  float imb = vb ? (float)(1.0 / m[(size_t)j * g.Ns + b0]) : 1.f;
-  for (int s = 0; s < 32; ++s) {
-    const int bi = J * 32 + ((lane + s) & 31);
-    const bool act = va && bi < g.N && (I != J || a > bi);
-    if (act) {
-      float dx[D], F[D];
-#pragma unroll
-      for (int d = 0; d < D; ++d) dx[d] = xa[d] - xb[d];
-      pair_eval32<D, KIND>(p, Lf, iLf, dx, F, stab, alpha, rc2, kmax);
-      const float inv = a > bi ? ima : imb;
-#pragma unroll
-      for (int d = 0; d < D; ++d) {
-        fa[d].add(F[d] * inv);
-        fb[d].add(-F[d] * inv);
-      }
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  // persistent warps: tile jobs (slice j, tile pair I <= J) in round-robin
+  for (int wi = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; wi < jobs * g.P; wi += nwarps) {
+    const int j = wi / jobs;
+    int job = wi % jobs, I = 0;
+    while (job >= T - I) {
+      job -= T - I;
+      ++I;
     }
-    const int src = (lane + 1) & 31;
+    const int J = I + job;
+    const int a = I * 32 + lane, b0 = J * 32 + lane;
+    const bool va = a < g.N, vb = b0 < g.N;
+    float Lf[3], iLf[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      Lf[d] = (float)g.box[d];
+      iLf[d] = (float)g.inv_box[d];
+    }
+    const float alpha = (float)p.alpha;
+    // FP32 cut-off (EW32_XCUT); kmax 0 selects the 8-image search (rc32 <= min L)
+    const double rc32 = p.alpha > 0 ? fmin(p.rcut, (double)EW32_XCUT / p.alpha) : 0.0;
+    const float rc2 = (float)(rc32 * rc32);
+    const double Lmin = fmin(g.box[0], fmin(g.box[1], g.box[2]));
+    int kmax = p.kmax[0] > p.kmax[1] ? (p.kmax[0] > p.kmax[2] ? p.kmax[0] : p.kmax[2])
+                                     : (p.kmax[1] > p.kmax[2] ? p.kmax[1] : p.kmax[2]);
+    if (KIND == PAIR_EWALD_REAL && rc32 <= Lmin) kmax = 0;
+    float xa[D], xb[D];
+    Kahan fa[D], fb[D];
 #pragma unroll
     for (int d = 0; d < D; ++d) {
-      xb[d] = __shfl_sync(FULL, xb[d], src);
-      fb[d].s = __shfl_sync(FULL, fb[d].s, src);
-      fb[d].c = __shfl_sync(FULL, fb[d].c, src);
+      xa[d] = va ? (float)x[sidx(j, d, a, D, g.Ns)] : 0.f;
+      xb[d] = vb ? (float)x[sidx(j, d, b0, D, g.Ns)] : 0.f;
     }
-    imb = __shfl_sync(FULL, imb, src);
+    const float ima = va ? (float)(1.0 / m[(size_t)j * g.Ns + a]) : 1.f;
+    float imb = vb ? (float)(1.0 / m[(size_t)j * g.Ns + b0]) : 1.f;
+    for (int s = 0; s < 32; ++s) {
+      const int bi = J * 32 + ((lane + s) & 31);
+      const bool act = va && bi < g.N && (I != J || a > bi);
+      if (act) {
+        float dx[D], F[D];
+#pragma unroll
+        for (int d = 0; d < D; ++d) dx[d] = xa[d] - xb[d];
+        pair_eval32<D, KIND>(p, Lf, iLf, dx, F, alpha, rc2, kmax);
+        const float inv = a > bi ? ima : imb;
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+          fa[d].add(F[d] * inv);
+          fb[d].add(-F[d] * inv);
+        }
+      }
+      const int src = (lane + 1) & 31;
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        xb[d] = __shfl_sync(FULL, xb[d], src);
+        fb[d].s = __shfl_sync(FULL, fb[d].s, src);
+        fb[d].c = __shfl_sync(FULL, fb[d].c, src);
+      }
+      imb = __shfl_sync(FULL, imb, src);
+    }
+    if (I == J) {
+      if (va) {
+#pragma unroll
+        for (int d = 0; d < D; ++d)
+          out[(((size_t)I * g.P + j) * D + d) * g.Ns + a] = fa[d].value() + fb[d].value();
+      }
+    } else {
+      if (va) {
+#pragma unroll
+        for (int d = 0; d < D; ++d) out[(((size_t)J * g.P + j) * D + d) * g.Ns + a] = fa[d].value();
+      }
+      if (vb) {
+#pragma unroll
+        for (int d = 0; d < D; ++d) out[(((size_t)I * g.P + j) * D + d) * g.Ns + b0] = fb[d].value();
+      }
+    }
   }
-  if (I == J) {
-    if (va) {
-#pragma unroll
-      for (int d = 0; d < D; ++d)
-        out[(((size_t)I * g.P + j) * D + d) * g.Ns + a] = fa[d].value() + fb[d].value();
-    }
-  } else {
-    if (va) {
-#pragma unroll
-      for (int d = 0; d < D; ++d) out[(((size_t)J * g.P + j) * D + d) * g.Ns + a] = fa[d].value();
-    }
-    if (vb) {
-#pragma unroll
-      for (int d = 0; d < D; ++d) out[(((size_t)I * g.P + j) * D + d) * g.Ns + b0] = fb[d].value();
-    }
+}
+
+// blocks of 256 threads resident at once (3 per SM), for the persistent grid
+static int pair32_grid(size_t warps_needed) {
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
   }
+  const size_t need = (warps_needed + 7) / 8, full = (size_t)sms * 3;
+  return (int)(need < full ? need : full);
 }
 
 cudaError_t pair_force32(const Geo &g, const PairPrm &p, const double *x, const double *m, double *f,
                          double *scratch, cudaStream_t st) {
   const int T = (g.N + 31) / 32;
   const int jobs = T * (T + 1) / 2;
-  const int nb = cdiv((size_t)jobs * g.P * 32, 256);
+  const int nb = pair32_grid((size_t)jobs * g.P);
   {
     XK_PROF(p.kind == PAIR_EWALD_REAL ? "pair_tiles32_ewald_real" : "pair_tiles32");
     switch (g.D * 16 + p.kind) {

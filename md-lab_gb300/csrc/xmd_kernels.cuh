@@ -87,8 +87,9 @@ cudaError_t wrap_box(const Geo &g, double *x, cudaStream_t st);
 cudaError_t zero(double *p, size_t n, cudaStream_t st);
 
 // ---- exchange ----
+// lt: scratch of N*N doubles (the table of bead-P -> bead-1 springs)
 cudaError_t fill_enk(const Geo &g, const double *x, const double *m, double w2, int image,
-                     double *Eint, double *ENk, cudaStream_t st);
+                     double *Eint, double *ENk, double *lt, cudaStream_t st);
 cudaError_t fill_enk2(const Geo &g, const double *x, const double *m, double w2, int image,
                       double *ENk2, cudaStream_t st);
 // the cubic path's table (md_pimd_fill_ENk2_x), a different quantity
@@ -101,6 +102,10 @@ cudaError_t fill_vb(int N, double beta, double vi, const double *ENk, double *VB
                     cudaStream_t st);
 cudaError_t back_vb(int N, double beta, double vi, const double *ENk, double *tmpV, double *rs,
                     cudaStream_t st);
+// both at once (the two recursions need only ENk): V_B into VBN and the
+// backward tmpV, on two SMs; rs_f and rs_b are separate weight scratch
+cudaError_t fill_vb_tv(int N, double beta, double vi, const double *ENk, double *VBN, double *tmpV, double *rs_f,
+                       double *rs_b, cudaStream_t st);
 cudaError_t fill_g(int N, double beta, double vi, const double *ENk, const double *VBN,
                    const double *tmpV, double *G, cudaStream_t st);
 // scratch: at least exch_scratch_doubles(g) doubles

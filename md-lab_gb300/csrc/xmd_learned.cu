@@ -865,7 +865,7 @@ cudaError_t mlp_train_grad(const MlpDev &w, const uint8_t *ximg, const float *V,
 // 64 features are then the histogram times a fixed basis (32 Gaussians in r
 // and the spherical average sin(k r)/(k r) of the 32 lowest reciprocal-lattice
 // shells), normalised and stored as BF16 tile images.
-constexpr int DS_ROWS = 32, DS_WARPS = 8, DS_HSTRIDE = DESC_BINS + 1;
+constexpr int DS_ROWS = 32, DS_WARPS = 8;
 
 template <bool RAW>
 __global__ void __launch_bounds__(DS_WARPS * 32) k_desc(Geo g, DescPrm p, const double *__restrict__ x,
@@ -873,13 +873,13 @@ __global__ void __launch_bounds__(DS_WARPS * 32) k_desc(Geo g, DescPrm p, const 
                                                         float *__restrict__ raw) {
   extern __shared__ __align__(16) float dsm[];
   float *basis = dsm;                                // DESC_BINS * 64
-  float *hist = basis + DESC_BINS * 64;              // DS_ROWS * DS_HSTRIDE
-  float *vacc = hist + DS_ROWS * DS_HSTRIDE;         // DS_WARPS * DS_ROWS * 9
-  float4 *pos = (float4 *)(vacc + DS_WARPS * DS_ROWS * 9);  // N; 58496 bytes in: 16-byte aligned
+  float *hist = basis + DESC_BINS * 64;              // [DESC_BINS][DS_ROWS]: lane t owns column t
+  float *vacc = hist + DESC_BINS * DS_ROWS;          // DS_WARPS * DS_ROWS * 9
+  float4 *pos = (float4 *)(vacc + DS_WARPS * DS_ROWS * 9);  // N; 58368 bytes in: 16-byte aligned
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int j = blockIdx.y, l0 = blockIdx.x * DS_ROWS;
   for (int q = tid; q < DESC_BINS * 64; q += blockDim.x) basis[q] = p.basis[q];
-  for (int q = tid; q < DS_ROWS * DS_HSTRIDE; q += blockDim.x) hist[q] = 0.f;
+  for (int q = tid; q < DS_ROWS * DESC_BINS; q += blockDim.x) hist[q] = 0.f;
   for (int q = tid; q < g.N; q += blockDim.x)
     pos[q] = make_float4((float)x[sidx(j, 0, q, 3, g.Ns)], (float)x[sidx(j, 1, q, 3, g.Ns)],
                          (float)x[sidx(j, 2, q, 3, g.Ns)], 0.f);
@@ -891,7 +891,9 @@ __global__ void __launch_bounds__(DS_WARPS * 32) k_desc(Geo g, DescPrm p, const 
   float vs[9];
 #pragma unroll
   for (int i = 0; i < 9; ++i) vs[i] = 0.f;
-  float *hrow = hist + lane * DS_HSTRIDE;
+  // bin b of row t at hist[b*32 + t]: the lanes of a warp (rows) always hit
+  // distinct banks, whatever bins they deposit into
+  float *hrow = hist + lane;
   for (int c = warp; c < g.N; c += DS_WARPS) {
     const float4 xc = pos[c];
     float d0 = xr.x - xc.x, d1 = xr.y - xc.y, d2 = xr.z - xc.z;
@@ -912,8 +914,8 @@ __global__ void __launch_bounds__(DS_WARPS * 32) k_desc(Geo g, DescPrm p, const 
       b0 = DESC_BINS - 1;
       w1 = 0.f;
     }
-    atomicAdd(&hrow[b0], fc * (1.f - w1));
-    if (w1 > 0.f) atomicAdd(&hrow[b0 + 1], fc * w1);
+    atomicAdd(&hrow[b0 * DS_ROWS], fc * (1.f - w1));
+    if (w1 > 0.f) atomicAdd(&hrow[(b0 + 1) * DS_ROWS], fc * w1);
     const float ir = 1.f / r;
 #pragma unroll
     for (int m = 0; m < 3; ++m) {
@@ -945,9 +947,9 @@ __global__ void __launch_bounds__(DS_WARPS * 32) k_desc(Geo g, DescPrm p, const 
   float acc[8];
 #pragma unroll
   for (int q = 0; q < 8; ++q) acc[q] = 0.f;
-  const float *hr = hist + rr * DS_HSTRIDE;
+  const float *hr = hist + rr;
   for (int b = 0; b < DESC_BINS; ++b) {
-    const float h = hr[b];
+    const float h = hr[b * DS_ROWS];
     const float4 u0 = *(const float4 *)(basis + b * 64 + f0), u1 = *(const float4 *)(basis + b * 64 + f0 + 4);
     acc[0] = fmaf(h, u0.x, acc[0]);
     acc[1] = fmaf(h, u0.y, acc[1]);
@@ -975,7 +977,7 @@ __global__ void __launch_bounds__(DS_WARPS * 32) k_desc(Geo g, DescPrm p, const 
 }
 
 static size_t desc_smem(int N) {
-  return sizeof(float) * ((size_t)DESC_BINS * 64 + DS_ROWS * DS_HSTRIDE + DS_WARPS * DS_ROWS * 9) +
+  return sizeof(float) * ((size_t)DESC_BINS * 64 + DS_ROWS * DESC_BINS + DS_WARPS * DS_ROWS * 9) +
          sizeof(float4) * (size_t)N;
 }
 

@@ -157,7 +157,7 @@ static void free_sim(SimDev *d) {
 }
 
 static void free_pimd(PimdDev *d) {
-  for (DevBuf *b : {&d->ENk, &d->ENk2, &d->Eint, &d->VBN, &d->tmpV, &d->G, &d->rec, &d->rc_coef,
+  for (DevBuf *b : {&d->ENk, &d->ENk2, &d->Eint, &d->VBN, &d->tmpV, &d->G, &d->linkt, &d->rec, &d->rc_coef,
                     &d->rc_cols, &d->rc_phase, &d->rc_S, &d->rc_T})
     release(*b);
 }
@@ -384,8 +384,10 @@ int pimd_device(md_pimd_t_x *pimd, SimDev **sd, PimdDev **pd) {
   XMD_TRY(reserve(d->VBN, (size_t)(N + 1) * 8));
   XMD_TRY(reserve(d->tmpV, (size_t)(N + 1) * 8));
   XMD_TRY(reserve(d->G, (size_t)N * N * 8));
-  XMD_TRY(reserve(d->rec, xk::rec_scratch_doubles(N) * 8));
-  XMD_CUDA(cudaMemsetAsync(d->rec.p, 0, xk::rec_scratch_doubles(N) * 8, stream()));
+  XMD_TRY(reserve(d->linkt, (size_t)N * N * 8));
+  XMD_TRY(reserve(d->rec, 2 * xk::rec_scratch_doubles(N) * 8));
+  XMD_CUDA(cudaMemsetAsync(d->rec.p, 0, 2 * xk::rec_scratch_doubles(N) * 8, stream()));
+  d->tmpv_fresh = false;
   XMD_CUDA(cudaMemsetAsync(d->tmpV.p, 0, (size_t)(N + 1) * 8, stream()));
   cudaStream_t st = stream();
   XMD_CUDA(cudaMemcpyAsync(d->ENk.p, pimd->ENk[0], nt * 8, cudaMemcpyHostToDevice, st));

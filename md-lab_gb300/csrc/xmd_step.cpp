@@ -266,7 +266,8 @@ int md_pimd_fast_fill_ENk_x(md_pimd_t_x *pimd, int image) {
   XMD_TRY(check_plain(pimd));
   XMD_TRY(check_image(sd, image));
   XMD_CUDA(xk::fill_enk(sd->geo, sd->x.as<double>(), sd->m.as<double>(), pimd->omegaP * pimd->omegaP, image,
-                        pd->Eint.as<double>(), pd->ENk.as<double>(), stream()));
+                        pd->Eint.as<double>(), pd->ENk.as<double>(), pd->linkt.as<double>(), stream()));
+  pd->tmpv_fresh = false;
   return 0;
 }
 
@@ -277,8 +278,15 @@ int md_pimd_fill_VB_x(md_pimd_t_x *pimd) {
   PimdDev *pd;
   XMD_TRY(pimd_device(pimd, &sd, &pd));
   XMD_TRY(check_plain(pimd));
-  XMD_CUDA(xk::fill_vb(pimd->N, pimd->beta, pimd->vi, pd->ENk.as<double>(), pd->VBN.as<double>(),
-                       pd->rec.as<double>(), stream()));
+  // the backward recursion (tmpV of the exchange forces) needs only ENk as
+  // well: both run now, side by side, and the force call reuses tmpV while
+  // ENk, beta and vi are unchanged
+  double *rs = pd->rec.as<double>();
+  XMD_CUDA(xk::fill_vb_tv(pimd->N, pimd->beta, pimd->vi, pd->ENk.as<double>(), pd->VBN.as<double>(),
+                          pd->tmpV.as<double>(), rs, rs + xk::rec_scratch_doubles(pimd->N), stream()));
+  pd->tmpv_fresh = true;
+  pd->tmpv_beta = pimd->beta;
+  pd->tmpv_vi = pimd->vi;
   return 0;
 }
 
@@ -294,8 +302,9 @@ int md_pimd_fast_fill_force_VB_x(md_pimd_t_x *pimd, int image) {
   if (rc) return rc;
   cudaStream_t st = stream();
   const int N = pimd->N;
-  XMD_CUDA(xk::back_vb(N, pimd->beta, pimd->vi, pd->ENk.as<double>(), pd->tmpV.as<double>(),
-                       pd->rec.as<double>(), st));
+  if (!(pd->tmpv_fresh && pd->tmpv_beta == pimd->beta && pd->tmpv_vi == pimd->vi))
+    XMD_CUDA(xk::back_vb(N, pimd->beta, pimd->vi, pd->ENk.as<double>(), pd->tmpV.as<double>(),
+                         pd->rec.as<double>(), st));
   XMD_CUDA(xk::fill_g(N, pimd->beta, pimd->vi, pd->ENk.as<double>(), pd->VBN.as<double>(), pd->tmpV.as<double>(),
                       pd->G.as<double>(), st));
   XMD_CUDA(xk::exch_force(sd->geo, sd->x.as<double>(), sd->m.as<double>(), pimd->omegaP * pimd->omegaP, image,
