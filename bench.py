@@ -369,6 +369,114 @@ def learned_form(lib, R, s, pair, step, args, ws):
     return m, form, prof, kps
 
 
+# ---------------------------------------------------------------------
+# batched ensemble (64 independent systems, one graph launch per step)
+# ---------------------------------------------------------------------
+ENS_N, ENS_P = (16, 24, 32, 48, 64, 96, 128), (16, 32, 64)
+
+
+def ensemble_specs(seed=4):
+    """8 xi in [0, 1] x 8 beta in 1..8; N and P drawn from the lists; even
+    systems 3D traps with Gaussian repulsion, odd ones electron gas"""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    specs = []
+    for a in range(8):
+        for b in range(8):
+            i = a * 8 + b
+            specs.append(("trap" if i % 2 == 0 else "ueg", int(rng.choice(ENS_N)), int(rng.choice(ENS_P)),
+                          a / 7.0, b + 1.0))
+    return specs
+
+
+def ensemble_form(lib, R, args):
+    import numpy as np
+    import xmd_x
+    lib.check(lib.md_gb300_set_precision_x(1))  # FP32 forces, FP64 recursion and NHC
+    specs = ensemble_specs()
+    rng = np.random.default_rng(11)
+    systems = []
+    for kind, n, p, vi, beta in specs:
+        T = 1.0 / beta
+        box = (4 * math.pi * n / 3) ** (1 / 3) * 2.0 if kind == "ueg" else 10.0
+        s = xmd_x.PimdSystem(lib, n, p, vi, T, box=box)
+        if kind == "ueg":
+            x = rng.uniform(0, box, (n, 1, 3)) + 0.05 * rng.standard_normal((n, p, 3))
+        else:
+            x = rng.standard_normal((n, p, 3))
+        s.set_state(m=np.ones(n * p), x=x.ravel(), v=rng.standard_normal(n * p * 3) * math.sqrt(T))
+        lib.md_init_nhc_x(s.sim, lib.md_get_quick_Q_x(T, s.pimd.contents.omegaP), 0, s.sim.contents.Nf, 0.0)
+        systems.append((kind, s, box))
+    ewald = lib.fn("md_coulomb_3d_ewald_force_x")
+    gauss = lib.fn("md_gaussian_force_x")
+    trapf = lib.fn("md_harmonic_trap_force_x")
+
+    def one(i):
+        kind, s, box = systems[i]
+        if kind == "ueg":
+            xmd_x.set_potentials(lib, coul_s=1.0, alpha=5.6 / box, nsum=8)
+            xmd_x.md_step(lib, s, 0.05, image=1, pair=ewald, pbc=True)
+        else:
+            xmd_x.set_potentials(lib, trap_w=1.0, gauss_g=0.75 * math.pi, gauss_s=0.5)
+            xmd_x.md_step(lib, s, 0.005, trap=trapf, pair=gauss)
+
+    for _ in range(2):
+        for i in range(len(systems)):
+            one(i)
+    # autotuned tile shapes, one per distinct system shape
+    tuned = {}
+    for i, (kind, s, box) in enumerate(systems):
+        key = (kind, specs[i][1], specs[i][2])
+        if key in tuned:
+            continue
+        if kind == "ueg":
+            xmd_x.set_potentials(lib, coul_s=1.0, alpha=5.6 / box, nsum=8)
+        else:
+            xmd_x.set_potentials(lib, trap_w=1.0, gauss_g=0.75 * math.pi, gauss_s=0.5)
+        w = C.c_int()
+        lib.check(lib.md_gb300_autotune_pair_x(s.pimd, ewald if kind == "ueg" else gauss, 5, C.byref(w), None))
+        tuned[key] = w.value
+    step_fn = C.CFUNCTYPE(C.c_int, C.c_int, C.c_void_p)
+
+    def cb(i, ctx):
+        try:
+            one(i)
+            return 0
+        except Exception:
+            return -1
+
+    fn = step_fn(cb)
+    g = C.c_void_p()
+    lib.check(lib.md_gb300_capture_ensemble_x(len(systems), C.cast(fn, C.c_void_p), None, C.byref(g)),
+              "ensemble capture")
+    kernels = lib.md_gb300_graph_kernel_count_x(g)
+    beads = sum(n * p for _, n, p, _, _ in specs)
+    nst = max(args.steps, 10)
+    ms, wall, clocks = R.time([R.launcher(g)] * nst, [R.launcher(g)] * 3)
+    # the same 64 steps as separate graphs, one after the other
+    singles = [R.capture(lambda i=i: one(i))[0] for i in range(len(systems))]
+
+    def seq():
+        for gi in singles:
+            lib.check(lib.md_gb300_graph_launch_x(gi, 1))
+
+    ms_seq, _, _ = R.time([seq] * nst, [seq] * 3)
+    for gi in singles:
+        lib.md_gb300_graph_free_x(gi)
+    lib.md_gb300_graph_free_x(g)
+    for _, s, _ in systems:
+        s.free()
+    lib.check(lib.md_gb300_set_precision_x(0))
+    return {"value": beads / (ms * 1e-3), "unit": "bead-steps/s", "ms_per_step": ms, "systems": len(specs),
+            "bead_slots": beads, "kernels_per_launch": kernels, "steps_timed": nst,
+            "sequential_graphs_ms_per_step": ms_seq, "gain_vs_sequential": ms_seq / ms,
+            "tile_warps_chosen": {f"{k[0]} N={k[1]} P={k[2]}": v for k, v in sorted(tuned.items())},
+            "clocks": clocks,
+            "workload": "64 systems: 8 xi in [0,1] x 8 beta in 1..8, N in {16..128}, P in {16,32,64}; "
+                        "even: 3D trap + Gaussian repulsion (g=0.75 pi, s=0.5, dt=0.005); odd: electron gas "
+                        "rs=2, Ewald alpha=5.6/L |n|<=8, dt=0.05; FP32 forces, FP64 recursion and NHC"}
+
+
 def run_gb300(args, dist, rank, ws):
     import torch
     import xmd_x
@@ -417,6 +525,8 @@ def run_gb300(args, dist, rank, ws):
                                   "kernels_per_step": mixed_kps, "force_error_vs_fp64": ferr,
                                   "clocks": mixed_clocks,
                                   "kernel_ms_per_step": {k: v[0] for k, v in mixed_prof.items()}}
+    if not args.no_ensemble:
+        forms["ensemble_64"] = ensemble_form(lib, R, args)
     headline = "plain_fp64"
     model = None
     if not args.no_learned:
@@ -501,6 +611,7 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=8.0, help="seconds of CPU sample")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned form")
+    ap.add_argument("--no-ensemble", action="store_true", help="skip the 64-system ensemble")
     ap.add_argument("--learn-configs", type=int, default=3125,
                     help="configurations collected for training (x P bead slices)")
     ap.add_argument("--learn-steps", type=int, default=3000)

@@ -54,6 +54,16 @@ typedef struct md_gb300_graph md_gb300_graph_t_x;
 int md_gb300_capture_begin_x(void);
 int md_gb300_capture_end_x(md_gb300_graph_t_x **graph);
 int md_gb300_graph_launch_x(md_gb300_graph_t_x *graph, int count);
+/* One step of several independent systems as one graph.  The library calls
+   step(i, ctx) for i = 0 .. n-1 while capturing, each call's md_* work
+   recorded on its own branch stream forked from and joined to the library
+   stream; replaying the graph advances every system with one launch, and
+   the GPU runs the independent branches concurrently.  step sets whatever
+   md_set_* parameters its system needs (they are frozen into the graph) and
+   returns 0, or an error code that ends the capture.  Each system's device
+   state must exist already (one ordinary step first). */
+typedef int (*md_gb300_system_step_fn_x)(int system, void *ctx);
+int md_gb300_capture_ensemble_x(int n, md_gb300_system_step_fn_x step, void *ctx, md_gb300_graph_t_x **graph);
 /* kernel nodes in a captured graph (kernels launched per replay) */
 int md_gb300_graph_kernel_count_x(md_gb300_graph_t_x *graph);
 void md_gb300_graph_free_x(md_gb300_graph_t_x *graph);
@@ -109,6 +119,16 @@ int md_gb300_pair_force_noalloc_x(md_pair_force_t_x pf, const double *x, const d
    phase products accumulated in double-float; positions, the exchange
    recursion, springs, the thermostat and every estimator stay FP64.  The
    force error against the FP64 form is about 1e-6 of the force scale. */
+/* Tile shape of the FP32 pair kernel (the mixed form) for pimd's system
+   shape, chosen by timing: warps of 32 x 32 pair tiles per thread block, 1,
+   2, 4 or 8 (small systems in an ensemble spread better over the SMs with
+   small blocks).  The choice is kept for this potential kind, D, N and P
+   and used by md_pimd_calc_pair_force_x; the forces do not depend on it.
+   *warps and *ms (may be NULL) receive the choice and its time per call. */
+int md_gb300_autotune_pair_x(md_pimd_t_x *pimd, md_pair_force_t_x pf, int repeats, int *warps, double *ms);
+/* set that choice directly (a tuning table kept by the caller) */
+int md_gb300_set_pair_tile_x(md_pair_force_t_x pf, int N, int P, int warps);
+
 #define MD_GB_PRECISION_FP64 0
 #define MD_GB_PRECISION_MIXED 1
 int md_gb300_set_precision_x(int mode);

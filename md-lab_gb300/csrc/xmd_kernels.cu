@@ -13,6 +13,7 @@
 // Reference counterparts (MD-Lab file:line) are cited at each kernel.
 #include <cuda_runtime.h>
 
+#include <array>
 #include <atomic>
 #include <cmath>
 #include <cstdio>
@@ -835,20 +836,17 @@ constexpr int TS_WARPS = 16, TS_CHUNK = 32;
 __device__ inline double scale2(double v, int d) {
   const long long b = __double_as_longlong(v);
   const int ex = (int)((b >> 52) & 0x7ff);
-  if (ex == 0 || ex + d <= 0) return 0.0;
-  return __longlong_as_double(b + ((long long)d << 52));
+  const long long r = b + ((long long)d << 52);
+  return __longlong_as_double((ex == 0 || ex + d <= 0) ? 0LL : r);  // selects, no branch
 }
 
 // normalise a non-negative extended value to a mantissa in [0.5, 1)
 __device__ inline void norm2(double &m, int &e) {
   const long long b = __double_as_longlong(m);
   const int ex = (int)((b >> 52) & 0x7ff);
-  if (ex == 0) {  // zero (values here are never subnormal)
-    m = 0.0;
-    return;
-  }
-  e += ex - 1022;
-  m = __longlong_as_double((b & ~(0x7ffLL << 52)) | (1022LL << 52));
+  const bool z = ex == 0;  // zero (values here are never subnormal) stays zero
+  e = z ? e : e + ex - 1022;
+  m = __longlong_as_double(z ? 0LL : ((b & ~(0x7ffLL << 52)) | (1022LL << 52)));
 }
 
 // Block b solves direction first + b (0 forward, 1 backward) with the
@@ -861,33 +859,53 @@ struct TriJob {
 };
 
 // Extended-range dot product of row i of the weights with the unknowns over
-// columns [j0, j1), reduced over the warp: (am, E) with value am 2^E.  An
-// integer pass finds the largest term exponent E; the terms are then scaled
-// to 2^E by exponent arithmetic and summed with one FMA each.  Zero weights
-// (xi = 0 beyond k = 1) are skipped by their bit pattern.
+// columns [j0, j1), reduced over the warp: (am, E) with value am 2^E.  One
+// pass: each lane keeps a running (am, E) and rescales when a larger term
+// exponent arrives; loads are issued four columns per lane at a time.  Zero
+// weights (xi = 0 beyond k = 1) are skipped by their bit pattern.  E is
+// EXT_NONE while a lane has no term.
+constexpr int EXT_NONE = -2147483647;
 __device__ inline void ext_dot(const double *__restrict__ mr, const int *__restrict__ er, const double *Xm,
-                               const int *Xe, int j0, int j1, int lane, double &am, int &E) {
-  E = -2147483647;
-  for (int j = j0 + lane; j < j1; j += 32)
-    if (__double_as_longlong(mr[j]) != 0) {
-      const int te = er[j] + Xe[j];
-      E = te > E ? te : E;
+                               const int *Xe, int j0, int j1, int lane, double &am_out, int &E_out) {
+  double am = 0.0;
+  int E = EXT_NONE;
+  for (int jb = j0 + lane; jb < j1; jb += 128) {
+    double mv[4], xv[4];
+    int ev[4], xe[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int j = jb + 32 * u;
+      const bool ok = j < j1;
+      mv[u] = ok ? mr[j] : 0.0;
+      ev[u] = ok ? er[j] : 0;
+      xv[u] = ok ? Xm[j] : 0.0;
+      xe[u] = ok ? Xe[j] : 0;
     }
 #pragma unroll
-  for (int o = 16; o; o >>= 1) {
-    const int oe = __shfl_xor_sync(FULL, E, o);
-    E = oe > E ? oe : E;
+    for (int u = 0; u < 4; ++u) {
+      const bool nz = __double_as_longlong(mv[u]) != 0;
+      const int te = ev[u] + xe[u];
+      const int ne = (nz && (E == EXT_NONE || te > E)) ? te : E;
+      const double a2 = scale2(am, E == EXT_NONE ? 0 : E - ne);
+      const double t2 = fma(mv[u], scale2(xv[u], nz ? te - ne : 0), a2);
+      am = nz ? t2 : am;
+      E = ne;
+    }
   }
-  am = 0.0;
-  if (E != -2147483647)
-    for (int j = j0 + lane; j < j1; j += 32)
-      if (__double_as_longlong(mr[j]) != 0) am = fma(mr[j], scale2(Xm[j], er[j] + Xe[j] - E), am);
-  am = warp_sum(am);
+  int Em = E;
+#pragma unroll
+  for (int o = 16; o; o >>= 1) {
+    const int oe = __shfl_xor_sync(FULL, Em, o);
+    Em = (Em == EXT_NONE || (oe != EXT_NONE && oe > Em)) ? oe : Em;
+  }
+  const double v = (E == EXT_NONE) ? 0.0 : scale2(am, E - Em);
+  am_out = warp_sum(v);
+  E_out = Em;
 }
 
 // (pm, pe) += (am, E), both non-negative extended-range values; normalised
 __device__ inline void ext_acc(double &pm, int &pe, double am, int E) {
-  if (__double_as_longlong(am) != 0) {
+  if (__double_as_longlong(am) != 0 && E != EXT_NONE) {
     if (__double_as_longlong(pm) == 0) {
       pm = am;
       pe = E;
@@ -904,22 +922,50 @@ __device__ inline void ext_acc(double &pm, int &pe, double am, int E) {
 // over the unknowns of earlier chunks is split: the part over all but the
 // previous chunk is computed by warps 1.. while warp 0 is still solving that
 // previous chunk (so it costs no time on the sequential path); the previous
-// chunk's 32 columns are added by all warps between the two solves.
+// chunk's 32 columns are added by all warps between the two solves.  The
+// weights the sequential steps need (the chunk's own triangle and the
+// 32 x 32 block of the previous chunk's columns) are staged in shared memory
+// by warps 1.. one chunk ahead, so the sequential path reads no global memory.
+constexpr int TS_LD = TS_CHUNK + 1;  // padded row of the staged blocks
+
 __global__ void __launch_bounds__(TS_WARPS * 32) k_tri_solve(int N, double beta, TriJob job, int first) {
   const int backward = first + blockIdx.x;
   const double *__restrict__ Mm = job.Mm[backward];
   const int *__restrict__ Me = job.Me[backward];
   double *__restrict__ out = job.out[backward];
   extern __shared__ double sh[];
-  double *Xm = sh;                        // N+1
-  double *Pm = Xm + N + 1;                // 2 x TS_CHUNK (double buffer)
-  int *Xe = (int *)(Pm + 2 * TS_CHUNK);   // N+1
-  int *Pe = Xe + N + 1;                   // 2 x TS_CHUNK
+  double *Wm = sh;                              // [2][TS_CHUNK][TS_LD] the chunk's triangle
+  double *Um = Wm + 2 * TS_CHUNK * TS_LD;       // [2][TS_CHUNK][TS_LD] previous chunk's columns
+  double *Pm = Um + 2 * TS_CHUNK * TS_LD;       // [2][TS_CHUNK] partial sums (double buffer)
+  double *Xm = Pm + 2 * TS_CHUNK;               // N+1
+  int *We = (int *)(Xm + N + 1);                // [2][TS_CHUNK][TS_LD]
+  int *Ue = We + 2 * TS_CHUNK * TS_LD;          // [2][TS_CHUNK][TS_LD]
+  int *Pe = Ue + 2 * TS_CHUNK * TS_LD;          // [2][TS_CHUNK]
+  int *Xe = Pe + 2 * TS_CHUNK;                  // N+1
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  // weights of chunk starting at n0 (triangle) and its block against the
+  // columns c0 .. c0+31 (c0 < 0: none) into buffer nb; threads t0, t0+stride..
+  auto stage = [&](int n0, int c0, int nb, int t0, int stride) {
+    for (int q = t0; q < 2 * TS_CHUNK * TS_CHUNK; q += stride) {
+      const int which = q / (TS_CHUNK * TS_CHUNK), rs = q % (TS_CHUNK * TS_CHUNK);
+      const int r = rs / TS_CHUNK, c = rs % TS_CHUNK, i = n0 + r;
+      const size_t o = ((size_t)nb * TS_CHUNK + r) * TS_LD + c;
+      if (which == 0) {
+        const bool in = i <= N && c < r;
+        Wm[o] = in ? Mm[moff(i, n0 + c)] : 0.0;
+        We[o] = in ? Me[moff(i, n0 + c)] : 0;
+      } else {
+        const bool in = i <= N && c0 >= 0;
+        Um[o] = in ? Mm[moff(i, c0 + c)] : 0.0;
+        Ue[o] = in ? Me[moff(i, c0 + c)] : 0;
+      }
+    }
+  };
   if (threadIdx.x == 0) {
     Xm[0] = 0.5;
     Xe[0] = 1;
   }
+  stage(1, -1, 0, threadIdx.x, blockDim.x);
   __syncthreads();
   // chunk 0: its rows against column 0
   for (int r = w; r < TS_CHUNK; r += TS_WARPS) {
@@ -940,14 +986,24 @@ __global__ void __launch_bounds__(TS_WARPS * 32) k_tri_solve(int N, double beta,
     const int buf = c & 1;
     double *Pmc = Pm + buf * TS_CHUNK;
     int *Pec = Pe + buf * TS_CHUNK;
-    // the previous chunk's columns [i0 - 32, i0)
+    // the previous chunk's columns [i0 - 32, i0), one per lane, from the
+    // staged block
     if (c > 0) {
+      const int col = i0 - TS_CHUNK + lane;
       for (int r = w; r < TS_CHUNK; r += TS_WARPS) {
-        const int i = i0 + r;
-        if (i > N) continue;  // warp-uniform
-        double am;
-        int E;
-        ext_dot(Mm + moff(i, 0), Me + moff(i, 0), Xm, Xe, i0 - TS_CHUNK, i0, lane, am, E);
+        if (i0 + r > N) continue;  // warp-uniform
+        const size_t o = ((size_t)buf * TS_CHUNK + r) * TS_LD + lane;
+        const double mv = Um[o];
+        const bool nz = __double_as_longlong(mv) != 0;
+        const int te = nz ? Ue[o] + Xe[col] : EXT_NONE;
+        int E = te;
+#pragma unroll
+        for (int o2 = 16; o2; o2 >>= 1) {
+          const int oe = __shfl_xor_sync(FULL, E, o2);
+          E = oe > E ? oe : E;
+        }
+        double am = nz ? mv * scale2(Xm[col], nz ? te - E : 0) : 0.0;
+        am = warp_sum(am);
         if (lane == 0) {
           double pm = Pmc[r];
           int pe = Pec[r];
@@ -968,11 +1024,11 @@ __global__ void __launch_bounds__(TS_WARPS * 32) k_tri_solve(int N, double beta,
       int ae = own ? Pec[lane] : 0;
       double mm[TS_CHUNK];
       int me[TS_CHUNK];
+      const size_t ro = ((size_t)buf * TS_CHUNK + lane) * TS_LD;
 #pragma unroll
       for (int s = 0; s < TS_CHUNK; ++s) {
-        const bool in = own && s < lane;
-        mm[s] = in ? Mm[moff(i, i0 + s)] : 0.0;
-        me[s] = in ? Me[moff(i, i0 + s)] : 0;
+        mm[s] = Wm[ro + s];
+        me[s] = We[ro + s];
       }
 #pragma unroll
       for (int s = 0; s < TS_CHUNK; ++s) {
@@ -985,18 +1041,20 @@ __global__ void __launch_bounds__(TS_WARPS * 32) k_tri_solve(int N, double beta,
         }
         const double xm = __shfl_sync(FULL, am, s);
         const int xe = __shfl_sync(FULL, ae, s);
-        if (lane > s && mm[s] != 0.0) {
-          const int te = me[s] + xe;
-          if (te > ae) {  // the new term sets the scale
-            am = scale2(am, ae - te);
-            ae = te;
-          }
-          am = fma(mm[s], scale2(xm, te - ae), am);
-        }
+        // later rows add their term; a larger term exponent sets the scale
+        // (straight-line code with selects: no divergence on the chain)
+        const bool upd = lane > s && __double_as_longlong(mm[s]) != 0;
+        const int te = me[s] + xe;
+        const int ne = (upd && te > ae) ? te : ae;
+        const double t2 = fma(mm[s], scale2(xm, upd ? te - ne : 0), scale2(am, ae - ne));
+        am = upd ? t2 : am;
+        ae = ne;
       }
     } else {
-      // next chunk's rows against the columns solved before this chunk
+      // next chunk: stage its weights, and its rows against the columns
+      // solved before this chunk
       const int n0 = i0 + TS_CHUNK;
+      if (n0 <= N) stage(n0, i0, buf ^ 1, threadIdx.x - 32, blockDim.x - 32);
       for (int r = w - 1; r < TS_CHUNK; r += TS_WARPS - 1) {
         const int i = n0 + r;
         if (i > N) break;  // warp-uniform; later rows are out of range too
@@ -1026,7 +1084,7 @@ size_t rec_scratch_doubles(int N) { return ntri(N) + (ntri(N) + 1) / 2 + 1; }
 
 // directions first .. first + count - 1 of job
 static cudaError_t tri_solve(int N, double beta, const TriJob &job, int first, int count, cudaStream_t st) {
-  const size_t smem = (sizeof(double) + sizeof(int)) * (N + 1 + 2 * TS_CHUNK) + 16;
+  const size_t smem = (sizeof(double) + sizeof(int)) * (N + 1 + 2 * TS_CHUNK + 4 * TS_CHUNK * TS_LD) + 16;
   static bool opted = false;
   if (!opted) {
     cudaError_t ea = cudaFuncSetAttribute(k_tri_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
@@ -1662,7 +1720,9 @@ __global__ void k_pair_finish(Geo g, const double *__restrict__ part, int T, dou
 size_t pair_scratch_doubles(const Geo &g) {
   const int T = (g.N + 31) / 32;
   const size_t jobs = (size_t)T * (T + 1) / 2;
-  size_t a = (size_t)T * g.slots();
+  // partial slots (doubles, or float2 in the FP32 form), then room for the
+  // FP32 form's copies of the positions and inverse masses
+  size_t a = (size_t)T * g.slots() + (g.slots() + (size_t)g.P * g.Ns + 1) / 2 + 1;
   size_t b = jobs * g.P;
   return a > b ? a : b;
 }
@@ -2432,19 +2492,29 @@ __device__ __forceinline__ float ew_h32(float R2, float alpha) {
   return e * fmaf(x, 1.1283791670955126f, q * t) * (ri * ri * ri);
 }
 
+// constants of the FP32 pair kernel, prepared on the host so that the
+// kernel issues no FP64 instruction (on GB300 the FP64 pipe is 58x slower
+// and also serves conversions and divisions of doubles)
+struct P32 {
+  float L[3], iL[3];
+  float igs2, gpre;  // Gaussian: 1/s^2 and (g / (pi s^2)) (2 / s^2)
+  float qs;          // Coulomb / Ewald strength
+  float alpha, rc2;  // Ewald: splitting, FP32 cut-off squared
+  int kmax;          // Ewald: 0 = 8-image search, else |k_d| <= kmax
+  int nsum;          // Ewald: the reference's image cube |n_d| <= nsum
+};
+
 template <int D, int KIND>
-__device__ inline void pair_eval32(const PairPrm &p, const float *Lf, const float *iLf, const float *dx,
-                                   float *F, float alpha, float rc2, int kmax) {
+__device__ inline void pair_eval32(const P32 &q, const float *dx, float *F) {
   if (KIND == PAIR_GAUSSIAN || KIND == PAIR_PERIODIC_GAUSSIAN) {
     float t[D], r2 = 0.f;
 #pragma unroll
     for (int d = 0; d < D; ++d) {
       t[d] = dx[d];
-      if (KIND == PAIR_PERIODIC_GAUSSIAN) t[d] = t[d] - Lf[d] * rintf(t[d] * iLf[d]);
+      if (KIND == PAIR_PERIODIC_GAUSSIAN) t[d] = t[d] - q.L[d] * rintf(t[d] * q.iL[d]);
       r2 = fmaf(t[d], t[d], r2);
     }
-    const float s2 = (float)(p.s * p.s);
-    const float mult = (float)(p.g / (M_PI * p.s * p.s)) * expf(-r2 / s2) * (2.f / s2);
+    const float mult = q.gpre * __expf(-r2 * q.igs2);
 #pragma unroll
     for (int d = 0; d < D; ++d) F[d] = mult * t[d];
   } else if (KIND == PAIR_COULOMB || KIND == PAIR_PERIODIC_COULOMB) {
@@ -2452,61 +2522,64 @@ __device__ inline void pair_eval32(const PairPrm &p, const float *Lf, const floa
 #pragma unroll
     for (int d = 0; d < D; ++d) {
       t[d] = dx[d];
-      if (KIND == PAIR_PERIODIC_COULOMB) t[d] = t[d] - Lf[d] * rintf(t[d] * iLf[d]);
+      if (KIND == PAIR_PERIODIC_COULOMB) t[d] = t[d] - q.L[d] * rintf(t[d] * q.iL[d]);
       r2 = fmaf(t[d], t[d], r2);
     }
     const float ri = rsqrtf(r2);
-    const float mult = (float)p.qs * ri * ri * ri;
+    const float mult = q.qs * ri * ri * ri;
 #pragma unroll
     for (int d = 0; d < D; ++d) F[d] = mult * t[d];
   } else if (KIND == PAIR_EWALD_REAL) {
-    // Minimum image m = dx - sh L; images t = m - k L.  Images beyond rc32
-    // (alpha rc32 <= EW32_XCUT) are left out.  When rc32 is at most the
-    // smallest box length only the 8 images with k_d in {0, sign(m_d)} can
-    // lie inside it (any other has a component of length >= L); otherwise
-    // all 27 with |k_d| <= 1 are tried.
-    float m[3], sg[3];
-    int sh[3];
+    // Minimum image m = dx - r L (r = rint(dx/L)); images t = m - k L.
+    // Images beyond rc32 (alpha rc32 <= EW32_XCUT) are left out.  When rc32
+    // is at most the smallest box length only the 8 images with k_d in
+    // {0, sign(m_d)} can lie inside it (any other has a component of length
+    // >= L); otherwise all 27 with |k_d| <= kmax are tried.  The reference's
+    // cube |r_d + k_d| <= nsum matters only for nsum < 2.
+    float m[3], sg[3], r[3];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-      const float r = rintf(dx[d] * iLf[d]);
-      sh[d] = (int)r;
-      m[d] = fmaf(-r, Lf[d], dx[d]);
+      r[d] = rintf(dx[d] * q.iL[d]);
+      m[d] = fmaf(-r[d], q.L[d], dx[d]);
       sg[d] = m[d] < 0.f ? -1.f : 1.f;
     }
+    const float ns = (float)q.nsum;
     float F0 = 0.f, F1 = 0.f, F2 = 0.f;
-    if (kmax == 0) {
+    if (q.kmax == 0) {
 #pragma unroll
       for (int c = 0; c < 8; ++c) {
         const int k0 = c & 1, k1 = (c >> 1) & 1, k2 = c >> 2;
-        const float t0 = k0 ? fmaf(-sg[0], Lf[0], m[0]) : m[0];
-        const float t1 = k1 ? fmaf(-sg[1], Lf[1], m[1]) : m[1];
-        const float t2 = k2 ? fmaf(-sg[2], Lf[2], m[2]) : m[2];
+        const float t0 = k0 ? fmaf(-sg[0], q.L[0], m[0]) : m[0];
+        const float t1 = k1 ? fmaf(-sg[1], q.L[1], m[1]) : m[1];
+        const float t2 = k2 ? fmaf(-sg[2], q.L[2], m[2]) : m[2];
         const float R2 = fmaf(t2, t2, fmaf(t1, t1, t0 * t0));
-        bool ok = R2 < rc2;
-        if (p.nsum < 2)
-          ok = ok && abs(sh[0] + k0 * (int)sg[0]) <= p.nsum && abs(sh[1] + k1 * (int)sg[1]) <= p.nsum &&
-               abs(sh[2] + k2 * (int)sg[2]) <= p.nsum;
+        bool ok = R2 < q.rc2;
+        if (q.nsum < 2)
+          ok = ok && fabsf(r[0] + (k0 ? sg[0] : 0.f)) <= ns && fabsf(r[1] + (k1 ? sg[1] : 0.f)) <= ns &&
+               fabsf(r[2] + (k2 ? sg[2] : 0.f)) <= ns;
         if (ok) {
-          const float mult = ew_h32(R2, alpha);
+          const float mult = ew_h32(R2, q.alpha);
           F0 = fmaf(t0, mult, F0);
           F1 = fmaf(t1, mult, F1);
           F2 = fmaf(t2, mult, F2);
         }
       }
     } else {
-      for (int k0 = -kmax; k0 <= kmax; ++k0) {
-        if (abs(sh[0] + k0) > p.nsum) continue;
-        const float t0 = fmaf(-(float)k0, Lf[0], m[0]);
-        for (int k1 = -kmax; k1 <= kmax; ++k1) {
-          if (abs(sh[1] + k1) > p.nsum) continue;
-          const float t1 = fmaf(-(float)k1, Lf[1], m[1]);
-          for (int k2 = -kmax; k2 <= kmax; ++k2) {
-            if (abs(sh[2] + k2) > p.nsum) continue;
-            const float t2 = fmaf(-(float)k2, Lf[2], m[2]);
+      for (int k0 = -q.kmax; k0 <= q.kmax; ++k0) {
+        const float f0 = (float)k0;
+        if (fabsf(r[0] + f0) > ns) continue;
+        const float t0 = fmaf(-f0, q.L[0], m[0]);
+        for (int k1 = -q.kmax; k1 <= q.kmax; ++k1) {
+          const float f1 = (float)k1;
+          if (fabsf(r[1] + f1) > ns) continue;
+          const float t1 = fmaf(-f1, q.L[1], m[1]);
+          for (int k2 = -q.kmax; k2 <= q.kmax; ++k2) {
+            const float f2 = (float)k2;
+            if (fabsf(r[2] + f2) > ns) continue;
+            const float t2 = fmaf(-f2, q.L[2], m[2]);
             const float R2 = fmaf(t2, t2, fmaf(t1, t1, t0 * t0));
-            if (R2 >= rc2) continue;
-            const float mult = ew_h32(R2, alpha);
+            if (R2 >= q.rc2) continue;
+            const float mult = ew_h32(R2, q.alpha);
             F0 = fmaf(t0, mult, F0);
             F1 = fmaf(t1, mult, F1);
             F2 = fmaf(t2, mult, F2);
@@ -2514,19 +2587,20 @@ __device__ inline void pair_eval32(const PairPrm &p, const float *Lf, const floa
         }
       }
     }
-    const float qs = (float)p.qs;
-    F[0] = qs * F0;
-    if (D > 1) F[1] = qs * F1;
-    if (D > 2) F[2] = qs * F2;
+    F[0] = q.qs * F0;
+    if (D > 1) F[1] = q.qs * F1;
+    if (D > 2) F[2] = q.qs * F2;
   }
 }
 
-// same tile/rotation scheme and scratch layout as k_pair_tiles, FP32 with
-// Kahan-compensated per-particle sums
+// same tile/rotation scheme as k_pair_tiles, on FP32 copies of the positions
+// and inverse masses; Kahan-compensated per-particle sums leave as (sum,
+// compensation) pairs in the partial slots, combined in double by
+// k_pair_finish32
 template <int D, int KIND>
-__global__ void __launch_bounds__(256, 3) k_pair_tiles32(Geo g, PairPrm p, const double *__restrict__ x,
-                                                      const double *__restrict__ m,
-                                                      double *__restrict__ out, int T, int jobs) {
+__global__ void __launch_bounds__(256, 3) k_pair_tiles32(Geo g, P32 q, const float *__restrict__ x,
+                                                      const float *__restrict__ im,
+                                                      float2 *__restrict__ out, int T, int jobs) {
   const int lane = threadIdx.x & 31;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   // persistent warps: tile jobs (slice j, tile pair I <= J) in round-robin
@@ -2540,29 +2614,15 @@ __global__ void __launch_bounds__(256, 3) k_pair_tiles32(Geo g, PairPrm p, const
     const int J = I + job;
     const int a = I * 32 + lane, b0 = J * 32 + lane;
     const bool va = a < g.N, vb = b0 < g.N;
-    float Lf[3], iLf[3];
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-      Lf[d] = (float)g.box[d];
-      iLf[d] = (float)g.inv_box[d];
-    }
-    const float alpha = (float)p.alpha;
-    // FP32 cut-off (EW32_XCUT); kmax 0 selects the 8-image search (rc32 <= min L)
-    const double rc32 = p.alpha > 0 ? fmin(p.rcut, (double)EW32_XCUT / p.alpha) : 0.0;
-    const float rc2 = (float)(rc32 * rc32);
-    const double Lmin = fmin(g.box[0], fmin(g.box[1], g.box[2]));
-    int kmax = p.kmax[0] > p.kmax[1] ? (p.kmax[0] > p.kmax[2] ? p.kmax[0] : p.kmax[2])
-                                     : (p.kmax[1] > p.kmax[2] ? p.kmax[1] : p.kmax[2]);
-    if (KIND == PAIR_EWALD_REAL && rc32 <= Lmin) kmax = 0;
     float xa[D], xb[D];
     Kahan fa[D], fb[D];
 #pragma unroll
     for (int d = 0; d < D; ++d) {
-      xa[d] = va ? (float)x[sidx(j, d, a, D, g.Ns)] : 0.f;
-      xb[d] = vb ? (float)x[sidx(j, d, b0, D, g.Ns)] : 0.f;
+      xa[d] = va ? x[sidx(j, d, a, D, g.Ns)] : 0.f;
+      xb[d] = vb ? x[sidx(j, d, b0, D, g.Ns)] : 0.f;
     }
-    const float ima = va ? (float)(1.0 / m[(size_t)j * g.Ns + a]) : 1.f;
-    float imb = vb ? (float)(1.0 / m[(size_t)j * g.Ns + b0]) : 1.f;
+    const float ima = va ? im[(size_t)j * g.Ns + a] : 1.f;
+    float imb = vb ? im[(size_t)j * g.Ns + b0] : 1.f;
     for (int s = 0; s < 32; ++s) {
       const int bi = J * 32 + ((lane + s) & 31);
       const bool act = va && bi < g.N && (I != J || a > bi);
@@ -2570,7 +2630,7 @@ __global__ void __launch_bounds__(256, 3) k_pair_tiles32(Geo g, PairPrm p, const
         float dx[D], F[D];
 #pragma unroll
         for (int d = 0; d < D; ++d) dx[d] = xa[d] - xb[d];
-        pair_eval32<D, KIND>(p, Lf, iLf, dx, F, alpha, rc2, kmax);
+        pair_eval32<D, KIND>(q, dx, F);
         const float inv = a > bi ? ima : imb;
 #pragma unroll
         for (int d = 0; d < D; ++d) {
@@ -2589,25 +2649,82 @@ __global__ void __launch_bounds__(256, 3) k_pair_tiles32(Geo g, PairPrm p, const
     }
     if (I == J) {
       if (va) {
+        // the diagonal tile's two sums for the same particle: Kahan-add them
 #pragma unroll
-        for (int d = 0; d < D; ++d)
-          out[(((size_t)I * g.P + j) * D + d) * g.Ns + a] = fa[d].value() + fb[d].value();
+        for (int d = 0; d < D; ++d) {
+          Kahan t = fa[d];
+          t.add(fb[d].s);
+          t.add(-fb[d].c);
+          out[(((size_t)I * g.P + j) * D + d) * g.Ns + a] = make_float2(t.s, t.c);
+        }
       }
     } else {
       if (va) {
 #pragma unroll
-        for (int d = 0; d < D; ++d) out[(((size_t)J * g.P + j) * D + d) * g.Ns + a] = fa[d].value();
+        for (int d = 0; d < D; ++d)
+          out[(((size_t)J * g.P + j) * D + d) * g.Ns + a] = make_float2(fa[d].s, fa[d].c);
       }
       if (vb) {
 #pragma unroll
-        for (int d = 0; d < D; ++d) out[(((size_t)I * g.P + j) * D + d) * g.Ns + b0] = fb[d].value();
+        for (int d = 0; d < D; ++d)
+          out[(((size_t)I * g.P + j) * D + d) * g.Ns + b0] = make_float2(fb[d].s, fb[d].c);
       }
     }
   }
 }
 
-// blocks of 256 threads resident at once (3 per SM), for the persistent grid
-static int pair32_grid(size_t warps_needed) {
+// FP32 copies of the positions and inverse masses for the FP32 pair kernel
+__global__ void k_to32(Geo g, const double *__restrict__ x, const double *__restrict__ m, float *__restrict__ x32,
+                       float *__restrict__ im32) {
+  const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < g.slots()) x32[t] = (float)x[t];
+  if (t < (size_t)g.P * g.Ns) im32[t] = (float)(1.0 / m[t]);
+}
+
+// f += scale * sum over the T partial slots of (sum - compensation), in double
+__global__ void k_pair_finish32(Geo g, const float2 *__restrict__ part, int T, double scale,
+                                double *__restrict__ f) {
+  const size_t s = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const size_t S = g.slots();
+  if (s >= S || (int)(s % g.Ns) >= g.N) return;
+  double acc = 0;
+  for (int t = 0; t < T; ++t) {
+    const float2 v = part[(size_t)t * S + s];
+    acc += (double)v.x - (double)v.y;
+  }
+  f[s] += acc * scale;
+}
+
+// Tile shape of the FP32 pair kernel: warps (32 x 32 pair tiles) per block,
+// by system shape.  Chosen by the autotuner (md_gb300_autotune_pair_x); 8
+// unless tuned.  Results do not depend on it: every tile job writes its own
+// partial-sum slots.
+static std::mutex g_tune_mu;
+static std::vector<std::pair<std::array<int, 4>, int>> g_tune;
+
+void set_pair32_warps(int kind, int D, int N, int P, int warps) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  for (auto &e : g_tune)
+    if (e.first == std::array<int, 4>{kind, D, N, P}) {
+      e.second = warps;
+      return;
+    }
+  g_tune.push_back({{kind, D, N, P}, warps});
+}
+
+int pair32_warps(int kind, int D, int N, int P) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  for (auto &e : g_tune)
+    if (e.first == std::array<int, 4>{kind, D, N, P}) return e.second;
+  return 8;
+}
+
+// persistent grid: as many blocks of `wpb` warps as the kernel keeps
+// resident, or fewer when the jobs run out
+template <int D, int K>
+static cudaError_t launch_pair32(const Geo &g, const P32 &q, const float *x, const float *im, float2 *part, int T,
+                                 int jobs, int wpb, cudaStream_t st) {
+  static int occ[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
   static int sms = 0;
   if (!sms) {
     int dev = 0;
@@ -2615,21 +2732,53 @@ static int pair32_grid(size_t warps_needed) {
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (sms <= 0) sms = 1;
   }
-  const size_t need = (warps_needed + 7) / 8, full = (size_t)sms * 3;
-  return (int)(need < full ? need : full);
+  if (!occ[wpb]) {
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[wpb], k_pair_tiles32<D, K>, wpb * 32, 0);
+    if (e != cudaSuccess) return e;
+    if (occ[wpb] < 1) occ[wpb] = 1;
+  }
+  const size_t need = ((size_t)jobs * g.P + wpb - 1) / wpb, full = (size_t)sms * occ[wpb];
+  k_pair_tiles32<D, K><<<(int)(need < full ? need : full), wpb * 32, 0, st>>>(g, q, x, im, part, T, jobs);
+  return cudaSuccess;
 }
 
 cudaError_t pair_force32(const Geo &g, const PairPrm &p, const double *x, const double *m, double *f,
                          double *scratch, cudaStream_t st) {
   const int T = (g.N + 31) / 32;
   const int jobs = T * (T + 1) / 2;
-  const int nb = pair32_grid((size_t)jobs * g.P);
+  int wpb = pair32_warps(p.kind, g.D, g.N, g.P);
+  if (wpb != 1 && wpb != 2 && wpb != 4 && wpb != 8) wpb = 8;
+  P32 q{};
+  for (int d = 0; d < 3; ++d) {
+    q.L[d] = (float)g.box[d];
+    q.iL[d] = (float)g.inv_box[d];
+  }
+  q.igs2 = p.s > 0 ? (float)(1.0 / (p.s * p.s)) : 0.f;
+  q.gpre = p.s > 0 ? (float)(p.g / (M_PI * p.s * p.s) * (2.0 / (p.s * p.s))) : 0.f;
+  q.qs = (float)p.qs;
+  q.alpha = (float)p.alpha;
+  q.nsum = p.nsum;
+  const double rc32 = p.alpha > 0 ? fmin(p.rcut, (double)EW32_XCUT / p.alpha) : 0.0;
+  q.rc2 = (float)(rc32 * rc32);
+  q.kmax = p.kmax[0] > p.kmax[1] ? (p.kmax[0] > p.kmax[2] ? p.kmax[0] : p.kmax[2])
+                                 : (p.kmax[1] > p.kmax[2] ? p.kmax[1] : p.kmax[2]);
+  if (p.kind == PAIR_EWALD_REAL && rc32 <= fmin(g.box[0], fmin(g.box[1], g.box[2]))) q.kmax = 0;
+  // scratch: T * slots float2 partials, then the FP32 positions and inverse masses
+  float2 *part = (float2 *)scratch;
+  float *x32 = (float *)(scratch + (size_t)T * g.slots());
+  float *im32 = x32 + g.slots();
+  {
+    XK_PROF("to32");
+    k_to32<<<cdiv(g.slots(), 256), 256, 0, st>>>(g, x, m, x32, im32);
+  }
+  cudaError_t le = XK_LAUNCHED();
+  if (le != cudaSuccess) return le;
   {
     XK_PROF(p.kind == PAIR_EWALD_REAL ? "pair_tiles32_ewald_real" : "pair_tiles32");
     switch (g.D * 16 + p.kind) {
 #define XK_P32_CASE(DV, K) \
   case DV * 16 + K:        \
-    k_pair_tiles32<DV, K><<<nb, 256, 0, st>>>(g, p, x, m, scratch, T, jobs); \
+    le = launch_pair32<DV, K>(g, q, x32, im32, part, T, jobs, wpb, st); \
     break;
       XK_P32_CASE(1, PAIR_GAUSSIAN)
       XK_P32_CASE(1, PAIR_PERIODIC_GAUSSIAN)
@@ -2649,11 +2798,12 @@ cudaError_t pair_force32(const Geo &g, const PairPrm &p, const double *x, const 
         return cudaErrorInvalidValue;
     }
   }
+  if (le != cudaSuccess) return le;
   cudaError_t e = XK_LAUNCHED();
   if (e != cudaSuccess) return e;
   {
     XK_PROF("pair_finish");
-    k_pair_finish<<<cdiv(g.slots(), 256), 256, 0, st>>>(g, scratch, T, 1.0 / g.P, f);
+    k_pair_finish32<<<cdiv(g.slots(), 256), 256, 0, st>>>(g, part, T, 1.0 / g.P, f);
   }
   return XK_LAUNCHED();
 }

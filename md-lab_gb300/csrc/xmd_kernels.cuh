@@ -188,6 +188,10 @@ cudaError_t recip_force_energy(const Geo &g, const Recip &r, const double *x, do
 // ---- mixed-precision form: FP32 arithmetic, compensated accumulation ----
 cudaError_t pair_force32(const Geo &g, const PairPrm &p, const double *x, const double *m,
                          double *f, double *scratch, cudaStream_t st);
+// tile shape (warps of 32 x 32 pair tiles per block: 1, 2, 4 or 8) of the
+// FP32 pair kernel for a system shape; 8 unless set
+void set_pair32_warps(int kind, int D, int N, int P, int warps);
+int pair32_warps(int kind, int D, int N, int P);
 // needs r.phase sized recip_phase_doubles(g, nsum) * 3 / 2 (FP32 copy behind)
 cudaError_t recip_force32(const Geo &g, const Recip &r, const double *x, double inv_mP, double *f,
                           cudaStream_t st);

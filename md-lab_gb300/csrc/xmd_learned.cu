@@ -902,7 +902,7 @@ __global__ void __launch_bounds__(DS_WARPS * 32) k_desc(Geo g, DescPrm p, const 
     d2 -= p.box[2] * rintf(d2 * p.inv_box[2]);
     const float r2 = d0 * d0 + d1 * d1 + d2 * d2;
     if (!live || c == l || !(r2 < rc2)) continue;
-    const float r = sqrtf(r2), u = 1.f - r2 * inv_rc2, fc = u * u;
+    const float ir = rsqrtf(r2), r = r2 * ir, u = 1.f - r2 * inv_rc2, fc = u * u;
     const float tb = r * p.inv_h - 0.5f;
     int b0 = (int)floorf(tb);
     float w1 = tb - (float)b0;
@@ -916,7 +916,6 @@ __global__ void __launch_bounds__(DS_WARPS * 32) k_desc(Geo g, DescPrm p, const 
     }
     atomicAdd(&hrow[b0 * DS_ROWS], fc * (1.f - w1));
     if (w1 > 0.f) atomicAdd(&hrow[(b0 + 1) * DS_ROWS], fc * w1);
-    const float ir = 1.f / r;
 #pragma unroll
     for (int m = 0; m < 3; ++m) {
       const float dr = r - p.vmu[m];

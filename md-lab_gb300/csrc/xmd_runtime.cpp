@@ -527,6 +527,62 @@ int md_gb300_capture_end_x(md_gb300_graph_t_x **out) {
   return 0;
 }
 
+// Branch streams of ensemble captures (created on first use, kept).
+static std::vector<cudaStream_t> g_branches;
+
+int md_gb300_capture_ensemble_x(int n, md_gb300_system_step_fn_x step, void *ctx, md_gb300_graph_t_x **out) {
+  if (n < 1 || !step || !out) return fail(MD_GB_ERR_ARG, "invalid ensemble capture arguments");
+  XMD_TRY(ensure_device());
+  if (capturing()) return fail(MD_GB_ERR_CAPTURE, "already capturing");
+  while ((int)g_branches.size() < n) {
+    cudaStream_t b;
+    XMD_CUDA(cudaStreamCreateWithFlags(&b, cudaStreamNonBlocking));
+    g_branches.push_back(b);
+  }
+  const cudaStream_t main = stream();
+  const cudaStream_t saved_user = g_user;
+  const bool saved_set = g_user_set;
+  std::vector<cudaEvent_t> ev(n + 1, nullptr);
+  for (auto &e : ev) XMD_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  int rc = 0;
+  cudaError_t ce = cudaStreamBeginCapture(main, cudaStreamCaptureModeThreadLocal);
+  if (ce == cudaSuccess) ce = cudaEventRecord(ev[n], main);
+  // every system's calls go to its own branch, forked from and joined to
+  // the library stream: independent chains of nodes in one graph
+  for (int i = 0; i < n && ce == cudaSuccess && !rc; ++i) {
+    ce = cudaStreamWaitEvent(g_branches[i], ev[n], 0);
+    if (ce != cudaSuccess) break;
+    g_user = g_branches[i];
+    g_user_set = true;
+    rc = step(i, ctx);
+    g_user = saved_user;
+    g_user_set = saved_set;
+    if (!rc) ce = cudaEventRecord(ev[i], g_branches[i]);
+  }
+  g_user = saved_user;
+  g_user_set = saved_set;
+  for (int i = 0; i < n && ce == cudaSuccess && !rc; ++i) ce = cudaStreamWaitEvent(main, ev[i], 0);
+  cudaGraph_t g = nullptr;
+  const cudaError_t ee = cudaStreamEndCapture(main, &g);
+  for (auto &e : ev) cudaEventDestroy(e);
+  if (rc || ce != cudaSuccess || ee != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    if (rc) return rc;
+    return cuda_fail(ce != cudaSuccess ? ce : ee, "ensemble capture");
+  }
+  md_gb300_graph *gr = new md_gb300_graph();
+  gr->g = g;
+  const cudaError_t ie = cudaGraphInstantiate(&gr->e, gr->g, 0);
+  if (ie != cudaSuccess) {
+    cudaGraphDestroy(gr->g);
+    delete gr;
+    return cuda_fail(ie, "cudaGraphInstantiate");
+  }
+  *out = gr;
+  return 0;
+}
+
 int md_gb300_graph_launch_x(md_gb300_graph_t_x *gr, int count) {
   if (!gr || count < 0) return fail(MD_GB_ERR_ARG, "invalid graph launch");
   for (int i = 0; i < count; ++i) XMD_CUDA(cudaGraphLaunch(gr->e, stream()));

@@ -439,6 +439,66 @@ int md_pimd_calc_pair_force_x(md_pimd_t_x *pimd, md_pair_force_t_x pf) {
   return 0;
 }
 
+int md_gb300_set_pair_tile_x(md_pair_force_t_x pf, int N, int P, int warps) {
+  const int kind = pair_kind_of((const void *)pf, false);
+  if (!kind) return fail(MD_GB_ERR_UNSUPPORTED, "pair force function has no device kernel");
+  if (warps != 1 && warps != 2 && warps != 4 && warps != 8) return fail(MD_GB_ERR_ARG, "warps must be 1, 2, 4 or 8");
+  if (N < 1 || P < 1) return fail(MD_GB_ERR_ARG, "invalid system shape");
+  xk::set_pair32_warps(kind, D, N, P, warps);
+  return 0;
+}
+
+// Tile-shape autotuner of the FP32 pair kernel (md_gb300_x.h): times each
+// shape on this system's own positions into a scratch force array.
+int md_gb300_autotune_pair_x(md_pimd_t_x *pimd, md_pair_force_t_x pf, int repeats, int *warps, double *ms) {
+  const int kind = pair_kind_of((const void *)pf, false);
+  if (!kind) return fail(MD_GB_ERR_UNSUPPORTED, "pair force function has no device kernel");
+  if (repeats < 1) return fail(MD_GB_ERR_ARG, "repeats must be positive");
+  if (capturing()) return fail(MD_GB_ERR_CAPTURE, "autotuning times kernels; not while capturing");
+  SimDev *sd;
+  PimdDev *pd;
+  XMD_TRY(pimd_device(pimd, &sd, &pd));
+  if (kind == xk::PAIR_EWALD_REAL && D != 3) return fail(MD_GB_ERR_UNSUPPORTED, "Ewald is 3D only");
+  int rc;
+  double *scr = scratch_for(sd, general_scratch(sd->geo), &rc);
+  if (rc) return rc;
+  xk::PairPrm prm = pair_params(kind);
+  ewald_shifts(prm, sd->geo);
+  const xk::Geo &g = sd->geo;
+  DevBuf ftmp;
+  XMD_TRY(reserve(ftmp, g.slots() * sizeof(double)));
+  cudaStream_t st = stream();
+  cudaEvent_t a = nullptr, b = nullptr;
+  cudaError_t e = cudaEventCreate(&a);
+  if (e == cudaSuccess) e = cudaEventCreate(&b);
+  const int cand[4] = {1, 2, 4, 8};
+  int best_w = 8;
+  double best = INFINITY;
+  for (int ci = 0; ci < 4 && e == cudaSuccess; ++ci) {
+    xk::set_pair32_warps(kind, D, g.N, g.P, cand[ci]);
+    e = xk::pair_force32(g, prm, sd->x.as<double>(), sd->m.as<double>(), ftmp.as<double>(), scr, st);
+    if (e == cudaSuccess) e = cudaEventRecord(a, st);
+    for (int r = 0; r < repeats && e == cudaSuccess; ++r)
+      e = xk::pair_force32(g, prm, sd->x.as<double>(), sd->m.as<double>(), ftmp.as<double>(), scr, st);
+    if (e == cudaSuccess) e = cudaEventRecord(b, st);
+    if (e == cudaSuccess) e = cudaEventSynchronize(b);
+    float t = 0;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&t, a, b);
+    if (e == cudaSuccess && t / repeats < best) {
+      best = t / repeats;
+      best_w = cand[ci];
+    }
+  }
+  if (a) cudaEventDestroy(a);
+  if (b) cudaEventDestroy(b);
+  release(ftmp);
+  xk::set_pair32_warps(kind, D, g.N, g.P, best_w);
+  if (e != cudaSuccess) return cuda_fail(e, "pair-kernel autotuning");
+  if (warps) *warps = best_w;
+  if (ms) *ms = best;
+  return 0;
+}
+
 int md_gb300_set_precision_x(int mode) {
   if (mode != MD_GB_PRECISION_FP64 && mode != MD_GB_PRECISION_MIXED)
     return fail(MD_GB_ERR_ARG, "unknown precision mode %d", mode);

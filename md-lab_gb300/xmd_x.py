@@ -153,6 +153,9 @@ class XLib:
                 "md_gb300_get_precision_x": (_i, []),
                 "md_gb300_pair_force_noalloc_x": (_i, [_vp, _vp, _vp, _vp, _i, _i, _i, _dp, _vp]),
                 "md_gb300_tc_selftest_x": (_i, [_dp]),
+                "md_gb300_autotune_pair_x": (_i, [pp, _vp, _i, C.POINTER(_i), _dp]),
+                "md_gb300_set_pair_tile_x": (_i, [_vp, _i, _i, _i]),
+                "md_gb300_capture_ensemble_x": (_i, [_i, _vp, _vp, C.POINTER(_vp)]),
                 "md_gb300_ewald_model_nparam_x": (_i, []),
                 "md_gb300_ewald_model_create_x": (_i, [C.POINTER(_vp), pp, _i, C.c_long, C.c_uint]),
                 "md_gb300_ewald_model_free_x": (None, [_vp]),

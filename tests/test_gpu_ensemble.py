@@ -1,0 +1,118 @@
+"""Ensembles: several independent systems advanced by one CUDA graph (one
+launch per step, each system on its own branch), and the tile-shape
+autotuner of the FP32 pair kernel.  The ensemble must give bit-for-bit the
+states that stepping each system on its own gives; the autotuner's choice
+must not change any force."""
+import ctypes as C
+import math
+
+import numpy as np
+import pytest
+
+import xmd_x
+from gpu_common import random_state
+
+pytestmark = pytest.mark.gpu
+
+STEP_FN = C.CFUNCTYPE(C.c_int, C.c_int, C.c_void_p)
+
+
+@pytest.fixture(scope="module")
+def lib():
+    return xmd_x.load(3, 4)
+
+
+def make(lib, spec, seed):
+    kind, N, P, vi, beta = spec
+    T = 1.0 / beta
+    if kind == "ueg":
+        box = (4 * math.pi * N / 3) ** (1 / 3) * 2.0
+        st = random_state(3, 4, N, P, T, box, True, seed)
+    else:
+        box = 10.0
+        st = random_state(3, 4, N, P, T, box, False, seed)
+    s = xmd_x.PimdSystem(lib, N, P, vi, T, box=box)
+    s.set_state(**st)
+    return s, box
+
+
+def potentials(lib, kind, box):
+    if kind == "ueg":
+        xmd_x.set_potentials(lib, coul_s=1.0, alpha=5.6 / box, nsum=4)
+    else:
+        xmd_x.set_potentials(lib, trap_w=1.0, gauss_g=0.75 * math.pi, gauss_s=0.5)
+
+
+def step(lib, kind, s, box):
+    potentials(lib, kind, box)
+    if kind == "ueg":
+        xmd_x.md_step(lib, s, 0.05, image=1, pair=lib.fn("md_coulomb_3d_ewald_force_x"), pbc=True)
+    else:
+        xmd_x.md_step(lib, s, 0.005, trap=lib.fn("md_harmonic_trap_force_x"), pair=lib.fn("md_gaussian_force_x"))
+
+
+SPECS = [("trap", 8, 16, 1.0, 2.0), ("ueg", 16, 8, 0.5, 1.0), ("trap", 12, 32, 0.25, 4.0), ("ueg", 24, 16, 0.75, 3.0)]
+
+
+@pytest.mark.parametrize("mixed", [0, 1])
+def test_ensemble_graph_matches_individual_steps(lib, mixed):
+    lib.check(lib.md_gb300_set_precision_x(mixed))
+    try:
+        ens = [make(lib, sp, 100 + i) for i, sp in enumerate(SPECS)]
+        ref = [make(lib, sp, 100 + i) for i, sp in enumerate(SPECS)]
+        for (s, box), sp in zip(ens + ref, SPECS + SPECS):
+            step(lib, sp[0], s, box)  # device state and tables exist before capture
+
+        def cb(i, ctx):
+            try:
+                s, box = ens[i]
+                step(lib, SPECS[i][0], s, box)
+                return 0
+            except Exception:
+                return -1
+
+        fn = STEP_FN(cb)
+        g = C.c_void_p()
+        lib.check(lib.md_gb300_capture_ensemble_x(len(SPECS), C.cast(fn, C.c_void_p), None, C.byref(g)),
+                  "ensemble capture")
+        assert lib.md_gb300_graph_kernel_count_x(g) > 10 * len(SPECS)
+        lib.check(lib.md_gb300_graph_launch_x(g, 3))
+        lib.check(lib.md_gb300_synchronize_x())
+        for _ in range(3):
+            for (s, box), sp in zip(ref, SPECS):
+                step(lib, sp[0], s, box)
+        for (a, _), (b, _) in zip(ens, ref):
+            sa, sb = a.state(), b.state()
+            for k in ("x", "v", "f", "vtheta", "theta"):
+                np.testing.assert_array_equal(sa[k], sb[k])
+        lib.md_gb300_graph_free_x(g)
+        for s, _ in ens + ref:
+            s.free()
+    finally:
+        lib.check(lib.md_gb300_set_precision_x(0))
+
+
+def test_autotuned_tile_shape_leaves_forces_unchanged(lib):
+    lib.check(lib.md_gb300_set_precision_x(1))
+    try:
+        for kind, N, P in (("ueg", 48, 16), ("trap", 32, 32)):
+            s, box = make(lib, (kind, N, P, 0.5, 2.0), 7)
+            potentials(lib, kind, box)
+            pf = lib.fn("md_coulomb_3d_ewald_force_x" if kind == "ueg" else "md_gaussian_force_x")
+            forces = []
+            for wpb in (1, 2, 4, 8):
+                lib.check(lib.md_gb300_set_pair_tile_x(pf, N, P, wpb))
+                lib.check(lib.md_reset_force_x(s.sim))
+                lib.check(lib.md_pimd_calc_pair_force_x(s.pimd, pf))
+                forces.append(s.state()["f"])
+            w, ms = C.c_int(), C.c_double()
+            lib.check(lib.md_gb300_autotune_pair_x(s.pimd, pf, 3, C.byref(w), C.byref(ms)), "autotune")
+            assert w.value in (1, 2, 4, 8) and ms.value > 0
+            lib.check(lib.md_reset_force_x(s.sim))
+            lib.check(lib.md_pimd_calc_pair_force_x(s.pimd, pf))
+            forces.append(s.state()["f"])
+            for f in forces[1:]:
+                np.testing.assert_array_equal(f, forces[0])
+            s.free()
+    finally:
+        lib.check(lib.md_gb300_set_precision_x(0))
