@@ -210,7 +210,23 @@ def kernel_flops(name, nsum=NSUM):
     if name in ("pair_tiles_ewald_real", "pair_tiles32_ewald_real"):
         pairs = P * N * (N - 1) / 2
         return pairs * (47.0 * n_images() + 39.0)
+    if name == "desc":
+        # per ordered pair: 12 flop for the minimum-image distance, and for the
+        # (4/3) pi (1/2)^3 = 52% inside rc = L/2 another 45 (cut-off weight,
+        # bins, two deposits, three vector features); per particle the
+        # 128 x 64 histogram-to-feature product
+        return N * N * P * (12.0 + 0.5236 * 45.0) + N * P * 2.0 * 128 * 64
+    if name == "mlp_forward":
+        return 2.0 * N * P * (64 * 128 + 128 * 128 + 128 * 16)
     return None
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return json.load(fh)
+    except (OSError, ValueError):
+        return {}
 
 
 def make_system(lib):
@@ -289,9 +305,14 @@ class Runner:
 
 
 def roofline(prof, peak, peak_name, unit_nsum=NSUM):
-    """FLOP roofline of the step's dominant kernel from its live per-launch time"""
+    """FLOP roofline of the step's dominant arithmetic kernel (the largest
+    with a FLOP model) from its live per-launch time; the overall largest
+    kernel is named beside it (the exchange recursion is latency-bound: N
+    dependent steps, no FLOP or byte roofline applies)"""
     total = sum(v[0] for v in prof.values())
-    name, (ms, launches) = max(prof.items(), key=lambda kv: kv[1][0])
+    top_name, (top_ms, _) = max(prof.items(), key=lambda kv: kv[1][0])
+    modelled = {k: v for k, v in prof.items() if kernel_flops(k, unit_nsum)}
+    name, (ms, launches) = max(modelled.items(), key=lambda kv: kv[1][0])
     per_launch_ms = ms / max(launches, 1)
     roof = {"kernel": name, "bound": "fp64" if peak_name == "fp64" else "fp32", "unit": "TFLOP/s",
             "share": ms / total if total else None, "launch_ms": per_launch_ms, "peak": peak,
@@ -302,6 +323,10 @@ def roofline(prof, peak, peak_name, unit_nsum=NSUM):
         roof["algorithmic_flop_per_launch"] = flops
         roof["achieved"] = flops / (per_launch_ms * 1e-3) / 1e12
         roof["frac"] = roof["achieved"] / peak if peak > 0 else None
+    roof["step_top_kernel"] = {"kernel": top_name, "share": top_ms / total if total else None,
+                               "ms_per_step": top_ms}
+    if "solve" in top_name:
+        roof["step_top_kernel"]["bound"] = f"latency: {N} dependent substitution steps, 2 SMs"
     return roof
 
 
@@ -313,6 +338,8 @@ def learned_form(lib, R, s, pair, step, args, ws):
     judgement are inside the timed region)."""
     import xmd_x
     lib.check(lib.md_gb300_set_precision_x(1))
+    box, _ = workload()
+    xmd_x.set_potentials(lib, coul_s=1.0, alpha=ALPHA_L / box, nsum=NSUM)
     m = xmd_x.EwaldModel(lib, s, nsum_cheap=NSUM_CHEAP, capacity=args.learn_configs, seed=7)
     t0 = time.perf_counter()
     for _ in range(args.learn_configs):
@@ -467,6 +494,8 @@ def ensemble_form(lib, R, args):
     for _, s, _ in systems:
         s.free()
     lib.check(lib.md_gb300_set_precision_x(0))
+    box, _ = workload()  # the ensemble left its last system's parameters in the globals
+    xmd_x.set_potentials(lib, coul_s=1.0, alpha=ALPHA_L / box, nsum=NSUM)
     return {"value": beads / (ms * 1e-3), "unit": "bead-steps/s", "ms_per_step": ms, "systems": len(specs),
             "bead_slots": beads, "kernels_per_launch": kernels, "steps_timed": nst,
             "sequential_graphs_ms_per_step": ms_seq, "gain_vs_sequential": ms_seq / ms,
@@ -498,41 +527,46 @@ def run_gb300(args, dist, rank, ws):
         lib.md_gb300_graph_free_x(g)
         return ms, kps, wall, clocks
 
-    # plain FP64: the form that reproduces MD-Lab to 1e-10
-    lib.check(lib.md_gb300_set_precision_x(0))
-    plain_ms, plain_kps, plain_wall, plain_clocks = graph_form()
-    plain_prof = R.profile(step)
-    fp64_peak = lib.md_gb300_fp64_peak_x()
-    forms = {"plain_fp64": {"value": ws * N * P / (plain_ms * 1e-3), "ms_per_step": plain_ms,
-                            "kernels_per_step": plain_kps, "clocks": plain_clocks,
-                            "kernel_ms_per_step": {k: v[0] for k, v in plain_prof.items()},
-                            "roofline": roofline(plain_prof, fp64_peak, "fp64")}}
-    # mixed precision, converged Ewald
-    import numpy as np
-
-    def forces(mode):
-        lib.check(lib.md_gb300_set_precision_x(mode))
-        lib.check(lib.md_reset_force_x(s.sim))
-        lib.check(lib.md_pimd_calc_pair_force_x(s.pimd, pair))
-        return s.state()["f"]
-
-    f64, f32 = forces(0), forces(1)
-    ferr = float(np.max(np.abs(f32 - f64)) / np.max(np.abs(f64)))
-    mixed_ms, mixed_kps, _, mixed_clocks = graph_form()
-    mixed_prof = R.profile(step)
+    want = set(args.forms.split(","))
+    forms = {}
+    if "plain" in want:
+        # plain FP64: the form that reproduces MD-Lab to 1e-10
+        lib.check(lib.md_gb300_set_precision_x(0))
+        plain_ms, plain_kps, plain_wall, plain_clocks = graph_form()
+        plain_prof = R.profile(step)
+        fp64_peak = lib.md_gb300_fp64_peak_x()
+        forms["plain_fp64"] = {"value": ws * N * P / (plain_ms * 1e-3), "ms_per_step": plain_ms,
+                               "kernels_per_step": plain_kps, "clocks": plain_clocks,
+                               "kernel_ms_per_step": {k: v[0] for k, v in plain_prof.items()},
+                               "roofline": roofline(plain_prof, fp64_peak, "fp64")}
     fp32_peak = lib.md_gb300_fp32_peak_x()
-    forms["mixed_fp32_forces"] = {"value": ws * N * P / (mixed_ms * 1e-3), "ms_per_step": mixed_ms,
-                                  "kernels_per_step": mixed_kps, "force_error_vs_fp64": ferr,
-                                  "clocks": mixed_clocks,
-                                  "kernel_ms_per_step": {k: v[0] for k, v in mixed_prof.items()}}
-    if not args.no_ensemble:
+    if "mixed" in want:
+        # mixed precision, converged Ewald
+        import numpy as np
+
+        def forces(mode):
+            lib.check(lib.md_gb300_set_precision_x(mode))
+            lib.check(lib.md_reset_force_x(s.sim))
+            lib.check(lib.md_pimd_calc_pair_force_x(s.pimd, pair))
+            return s.state()["f"]
+
+        f64, f32 = forces(0), forces(1)
+        ferr = float(np.max(np.abs(f32 - f64)) / np.max(np.abs(f64)))
+        mixed_ms, mixed_kps, _, mixed_clocks = graph_form()
+        mixed_prof = R.profile(step)
+        forms["mixed_fp32_forces"] = {"value": ws * N * P / (mixed_ms * 1e-3), "ms_per_step": mixed_ms,
+                                      "kernels_per_step": mixed_kps, "force_error_vs_fp64": ferr,
+                                      "clocks": mixed_clocks,
+                                      "kernel_ms_per_step": {k: v[0] for k, v in mixed_prof.items()}}
+    if "ensemble" in want:
         forms["ensemble_64"] = ensemble_form(lib, R, args)
-    headline = "plain_fp64"
+    headline = "plain_fp64" if "plain" in want else "mixed_fp32_forces"
     model = None
-    if not args.no_learned:
+    if "learned" in want:
         model, lform, lprof, lkps = learned_form(lib, R, s, pair, step, args, ws)
         lform["roofline"] = roofline(lprof, fp32_peak, "fp32")
-        lform["speedup_vs_plain_fp64"] = lform["value"] / forms["plain_fp64"]["value"]
+        if "plain_fp64" in forms:
+            lform["speedup_vs_plain_fp64"] = lform["value"] / forms["plain_fp64"]["value"]
         forms["learned_fp32"] = lform
         headline = "learned_fp32"
     H = forms[headline]
@@ -567,11 +601,11 @@ def run_gb300(args, dist, rank, ws):
               "gpu_launches": kps * H.get("steps_timed", args.steps), "forms": forms,
               "e2e": {"value": ws * N * P / e2e_s, "unit": "bead-steps/s", "h2d_bytes_per_step": h2d,
                       "d2h_bytes_per_step": h2d + 8, "steps": ke, "form": headline},
-              "roofline": H.get("roofline", forms["plain_fp64"]["roofline"]),
+              "roofline": H.get("roofline", forms.get("plain_fp64", {}).get("roofline")),
               "clocks": H["clocks"]}
     if headline == "learned_fp32":
         result["delta_E_per_particle_Ha"] = H["delta_E_per_particle_Ha"]
-        result["speedup_vs_plain_fp64"] = H["speedup_vs_plain_fp64"]
+        result["speedup_vs_plain_fp64"] = H.get("speedup_vs_plain_fp64")
     if rank == 0 and ws == 1 and not args.no_cpu:
         st, sample = cpu_step_estimate(1, args.cpu_budget)
         result["cpu_baseline"] = {"value": N * P / st, "unit": "bead-steps/s", "cores": 1,
@@ -610,8 +644,8 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--cpu-budget", type=float, default=8.0, help="seconds of CPU sample")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--no-learned", action="store_true", help="skip the learned form")
-    ap.add_argument("--no-ensemble", action="store_true", help="skip the 64-system ensemble")
+    ap.add_argument("--forms", default="plain,mixed,ensemble,learned",
+                    help="forms to run (comma list of plain, mixed, ensemble, learned)")
     ap.add_argument("--learn-configs", type=int, default=3125,
                     help="configurations collected for training (x P bead slices)")
     ap.add_argument("--learn-steps", type=int, default=3000)

@@ -37,6 +37,18 @@ int ensure_device();       // MD_GB_ERR_NO_DEVICE when CUDA has no device
 bool device_present();     // without setting an error
 cudaStream_t stream();
 bool capturing();
+struct SimDev;
+// side stream of the exchange chain (xmd_runtime.cpp): fork from the library
+// stream, mark its work (with the simulation whose exchange forces wait in
+// fex) for the next join; join_side makes the library stream wait and adds
+// fex to f.  NoJoin suppresses the join for the calls that may overlap.
+int side_begin(cudaStream_t *side);
+int side_end(SimDev *fex);
+int join_side();
+struct NoJoin {
+  NoJoin();
+  ~NoJoin();
+};
 
 struct DevBuf {
   void *p = nullptr;
@@ -63,12 +75,15 @@ struct SimDev {
   DevBuf cf, c0, c2;
   DevBuf stage;    // AoS records on the device
   DevBuf scratch;  // partial sums of pair / exchange / reduction kernels
+  DevBuf fex;      // exchange spring forces computed on the side stream
+  DevBuf xscr;     // partial sums of the exchange forces (side stream)
 };
 
 struct PimdDev {
   bool valid = false;  // ENk / ENk2 / VBN / Eint on the device authoritative
   DevBuf ENk, ENk2, Eint, VBN, tmpV, G;
   DevBuf linkt;  // N x N bead-P -> bead-1 springs (scratch of the ENk fill)
+  DevBuf lnn;    // ln l for l = 0..N (entry 0 unused), host values
   DevBuf rec;  // weights of the forward and backward recursions (two halves)
   // tmpV (backward recursion) computed by the last md_pimd_fill_VB_x from
   // the current ENk with these beta and vi

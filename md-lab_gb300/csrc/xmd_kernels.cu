@@ -302,10 +302,16 @@ __device__ inline void chain_forces(const ChainState<L> &c, double kin, double c
 template <int L>
 __device__ inline void chain_odd(ChainState<L> &c, double h, const double *nhf) {
   constexpr int M2 = L / 2;
+  // exp(-h x / 2) is taken as exp(-h x / 4)^2 (one FP64 exp instead of two,
+  // equal to rounding); the last member has no successor, both factors are 1
 #pragma unroll
   for (int j = 1; j <= M2; ++j) {
-    const double nxt = (j == M2) ? 0.0 : c.vt[2 * j];
-    c.vt[2 * j - 1] = c.vt[2 * j - 1] * exp(-0.5 * h * nxt) + 0.5 * h * nhf[2 * j - 1] * exp(-0.25 * h * nxt);
+    if (j == M2) {
+      c.vt[2 * j - 1] = c.vt[2 * j - 1] + 0.5 * h * nhf[2 * j - 1];
+    } else {
+      const double e = exp(-0.25 * h * c.vt[2 * j]);
+      c.vt[2 * j - 1] = c.vt[2 * j - 1] * (e * e) + 0.5 * h * nhf[2 * j - 1] * e;
+    }
   }
 }
 
@@ -337,7 +343,8 @@ __global__ void __launch_bounds__(256) k_nhc_fast(Geo g, int half, double *__res
   double nhf[L];
   if (half == 1) chain_forces<L>(c, mass * vv * vv, 1.0, kT, nhf);
   // thermostatted half kick: md_simulation_x.c:674-678
-  vv = vv * exp(-0.5 * h * c.vt[0]) + 0.5 * h * F * exp(-0.25 * h * c.vt[0]);
+  const double ek = exp(-0.25 * h * c.vt[0]);
+  vv = vv * (ek * ek) + 0.5 * h * F * ek;
 #pragma unroll
   for (int k = 1; k <= M2; ++k) c.th[2 * k - 2] = c.th[2 * k - 2] + h * c.vt[2 * k - 2] / 2;
   if (half == 2) chain_forces<L>(c, mass * vv * vv, 1.0, kT, nhf);
@@ -349,8 +356,10 @@ __global__ void __launch_bounds__(256) k_nhc_fast(Geo g, int half, double *__res
     chain_forces<L>(c, mass * vv * vv, 1.0, kT, nhf);
 #pragma unroll
     for (int k = 1; k <= M2; ++k)
-      c.vt[2 * k - 2] = c.vt[2 * k - 2] * exp(-h * c.vt[2 * k - 1]) +
-                        h * nhf[2 * k - 2] * exp(-0.5 * h * c.vt[2 * k - 1]);
+      {
+        const double e = exp(-0.5 * h * c.vt[2 * k - 1]);
+        c.vt[2 * k - 2] = c.vt[2 * k - 2] * (e * e) + h * nhf[2 * k - 2] * e;
+      }
   }
   v[s] = vv;
 #pragma unroll
@@ -399,7 +408,7 @@ __global__ void k_nhc_grouped(Geo g, int half, int nf, const int *__restrict__ c
   };
   double nhf[L];
   if (half == 1) chain_forces<L>(c, kinetic(), cfv, kT, nhf);
-  const double e1 = exp(-0.5 * h * c.vt[0]), e2 = exp(-0.25 * h * c.vt[0]);
+  const double e2 = exp(-0.25 * h * c.vt[0]), e1 = e2 * e2;
   for (int q = 0; q < f2; ++q) {
     const size_t s = slot(f0 + q);
     v[s] = v[s] * e1 + 0.5 * h * f[s] * e2;
@@ -418,8 +427,10 @@ __global__ void k_nhc_grouped(Geo g, int half, int nf, const int *__restrict__ c
     chain_forces<L>(c, kinetic(), cfv, kT, nhf);
 #pragma unroll
     for (int k = 1; k <= M2; ++k)
-      c.vt[2 * k - 2] = c.vt[2 * k - 2] * exp(-h * c.vt[2 * k - 1]) +
-                        h * nhf[2 * k - 2] * exp(-0.5 * h * c.vt[2 * k - 1]);
+      {
+        const double e = exp(-0.5 * h * c.vt[2 * k - 1]);
+        c.vt[2 * k - 2] = c.vt[2 * k - 2] * (e * e) + h * nhf[2 * k - 2] * e;
+      }
   }
 #pragma unroll
   for (int k = 0; k < L; ++k) {
@@ -792,37 +803,39 @@ __device__ inline void ext_norm(double &m, int &e) {
 // packed lower triangle: row i (1..N), column j (0..i-1) at tri(i) + j
 __device__ inline size_t moff(int i, int j) { return (size_t)i * (i - 1) / 2 + j; }
 
-// forward weights M_{n,j}, one warp per row n
-__global__ void k_vb_weights(int N, double beta, double vi, const double *__restrict__ ENk,
-                             double *__restrict__ Mm, int *__restrict__ Me) {
-  const int n = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) + 1;
-  const int lane = threadIdx.x & 31;
-  if (n > N) return;
-  const double lnvi = vi != 0.0 ? log(vi) : 0.0;
-  const double lnn = log((double)n);
-  for (int j = lane; j < n; j += 32) {
-    const int k = n - j;
+// Both weight triangles in one launch: block (row, direction), threads
+// along the row.  Forward row n: M_{n,j} = exp(-beta ENk[n][n-j] + (n-j-1)
+// ln xi - ln n); backward row i <-> u = N-i+1, column j <-> l = N-j:
+// exp(-beta ENk[l][i-j] + (i-j-1) ln xi - ln l).  ln xi and the table
+// lnn[l] = ln l come from the host.
+__global__ void __launch_bounds__(128) k_weights(int N, double beta, double vi, double lnvi,
+                                                 const double *__restrict__ ENk, const double *__restrict__ lnn,
+                                                 double *__restrict__ Mf, int *__restrict__ Ef,
+                                                 double *__restrict__ Mb, int *__restrict__ Eb, int first) {
+  const int row = blockIdx.x + 1;
+  const int dir = first + blockIdx.y;
+  double *Mm = dir ? Mb : Mf;
+  int *Me = dir ? Eb : Ef;
+  for (int j = threadIdx.x; j < row; j += blockDim.x) {
+    const int k = row - j;
+    const int l = dir ? N - j : row;
     Ext w{0.0, 0};
-    if (vi != 0.0 || k == 1) w = ext_exp(-beta * ENk[dtri(n) + k - 1] + (k - 1) * lnvi - lnn);
-    Mm[moff(n, j)] = w.m;
-    Me[moff(n, j)] = w.e;
+    if (vi != 0.0 || k == 1) w = ext_exp(-beta * ENk[dtri(l) + k - 1] + (k - 1) * lnvi - lnn[l]);
+    Mm[moff(row, j)] = w.m;
+    Me[moff(row, j)] = w.e;
   }
 }
 
-// backward weights M'_{i,j}, row i <-> u = N-i+1, column j <-> l = N-j
-__global__ void k_tv_weights(int N, double beta, double vi, const double *__restrict__ ENk,
-                             double *__restrict__ Mm, int *__restrict__ Me) {
-  const int i = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) + 1;
-  const int lane = threadIdx.x & 31;
-  if (i > N) return;
+static cudaError_t weights(int N, double beta, double vi, const double *ENk, const double *lnn, double *rs_f,
+                           double *rs_b, int first, int count, cudaStream_t st) {
   const double lnvi = vi != 0.0 ? log(vi) : 0.0;
-  for (int j = lane; j < i; j += 32) {
-    const int k = i - j, l = N - j;
-    Ext w{0.0, 0};
-    if (vi != 0.0 || k == 1) w = ext_exp(-beta * ENk[dtri(l) + k - 1] + (k - 1) * lnvi - log((double)l));
-    Mm[moff(i, j)] = w.m;
-    Me[moff(i, j)] = w.e;
+  dim3 grid(N, count);
+  {
+    XK_PROF("weights");
+    k_weights<<<grid, 128, 0, st>>>(N, beta, vi, lnvi, ENk, lnn, rs_f, rs_f ? (int *)(rs_f + ntri(N)) : nullptr,
+                                    rs_b, rs_b ? (int *)(rs_b + ntri(N)) : nullptr, first);
   }
+  return XK_LAUNCHED();
 }
 
 // X_0 = 1, X_i = sum_{j<i} M_{i,j} X_j (i = 1..N); out_i = -ln(X_i)/beta written
@@ -1109,45 +1122,23 @@ static TriJob tri_job(int N, double *rs_f, double *rs_b, double *VBN, double *tm
   return j;
 }
 
-cudaError_t fill_vb(int N, double beta, double vi, const double *ENk, double *VBN, double *rs,
+cudaError_t fill_vb(int N, double beta, double vi, const double *ENk, const double *lnn, double *VBN, double *rs,
                     cudaStream_t st) {
-  double *Mm = rs;
-  int *Me = (int *)(rs + ntri(N));
-  {
-    XK_PROF("vb_weights");
-    k_vb_weights<<<cdiv((size_t)N * 32, 256), 256, 0, st>>>(N, beta, vi, ENk, Mm, Me);
-  }
-  cudaError_t e = XK_LAUNCHED();
+  cudaError_t e = weights(N, beta, vi, ENk, lnn, rs, nullptr, 0, 1, st);
   if (e != cudaSuccess) return e;
   return tri_solve(N, beta, tri_job(N, rs, nullptr, VBN, nullptr), 0, 1, st);
 }
 
-cudaError_t back_vb(int N, double beta, double vi, const double *ENk, double *tmpV, double *rs,
+cudaError_t back_vb(int N, double beta, double vi, const double *ENk, const double *lnn, double *tmpV, double *rs,
                     cudaStream_t st) {
-  double *Mm = rs;
-  int *Me = (int *)(rs + ntri(N));
-  {
-    XK_PROF("tv_weights");
-    k_tv_weights<<<cdiv((size_t)N * 32, 256), 256, 0, st>>>(N, beta, vi, ENk, Mm, Me);
-  }
-  cudaError_t e = XK_LAUNCHED();
+  cudaError_t e = weights(N, beta, vi, ENk, lnn, nullptr, rs, 1, 1, st);
   if (e != cudaSuccess) return e;
   return tri_solve(N, beta, tri_job(N, nullptr, rs, nullptr, tmpV), 1, 1, st);
 }
 
-cudaError_t fill_vb_tv(int N, double beta, double vi, const double *ENk, double *VBN, double *tmpV, double *rs_f,
-                       double *rs_b, cudaStream_t st) {
-  {
-    XK_PROF("vb_weights");
-    k_vb_weights<<<cdiv((size_t)N * 32, 256), 256, 0, st>>>(N, beta, vi, ENk, rs_f, (int *)(rs_f + ntri(N)));
-  }
-  cudaError_t e = XK_LAUNCHED();
-  if (e != cudaSuccess) return e;
-  {
-    XK_PROF("tv_weights");
-    k_tv_weights<<<cdiv((size_t)N * 32, 256), 256, 0, st>>>(N, beta, vi, ENk, rs_b, (int *)(rs_b + ntri(N)));
-  }
-  e = XK_LAUNCHED();
+cudaError_t fill_vb_tv(int N, double beta, double vi, const double *ENk, const double *lnn, double *VBN,
+                       double *tmpV, double *rs_f, double *rs_b, cudaStream_t st) {
+  cudaError_t e = weights(N, beta, vi, ENk, lnn, rs_f, rs_b, 0, 2, st);
   if (e != cudaSuccess) return e;
   return tri_solve(N, beta, tri_job(N, rs_f, rs_b, VBN, tmpV), 0, 2, st);
 }
@@ -2261,6 +2252,19 @@ cudaError_t force_virial(const Geo &g, const double *x, const double *f, const d
   cudaError_t e = XK_LAUNCHED();
   if (e != cudaSuccess) return e;
   return reduce_into(scratch, nb, 0.5, 0.0, acc, st);
+}
+
+__global__ void k_add_into(double *__restrict__ f, const double *__restrict__ a, size_t n) {
+  const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) f[t] += a[t];
+}
+
+cudaError_t add_into(double *f, const double *a, size_t n, cudaStream_t st) {
+  {
+    XK_PROF("add_exchange");
+    k_add_into<<<cdiv(n, 256), 256, 0, st>>>(f, a, n);
+  }
+  return XK_LAUNCHED();
 }
 
 __global__ void k_add_scalar(double *acc, double v) { *acc += v; }

@@ -98,14 +98,16 @@ cudaError_t fill_enk2_cubic(const Geo &g, const double *x, const double *m, doub
 // V_B^(n) (forward) and tmpV (backward) recursions, solved as extended-
 // range triangular systems.  rs: rec_scratch_doubles(N) doubles of scratch.
 size_t rec_scratch_doubles(int N);
-cudaError_t fill_vb(int N, double beta, double vi, const double *ENk, double *VBN, double *rs,
+// lnn[l] = ln l for l = 1..N (host values); rs: weight scratch of
+// rec_scratch_doubles(N) doubles per direction
+cudaError_t fill_vb(int N, double beta, double vi, const double *ENk, const double *lnn, double *VBN, double *rs,
                     cudaStream_t st);
-cudaError_t back_vb(int N, double beta, double vi, const double *ENk, double *tmpV, double *rs,
+cudaError_t back_vb(int N, double beta, double vi, const double *ENk, const double *lnn, double *tmpV, double *rs,
                     cudaStream_t st);
 // both at once (the two recursions need only ENk): V_B into VBN and the
 // backward tmpV, on two SMs; rs_f and rs_b are separate weight scratch
-cudaError_t fill_vb_tv(int N, double beta, double vi, const double *ENk, double *VBN, double *tmpV, double *rs_f,
-                       double *rs_b, cudaStream_t st);
+cudaError_t fill_vb_tv(int N, double beta, double vi, const double *ENk, const double *lnn, double *VBN,
+                       double *tmpV, double *rs_f, double *rs_b, cudaStream_t st);
 cudaError_t fill_g(int N, double beta, double vi, const double *ENk, const double *VBN,
                    const double *tmpV, double *G, cudaStream_t st);
 // scratch: at least exch_scratch_doubles(g) doubles
@@ -202,5 +204,7 @@ cudaError_t vbn_energy(int N, double beta, double vi, double add, const double *
 cudaError_t force_virial(const Geo &g, const double *x, const double *f, const double *m,
                          int image, double *acc, double *scratch, cudaStream_t st);
 cudaError_t add_scalar(double *acc, double v, cudaStream_t st);
+// f[i] += a[i], i < n
+cudaError_t add_into(double *f, const double *a, size_t n, cudaStream_t st);
 
 }  // namespace xk

@@ -7,6 +7,8 @@
 // OpenCL queue does; host <-> device copies use page-locked host memory.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstdlib>
@@ -72,6 +74,60 @@ bool capturing() {
   cudaStreamCaptureStatus s = cudaStreamCaptureStatusNone;
   if (cudaStreamIsCapturing(stream(), &s) != cudaSuccess) return false;
   return s != cudaStreamCaptureStatusNone;
+}
+
+// ------------------------------------------------------------------
+// side stream: the exchange chain (recursions, G, exchange spring forces)
+// runs on a second stream forked from the library stream, so that it
+// overlaps the pair forces queued after it.  Every access to device state
+// (sim_device, pimd_device, the host synchronisations, ...) first joins it;
+// the pair- and trap-force entry points do not (NoJoin), and the exchange
+// forces land in a separate array that the join adds to f.
+// ------------------------------------------------------------------
+struct Side {
+  cudaStream_t s = nullptr;
+  cudaEvent_t fork = nullptr, done = nullptr;
+  bool pending = false;
+  std::vector<SimDev *> fex;  // simulations whose exchange forces wait to be added to f
+};
+static std::unordered_map<cudaStream_t, Side> g_side;  // by library stream
+static thread_local int t_nojoin = 0;
+
+NoJoin::NoJoin() { ++t_nojoin; }
+NoJoin::~NoJoin() { --t_nojoin; }
+
+int side_begin(cudaStream_t *out) {
+  Side &sd = g_side[stream()];
+  if (!sd.s) {
+    XMD_CUDA(cudaStreamCreateWithFlags(&sd.s, cudaStreamNonBlocking));
+    XMD_CUDA(cudaEventCreateWithFlags(&sd.fork, cudaEventDisableTiming));
+    XMD_CUDA(cudaEventCreateWithFlags(&sd.done, cudaEventDisableTiming));
+  }
+  XMD_CUDA(cudaEventRecord(sd.fork, stream()));
+  XMD_CUDA(cudaStreamWaitEvent(sd.s, sd.fork, 0));
+  *out = sd.s;
+  return 0;
+}
+
+int side_end(SimDev *fex) {
+  Side &sd = g_side[stream()];
+  XMD_CUDA(cudaEventRecord(sd.done, sd.s));
+  sd.pending = true;
+  if (fex && std::find(sd.fex.begin(), sd.fex.end(), fex) == sd.fex.end()) sd.fex.push_back(fex);
+  return 0;
+}
+
+int join_side() {
+  if (t_nojoin) return 0;
+  auto it = g_side.find(stream());
+  if (it == g_side.end() || !it->second.pending) return 0;
+  Side &sd = it->second;
+  sd.pending = false;
+  XMD_CUDA(cudaStreamWaitEvent(stream(), sd.done, 0));
+  std::vector<SimDev *> add;
+  add.swap(sd.fex);
+  for (SimDev *d : add) XMD_CUDA(xk::add_into(d->f.as<double>(), d->fex.as<double>(), d->geo.slots(), stream()));
+  return 0;
 }
 
 int reserve(DevBuf &b, size_t bytes) {
@@ -151,13 +207,21 @@ static T *lookup(std::unordered_map<const void *, T *> &m, const void *k, bool c
 }
 
 static void free_sim(SimDev *d) {
+  // side-stream work of this simulation finishes first; its pending forces
+  // are dropped with it
+  for (auto &kv : g_side)
+    if (kv.second.s && kv.second.pending) {
+      cudaStreamSynchronize(kv.second.s);
+      auto &v = kv.second.fex;
+      v.erase(std::remove(v.begin(), v.end(), d), v.end());
+    }
   for (DevBuf *b : {&d->x, &d->v, &d->f, &d->m, &d->th, &d->vt, &d->Q, &d->cf, &d->c0, &d->c2,
-                    &d->stage, &d->scratch})
+                    &d->stage, &d->scratch, &d->fex, &d->xscr})
     release(*b);
 }
 
 static void free_pimd(PimdDev *d) {
-  for (DevBuf *b : {&d->ENk, &d->ENk2, &d->Eint, &d->VBN, &d->tmpV, &d->G, &d->linkt, &d->rec, &d->rc_coef,
+  for (DevBuf *b : {&d->ENk, &d->ENk2, &d->Eint, &d->VBN, &d->tmpV, &d->G, &d->linkt, &d->lnn, &d->rec, &d->rc_coef,
                     &d->rc_cols, &d->rc_phase, &d->rc_S, &d->rc_T})
     release(*b);
 }
@@ -238,6 +302,7 @@ static xk::Geo make_geo(md_simulation_t_x *sim) {
 int sim_device(md_simulation_t_x *sim, SimDev **out) {
   if (!sim || !sim->particles || sim->N < 1) return fail(MD_GB_ERR_ARG, "invalid simulation");
   XMD_TRY(ensure_device());
+  XMD_TRY(join_side());
   SimDev *d = lookup(g_sim, sim, true);
   *out = d;
   // the box may change between calls (md_init_nd_rect_box_x)
@@ -323,6 +388,7 @@ int sim_device(md_simulation_t_x *sim, SimDev **out) {
 }
 
 int sim_to_host(md_simulation_t_x *sim, bool keep) {
+  if (device_present() && g_own) XMD_TRY(join_side());
   if (!sim) return fail(MD_GB_ERR_ARG, "NULL simulation");
   SimDev *d = lookup(g_sim, sim, false);
   if (!d || !d->valid) return 0;
@@ -385,6 +451,13 @@ int pimd_device(md_pimd_t_x *pimd, SimDev **sd, PimdDev **pd) {
   XMD_TRY(reserve(d->tmpV, (size_t)(N + 1) * 8));
   XMD_TRY(reserve(d->G, (size_t)N * N * 8));
   XMD_TRY(reserve(d->linkt, (size_t)N * N * 8));
+  {
+    std::vector<double> ln(N + 1, 0.0);
+    for (int l = 1; l <= N; ++l) ln[l] = log((double)l);
+    XMD_TRY(reserve(d->lnn, (size_t)(N + 1) * 8));
+    XMD_CUDA(cudaMemcpyAsync(d->lnn.p, ln.data(), (size_t)(N + 1) * 8, cudaMemcpyHostToDevice, stream()));
+    XMD_CUDA(cudaStreamSynchronize(stream()));
+  }
   XMD_TRY(reserve(d->rec, 2 * xk::rec_scratch_doubles(N) * 8));
   XMD_CUDA(cudaMemsetAsync(d->rec.p, 0, 2 * xk::rec_scratch_doubles(N) * 8, stream()));
   d->tmpv_fresh = false;
@@ -399,6 +472,7 @@ int pimd_device(md_pimd_t_x *pimd, SimDev **sd, PimdDev **pd) {
 }
 
 int pimd_to_host(md_pimd_t_x *pimd, bool keep) {
+  if (device_present() && g_own) XMD_TRY(join_side());
   if (!pimd) return fail(MD_GB_ERR_ARG, "NULL path-integral state");
   PimdDev *d = lookup(g_pimd, pimd, false);
   if (!d || !d->valid) return 0;
@@ -419,6 +493,7 @@ int pimd_to_host(md_pimd_t_x *pimd, bool keep) {
 // accumulators
 // ------------------------------------------------------------------
 int stats_device(md_stats_t_x *s, double **acc) {
+  if (device_present() && g_own) XMD_TRY(join_side());
   if (!s || !s->es || s->N < 1) return fail(MD_GB_ERR_ARG, "invalid statistics accumulator");
   XMD_TRY(ensure_device());
   StatsDev *d = lookup(g_stats, s, true);
@@ -434,6 +509,7 @@ int stats_device(md_stats_t_x *s, double **acc) {
 }
 
 int stats_to_host(md_stats_t_x *s) {
+  if (device_present() && g_own) XMD_TRY(join_side());
   if (!s) return fail(MD_GB_ERR_ARG, "NULL accumulator");
   StatsDev *d = lookup(g_stats, s, false);
   if (!d || !d->valid) return 0;
@@ -497,6 +573,7 @@ void *md_gb300_get_stream_x(void) {
 
 int md_gb300_synchronize_x(void) {
   XMD_TRY(ensure_device());
+  XMD_TRY(join_side());
   XMD_CUDA(cudaStreamSynchronize(stream()));
   return 0;
 }
@@ -504,6 +581,7 @@ int md_gb300_synchronize_x(void) {
 int md_gb300_capture_begin_x(void) {
   XMD_TRY(ensure_device());
   if (capturing()) return fail(MD_GB_ERR_CAPTURE, "already capturing");
+  XMD_TRY(join_side());  // no side-stream work from before the capture stays open
   XMD_CUDA(cudaStreamBeginCapture(stream(), cudaStreamCaptureModeThreadLocal));
   return 0;
 }
@@ -511,6 +589,7 @@ int md_gb300_capture_begin_x(void) {
 int md_gb300_capture_end_x(md_gb300_graph_t_x **out) {
   if (!out) return fail(MD_GB_ERR_ARG, "NULL graph pointer");
   XMD_TRY(ensure_device());
+  XMD_TRY(join_side());  // side-stream work must rejoin before the capture ends
   md_gb300_graph *gr = new md_gb300_graph();
   cudaError_t e = cudaStreamEndCapture(stream(), &gr->g);
   if (e != cudaSuccess) {
@@ -534,6 +613,7 @@ int md_gb300_capture_ensemble_x(int n, md_gb300_system_step_fn_x step, void *ctx
   if (n < 1 || !step || !out) return fail(MD_GB_ERR_ARG, "invalid ensemble capture arguments");
   XMD_TRY(ensure_device());
   if (capturing()) return fail(MD_GB_ERR_CAPTURE, "already capturing");
+  XMD_TRY(join_side());
   while ((int)g_branches.size() < n) {
     cudaStream_t b;
     XMD_CUDA(cudaStreamCreateWithFlags(&b, cudaStreamNonBlocking));
@@ -555,6 +635,7 @@ int md_gb300_capture_ensemble_x(int n, md_gb300_system_step_fn_x step, void *ctx
     g_user = g_branches[i];
     g_user_set = true;
     rc = step(i, ctx);
+    if (!rc) rc = join_side();
     g_user = saved_user;
     g_user_set = saved_set;
     if (!rc) ce = cudaEventRecord(ev[i], g_branches[i]);
@@ -585,6 +666,7 @@ int md_gb300_capture_ensemble_x(int n, md_gb300_system_step_fn_x step, void *ctx
 
 int md_gb300_graph_launch_x(md_gb300_graph_t_x *gr, int count) {
   if (!gr || count < 0) return fail(MD_GB_ERR_ARG, "invalid graph launch");
+  XMD_TRY(join_side());
   for (int i = 0; i < count; ++i) XMD_CUDA(cudaGraphLaunch(gr->e, stream()));
   return 0;
 }

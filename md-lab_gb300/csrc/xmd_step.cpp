@@ -281,9 +281,14 @@ int md_pimd_fill_VB_x(md_pimd_t_x *pimd) {
   // the backward recursion (tmpV of the exchange forces) needs only ENk as
   // well: both run now, side by side, and the force call reuses tmpV while
   // ENk, beta and vi are unchanged
+  // Both run on the side stream, which overlaps whatever the driver queues
+  // next that does not read them (the pair and trap forces).
   double *rs = pd->rec.as<double>();
-  XMD_CUDA(xk::fill_vb_tv(pimd->N, pimd->beta, pimd->vi, pd->ENk.as<double>(), pd->VBN.as<double>(),
-                          pd->tmpV.as<double>(), rs, rs + xk::rec_scratch_doubles(pimd->N), stream()));
+  cudaStream_t s2;
+  XMD_TRY(side_begin(&s2));
+  XMD_CUDA(xk::fill_vb_tv(pimd->N, pimd->beta, pimd->vi, pd->ENk.as<double>(), pd->lnn.as<double>(),
+                          pd->VBN.as<double>(), pd->tmpV.as<double>(), rs, rs + xk::rec_scratch_doubles(pimd->N), s2));
+  XMD_TRY(side_end(nullptr));
   pd->tmpv_fresh = true;
   pd->tmpv_beta = pimd->beta;
   pd->tmpv_vi = pimd->vi;
@@ -291,24 +296,35 @@ int md_pimd_fill_VB_x(md_pimd_t_x *pimd) {
 }
 
 int md_pimd_fast_fill_force_VB_x(md_pimd_t_x *pimd, int image) {
+  // continues the side stream after md_pimd_fill_VB_x (no join): G and the
+  // exchange spring forces are computed there, into sd->fex, which the next
+  // join adds to f
+  NoJoin nj;
   SimDev *sd;
   PimdDev *pd;
   XMD_TRY(pimd_device(pimd, &sd, &pd));
   XMD_TRY(check_plain(pimd));
   XMD_TRY(check_image(sd, image));
   if (pimd->P < 2) return fail(MD_GB_ERR_ARG, "the exchange spring force needs P >= 2 beads");
-  int rc;
-  double *scr = scratch_for(sd, general_scratch(sd->geo), &rc);
-  if (rc) return rc;
-  cudaStream_t st = stream();
+  const size_t nx = xk::exch_scratch_doubles(sd->geo);
+  if (sd->fex.bytes < sd->geo.slots() * sizeof(double) || sd->xscr.bytes < nx * sizeof(double)) {
+    if (capturing()) return fail(MD_GB_ERR_CAPTURE, "exchange buffers are not allocated yet");
+    XMD_TRY(reserve(sd->fex, sd->geo.slots() * sizeof(double)));
+    XMD_TRY(reserve(sd->xscr, nx * sizeof(double)));
+  }
+  double *scr = sd->xscr.as<double>();
+  cudaStream_t st;
+  XMD_TRY(side_begin(&st));
   const int N = pimd->N;
   if (!(pd->tmpv_fresh && pd->tmpv_beta == pimd->beta && pd->tmpv_vi == pimd->vi))
-    XMD_CUDA(xk::back_vb(N, pimd->beta, pimd->vi, pd->ENk.as<double>(), pd->tmpV.as<double>(),
-                         pd->rec.as<double>(), st));
+    XMD_CUDA(xk::back_vb(N, pimd->beta, pimd->vi, pd->ENk.as<double>(), pd->lnn.as<double>(),
+                         pd->tmpV.as<double>(), pd->rec.as<double>(), st));
   XMD_CUDA(xk::fill_g(N, pimd->beta, pimd->vi, pd->ENk.as<double>(), pd->VBN.as<double>(), pd->tmpV.as<double>(),
                       pd->G.as<double>(), st));
+  XMD_CUDA(cudaMemsetAsync(sd->fex.p, 0, sd->geo.slots() * sizeof(double), st));
   XMD_CUDA(xk::exch_force(sd->geo, sd->x.as<double>(), sd->m.as<double>(), pimd->omegaP * pimd->omegaP, image,
-                          pd->G.as<double>(), sd->f.as<double>(), scr, st));
+                          pd->G.as<double>(), sd->fex.as<double>(), scr, st));
+  XMD_TRY(side_end(sd));
   return 0;
 }
 
@@ -318,6 +334,7 @@ int md_pimd_fill_force_VB_x(md_pimd_t_x *pimd, int image) { return md_pimd_fast_
 // external forces: md_pimd_x.c:1297-1391, :1527-1677
 // ------------------------------------------------------------------
 int md_pimd_calc_trap_force_x(md_pimd_t_x *pimd, md_trap_force_t_x tf) {
+  NoJoin nj;  // adds to f only: may overlap the side stream's exchange work
   const int kind = trap_kind_of((const void *)tf, false);
   if (!kind) return fail(MD_GB_ERR_UNSUPPORTED, "trap force function has no device kernel");
   SimDev *sd;
@@ -401,6 +418,7 @@ void xmd::ewald_shifts(xk::PairPrm &p, const xk::Geo &g) {
 extern "C" {
 
 int md_pimd_calc_pair_force_x(md_pimd_t_x *pimd, md_pair_force_t_x pf) {
+  NoJoin nj;  // adds to f only: may overlap the side stream's exchange work
   const int kind = pair_kind_of((const void *)pf, false);
   if (!kind) return fail(MD_GB_ERR_UNSUPPORTED, "pair force function has no device kernel");
   SimDev *sd;
