@@ -192,6 +192,12 @@ int md_gb300_ewald_model_desc_info_x(md_gb300_ewald_model_t_x *model, double *rc
    K-major operands and the two readings of MN-major descriptors */
 int md_gb300_tc_selftest_x(double err[5]);
 
+/* Text checkpoints (md_fprint_particle_pos_x / _vel_x / _force_x,
+   md_fprint_nhcs_x, md_fprint_sim_box_x):
+   on != 0 writes "%.17g" instead of the reference's lossy "%f", so that a
+   resumed run continues bit for bit; the reference reads both. */
+int md_gb300_set_text_exact_x(int on);
+
 /* release the device copies (and, for *_free_*, the host structs) */
 int md_gb300_release_simulation_x(md_simulation_t_x *sim);
 void md_gb300_free_simulation_x(md_simulation_t_x *sim);

@@ -101,9 +101,15 @@ int md_stats_copy_to_x(md_stats_t_x *stats, md_stats_t_x *stats2);
 int md_stats_mult_to_x(md_stats_t_x *stats, md_stats_t_x *stats2);
 
 /* xi -> xi' reweighting with sign, e.g. bosons to fermions:
-   md_pimd_x.h:171-172 (host side, on the synced ENk/VBN) */
+   md_pimd_x.h:171-172 (md_pimd_calc_vi_sign_x: the signed recursion runs on
+   the GPU, es[0] of both accumulators is scaled on the host as in the
+   reference; md_pimd_xminE2_x on the synced host tables) */
 md_num_t_x md_pimd_xminE2_x(md_pimd_t_x *pimd, int N2, md_num_t_x *VBN2, md_num_t_x vi2);
 int md_pimd_calc_vi_sign_x(md_pimd_t_x *pimd, md_stats_t_x *e_s, md_stats_t_x *s_s, md_num_t_x vi2);
+/* md_pimd_x.h:190 (md_pimd_x.c:5404-5448): static structure factor between
+   bead 1 and bead pi for the first min(sk_sphere->N, stats->points) wave
+   vectors, added to stats->fxs[stats->N - 1][j]; the sums run on the GPU */
+int md_pimd_calc_sphere_Sk_structure_x(md_pimd_t_x *pimd, md_stats_t_x *stats, int pi, md_sk_sphere_t_x *sk_sphere);
 
 #ifdef __cplusplus
 }

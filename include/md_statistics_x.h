@@ -35,6 +35,16 @@ typedef struct {
   md_num_t_x **fxs;
 } md_stats_t_x;
 
+/* md_statistics_x.h:28-34: one wave vector per distinct |q| of the cubic
+   grid q0, q0 + qincre, ... <= qmax in each component, sorted by |q| */
+typedef struct {
+  int N;
+  md_num_t_x *qs;
+  md_num_t_x *qis;
+} md_sk_sphere_t_x;
+
+md_sk_sphere_t_x *md_alloc_sk_sphere_3d_x(md_num_t_x q0, md_num_t_x qincre, md_num_t_x qmax);
+
 /* md_statistics_x.h:40 */
 md_stats_t_x *md_stats_sync_host_x(md_stats_t_x *stats);
 

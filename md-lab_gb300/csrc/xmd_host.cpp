@@ -10,6 +10,9 @@
 // Random numbers must match the reference bit for bit, so they come from
 // the same glibc rand() stream through the same Box-Muller pairing.
 #include <cmath>
+#include <vector>
+#include <array>
+#include <algorithm>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -529,6 +532,16 @@ int md_simulation_rescale_velocity_x(md_simulation_t_x *sim, md_num_t_x T) {
   return 0;
 }
 
+// number format of the text checkpoints: the reference's "%f " (6 decimals,
+// lossy) by default; "%.17g " (md_gb300_set_text_exact_x(1)) round-trips
+// every double exactly and is still read by the reference's fscanf("%lf")
+static const char *g_text_fmt = "%f ";
+
+extern "C" int md_gb300_set_text_exact_x(int on) {
+  g_text_fmt = on ? "%.17g " : "%f ";
+  return 0;
+}
+
 // ------------------------------------------------------------------
 // text checkpoints (md_util_x.c:838-1011), same format
 // ------------------------------------------------------------------
@@ -538,7 +551,7 @@ static int print_field(FILE *out, md_simulation_t_x *sim, char tag) {
   for (int i = 0; i < sim->N; ++i) {
     const md_particle_t_x *p = &sim->particles[i];
     const double *v = tag == 'x' ? p->x : tag == 'v' ? p->v : p->f;
-    for (int d = 0; d < D; ++d) fprintf(out, "%f ", v[d]);
+    for (int d = 0; d < D; ++d) fprintf(out, g_text_fmt, v[d]);
     fprintf(out, "\n");
   }
   return ferror(out);
@@ -556,7 +569,7 @@ int md_fprint_nhcs_x(FILE *out, md_simulation_t_x *sim) {
     fprintf(out, "%d\n", c->f);
     const double *rows[3] = {c->theta, c->vtheta, c->Q};
     for (int r = 0; r < 3; ++r) {
-      for (int j = 0; j < LC; ++j) fprintf(out, "%f ", rows[r][j]);
+      for (int j = 0; j < LC; ++j) fprintf(out, g_text_fmt, rows[r][j]);
       fprintf(out, "\n");
     }
   }
@@ -567,7 +580,7 @@ int md_fprint_sim_box_x(FILE *out, simulation_box_t_x *box) {
   fprintf(out, "box %d %d\n", box->type, D);
   if (box->type == MD_ND_RECT_BOX_X) {
     const nd_rect_t_x *r = (const nd_rect_t_x *)box->box;
-    for (int d = 0; d < D; ++d) fprintf(out, "%f ", r->L[d]);
+    for (int d = 0; d < D; ++d) fprintf(out, g_text_fmt, r->L[d]);
     fprintf(out, "\n");
   }
   return ferror(out);
@@ -616,6 +629,46 @@ int md_fread_nhcs_x(FILE *in, md_simulation_t_x *sim) {
 // ------------------------------------------------------------------
 md_stats_t_x *md_stats_sync_host_x(md_stats_t_x *stats) {
   return xmd::stats_to_host(stats) == 0 ? stats : NULL;
+}
+
+// md_statistics_x.c:104-161: wave vectors on the cube q0, q0 + qincre, ...
+// <= qmax per component (loop order x, y, z), one per distinct |q| (first
+// found within 1e-4), skipping |q| < 1e-4; ascending |q|
+md_sk_sphere_t_x *md_alloc_sk_sphere_3d_x(md_num_t_x q0, md_num_t_x qincre, md_num_t_x qmax) {
+  if (D != 3 || !(qincre > 0)) return NULL;
+  std::vector<std::array<double, 4>> v;  // |q|, qx, qy, qz
+  for (double qx = q0; qx <= qmax; qx += qincre)
+    for (double qy = q0; qy <= qmax; qy += qincre)
+      for (double qz = q0; qz <= qmax; qz += qincre) {
+        const double q = sqrt(qx * qx + qy * qy + qz * qz);
+        if (fabs(q) < 1e-4) continue;
+        bool found = false;
+        for (const auto &e : v)
+          if (fabs(e[0] - q) < 1e-4) {
+            found = true;
+            break;
+          }
+        if (!found) v.push_back({q, qx, qy, qz});
+      }
+  std::stable_sort(v.begin(), v.end(), [](const std::array<double, 4> &a, const std::array<double, 4> &b) {
+    return a[0] < b[0];
+  });
+  md_sk_sphere_t_x *r = (md_sk_sphere_t_x *)calloc(1, sizeof(md_sk_sphere_t_x));
+  if (!r) return NULL;
+  r->N = (int)v.size();
+  r->qs = (md_num_t_x *)malloc(sizeof(md_num_t_x) * (v.empty() ? 1 : v.size()));
+  r->qis = (md_num_t_x *)malloc(sizeof(md_num_t_x) * 3 * (v.empty() ? 1 : v.size()));
+  if (!r->qs || !r->qis) {
+    free(r->qs);
+    free(r->qis);
+    free(r);
+    return NULL;
+  }
+  for (size_t i = 0; i < v.size(); ++i) {
+    r->qs[i] = v[i][0];
+    for (int d = 0; d < 3; ++d) r->qis[3 * i + d] = v[i][1 + d];
+  }
+  return r;
 }
 
 md_stats_t_x *md_alloc_stats_x(int points) {

@@ -84,6 +84,8 @@ struct PimdDev {
   DevBuf ENk, ENk2, Eint, VBN, tmpV, G;
   DevBuf linkt;  // N x N bead-P -> bead-1 springs (scratch of the ENk fill)
   DevBuf lnn;    // ln l for l = 0..N (entry 0 unused), host values
+  DevBuf vsign;  // V_B and signs of md_pimd_calc_vi_sign_x
+  DevBuf sk_buf; // wave vectors and results of md_pimd_calc_sphere_Sk_structure_x
   DevBuf rec;  // weights of the forward and backward recursions (two halves)
   // tmpV (backward recursion) computed by the last md_pimd_fill_VB_x from
   // the current ENk with these beta and vi

@@ -808,10 +808,12 @@ __device__ inline size_t moff(int i, int j) { return (size_t)i * (i - 1) / 2 + j
 // ln xi - ln n); backward row i <-> u = N-i+1, column j <-> l = N-j:
 // exp(-beta ENk[l][i-j] + (i-j-1) ln xi - ln l).  ln xi and the table
 // lnn[l] = ln l come from the host.
+// sgn = -1 gives the weights of a negative xi' (|xi'| in vi and lnvi): the
+// mantissa of every term with odd k - 1 changes sign.
 __global__ void __launch_bounds__(128) k_weights(int N, double beta, double vi, double lnvi,
                                                  const double *__restrict__ ENk, const double *__restrict__ lnn,
                                                  double *__restrict__ Mf, int *__restrict__ Ef,
-                                                 double *__restrict__ Mb, int *__restrict__ Eb, int first) {
+                                                 double *__restrict__ Mb, int *__restrict__ Eb, int first, int sgn) {
   const int row = blockIdx.x + 1;
   const int dir = first + blockIdx.y;
   double *Mm = dir ? Mb : Mf;
@@ -821,19 +823,20 @@ __global__ void __launch_bounds__(128) k_weights(int N, double beta, double vi, 
     const int l = dir ? N - j : row;
     Ext w{0.0, 0};
     if (vi != 0.0 || k == 1) w = ext_exp(-beta * ENk[dtri(l) + k - 1] + (k - 1) * lnvi - lnn[l]);
+    if (sgn < 0 && ((k - 1) & 1)) w.m = -w.m;
     Mm[moff(row, j)] = w.m;
     Me[moff(row, j)] = w.e;
   }
 }
 
 static cudaError_t weights(int N, double beta, double vi, const double *ENk, const double *lnn, double *rs_f,
-                           double *rs_b, int first, int count, cudaStream_t st) {
+                           double *rs_b, int first, int count, cudaStream_t st, int sgn = 1) {
   const double lnvi = vi != 0.0 ? log(vi) : 0.0;
   dim3 grid(N, count);
   {
     XK_PROF("weights");
     k_weights<<<grid, 128, 0, st>>>(N, beta, vi, lnvi, ENk, lnn, rs_f, rs_f ? (int *)(rs_f + ntri(N)) : nullptr,
-                                    rs_b, rs_b ? (int *)(rs_b + ntri(N)) : nullptr, first);
+                                    rs_b, rs_b ? (int *)(rs_b + ntri(N)) : nullptr, first, sgn);
   }
   return XK_LAUNCHED();
 }
@@ -869,6 +872,7 @@ struct TriJob {
   const double *Mm[2];
   const int *Me[2];
   double *out[2];
+  double *sign;  // optional: sign of X_i (signed weights), forward direction only
 };
 
 // Extended-range dot product of row i of the weights with the unknowns over
@@ -1086,10 +1090,14 @@ __global__ void __launch_bounds__(TS_WARPS * 32) k_tri_solve(int N, double beta,
     __syncthreads();
   }
   for (int i = threadIdx.x + 1; i <= N; i += blockDim.x) {
-    const double lnx = log(Xm[i]) + Xe[i] * LN2_HI + Xe[i] * LN2_LO;
+    const double lnx = log(fabs(Xm[i])) + Xe[i] * LN2_HI + Xe[i] * LN2_LO;
     out[backward ? N - i : i] = -lnx / beta;
+    if (job.sign && !backward) job.sign[i] = Xm[i] < 0.0 ? -1.0 : 1.0;
   }
-  if (threadIdx.x == 0) out[backward ? N : 0] = 0.0;
+  if (threadIdx.x == 0) {
+    out[backward ? N : 0] = 0.0;
+    if (job.sign && !backward) job.sign[0] = 1.0;
+  }
 }
 
 // scratch: mantissas (ntri(N) doubles) then exponents (ntri(N) ints)
@@ -1141,6 +1149,15 @@ cudaError_t fill_vb_tv(int N, double beta, double vi, const double *ENk, const d
   cudaError_t e = weights(N, beta, vi, ENk, lnn, rs_f, rs_b, 0, 2, st);
   if (e != cudaSuccess) return e;
   return tri_solve(N, beta, tri_job(N, rs_f, rs_b, VBN, tmpV), 0, 2, st);
+}
+
+cudaError_t fill_vb_signed(int N, double beta, double vi2, const double *ENk, const double *lnn, double *V2,
+                           double *sign, double *rs, cudaStream_t st) {
+  cudaError_t e = weights(N, beta, fabs(vi2), ENk, lnn, rs, nullptr, 0, 1, st, vi2 < 0 ? -1 : 1);
+  if (e != cudaSuccess) return e;
+  TriJob j = tri_job(N, rs, nullptr, V2, nullptr);
+  j.sign = sign;
+  return tri_solve(N, beta, j, 0, 1, st);
 }
 
 // connection probabilities G[l][j]: md_pimd_x.c:2660-2673
@@ -2161,6 +2178,43 @@ cudaError_t recip_energy(const Geo &g, const Recip &r, const double *x, double *
   e = XK_LAUNCHED();
   if (e != cudaSuccess) return e;
   return reduce_into(scratch, g.P, 1.0 / g.P, 0.0, acc, st);
+}
+
+// ===================================================================
+// static structure factor between two bead slices: md_pimd_x.c:5404-5448
+// ===================================================================
+// one block per wave vector q: cos and sin sums of q.x over the particles of
+// slices ja and jb; out[q] = (C_a C_b + S_a S_b) / N
+__global__ void k_sk_structure(Geo g, const double *__restrict__ x, int ja, int jb,
+                               const double *__restrict__ qis, double *__restrict__ out) {
+  __shared__ double buf[33];
+  const int q = blockIdx.x;
+  const double q0 = qis[3 * q], q1 = qis[3 * q + 1], q2 = qis[3 * q + 2];
+  double ca = 0, sa = 0, cb = 0, sb = 0;
+  for (int l = threadIdx.x; l < g.N; l += blockDim.x) {
+    double s, c;
+    sincos(q0 * x[sidx(ja, 0, l, 3, g.Ns)] + q1 * x[sidx(ja, 1, l, 3, g.Ns)] + q2 * x[sidx(ja, 2, l, 3, g.Ns)], &s, &c);
+    ca += c;
+    sa += s;
+    sincos(q0 * x[sidx(jb, 0, l, 3, g.Ns)] + q1 * x[sidx(jb, 1, l, 3, g.Ns)] + q2 * x[sidx(jb, 2, l, 3, g.Ns)], &s, &c);
+    cb += c;
+    sb += s;
+  }
+  ca = block_sum(ca, buf);
+  sa = block_sum(sa, buf);
+  cb = block_sum(cb, buf);
+  sb = block_sum(sb, buf);
+  if (threadIdx.x == 0) out[q] = ca * cb / g.N + sa * sb / g.N;
+}
+
+cudaError_t sk_structure(const Geo &g, const double *x, int ja, int jb, const double *qis, int nq, double *out,
+                         cudaStream_t st) {
+  if (g.D != 3 || nq <= 0) return nq == 0 ? cudaSuccess : cudaErrorInvalidValue;
+  {
+    XK_PROF("sk_structure");
+    k_sk_structure<<<nq, 128, 0, st>>>(g, x, ja, jb, qis, out);
+  }
+  return XK_LAUNCHED();
 }
 
 // ===================================================================

@@ -108,6 +108,10 @@ cudaError_t back_vb(int N, double beta, double vi, const double *ENk, const doub
 // backward tmpV, on two SMs; rs_f and rs_b are separate weight scratch
 cudaError_t fill_vb_tv(int N, double beta, double vi, const double *ENk, const double *lnn, double *VBN,
                        double *tmpV, double *rs_f, double *rs_b, cudaStream_t st);
+// V_B for a signed xi' (md_pimd_calc_vi_sign_x): V2[n] = -ln|Z'_n|/beta and
+// sign[n] = sign of Z'_n, n = 0..N
+cudaError_t fill_vb_signed(int N, double beta, double vi2, const double *ENk, const double *lnn, double *V2,
+                           double *sign, double *rs, cudaStream_t st);
 cudaError_t fill_g(int N, double beta, double vi, const double *ENk, const double *VBN,
                    const double *tmpV, double *G, cudaStream_t st);
 // scratch: at least exch_scratch_doubles(g) doubles
@@ -197,6 +201,11 @@ int pair32_warps(int kind, int D, int N, int P);
 // needs r.phase sized recip_phase_doubles(g, nsum) * 3 / 2 (FP32 copy behind)
 cudaError_t recip_force32(const Geo &g, const Recip &r, const double *x, double inv_mP, double *f,
                           cudaStream_t st);
+
+// static structure factor of slices ja, jb for nq wave vectors qis[3q..]:
+// out[q] = (sum_l cos q.x_a)(sum_l cos q.x_b)/N + (sin)(sin)/N
+cudaError_t sk_structure(const Geo &g, const double *x, int ja, int jb, const double *qis, int nq, double *out,
+                         cudaStream_t st);
 
 // ---- estimators ----
 cudaError_t vbn_energy(int N, double beta, double vi, double add, const double *ENk,

@@ -221,7 +221,7 @@ static void free_sim(SimDev *d) {
 }
 
 static void free_pimd(PimdDev *d) {
-  for (DevBuf *b : {&d->ENk, &d->ENk2, &d->Eint, &d->VBN, &d->tmpV, &d->G, &d->linkt, &d->lnn, &d->rec, &d->rc_coef,
+  for (DevBuf *b : {&d->ENk, &d->ENk2, &d->Eint, &d->VBN, &d->tmpV, &d->G, &d->linkt, &d->lnn, &d->vsign, &d->sk_buf, &d->rec, &d->rc_coef,
                     &d->rc_cols, &d->rc_phase, &d->rc_S, &d->rc_T})
     release(*b);
 }

@@ -6,6 +6,7 @@
 // the library stream.  Reference counterparts are cited per function
 // (MD-Lab file:line); the OpenCL branch of each is what these replace.
 #include <cmath>
+#include <vector>
 #include <cstdlib>
 #include <cstring>
 
@@ -260,6 +261,9 @@ int md_pimd_init_particle_uniform_pos_x(md_pimd_t_x *p, md_num_t_x *center, md_n
 // exchange: md_pimd_x.c:593-665, :814-953, :997-1109, :1969-2210, :2369-2721
 // ------------------------------------------------------------------
 int md_pimd_fast_fill_ENk_x(md_pimd_t_x *pimd, int image) {
+  // on the library stream: on the side stream its many small blocks would
+  // compete with the structure-factor kernels that start the pair forces,
+  // which costs more than the overlap gains
   SimDev *sd;
   PimdDev *pd;
   XMD_TRY(pimd_device(pimd, &sd, &pd));
@@ -274,6 +278,7 @@ int md_pimd_fast_fill_ENk_x(md_pimd_t_x *pimd, int image) {
 int md_pimd_fill_ENk_x(md_pimd_t_x *pimd, int image) { return md_pimd_fast_fill_ENk_x(pimd, image); }
 
 int md_pimd_fill_VB_x(md_pimd_t_x *pimd) {
+  NoJoin nj;  // the exchange chain starts on the side stream here
   SimDev *sd;
   PimdDev *pd;
   XMD_TRY(pimd_device(pimd, &sd, &pd));
@@ -754,36 +759,60 @@ md_num_t_x md_pimd_fast_xminE_x(md_pimd_t_x *pimd, int u, md_num_t_x *V) {
   return m;
 }
 
-// signed V_B for xi' (possibly negative) on the current ENk; multiplies both
-// accumulators' es[0] by sign * exp(-beta (V'_N - V_N))
+// md_pimd_x.c:5404-5448: S(q) between bead 1 and bead pi of every particle
+// for the first min(sk->N, stats->points) wave vectors, added to
+// stats->fxs[stats->N - 1][j]; the sums over particles run on the GPU
+int md_pimd_calc_sphere_Sk_structure_x(md_pimd_t_x *pimd, md_stats_t_x *stats, int pi, md_sk_sphere_t_x *sk) {
+  if (!stats || !sk || !stats->fxs) return fail(MD_GB_ERR_ARG, "NULL argument");
+  if (D != 3) return fail(MD_GB_ERR_UNSUPPORTED, "the spherical S(k) is 3D only");
+  if (capturing()) return fail(MD_GB_ERR_CAPTURE, "reads a result back; not while capturing");
+  SimDev *sd;
+  PimdDev *pd;
+  XMD_TRY(pimd_device(pimd, &sd, &pd));
+  const int n = sk->N < stats->points ? sk->N : stats->points;
+  if (n <= 0) return 0;
+  if (pi < 1) return fail(MD_GB_ERR_ARG, "bead index pi must be >= 1");
+  const int jb = (pi - 1) % pimd->P;
+  XMD_TRY(reserve(pd->sk_buf, sizeof(double) * 4 * (size_t)n));
+  cudaStream_t st = stream();
+  double *qd = pd->sk_buf.as<double>(), *out = qd + 3 * (size_t)n;
+  std::vector<double> res(n);
+  XMD_CUDA(cudaMemcpyAsync(qd, sk->qis, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, st));
+  XMD_CUDA(xk::sk_structure(sd->geo, sd->x.as<double>(), 0, jb, qd, n, out, st));
+  XMD_CUDA(cudaMemcpyAsync(res.data(), out, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+  XMD_CUDA(cudaStreamSynchronize(st));
+  if (!md_stats_sync_host_x(stats)) return -1;
+  for (int j = 0; j < n; ++j) stats->fxs[stats->N - 1][j] += res[j];
+  return 0;
+}
+
+// signed V_B for xi' (possibly negative) on the current ENk, on the GPU:
+// the same extended-range solve as V_B with the terms of odd k-1 negated
+// for xi' < 0 (md_pimd_x.c:4665-4706).  Both accumulators' es[0] are then
+// multiplied by sign * exp(-beta (V'_N - V_N)), on the host as in the
+// reference.
 int md_pimd_calc_vi_sign_x(md_pimd_t_x *pimd, md_stats_t_x *e_s, md_stats_t_x *s_s, md_num_t_x vi2) {
-  if (!md_pimd_sync_host_x(pimd, 1) || !md_stats_sync_host_x(e_s) || !md_stats_sync_host_x(s_s)) return -1;
+  if (!e_s || !s_s) return fail(MD_GB_ERR_ARG, "NULL accumulator");
+  if (capturing()) return fail(MD_GB_ERR_CAPTURE, "reads a result back; not while capturing");
+  SimDev *sd;
+  PimdDev *pd;
+  XMD_TRY(pimd_device(pimd, &sd, &pd));
+  XMD_TRY(check_plain(pimd));
   const int N = pimd->N;
-  double *V2 = (double *)malloc(sizeof(double) * (N + 1));
-  double *sg = (double *)malloc(sizeof(double) * (N + 1));
-  if (!V2 || !sg) {
-    free(V2);
-    free(sg);
-    return -1;
-  }
-  V2[0] = 0;
-  sg[0] = 1;
-  const double sv = vi2 < 0 ? -1 : 1, av = fabs(vi2);
-  for (int n = 1; n <= N; ++n) {
-    const double m = min_shift(pimd, n, V2, av);
-    double sum = 0;
-    for (int k = 1; k <= n; ++k) {
-      if (vi2 == 0 && k != 1) continue;
-      sum += sg[n - k] * pow(sv, k - 1) * md_pimd_xexp_x(k, pimd->ENk[n - 1][k - 1] + V2[n - k], m, pimd->beta, av);
-    }
-    sg[n] = sum >= 0 ? 1 : -1;
-    V2[n] = (m - log(fabs(sum)) + log(n)) / pimd->beta;
-  }
-  const double s = sg[N] * exp(-pimd->beta * V2[N] + pimd->beta * pimd->VBN[N]);
+  XMD_TRY(reserve(pd->vsign, sizeof(double) * 2 * (N + 1)));
+  cudaStream_t st = stream();
+  double *V2 = pd->vsign.as<double>(), *sg = V2 + (N + 1);
+  XMD_CUDA(xk::fill_vb_signed(N, pimd->beta, vi2, pd->ENk.as<double>(), pd->lnn.as<double>(), V2, sg,
+                              pd->rec.as<double>(), st));
+  double r[3];
+  XMD_CUDA(cudaMemcpyAsync(&r[0], V2 + N, 8, cudaMemcpyDeviceToHost, st));
+  XMD_CUDA(cudaMemcpyAsync(&r[1], sg + N, 8, cudaMemcpyDeviceToHost, st));
+  XMD_CUDA(cudaMemcpyAsync(&r[2], pd->VBN.as<double>() + N, 8, cudaMemcpyDeviceToHost, st));
+  XMD_CUDA(cudaStreamSynchronize(st));
+  if (!md_stats_sync_host_x(e_s) || !md_stats_sync_host_x(s_s)) return -1;
+  const double s = r[1] * exp(-pimd->beta * r[0] + pimd->beta * r[2]);
   e_s->es[0] *= s;
   s_s->es[0] *= s;
-  free(V2);
-  free(sg);
   return 0;
 }
 

@@ -70,6 +70,10 @@ def structs(D, L):
     return Particle, Nhc, Box, Rect, Sim, Pimd, Stats
 
 
+class SkSphere(C.Structure):
+    _fields_ = [("N", _i), ("qs", _dp), ("qis", _dp)]
+
+
 class XLib:
     """One loaded library exporting the MD-Lab ABI for dimension D, chain length L."""
 
@@ -127,6 +131,8 @@ class XLib:
             "md_set_coulomb_truc_x": (None, [_d]),
             "md_set_coulomb_n_sum_x": (None, [_i]),
             "md_reset_stats_x": (_i, [pst, _d]),
+            "md_alloc_sk_sphere_3d_x": (C.POINTER(SkSphere), [_d, _d, _d]),
+            "md_pimd_calc_sphere_Sk_structure_x": (_i, [pp, pst, _i, C.POINTER(SkSphere)]),
         }
         if gb300:
             sig.update({

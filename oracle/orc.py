@@ -85,6 +85,8 @@ def lib():
             "orc_mlp_forward": (None, [i, _dp, _dp, i, _dp, _dp, _dp]),
             "orc_mlp_loss": (d, [i, _dp, _dp, _dp, _dp, d, d, d, i]),
             "orc_mlp_grad": (None, [i, _dp, _dp, _dp, _dp, d, d, d, i, _dp, _dp]),
+            "orc_sk_sphere": (i, [d, d, d, i, _dp, _dp]),
+            "orc_sk_structure": (None, [i, i, _dp, i, i, _dp, _dp]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -198,3 +200,18 @@ def desc_features(x, box, rc, basis, vmu, vsig, nb=128):
     V = np.zeros((N, 9))
     lib().orc_desc_features(N, ptr(x), ptr(L), rc, nb, ptr(B), ptr(mu), ptr(sg), ptr(F), ptr(V))
     return F, V
+
+
+def sk_sphere(q0, qincre, qmax, max_n=4096):
+    qs = np.zeros(max_n)
+    qis = np.zeros(3 * max_n)
+    n = lib().orc_sk_sphere(q0, qincre, qmax, max_n, ptr(qs), ptr(qis))
+    return qs[:n].copy(), qis[:3 * n].reshape(n, 3).copy()
+
+
+def sk_structure(N, P, x, pi, qis):
+    x = np.ascontiguousarray(x, np.float64)
+    q = np.ascontiguousarray(qis, np.float64).reshape(-1)
+    res = np.zeros(len(q) // 3)
+    lib().orc_sk_structure(N, P, ptr(x), pi, len(res), ptr(q), ptr(res))
+    return res

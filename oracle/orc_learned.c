@@ -1,6 +1,8 @@
 /*
  * orc_learned.c -- CPU restatement of the learned Ewald residual's parts
- * (descriptors, the 64-128-128-4 network, its loss and gradients).
+ * (descriptors, the 64-128-128-4 network, its loss and gradients), and of
+ * MD-Lab's spherical static structure factor (orc_sk_sphere,
+ * orc_sk_structure).
  *
  * TEST INFRASTRUCTURE ONLY, like the rest of oracle/.  MD-Lab has no learned
  * part, so there is no reference code to follow: this file states the
@@ -193,5 +195,80 @@ void orc_mlp_grad(int rows, const double *X, const double *V, const double *T, c
       for (int i = 0; i < ORC_H; ++i) grad[ORC_W2 + o * ORC_H + i] += a * h1[i];
       for (int i = 0; i < ORC_IN; ++i) grad[ORC_W1 + o * ORC_IN + i] += b * rnd(x[i], bf);
     }
+  }
+}
+
+/*
+ * md_statistics_x.c:104-161 (md_alloc_sk_sphere_3d_x): wave vectors of the
+ * cube q0, q0 + qincre, ... <= qmax (loop order x, y, z), one per distinct |q|
+ * (first found within 1e-4), |q| >= 1e-4, then the reference's exchange sort
+ * by |q|.  qs[n], qis[3n] must hold max entries; returns the count.
+ */
+int orc_sk_sphere(double q0, double qincre, double qmax, int max, double *qs, double *qis) {
+  int n = 0;
+  for (double qx = q0; qx <= qmax; qx += qincre)
+    for (double qy = q0; qy <= qmax; qy += qincre)
+      for (double qz = q0; qz <= qmax; qz += qincre) {
+        const double q = sqrt(qx * qx + qy * qy + qz * qz);
+        if (fabs(q) < 1e-4) continue;
+        int found = 0;
+        for (int i = 0; i < n && !found; ++i)
+          if (fabs(qs[i] - q) < 1e-4) found = 1;
+        if (found || n >= max) continue;
+        qs[n] = q;
+        qis[3 * n] = qx;
+        qis[3 * n + 1] = qy;
+        qis[3 * n + 2] = qz;
+        ++n;
+      }
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < i; ++j)
+      if (qs[j] > qs[i]) {
+        double t = qs[i];
+        qs[i] = qs[j];
+        qs[j] = t;
+        for (int k = 0; k < 3; ++k) {
+          t = qis[3 * i + k];
+          qis[3 * i + k] = qis[3 * j + k];
+          qis[3 * j + k] = t;
+        }
+      }
+  return n;
+}
+
+/*
+ * md_pimd_x.c:5404-5448: for wave vector j, with a = bead 1 and b = bead
+ * (pi-1) mod P + 1 of every particle (positions x[(l*P + bead)*3 + d],
+ * bead 0-based), res[j] = (sum cos q.x_a)(sum cos q.x_b)/N +
+ * (sum sin q.x_a)(sum sin q.x_b)/N, sums in particle order.
+ */
+void orc_sk_structure(int N, int P, const double *x, int pi, int nq, const double *qis, double *res) {
+  const int jb = (pi - 1) % P;
+  for (int j = 0; j < nq; ++j) {
+    double out = 0, sum = 0, sum2 = 0;
+    for (int l = 0; l < N; ++l) {
+      double t = 0;
+      for (int d = 0; d < 3; ++d) t += qis[3 * j + d] * x[((size_t)l * P) * 3 + d];
+      sum += cos(t);
+    }
+    for (int l = 0; l < N; ++l) {
+      double t = 0;
+      for (int d = 0; d < 3; ++d) t += qis[3 * j + d] * x[((size_t)l * P + jb) * 3 + d];
+      sum2 += cos(t);
+    }
+    out += sum * sum2 / N;
+    sum = sum2 = 0;
+    for (int l = 0; l < N; ++l) {
+      double t = 0;
+      for (int d = 0; d < 3; ++d) t += qis[3 * j + d] * x[((size_t)l * P) * 3 + d];
+      sum += sin(t);
+    }
+    for (int l = 0; l < N; ++l) {
+      double t = 0;
+      for (int d = 0; d < 3; ++d) t += qis[3 * j + d] * x[((size_t)l * P + jb) * 3 + d];
+      sum2 += sin(t);
+    }
+    out += sum * sum2 / N;
+    res[j] = out;
   }
 }

@@ -215,6 +215,17 @@ static void run(const scen_t *c) {
     md_pimd_calc_vi_sign_x(pimd, es, ss, -1.0);
     rec1("s1/sign_m1", es->es[0]);
   }
+#if MD_DIMENSION_X == 3
+  {
+    /* spherical S(k) between bead 1 and bead P/2+1 at these positions */
+    md_sk_sphere_t_x *sk = md_alloc_sk_sphere_3d_x(0.0, 0.5, 2.0);
+    md_stats_t_x *st = md_alloc_stats_x(sk->N);
+    md_pimd_calc_sphere_Sk_structure_x(pimd, st, c->P / 2 + 1, sk);
+    rec("sk/qs", sk->qs, sk->N);
+    rec("sk/qis", sk->qis, 3L * sk->N);
+    rec("sk/res", st->fxs[st->N - 1], sk->N);
+  }
+#endif
   md_update_nhc_VV3_2_x(sim, c->dt);
   rec_state("s2/", sim);
   if (c->pbc) {

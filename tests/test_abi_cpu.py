@@ -163,3 +163,15 @@ def test_no_gpu_fails_loudly():
     assert lib.md_pimd_fast_fill_ENk_x(s.pimd, 0) == -1001
     assert lib.md_update_nhc_VV3_1_x(s.sim, 0.01) == -1001
     assert "no CUDA device" in lib.err()
+
+
+def test_sk_sphere_builder_matches_reference():
+    """md_alloc_sk_sphere_3d_x (host) against the reference's own shells"""
+    import fixtures
+    lib = xmd_x.load(3, 4)
+    fx = fixtures.load("d3l4_trap_vi1")
+    sk = lib.md_alloc_sk_sphere_3d_x(0.0, 0.5, 2.0)
+    n = sk.contents.N
+    assert n == len(fx["sk/qs"])
+    np.testing.assert_array_equal(np.ctypeslib.as_array(sk.contents.qs, (n,)), fx["sk/qs"])
+    np.testing.assert_array_equal(np.ctypeslib.as_array(sk.contents.qis, (3 * n,)), fx["sk/qis"])

@@ -70,6 +70,13 @@ def test_step_stages_match_reference(name):
     ss.contents.es[0] = 1.0
     ck(lib.md_pimd_calc_vi_sign_x(s.pimd, es, ss, -1.0))
     assert_close([es.contents.es[0]], fx["s1/sign_m1"], 1e-9, "xi=-1 reweighting")
+    if lib.D == 3:
+        sk = lib.md_alloc_sk_sphere_3d_x(0.0, 0.5, 2.0)
+        n = sk.contents.N
+        st = lib.md_alloc_stats_x(n)
+        ck(lib.md_pimd_calc_sphere_Sk_structure_x(s.pimd, st, h["P"] // 2 + 1, sk))
+        got = np.array([st.contents.fxs[0][j] for j in range(n)])
+        assert_close(got, fx["sk/res"], PARITY, "spherical S(k)")
     ck(lib.md_update_nhc_VV3_2_x(s.sim, h["dt"]))
     st = s.state()
     for k in ("x", "v", "theta", "vtheta"):

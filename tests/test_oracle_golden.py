@@ -63,6 +63,12 @@ def test_oracle_one_step_stages(name):
     assert_close([ep], fx["s1/e_pair"], 1e-12, "pair energy")
     sg = L.orc_vi_sign(N, h["beta"], h["vi"], -1.0, orc.ptr(ENk), orc.ptr(VBN))
     assert_close([sg], fx["s1/sign_m1"], 1e-11, "xi=-1 reweighting")
+    if D == 3:
+        qs, qis = orc.sk_sphere(0.0, 0.5, 2.0)
+        np.testing.assert_array_equal(qs, fx["sk/qs"])
+        np.testing.assert_array_equal(qis.ravel(), fx["sk/qis"])
+        res = orc.sk_structure(N, P, s.x, P // 2 + 1, qis)
+        assert_close(res, fx["sk/res"], 1e-12, "spherical S(k)")
     assert L.orc_nhc_vv3_2(s.ref, h["dt"]) == 0
     for k in ("x", "v", "theta", "vtheta"):
         assert_close(getattr(s, k), fx["s2/" + k], TIGHT, f"VV3_2 {k}")
