@@ -58,12 +58,15 @@ def config(form):
 # ---------------------------------------------------------------------
 # distributed plumbing (one independent replica per rank)
 # ---------------------------------------------------------------------
-def dist_init():
+def dist_init(backend=None):
+    """one process per GPU (torchrun); NCCL on GPUs, gloo otherwise"""
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     if ws <= 1:
         return None, 0, 1
+    import torch
     import torch.distributed as dist
-    backend = "nccl"
+    if backend is None:
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
     dist.init_process_group(backend=backend)
     return dist, dist.get_rank(), ws
 
@@ -77,9 +80,17 @@ def max_over_ranks(dist, v):
     if dist is None:
         return v
     import torch
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def replica_result(dist, ws, beads_per_replica, ms_local):
+    """whole-job throughput of independent replicas: every rank advances its
+    own system; the job's step time is the slowest rank's"""
+    ms = max_over_ranks(dist, ms_local)
+    return ws * beads_per_replica / (ms * 1e-3), ms
 
 
 class Clocks:
