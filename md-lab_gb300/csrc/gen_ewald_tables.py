@@ -24,7 +24,7 @@ import mpmath as mp
 import numpy as np
 
 mp.mp.dps = 40
-W, NINT, DEG = 0.25, 25, 12
+W, NINT, DEG = 0.0625, 98, 8
 XMAX = (NINT - 0.5) * W
 
 

@@ -1617,7 +1617,7 @@ __device__ inline void pair_eval(const PairPrm &p, const Geo &g, const double *d
 }
 
 template <int D, int KIND, bool ENERGY>
-__global__ void __launch_bounds__(256, 1) k_pair_tiles(Geo g, PairPrm p,
+__global__ void __launch_bounds__(256, 2) k_pair_tiles(Geo g, PairPrm p,
                                                     const double *__restrict__ x,
                                                     const double *__restrict__ m,
                                                     double *__restrict__ out, int T, int jobs) {
@@ -1630,87 +1630,90 @@ __global__ void __launch_bounds__(256, 1) k_pair_tiles(Geo g, PairPrm p,
   }
   __shared__ EwWarp ewq[KIND == PAIR_EWALD_REAL ? 8 : 1];
   EwWarp *ews = &ewq[KIND == PAIR_EWALD_REAL ? (threadIdx.x >> 5) : 0];
-  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
-  if (warp >= jobs * g.P) return;
-  const int j = warp / jobs;
-  int job = warp % jobs, I = 0;
-  while (job >= T - I) {
-    job -= T - I;
-    ++I;
-  }
-  const int J = I + job;
-  const int a = I * 32 + lane, b0 = J * 32 + lane;
-  const bool va = a < g.N, vb = b0 < g.N;
-  double xa[D], xb[D], fa[D], fb[D];
-  float xaf[D], xbf[D];  // FP32 copies for the Ewald image culling
-#pragma unroll
-  for (int d = 0; d < D; ++d) {
-    xa[d] = va ? x[sidx(j, d, a, D, g.Ns)] : 0.0;
-    xb[d] = vb ? x[sidx(j, d, b0, D, g.Ns)] : 0.0;
-    xaf[d] = (float)xa[d];
-    xbf[d] = (float)xb[d];
-    fa[d] = fb[d] = 0.0;
-  }
-  // inverse masses, so that each pair multiplies instead of dividing
-  const double ima = (!ENERGY && va) ? 1.0 / m[(size_t)j * g.Ns + a] : 1.0;
-  double imb = (!ENERGY && vb) ? 1.0 / m[(size_t)j * g.Ns + b0] : 1.0;
-  double ea = 0;
-  for (int s = 0; s < 32; ++s) {
-    const int bi = J * 32 + ((lane + s) & 31);
-    const bool act = va && bi < g.N && (I != J || a > bi);
-    double dx[D], F[D], E = 0;
-    float dxf[D];
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  // warps loop over the tile jobs (slice j, tile pair I <= J) round-robin, so
+  // that a grid of resident blocks (pair_launch) stages the tables once
+  for (int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; warp < jobs * g.P; warp += nwarps) {
+    const int j = warp / jobs;
+    int job = warp % jobs, I = 0;
+    while (job >= T - I) {
+      job -= T - I;
+      ++I;
+    }
+    const int J = I + job;
+    const int a = I * 32 + lane, b0 = J * 32 + lane;
+    const bool va = a < g.N, vb = b0 < g.N;
+    double xa[D], xb[D], fa[D], fb[D];
+    float xaf[D], xbf[D];  // FP32 copies for the Ewald image culling
 #pragma unroll
     for (int d = 0; d < D; ++d) {
-      dx[d] = xa[d] - xb[d];
-      dxf[d] = xaf[d] - xbf[d];
-      F[d] = 0;
+      xa[d] = va ? x[sidx(j, d, a, D, g.Ns)] : 0.0;
+      xb[d] = vb ? x[sidx(j, d, b0, D, g.Ns)] : 0.0;
+      xaf[d] = (float)xa[d];
+      xbf[d] = (float)xb[d];
+      fa[d] = fb[d] = 0.0;
     }
-    if (KIND == PAIR_EWALD_REAL) pair_eval<D, KIND, ENERGY>(p, g, dx, dxf, F, E, ENERGY, stab, act, ews, lane);
-    if (act) {
-      if (KIND != PAIR_EWALD_REAL)
-        pair_eval<D, KIND, ENERGY>(p, g, dx, dxf, F, E, ENERGY, stab, true, nullptr, lane);
-      if (ENERGY) {
-        ea += E;
-      } else {
-        // the reference divides by the mass of the higher-index particle
-        const double inv = a > bi ? ima : imb;
+    // inverse masses, so that each pair multiplies instead of dividing
+    const double ima = (!ENERGY && va) ? 1.0 / m[(size_t)j * g.Ns + a] : 1.0;
+    double imb = (!ENERGY && vb) ? 1.0 / m[(size_t)j * g.Ns + b0] : 1.0;
+    double ea = 0;
+    for (int s = 0; s < 32; ++s) {
+      const int bi = J * 32 + ((lane + s) & 31);
+      const bool act = va && bi < g.N && (I != J || a > bi);
+      double dx[D], F[D], E = 0;
+      float dxf[D];
 #pragma unroll
-        for (int d = 0; d < D; ++d) {
-          fa[d] += F[d] * inv;
-          fb[d] -= F[d] * inv;
+      for (int d = 0; d < D; ++d) {
+        dx[d] = xa[d] - xb[d];
+        dxf[d] = xaf[d] - xbf[d];
+        F[d] = 0;
+      }
+      if (KIND == PAIR_EWALD_REAL) pair_eval<D, KIND, ENERGY>(p, g, dx, dxf, F, E, ENERGY, stab, act, ews, lane);
+      if (act) {
+        if (KIND != PAIR_EWALD_REAL)
+          pair_eval<D, KIND, ENERGY>(p, g, dx, dxf, F, E, ENERGY, stab, true, nullptr, lane);
+        if (ENERGY) {
+          ea += E;
+        } else {
+          // the reference divides by the mass of the higher-index particle
+          const double inv = a > bi ? ima : imb;
+#pragma unroll
+          for (int d = 0; d < D; ++d) {
+            fa[d] += F[d] * inv;
+            fb[d] -= F[d] * inv;
+          }
         }
       }
-    }
-    const int src = (lane + 1) & 31;
+      const int src = (lane + 1) & 31;
 #pragma unroll
-    for (int d = 0; d < D; ++d) {
-      xb[d] = __shfl_sync(FULL, xb[d], src);
-      if (KIND == PAIR_EWALD_REAL) xbf[d] = __shfl_sync(FULL, xbf[d], src);
-      if (!ENERGY) fb[d] = __shfl_sync(FULL, fb[d], src);
+      for (int d = 0; d < D; ++d) {
+        xb[d] = __shfl_sync(FULL, xb[d], src);
+        if (KIND == PAIR_EWALD_REAL) xbf[d] = __shfl_sync(FULL, xbf[d], src);
+        if (!ENERGY) fb[d] = __shfl_sync(FULL, fb[d], src);
+      }
+      if (!ENERGY) imb = __shfl_sync(FULL, imb, src);
     }
-    if (!ENERGY) imb = __shfl_sync(FULL, imb, src);
-  }
-  if (ENERGY) {
-    ea = warp_sum(ea);
-    if (lane == 0) out[warp] = ea;
-    return;
-  }
-  // slot layout: out[((t*P + j)*D + d)*Ns + l]
-  if (I == J) {
-    if (va) {
-#pragma unroll
-      for (int d = 0; d < D; ++d) out[(((size_t)I * g.P + j) * D + d) * g.Ns + a] = fa[d] + fb[d];
+    if (ENERGY) {
+      ea = warp_sum(ea);
+      if (lane == 0) out[warp] = ea;
+      continue;
     }
-  } else {
-    if (va) {
+    // slot layout: out[((t*P + j)*D + d)*Ns + l]
+    if (I == J) {
+      if (va) {
 #pragma unroll
-      for (int d = 0; d < D; ++d) out[(((size_t)J * g.P + j) * D + d) * g.Ns + a] = fa[d];
-    }
-    if (vb) {
+        for (int d = 0; d < D; ++d) out[(((size_t)I * g.P + j) * D + d) * g.Ns + a] = fa[d] + fb[d];
+      }
+    } else {
+      if (va) {
 #pragma unroll
-      for (int d = 0; d < D; ++d) out[(((size_t)I * g.P + j) * D + d) * g.Ns + b0] = fb[d];
+        for (int d = 0; d < D; ++d) out[(((size_t)J * g.P + j) * D + d) * g.Ns + a] = fa[d];
+      }
+      if (vb) {
+#pragma unroll
+        for (int d = 0; d < D; ++d) out[(((size_t)I * g.P + j) * D + d) * g.Ns + b0] = fb[d];
+      }
     }
   }
 }
@@ -1735,41 +1738,61 @@ size_t pair_scratch_doubles(const Geo &g) {
   return a > b ? a : b;
 }
 
+// resident blocks of a kernel of 256 threads (the persistent grid), or fewer
+// when the warps needed run out
+template <class K>
+static int resident_grid(K kernel, size_t warps_needed, int &occ, int &sms) {
+  if (!occ) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, 256, 0) != cudaSuccess || occ < 1) occ = 1;
+    if (sms < 1) sms = 1;
+  }
+  const size_t need = (warps_needed + 7) / 8, full = (size_t)sms * occ;
+  return (int)(need < full ? need : full);
+}
+
+template <int D, int KIND, bool ENERGY>
+static int pair_grid(size_t warps_needed) {
+  static int occ = 0, sms = 0;
+  return resident_grid(k_pair_tiles<D, KIND, ENERGY>, warps_needed, occ, sms);
+}
+
 template <int D, bool ENERGY>
 static cudaError_t pair_launch(const Geo &g, const PairPrm &p, const double *x, const double *m,
                                double *out, int T, int jobs, cudaStream_t st) {
-  const size_t thr = (size_t)jobs * g.P * 32;
-  const int nb = cdiv(thr, 256);
+  const size_t warps = (size_t)jobs * g.P;
   switch (p.kind) {
     case PAIR_GAUSSIAN:
       {
         XK_PROF("pair_tiles_gauss");
-        k_pair_tiles<D, PAIR_GAUSSIAN, ENERGY><<<nb, 256, 0, st>>>(g, p, x, m, out, T, jobs);
+        k_pair_tiles<D, PAIR_GAUSSIAN, ENERGY><<<pair_grid<D, PAIR_GAUSSIAN, ENERGY>(warps), 256, 0, st>>>(g, p, x, m, out, T, jobs);
       }
       break;
     case PAIR_PERIODIC_GAUSSIAN:
       {
         XK_PROF("pair_tiles_pgauss");
-        k_pair_tiles<D, PAIR_PERIODIC_GAUSSIAN, ENERGY><<<nb, 256, 0, st>>>(g, p, x, m, out, T, jobs);
+        k_pair_tiles<D, PAIR_PERIODIC_GAUSSIAN, ENERGY><<<pair_grid<D, PAIR_PERIODIC_GAUSSIAN, ENERGY>(warps), 256, 0, st>>>(g, p, x, m, out, T, jobs);
       }
       break;
     case PAIR_COULOMB:
       {
         XK_PROF("pair_tiles_coul");
-        k_pair_tiles<D, PAIR_COULOMB, ENERGY><<<nb, 256, 0, st>>>(g, p, x, m, out, T, jobs);
+        k_pair_tiles<D, PAIR_COULOMB, ENERGY><<<pair_grid<D, PAIR_COULOMB, ENERGY>(warps), 256, 0, st>>>(g, p, x, m, out, T, jobs);
       }
       break;
     case PAIR_PERIODIC_COULOMB:
       {
         XK_PROF("pair_tiles_pcoul");
-        k_pair_tiles<D, PAIR_PERIODIC_COULOMB, ENERGY><<<nb, 256, 0, st>>>(g, p, x, m, out, T, jobs);
+        k_pair_tiles<D, PAIR_PERIODIC_COULOMB, ENERGY><<<pair_grid<D, PAIR_PERIODIC_COULOMB, ENERGY>(warps), 256, 0, st>>>(g, p, x, m, out, T, jobs);
       }
       break;
     case PAIR_EWALD_REAL:
       if (D != 3) return cudaErrorInvalidValue;
       {
         XK_PROF("pair_tiles_ewald_real");
-        k_pair_tiles<D, PAIR_EWALD_REAL, ENERGY><<<nb, 256, 0, st>>>(g, p, x, m, out, T, jobs);
+        k_pair_tiles<D, PAIR_EWALD_REAL, ENERGY><<<pair_grid<D, PAIR_EWALD_REAL, ENERGY>(warps), 256, 0, st>>>(g, p, x, m, out, T, jobs);
       }
       break;
     default:

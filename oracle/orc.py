@@ -66,6 +66,8 @@ def lib():
             "orc_trap_force": (i, [vp, i, i, i, vp]),
             "orc_pair_force": (i, [vp, i, i, i, vp]),
             "orc_pair_force_one": (None, [i, vp, i, _dp, _dp, _dp, _dp, d]),
+            "orc_pair_force_2": (i, [vp, i, vp, i, i, i, vp]),
+            "orc_pair_energy_2": (d, [vp, i, vp, i, i, i, vp]),
             "orc_vbn_energy": (d, [i, i, i, d, d, _dp, _dp]),
             "orc_fast_fill_ENk2": (i, [vp, i, i, d, i, _dp]),
             "orc_fill_ENk2_cubic": (i, [vp, i, i, d, i, _dp]),
@@ -133,6 +135,53 @@ class OrcSim:
         return cls(D, L, N * P, fx["m"], fx[prefix + "x"], fx[prefix + "v"], fx[prefix + "f"],
                    fx[prefix + "cf"], fx[prefix + "theta"], fx[prefix + "vtheta"], fx[prefix + "Q"],
                    T, [box] * 3)
+
+
+def two_from_fixture(fx, prefix="init/"):
+    """The two species' states ("a/" and "b/" records) of a two-species fixture."""
+    h = fx["hdr"]
+    D, L, Na, Nb, P = (int(v) for v in h[:5])
+    T, box, mb = h[8], h[9], h[19]
+    out = []
+    for sp, N, m in (("a/", Na, 1.0), ("b/", Nb, mb)):
+        q = sp + prefix
+        out.append(OrcSim(D, L, N * P, np.full(N * P, m), fx[q + "x"], fx[q + "v"], fx[q + "f"], fx[q + "cf"],
+                          fx[q + "theta"], fx[q + "vtheta"], fx[q + "Q"], T, [box] * 3))
+    return out
+
+
+def pair_force_2(a, Na, b, Nb, P, kind, prm):
+    """Cross-species pair forces added into a.f and b.f (md_pimd_calc_pair_force_2_x)."""
+    assert lib().orc_pair_force_2(a.ref, Na, b.ref, Nb, P, kind, C.byref(prm)) == 0
+
+
+def pair_energy_2(a, Na, b, Nb, P, kind, prm):
+    return lib().orc_pair_energy_2(a.ref, Na, b.ref, Nb, P, kind, C.byref(prm))
+
+
+def two_species_forces(a, b, Na, Nb, P, beta, vi, omegaP, image, trap, pair, prm):
+    """Forces of a two-species step in the order a driver calls the reference:
+    each species' exchange, trap and pair forces, then the cross term."""
+    L = lib()
+    for s, N in ((a, Na), (b, Nb)):
+        L.orc_reset_force(s.ref)
+        ENk, _ = fast_fill_ENk(s, N, P, omegaP, image)
+        VBN = fill_VB(N, beta, vi, ENk)
+        fast_force_VB(s, N, P, beta, vi, omegaP, image, ENk, VBN)
+        if trap:
+            L.orc_trap_force(s.ref, N, P, trap, C.byref(prm))
+        L.orc_pair_force(s.ref, N, P, pair, C.byref(prm))
+    pair_force_2(a, Na, b, Nb, P, pair, prm)
+
+
+def two_species_step(a, b, Na, Nb, P, beta, vi, omegaP, image, trap, pair, prm, dt, pbc):
+    L = lib()
+    assert L.orc_nhc_vv3_1(a.ref, dt) == 0 and L.orc_nhc_vv3_1(b.ref, dt) == 0
+    two_species_forces(a, b, Na, Nb, P, beta, vi, omegaP, image, trap, pair, prm)
+    assert L.orc_nhc_vv3_2(a.ref, dt) == 0 and L.orc_nhc_vv3_2(b.ref, dt) == 0
+    if pbc:
+        L.orc_periodic_boundary(a.ref)
+        L.orc_periodic_boundary(b.ref)
 
 
 def params(trap_w=1.0, trap_c=(0, 0, 0), trap_w2=(1, 1, 1), gauss_g=0.0, gauss_s=1.0,

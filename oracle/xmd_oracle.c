@@ -526,6 +526,27 @@ int orc_pair_force(orc_sim_t *s, int N, int P, int kind, const orc_params_t *p) 
   return 0;
 }
 
+/* two species, md_pimd_x.c:3444-3467 (the CPU branch of
+   md_pimd_calc_pair_force_2_x): in every bead slice each bead of species a
+   meets each bead of species b once; the callback gets a's mass and a's box,
+   f_a += F/P and f_b -= m_a F/(P m_b) */
+int orc_pair_force_2(orc_sim_t *a, int Na, orc_sim_t *b, int Nb, int P, int kind, const orc_params_t *p) {
+  const int D = a->D;
+  if (b->D != D) return -1;
+  for (int j = 1; j <= P; ++j)
+    for (int l = 1; l <= Na; ++l)
+      for (int l2 = 1; l2 <= Nb; ++l2) {
+        int ia = bidx(l, j, P), ib = bidx(l2, j, P);
+        double f[8] = {0};
+        orc_pair_force_one(kind, p, D, a->x + (size_t)ia * D, b->x + (size_t)ib * D, f, a->box, a->m[ia]);
+        for (int i = 0; i < D; ++i) {
+          a->f[(size_t)ia * D + i] += f[i] / P;
+          b->f[(size_t)ib * D + i] -= a->m[ia] * f[i] / P / b->m[ib];
+        }
+      }
+  return 0;
+}
+
 /* ------------------------------------------------------------------ */
 /* estimators                                                           */
 /* ------------------------------------------------------------------ */
@@ -730,6 +751,21 @@ double orc_pair_energy(const orc_sim_t *s, int N, int P, int kind, const orc_par
       for (int l2 = 1; l2 < l; ++l2) {
         int b = bidx(l, j, P), b2 = bidx(l2, j, P);
         e += orc_pair_energy_one(kind, p, s->D, s->x + (size_t)b * s->D, s->x + (size_t)b2 * s->D, s->box) / P;
+      }
+  return e;
+}
+
+/* two species, md_pimd_x.c:3606-3627 (the CPU branch of
+   md_pimd_calc_pair_energy_2_x): sum over slices and all (a, b) pairs of
+   V/P with a's box */
+double orc_pair_energy_2(const orc_sim_t *a, int Na, const orc_sim_t *b, int Nb, int P, int kind,
+                         const orc_params_t *p) {
+  double e = 0;
+  for (int j = 1; j <= P; ++j)
+    for (int l = 1; l <= Na; ++l)
+      for (int l2 = 1; l2 <= Nb; ++l2) {
+        int ia = bidx(l, j, P), ib = bidx(l2, j, P);
+        e += orc_pair_energy_one(kind, p, a->D, a->x + (size_t)ia * a->D, b->x + (size_t)ib * b->D, a->box) / P;
       }
   return e;
 }

@@ -97,6 +97,9 @@ int orc_trap_force(orc_sim_t *s, int N, int P, int kind, const orc_params_t *p);
 int orc_pair_force(orc_sim_t *s, int N, int P, int kind, const orc_params_t *p);
 void orc_pair_force_one(int kind, const orc_params_t *p, int D, const double *p1,
                         const double *p2, double *f, const double *L, double m);
+/* two species with the same P: cross pairs only (md_pimd_calc_pair_force_2_x) */
+int orc_pair_force_2(orc_sim_t *a, int Na, orc_sim_t *b, int Nb, int P, int kind,
+                     const orc_params_t *p);
 
 /* ---- estimators ---- */
 double orc_vbn_energy(int D, int N, int P, double beta, double vi,
@@ -114,6 +117,8 @@ double orc_pair_energy(const orc_sim_t *s, int N, int P, int kind,
                        const orc_params_t *p);
 double orc_pair_energy_one(int kind, const orc_params_t *p, int D,
                            const double *p1, const double *p2, const double *L);
+double orc_pair_energy_2(const orc_sim_t *a, int Na, const orc_sim_t *b, int Nb,
+                         int P, int kind, const orc_params_t *p);
 double orc_madelung(const double *L, const orc_params_t *p);
 double orc_vi_sign(int N, double beta, double vi, double vi2, const double *ENk,
                    const double *VBN);

@@ -12,6 +12,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 HDR_PIMD = ["D", "L", "N", "P", "f", "fc", "vi", "beta", "omegaP", "T", "box", "dt",
             "image", "pbc", "ueg", "g", "s", "alpha", "nsum", "steps", "every"]
 HDR_CUBIC = ["D", "L", "N", "P", "vi", "beta", "omegaP", "image", "box"]
+HDR_TWO = ["D", "L", "N", "Nb", "P", "vi", "beta", "omegaP", "T", "box", "dt", "image", "pbc",
+           "ueg", "g", "s", "alpha", "nsum", "steps", "mb"]
 
 
 def load(name):
@@ -31,11 +33,11 @@ def load(name):
 
 
 def header(fx, kind="pimd"):
-    keys = HDR_PIMD if kind == "pimd" else HDR_CUBIC
+    keys = {"pimd": HDR_PIMD, "cubic": HDR_CUBIC, "two": HDR_TWO}[kind]
     h = fx["hdr"]
     out = {}
     for k, v in zip(keys, h):
-        out[k] = int(v) if k in ("D", "L", "N", "P", "f", "fc", "image", "pbc", "ueg",
+        out[k] = int(v) if k in ("D", "L", "N", "Nb", "P", "f", "fc", "image", "pbc", "ueg",
                                  "nsum", "steps", "every") else float(v)
     return out
 
@@ -44,3 +46,4 @@ PIMD_FIXTURES = ["d2l4_cfg1", "d3l4_trap_vi1", "d3l4_trap_vi05", "d3l4_trap_vi0"
                  "d3l4_trap_n37p6", "d3l4_trap_p2", "d3l4_trap_n1", "d3l4_trap_chain3",
                  "d3l4_ueg", "d3l8_trap"]
 CUBIC_FIXTURES = ["d3l4_cubic", "d3l4_cubic_img"]
+TWO_FIXTURES = ["d3l4_two_ueg", "d3l4_two_trap", "d2l4_two_trap"]

@@ -358,6 +358,115 @@ static void run_pairs(void) {
   free(p);
 }
 
+/* two species with the same P (md_pimd_calc_pair_force_2_x,
+   md_pimd_calc_pair_energy_2_x): a spin-unpolarised electron gas, N up and
+   Nb down electrons in one box with Ewald everywhere (ueg=1), or two trapped
+   species with Gaussian interactions (ueg=0).  Species b has mass mb.
+   Records both initial states, the cross forces and cross energy alone, the
+   forces of a full two-species force call, and a short trajectory in which
+   each species has its own exchange and pair forces plus the cross term. */
+static md_pair_force_t_x g_pf2;
+static md_pair_energy_t_x g_pe2;
+
+static void forces2(md_pimd_t_x *pa, md_pimd_t_x *pb, const scen_t *c) {
+  md_pimd_t_x *ps[2] = {pa, pb};
+  for (int s = 0; s < 2; ++s) {
+    md_reset_force_x(ps[s]->sim);
+    md_pimd_fast_fill_ENk_x(ps[s], c->image);
+    md_pimd_fill_VB_x(ps[s]);
+    md_pimd_fast_fill_force_VB_x(ps[s], c->image);
+    if (!c->ueg) md_pimd_calc_trap_force_x(ps[s], md_harmonic_trap_force_x);
+    md_pimd_calc_pair_force_x(ps[s], g_pf2);
+  }
+  md_pimd_calc_pair_force_2_x(pa, pb, g_pf2);
+}
+
+static void run_two(const scen_t *c, int Nb, double mb) {
+  md_set_pimd_mode_x(1);
+  md_set_seed_x((unsigned)c->seed);
+  const int Na = c->N, P = c->P;
+  md_simulation_t_x *sa = md_alloc_simulation_x(Na * P, c->f, c->fc, MD_ND_RECT_BOX_X);
+  md_simulation_t_x *sb = md_alloc_simulation_x(Nb * P, c->f, c->fc, MD_ND_RECT_BOX_X);
+  double T, Lb;
+  if (c->ueg) {
+    /* unpolarised gas: n = (Na + Nb)/L^3 = 3/(4 pi rs^3), T_F = (3 pi^2 n)^(2/3)/2 */
+    Lb = cbrt(4.0 * M_PI * (Na + Nb) / 3.0) * c->rs;
+    double n = (Na + Nb) / (Lb * Lb * Lb);
+    T = c->theta * 0.5 * pow(3.0 * M_PI * M_PI * n, 2.0 / 3.0);
+    g_pf2 = md_coulomb_3d_ewald_force_x;
+    g_pe2 = md_coulomb_3d_ewald_energy_x;
+  } else {
+    Lb = c->box;
+    T = 1.0 / c->beta;
+    g_pf2 = md_gaussian_force_x;
+    g_pe2 = md_gaussian_energy_x;
+  }
+  double Lv[D], center[D], zero[D];
+  for (int d = 0; d < D; ++d) {
+    Lv[d] = Lb;
+    center[d] = Lb / 2;
+    zero[d] = 0;
+  }
+  md_init_nd_rect_box_x(sa->box, Lv);
+  md_init_nd_rect_box_x(sb->box, Lv);
+  md_pimd_t_x *pa = md_alloc_pimd_x(sa, Na, P, c->vi, T);
+  md_pimd_t_x *pb = md_alloc_pimd_x(sb, Nb, P, c->vi, T);
+  md_init_particle_mass_x(sa, 1.0, 0, Na * P);
+  md_init_particle_mass_x(sb, mb, 0, Nb * P);
+  md_simulation_t_x *ss[2] = {sa, sb};
+  md_pimd_t_x *ps[2] = {pa, pb};
+  for (int s = 0; s < 2; ++s) {
+    if (c->ueg)
+      md_pimd_init_particle_uniform_pos_x(ps[s], center, Lv, 0.05 * c->rs);
+    else
+      for (int b = 0; b < ss[s]->N; ++b)
+        for (int d = 0; d < D; ++d) ss[s]->particles[b].x[d] = md_random_gaussian_x();
+    md_init_maxwell_vel_x(ss[s], T);
+    md_init_nhc_x(ss[s], md_get_quick_Q_x(T, ps[s]->omegaP), 0, ss[s]->Nf, 0);
+    for (int b = 0; b < ss[s]->N; ++b)
+      for (int d = 0; d < D; ++d) ss[s]->particles[b].f[d] = 0;
+  }
+  md_set_harmonic_trap_frequency_x(1.0);
+  md_set_harmonic_trap_center_x(zero);
+  md_set_gaussian_force_strength_x(c->g);
+  md_set_guassian_force_range_x(c->s);
+  md_set_coulomb_force_strength_x(1.0);
+  md_set_coulomb_truc_x(c->alpha_L / Lb);
+  md_set_coulomb_n_sum_x(c->nsum);
+  double hdr[] = {D, LC, Na, Nb, P, c->vi, pa->beta, pa->omegaP, T, Lb, c->dt, c->image, c->pbc, c->ueg,
+                  c->g, c->s, c->alpha_L / Lb, c->nsum, c->steps, mb};
+  rec("hdr", hdr, sizeof hdr / sizeof hdr[0]);
+  rec_state("a/init/", sa);
+  rec_state("b/init/", sb);
+  /* the cross term alone */
+  md_reset_force_x(sa);
+  md_reset_force_x(sb);
+  md_pimd_calc_pair_force_2_x(pa, pb, g_pf2);
+  rec_field("a/cross/", sa, 'f');
+  rec_field("b/cross/", sb, 'f');
+  md_pimd_calc_pair_energy_2_x(pa, pb, g_pe2, g_st);
+  rec1("cross/e", take());
+  /* a full force call, then a trajectory starting from those forces */
+  forces2(pa, pb, c);
+  rec_field("a/all/", sa, 'f');
+  rec_field("b/all/", sb, 'f');
+  for (int st = 1; st <= c->steps; ++st) {
+    md_update_nhc_VV3_1_x(sa, c->dt);
+    md_update_nhc_VV3_1_x(sb, c->dt);
+    forces2(pa, pb, c);
+    md_update_nhc_VV3_2_x(sa, c->dt);
+    md_update_nhc_VV3_2_x(sb, c->dt);
+    if (c->pbc) {
+      md_periodic_boundary_x(sa);
+      md_periodic_boundary_x(sb);
+    }
+  }
+  rec_state("a/final/", sa);
+  rec_state("b/final/", sb);
+  md_pimd_calc_pair_energy_2_x(pa, pb, g_pe2, g_st);
+  rec1("final/cross_e", take());
+}
+
 static int geti(int argc, char **argv, const char *k, int dflt) {
   size_t n = strlen(k);
   for (int i = 3; i < argc; ++i)
@@ -408,6 +517,8 @@ int main(int argc, char **argv) {
     run_rng();
   else if (!strcmp(argv[1], "pairs"))
     run_pairs();
+  else if (!strcmp(argv[1], "two"))
+    run_two(&c, geti(argc, argv, "Nb", 4), getd(argc, argv, "mb", 1.0));
   else
     return 2;
   fclose(g_out);

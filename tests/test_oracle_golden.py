@@ -181,3 +181,31 @@ def test_oracle_pair_callbacks(fname, D):
         if nm.startswith("ewald"):
             mad = L.orc_madelung(orc.ptr(box), orc.C.byref(p))
             assert_close([mad], fx[nm + "/mad"], TIGHT, nm + " Madelung")
+
+
+@pytest.mark.parametrize("name", fixtures.TWO_FIXTURES)
+def test_oracle_two_species(name):
+    """Cross-species forces and energy (md_pimd_calc_pair_force_2_x,
+    md_pimd_calc_pair_energy_2_x) and a two-species trajectory."""
+    fx = fixtures.load(name)
+    h = fixtures.header(fx, "two")
+    Na, Nb, P = h["N"], h["Nb"], h["P"]
+    prm, trap, pair = _cfg(h)
+    a, b = orc.two_from_fixture(fx)
+    a.f[:] = 0
+    b.f[:] = 0
+    orc.pair_force_2(a, Na, b, Nb, P, pair, prm)
+    assert_close(a.f, fx["a/cross/f"], TIGHT, "cross force on a")
+    assert_close(b.f, fx["b/cross/f"], TIGHT, "cross force on b")
+    assert_close([orc.pair_energy_2(a, Na, b, Nb, P, pair, prm)], fx["cross/e"], TIGHT, "cross energy")
+    orc.two_species_forces(a, b, Na, Nb, P, h["beta"], h["vi"], h["omegaP"], h["image"], trap, pair, prm)
+    assert_close(a.f, fx["a/all/f"], TIGHT, "all forces on a")
+    assert_close(b.f, fx["b/all/f"], TIGHT, "all forces on b")
+    # the trajectory starts from these forces, as the reference's run did
+    for _ in range(h["steps"]):
+        orc.two_species_step(a, b, Na, Nb, P, h["beta"], h["vi"], h["omegaP"], h["image"], trap, pair, prm,
+                             h["dt"], h["pbc"])
+    for sp, s in (("a/", a), ("b/", b)):
+        for k in ("x", "v", "theta", "vtheta"):
+            assert_close(getattr(s, k), fx[sp + "final/" + k], 1e-9, f"{name} {sp} final {k}")
+    assert_close([orc.pair_energy_2(a, Na, b, Nb, P, pair, prm)], fx["final/cross_e"], 1e-9, "final cross energy")
