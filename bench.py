@@ -517,6 +517,55 @@ def ensemble_form(lib, R, args):
                         "rs=2, Ewald alpha=5.6/L |n|<=8, dt=0.05; FP32 forces, FP64 recursion and NHC"}
 
 
+def two_species_form(lib, R, args, fp64_peak):
+    """Spin-unpolarised electron gas through md_pimd_calc_pair_force_2_x:
+    N/2 up + N/2 down electrons, P beads, the headline box and density
+    (rs=1), theta=0.5 of the unpolarised gas's Fermi temperature.  Each
+    species has its own exchange recursion and Ewald pairs, plus the cross
+    pairs (real space and structure factors); plain FP64, converged |n|<=10."""
+    import xmd_x
+    box, _ = workload()
+    T = THETA * 0.5 * (3 * math.pi ** 2 * N / box ** 3) ** (2 / 3)
+    Na = N // 2
+    lib.check(lib.md_gb300_set_precision_x(0))
+    xmd_x.set_potentials(lib, coul_s=1.0, alpha=ALPHA_L / box, nsum=NSUM)
+    lib.md_set_seed_x(77)
+    c = (C.c_double * 3)(box / 2, box / 2, box / 2)
+    Lv = (C.c_double * 3)(box, box, box)
+    pair_of = []
+    for _ in range(2):
+        s = xmd_x.PimdSystem(lib, Na, P, XI, T, box=box)
+        lib.md_init_particle_mass_x(s.sim, 1.0, 0, Na * P)
+        lib.md_pimd_init_particle_uniform_pos_x(s.pimd, c, Lv, 0.05 * RS)
+        lib.md_init_maxwell_vel_x(s.sim, T)
+        lib.md_init_nhc_x(s.sim, lib.md_get_quick_Q_x(T, s.pimd.contents.omegaP), 0, s.sim.contents.Nf, 0.0)
+        pair_of.append(s)
+    a, b = pair_of
+    pair = lib.fn("md_coulomb_3d_ewald_force_x")
+    step = lambda: xmd_x.two_species_step(lib, a, b, DT, image=1, pair=pair, pbc=True)  # noqa: E731
+    for _ in range(args.warmup):
+        step()
+    g, kps = R.capture(step)
+    ms, _, clocks = R.time([R.launcher(g)] * args.steps, [R.launcher(g)] * max(3, args.warmup))
+    lib.md_gb300_graph_free_x(g)
+    prof = R.profile(step)
+    out = {"value": N * P / (ms * 1e-3), "unit": "bead-steps/s", "ms_per_step": ms, "kernels_per_step": kps,
+           "clocks": clocks, "species": [Na, N - Na], "T": T,
+           "kernel_ms_per_step": {k: v[0] for k, v in prof.items()}}
+    if "pair_cross" in prof:
+        cross_ms, launches = prof["pair_cross"]
+        flops = P * Na * (N - Na) * (47.0 * n_images() + 39.0)
+        per = cross_ms / max(launches, 1)
+        achieved = flops / (per * 1e-3) / 1e12
+        out["cross_roofline"] = {"kernel": "pair_cross (Ewald real space, cross pairs)", "bound": "fp64",
+                                 "unit": "TFLOP/s", "launch_ms": per, "algorithmic_flop_per_launch": flops,
+                                 "achieved": achieved, "peak": fp64_peak,
+                                 "frac": achieved / fp64_peak if fp64_peak > 0 else None}
+    a.free()
+    b.free()
+    return out
+
+
 def run_gb300(args, dist, rank, ws):
     import torch
     import xmd_x
@@ -551,6 +600,9 @@ def run_gb300(args, dist, rank, ws):
                                "kernel_ms_per_step": {k: v[0] for k, v in plain_prof.items()},
                                "roofline": roofline(plain_prof, fp64_peak, "fp64")}
     fp32_peak = lib.md_gb300_fp32_peak_x()
+    if "two" in want:
+        forms["two_species_fp64"] = two_species_form(lib, R, args, lib.md_gb300_fp64_peak_x())
+        xmd_x.set_potentials(lib, coul_s=1.0, alpha=ALPHA_L / workload()[0], nsum=NSUM)
     if "mixed" in want:
         # mixed precision, converged Ewald
         import numpy as np
@@ -655,8 +707,8 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--cpu-budget", type=float, default=8.0, help="seconds of CPU sample")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--forms", default="plain,mixed,ensemble,learned",
-                    help="forms to run (comma list of plain, mixed, ensemble, learned)")
+    ap.add_argument("--forms", default="plain,two,mixed,ensemble,learned",
+                    help="forms to run (comma list of plain, two, mixed, ensemble, learned)")
     ap.add_argument("--learn-configs", type=int, default=3125,
                     help="configurations collected for training (x P bead slices)")
     ap.add_argument("--learn-steps", type=int, default=3000)

@@ -88,6 +88,15 @@ int md_pimd_calc_trap_energy_x(md_pimd_t_x *pimd, md_trap_energy_t_x te, md_stat
 int md_pimd_calc_pair_force_x(md_pimd_t_x *pimd, md_pair_force_t_x pf);
 int md_pimd_calc_pair_energy_x(md_pimd_t_x *pimd, md_pair_energy_t_x pe, md_stats_t_x *stats);
 
+/* two species with the same P, e.g. the two spins of an unpolarised
+   electron gas: md_pimd_x.h:146-147 (md_pimd_x.c:3282-3481, :3483-3632).
+   Cross pairs only (each species' own pairs come from
+   md_pimd_calc_pair_force_x), pimd's box; -1 when P differs, as in the
+   reference.  The Ewald callback needs both species in one box and equal
+   bead masses within each species.  FP64 in every precision mode. */
+int md_pimd_calc_pair_force_2_x(md_pimd_t_x *pimd, md_pimd_t_x *pimd2, md_pair_force_t_x pf);
+int md_pimd_calc_pair_energy_2_x(md_pimd_t_x *pimd, md_pimd_t_x *pimd2, md_pair_energy_t_x pe, md_stats_t_x *stats);
+
 /* virial estimator: md_pimd_x.h:157-162 */
 int md_pimd_fill_ENk2_x(md_pimd_t_x *pimd, int image);
 int md_pimd_fprint_ENk2_x(FILE *out, md_pimd_t_x *pimd);

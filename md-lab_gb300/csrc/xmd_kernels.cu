@@ -1728,6 +1728,100 @@ __global__ void k_pair_finish(Geo g, const double *__restrict__ part, int T, dou
   f[s] += acc * scale;
 }
 
+// ===================================================================
+// two species: md_pimd_calc_pair_force_2_x / _energy_2_x (md_pimd_x.c:
+// 3282-3632).  Every bead of species a meets every bead of species b in the
+// same slice.  A warp takes the rectangular tile (a-tile I, b-tile J) of one
+// slice; a's beads stay in the lanes and b's rotate through them with their
+// accumulated forces, as in k_pair_tiles but without the triangle.  The
+// reference's callback divides by a's mass and gives b -m_a F/(m_b P), so
+// a gains F/(m_a P) and b loses F/(m_b P).  Partials go per partner tile:
+//   outa[((J*P + j)*D + d)*Ns_a + l],  outb[((I*P + j)*D + d)*Ns_b + l]
+// ===================================================================
+template <int D, int KIND, bool ENERGY>
+__global__ void __launch_bounds__(256, 2) k_pair_cross(Geo ga, Geo gb, PairPrm p, const double *__restrict__ xa,
+                                                    const double *__restrict__ ma, const double *__restrict__ xb,
+                                                    const double *__restrict__ mb, double *__restrict__ outa,
+                                                    double *__restrict__ outb, int TA, int TB) {
+  __shared__ double stab[KIND == PAIR_EWALD_REAL ? 2 * EW_NINT * (EW_DEG + 1) : 1];
+  if (KIND == PAIR_EWALD_REAL) {
+    for (int i = threadIdx.x; i < 2 * EW_NINT * (EW_DEG + 1); i += blockDim.x)
+      stab[i] = i < EW_NINT * (EW_DEG + 1) ? (&c_ew_h[0][0])[i] : (&c_ew_erfc[0][0])[i - EW_NINT * (EW_DEG + 1)];
+    __syncthreads();
+  }
+  __shared__ EwWarp ewq[KIND == PAIR_EWALD_REAL ? 8 : 1];
+  EwWarp *ews = &ewq[KIND == PAIR_EWALD_REAL ? (threadIdx.x >> 5) : 0];
+  const int lane = threadIdx.x & 31;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  const int jobs = TA * TB;
+  for (int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; warp < jobs * ga.P; warp += nwarps) {
+    const int j = warp / jobs, job = warp % jobs;
+    const int I = job / TB, J = job % TB;
+    const int a = I * 32 + lane, b0 = J * 32 + lane;
+    const bool va = a < ga.N, vb = b0 < gb.N;
+    double xa_[D], xb_[D], fa[D], fb[D];
+    float xaf[D], xbf[D];
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      xa_[d] = va ? xa[sidx(j, d, a, D, ga.Ns)] : 0.0;
+      xb_[d] = vb ? xb[sidx(j, d, b0, D, gb.Ns)] : 0.0;
+      xaf[d] = (float)xa_[d];
+      xbf[d] = (float)xb_[d];
+      fa[d] = fb[d] = 0.0;
+    }
+    const double ima = (!ENERGY && va) ? 1.0 / ma[(size_t)j * ga.Ns + a] : 1.0;
+    double imb = (!ENERGY && vb) ? 1.0 / mb[(size_t)j * gb.Ns + b0] : 1.0;
+    double ea = 0;
+    for (int s = 0; s < 32; ++s) {
+      const int bi = J * 32 + ((lane + s) & 31);
+      const bool act = va && bi < gb.N;
+      double dx[D], F[D], E = 0;
+      float dxf[D];
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        dx[d] = xa_[d] - xb_[d];
+        dxf[d] = xaf[d] - xbf[d];
+        F[d] = 0;
+      }
+      if (KIND == PAIR_EWALD_REAL) pair_eval<D, KIND, ENERGY>(p, ga, dx, dxf, F, E, ENERGY, stab, act, ews, lane);
+      if (act) {
+        if (KIND != PAIR_EWALD_REAL)
+          pair_eval<D, KIND, ENERGY>(p, ga, dx, dxf, F, E, ENERGY, stab, true, nullptr, lane);
+        if (ENERGY) {
+          ea += E;
+        } else {
+#pragma unroll
+          for (int d = 0; d < D; ++d) {
+            fa[d] += F[d] * ima;
+            fb[d] -= F[d] * imb;
+          }
+        }
+      }
+      const int src = (lane + 1) & 31;
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        xb_[d] = __shfl_sync(FULL, xb_[d], src);
+        if (KIND == PAIR_EWALD_REAL) xbf[d] = __shfl_sync(FULL, xbf[d], src);
+        if (!ENERGY) fb[d] = __shfl_sync(FULL, fb[d], src);
+      }
+      if (!ENERGY) imb = __shfl_sync(FULL, imb, src);
+    }
+    if (ENERGY) {
+      ea = warp_sum(ea);
+      if (lane == 0) outa[warp] = ea;
+      continue;
+    }
+    if (va) {
+#pragma unroll
+      for (int d = 0; d < D; ++d) outa[(((size_t)J * ga.P + j) * D + d) * ga.Ns + a] = fa[d];
+    }
+    if (vb) {
+#pragma unroll
+      for (int d = 0; d < D; ++d) outb[(((size_t)I * gb.P + j) * D + d) * gb.Ns + b0] = fb[d];
+    }
+  }
+}
+
 size_t pair_scratch_doubles(const Geo &g) {
   const int T = (g.N + 31) / 32;
   const size_t jobs = (size_t)T * (T + 1) / 2;
@@ -1829,6 +1923,83 @@ cudaError_t pair_energy(const Geo &g, const PairPrm &p, const double *x, double 
     add = -p.qs * M_PI / (p.alpha * p.alpha * V) * ((double)g.N * (g.N - 1) / 2);
   }
   return reduce_into(scratch, jobs * g.P, 1.0 / g.P, add, acc, st);
+}
+
+size_t pair2_scratch_doubles(const Geo &ga, const Geo &gb) {
+  const int TA = (ga.N + 31) / 32, TB = (gb.N + 31) / 32;
+  const size_t forces = (size_t)TB * ga.slots() + (size_t)TA * gb.slots();
+  const size_t energy = (size_t)TA * TB * ga.P;
+  return forces > energy ? forces : energy;
+}
+
+template <int D, int KIND, bool ENERGY>
+static cudaError_t cross_launch(const Geo &ga, const Geo &gb, const PairPrm &p, const double *xa, const double *ma,
+                                const double *xb, const double *mb, double *outa, double *outb, int TA, int TB,
+                                cudaStream_t st) {
+  static int occ = 0, sms = 0;
+  const int grid = resident_grid(k_pair_cross<D, KIND, ENERGY>, (size_t)TA * TB * ga.P, occ, sms);
+  XK_PROF("pair_cross");
+  k_pair_cross<D, KIND, ENERGY><<<grid, 256, 0, st>>>(ga, gb, p, xa, ma, xb, mb, outa, outb, TA, TB);
+  return XK_LAUNCHED();
+}
+
+template <int D, bool ENERGY>
+static cudaError_t cross_dispatch(const Geo &ga, const Geo &gb, const PairPrm &p, const double *xa,
+                                  const double *ma, const double *xb, const double *mb, double *outa,
+                                  double *outb, int TA, int TB, cudaStream_t st) {
+  switch (p.kind) {
+    case PAIR_GAUSSIAN:
+      return cross_launch<D, PAIR_GAUSSIAN, ENERGY>(ga, gb, p, xa, ma, xb, mb, outa, outb, TA, TB, st);
+    case PAIR_PERIODIC_GAUSSIAN:
+      return cross_launch<D, PAIR_PERIODIC_GAUSSIAN, ENERGY>(ga, gb, p, xa, ma, xb, mb, outa, outb, TA, TB, st);
+    case PAIR_COULOMB:
+      return cross_launch<D, PAIR_COULOMB, ENERGY>(ga, gb, p, xa, ma, xb, mb, outa, outb, TA, TB, st);
+    case PAIR_PERIODIC_COULOMB:
+      return cross_launch<D, PAIR_PERIODIC_COULOMB, ENERGY>(ga, gb, p, xa, ma, xb, mb, outa, outb, TA, TB, st);
+    case PAIR_EWALD_REAL:
+      if (D != 3) return cudaErrorInvalidValue;
+      return cross_launch<D, PAIR_EWALD_REAL, ENERGY>(ga, gb, p, xa, ma, xb, mb, outa, outb, TA, TB, st);
+    default:
+      return cudaErrorInvalidValue;
+  }
+}
+
+cudaError_t pair_force_2(const Geo &ga, const Geo &gb, const PairPrm &p, const double *xa, const double *ma,
+                         const double *xb, const double *mb, double *fa, double *fb, double *scratch,
+                         cudaStream_t st) {
+  if (ga.D != gb.D || ga.P != gb.P) return cudaErrorInvalidValue;
+  const int TA = (ga.N + 31) / 32, TB = (gb.N + 31) / 32;
+  double *outa = scratch, *outb = scratch + (size_t)TB * ga.slots();
+  cudaError_t e;
+  DISPATCH_D(ga.D, e = (cross_dispatch<D, false>(ga, gb, p, xa, ma, xb, mb, outa, outb, TA, TB, st)));
+  if (e != cudaSuccess) return e;
+  {
+    XK_PROF("pair_finish");
+    k_pair_finish<<<cdiv(ga.slots(), 256), 256, 0, st>>>(ga, outa, TB, 1.0 / ga.P, fa);
+  }
+  e = XK_LAUNCHED();
+  if (e != cudaSuccess) return e;
+  {
+    XK_PROF("pair_finish");
+    k_pair_finish<<<cdiv(gb.slots(), 256), 256, 0, st>>>(gb, outb, TA, 1.0 / gb.P, fb);
+  }
+  return XK_LAUNCHED();
+}
+
+cudaError_t pair_energy_2(const Geo &ga, const Geo &gb, const PairPrm &p, const double *xa, const double *xb,
+                          double *acc, double *scratch, cudaStream_t st) {
+  if (ga.D != gb.D || ga.P != gb.P) return cudaErrorInvalidValue;
+  const int TA = (ga.N + 31) / 32, TB = (gb.N + 31) / 32;
+  cudaError_t e;
+  DISPATCH_D(ga.D, e = (cross_dispatch<D, true>(ga, gb, p, xa, nullptr, xb, nullptr, scratch, nullptr, TA, TB, st)));
+  if (e != cudaSuccess) return e;
+  // -pi/(alpha^2 V) per pair of the Ewald energy (md_statistics_x.c:385)
+  double add = 0;
+  if (p.kind == PAIR_EWALD_REAL) {
+    const double V = ga.box[0] * ga.box[1] * ga.box[2];
+    add = -p.qs * M_PI / (p.alpha * p.alpha * V) * ((double)ga.N * gb.N);
+  }
+  return reduce_into(scratch, TA * TB * ga.P, 1.0 / ga.P, add, acc, st);
 }
 
 // ===================================================================
@@ -2201,6 +2372,89 @@ cudaError_t recip_energy(const Geo &g, const Recip &r, const double *x, double *
   e = XK_LAUNCHED();
   if (e != cudaSuccess) return e;
   return reduce_into(scratch, g.P, 1.0 / g.P, 0.0, acc, st);
+}
+
+// Two species (md_pimd_calc_pair_force_2_x with the Ewald callback): the
+// reciprocal part of the cross pairs, regrouped like the one-species sums,
+//   F_a = 4 pi/(m_a P) sum_{n in H} (n/L) c(n) Im(e^{i theta_a} S_b(n)*)
+// and the same with a and b exchanged; there is no l = l2 term to drop.  The
+// cross energy of slice j is sum_{n in H} 2 c(n) Re(S_a,j(n) S_b,j(n)*).
+// Each species keeps its own phases, structure factors and tables (T from
+// its own S); a's forces read b's tables and b's read a's.
+static cudaError_t recip_tables_of(const Geo &g, const Recip &r, cudaStream_t st) {
+  const int nc = ncols(r.nsum);
+  dim3 tgrid((nc + 7) / 8, g.P), tblk(r.nsum + 1, 8);
+  DISPATCH_NS(r.nsum, {
+    XK_PROF("recip_tables");
+    k_recip_tables<NS><<<tgrid, tblk, 0, st>>>((const int4 *)r.kvec, nc, (const double2 *)r.S, r.coef, r.nk,
+                                               (double2 *)r.T);
+  });
+  return XK_LAUNCHED();
+}
+
+static cudaError_t recip_force_from(const Geo &g, const Recip &own, const double *T_other, double scale, double *f,
+                                    cudaStream_t st) {
+  const int nc = ncols(own.nsum);
+  const size_t smem = sizeof(double2) * nc * (4 * own.nsum + 1);
+  dim3 grid((g.N + 127) / 128, g.P);
+  DISPATCH_NS(own.nsum, {
+    auto kf = k_recip_force<NS>;
+    static bool opted = false;
+    if (!opted) {
+      cudaError_t ea = cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+      if (ea != cudaSuccess) return ea;
+      opted = true;
+    }
+    XK_PROF("recip_force");
+    kf<<<grid, 128, smem, st>>>(g, (const double2 *)own.phase, (const int4 *)own.kvec, nc, (const double2 *)T_other,
+                                scale, f, nullptr, 0.0);
+  });
+  return XK_LAUNCHED();
+}
+
+static bool recip_pair_ok(const Geo &ga, const Recip &ra, const Geo &gb, const Recip &rb) {
+  return ga.D == 3 && gb.D == 3 && ga.P == gb.P && ra.nsum == rb.nsum && ra.nk == rb.nk;
+}
+
+cudaError_t recip_force_2(const Geo &ga, const Recip &ra, const double *xa, double inv_mPa, double *fa,
+                          const Geo &gb, const Recip &rb, const double *xb, double inv_mPb, double *fb,
+                          cudaStream_t st) {
+  if (!recip_pair_ok(ga, ra, gb, rb)) return cudaErrorInvalidValue;
+  cudaError_t e = structure_factors(ga, ra, xa, st);
+  if (e == cudaSuccess) e = structure_factors(gb, rb, xb, st);
+  if (e == cudaSuccess) e = recip_tables_of(ga, ra, st);
+  if (e == cudaSuccess) e = recip_tables_of(gb, rb, st);
+  if (e == cudaSuccess) e = recip_force_from(ga, ra, rb.T, 4 * M_PI * inv_mPa, fa, st);
+  if (e == cudaSuccess) e = recip_force_from(gb, rb, ra.T, 4 * M_PI * inv_mPb, fb, st);
+  return e;
+}
+
+__global__ void k_recip_energy_2(const double2 *__restrict__ Sa, const double2 *__restrict__ Sb,
+                                 const double *__restrict__ coef, int nk, double *part) {
+  __shared__ double buf[33];
+  const int j = blockIdx.x;
+  double e = 0;
+  for (int k = threadIdx.x; k < nk; k += blockDim.x) {
+    const double2 a = Sa[(size_t)j * nk + k], b = Sb[(size_t)j * nk + k];
+    e += 2 * coef[k] * (a.x * b.x + a.y * b.y);
+  }
+  e = block_sum(e, buf);
+  if (threadIdx.x == 0) part[j] = e;
+}
+
+cudaError_t recip_energy_2(const Geo &ga, const Recip &ra, const double *xa, const Geo &gb, const Recip &rb,
+                           const double *xb, double *acc, double *scratch, cudaStream_t st) {
+  if (!recip_pair_ok(ga, ra, gb, rb)) return cudaErrorInvalidValue;
+  cudaError_t e = structure_factors(ga, ra, xa, st);
+  if (e == cudaSuccess) e = structure_factors(gb, rb, xb, st);
+  if (e != cudaSuccess) return e;
+  {
+    XK_PROF("recip_energy");
+    k_recip_energy_2<<<ga.P, 256, 0, st>>>((const double2 *)ra.S, (const double2 *)rb.S, ra.coef, ra.nk, scratch);
+  }
+  e = XK_LAUNCHED();
+  if (e != cudaSuccess) return e;
+  return reduce_into(scratch, ga.P, 1.0 / ga.P, 0.0, acc, st);
 }
 
 // ===================================================================

@@ -164,6 +164,18 @@ size_t pair_force_noalloc_need(const Geo &g);
 cudaError_t pair_force_noalloc(const Geo &g, const PairPrm &p, const double *x, const double *m,
                                double *f, cudaStream_t st);
 
+// two species with the same P and box (md_pimd_x.c:3282-3632): cross pairs
+// only, every bead of species a with every bead of species b in its slice;
+// f_a += F/(m_a P), f_b -= F/(m_b P), with a's box.  scratch: at least
+// pair2_scratch_doubles(ga, gb) doubles.
+size_t pair2_scratch_doubles(const Geo &ga, const Geo &gb);
+cudaError_t pair_force_2(const Geo &ga, const Geo &gb, const PairPrm &p, const double *xa, const double *ma,
+                         const double *xb, const double *mb, double *fa, double *fb, double *scratch,
+                         cudaStream_t st);
+// sum over slices and cross pairs of V/P (plus -pi/(alpha^2 V) per pair for Ewald), added to *acc
+cudaError_t pair_energy_2(const Geo &ga, const Geo &gb, const PairPrm &p, const double *xa, const double *xb,
+                          double *acc, double *scratch, cudaStream_t st);
+
 // Ewald reciprocal space through structure factors (D = 3)
 struct Recip {
   int nsum;
@@ -184,6 +196,15 @@ cudaError_t recip_force(const Geo &g, const Recip &r, const double *x, double in
                         double *f, cudaStream_t st);
 cudaError_t recip_energy(const Geo &g, const Recip &r, const double *x, double *acc,
                          double *scratch, cudaStream_t st);
+
+// two species (same P, box and Ewald parameters): a's forces from b's
+// structure factors and b's from a's (both Recip's phase, S and T are
+// rewritten); the cross energy sum_j sum_{n in H} 2 c(n) Re(S_a S_b*) / P
+cudaError_t recip_force_2(const Geo &ga, const Recip &ra, const double *xa, double inv_mPa, double *fa,
+                          const Geo &gb, const Recip &rb, const double *xb, double inv_mPb, double *fb,
+                          cudaStream_t st);
+cudaError_t recip_energy_2(const Geo &ga, const Recip &ra, const double *xa, const Geo &gb, const Recip &rb,
+                           const double *xb, double *acc, double *scratch, cudaStream_t st);
 
 // reciprocal-space forces plus per-particle energies
 //   e[j*Ns + l] = sum_k c(k) (Re(e^{i k x_l} conj S_j(k)) - 1)  (half space)

@@ -462,6 +462,88 @@ int md_pimd_calc_pair_force_x(md_pimd_t_x *pimd, md_pair_force_t_x pf) {
   return 0;
 }
 
+// Two species (md_pimd_x.c:3282-3481, :3483-3632): the cross pairs between
+// pimd and pimd2, with pimd's box.  Both species stay on the device; the
+// cross call adds to both f arrays only (NoJoin, like the one-species call).
+// The Ewald callback needs both species in one box (the reciprocal sums use
+// each species' structure factors with one set of coefficients) and equal
+// bead masses within each species.  Always FP64, in every precision mode.
+static int two_species(md_pimd_t_x *pimd, md_pimd_t_x *pimd2, int kind, SimDev **sa, PimdDev **pa, SimDev **sb,
+                       PimdDev **pb) {
+  XMD_TRY(pimd_device(pimd, sa, pa));
+  XMD_TRY(pimd_device(pimd2, sb, pb));
+  if (kind == xk::PAIR_PERIODIC_GAUSSIAN || kind == xk::PAIR_PERIODIC_COULOMB || kind == xk::PAIR_EWALD_REAL)
+    XMD_TRY(check_image(*sa, 1));
+  if (kind == xk::PAIR_EWALD_REAL) {
+    for (int d = 0; d < 3; ++d)
+      if ((*sa)->geo.box[d] != (*sb)->geo.box[d])
+        return fail(MD_GB_ERR_UNSUPPORTED, "Ewald between species in different boxes");
+    xk::PairPrm prm = pair_params(kind);
+    ewald_shifts(prm, (*sa)->geo);
+    if (prm.kmax[0] > 1 || prm.kmax[1] > 1 || prm.kmax[2] > 1)
+      return fail(MD_GB_ERR_UNSUPPORTED, "Ewald alpha*L below %.1f (images beyond the neighbouring boxes)",
+                  2 * EWALD_XCUT / 3);
+    XMD_TRY(ewald_tables(pimd, *sa, *pa));
+    XMD_TRY(ewald_tables(pimd2, *sb, *pb));
+  }
+  return 0;
+}
+
+int md_pimd_calc_pair_force_2_x(md_pimd_t_x *pimd, md_pimd_t_x *pimd2, md_pair_force_t_x pf) {
+  if (!pimd || !pimd2) return fail(MD_GB_ERR_ARG, "NULL simulation");
+  if (pimd->P != pimd2->P) return -1;  // md_pimd_x.c:3283-3284
+  NoJoin nj;
+  const int kind = pair_kind_of((const void *)pf, false);
+  if (!kind) return fail(MD_GB_ERR_UNSUPPORTED, "pair force function has no device kernel");
+  if (kind == xk::PAIR_EWALD_REAL && D != 3) return 0;  // the reference's Ewald is 3D only
+  SimDev *sa, *sb;
+  PimdDev *pa, *pb;
+  XMD_TRY(two_species(pimd, pimd2, kind, &sa, &pa, &sb, &pb));
+  int rc;
+  double *scr = scratch_for(sa, xk::pair2_scratch_doubles(sa->geo, sb->geo), &rc);
+  if (rc) return rc;
+  cudaStream_t st = stream();
+  xk::PairPrm prm = pair_params(kind);
+  ewald_shifts(prm, sa->geo);
+  if (kind == xk::PAIR_EWALD_REAL) {
+    if (!sa->uniform_mass || !sb->uniform_mass)
+      return fail(MD_GB_ERR_UNSUPPORTED, "structure-factor Ewald needs equal bead masses within each species");
+    XMD_CUDA(xk::recip_force_2(sa->geo, recip_of(pa), sa->x.as<double>(), 1.0 / (sa->mass0 * pimd->P),
+                               sa->f.as<double>(), sb->geo, recip_of(pb), sb->x.as<double>(),
+                               1.0 / (sb->mass0 * pimd2->P), sb->f.as<double>(), st));
+  }
+  XMD_CUDA(xk::pair_force_2(sa->geo, sb->geo, prm, sa->x.as<double>(), sa->m.as<double>(), sb->x.as<double>(),
+                            sb->m.as<double>(), sa->f.as<double>(), sb->f.as<double>(), scr, st));
+  return 0;
+}
+
+int md_pimd_calc_pair_energy_2_x(md_pimd_t_x *pimd, md_pimd_t_x *pimd2, md_pair_energy_t_x pe,
+                                 md_stats_t_x *stats) {
+  if (!pimd || !pimd2) return fail(MD_GB_ERR_ARG, "NULL simulation");
+  if (pimd->P != pimd2->P) return -1;  // md_pimd_x.c:3484-3485
+  const int kind = pair_kind_of((const void *)pe, true);
+  if (!kind) return fail(MD_GB_ERR_UNSUPPORTED, "pair energy function has no device kernel");
+  if (kind == xk::PAIR_EWALD_REAL && D != 3) return 0;
+  SimDev *sa, *sb;
+  PimdDev *pa, *pb;
+  double *acc;
+  XMD_TRY(two_species(pimd, pimd2, kind, &sa, &pa, &sb, &pb));
+  XMD_TRY(stats_device(stats, &acc));
+  int rc;
+  size_t need = xk::pair2_scratch_doubles(sa->geo, sb->geo);
+  if (need < (size_t)pimd->P) need = pimd->P;
+  double *scr = scratch_for(sa, need, &rc);
+  if (rc) return rc;
+  cudaStream_t st = stream();
+  if (kind == xk::PAIR_EWALD_REAL)
+    XMD_CUDA(xk::recip_energy_2(sa->geo, recip_of(pa), sa->x.as<double>(), sb->geo, recip_of(pb),
+                                sb->x.as<double>(), acc, scr, st));
+  xk::PairPrm prm = pair_params(kind);
+  ewald_shifts(prm, sa->geo);
+  XMD_CUDA(xk::pair_energy_2(sa->geo, sb->geo, prm, sa->x.as<double>(), sb->x.as<double>(), acc, scr, st));
+  return 0;
+}
+
 int md_gb300_set_pair_tile_x(md_pair_force_t_x pf, int N, int P, int warps) {
   const int kind = pair_kind_of((const void *)pf, false);
   if (!kind) return fail(MD_GB_ERR_UNSUPPORTED, "pair force function has no device kernel");

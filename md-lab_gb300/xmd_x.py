@@ -121,6 +121,8 @@ class XLib:
             "md_pimd_calc_vi_virial_energy_x": (_i, [pp, pst, _i]),
             "md_pimd_calc_trap_energy_x": (_i, [pp, _vp, pst]),
             "md_pimd_calc_pair_energy_x": (_i, [pp, _vp, pst]),
+            "md_pimd_calc_pair_force_2_x": (_i, [pp, pp, _vp]),
+            "md_pimd_calc_pair_energy_2_x": (_i, [pp, pp, _vp, pst]),
             "md_pimd_calc_vi_sign_x": (_i, [pp, pst, pst, _d]),
             "md_calc_3d_ueg_madelung_x": (_d, [_dp]),
             "md_set_harmonic_trap_frequency_x": (None, [_d]),
@@ -347,6 +349,37 @@ def md_step(lib, s, dt, image=0, trap=None, pair=None, pbc=False):
     ck(lib.md_update_nhc_VV3_2_x(s.sim, dt), "VV3_2")
     if pbc:
         ck(lib.md_periodic_boundary_x(s.sim), "periodic boundary")
+    return 0
+
+
+def two_species_forces(lib, a, b, image=0, trap=None, pair=None):
+    """Forces of two species (same P) in the reference driver's call order:
+    each species' exchange, trap and pair forces, then the cross pairs
+    (md_pimd_calc_pair_force_2_x)."""
+    ck = lib.check
+    for s in (a, b):
+        ck(lib.md_reset_force_x(s.sim), "reset_force")
+        ck(lib.md_pimd_fast_fill_ENk_x(s.pimd, image), "fast_fill_ENk")
+        ck(lib.md_pimd_fill_VB_x(s.pimd), "fill_VB")
+        ck(lib.md_pimd_fast_fill_force_VB_x(s.pimd, image), "fast_fill_force_VB")
+        if trap:
+            ck(lib.md_pimd_calc_trap_force_x(s.pimd, trap), "trap force")
+        if pair:
+            ck(lib.md_pimd_calc_pair_force_x(s.pimd, pair), "pair force")
+    if pair:
+        ck(lib.md_pimd_calc_pair_force_2_x(a.pimd, b.pimd, pair), "cross-species pair force")
+
+
+def two_species_step(lib, a, b, dt, image=0, trap=None, pair=None, pbc=False):
+    """One MD step of two species; returns 0 or raises."""
+    ck = lib.check
+    for s in (a, b):
+        ck(lib.md_update_nhc_VV3_1_x(s.sim, dt), "VV3_1")
+    two_species_forces(lib, a, b, image, trap, pair)
+    for s in (a, b):
+        ck(lib.md_update_nhc_VV3_2_x(s.sim, dt), "VV3_2")
+        if pbc:
+            ck(lib.md_periodic_boundary_x(s.sim), "periodic boundary")
     return 0
 
 
