@@ -203,10 +203,12 @@ def cpu_step_estimate(cores, budget_s):
 # ---------------------------------------------------------------------
 # GB300 arm
 # ---------------------------------------------------------------------
-def n_images():
+def n_images(xcut=5.8):
+    """expected real-space images per pair inside the cut-off alpha R < xcut
+    (5.8 in the FP64 kernels, 4.6 in the FP32 ones)"""
     box, _ = workload()
-    rc = 5.8 / (ALPHA_L / box)
-    return 4 / 3 * math.pi * rc ** 3 / box ** 3  # expected images inside the cut-off per pair
+    rc = xcut / (ALPHA_L / box)
+    return 4 / 3 * math.pi * rc ** 3 / box ** 3
 
 
 # algorithmic work per launch of each kernel (FMA = 2 flops); the same count
@@ -218,9 +220,12 @@ def kernel_flops(name, nsum=NSUM):
         return 177.0 * ncol * N * P * nsum / NSUM
     if name in ("sk", "sk32"):
         return 88.0 * ncol * N * P * nsum / NSUM
-    if name in ("pair_tiles_ewald_real", "pair_tiles32_ewald_real"):
+    if name == "pair_tiles_ewald_real":
         pairs = P * N * (N - 1) / 2
         return pairs * (47.0 * n_images() + 39.0)
+    if name == "pair_tiles32_ewald_real":
+        pairs = P * N * (N - 1) / 2
+        return pairs * (47.0 * n_images(4.6) + 39.0)
     if name == "desc":
         # per ordered pair: 12 flop for the minimum-image distance, and for the
         # (4/3) pi (1/2)^3 = 52% inside rc = L/2 another 45 (cut-off weight,
@@ -623,7 +628,8 @@ def run_gb300(args, dist, rank, ws):
                                       "kernel_ms_per_step": {k: v[0] for k, v in mixed_prof.items()}}
     if "ensemble" in want:
         forms["ensemble_64"] = ensemble_form(lib, R, args)
-    headline = "plain_fp64" if "plain" in want else "mixed_fp32_forces"
+    headline = next((k for k in ("plain_fp64", "mixed_fp32_forces", "two_species_fp64", "ensemble_64")
+                     if k in forms), None)
     model = None
     if "learned" in want:
         model, lform, lprof, lkps = learned_form(lib, R, s, pair, step, args, ws)

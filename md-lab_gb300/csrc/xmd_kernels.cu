@@ -728,13 +728,6 @@ cudaError_t fill_enk2(const Geo &g, const double *x, const double *m, double w2,
 // exchange recursions (single persistent block each)
 // ===================================================================
 
-static int rec_threads(int N) {
-  int t = ((N + 31) / 32) * 32;
-  if (t < 64) t = 64;
-  if (t > 1024) t = 1024;
-  return t;
-}
-
 // ---- linear-solve form ----------------------------------------------
 // With Z_n = exp(-beta V_n) the forward recursion is linear:
 //   Z_0 = 1,  Z_n = sum_{k=1..n} M_{n,n-k} Z_{n-k},
@@ -1633,8 +1626,10 @@ __global__ void __launch_bounds__(256, 2) k_pair_tiles(Geo g, PairPrm p,
   const int lane = threadIdx.x & 31;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   // warps loop over the tile jobs (slice j, tile pair I <= J) round-robin, so
-  // that a grid of resident blocks (pair_launch) stages the tables once
-  for (int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; warp < jobs * g.P; warp += nwarps) {
+  // that a grid of resident blocks (pair_launch) stages the tables once.  The
+  // warps are numbered across blocks first: the jobs of the last, partial
+  // round spread over all blocks (and SMs) instead of filling the first ones.
+  for (int warp = (threadIdx.x >> 5) * gridDim.x + blockIdx.x; warp < jobs * g.P; warp += nwarps) {
     const int j = warp / jobs;
     int job = warp % jobs, I = 0;
     while (job >= T - I) {
@@ -1754,7 +1749,8 @@ __global__ void __launch_bounds__(256, 2) k_pair_cross(Geo ga, Geo gb, PairPrm p
   const int lane = threadIdx.x & 31;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   const int jobs = TA * TB;
-  for (int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; warp < jobs * ga.P; warp += nwarps) {
+  // warps numbered across blocks first, as in k_pair_tiles
+  for (int warp = (threadIdx.x >> 5) * gridDim.x + blockIdx.x; warp < jobs * ga.P; warp += nwarps) {
     const int j = warp / jobs, job = warp % jobs;
     const int I = job / TB, J = job % TB;
     const int a = I * 32 + lane, b0 = J * 32 + lane;
@@ -2498,54 +2494,157 @@ cudaError_t sk_structure(const Geo &g, const double *x, int ja, int jb, const do
 // estimators
 // ===================================================================
 
-// primitive (md_pimd_x.c:1267-1293) and, with ENk2, virial
-// (md_pimd_x.c:4288-4322) exchange recursions; adds res[N] + add to *acc
-__global__ void k_vbn_energy(int N, double beta, double vi, double add,
-                             const double *__restrict__ ENk, const double *__restrict__ VBN,
-                             const double *__restrict__ ENk2, double *acc) {
-  extern __shared__ double sh[];
-  double *res = sh;            // N+1
-  double *bmin = sh + N + 1;   // 33
-  double *bs1 = bmin + 33;     // 33
-  double *bs2 = bs1 + 33;      // 33
-  const double lnvi = vi != 0.0 ? log(vi) : 0.0;
-  const double *E2 = ENk2 ? ENk2 : ENk;
-  if (threadIdx.x == 0) res[0] = 0;
-  __syncthreads();
-  for (int n = 1; n <= N; ++n) {
-    const double *row = ENk + dtri(n), *row2 = E2 + dtri(n);
-    double mloc = 1e10;
-    if (vi == 0.0) {
-      mloc = beta * (row[0] + VBN[n - 1]);
-    } else {
-      for (int k = threadIdx.x + 1; k <= n; k += blockDim.x) {
-        const double t = -(k - 1) * lnvi + beta * (row[k - 1] + VBN[n - k]);
-        if (t < mloc) mloc = t;
-      }
-      mloc = block_min(mloc, 1e10, bmin);
-    }
-    double s1 = 0, s2 = 0;
-    for (int k = threadIdx.x + 1; k <= n; k += blockDim.x) {
-      if (vi == 0.0 && k != 1) continue;
-      const double E = row[k - 1] + VBN[n - k];
-      const double w = (vi == 0.0) ? exp(-beta * E + mloc) : exp((k - 1) * lnvi - beta * E + mloc);
-      s1 += w;
-      s2 += (res[n - k] - row2[k - 1]) * w;
-    }
-    s1 = block_sum(s1, bs1);
-    s2 = block_sum(s2, bs2);
-    if (threadIdx.x == 0) res[n] = s2 / s1;
-    __syncthreads();
+// Primitive (md_pimd_x.c:1267-1293) and, with ENk2, virial
+// (md_pimd_x.c:4288-4322) exchange estimators.  The reference's recursion
+//   res[n] = sum_k (res[n-k] - E2[n][k]) w_{n,k} / sum_k w_{n,k},
+//   w_{n,k} = exp((k-1) ln xi - beta (ENk[n][k] + VBN[n-k]) + m_n)
+// is a unit lower-triangular system res = p res + c in the normalised
+// weights p_{n,n-k} = w_{n,k} / sum_k w_{n,k} and c_n = -sum_k p_{n,n-k}
+// E2[n][k].  The weights need only ENk and VBN, so they are computed for all
+// rows at once (a warp per row); the solve then takes the chunked scheme of
+// k_tri_solve in plain FP64 (the normalised weights are at most 1 and res
+// is an energy: no extended range is needed).
+__global__ void k_est_weights(int N, double beta, double vi, const double *__restrict__ ENk,
+                              const double *__restrict__ VBN, const double *__restrict__ E2, double *__restrict__ Pw,
+                              double *__restrict__ cvec) {
+  const int lane = threadIdx.x & 31;
+  const int n = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) + 1;
+  if (n > N) return;
+  const double *row = ENk + dtri(n), *row2 = E2 + dtri(n);
+  double *prow = Pw + moff(n, 0);
+  if (vi == 0.0) {
+    // only k = 1 carries weight (md_pimd_x.c:1280): p = 1, the rest 0
+    for (int j = lane; j < n; j += 32) prow[j] = j == n - 1 ? 1.0 : 0.0;
+    if (lane == 0) cvec[n] = -row2[0];
+    return;
   }
-  if (threadIdx.x == 0) *acc += res[N] + add;
+  const double lnvi = log(vi);
+  double mloc = 1e10;
+  for (int k = lane + 1; k <= n; k += 32) {
+    const double t = -(k - 1) * lnvi + beta * (row[k - 1] + VBN[n - k]);
+    mloc = t < mloc ? t : mloc;
+  }
+#pragma unroll
+  for (int o = 16; o; o >>= 1) {
+    const double t = __shfl_xor_sync(FULL, mloc, o);
+    mloc = t < mloc ? t : mloc;
+  }
+  double s1 = 0.0;
+  for (int k = lane + 1; k <= n; k += 32)
+    s1 += exp((k - 1) * lnvi - beta * (row[k - 1] + VBN[n - k]) + mloc);
+  s1 = warp_sum(s1);
+  const double inv = 1.0 / s1;
+  double cs = 0.0;
+  for (int k = lane + 1; k <= n; k += 32) {
+    const double pk = exp((k - 1) * lnvi - beta * (row[k - 1] + VBN[n - k]) + mloc) * inv;
+    prow[n - k] = pk;
+    cs = fma(-pk, row2[k - 1], cs);
+  }
+  cs = warp_sum(cs);
+  if (lane == 0) cvec[n] = cs;
 }
 
-cudaError_t vbn_energy(int N, double beta, double vi, double add, const double *ENk,
-                       const double *VBN, const double *ENk2, double *acc, cudaStream_t st) {
-  const size_t smem = sizeof(double) * (N + 1 + 99);
+// x_0 = 0, x_i = c_i + sum_{j<i} Pw[moff(i, j)] x_j; adds x_N + add to *acc.
+// Chunks of TS_CHUNK rows are substituted in order by warp 0 (one FMA and
+// one shuffle per step on the sequential path) while the other warps stage
+// the next chunk's weights in shared memory and sum its rows over all
+// columns solved before the current chunk.
+__global__ void __launch_bounds__(TS_WARPS * 32) k_lin_solve(int N, const double *__restrict__ Pw,
+                                                             const double *__restrict__ cvec, double add,
+                                                             double *acc) {
+  extern __shared__ double sh[];
+  double *W = sh;                              // [2][TS_CHUNK][TS_LD] the chunk's triangle
+  double *U = W + 2 * TS_CHUNK * TS_LD;        // [2][TS_CHUNK][TS_LD] previous chunk's columns
+  double *Ps = U + 2 * TS_CHUNK * TS_LD;       // [2][TS_CHUNK] partial sums (double buffer)
+  double *X = Ps + 2 * TS_CHUNK;               // N+1
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  auto stage = [&](int n0, int c0, int nb, int t0, int stride) {
+    for (int q = t0; q < 2 * TS_CHUNK * TS_CHUNK; q += stride) {
+      const int which = q / (TS_CHUNK * TS_CHUNK), rs = q % (TS_CHUNK * TS_CHUNK);
+      const int r = rs / TS_CHUNK, c = rs % TS_CHUNK, i = n0 + r;
+      const size_t o = ((size_t)nb * TS_CHUNK + r) * TS_LD + c;
+      if (which == 0)
+        W[o] = (i <= N && c < r) ? Pw[moff(i, n0 + c)] : 0.0;
+      else
+        U[o] = (i <= N && c0 >= 0) ? Pw[moff(i, c0 + c)] : 0.0;
+    }
+  };
+  if (threadIdx.x == 0) X[0] = 0.0;
+  stage(1, -1, 0, threadIdx.x, blockDim.x);
+  // chunk 0: column 0 holds x_0 = 0, so its rows start from c
+  for (int r = threadIdx.x; r < TS_CHUNK; r += blockDim.x) Ps[r] = 1 + r <= N ? cvec[1 + r] : 0.0;
+  __syncthreads();
+  for (int i0 = 1, c = 0; i0 <= N; i0 += TS_CHUNK, ++c) {
+    const int buf = c & 1;
+    double *Psc = Ps + buf * TS_CHUNK;
+    if (c > 0) {
+      const int col = i0 - TS_CHUNK + lane;
+      for (int r = w; r < TS_CHUNK; r += TS_WARPS) {
+        if (i0 + r > N) continue;  // warp-uniform
+        double v = U[((size_t)buf * TS_CHUNK + r) * TS_LD + lane] * X[col];
+        v = warp_sum(v);
+        if (lane == 0) Psc[r] += v;
+      }
+      __syncthreads();
+    }
+    if (w == 0) {
+      const int i = i0 + lane;
+      const bool own = i <= N;
+      double a = own ? Psc[lane] : 0.0;
+      double mm[TS_CHUNK];
+      const size_t ro = ((size_t)buf * TS_CHUNK + lane) * TS_LD;
+#pragma unroll
+      for (int s2 = 0; s2 < TS_CHUNK; ++s2) mm[s2] = W[ro + s2];
+#pragma unroll
+      for (int s2 = 0; s2 < TS_CHUNK; ++s2) {
+        if (lane == s2 && own) X[i] = a;
+        const double xs = __shfl_sync(FULL, a, s2);
+        a = lane > s2 ? fma(mm[s2], xs, a) : a;
+      }
+    } else {
+      const int n0 = i0 + TS_CHUNK;
+      if (n0 <= N) stage(n0, i0, buf ^ 1, threadIdx.x - 32, blockDim.x - 32);
+      for (int r = w - 1; r < TS_CHUNK; r += TS_WARPS - 1) {
+        const int i = n0 + r;
+        if (i > N) break;  // warp-uniform; later rows are out of range too
+        const double *prow = Pw + moff(i, 0);
+        double v0 = 0.0, v1 = 0.0;
+        int j = lane;
+        for (; j + 32 < i0; j += 64) {
+          v0 = fma(prow[j], X[j], v0);
+          v1 = fma(prow[j + 32], X[j + 32], v1);
+        }
+        if (j < i0) v0 = fma(prow[j], X[j], v0);
+        const double v = warp_sum(v0 + v1);
+        if (lane == 0) Ps[(buf ^ 1) * TS_CHUNK + r] = cvec[i] + v;
+      }
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *acc += X[N] + add;
+}
+
+size_t vbn_scratch_doubles(int N) { return ntri(N) + N + 2; }
+
+cudaError_t vbn_energy(int N, double beta, double vi, double add, const double *ENk, const double *VBN,
+                       const double *ENk2, double *acc, double *scratch, cudaStream_t st) {
+  double *Pw = scratch, *cvec = scratch + ntri(N) + 1;
   {
-    XK_PROF("vbn_energy");
-    k_vbn_energy<<<1, rec_threads(N), smem, st>>>(N, beta, vi, add, ENk, VBN, ENk2, acc);
+    XK_PROF("est_weights");
+    k_est_weights<<<cdiv((size_t)N * 32, 256), 256, 0, st>>>(N, beta, vi, ENk, VBN, ENk2 ? ENk2 : ENk, Pw, cvec);
+  }
+  cudaError_t e = XK_LAUNCHED();
+  if (e != cudaSuccess) return e;
+  const size_t smem = sizeof(double) * (N + 1 + 2 * TS_CHUNK + 4 * TS_CHUNK * TS_LD);
+  static bool opted = false;
+  if (!opted) {
+    e = cudaFuncSetAttribute(k_lin_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    if (e != cudaSuccess) return e;
+    opted = true;
+  }
+  {
+    XK_PROF("est_solve");
+    k_lin_solve<<<1, TS_WARPS * 32, smem, st>>>(N, Pw, cvec, add, acc);
   }
   return XK_LAUNCHED();
 }
@@ -2837,6 +2936,8 @@ struct P32 {
   float alpha, rc2;  // Ewald: splitting, FP32 cut-off squared
   int kmax;          // Ewald: 0 = 8-image search, else |k_d| <= kmax
   int nsum;          // Ewald: the reference's image cube |n_d| <= nsum
+  int uniform;       // all beads of the system have one mass (1/m = im0)
+  float im0;
 };
 
 template <int D, int KIND>
@@ -2881,23 +2982,37 @@ __device__ inline void pair_eval32(const P32 &q, const float *dx, float *F) {
     const float ns = (float)q.nsum;
     float F0 = 0.f, F1 = 0.f, F2 = 0.f;
     if (q.kmax == 0) {
+      // With a_d = |m_d| the shifted component has length L_d - a_d, so an
+      // image's squared distance is |m|^2 plus dl_d = L_d (L_d - 2 a_d) for
+      // each shifted axis: the 8 candidates are tested with a few adds.  The
+      // accepted ones (2.3 per pair on average at alpha L = 5.6) are then
+      // evaluated lowest bit first, so the warp runs as many rounds as its
+      // busiest lane has images instead of one round per candidate.
+      const float R0 = fmaf(m[2], m[2], fmaf(m[1], m[1], m[0] * m[0]));
+      float dl[3];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) dl[d] = q.L[d] * fmaf(-2.f, fabsf(m[d]), q.L[d]);
+      unsigned mask = 0u;
 #pragma unroll
       for (int c = 0; c < 8; ++c) {
-        const int k0 = c & 1, k1 = (c >> 1) & 1, k2 = c >> 2;
-        const float t0 = k0 ? fmaf(-sg[0], q.L[0], m[0]) : m[0];
-        const float t1 = k1 ? fmaf(-sg[1], q.L[1], m[1]) : m[1];
-        const float t2 = k2 ? fmaf(-sg[2], q.L[2], m[2]) : m[2];
-        const float R2 = fmaf(t2, t2, fmaf(t1, t1, t0 * t0));
+        const float R2 = R0 + ((c & 1) ? dl[0] : 0.f) + ((c & 2) ? dl[1] : 0.f) + ((c & 4) ? dl[2] : 0.f);
         bool ok = R2 < q.rc2;
         if (q.nsum < 2)
-          ok = ok && fabsf(r[0] + (k0 ? sg[0] : 0.f)) <= ns && fabsf(r[1] + (k1 ? sg[1] : 0.f)) <= ns &&
-               fabsf(r[2] + (k2 ? sg[2] : 0.f)) <= ns;
-        if (ok) {
-          const float mult = ew_h32(R2, q.alpha);
-          F0 = fmaf(t0, mult, F0);
-          F1 = fmaf(t1, mult, F1);
-          F2 = fmaf(t2, mult, F2);
-        }
+          ok = ok && fabsf(r[0] + ((c & 1) ? sg[0] : 0.f)) <= ns && fabsf(r[1] + ((c & 2) ? sg[1] : 0.f)) <= ns &&
+               fabsf(r[2] + ((c & 4) ? sg[2] : 0.f)) <= ns;
+        mask |= ok ? 1u << c : 0u;
+      }
+      while (mask) {
+        const int c = __ffs(mask) - 1;
+        mask &= mask - 1;
+        const float t0 = (c & 1) ? fmaf(-sg[0], q.L[0], m[0]) : m[0];
+        const float t1 = (c & 2) ? fmaf(-sg[1], q.L[1], m[1]) : m[1];
+        const float t2 = (c & 4) ? fmaf(-sg[2], q.L[2], m[2]) : m[2];
+        const float R2 = fmaf(t2, t2, fmaf(t1, t1, t0 * t0));
+        const float mult = ew_h32(R2, q.alpha);
+        F0 = fmaf(t0, mult, F0);
+        F1 = fmaf(t1, mult, F1);
+        F2 = fmaf(t2, mult, F2);
       }
     } else {
       for (int k0 = -q.kmax; k0 <= q.kmax; ++k0) {
@@ -2929,17 +3044,20 @@ __device__ inline void pair_eval32(const P32 &q, const float *dx, float *F) {
 }
 
 // same tile/rotation scheme as k_pair_tiles, on FP32 copies of the positions
-// and inverse masses; Kahan-compensated per-particle sums leave as (sum,
-// compensation) pairs in the partial slots, combined in double by
-// k_pair_finish32
+// and inverse masses.  Each lane's sums within a tile have 32 terms at most,
+// added in FP32 (rounding ~ sqrt(32) ulp of the partial, far below the
+// rounding of the FP32 positions); the per-tile partials are added in double
+// by k_pair_finish32.  With one mass for all beads (q.uniform) the inverse
+// mass is applied to the partials instead of to every pair.
 template <int D, int KIND>
 __global__ void __launch_bounds__(256, 3) k_pair_tiles32(Geo g, P32 q, const float *__restrict__ x,
                                                       const float *__restrict__ im,
-                                                      float2 *__restrict__ out, int T, int jobs) {
+                                                      float *__restrict__ out, int T, int jobs) {
   const int lane = threadIdx.x & 31;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
-  // persistent warps: tile jobs (slice j, tile pair I <= J) in round-robin
-  for (int wi = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; wi < jobs * g.P; wi += nwarps) {
+  // persistent warps: tile jobs (slice j, tile pair I <= J) in round-robin,
+  // warps numbered across blocks first (the last round spreads over all SMs)
+  for (int wi = (threadIdx.x >> 5) * gridDim.x + blockIdx.x; wi < jobs * g.P; wi += nwarps) {
     const int j = wi / jobs;
     int job = wi % jobs, I = 0;
     while (job >= T - I) {
@@ -2949,60 +3067,78 @@ __global__ void __launch_bounds__(256, 3) k_pair_tiles32(Geo g, P32 q, const flo
     const int J = I + job;
     const int a = I * 32 + lane, b0 = J * 32 + lane;
     const bool va = a < g.N, vb = b0 < g.N;
-    float xa[D], xb[D];
-    Kahan fa[D], fb[D];
+    float xa[D], xb[D], fa[D], fb[D];
 #pragma unroll
     for (int d = 0; d < D; ++d) {
       xa[d] = va ? x[sidx(j, d, a, D, g.Ns)] : 0.f;
       xb[d] = vb ? x[sidx(j, d, b0, D, g.Ns)] : 0.f;
+      fa[d] = fb[d] = 0.f;
     }
-    const float ima = va ? im[(size_t)j * g.Ns + a] : 1.f;
-    float imb = vb ? im[(size_t)j * g.Ns + b0] : 1.f;
-    for (int s = 0; s < 32; ++s) {
-      const int bi = J * 32 + ((lane + s) & 31);
-      const bool act = va && bi < g.N && (I != J || a > bi);
-      if (act) {
-        float dx[D], F[D];
+    const int src = (lane + 1) & 31;
+    if (q.uniform) {
+      for (int s = 0; s < 32; ++s) {
+        const int bi = J * 32 + ((lane + s) & 31);
+        if (va && bi < g.N && (I != J || a > bi)) {
+          float dx[D], F[D];
 #pragma unroll
-        for (int d = 0; d < D; ++d) dx[d] = xa[d] - xb[d];
-        pair_eval32<D, KIND>(q, dx, F);
-        const float inv = a > bi ? ima : imb;
+          for (int d = 0; d < D; ++d) dx[d] = xa[d] - xb[d];
+          pair_eval32<D, KIND>(q, dx, F);
+#pragma unroll
+          for (int d = 0; d < D; ++d) {
+            fa[d] += F[d];
+            fb[d] -= F[d];
+          }
+        }
 #pragma unroll
         for (int d = 0; d < D; ++d) {
-          fa[d].add(F[d] * inv);
-          fb[d].add(-F[d] * inv);
+          xb[d] = __shfl_sync(FULL, xb[d], src);
+          fb[d] = __shfl_sync(FULL, fb[d], src);
         }
       }
-      const int src = (lane + 1) & 31;
 #pragma unroll
       for (int d = 0; d < D; ++d) {
-        xb[d] = __shfl_sync(FULL, xb[d], src);
-        fb[d].s = __shfl_sync(FULL, fb[d].s, src);
-        fb[d].c = __shfl_sync(FULL, fb[d].c, src);
+        fa[d] *= q.im0;
+        fb[d] *= q.im0;
       }
-      imb = __shfl_sync(FULL, imb, src);
+    } else {
+      const float ima = va ? im[(size_t)j * g.Ns + a] : 1.f;
+      float imb = vb ? im[(size_t)j * g.Ns + b0] : 1.f;
+      for (int s = 0; s < 32; ++s) {
+        const int bi = J * 32 + ((lane + s) & 31);
+        if (va && bi < g.N && (I != J || a > bi)) {
+          float dx[D], F[D];
+#pragma unroll
+          for (int d = 0; d < D; ++d) dx[d] = xa[d] - xb[d];
+          pair_eval32<D, KIND>(q, dx, F);
+          // the reference divides by the mass of the higher-index particle
+          const float inv = a > bi ? ima : imb;
+#pragma unroll
+          for (int d = 0; d < D; ++d) {
+            fa[d] = fmaf(F[d], inv, fa[d]);
+            fb[d] = fmaf(-F[d], inv, fb[d]);
+          }
+        }
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+          xb[d] = __shfl_sync(FULL, xb[d], src);
+          fb[d] = __shfl_sync(FULL, fb[d], src);
+        }
+        imb = __shfl_sync(FULL, imb, src);
+      }
     }
     if (I == J) {
       if (va) {
-        // the diagonal tile's two sums for the same particle: Kahan-add them
 #pragma unroll
-        for (int d = 0; d < D; ++d) {
-          Kahan t = fa[d];
-          t.add(fb[d].s);
-          t.add(-fb[d].c);
-          out[(((size_t)I * g.P + j) * D + d) * g.Ns + a] = make_float2(t.s, t.c);
-        }
+        for (int d = 0; d < D; ++d) out[(((size_t)I * g.P + j) * D + d) * g.Ns + a] = fa[d] + fb[d];
       }
     } else {
       if (va) {
 #pragma unroll
-        for (int d = 0; d < D; ++d)
-          out[(((size_t)J * g.P + j) * D + d) * g.Ns + a] = make_float2(fa[d].s, fa[d].c);
+        for (int d = 0; d < D; ++d) out[(((size_t)J * g.P + j) * D + d) * g.Ns + a] = fa[d];
       }
       if (vb) {
 #pragma unroll
-        for (int d = 0; d < D; ++d)
-          out[(((size_t)I * g.P + j) * D + d) * g.Ns + b0] = make_float2(fb[d].s, fb[d].c);
+        for (int d = 0; d < D; ++d) out[(((size_t)I * g.P + j) * D + d) * g.Ns + b0] = fb[d];
       }
     }
   }
@@ -3016,17 +3152,14 @@ __global__ void k_to32(Geo g, const double *__restrict__ x, const double *__rest
   if (t < (size_t)g.P * g.Ns) im32[t] = (float)(1.0 / m[t]);
 }
 
-// f += scale * sum over the T partial slots of (sum - compensation), in double
-__global__ void k_pair_finish32(Geo g, const float2 *__restrict__ part, int T, double scale,
+// f += scale * sum over the T partial slots, in double
+__global__ void k_pair_finish32(Geo g, const float *__restrict__ part, int T, double scale,
                                 double *__restrict__ f) {
   const size_t s = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   const size_t S = g.slots();
   if (s >= S || (int)(s % g.Ns) >= g.N) return;
   double acc = 0;
-  for (int t = 0; t < T; ++t) {
-    const float2 v = part[(size_t)t * S + s];
-    acc += (double)v.x - (double)v.y;
-  }
+  for (int t = 0; t < T; ++t) acc += (double)part[(size_t)t * S + s];
   f[s] += acc * scale;
 }
 
@@ -3057,7 +3190,7 @@ int pair32_warps(int kind, int D, int N, int P) {
 // persistent grid: as many blocks of `wpb` warps as the kernel keeps
 // resident, or fewer when the jobs run out
 template <int D, int K>
-static cudaError_t launch_pair32(const Geo &g, const P32 &q, const float *x, const float *im, float2 *part, int T,
+static cudaError_t launch_pair32(const Geo &g, const P32 &q, const float *x, const float *im, float *part, int T,
                                  int jobs, int wpb, cudaStream_t st) {
   static int occ[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
   static int sms = 0;
@@ -3098,8 +3231,11 @@ cudaError_t pair_force32(const Geo &g, const PairPrm &p, const double *x, const 
   q.kmax = p.kmax[0] > p.kmax[1] ? (p.kmax[0] > p.kmax[2] ? p.kmax[0] : p.kmax[2])
                                  : (p.kmax[1] > p.kmax[2] ? p.kmax[1] : p.kmax[2]);
   if (p.kind == PAIR_EWALD_REAL && rc32 <= fmin(g.box[0], fmin(g.box[1], g.box[2]))) q.kmax = 0;
-  // scratch: T * slots float2 partials, then the FP32 positions and inverse masses
-  float2 *part = (float2 *)scratch;
+  q.uniform = p.inv_mass > 0;
+  q.im0 = (float)p.inv_mass;
+  // scratch: T * slots float partials (room for twice that is reserved),
+  // then the FP32 positions and inverse masses
+  float *part = (float *)scratch;
   float *x32 = (float *)(scratch + (size_t)T * g.slots());
   float *im32 = x32 + g.slots();
   {

@@ -148,6 +148,7 @@ struct PairPrm {
   int nsum;             // Ewald image cube
   double rcut;          // Ewald real-space cut-off radius
   int kmax[3];          // Ewald: image shifts |k| <= kmax around the minimum image
+  double inv_mass;      // > 0: every bead has this inverse mass (FP32 kernel shortcut)
 };
 size_t pair_scratch_doubles(const Geo &g);
 cudaError_t pair_force(const Geo &g, const PairPrm &p, const double *x, const double *m,
@@ -229,8 +230,11 @@ cudaError_t sk_structure(const Geo &g, const double *x, int ja, int jb, const do
                          cudaStream_t st);
 
 // ---- estimators ----
+// primitive (ENk2 == nullptr) or virial exchange estimator; res[N] + add is
+// added to *acc.  scratch: vbn_scratch_doubles(N) doubles.
+size_t vbn_scratch_doubles(int N);
 cudaError_t vbn_energy(int N, double beta, double vi, double add, const double *ENk,
-                       const double *VBN, const double *ENk2, double *acc, cudaStream_t st);
+                       const double *VBN, const double *ENk2, double *acc, double *scratch, cudaStream_t st);
 cudaError_t force_virial(const Geo &g, const double *x, const double *f, const double *m,
                          int image, double *acc, double *scratch, cudaStream_t st);
 cudaError_t add_scalar(double *acc, double v, cudaStream_t st);

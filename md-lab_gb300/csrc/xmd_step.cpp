@@ -438,6 +438,7 @@ int md_pimd_calc_pair_force_x(md_pimd_t_x *pimd, md_pair_force_t_x pf) {
   cudaStream_t st = stream();
   xk::PairPrm prm = pair_params(kind);
   ewald_shifts(prm, sd->geo);
+  prm.inv_mass = sd->uniform_mass ? 1.0 / sd->mass0 : 0.0;
   const bool mixed = g_precision == MD_GB_PRECISION_MIXED;
   int learned = 0;
   if (kind == xk::PAIR_EWALD_REAL) {
@@ -569,6 +570,7 @@ int md_gb300_autotune_pair_x(md_pimd_t_x *pimd, md_pair_force_t_x pf, int repeat
   if (rc) return rc;
   xk::PairPrm prm = pair_params(kind);
   ewald_shifts(prm, sd->geo);
+  prm.inv_mass = sd->uniform_mass ? 1.0 / sd->mass0 : 0.0;
   const xk::Geo &g = sd->geo;
   DevBuf ftmp;
   XMD_TRY(reserve(ftmp, g.slots() * sizeof(double)));
@@ -661,9 +663,12 @@ int md_pimd_calc_VBN_energy_x(md_pimd_t_x *pimd, md_stats_t_x *stats) {
   XMD_TRY(pimd_device(pimd, &sd, &pd));
   XMD_TRY(check_plain(pimd));
   XMD_TRY(stats_device(stats, &acc));
+  int rc;
+  double *scr = scratch_for(sd, xk::vbn_scratch_doubles(pimd->N), &rc);
+  if (rc) return rc;
   const double add = D * pimd->N * pimd->P / (2 * pimd->beta);
   XMD_CUDA(xk::vbn_energy(pimd->N, pimd->beta, pimd->vi, add, pd->ENk.as<double>(), pd->VBN.as<double>(), nullptr,
-                          acc, stream()));
+                          acc, scr, stream()));
   return 0;
 }
 
@@ -700,12 +705,14 @@ int md_pimd_calc_vi_virial_energy_x(md_pimd_t_x *pimd, md_stats_t_x *stats, int 
   XMD_TRY(check_image(sd, image));
   XMD_TRY(stats_device(stats, &acc));
   int rc;
-  double *scr = scratch_for(sd, general_scratch(sd->geo), &rc);
+  size_t need = general_scratch(sd->geo);
+  if (need < xk::vbn_scratch_doubles(pimd->N)) need = xk::vbn_scratch_doubles(pimd->N);
+  double *scr = scratch_for(sd, need, &rc);
   if (rc) return rc;
   cudaStream_t st = stream();
   const double add = D * pimd->N / (2 * pimd->beta);
   XMD_CUDA(xk::vbn_energy(pimd->N, pimd->beta, pimd->vi, add, pd->ENk.as<double>(), pd->VBN.as<double>(),
-                          pd->ENk2.as<double>(), acc, st));
+                          pd->ENk2.as<double>(), acc, scr, st));
   XMD_CUDA(xk::force_virial(sd->geo, sd->x.as<double>(), sd->f.as<double>(), sd->m.as<double>(), image, acc, scr, st));
   return 0;
 }
