@@ -74,6 +74,7 @@ struct SimDev {
   DevBuf th, vt, Q;
   DevBuf cf, c0, c2;
   DevBuf stage;    // AoS records on the device
+  DevBuf cstage;   // chain records on their way back to the host
   DevBuf scratch;  // partial sums of pair / exchange / reduction kernels
   DevBuf fex;      // exchange spring forces computed on the side stream
   DevBuf xscr;     // partial sums of the exchange forces (side stream)

@@ -229,7 +229,7 @@ cudaError_t soa_to_aos(const Geo &g, double *aos, const double *x, const double 
 // the chain order.
 template <int D>
 __global__ void k_chains(Geo g, int L, int nf, bool fast, bool to_dev, unsigned char *rec,
-                         size_t rb, double *th, double *vt, double *Q) {
+                         size_t rb, double *th, double *vt, double *Q, const int *cf) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= nf) return;
   size_t slot, stride;
@@ -243,6 +243,12 @@ __global__ void k_chains(Geo g, int L, int nf, bool fast, bool to_dev, unsigned 
     stride = nf;
   }
   double *r = (double *)(rec + (size_t)c * rb + 8);
+  if (!to_dev) {
+    // whole records go back: f (1 for one-DOF chains, else as uploaded), zero padding
+    int *fi = (int *)(rec + (size_t)c * rb);
+    fi[0] = fast ? 1 : cf[c];
+    fi[1] = 0;
+  }
   for (int i = 0; i < L; ++i) {
     if (to_dev) {
       th[i * stride + slot] = r[i];
@@ -261,18 +267,19 @@ cudaError_t chains_to_dev(const Geo &g, int L, int nf, bool fast, const unsigned
   {
     XK_PROF("chains");
     DISPATCH_D(g.D, k_chains<D><<<cdiv(nf, 256), 256, 0, st>>>(g, L, nf, fast, true,
-                                                              (unsigned char *)rec, rb, th, vt, Q));
+                                                              (unsigned char *)rec, rb, th, vt, Q, nullptr));
   }
   return XK_LAUNCHED();
 }
 
 cudaError_t chains_to_host(const Geo &g, int L, int nf, bool fast, unsigned char *rec, size_t rb,
-                           const double *th, const double *vt, const double *Q,
+                           const double *th, const double *vt, const double *Q, const int *cf,
                            cudaStream_t st) {
+  if (!fast && !cf) return cudaErrorInvalidValue;
   {
     XK_PROF("chains");
     DISPATCH_D(g.D, k_chains<D><<<cdiv(nf, 256), 256, 0, st>>>(
-                        g, L, nf, fast, false, rec, rb, (double *)th, (double *)vt, (double *)Q));
+                        g, L, nf, fast, false, rec, rb, (double *)th, (double *)vt, (double *)Q, cf));
   }
   return XK_LAUNCHED();
 }

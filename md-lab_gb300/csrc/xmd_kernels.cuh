@@ -67,9 +67,10 @@ cudaError_t soa_to_aos(const Geo &g, double *aos, const double *x, const double 
 // chains: host records {int f; double theta[L], vtheta[L], Q[L]} of rec_bytes each
 cudaError_t chains_to_dev(const Geo &g, int L, int nf, bool fast, const unsigned char *rec,
                           size_t rec_bytes, double *th, double *vt, double *Q, cudaStream_t st);
+// whole records back, f included: 1 for one-DOF chains, cf[c] for grouped ones
 cudaError_t chains_to_host(const Geo &g, int L, int nf, bool fast, unsigned char *rec,
                            size_t rec_bytes, const double *th, const double *vt,
-                           const double *Q, cudaStream_t st);
+                           const double *Q, const int *cf, cudaStream_t st);
 
 // ---- integrator ----
 struct Chains {

@@ -216,7 +216,7 @@ static void free_sim(SimDev *d) {
       v.erase(std::remove(v.begin(), v.end(), d), v.end());
     }
   for (DevBuf *b : {&d->x, &d->v, &d->f, &d->m, &d->th, &d->vt, &d->Q, &d->cf, &d->c0, &d->c2,
-                    &d->stage, &d->scratch, &d->fex, &d->xscr})
+                    &d->stage, &d->cstage, &d->scratch, &d->fex, &d->xscr})
     release(*b);
 }
 
@@ -400,22 +400,14 @@ int sim_to_host(md_simulation_t_x *sim, bool keep) {
                           d->f.as<double>(), d->m.as<double>(), st));
   XMD_CUDA(cudaMemcpyAsync(sim->particles, d->stage.p, pbytes, cudaMemcpyDeviceToHost, st));
   if (sim->nhcs && sim->Nf > 0) {
-    // the particle copy must leave the stage before the chains reuse it
-    XMD_CUDA(cudaStreamSynchronize(st));
+    // whole chain records (f as uploaded) through their own stage, straight
+    // into the page-locked host array
     const size_t cbytes = sizeof(md_nhc_t_x) * (size_t)sim->Nf;
-    XMD_CUDA(xk::chains_to_host(g, d->L, sim->Nf, d->fast_chains, d->stage.as<unsigned char>(),
+    XMD_TRY(reserve(d->cstage, cbytes));
+    XMD_CUDA(xk::chains_to_host(g, d->L, sim->Nf, d->fast_chains, d->cstage.as<unsigned char>(),
                                 sizeof(md_nhc_t_x), d->th.as<double>(), d->vt.as<double>(),
-                                d->Q.as<double>(), st));
-    // f of each chain is not changed on the device: copy everything but f
-    XMD_CUDA(cudaStreamSynchronize(st));
-    std::vector<unsigned char> tmp(cbytes);
-    XMD_CUDA(cudaMemcpy(tmp.data(), d->stage.p, cbytes, cudaMemcpyDeviceToHost));
-    for (int i = 0; i < sim->Nf; ++i) {
-      const md_nhc_t_x *src = (const md_nhc_t_x *)(tmp.data() + (size_t)i * sizeof(md_nhc_t_x));
-      memcpy(sim->nhcs[i].theta, src->theta, sizeof(src->theta));
-      memcpy(sim->nhcs[i].vtheta, src->vtheta, sizeof(src->vtheta));
-      memcpy(sim->nhcs[i].Q, src->Q, sizeof(src->Q));
-    }
+                                d->Q.as<double>(), d->cf.as<int>(), st));
+    XMD_CUDA(cudaMemcpyAsync(sim->nhcs, d->cstage.p, cbytes, cudaMemcpyDeviceToHost, st));
   }
   XMD_CUDA(cudaStreamSynchronize(st));
   if (!keep) d->valid = false;
