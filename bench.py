@@ -214,12 +214,33 @@ def n_images(xcut=5.8):
 # algorithmic work per launch of each kernel (FMA = 2 flops); the same count
 # for the FP64 and FP32 versions of a kernel (the design doc section 4 derives
 # each from the kernel's arithmetic)
+def kept_nz_pairs(nsum):
+    """sum over the kept wave-vector columns (nx, ny) of their largest kept
+    |nz|: the library leaves out vectors whose force weight |G| c(n) is
+    below 1e-17 of the largest (RECIP_KEEP), so the column kernels run
+    this many +-nz pairs instead of ncol * nsum (cubic box, alpha L = ALPHA_L)"""
+    w = {}
+    for nx in range(nsum + 1):
+        for ny in range(-nsum, nsum + 1):
+            if nx == 0 and ny < 0:
+                continue
+            for nz in range(1 if nx == 0 and ny == 0 else -nsum, nsum + 1):
+                g2 = nx * nx + ny * ny + nz * nz
+                w[(nx, ny, nz)] = math.exp(-math.pi ** 2 * g2 / ALPHA_L ** 2) / math.sqrt(g2)
+    wmax = max(w.values())
+    nzmax = {}
+    for (nx, ny, nz), v in w.items():
+        if v >= 1e-17 * wmax:
+            nzmax[(nx, ny)] = max(nzmax.get((nx, ny), 0), abs(nz))
+    return sum(nzmax.values())
+
+
 def kernel_flops(name, nsum=NSUM):
-    ncol = nsum * (2 * nsum + 1) + nsum + 1  # wave-vector columns (nx, ny)
     if name in ("recip_force", "recip_force32"):
-        return 177.0 * ncol * N * P * nsum / NSUM
+        # 17.7 flop per +-nz pair of a kept column per particle and slice
+        return 17.7 * kept_nz_pairs(nsum) * N * P
     if name in ("sk", "sk32"):
-        return 88.0 * ncol * N * P * nsum / NSUM
+        return 8.8 * kept_nz_pairs(nsum) * N * P
     if name == "pair_tiles_ewald_real":
         pairs = P * N * (N - 1) / 2
         return pairs * (47.0 * n_images() + 39.0)

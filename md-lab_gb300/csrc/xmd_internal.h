@@ -97,6 +97,7 @@ struct PimdDev {
   int rc_nsum = -1;
   double rc_alpha = 0, rc_qs = 0, rc_box[3] = {0, 0, 0};
   int rc_nk = 0;
+  int rc_ncol = 0;  // kept wave-vector columns
   double rc_csum = 0;
 };
 

@@ -13,6 +13,7 @@
 // Reference counterparts (MD-Lab file:line) are cited at each kernel.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <array>
 #include <atomic>
 #include <cmath>
@@ -2037,6 +2038,10 @@ static std::vector<Col> columns(int ns) {
 
 int recip_count(int ns) { return ((2 * ns + 1) * (2 * ns + 1) * (2 * ns + 1) - 1) / 2; }
 
+// a column's nx and its largest kept |nz| share the int4's x field
+__host__ __device__ inline int col_nx(const int4 &c) { return c.x & 255; }
+__host__ __device__ inline int col_nz(const int4 &c) { return c.x >> 8; }
+
 size_t recip_phase_doubles(const Geo &g, int ns) { return (size_t)g.P * 3 * (ns + 1) * g.Ns * 2; }
 
 // phase[((j*3 + d)*(ns+1) + n)*Ns + l] = exp(i 2 pi n x / L) as (re, im)
@@ -2088,8 +2093,11 @@ __global__ void __launch_bounds__(SK_THREADS) k_sk(Geo g, const double2 *__restr
   const int ci = blockIdx.x * SK_THREADS + threadIdx.x;
   const bool live = ci < ncol;
   const int4 c = live ? cols[ci] : make_int4(0, 0, 1, 0);
-  const int ax = c.x, ay = c.y < 0 ? -c.y : c.y;
+  const int ax = col_nx(c), ay = c.y < 0 ? -c.y : c.y;
   const bool cy = c.y < 0;  // conjugate the y factor
+  // the warp's largest kept |nz| (columns come longest first, so lanes
+  // agree closely); terms beyond a lane's own bound meet c(n) = 0 later
+  const int nzw = __reduce_max_sync(FULL, live ? col_nz(c) : 0);
   double s0r = 0, s0i = 0, P[NS][2], Q[NS][2];
 #pragma unroll
   for (int n = 0; n < NS; ++n) P[n][0] = P[n][1] = Q[n][0] = Q[n][1] = 0.0;
@@ -2112,6 +2120,7 @@ __global__ void __launch_bounds__(SK_THREADS) k_sk(Geo g, const double2 *__restr
       s0i += exy.y;
 #pragma unroll
       for (int n = 1; n <= NS; ++n) {
+        if (n > nzw) break;  // warp-uniform
         const double2 ez = sp[2][n][l];
         P[n - 1][0] = fma(exy.x, ez.x, P[n - 1][0]);
         P[n - 1][1] = fma(exy.y, ez.x, P[n - 1][1]);
@@ -2193,11 +2202,13 @@ __global__ void __launch_bounds__(128) k_recip_force(Geo g, const double2 *__res
   double Fx = 0, Fy = 0, Fz = 0, Er = 0;
   for (int ci = 0; ci < ncol; ++ci) {
     const int4 c = cols[ci];
-    const double2 exy = cmul(phase_at(ph, g, NS, j, 0, c.x, l), phase_at(ph, g, NS, j, 1, c.y, l));
+    const int nzc = col_nz(c);
+    const double2 exy = cmul(phase_at(ph, g, NS, j, 0, col_nx(c), l), phase_at(ph, g, NS, j, 1, c.y, l));
     const double2 *t = sT + ci * NT;
     double Ur = t[0].x, Ui = t[0].y, Vr = 0, Vi = 0;
 #pragma unroll
     for (int n = 1; n <= NS; ++n) {
+      if (n > nzc) break;  // uniform: every thread walks the same column
       const double2 A = t[4 * n - 3], B = t[4 * n - 2], nA = t[4 * n - 1], nB = t[4 * n];
       const double cz = ez[n].x, sz = ez[n].y;
       Ur = fma(cz, A.x, fma(-sz, B.y, Ur));
@@ -2207,7 +2218,7 @@ __global__ void __launch_bounds__(128) k_recip_force(Geo g, const double2 *__res
     }
     const double Tm = fma(exy.x, Ui, exy.y * Ur);  // Im(e_xy U)
     const double Zm = fma(exy.x, Vi, exy.y * Vr);  // Im(e_xy V)
-    Fx = fma((double)c.x, Tm, Fx);
+    Fx = fma((double)col_nx(c), Tm, Fx);
     Fy = fma((double)c.y, Tm, Fy);
     Fz += Zm;
     if (WITH_E) Er += fma(exy.x, Ur, -exy.y * Ui);  // Re(e_xy U)
@@ -2224,8 +2235,10 @@ __global__ void k_recip_energy(Geo g, const double2 *__restrict__ S, const doubl
   const int j = blockIdx.x;
   double e = 0;
   for (int k = threadIdx.x; k < nk; k += blockDim.x) {
+    const double ck = coef[k];
+    if (__double_as_longlong(ck) == 0) continue;  // a dropped vector
     const double2 s = S[(size_t)j * nk + k];
-    e += coef[k] * (s.x * s.x + s.y * s.y - g.N);
+    e += ck * (s.x * s.x + s.y * s.y - g.N);
   }
   e = block_sum(e, buf);
   if (threadIdx.x == 0) part[j] = e;
@@ -2233,31 +2246,62 @@ __global__ void k_recip_energy(Geo g, const double2 *__restrict__ S, const doubl
 
 cudaError_t recip_setup(const Geo &g, int ns, double alpha, double qs, Recip &r,
                         cudaStream_t st) {
-  // host-side tables: column descriptors then c(n) in column order
+  // host-side tables: c(n) in the full column order, then the kept columns
   std::vector<Col> cols = columns(ns);
   const int nk = recip_count(ns);
-  std::vector<double> coef(nk);
-  std::vector<int4> cd(cols.size());
+  std::vector<double> coef(nk), wgt(nk);
   const double V = g.box[0] * g.box[1] * g.box[2];
-  for (size_t i = 0; i < cols.size(); ++i) {
-    const Col &c = cols[i];
-    cd[i] = make_int4(c.nx, c.ny, c.nz0, c.off);
+  double wmax = 0;
+  for (const Col &c : cols)
     for (int nz = c.nz0; nz <= ns; ++nz) {
       const double gx = c.nx / g.box[0], gy = c.ny / g.box[1], gz = nz / g.box[2];
       const double G = sqrt(gx * gx + gy * gy + gz * gz);
-      coef[c.off + nz - c.nz0] = qs * pow(G, -2) * exp(-M_PI * M_PI * G * G / (alpha * alpha)) / (V * M_PI);
+      const int k = c.off + nz - c.nz0;
+      coef[k] = qs * pow(G, -2) * exp(-M_PI * M_PI * G * G / (alpha * alpha)) / (V * M_PI);
+      wgt[k] = fabs(coef[k]) * G;  // weight of the vector in the forces
+      wmax = wgt[k] > wmax ? wgt[k] : wmax;
     }
+  // per column the largest |nz| whose vector is kept (+nz and -nz have the
+  // same |G|); columns without one are left out, the rest sorted longest first
+  std::vector<std::pair<int, int4>> kept;
+  for (const Col &c : cols) {
+    int nzmax = -1;
+    for (int nz = c.nz0; nz <= ns; ++nz) {
+      const int k = c.off + nz - c.nz0;
+      if (wgt[k] >= RECIP_KEEP * wmax) {
+        nzmax = abs(nz) > nzmax ? abs(nz) : nzmax;
+      }
+    }
+    for (int nz = c.nz0; nz <= ns; ++nz)
+      if (abs(nz) > nzmax) coef[c.off + nz - c.nz0] = 0.0;
+    if (nzmax < 0 || (c.nz0 > 0 && nzmax < c.nz0)) continue;
+    kept.push_back({nzmax, make_int4(c.nx | (nzmax << 8), c.ny, c.nz0, c.off)});
   }
+  std::stable_sort(kept.begin(), kept.end(), [](const std::pair<int, int4> &a, const std::pair<int, int4> &b) {
+    return a.first > b.first;
+  });
+  std::vector<int4> cd(kept.size());
+  for (size_t i = 0; i < kept.size(); ++i) cd[i] = kept[i].second;
   r.nsum = ns;
   r.nk = nk;
+  r.ncol = (int)cd.size();
   r.csum = 0;
   for (double c : coef) r.csum += c;
   cudaError_t e = cudaMemcpyAsync(r.coef, coef.data(), sizeof(double) * nk, cudaMemcpyHostToDevice, st);
   if (e != cudaSuccess) return e;
-  e = cudaMemcpyAsync(r.kvec, cd.data(), sizeof(int4) * cd.size(), cudaMemcpyHostToDevice, st);
-  if (e != cudaSuccess) return e;
+  if (!cd.empty()) {
+    e = cudaMemcpyAsync(r.kvec, cd.data(), sizeof(int4) * cd.size(), cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return e;
+  }
+  // dropped vectors keep S = 0 (their c(n) = 0 multiplies them in the energies)
+  if (r.S) {
+    e = cudaMemsetAsync(r.S, 0, sizeof(double2) * (size_t)nk * g.P, st);
+    if (e != cudaSuccess) return e;
+  }
   return cudaStreamSynchronize(st);
 }
+
+size_t recip_cols_ints(int ns) { return 4 * (size_t)(ns * (2 * ns + 1) + ns + 1); }
 
 static int ncols(int ns) { return ns * (2 * ns + 1) + ns + 1; }
 
@@ -2287,7 +2331,7 @@ static cudaError_t structure_factors(const Geo &g, const Recip &r, const double 
   }
   cudaError_t e = XK_LAUNCHED();
   if (e != cudaSuccess) return e;
-  const int nc = ncols(r.nsum);
+  const int nc = r.ncol;
   dim3 grid((nc + SK_THREADS - 1) / SK_THREADS, g.P);
   {
     XK_PROF("sk");
@@ -2304,7 +2348,7 @@ cudaError_t recip_force(const Geo &g, const Recip &r, const double *x, double in
   if (g.D != 3) return cudaErrorInvalidValue;
   cudaError_t e = structure_factors(g, r, x, st);
   if (e != cudaSuccess) return e;
-  const int nc = ncols(r.nsum);
+  const int nc = r.ncol;
   const size_t smem = sizeof(double2) * nc * (4 * r.nsum + 1);
   dim3 tgrid((nc + 7) / 8, g.P), tblk(r.nsum + 1, 8);
   dim3 grid((g.N + 127) / 128, g.P);
@@ -2336,7 +2380,7 @@ cudaError_t recip_force_energy(const Geo &g, const Recip &r, const double *x, do
   if (g.D != 3) return cudaErrorInvalidValue;
   cudaError_t err = structure_factors(g, r, x, st);
   if (err != cudaSuccess) return err;
-  const int nc = ncols(r.nsum);
+  const int nc = r.ncol;
   const double e0 = r.csum;
   const size_t smem = sizeof(double2) * nc * (4 * r.nsum + 1);
   dim3 tgrid((nc + 7) / 8, g.P), tblk(r.nsum + 1, 8);
@@ -2385,7 +2429,7 @@ cudaError_t recip_energy(const Geo &g, const Recip &r, const double *x, double *
 // Each species keeps its own phases, structure factors and tables (T from
 // its own S); a's forces read b's tables and b's read a's.
 static cudaError_t recip_tables_of(const Geo &g, const Recip &r, cudaStream_t st) {
-  const int nc = ncols(r.nsum);
+  const int nc = r.ncol;
   dim3 tgrid((nc + 7) / 8, g.P), tblk(r.nsum + 1, 8);
   DISPATCH_NS(r.nsum, {
     XK_PROF("recip_tables");
@@ -2397,7 +2441,7 @@ static cudaError_t recip_tables_of(const Geo &g, const Recip &r, cudaStream_t st
 
 static cudaError_t recip_force_from(const Geo &g, const Recip &own, const double *T_other, double scale, double *f,
                                     cudaStream_t st) {
-  const int nc = ncols(own.nsum);
+  const int nc = own.ncol;
   const size_t smem = sizeof(double2) * nc * (4 * own.nsum + 1);
   dim3 grid((g.N + 127) / 128, g.P);
   DISPATCH_NS(own.nsum, {
@@ -2416,7 +2460,7 @@ static cudaError_t recip_force_from(const Geo &g, const Recip &own, const double
 }
 
 static bool recip_pair_ok(const Geo &ga, const Recip &ra, const Geo &gb, const Recip &rb) {
-  return ga.D == 3 && gb.D == 3 && ga.P == gb.P && ra.nsum == rb.nsum && ra.nk == rb.nk;
+  return ga.D == 3 && gb.D == 3 && ga.P == gb.P && ra.nsum == rb.nsum && ra.nk == rb.nk && ra.ncol == rb.ncol;
 }
 
 cudaError_t recip_force_2(const Geo &ga, const Recip &ra, const double *xa, double inv_mPa, double *fa,
@@ -2438,8 +2482,10 @@ __global__ void k_recip_energy_2(const double2 *__restrict__ Sa, const double2 *
   const int j = blockIdx.x;
   double e = 0;
   for (int k = threadIdx.x; k < nk; k += blockDim.x) {
+    const double ck = coef[k];
+    if (__double_as_longlong(ck) == 0) continue;  // a dropped vector
     const double2 a = Sa[(size_t)j * nk + k], b = Sb[(size_t)j * nk + k];
-    e += 2 * coef[k] * (a.x * b.x + a.y * b.y);
+    e += 2 * ck * (a.x * b.x + a.y * b.y);
   }
   e = block_sum(e, buf);
   if (threadIdx.x == 0) part[j] = e;
@@ -3310,8 +3356,9 @@ __global__ void __launch_bounds__(SK_THREADS) k_sk32(Geo g, const float2 *__rest
   const int ci = blockIdx.x * SK_THREADS + threadIdx.x;
   const bool live = ci < ncol;
   const int4 c = live ? cols[ci] : make_int4(0, 0, 1, 0);
-  const int ax = c.x, ay = c.y < 0 ? -c.y : c.y;
+  const int ax = col_nx(c), ay = c.y < 0 ? -c.y : c.y;
   const bool cy = c.y < 0;
+  const int nzw = __reduce_max_sync(FULL, live ? col_nz(c) : 0);  // as in k_sk
   DF s0r, s0i, P[NS][2], Q[NS][2];
   const float2 *base = ph + (size_t)j * 3 * (NS + 1) * g.Ns;
   for (int l0 = 0; l0 < g.N; l0 += SK_CHUNK) {
@@ -3331,6 +3378,7 @@ __global__ void __launch_bounds__(SK_THREADS) k_sk32(Geo g, const float2 *__rest
       s0i.add(exy.y);
 #pragma unroll
       for (int n = 1; n <= NS; ++n) {
+        if (n > nzw) break;  // warp-uniform
         const float2 ez = sp[2][n][l];
         P[n - 1][0].add(exy.x * ez.x);
         P[n - 1][1].add(exy.y * ez.x);
@@ -3402,13 +3450,15 @@ __global__ void __launch_bounds__(128) k_recip_force32(Geo g, const float2 *__re
   Kahan Fx, Fy, Fz;
   for (int ci = 0; ci < ncol; ++ci) {
     const int4 c = cols[ci];
+    const int nzc = col_nz(c);
     float2 ey = pj[((size_t)(NS + 1) + (c.y < 0 ? -c.y : c.y)) * g.Ns];
     if (c.y < 0) ey.y = -ey.y;
-    const float2 exy = cmulf(pj[(size_t)c.x * g.Ns], ey);
+    const float2 exy = cmulf(pj[(size_t)col_nx(c) * g.Ns], ey);
     const float2 *t = sT + ci * NT;
     float Ur = t[0].x, Ui = t[0].y, Vr = 0.f, Vi = 0.f;
 #pragma unroll
     for (int n = 1; n <= NS; ++n) {
+      if (n > nzc) break;  // uniform across the block
       const float2 A = t[4 * n - 3], B = t[4 * n - 2], nA = t[4 * n - 1], nB = t[4 * n];
       const float cz = ez[n].x, sz = ez[n].y;
       Ur = fmaf(cz, A.x, fmaf(-sz, B.y, Ur));
@@ -3418,7 +3468,7 @@ __global__ void __launch_bounds__(128) k_recip_force32(Geo g, const float2 *__re
     }
     const float Tm = fmaf(exy.x, Ui, exy.y * Ur);
     const float Zm = fmaf(exy.x, Vi, exy.y * Vr);
-    Fx.add((float)c.x * Tm);
+    Fx.add((float)col_nx(c) * Tm);
     Fy.add((float)c.y * Tm);
     Fz.add(Zm);
   }
@@ -3446,7 +3496,7 @@ cudaError_t recip_force32(const Geo &g, const Recip &r, const double *x, double 
   }
   e = XK_LAUNCHED();
   if (e != cudaSuccess) return e;
-  const int nc = ncols(r.nsum);
+  const int nc = r.ncol;
   dim3 sgrid((nc + SK_THREADS - 1) / SK_THREADS, g.P);
   dim3 tgrid((nc + 7) / 8, g.P), tblk(r.nsum + 1, 8);
   dim3 grid((g.N + 127) / 128, g.P);

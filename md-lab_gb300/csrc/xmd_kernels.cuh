@@ -179,11 +179,19 @@ cudaError_t pair_energy_2(const Geo &ga, const Geo &gb, const PairPrm &p, const 
                           double *acc, double *scratch, cudaStream_t st);
 
 // Ewald reciprocal space through structure factors (D = 3)
+// Wave vectors whose force weight |G| c(n) is below RECIP_KEEP of the
+// largest are left out (c(n) = 0 and no column work): each is below the
+// resolution of a double, and the reference's cube |n_i| <= nsum keeps them
+// only because it is a cube (at alpha L = 5.6, nsum = 10 the kept ones are
+// the 52% inside |n|^2 <= 111).
+constexpr double RECIP_KEEP = 1e-17;
 struct Recip {
   int nsum;
-  int nk;              // half-space wave vectors
-  double *coef;        // [nk] s * exp(-pi^2 G^2/alpha^2) / (pi V G^2)
-  int *kvec;           // column table: int4 (nx, ny, first nz, offset of its first k)
+  int nk;              // half-space wave vectors of the cube
+  int ncol;            // kept columns (set by recip_setup)
+  double *coef;        // [nk] s * exp(-pi^2 G^2/alpha^2) / (pi V G^2), 0 for a dropped vector
+  int *kvec;           // kept columns, longest first: int4 (nx | nzmax << 8, ny, first nz,
+                       // offset of its first k); recip_cols_ints(nsum) ints
   double *phase;       // [P][3][nsum+1][Ns] complex
   double *S;           // [P][nk] complex
   double *T;           // [P][columns][2 nsum + 1] complex force tables
@@ -191,6 +199,7 @@ struct Recip {
 };
 size_t recip_phase_doubles(const Geo &g, int nsum);
 int recip_count(int nsum);
+size_t recip_cols_ints(int nsum);
 size_t recip_table_doubles(const Geo &g, int nsum);
 cudaError_t recip_setup(const Geo &g, int nsum, double alpha, double qs, Recip &r,
                         cudaStream_t st);

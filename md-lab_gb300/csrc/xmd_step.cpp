@@ -363,7 +363,7 @@ int xmd::ewald_tables(md_pimd_t_x *pimd, SimDev *sd, PimdDev *pd) {
   if (capturing()) return fail(MD_GB_ERR_CAPTURE, "Ewald tables change while capturing a graph");
   const int nk = xk::recip_count(ns);
   XMD_TRY(reserve(pd->rc_coef, sizeof(double) * nk));
-  XMD_TRY(reserve(pd->rc_cols, sizeof(int) * 4 * (ns * (2 * ns + 1) + ns + 1)));
+  XMD_TRY(reserve(pd->rc_cols, sizeof(int) * xk::recip_cols_ints(ns)));
   // FP64 phases, then their FP32 copy for the mixed form
   XMD_TRY(reserve(pd->rc_phase, sizeof(double) * xk::recip_phase_doubles(g, ns) * 3 / 2));
   XMD_TRY(reserve(pd->rc_S, sizeof(double) * 2 * (size_t)nk * g.P));
@@ -371,7 +371,9 @@ int xmd::ewald_tables(md_pimd_t_x *pimd, SimDev *sd, PimdDev *pd) {
   xk::Recip r{};
   r.coef = pd->rc_coef.as<double>();
   r.kvec = pd->rc_cols.as<int>();
+  r.S = pd->rc_S.as<double>();
   XMD_CUDA(xk::recip_setup(g, ns, a, qs, r, stream()));
+  pd->rc_ncol = r.ncol;
   pd->rc_nsum = ns;
   pd->rc_alpha = a;
   pd->rc_qs = qs;
@@ -389,6 +391,7 @@ xk::Recip xmd::recip_of(PimdDev *pd) {
   xk::Recip r{};
   r.nsum = pd->rc_nsum;
   r.nk = pd->rc_nk;
+  r.ncol = pd->rc_ncol;
   r.coef = pd->rc_coef.as<double>();
   r.kvec = pd->rc_cols.as<int>();
   r.phase = pd->rc_phase.as<double>();
