@@ -2081,23 +2081,26 @@ __device__ inline double2 phase_at(const double2 *ph, const Geo &g, int ns, int 
 // column) sums over the slice's particles, whose phase factors are staged in
 // shared memory in chunks, so no cross-thread reduction is needed.  With
 // P = sum e_xy c and Q = sum e_xy s:  S(+nz) = P + iQ,  S(-nz) = P - iQ.
-constexpr int SK_THREADS = 64, SK_CHUNK = 64;
+// Block = SK_COLS columns of one slice x SK_GROUPS particle groups: the 16
+// lanes of a column (adjacent in the warp) sum every 16th particle of each
+// staged chunk and combine by four shuffles at the end, so that a slice's
+// columns give 16 times as many warps to hide the FP64 latency and the grid
+// (12 blocks per slice at |n| <= 10) fills the SMs in even rounds.
+constexpr int SK_COLS = 16, SK_GROUPS = 16, SK_THREADS = SK_COLS * SK_GROUPS, SK_CHUNK = 64;
 
 template <int NS>
-__global__ void __launch_bounds__(SK_THREADS) k_sk(Geo g, const double2 *__restrict__ ph,
+__global__ void __launch_bounds__(SK_THREADS, 2) k_sk(Geo g, const double2 *__restrict__ ph,
                                                    const int4 *__restrict__ cols, int ncol,
                                                    double2 *__restrict__ S, int nk) {
   // staged phases of SK_CHUNK particles: x, y, z factors for n = 0..NS
   __shared__ double2 sp[3][NS + 1][SK_CHUNK];
   const int j = blockIdx.y;
-  const int ci = blockIdx.x * SK_THREADS + threadIdx.x;
+  const int gq = threadIdx.x & (SK_GROUPS - 1);
+  const int ci = blockIdx.x * SK_COLS + threadIdx.x / SK_GROUPS;
   const bool live = ci < ncol;
   const int4 c = live ? cols[ci] : make_int4(0, 0, 1, 0);
   const int ax = col_nx(c), ay = c.y < 0 ? -c.y : c.y;
   const bool cy = c.y < 0;  // conjugate the y factor
-  // the warp's largest kept |nz| (columns come longest first, so lanes
-  // agree closely); terms beyond a lane's own bound meet c(n) = 0 later
-  const int nzw = __reduce_max_sync(FULL, live ? col_nz(c) : 0);
   double s0r = 0, s0i = 0, P[NS][2], Q[NS][2];
 #pragma unroll
   for (int n = 0; n < NS; ++n) P[n][0] = P[n][1] = Q[n][0] = Q[n][1] = 0.0;
@@ -2111,7 +2114,7 @@ __global__ void __launch_bounds__(SK_THREADS) k_sk(Geo g, const double2 *__restr
     }
     __syncthreads();
     if (!live) continue;
-    for (int l = 0; l < cnt; ++l) {
+    for (int l = gq; l < cnt; l += SK_GROUPS) {
       const double2 ex = sp[0][ax][l];
       double2 ey = sp[1][ay][l];
       if (cy) ey.y = -ey.y;
@@ -2120,7 +2123,6 @@ __global__ void __launch_bounds__(SK_THREADS) k_sk(Geo g, const double2 *__restr
       s0i += exy.y;
 #pragma unroll
       for (int n = 1; n <= NS; ++n) {
-        if (n > nzw) break;  // warp-uniform
         const double2 ez = sp[2][n][l];
         P[n - 1][0] = fma(exy.x, ez.x, P[n - 1][0]);
         P[n - 1][1] = fma(exy.y, ez.x, P[n - 1][1]);
@@ -2129,7 +2131,20 @@ __global__ void __launch_bounds__(SK_THREADS) k_sk(Geo g, const double2 *__restr
       }
     }
   }
-  if (!live) return;
+  // the column's 16 lanes, pairwise in a fixed order
+#pragma unroll
+  for (int o = 1; o < SK_GROUPS; o <<= 1) {
+    s0r += __shfl_xor_sync(FULL, s0r, o);
+    s0i += __shfl_xor_sync(FULL, s0i, o);
+#pragma unroll
+    for (int n = 0; n < NS; ++n) {
+      P[n][0] += __shfl_xor_sync(FULL, P[n][0], o);
+      P[n][1] += __shfl_xor_sync(FULL, P[n][1], o);
+      Q[n][0] += __shfl_xor_sync(FULL, Q[n][0], o);
+      Q[n][1] += __shfl_xor_sync(FULL, Q[n][1], o);
+    }
+  }
+  if (!live || gq != 0) return;
   double2 *o = S + (size_t)j * nk + c.w - c.z;  // o[nz] for nz = c.z..NS
   if (c.z <= 0) o[0] = make_double2(s0r, s0i);
 #pragma unroll
@@ -2332,7 +2347,7 @@ static cudaError_t structure_factors(const Geo &g, const Recip &r, const double 
   cudaError_t e = XK_LAUNCHED();
   if (e != cudaSuccess) return e;
   const int nc = r.ncol;
-  dim3 grid((nc + SK_THREADS - 1) / SK_THREADS, g.P);
+  dim3 grid((nc + SK_COLS - 1) / SK_COLS, g.P);
   {
     XK_PROF("sk");
     DISPATCH_NS(r.nsum, k_sk<NS><<<grid, SK_THREADS, 0, st>>>(g, (const double2 *)r.phase,
@@ -3353,12 +3368,12 @@ __global__ void __launch_bounds__(SK_THREADS) k_sk32(Geo g, const float2 *__rest
                                                      double2 *__restrict__ S, int nk) {
   __shared__ float2 sp[3][NS + 1][SK_CHUNK];
   const int j = blockIdx.y;
-  const int ci = blockIdx.x * SK_THREADS + threadIdx.x;
+  const int gq = threadIdx.x & (SK_GROUPS - 1);
+  const int ci = blockIdx.x * SK_COLS + threadIdx.x / SK_GROUPS;
   const bool live = ci < ncol;
   const int4 c = live ? cols[ci] : make_int4(0, 0, 1, 0);
   const int ax = col_nx(c), ay = c.y < 0 ? -c.y : c.y;
   const bool cy = c.y < 0;
-  const int nzw = __reduce_max_sync(FULL, live ? col_nz(c) : 0);  // as in k_sk
   DF s0r, s0i, P[NS][2], Q[NS][2];
   const float2 *base = ph + (size_t)j * 3 * (NS + 1) * g.Ns;
   for (int l0 = 0; l0 < g.N; l0 += SK_CHUNK) {
@@ -3370,7 +3385,7 @@ __global__ void __launch_bounds__(SK_THREADS) k_sk32(Geo g, const float2 *__rest
     }
     __syncthreads();
     if (!live) continue;
-    for (int l = 0; l < cnt; ++l) {
+    for (int l = gq; l < cnt; l += SK_GROUPS) {
       float2 ey = sp[1][ay][l];
       if (cy) ey.y = -ey.y;
       const float2 exy = cmulf(sp[0][ax][l], ey);
@@ -3378,7 +3393,6 @@ __global__ void __launch_bounds__(SK_THREADS) k_sk32(Geo g, const float2 *__rest
       s0i.add(exy.y);
 #pragma unroll
       for (int n = 1; n <= NS; ++n) {
-        if (n > nzw) break;  // warp-uniform
         const float2 ez = sp[2][n][l];
         P[n - 1][0].add(exy.x * ez.x);
         P[n - 1][1].add(exy.y * ez.x);
@@ -3387,7 +3401,25 @@ __global__ void __launch_bounds__(SK_THREADS) k_sk32(Geo g, const float2 *__rest
       }
     }
   }
-  if (!live) return;
+  // the column's 16 lanes, pairwise in a fixed order (both parts of each sum)
+  auto comb = [](DF &v, int o) {
+    const float h = __shfl_xor_sync(FULL, v.hi, o), lo = __shfl_xor_sync(FULL, v.lo, o);
+    v.add(h);
+    v.lo += lo;
+  };
+#pragma unroll
+  for (int o = 1; o < SK_GROUPS; o <<= 1) {
+    comb(s0r, o);
+    comb(s0i, o);
+#pragma unroll
+    for (int n = 0; n < NS; ++n) {
+      comb(P[n][0], o);
+      comb(P[n][1], o);
+      comb(Q[n][0], o);
+      comb(Q[n][1], o);
+    }
+  }
+  if (!live || gq != 0) return;
   double2 *o = S + (size_t)j * nk + c.w - c.z;
   if (c.z <= 0) o[0] = make_double2(s0r.value(), s0i.value());
 #pragma unroll
@@ -3497,7 +3529,7 @@ cudaError_t recip_force32(const Geo &g, const Recip &r, const double *x, double 
   e = XK_LAUNCHED();
   if (e != cudaSuccess) return e;
   const int nc = r.ncol;
-  dim3 sgrid((nc + SK_THREADS - 1) / SK_THREADS, g.P);
+  dim3 sgrid((nc + SK_COLS - 1) / SK_COLS, g.P);
   dim3 tgrid((nc + 7) / 8, g.P), tblk(r.nsum + 1, 8);
   dim3 grid((g.N + 127) / 128, g.P);
   const size_t smem = sizeof(float2) * nc * (4 * r.nsum + 1);

@@ -871,14 +871,14 @@ template <bool RAW>
 __global__ void __launch_bounds__(DS_WARPS * 32) k_desc(Geo g, DescPrm p, const double *__restrict__ x,
                                                         uint8_t *__restrict__ ximg, float *__restrict__ V,
                                                         float *__restrict__ raw) {
+  // the 32 KB basis is read through L1 (shared by every block on the SM),
+  // so that shared memory holds only per-block data and more blocks fit
   extern __shared__ __align__(16) float dsm[];
-  float *basis = dsm;                                // DESC_BINS * 64
-  float *hist = basis + DESC_BINS * 64;              // [DESC_BINS][DS_ROWS]: lane t owns column t
+  float *hist = dsm;                                 // [DESC_BINS][DS_ROWS]: lane t owns column t
   float *vacc = hist + DESC_BINS * DS_ROWS;          // DS_WARPS * DS_ROWS * 9
-  float4 *pos = (float4 *)(vacc + DS_WARPS * DS_ROWS * 9);  // N; 58368 bytes in: 16-byte aligned
+  float4 *pos = (float4 *)(vacc + DS_WARPS * DS_ROWS * 9);  // N; 25600 bytes in: 16-byte aligned
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int j = blockIdx.y, l0 = blockIdx.x * DS_ROWS;
-  for (int q = tid; q < DESC_BINS * 64; q += blockDim.x) basis[q] = p.basis[q];
   for (int q = tid; q < DS_ROWS * DESC_BINS; q += blockDim.x) hist[q] = 0.f;
   for (int q = tid; q < g.N; q += blockDim.x)
     pos[q] = make_float4((float)x[sidx(j, 0, q, 3, g.Ns)], (float)x[sidx(j, 1, q, 3, g.Ns)],
@@ -949,7 +949,8 @@ __global__ void __launch_bounds__(DS_WARPS * 32) k_desc(Geo g, DescPrm p, const 
   const float *hr = hist + rr;
   for (int b = 0; b < DESC_BINS; ++b) {
     const float h = hr[b * DS_ROWS];
-    const float4 u0 = *(const float4 *)(basis + b * 64 + f0), u1 = *(const float4 *)(basis + b * 64 + f0 + 4);
+    const float4 u0 = __ldg((const float4 *)(p.basis + b * 64 + f0));
+    const float4 u1 = __ldg((const float4 *)(p.basis + b * 64 + f0 + 4));
     acc[0] = fmaf(h, u0.x, acc[0]);
     acc[1] = fmaf(h, u0.y, acc[1]);
     acc[2] = fmaf(h, u0.z, acc[2]);
@@ -976,8 +977,7 @@ __global__ void __launch_bounds__(DS_WARPS * 32) k_desc(Geo g, DescPrm p, const 
 }
 
 static size_t desc_smem(int N) {
-  return sizeof(float) * ((size_t)DESC_BINS * 64 + DS_ROWS * DESC_BINS + DS_WARPS * DS_ROWS * 9) +
-         sizeof(float4) * (size_t)N;
+  return sizeof(float) * ((size_t)DS_ROWS * DESC_BINS + DS_WARPS * DS_ROWS * 9) + sizeof(float4) * (size_t)N;
 }
 
 cudaError_t desc_build(const Geo &g, const DescPrm &p, const double *x, uint8_t *ximg, float *V, float *raw,
