@@ -2081,22 +2081,25 @@ __device__ inline double2 phase_at(const double2 *ph, const Geo &g, int ns, int 
 // column) sums over the slice's particles, whose phase factors are staged in
 // shared memory in chunks, so no cross-thread reduction is needed.  With
 // P = sum e_xy c and Q = sum e_xy s:  S(+nz) = P + iQ,  S(-nz) = P - iQ.
-// Block = SK_COLS columns of one slice x SK_GROUPS particle groups: the 16
-// lanes of a column (adjacent in the warp) sum every 16th particle of each
-// staged chunk and combine by four shuffles at the end, so that a slice's
-// columns give 16 times as many warps to hide the FP64 latency and the grid
-// (12 blocks per slice at |n| <= 10) fills the SMs in even rounds.
-constexpr int SK_COLS = 16, SK_GROUPS = 16, SK_THREADS = SK_COLS * SK_GROUPS, SK_CHUNK = 64;
+// Block = COLS columns of one slice x GR particle groups.  For large slices
+// (N >= 256) the 16 lanes of a column (adjacent in the warp) sum every 16th
+// particle of each staged chunk and combine by four shuffles at the end, so
+// that a slice's columns give 16 times as many warps to hide the FP64
+// latency and the grid (12 blocks per slice at |n| <= 10) fills the SMs in
+// even rounds; small slices keep one thread per column.
+constexpr int SK_CHUNK = 64;
+constexpr int SK_BIG_N = 256;  // slices of at least this many particles use 16 groups
 
-template <int NS>
-__global__ void __launch_bounds__(SK_THREADS, 2) k_sk(Geo g, const double2 *__restrict__ ph,
-                                                   const int4 *__restrict__ cols, int ncol,
-                                                   double2 *__restrict__ S, int nk) {
+template <int NS, int COLS, int GR>
+__global__ void __launch_bounds__(COLS * GR, COLS * GR >= 256 ? 2 : 1) k_sk(Geo g, const double2 *__restrict__ ph,
+                                                                       const int4 *__restrict__ cols, int ncol,
+                                                                       double2 *__restrict__ S, int nk) {
+  constexpr int SK_THREADS = COLS * GR, SK_GROUPS = GR;
   // staged phases of SK_CHUNK particles: x, y, z factors for n = 0..NS
   __shared__ double2 sp[3][NS + 1][SK_CHUNK];
   const int j = blockIdx.y;
   const int gq = threadIdx.x & (SK_GROUPS - 1);
-  const int ci = blockIdx.x * SK_COLS + threadIdx.x / SK_GROUPS;
+  const int ci = blockIdx.x * COLS + threadIdx.x / SK_GROUPS;
   const bool live = ci < ncol;
   const int4 c = live ? cols[ci] : make_int4(0, 0, 1, 0);
   const int ax = col_nx(c), ay = c.y < 0 ? -c.y : c.y;
@@ -2131,7 +2134,7 @@ __global__ void __launch_bounds__(SK_THREADS, 2) k_sk(Geo g, const double2 *__re
       }
     }
   }
-  // the column's 16 lanes, pairwise in a fixed order
+  // the column's lanes, pairwise in a fixed order
 #pragma unroll
   for (int o = 1; o < SK_GROUPS; o <<= 1) {
     s0r += __shfl_xor_sync(FULL, s0r, o);
@@ -2347,11 +2350,17 @@ static cudaError_t structure_factors(const Geo &g, const Recip &r, const double 
   cudaError_t e = XK_LAUNCHED();
   if (e != cudaSuccess) return e;
   const int nc = r.ncol;
-  dim3 grid((nc + SK_COLS - 1) / SK_COLS, g.P);
   {
     XK_PROF("sk");
-    DISPATCH_NS(r.nsum, k_sk<NS><<<grid, SK_THREADS, 0, st>>>(g, (const double2 *)r.phase,
-                                                             (const int4 *)r.kvec, nc, (double2 *)r.S, r.nk));
+    if (g.N >= SK_BIG_N) {
+      dim3 grid((nc + 15) / 16, g.P);
+      DISPATCH_NS(r.nsum, (k_sk<NS, 16, 16><<<grid, 256, 0, st>>>(g, (const double2 *)r.phase,
+                                                                  (const int4 *)r.kvec, nc, (double2 *)r.S, r.nk)));
+    } else {
+      dim3 grid((nc + 63) / 64, g.P);
+      DISPATCH_NS(r.nsum, (k_sk<NS, 64, 1><<<grid, 64, 0, st>>>(g, (const double2 *)r.phase,
+                                                                (const int4 *)r.kvec, nc, (double2 *)r.S, r.nk)));
+    }
   }
   return XK_LAUNCHED();
 }
@@ -3362,14 +3371,15 @@ __device__ inline float2 cmulf(float2 a, float2 b) {
 }
 
 // structure factors as k_sk, FP32 products accumulated in double-float
-template <int NS>
-__global__ void __launch_bounds__(SK_THREADS) k_sk32(Geo g, const float2 *__restrict__ ph,
-                                                     const int4 *__restrict__ cols, int ncol,
-                                                     double2 *__restrict__ S, int nk) {
+template <int NS, int COLS, int GR>
+__global__ void __launch_bounds__(COLS * GR) k_sk32(Geo g, const float2 *__restrict__ ph,
+                                                   const int4 *__restrict__ cols, int ncol,
+                                                   double2 *__restrict__ S, int nk) {
+  constexpr int SK_THREADS = COLS * GR, SK_GROUPS = GR;
   __shared__ float2 sp[3][NS + 1][SK_CHUNK];
   const int j = blockIdx.y;
   const int gq = threadIdx.x & (SK_GROUPS - 1);
-  const int ci = blockIdx.x * SK_COLS + threadIdx.x / SK_GROUPS;
+  const int ci = blockIdx.x * COLS + threadIdx.x / SK_GROUPS;
   const bool live = ci < ncol;
   const int4 c = live ? cols[ci] : make_int4(0, 0, 1, 0);
   const int ax = col_nx(c), ay = c.y < 0 ? -c.y : c.y;
@@ -3401,7 +3411,7 @@ __global__ void __launch_bounds__(SK_THREADS) k_sk32(Geo g, const float2 *__rest
       }
     }
   }
-  // the column's 16 lanes, pairwise in a fixed order (both parts of each sum)
+  // the column's lanes, pairwise in a fixed order (both parts of each sum)
   auto comb = [](DF &v, int o) {
     const float h = __shfl_xor_sync(FULL, v.hi, o), lo = __shfl_xor_sync(FULL, v.lo, o);
     v.add(h);
@@ -3529,15 +3539,21 @@ cudaError_t recip_force32(const Geo &g, const Recip &r, const double *x, double 
   e = XK_LAUNCHED();
   if (e != cudaSuccess) return e;
   const int nc = r.ncol;
-  dim3 sgrid((nc + SK_COLS - 1) / SK_COLS, g.P);
   dim3 tgrid((nc + 7) / 8, g.P), tblk(r.nsum + 1, 8);
   dim3 grid((g.N + 127) / 128, g.P);
   const size_t smem = sizeof(float2) * nc * (4 * r.nsum + 1);
   float2 *T32 = (float2 *)r.T;
   DISPATCH_NS(r.nsum, {
     {
+      // 16 groups per column for large slices at small |n| (registers stay
+      // low); one thread per column otherwise
       XK_PROF("sk32");
-      k_sk32<NS><<<sgrid, SK_THREADS, 0, st>>>(g, ph32, (const int4 *)r.kvec, nc, (double2 *)r.S, r.nk);
+      if (g.N >= SK_BIG_N && NS <= 6)
+        k_sk32<NS, 16, 16><<<dim3((nc + 15) / 16, g.P), 256, 0, st>>>(g, ph32, (const int4 *)r.kvec, nc,
+                                                                     (double2 *)r.S, r.nk);
+      else
+        k_sk32<NS, 64, 1><<<dim3((nc + 63) / 64, g.P), 64, 0, st>>>(g, ph32, (const int4 *)r.kvec, nc,
+                                                                   (double2 *)r.S, r.nk);
     }
     {
       XK_PROF("recip_tables32");
