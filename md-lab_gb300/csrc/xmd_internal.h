@@ -74,7 +74,8 @@ struct SimDev {
   DevBuf th, vt, Q;
   DevBuf cf, c0, c2;
   DevBuf stage;    // AoS records on the device
-  DevBuf cstage;   // chain records on their way back to the host
+  DevBuf cstage;   // chain records on their way to and from the host
+  DevBuf upflags;  // results of the upload checks (equal masses, one-DOF chains)
   DevBuf scratch;  // partial sums of pair / exchange / reduction kernels
   DevBuf fex;      // exchange spring forces computed on the side stream
   DevBuf xscr;     // partial sums of the exchange forces (side stream)

@@ -263,6 +263,32 @@ __global__ void k_chains(Geo g, int L, int nf, bool fast, bool to_dev, unsigned 
   }
 }
 
+// Checks of freshly uploaded host records, so that the host need not walk
+// them: flags[0] stays nonzero when every particle has the first one's mass
+// (bit pattern), flags[1] when every chain record has f == 1.  The caller
+// sets both flags nonzero before the launch.
+__global__ void k_upload_checks(const unsigned char *__restrict__ prec, int np, size_t pbytes,
+                                const unsigned char *__restrict__ crec, int nc, size_t cbytes, int *flags) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  bool mass_ok = true, f_ok = true;
+  if (t < np)
+    mass_ok = *(const long long *)(prec + (size_t)t * pbytes) == *(const long long *)prec;
+  if (t < nc) f_ok = *(const int *)(crec + (size_t)t * cbytes) == 1;
+  if (!__all_sync(FULL, mass_ok) && (threadIdx.x & 31) == 0) atomicAnd(&flags[0], 0);
+  if (!__all_sync(FULL, f_ok) && (threadIdx.x & 31) == 0) atomicAnd(&flags[1], 0);
+}
+
+cudaError_t upload_checks(const unsigned char *prec, int np, size_t pbytes, const unsigned char *crec, int nc,
+                          size_t cbytes, int *flags, cudaStream_t st) {
+  const int n = np > nc ? np : nc;
+  if (n <= 0) return cudaSuccess;
+  {
+    XK_PROF("upload_checks");
+    k_upload_checks<<<cdiv(n, 256), 256, 0, st>>>(prec, np, pbytes, crec, nc, cbytes, flags);
+  }
+  return XK_LAUNCHED();
+}
+
 cudaError_t chains_to_dev(const Geo &g, int L, int nf, bool fast, const unsigned char *rec,
                           size_t rb, double *th, double *vt, double *Q, cudaStream_t st) {
   {

@@ -67,6 +67,11 @@ cudaError_t soa_to_aos(const Geo &g, double *aos, const double *x, const double 
 // chains: host records {int f; double theta[L], vtheta[L], Q[L]} of rec_bytes each
 cudaError_t chains_to_dev(const Geo &g, int L, int nf, bool fast, const unsigned char *rec,
                           size_t rec_bytes, double *th, double *vt, double *Q, cudaStream_t st);
+// flags[0] := 0 unless every particle record (np of pbytes, mass first) has
+// the first one's mass; flags[1] := 0 unless every chain record (nc of
+// cbytes, int f first) has f == 1.  Flags start nonzero.
+cudaError_t upload_checks(const unsigned char *prec, int np, size_t pbytes, const unsigned char *crec, int nc,
+                          size_t cbytes, int *flags, cudaStream_t st);
 // whole records back, f included: 1 for one-DOF chains, cf[c] for grouped ones
 cudaError_t chains_to_host(const Geo &g, int L, int nf, bool fast, unsigned char *rec,
                            size_t rec_bytes, const double *th, const double *vt,

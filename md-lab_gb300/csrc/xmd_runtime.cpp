@@ -216,7 +216,7 @@ static void free_sim(SimDev *d) {
       v.erase(std::remove(v.begin(), v.end(), d), v.end());
     }
   for (DevBuf *b : {&d->x, &d->v, &d->f, &d->m, &d->th, &d->vt, &d->Q, &d->cf, &d->c0, &d->c2,
-                    &d->stage, &d->cstage, &d->scratch, &d->fex, &d->xscr})
+                    &d->stage, &d->cstage, &d->upflags, &d->scratch, &d->fex, &d->xscr})
     release(*b);
 }
 
@@ -329,25 +329,31 @@ int sim_device(md_simulation_t_x *sim, SimDev **out) {
   XMD_CUDA(cudaMemsetAsync(d->v.p, 0, S * 8, st));
   XMD_CUDA(cudaMemsetAsync(d->f.p, 0, S * 8, st));
   XMD_CUDA(cudaMemsetAsync(d->m.p, 0, (size_t)g.P * g.Ns * 8, st));
-  // chains: one DOF each in the reference's order -> slot order
+  // particle and chain records go up to their stages; whether all masses
+  // are equal and all chains have one DOF is checked there on the device
+  // (walking 13 MB of records on one host core took longer than the copies)
   d->nf = sim->Nf;
   d->L = L;
-  bool fast = sim->nhcs != nullptr && sim->Nf == D * sim->N;
-  for (int i = 0; fast && i < sim->Nf; ++i) fast = sim->nhcs[i].f == 1;
-  d->fast_chains = fast;
+  const int nchain = sim->nhcs ? sim->Nf : 0;
   const size_t pbytes = sizeof(md_particle_t_x) * (size_t)sim->N;
-  const size_t cbytes = sizeof(md_nhc_t_x) * (size_t)(sim->nhcs ? sim->Nf : 0);
-  XMD_TRY(reserve(d->stage, pbytes > cbytes ? pbytes : cbytes));
-  d->uniform_mass = true;
-  d->mass0 = sim->particles[0].m;
-  for (int b = 1; b < sim->N; ++b)
-    if (sim->particles[b].m != d->mass0) {
-      d->uniform_mass = false;
-      break;
-    }
+  const size_t cbytes = sizeof(md_nhc_t_x) * (size_t)nchain;
+  XMD_TRY(reserve(d->stage, pbytes));
+  if (cbytes) XMD_TRY(reserve(d->cstage, cbytes));
+  XMD_TRY(reserve(d->upflags, 2 * sizeof(int)));
+  XMD_CUDA(cudaMemsetAsync(d->upflags.p, 0xff, 2 * sizeof(int), st));
   XMD_CUDA(cudaMemcpyAsync(d->stage.p, sim->particles, pbytes, cudaMemcpyHostToDevice, st));
+  if (cbytes) XMD_CUDA(cudaMemcpyAsync(d->cstage.p, sim->nhcs, cbytes, cudaMemcpyHostToDevice, st));
+  XMD_CUDA(xk::upload_checks(d->stage.as<unsigned char>(), sim->N, sizeof(md_particle_t_x),
+                             d->cstage.as<unsigned char>(), nchain, sizeof(md_nhc_t_x), d->upflags.as<int>(), st));
   XMD_CUDA(xk::aos_to_soa(g, d->stage.as<double>(), d->x.as<double>(), d->v.as<double>(),
                           d->f.as<double>(), d->m.as<double>(), st));
+  int flags[2] = {0, 0};
+  XMD_CUDA(cudaMemcpyAsync(flags, d->upflags.p, sizeof flags, cudaMemcpyDeviceToHost, st));
+  XMD_CUDA(cudaStreamSynchronize(st));
+  d->uniform_mass = flags[0] != 0;
+  d->mass0 = sim->particles[0].m;
+  const bool fast = nchain > 0 && sim->Nf == D * sim->N && flags[1] != 0;
+  d->fast_chains = fast;
   if (sim->nhcs && sim->Nf > 0) {
     const size_t cs = fast ? S : (size_t)sim->Nf;
     XMD_TRY(reserve(d->th, cs * L * 8));
@@ -379,8 +385,7 @@ int sim_device(md_simulation_t_x *sim, SimDev **out) {
       XMD_CUDA(cudaMemcpyAsync(d->c2.p, c2.data(), sizeof(int) * sim->Nf, cudaMemcpyHostToDevice, st));
       XMD_CUDA(cudaStreamSynchronize(st));  // the vectors above go out of scope
     }
-    XMD_CUDA(cudaMemcpyAsync(d->stage.p, sim->nhcs, cbytes, cudaMemcpyHostToDevice, st));
-    XMD_CUDA(xk::chains_to_dev(g, L, sim->Nf, fast, d->stage.as<unsigned char>(), sizeof(md_nhc_t_x),
+    XMD_CUDA(xk::chains_to_dev(g, L, sim->Nf, fast, d->cstage.as<unsigned char>(), sizeof(md_nhc_t_x),
                                d->th.as<double>(), d->vt.as<double>(), d->Q.as<double>(), st));
   }
   d->valid = true;
