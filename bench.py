@@ -205,7 +205,7 @@ def cpu_step_estimate(cores, budget_s):
 # ---------------------------------------------------------------------
 def n_images(xcut=5.8):
     """expected real-space images per pair inside the cut-off alpha R < xcut
-    (5.8 in the FP64 kernels, 4.6 in the FP32 ones)"""
+    (5.8 in the FP64 kernels, 3.6 in the FP32 ones)"""
     box, _ = workload()
     rc = xcut / (ALPHA_L / box)
     return 4 / 3 * math.pi * rc ** 3 / box ** 3
@@ -246,7 +246,7 @@ def kernel_flops(name, nsum=NSUM):
         return pairs * (47.0 * n_images() + 39.0)
     if name == "pair_tiles32_ewald_real":
         pairs = P * N * (N - 1) / 2
-        return pairs * (47.0 * n_images(4.6) + 39.0)
+        return pairs * (47.0 * n_images(3.6) + 39.0)
     if name == "desc":
         # per ordered pair: 12 flop for the minimum-image distance, and for the
         # (4/3) pi (1/2)^3 = 52% inside rc = L/2 another 45 (cut-off weight,
