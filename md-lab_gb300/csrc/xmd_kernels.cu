@@ -1188,31 +1188,36 @@ cudaError_t fill_vb_signed(int N, double beta, double vi2, const double *ENk, co
 }
 
 // connection probabilities G[l][j]: md_pimd_x.c:2660-2673
-__global__ void k_fill_g(int N, double beta, double vi, const double *__restrict__ ENk,
+// G[l][j] (md_pimd_x.c:2588-2620); ln xi comes from the host and 1/l from
+// a host table, so an element costs one exp on the FP64 pipe
+__global__ void k_fill_g(int N, double beta, double vi, double lnvi, const double *__restrict__ ENk,
                          const double *__restrict__ VBN, const double *__restrict__ tmpV,
-                         double *__restrict__ G) {
-  const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (size_t)N * N) return;
-  const int l = (int)(t / N) + 1, j = (int)(t % N) + 1;  // 1-based
-  double gv;
-  if (j > l + 1)
-    gv = 0;
-  else if (j == l + 1)
-    gv = 1 - exp(-beta * (VBN[l] + tmpV[l] - VBN[N]));
-  else if (vi == 0.0 && l - j != 0)
-    gv = 0;
-  else if (vi == 0.0)
-    gv = exp(-beta * (VBN[j - 1] + ENk[dtri(l) + l - j] + tmpV[l] - VBN[N])) / l;
-  else
-    gv = exp(-beta * (VBN[j - 1] + ENk[dtri(l) + l - j] + tmpV[l] - VBN[N]) + (l - j) * log(vi)) / l;
-  G[t] = gv;
+                         const double *__restrict__ invl, double *__restrict__ G) {
+  const int l = blockIdx.y + 1;  // 1-based row
+  const double base = tmpV[l] - VBN[N];
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x + 1; j <= N; j += gridDim.x * blockDim.x) {
+    double gv;
+    if (j > l + 1)
+      gv = 0;
+    else if (j == l + 1)
+      gv = 1 - exp(-beta * (VBN[l] + base));
+    else if (vi == 0.0 && l - j != 0)
+      gv = 0;
+    else if (vi == 0.0)
+      gv = exp(-beta * (VBN[j - 1] + ENk[dtri(l) + l - j] + base)) * invl[l];
+    else
+      gv = exp(-beta * (VBN[j - 1] + ENk[dtri(l) + l - j] + base) + (l - j) * lnvi) * invl[l];
+    G[(size_t)(l - 1) * N + (j - 1)] = gv;
+  }
 }
 
 cudaError_t fill_g(int N, double beta, double vi, const double *ENk, const double *VBN,
-                   const double *tmpV, double *G, cudaStream_t st) {
+                   const double *tmpV, const double *lnn, double *G, cudaStream_t st) {
+  const double lnvi = vi != 0.0 ? log(vi) : 0.0;
+  dim3 grid((N + 255) / 256, N);
   {
     XK_PROF("fill_g");
-    k_fill_g<<<cdiv((size_t)N * N, 256), 256, 0, st>>>(N, beta, vi, ENk, VBN, tmpV, G);
+    k_fill_g<<<grid, 256, 0, st>>>(N, beta, vi, lnvi, ENk, VBN, tmpV, lnn + N + 1, G);
   }
   return XK_LAUNCHED();
 }

@@ -118,8 +118,9 @@ cudaError_t fill_vb_tv(int N, double beta, double vi, const double *ENk, const d
 // sign[n] = sign of Z'_n, n = 0..N
 cudaError_t fill_vb_signed(int N, double beta, double vi2, const double *ENk, const double *lnn, double *V2,
                            double *sign, double *rs, cudaStream_t st);
+// lnn: the host table of ln l then 1/l (2 (N+1) doubles)
 cudaError_t fill_g(int N, double beta, double vi, const double *ENk, const double *VBN,
-                   const double *tmpV, double *G, cudaStream_t st);
+                   const double *tmpV, const double *lnn, double *G, cudaStream_t st);
 // scratch: at least exch_scratch_doubles(g) doubles
 size_t exch_scratch_doubles(const Geo &g);
 cudaError_t exch_force(const Geo &g, const double *x, const double *m, double w2, int image,

@@ -52,6 +52,10 @@ struct md_gb300_ewald_model {
   int judged = 0;
   bool reverted = false;
   double last[4] = {NAN, NAN, NAN, NAN};
+  // the network's branch of a learned force call (descriptors and forward
+  // pass need only positions, so they run beside the truncated Ewald sums)
+  cudaStream_t ms = nullptr;
+  cudaEvent_t mfork = nullptr, mdone = nullptr;
 };
 
 typedef md_gb300_ewald_model Model;
@@ -155,8 +159,7 @@ static int both_sums(Model *M, md_pimd_t_x *pimd, SimDev *sd, PimdDev *pd) {
 }
 
 // descriptors and network output of the current configuration (live buffers)
-static int predict(Model *M, SimDev *sd) {
-  cudaStream_t st = stream();
+static int predict(Model *M, SimDev *sd, cudaStream_t st) {
   XMD_CUDA(xk::desc_build(sd->geo, M->dp, sd->x.as<double>(), M->lx.as<uint8_t>(), M->lv.as<float>(), nullptr, st));
   XMD_CUDA(xk::mlp_forward(dev_view(M), M->lx.as<uint8_t>(), tiles_of(M->N * M->P), M->ly.as<float4>(),
                            M->err.as<int>(), st));
@@ -224,7 +227,7 @@ static int judge_now(Model *M, md_pimd_t_x *pimd, SimDev *sd, PimdDev *pd, doubl
   if (capturing()) return fail(MD_GB_ERR_CAPTURE, "judging reads results back; not while capturing");
   cudaStream_t st = stream();
   XMD_TRY(both_sums(M, pimd, sd, pd));
-  XMD_TRY(predict(M, sd));
+  XMD_TRY(predict(M, sd, stream()));
   XMD_CUDA(xk::resid_apply(sd->geo, M->rp, M->ly.as<float4>(), M->lv.as<float>(), 1.0, nullptr, M->fp.as<double>(),
                            M->ep.as<double>(), st));
   XMD_TRY(zero(M->jacc));
@@ -274,6 +277,17 @@ int learned_pair_force(md_pimd_t_x *pimd, SimDev *sd, PimdDev *pd, const xk::Pai
   const double inv_mP = 1.0 / (sd->mass0 * pimd->P);
   const double *x = sd->x.as<double>();
   double *f = sd->f.as<double>();
+  // fork: the network's branch on its own stream, joined before its
+  // forces are added (graph capture records the fork and the join)
+  if (!M->ms) {
+    XMD_CUDA(cudaStreamCreateWithFlags(&M->ms, cudaStreamNonBlocking));
+    XMD_CUDA(cudaEventCreateWithFlags(&M->mfork, cudaEventDisableTiming));
+    XMD_CUDA(cudaEventCreateWithFlags(&M->mdone, cudaEventDisableTiming));
+  }
+  XMD_CUDA(cudaEventRecord(M->mfork, st));
+  XMD_CUDA(cudaStreamWaitEvent(M->ms, M->mfork, 0));
+  XMD_TRY(predict(M, sd, M->ms));
+  XMD_CUDA(cudaEventRecord(M->mdone, M->ms));
   if (md_gb300_get_precision_x() == MD_GB_PRECISION_MIXED) {
     XMD_CUDA(xk::recip_force32(sd->geo, M->cheap, x, inv_mP, f, st));
     XMD_CUDA(xk::pair_force32(sd->geo, prm, x, sd->m.as<double>(), f, scr, st));
@@ -281,7 +295,7 @@ int learned_pair_force(md_pimd_t_x *pimd, SimDev *sd, PimdDev *pd, const xk::Pai
     XMD_CUDA(xk::recip_force(sd->geo, M->cheap, x, inv_mP, f, st));
     XMD_CUDA(xk::pair_force(sd->geo, prm, x, sd->m.as<double>(), f, scr, st));
   }
-  XMD_TRY(predict(M, sd));
+  XMD_CUDA(cudaStreamWaitEvent(st, M->mdone, 0));
   XMD_CUDA(xk::resid_apply(sd->geo, M->rp, M->ly.as<float4>(), M->lv.as<float>(), inv_mP, f, nullptr, nullptr, st));
   return 0;
 }
@@ -299,7 +313,7 @@ int learned_recip_energy(md_pimd_t_x *pimd, SimDev *sd, double *acc, double *scr
   XMD_TRY(geometry_matches(M, sd));
   cudaStream_t st = stream();
   XMD_CUDA(xk::recip_energy(sd->geo, M->cheap, sd->x.as<double>(), acc, scr, st));
-  XMD_TRY(predict(M, sd));
+  XMD_TRY(predict(M, sd, stream()));
   XMD_CUDA(xk::resid_apply(sd->geo, M->rp, M->ly.as<float4>(), M->lv.as<float>(), 0.0, nullptr, M->fp.as<double>(),
                            M->ep.as<double>(), st));
   XMD_CUDA(xk::sum_particles(sd->geo, M->ep.as<double>(), 1.0 / M->P, acc, st));
@@ -332,6 +346,12 @@ void md_gb300_ewald_model_free_x(md_gb300_ewald_model_t_x *M) {
                     &M->ly,   &M->raw,  &M->fa,   &M->fb,    &M->ea,      &M->eb,   &M->fp,   &M->ep,   &M->jacc,
                     &M->rc_coef, &M->rc_cols, &M->rc_phase, &M->rc_S, &M->rc_T};
   for (DevBuf *b : bufs) release(*b);
+  if (M->ms) {
+    cudaStreamSynchronize(M->ms);
+    cudaStreamDestroy(M->ms);
+    cudaEventDestroy(M->mfork);
+    cudaEventDestroy(M->mdone);
+  }
   delete M;
 }
 

@@ -449,10 +449,14 @@ int pimd_device(md_pimd_t_x *pimd, SimDev **sd, PimdDev **pd) {
   XMD_TRY(reserve(d->G, (size_t)N * N * 8));
   XMD_TRY(reserve(d->linkt, (size_t)N * N * 8));
   {
-    std::vector<double> ln(N + 1, 0.0);
-    for (int l = 1; l <= N; ++l) ln[l] = log((double)l);
-    XMD_TRY(reserve(d->lnn, (size_t)(N + 1) * 8));
-    XMD_CUDA(cudaMemcpyAsync(d->lnn.p, ln.data(), (size_t)(N + 1) * 8, cudaMemcpyHostToDevice, stream()));
+    // ln l, then 1/l, for l = 0..N (entries 0 unused), host values
+    std::vector<double> ln(2 * (size_t)(N + 1), 0.0);
+    for (int l = 1; l <= N; ++l) {
+      ln[l] = log((double)l);
+      ln[N + 1 + l] = 1.0 / l;
+    }
+    XMD_TRY(reserve(d->lnn, 2 * (size_t)(N + 1) * 8));
+    XMD_CUDA(cudaMemcpyAsync(d->lnn.p, ln.data(), 2 * (size_t)(N + 1) * 8, cudaMemcpyHostToDevice, stream()));
     XMD_CUDA(cudaStreamSynchronize(stream()));
   }
   XMD_TRY(reserve(d->rec, 2 * xk::rec_scratch_doubles(N) * 8));

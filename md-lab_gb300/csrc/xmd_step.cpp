@@ -325,7 +325,7 @@ int md_pimd_fast_fill_force_VB_x(md_pimd_t_x *pimd, int image) {
     XMD_CUDA(xk::back_vb(N, pimd->beta, pimd->vi, pd->ENk.as<double>(), pd->lnn.as<double>(),
                          pd->tmpV.as<double>(), pd->rec.as<double>(), st));
   XMD_CUDA(xk::fill_g(N, pimd->beta, pimd->vi, pd->ENk.as<double>(), pd->VBN.as<double>(), pd->tmpV.as<double>(),
-                      pd->G.as<double>(), st));
+                      pd->lnn.as<double>(), pd->G.as<double>(), st));
   XMD_CUDA(cudaMemsetAsync(sd->fex.p, 0, sd->geo.slots() * sizeof(double), st));
   XMD_CUDA(xk::exch_force(sd->geo, sd->x.as<double>(), sd->m.as<double>(), pimd->omegaP * pimd->omegaP, image,
                           pd->G.as<double>(), sd->fex.as<double>(), scr, st));
