@@ -99,7 +99,11 @@ NoJoin::~NoJoin() { --t_nojoin; }
 int side_begin(cudaStream_t *out) {
   Side &sd = g_side[stream()];
   if (!sd.s) {
-    XMD_CUDA(cudaStreamCreateWithFlags(&sd.s, cudaStreamNonBlocking));
+    // highest priority: the exchange chain is latency-bound and should get
+    // SMs as soon as any free up
+    int lo = 0, hi = 0;
+    XMD_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+    XMD_CUDA(cudaStreamCreateWithPriority(&sd.s, cudaStreamNonBlocking, hi));
     XMD_CUDA(cudaEventCreateWithFlags(&sd.fork, cudaEventDisableTiming));
     XMD_CUDA(cudaEventCreateWithFlags(&sd.done, cudaEventDisableTiming));
   }
