@@ -1867,11 +1867,6 @@ size_t pair_scratch_doubles(const Geo &g) {
   return a > b ? a : b;
 }
 
-// SMs the persistent grids leave free, so that the exchange recursion (two
-// single-block solves on the side stream) need not wait for them to finish
-constexpr int SIDE_SMS = 2;
-static int grid_sms(int sms) { return sms > 8 * SIDE_SMS ? sms - SIDE_SMS : sms; }
-
 // resident blocks of a kernel of 256 threads (the persistent grid), or fewer
 // when the warps needed run out
 template <class K>
@@ -1883,7 +1878,7 @@ static int resident_grid(K kernel, size_t warps_needed, int &occ, int &sms) {
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, 256, 0) != cudaSuccess || occ < 1) occ = 1;
     if (sms < 1) sms = 1;
   }
-  const size_t need = (warps_needed + 7) / 8, full = (size_t)grid_sms(sms) * occ;
+  const size_t need = (warps_needed + 7) / 8, full = (size_t)sms * occ;
   return (int)(need < full ? need : full);
 }
 
@@ -3321,7 +3316,7 @@ static cudaError_t launch_pair32(const Geo &g, const P32 &q, const float *x, con
     if (e != cudaSuccess) return e;
     if (occ[wpb] < 1) occ[wpb] = 1;
   }
-  const size_t need = ((size_t)jobs * g.P + wpb - 1) / wpb, full = (size_t)grid_sms(sms) * occ[wpb];
+  const size_t need = ((size_t)jobs * g.P + wpb - 1) / wpb, full = (size_t)sms * occ[wpb];
   k_pair_tiles32<D, K><<<(int)(need < full ? need : full), wpb * 32, 0, st>>>(g, q, x, im, part, T, jobs);
   return cudaSuccess;
 }
