@@ -900,6 +900,8 @@ struct TriJob {
   const int *Me[2];
   double *out[2];
   double *sign;  // optional: sign of X_i (signed weights), forward direction only
+  double *Bm[2];  // inverses of the 32 x 32 diagonal blocks (unsigned weights):
+  int *Be[2];     // [chunk][32][32] mantissas and exponents
 };
 
 // Extended-range dot product of row i of the weights with the unknowns over
@@ -1128,10 +1130,226 @@ __global__ void __launch_bounds__(TS_WARPS * 32) k_tri_solve(int N, double beta,
 }
 
 // scratch: mantissas (ntri(N) doubles) then exponents (ntri(N) ints)
-size_t rec_scratch_doubles(int N) { return ntri(N) + (ntri(N) + 1) / 2 + 1; }
+size_t rec_scratch_doubles(int N) {
+  const size_t nch = (N + TS_CHUNK - 1) / TS_CHUNK;
+  return ntri(N) + (ntri(N) + 1) / 2 + 1 + nch * TS_CHUNK * TS_CHUNK * 3 / 2;
+}
 
 // directions first .. first + count - 1 of job
+// ---- block-inverse form (unsigned weights) ----------------------------
+// Within chunk c (rows i0 .. i0+31) the system reads X = R + A X with A the
+// strictly lower 32 x 32 block of the weights and R the rows' sums over all
+// earlier unknowns, so X = B R with B = (I - A)^-1 = I + A + A^2 + ...  B
+// depends only on the weights: k_block_inv computes it for every chunk at
+// once (a warp per column, all chunks in parallel over the GPU), and the
+// solve then replaces the 32-step substitution by a 32-term product per row,
+// done by all warps.  With non-negative weights every term is non-negative,
+// so the extended-range sums have no cancellation.
+
+// (sum, E) of the warp's non-negative extended terms (pm, pe), nz marking
+// lanes with a term; E = EXT_NONE when none has
+__device__ inline void ext_warp_sum(bool nz, double pm, int pe, double &sum, int &E) {
+  int Em = nz ? pe : EXT_NONE;
+#pragma unroll
+  for (int o = 16; o; o >>= 1) {
+    const int oe = __shfl_xor_sync(FULL, Em, o);
+    Em = (Em == EXT_NONE || (oe != EXT_NONE && oe > Em)) ? oe : Em;
+  }
+  const double v = nz ? scale2(pm, pe - Em) : 0.0;
+  sum = warp_sum(v);
+  E = Em;
+}
+
+// B_c column s for every chunk c: grid (chunks x 4 column groups, directions),
+// 8 warps per block, warp w of group g takes column s = 8 g + w.  Lane t
+// holds B[t][s]; step r adds row r: B[r][s] = sum_{s<=t<r} A[r][t] B[t][s].
+__global__ void __launch_bounds__(256) k_block_inv(int N, TriJob job, int first) {
+  const int dir = first + blockIdx.y;
+  const double *__restrict__ Mm = job.Mm[dir];
+  const int *__restrict__ Me = job.Me[dir];
+  const int lane = threadIdx.x & 31;
+  const int c = blockIdx.x >> 2, s = ((blockIdx.x & 3) << 3) + (threadIdx.x >> 5);
+  const int i0 = 1 + c * TS_CHUNK;
+  double bm = lane == s ? 0.5 : 0.0;  // B[s][s] = 1 = 0.5 * 2^1
+  int be = lane == s ? 1 : 0;
+  for (int r = s + 1; r < TS_CHUNK && i0 + r <= N; ++r) {
+    const bool in = lane >= s && lane < r;
+    const double am = in ? Mm[moff(i0 + r, i0 + lane)] : 0.0;
+    const int ae = in ? Me[moff(i0 + r, i0 + lane)] : 0;
+    const bool nz = in && __double_as_longlong(am) != 0 && __double_as_longlong(bm) != 0;
+    double sm;
+    int se;
+    ext_warp_sum(nz, am * bm, ae + be, sm, se);
+    if (lane == r) {
+      bm = se == EXT_NONE ? 0.0 : sm;
+      be = se == EXT_NONE ? 0 : se;
+      norm2(bm, be);
+    }
+  }
+  double *Bm = job.Bm[dir] + (size_t)c * TS_CHUNK * TS_CHUNK;
+  int *Be = job.Be[dir] + (size_t)c * TS_CHUNK * TS_CHUNK;
+  Bm[lane * TS_CHUNK + s] = lane >= s ? bm : 0.0;
+  Be[lane * TS_CHUNK + s] = lane >= s ? be : 0;
+}
+
+// One block per direction, 16 warps, three phases per chunk c:
+//   U: R_r = (row r's sum over the unknowns before chunk c-1) + (its terms
+//      over chunk c-1's 32 unknowns), one warp per row;
+//   B: X_{i0+r} = sum_s B[r][s] R_s, one warp per row;
+//   next: chunk c+1's weights against chunk c and its B block are staged in
+//      shared memory, and its rows' sums over the unknowns before chunk c
+//      are taken (the long dot products, split over the warps).
+__global__ void __launch_bounds__(TS_WARPS * 32) k_tri_solve_b(int N, double beta, TriJob job, int first) {
+  const int backward = first + blockIdx.x;
+  const double *__restrict__ Mm = job.Mm[backward];
+  const int *__restrict__ Me = job.Me[backward];
+  const double *__restrict__ Bgm = job.Bm[backward];
+  const int *__restrict__ Bge = job.Be[backward];
+  double *__restrict__ out = job.out[backward];
+  extern __shared__ double sh[];
+  double *Um = sh;                          // [TS_CHUNK][TS_LD] next chunk vs the chunk before it
+  double *Bsm = Um + TS_CHUNK * TS_LD;      // [TS_CHUNK][TS_LD] the chunk's B block
+  double *Pm = Bsm + TS_CHUNK * TS_LD;      // [TS_CHUNK] sums over the unknowns before the previous chunk
+  double *Rm = Pm + TS_CHUNK;               // [TS_CHUNK] right-hand sides of the chunk
+  double *Xm = Rm + TS_CHUNK;               // N+1
+  int *Ue = (int *)(Xm + N + 1);            // [TS_CHUNK][TS_LD]
+  int *Bse = Ue + TS_CHUNK * TS_LD;         // [TS_CHUNK][TS_LD]
+  int *Pe = Bse + TS_CHUNK * TS_LD;         // [TS_CHUNK]
+  int *Re = Pe + TS_CHUNK;                  // [TS_CHUNK]
+  int *Xe = Re + TS_CHUNK;                  // N+1
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  // stage chunk n0's B block and its rows' weights against columns c0..c0+31
+  auto stage = [&](int n0, int c0) {
+    const int cc = (n0 - 1) / TS_CHUNK;
+    for (int q = threadIdx.x; q < 2 * TS_CHUNK * TS_CHUNK; q += blockDim.x) {
+      const int which = q / (TS_CHUNK * TS_CHUNK), rs = q % (TS_CHUNK * TS_CHUNK);
+      const int r = rs / TS_CHUNK, k = rs % TS_CHUNK, i = n0 + r;
+      const size_t o = (size_t)r * TS_LD + k;
+      if (which == 0) {
+        const bool in = i <= N && c0 >= 0;
+        Um[o] = in ? Mm[moff(i, c0 + k)] : 0.0;
+        Ue[o] = in ? Me[moff(i, c0 + k)] : 0;
+      } else {
+        Bsm[o] = i <= N ? Bgm[(size_t)cc * TS_CHUNK * TS_CHUNK + rs] : 0.0;
+        Bse[o] = i <= N ? Bge[(size_t)cc * TS_CHUNK * TS_CHUNK + rs] : 0;
+      }
+    }
+  };
+  if (threadIdx.x == 0) {
+    Xm[0] = 0.5;
+    Xe[0] = 1;
+  }
+  stage(1, -1);
+  __syncthreads();
+  // chunk 0: its rows against column 0 (X_0 = 1)
+  for (int r = w; r < TS_CHUNK; r += TS_WARPS) {
+    const int i = 1 + r;
+    double am = 0.0;
+    int E = 0;
+    if (i <= N) ext_dot(Mm + moff(i, 0), Me + moff(i, 0), Xm, Xe, 0, 1, lane, am, E);
+    if (lane == 0) {
+      double pm = 0.0;
+      int pe = 0;
+      if (i <= N) ext_acc(pm, pe, am, E);
+      Pm[r] = pm;
+      Pe[r] = pe;
+    }
+  }
+  __syncthreads();
+  for (int i0 = 1, c = 0; i0 <= N; i0 += TS_CHUNK, ++c) {
+    // U: right-hand sides
+    for (int r = w; r < TS_CHUNK; r += TS_WARPS) {
+      if (i0 + r > N) continue;  // warp-uniform
+      double pm = Pm[r];
+      int pe = Pe[r];
+      if (c > 0) {
+        const int col = i0 - TS_CHUNK + lane;
+        const size_t o = (size_t)r * TS_LD + lane;
+        const double mv = Um[o];
+        const bool nz = __double_as_longlong(mv) != 0 && __double_as_longlong(Xm[col]) != 0;
+        double sm;
+        int se;
+        ext_warp_sum(nz, mv * Xm[col], Ue[o] + Xe[col], sm, se);
+        if (lane == 0 && se != EXT_NONE) ext_acc(pm, pe, sm, se);
+      }
+      if (lane == 0) {
+        norm2(pm, pe);
+        Rm[r] = pm;
+        Re[r] = pe;
+      }
+    }
+    __syncthreads();
+    // B: the chunk's unknowns
+    for (int r = w; r < TS_CHUNK; r += TS_WARPS) {
+      const int i = i0 + r;
+      if (i > N) continue;  // warp-uniform
+      const size_t o = (size_t)r * TS_LD + lane;
+      const double bv = Bsm[o], rv = Rm[lane];
+      const bool nz = lane <= r && __double_as_longlong(bv) != 0 && __double_as_longlong(rv) != 0;
+      double sm;
+      int se;
+      ext_warp_sum(nz, bv * rv, Bse[o] + Re[lane], sm, se);
+      if (lane == 0) {
+        double xm = se == EXT_NONE ? 0.0 : sm;
+        int xe = se == EXT_NONE ? 0 : se;
+        norm2(xm, xe);
+        Xm[i] = xm;
+        Xe[i] = xe;
+      }
+    }
+    __syncthreads();
+    // next chunk: its weights against this chunk, its B block, and its rows'
+    // sums over the unknowns before this chunk
+    const int n0 = i0 + TS_CHUNK;
+    if (n0 <= N) {
+      stage(n0, i0);
+      for (int r = w; r < TS_CHUNK; r += TS_WARPS) {
+        const int i = n0 + r;
+        if (i > N) break;  // warp-uniform; later rows are out of range too
+        double am;
+        int E;
+        ext_dot(Mm + moff(i, 0), Me + moff(i, 0), Xm, Xe, 0, i0, lane, am, E);
+        if (lane == 0) {
+          double pm = 0.0;
+          int pe = 0;
+          ext_acc(pm, pe, am, E);
+          Pm[r] = pm;
+          Pe[r] = pe;
+        }
+      }
+    }
+    __syncthreads();
+  }
+  for (int i = threadIdx.x + 1; i <= N; i += blockDim.x) {
+    const double lnx = log(fabs(Xm[i])) + Xe[i] * LN2_HI + Xe[i] * LN2_LO;
+    out[backward ? N - i : i] = -lnx / beta;
+  }
+  if (threadIdx.x == 0) out[backward ? N : 0] = 0.0;
+}
+
 static cudaError_t tri_solve(int N, double beta, const TriJob &job, int first, int count, cudaStream_t st) {
+  if (!job.sign) {
+    // unsigned weights: diagonal-block inverses, then the block solve
+    const int nch = (N + TS_CHUNK - 1) / TS_CHUNK;
+    {
+      XK_PROF("block_inv");
+      k_block_inv<<<dim3(nch * 4, count), 256, 0, st>>>(N, job, first);
+    }
+    cudaError_t e = XK_LAUNCHED();
+    if (e != cudaSuccess) return e;
+    const size_t smem = (sizeof(double) + sizeof(int)) * (N + 1 + 2 * TS_CHUNK + 2 * TS_CHUNK * TS_LD) + 16;
+    static bool opted_b = false;
+    if (!opted_b) {
+      cudaError_t ea = cudaFuncSetAttribute(k_tri_solve_b, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+      if (ea != cudaSuccess) return ea;
+      opted_b = true;
+    }
+    {
+      XK_PROF(count == 2 ? "vb_tv_solve" : (first ? "tv_solve" : "vb_solve"));
+      k_tri_solve_b<<<count, TS_WARPS * 32, smem, st>>>(N, beta, job, first);
+    }
+    return XK_LAUNCHED();
+  }
   const size_t smem = (sizeof(double) + sizeof(int)) * (N + 1 + 2 * TS_CHUNK + 4 * TS_CHUNK * TS_LD) + 16;
   static bool opted = false;
   if (!opted) {
@@ -1148,6 +1366,13 @@ static cudaError_t tri_solve(int N, double beta, const TriJob &job, int first, i
 
 static TriJob tri_job(int N, double *rs_f, double *rs_b, double *VBN, double *tmpV) {
   TriJob j{};
+  const size_t boff = ntri(N) + (ntri(N) + 1) / 2 + 1;
+  const size_t nb = (size_t)((N + TS_CHUNK - 1) / TS_CHUNK) * TS_CHUNK * TS_CHUNK;
+  double *rs[2] = {rs_f, rs_b};
+  for (int d = 0; d < 2; ++d) {
+    j.Bm[d] = rs[d] ? rs[d] + boff : nullptr;
+    j.Be[d] = rs[d] ? (int *)(rs[d] + boff + nb) : nullptr;
+  }
   j.Mm[0] = rs_f;
   j.Me[0] = (const int *)(rs_f + ntri(N));
   j.out[0] = VBN;
