@@ -911,11 +911,43 @@ struct TriJob {
 // weights (xi = 0 beyond k = 1) are skipped by their bit pattern.  E is
 // EXT_NONE while a lane has no term.
 constexpr int EXT_NONE = -2147483647;
+
+// Warp sums of extended-range terms are taken in 64-bit fixed point on the
+// integer pipe: a warp-wide FP64 add holds GB300's FP64 pipe for many cycles,
+// and a five-level reduction of doubles cost more than the dot products
+// around it.  fx(v, d, FB): v * 2^d (d <= 0) as a signed integer with FB
+// fractional bits, built from the bit pattern (truncated); the caller keeps
+// 32 |v| 2^FB below 2^63.
+__device__ inline long long fx(double v, int d, int FB) {
+  const long long b = __double_as_longlong(v);
+  const int ex = (int)((b >> 52) & 0x7ff);
+  const long long sig = (b & 0xFFFFFFFFFFFFFLL) | (1LL << 52);
+  const int sh = ex - 1075 + FB + d;
+  const long long q = sh >= 0 ? (sig << sh) : (sh > -63 ? (sig >> -sh) : 0LL);
+  return ex == 0 ? 0LL : (b < 0 ? -q : q);
+}
+// q * 2^-FB as a double (truncated to 53 bits), by integer arithmetic
+__device__ inline double fx_to_double(long long q, int FB) {
+  if (q == 0) return 0.0;
+  const bool neg = q < 0;
+  const unsigned long long u = neg ? (unsigned long long)(-q) : (unsigned long long)q;
+  const int top = 63 - __clzll((long long)u);
+  const unsigned long long m = top > 52 ? (u >> (top - 52)) : (u << (52 - top));
+  const long long bits = ((long long)(neg ? 1 : 0) << 63) | ((long long)(top - FB + 1023) << 52) |
+                         (long long)(m & 0xFFFFFFFFFFFFFULL);
+  return __longlong_as_double(bits);
+}
+__device__ inline long long warp_sum_ll(long long q) {
+#pragma unroll
+  for (int o = 16; o; o >>= 1) q += __shfl_xor_sync(FULL, q, o);
+  return q;
+}
+
 __device__ inline void ext_dot(const double *__restrict__ mr, const int *__restrict__ er, const double *Xm,
                                const int *Xe, int j0, int j1, int lane, double &am_out, int &E_out) {
   double am = 0.0;
   int E = EXT_NONE;
-  for (int jb = j0 + lane; jb < j1; jb += 128) {
+  for (int jb = j0 + lane; jb - lane < j1; jb += 128) {
     double mv[4], xv[4];
     int ev[4], xe[4];
 #pragma unroll
@@ -929,6 +961,7 @@ __device__ inline void ext_dot(const double *__restrict__ mr, const int *__restr
     }
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
+      if (jb - lane + 32 * u >= j1) break;  // warp-uniform: no lane has this slot
       const bool nz = __double_as_longlong(mv[u]) != 0;
       const int te = ev[u] + xe[u];
       const int ne = (nz && (E == EXT_NONE || te > E)) ? te : E;
@@ -938,14 +971,18 @@ __device__ inline void ext_dot(const double *__restrict__ mr, const int *__restr
       E = ne;
     }
   }
+  // each lane's sum normalised to a mantissa below 1, so that 57 fractional
+  // bits keep the 32-lane sum below 2^62 and resolve it to 2^-51 of itself
+  if (E != EXT_NONE) norm2(am, E);
+  if (__double_as_longlong(am) == 0) E = EXT_NONE;
   int Em = E;
 #pragma unroll
   for (int o = 16; o; o >>= 1) {
     const int oe = __shfl_xor_sync(FULL, Em, o);
     Em = (Em == EXT_NONE || (oe != EXT_NONE && oe > Em)) ? oe : Em;
   }
-  const double v = (E == EXT_NONE) ? 0.0 : scale2(am, E - Em);
-  am_out = warp_sum(v);
+  const long long q = warp_sum_ll(E == EXT_NONE ? 0LL : fx(am, E - Em, 57));
+  am_out = fx_to_double(q, 57);
   E_out = Em;
 }
 
@@ -1149,14 +1186,14 @@ size_t rec_scratch_doubles(int N) {
 // (sum, E) of the warp's non-negative extended terms (pm, pe), nz marking
 // lanes with a term; E = EXT_NONE when none has
 __device__ inline void ext_warp_sum(bool nz, double pm, int pe, double &sum, int &E) {
+  if (nz) norm2(pm, pe);  // mantissa below 1 (see ext_dot)
   int Em = nz ? pe : EXT_NONE;
 #pragma unroll
   for (int o = 16; o; o >>= 1) {
     const int oe = __shfl_xor_sync(FULL, Em, o);
     Em = (Em == EXT_NONE || (oe != EXT_NONE && oe > Em)) ? oe : Em;
   }
-  const double v = nz ? scale2(pm, pe - Em) : 0.0;
-  sum = warp_sum(v);
+  sum = fx_to_double(warp_sum_ll(nz ? fx(pm, pe - Em, 57) : 0LL), 57);
   E = Em;
 }
 
