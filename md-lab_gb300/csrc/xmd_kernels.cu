@@ -943,15 +943,16 @@ __device__ inline long long warp_sum_ll(long long q) {
   return q;
 }
 
+constexpr int XD_SLOTS = 4;  // columns per lane per pass (loads in flight against L2 latency)
 __device__ inline void ext_dot(const double *__restrict__ mr, const int *__restrict__ er, const double *Xm,
                                const int *Xe, int j0, int j1, int lane, double &am_out, int &E_out) {
   double am = 0.0;
   int E = EXT_NONE;
-  for (int jb = j0 + lane; jb - lane < j1; jb += 128) {
-    double mv[4], xv[4];
-    int ev[4], xe[4];
+  for (int jb = j0 + lane; jb - lane < j1; jb += 32 * XD_SLOTS) {
+    double mv[XD_SLOTS], xv[XD_SLOTS];
+    int ev[XD_SLOTS], xe[XD_SLOTS];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
+    for (int u = 0; u < XD_SLOTS; ++u) {
       const int j = jb + 32 * u;
       const bool ok = j < j1;
       mv[u] = ok ? mr[j] : 0.0;
@@ -960,7 +961,7 @@ __device__ inline void ext_dot(const double *__restrict__ mr, const int *__restr
       xe[u] = ok ? Xe[j] : 0;
     }
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
+    for (int u = 0; u < XD_SLOTS; ++u) {
       if (jb - lane + 32 * u >= j1) break;  // warp-uniform: no lane has this slot
       const bool nz = __double_as_longlong(mv[u]) != 0;
       const int te = ev[u] + xe[u];
@@ -1207,12 +1208,22 @@ __global__ void __launch_bounds__(256) k_block_inv(int N, TriJob job, int first)
   const int lane = threadIdx.x & 31;
   const int c = blockIdx.x >> 2, s = ((blockIdx.x & 3) << 3) + (threadIdx.x >> 5);
   const int i0 = 1 + c * TS_CHUNK;
+  // the chunk's block A[r][t] = M_{i0+r, i0+t} (t < r) staged once per block
+  __shared__ double Am[TS_CHUNK][TS_LD];
+  __shared__ int Ae[TS_CHUNK][TS_LD];
+  for (int q = threadIdx.x; q < TS_CHUNK * TS_CHUNK; q += blockDim.x) {
+    const int r = q / TS_CHUNK, t = q % TS_CHUNK;
+    const bool in = t < r && i0 + r <= N;
+    Am[r][t] = in ? Mm[moff(i0 + r, i0 + t)] : 0.0;
+    Ae[r][t] = in ? Me[moff(i0 + r, i0 + t)] : 0;
+  }
+  __syncthreads();
   double bm = lane == s ? 0.5 : 0.0;  // B[s][s] = 1 = 0.5 * 2^1
   int be = lane == s ? 1 : 0;
   for (int r = s + 1; r < TS_CHUNK && i0 + r <= N; ++r) {
     const bool in = lane >= s && lane < r;
-    const double am = in ? Mm[moff(i0 + r, i0 + lane)] : 0.0;
-    const int ae = in ? Me[moff(i0 + r, i0 + lane)] : 0;
+    const double am = in ? Am[r][lane] : 0.0;
+    const int ae = in ? Ae[r][lane] : 0;
     const bool nz = in && __double_as_longlong(am) != 0 && __double_as_longlong(bm) != 0;
     double sm;
     int se;
@@ -1236,7 +1247,9 @@ __global__ void __launch_bounds__(256) k_block_inv(int N, TriJob job, int first)
 //   next: chunk c+1's weights against chunk c and its B block are staged in
 //      shared memory, and its rows' sums over the unknowns before chunk c
 //      are taken (the long dot products, split over the warps).
-__global__ void __launch_bounds__(TS_WARPS * 32) k_tri_solve_b(int N, double beta, TriJob job, int first) {
+constexpr int TSB_WARPS = 32;  // one warp per row of a chunk in every phase
+
+__global__ void __launch_bounds__(TSB_WARPS * 32) k_tri_solve_b(int N, double beta, TriJob job, int first) {
   const int backward = first + blockIdx.x;
   const double *__restrict__ Mm = job.Mm[backward];
   const int *__restrict__ Me = job.Me[backward];
@@ -1279,7 +1292,7 @@ __global__ void __launch_bounds__(TS_WARPS * 32) k_tri_solve_b(int N, double bet
   stage(1, -1);
   __syncthreads();
   // chunk 0: its rows against column 0 (X_0 = 1)
-  for (int r = w; r < TS_CHUNK; r += TS_WARPS) {
+  for (int r = w; r < TS_CHUNK; r += TSB_WARPS) {
     const int i = 1 + r;
     double am = 0.0;
     int E = 0;
@@ -1295,7 +1308,7 @@ __global__ void __launch_bounds__(TS_WARPS * 32) k_tri_solve_b(int N, double bet
   __syncthreads();
   for (int i0 = 1, c = 0; i0 <= N; i0 += TS_CHUNK, ++c) {
     // U: right-hand sides
-    for (int r = w; r < TS_CHUNK; r += TS_WARPS) {
+    for (int r = w; r < TS_CHUNK; r += TSB_WARPS) {
       if (i0 + r > N) continue;  // warp-uniform
       double pm = Pm[r];
       int pe = Pe[r];
@@ -1317,7 +1330,7 @@ __global__ void __launch_bounds__(TS_WARPS * 32) k_tri_solve_b(int N, double bet
     }
     __syncthreads();
     // B: the chunk's unknowns
-    for (int r = w; r < TS_CHUNK; r += TS_WARPS) {
+    for (int r = w; r < TS_CHUNK; r += TSB_WARPS) {
       const int i = i0 + r;
       if (i > N) continue;  // warp-uniform
       const size_t o = (size_t)r * TS_LD + lane;
@@ -1340,7 +1353,7 @@ __global__ void __launch_bounds__(TS_WARPS * 32) k_tri_solve_b(int N, double bet
     const int n0 = i0 + TS_CHUNK;
     if (n0 <= N) {
       stage(n0, i0);
-      for (int r = w; r < TS_CHUNK; r += TS_WARPS) {
+      for (int r = w; r < TS_CHUNK; r += TSB_WARPS) {
         const int i = n0 + r;
         if (i > N) break;  // warp-uniform; later rows are out of range too
         double am;
@@ -1383,7 +1396,7 @@ static cudaError_t tri_solve(int N, double beta, const TriJob &job, int first, i
     }
     {
       XK_PROF(count == 2 ? "vb_tv_solve" : (first ? "tv_solve" : "vb_solve"));
-      k_tri_solve_b<<<count, TS_WARPS * 32, smem, st>>>(N, beta, job, first);
+      k_tri_solve_b<<<count, TSB_WARPS * 32, smem, st>>>(N, beta, job, first);
     }
     return XK_LAUNCHED();
   }
