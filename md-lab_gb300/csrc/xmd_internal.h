@@ -72,6 +72,7 @@ struct SimDev {
   double mass0 = 1.0;
   DevBuf x, v, f, m;
   DevBuf th, vt, Q;
+  DevBuf iQ;       // 1/Q of one-DOF chains
   DevBuf cf, c0, c2;
   DevBuf stage;    // AoS records on the device
   DevBuf cstage;   // chain records on their way to and from the host

@@ -322,15 +322,34 @@ cudaError_t chains_to_host(const Geo &g, int L, int nf, bool fast, unsigned char
 template <int L>
 struct ChainState {
   double th[L], vt[L], Q[L];
+  double iQ[L];  // 1/Q (one-DOF chains): multiplications instead of FP64 divisions
 };
 
-template <int L>
+// md_simulation_x.c:599-613; INV: divide by multiplying with the stored 1/Q
+// (a double division is a multi-instruction sequence on the slow FP64 pipe)
+template <int L, bool INV = false>
 __device__ inline void chain_forces(const ChainState<L> &c, double kin, double cfv, double kT,
                                     double *nhf) {
-  // md_simulation_x.c:599-613
-  nhf[0] = (kin - cfv * kT) / c.Q[0];
+  nhf[0] = INV ? (kin - cfv * kT) * c.iQ[0] : (kin - cfv * kT) / c.Q[0];
 #pragma unroll
-  for (int j = 1; j < L; ++j) nhf[j] = (c.Q[j - 1] * c.vt[j - 1] * c.vt[j - 1] - kT) / c.Q[j];
+  for (int j = 1; j < L; ++j) {
+    const double num = c.Q[j - 1] * c.vt[j - 1] * c.vt[j - 1] - kT;
+    nhf[j] = INV ? num * c.iQ[j] : num / c.Q[j];
+  }
+}
+
+// iQ[s] = 1/Q[s] for the n entries of the one-DOF chains' Q
+__global__ void k_inv_q(size_t n, const double *__restrict__ Q, double *__restrict__ iQ) {
+  const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) iQ[t] = Q[t] != 0.0 ? 1.0 / Q[t] : 0.0;
+}
+
+cudaError_t inv_q(size_t n, const double *Q, double *iQ, cudaStream_t st) {
+  {
+    XK_PROF("inv_q");
+    k_inv_q<<<cdiv(n, 256), 256, 0, st>>>(n, Q, iQ);
+  }
+  return XK_LAUNCHED();
 }
 
 template <int L>
@@ -355,8 +374,8 @@ __global__ void __launch_bounds__(256) k_nhc_fast(Geo g, int half, double *__res
                                                   const double *__restrict__ f,
                                                   const double *__restrict__ m,
                                                   double *__restrict__ th, double *__restrict__ vt,
-                                                  const double *__restrict__ Q, double kT,
-                                                  double h) {
+                                                  const double *__restrict__ Q, const double *__restrict__ iQ,
+                                                  double kT, double h) {
   const size_t S = g.slots();
   const size_t s = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= S) return;
@@ -370,24 +389,25 @@ __global__ void __launch_bounds__(256) k_nhc_fast(Geo g, int half, double *__res
     c.th[i] = th[i * S + s];
     c.vt[i] = vt[i * S + s];
     c.Q[i] = Q[i * S + s];
+    c.iQ[i] = iQ[i * S + s];
   }
   const double mass = m[(size_t)j * g.Ns + l];
   double vv = v[s];
   const double F = f[s];
   double nhf[L];
-  if (half == 1) chain_forces<L>(c, mass * vv * vv, 1.0, kT, nhf);
+  if (half == 1) chain_forces<L, true>(c, mass * vv * vv, 1.0, kT, nhf);
   // thermostatted half kick: md_simulation_x.c:674-678
   const double ek = exp(-0.25 * h * c.vt[0]);
   vv = vv * (ek * ek) + 0.5 * h * F * ek;
 #pragma unroll
   for (int k = 1; k <= M2; ++k) c.th[2 * k - 2] = c.th[2 * k - 2] + h * c.vt[2 * k - 2] / 2;
-  if (half == 2) chain_forces<L>(c, mass * vv * vv, 1.0, kT, nhf);
+  if (half == 2) chain_forces<L, true>(c, mass * vv * vv, 1.0, kT, nhf);
   chain_odd<L>(c, h, nhf);
   if (half == 1) {
     x[s] = x[s] + h * vv;  // drift: md_simulation_x.c:684-689
 #pragma unroll
     for (int k = 1; k <= M2; ++k) c.th[2 * k - 1] = c.th[2 * k - 1] + h * c.vt[2 * k - 1];
-    chain_forces<L>(c, mass * vv * vv, 1.0, kT, nhf);
+    chain_forces<L, true>(c, mass * vv * vv, 1.0, kT, nhf);
 #pragma unroll
     for (int k = 1; k <= M2; ++k)
       {
@@ -502,7 +522,7 @@ cudaError_t nhc_vv3(const Geo &g, int half, const Chains &c, double *x, double *
     {
       XK_PROF("nhc_fast");
       DISPATCH_D(g.D, DISPATCH_L(c.L, k_nhc_fast<D, LL><<<cdiv(S, 256), 256, 0, st>>>(
-                                          g, half, x, v, f, m, c.th, c.vt, c.Q, kT, h)));
+                                          g, half, x, v, f, m, c.th, c.vt, c.Q, c.iQ, kT, h)));
     }
   } else {
     {

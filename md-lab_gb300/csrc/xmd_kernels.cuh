@@ -82,6 +82,7 @@ struct Chains {
   bool fast;            // one DOF per chain, chains in slot order
   int L, nf;            // chain length, number of chains
   double *th, *vt, *Q;  // [L][S] (fast) or [L][nf] (grouped)
+  const double *iQ;     // fast: 1/Q, same layout (inv_q)
   const int *cf;        // grouped: nhcs[i].f
   const int *c0;        // grouped: first DOF (reference numbering)
   const int *c2;        // grouped: number of DOFs updated
@@ -89,6 +90,8 @@ struct Chains {
 };
 cudaError_t nhc_vv3(const Geo &g, int half, const Chains &c, double *x, double *v,
                     const double *f, const double *m, double kT, double h, cudaStream_t st);
+// iQ[s] = 1/Q[s] (0 where Q = 0) for the n entries of the one-DOF chains
+cudaError_t inv_q(size_t n, const double *Q, double *iQ, cudaStream_t st);
 cudaError_t wrap_box(const Geo &g, double *x, cudaStream_t st);
 cudaError_t zero(double *p, size_t n, cudaStream_t st);
 

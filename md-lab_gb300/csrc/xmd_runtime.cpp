@@ -219,7 +219,7 @@ static void free_sim(SimDev *d) {
       auto &v = kv.second.fex;
       v.erase(std::remove(v.begin(), v.end(), d), v.end());
     }
-  for (DevBuf *b : {&d->x, &d->v, &d->f, &d->m, &d->th, &d->vt, &d->Q, &d->cf, &d->c0, &d->c2,
+  for (DevBuf *b : {&d->x, &d->v, &d->f, &d->m, &d->th, &d->vt, &d->Q, &d->iQ, &d->cf, &d->c0, &d->c2,
                     &d->stage, &d->cstage, &d->upflags, &d->scratch, &d->fex, &d->xscr})
     release(*b);
 }
@@ -391,6 +391,10 @@ int sim_device(md_simulation_t_x *sim, SimDev **out) {
     }
     XMD_CUDA(xk::chains_to_dev(g, L, sim->Nf, fast, d->cstage.as<unsigned char>(), sizeof(md_nhc_t_x),
                                d->th.as<double>(), d->vt.as<double>(), d->Q.as<double>(), st));
+    if (fast) {
+      XMD_TRY(reserve(d->iQ, S * L * 8));
+      XMD_CUDA(xk::inv_q(S * L, d->Q.as<double>(), d->iQ.as<double>(), st));
+    }
   }
   d->valid = true;
   return 0;

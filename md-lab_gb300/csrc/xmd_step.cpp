@@ -75,6 +75,7 @@ static xk::Chains chains_of(SimDev *sd) {
   c.th = sd->th.as<double>();
   c.vt = sd->vt.as<double>();
   c.Q = sd->Q.as<double>();
+  c.iQ = sd->iQ.as<double>();
   c.cf = sd->cf.as<int>();
   c.c0 = sd->c0.as<int>();
   c.c2 = sd->c2.as<int>();
