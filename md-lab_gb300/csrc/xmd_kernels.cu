@@ -962,6 +962,20 @@ __device__ inline long long warp_sum_ll(long long q) {
   for (int o = 16; o; o >>= 1) q += __shfl_xor_sync(FULL, q, o);
   return q;
 }
+// warp sum of arbitrary finite doubles on the integer pipe: every lane's
+// value in 57-bit fixed point relative to the largest lane's binade, summed
+// exactly, rounded once (truncation) to 53 bits; the result reaches every lane
+__device__ inline double warp_sum_fx(double v) {
+  const int ex = (int)((__double_as_longlong(v) >> 52) & 0x7ff);
+  int em = ex;
+#pragma unroll
+  for (int o = 16; o; o >>= 1) em = max(em, __shfl_xor_sync(FULL, em, o));
+  if (em == 0) return 0.0;  // all zero (subnormals do not occur in these sums)
+  const long long q = warp_sum_ll(fx(v, 1022 - em, 57));
+  if (q == 0) return 0.0;
+  const double r = fx_to_double(q, 57);  // value 2^(1022 - em) too large
+  return __longlong_as_double(__double_as_longlong(r) + ((long long)(em - 1022) << 52));
+}
 
 constexpr int XD_SLOTS = 4;  // columns per lane per pass (loads in flight against L2 latency)
 __device__ inline void ext_dot(const double *__restrict__ mr, const int *__restrict__ er, const double *Xm,
@@ -2985,7 +2999,7 @@ __global__ void __launch_bounds__(TS_WARPS * 32) k_lin_solve(int N, const double
       for (int r = w; r < TS_CHUNK; r += TS_WARPS) {
         if (i0 + r > N) continue;  // warp-uniform
         double v = U[((size_t)buf * TS_CHUNK + r) * TS_LD + lane] * X[col];
-        v = warp_sum(v);
+        v = warp_sum_fx(v);
         if (lane == 0) Psc[r] += v;
       }
       __syncthreads();
@@ -3018,7 +3032,7 @@ __global__ void __launch_bounds__(TS_WARPS * 32) k_lin_solve(int N, const double
           v1 = fma(prow[j + 32], X[j + 32], v1);
         }
         if (j < i0) v0 = fma(prow[j], X[j], v0);
-        const double v = warp_sum(v0 + v1);
+        const double v = warp_sum_fx(v0 + v1);
         if (lane == 0) Ps[(buf ^ 1) * TS_CHUNK + r] = cvec[i] + v;
       }
     }
