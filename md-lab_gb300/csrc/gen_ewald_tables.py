@@ -24,7 +24,7 @@ import mpmath as mp
 import numpy as np
 
 mp.mp.dps = 40
-W, NINT, DEG = 0.0625, 98, 8
+W, NINT, DEG = 0.015625, 373, 6
 XMAX = (NINT - 0.5) * W
 
 

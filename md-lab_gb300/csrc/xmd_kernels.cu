@@ -1781,6 +1781,7 @@ cudaError_t trap_energy(const Geo &g, const TrapPrm &p, const double *x, const d
 // ===================================================================
 
 __constant__ double c_ew_h[EW_NINT][EW_DEG + 1] = EW_H_INIT;
+constexpr size_t EW_TAB_BYTES = sizeof(double) * 2 * EW_NINT * (EW_DEG + 1);
 __constant__ double c_ew_erfc[EW_NINT][EW_DEG + 1] = EW_ERFC_INIT;
 
 // Force F(dx) (times the pair's strength, before the 1/m and 1/P factors)
@@ -1963,7 +1964,7 @@ __global__ void __launch_bounds__(256, 2) k_pair_tiles(Geo g, PairPrm p,
                                                     const double *__restrict__ m,
                                                     double *__restrict__ out, int T, int jobs) {
   // Ewald polynomial tables staged in shared memory (lanes index them freely)
-  __shared__ double stab[KIND == PAIR_EWALD_REAL ? 2 * EW_NINT * (EW_DEG + 1) : 1];
+  extern __shared__ double stab[];  // Ewald: the two tables (EW_TAB_BYTES of dynamic shared memory)
   if (KIND == PAIR_EWALD_REAL) {
     for (int i = threadIdx.x; i < 2 * EW_NINT * (EW_DEG + 1); i += blockDim.x)
       stab[i] = i < EW_NINT * (EW_DEG + 1) ? (&c_ew_h[0][0])[i] : (&c_ew_erfc[0][0])[i - EW_NINT * (EW_DEG + 1)];
@@ -2086,7 +2087,7 @@ __global__ void __launch_bounds__(256, 2) k_pair_cross(Geo ga, Geo gb, PairPrm p
                                                     const double *__restrict__ ma, const double *__restrict__ xb,
                                                     const double *__restrict__ mb, double *__restrict__ outa,
                                                     double *__restrict__ outb, int TA, int TB) {
-  __shared__ double stab[KIND == PAIR_EWALD_REAL ? 2 * EW_NINT * (EW_DEG + 1) : 1];
+  extern __shared__ double stab[];  // Ewald: the two tables (EW_TAB_BYTES of dynamic shared memory)
   if (KIND == PAIR_EWALD_REAL) {
     for (int i = threadIdx.x; i < 2 * EW_NINT * (EW_DEG + 1); i += blockDim.x)
       stab[i] = i < EW_NINT * (EW_DEG + 1) ? (&c_ew_h[0][0])[i] : (&c_ew_erfc[0][0])[i - EW_NINT * (EW_DEG + 1)];
@@ -2179,12 +2180,13 @@ size_t pair_scratch_doubles(const Geo &g) {
 // resident blocks of a kernel of 256 threads (the persistent grid), or fewer
 // when the warps needed run out
 template <class K>
-static int resident_grid(K kernel, size_t warps_needed, int &occ, int &sms) {
+static int resident_grid(K kernel, size_t warps_needed, int &occ, int &sms, size_t dyn = 0) {
   if (!occ) {
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, 256, 0) != cudaSuccess || occ < 1) occ = 1;
+    if (dyn > 48 * 1024) cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, 256, dyn) != cudaSuccess || occ < 1) occ = 1;
     if (sms < 1) sms = 1;
   }
   const size_t need = (warps_needed + 7) / 8, full = (size_t)sms * occ;
@@ -2194,7 +2196,8 @@ static int resident_grid(K kernel, size_t warps_needed, int &occ, int &sms) {
 template <int D, int KIND, bool ENERGY>
 static int pair_grid(size_t warps_needed) {
   static int occ = 0, sms = 0;
-  return resident_grid(k_pair_tiles<D, KIND, ENERGY>, warps_needed, occ, sms);
+  return resident_grid(k_pair_tiles<D, KIND, ENERGY>, warps_needed, occ, sms,
+                       KIND == PAIR_EWALD_REAL ? EW_TAB_BYTES : 0);
 }
 
 template <int D, bool ENERGY>
@@ -2230,7 +2233,7 @@ static cudaError_t pair_launch(const Geo &g, const PairPrm &p, const double *x, 
       if (D != 3) return cudaErrorInvalidValue;
       {
         XK_PROF("pair_tiles_ewald_real");
-        k_pair_tiles<D, PAIR_EWALD_REAL, ENERGY><<<pair_grid<D, PAIR_EWALD_REAL, ENERGY>(warps), 256, 0, st>>>(g, p, x, m, out, T, jobs);
+        k_pair_tiles<D, PAIR_EWALD_REAL, ENERGY><<<pair_grid<D, PAIR_EWALD_REAL, ENERGY>(warps), 256, EW_TAB_BYTES, st>>>(g, p, x, m, out, T, jobs);
       }
       break;
     default:
@@ -2281,9 +2284,10 @@ static cudaError_t cross_launch(const Geo &ga, const Geo &gb, const PairPrm &p, 
                                 const double *xb, const double *mb, double *outa, double *outb, int TA, int TB,
                                 cudaStream_t st) {
   static int occ = 0, sms = 0;
-  const int grid = resident_grid(k_pair_cross<D, KIND, ENERGY>, (size_t)TA * TB * ga.P, occ, sms);
+  const size_t dyn = KIND == PAIR_EWALD_REAL ? EW_TAB_BYTES : 0;
+  const int grid = resident_grid(k_pair_cross<D, KIND, ENERGY>, (size_t)TA * TB * ga.P, occ, sms, dyn);
   XK_PROF("pair_cross");
-  k_pair_cross<D, KIND, ENERGY><<<grid, 256, 0, st>>>(ga, gb, p, xa, ma, xb, mb, outa, outb, TA, TB);
+  k_pair_cross<D, KIND, ENERGY><<<grid, 256, dyn, st>>>(ga, gb, p, xa, ma, xb, mb, outa, outb, TA, TB);
   return XK_LAUNCHED();
 }
 
