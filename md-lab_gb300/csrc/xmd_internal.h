@@ -100,6 +100,7 @@ struct PimdDev {
   double rc_alpha = 0, rc_qs = 0, rc_box[3] = {0, 0, 0};
   int rc_nk = 0;
   int rc_ncol = 0;  // kept wave-vector columns
+  int rc_tsz = 0;   // entries of their compact force tables
   double rc_csum = 0;
 };
 

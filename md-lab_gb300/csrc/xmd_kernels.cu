@@ -2185,7 +2185,8 @@ static int resident_grid(K kernel, size_t warps_needed, int &occ, int &sms, size
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (dyn > 48 * 1024) cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+    // static plus dynamic shared memory above 48 KB needs the opt-in
+    if (dyn > 0) cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, 256, dyn) != cudaSuccess || occ < 1) occ = 1;
     if (sms < 1) sms = 1;
   }
@@ -2544,16 +2545,21 @@ __global__ void k_recip_tables(const int4 *__restrict__ cols, int ncol, const do
 // with e0 = sum_n c(n), so that sum_l e = sum_n c(n) (|S(n)|^2 - N).
 template <int NS, bool WITH_E = false>
 __global__ void __launch_bounds__(128) k_recip_force(Geo g, const double2 *__restrict__ ph,
-                                                     const int4 *__restrict__ cols, int ncol,
-                                                     const double2 *__restrict__ T, double scale,
+                                                     const int4 *__restrict__ cols, const int *__restrict__ toff,
+                                                     int ncol, const double2 *__restrict__ T, double scale,
                                                      double *__restrict__ f, double *__restrict__ e = nullptr,
                                                      double e0 = 0.0) {
   constexpr int NT = 4 * NS + 1;
+  // the slice's tables in shared memory, each column only up to its largest
+  // kept |nz| (toff: compact offsets), so that two blocks fit on an SM
   extern __shared__ double sm[];
   double2 *sT = (double2 *)sm;
   const int j = blockIdx.y;
   const double2 *Tj = T + (size_t)j * ncol * NT;
-  for (int q = threadIdx.x; q < ncol * NT; q += blockDim.x) sT[q] = Tj[q];
+  for (int ci = threadIdx.x >> 5; ci < ncol; ci += blockDim.x >> 5) {
+    const int n = toff[ci + 1] - toff[ci];
+    for (int q = threadIdx.x & 31; q < n; q += 32) sT[toff[ci] + q] = Tj[(size_t)ci * NT + q];
+  }
   __syncthreads();
   const int l = blockIdx.x * blockDim.x + threadIdx.x;
   if (l >= g.N) return;
@@ -2566,7 +2572,7 @@ __global__ void __launch_bounds__(128) k_recip_force(Geo g, const double2 *__res
     const int4 c = cols[ci];
     const int nzc = col_nz(c);
     const double2 exy = cmul(phase_at(ph, g, NS, j, 0, col_nx(c), l), phase_at(ph, g, NS, j, 1, c.y, l));
-    const double2 *t = sT + ci * NT;
+    const double2 *t = sT + toff[ci];
     double Ur = t[0].x, Ui = t[0].y, Vr = 0, Vi = 0;
 #pragma unroll
     for (int n = 1; n <= NS; ++n) {
@@ -2644,9 +2650,13 @@ cudaError_t recip_setup(const Geo &g, int ns, double alpha, double qs, Recip &r,
   });
   std::vector<int4> cd(kept.size());
   for (size_t i = 0; i < kept.size(); ++i) cd[i] = kept[i].second;
+  // compact table offsets of the kept columns (4 nzmax + 1 entries each)
+  std::vector<int> toff(kept.size() + 1, 0);
+  for (size_t i = 0; i < kept.size(); ++i) toff[i + 1] = toff[i] + 4 * kept[i].first + 1;
   r.nsum = ns;
   r.nk = nk;
   r.ncol = (int)cd.size();
+  r.tsz = toff.back();
   r.csum = 0;
   for (double c : coef) r.csum += c;
   cudaError_t e = cudaMemcpyAsync(r.coef, coef.data(), sizeof(double) * nk, cudaMemcpyHostToDevice, st);
@@ -2655,6 +2665,9 @@ cudaError_t recip_setup(const Geo &g, int ns, double alpha, double qs, Recip &r,
     e = cudaMemcpyAsync(r.kvec, cd.data(), sizeof(int4) * cd.size(), cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) return e;
   }
+  e = cudaMemcpyAsync(r.kvec + 4 * (size_t)(ns * (2 * ns + 1) + ns + 1), toff.data(), sizeof(int) * toff.size(),
+                      cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return e;
   // dropped vectors keep S = 0 (their c(n) = 0 multiplies them in the energies)
   if (r.S) {
     e = cudaMemsetAsync(r.S, 0, sizeof(double2) * (size_t)nk * g.P, st);
@@ -2663,7 +2676,12 @@ cudaError_t recip_setup(const Geo &g, int ns, double alpha, double qs, Recip &r,
   return cudaStreamSynchronize(st);
 }
 
-size_t recip_cols_ints(int ns) { return 4 * (size_t)(ns * (2 * ns + 1) + ns + 1); }
+size_t recip_cols_ints(int ns) { return 5 * (size_t)(ns * (2 * ns + 1) + ns + 1) + 1; }
+
+// compact table offsets behind the column table in the same buffer
+static const int *recip_toff(const Recip &r) {
+  return r.kvec + 4 * (size_t)(r.nsum * (2 * r.nsum + 1) + r.nsum + 1);
+}
 
 static int ncols(int ns) { return ns * (2 * ns + 1) + ns + 1; }
 
@@ -2717,7 +2735,7 @@ cudaError_t recip_force(const Geo &g, const Recip &r, const double *x, double in
   cudaError_t e = structure_factors(g, r, x, st);
   if (e != cudaSuccess) return e;
   const int nc = r.ncol;
-  const size_t smem = sizeof(double2) * nc * (4 * r.nsum + 1);
+  const size_t smem = sizeof(double2) * r.tsz;
   dim3 tgrid((nc + 7) / 8, g.P), tblk(r.nsum + 1, 8);
   dim3 grid((g.N + 127) / 128, g.P);
   DISPATCH_NS(r.nsum, {
@@ -2736,7 +2754,7 @@ cudaError_t recip_force(const Geo &g, const Recip &r, const double *x, double in
     }
     {
       XK_PROF("recip_force");
-      kf<<<grid, 128, smem, st>>>(g, (const double2 *)r.phase, (const int4 *)r.kvec, nc,
+      kf<<<grid, 128, smem, st>>>(g, (const double2 *)r.phase, (const int4 *)r.kvec, recip_toff(r), nc,
                                   (const double2 *)r.T, 4 * M_PI * inv_mP, f, nullptr, 0.0);
     }
   });
@@ -2750,7 +2768,7 @@ cudaError_t recip_force_energy(const Geo &g, const Recip &r, const double *x, do
   if (err != cudaSuccess) return err;
   const int nc = r.ncol;
   const double e0 = r.csum;
-  const size_t smem = sizeof(double2) * nc * (4 * r.nsum + 1);
+  const size_t smem = sizeof(double2) * r.tsz;
   dim3 tgrid((nc + 7) / 8, g.P), tblk(r.nsum + 1, 8);
   dim3 grid((g.N + 127) / 128, g.P);
   DISPATCH_NS(r.nsum, {
@@ -2768,8 +2786,8 @@ cudaError_t recip_force_energy(const Geo &g, const Recip &r, const double *x, do
     }
     {
       XK_PROF("recip_force_energy");
-      kf<<<grid, 128, smem, st>>>(g, (const double2 *)r.phase, (const int4 *)r.kvec, nc, (const double2 *)r.T,
-                                  4 * M_PI * scale, f, e, e0);
+      kf<<<grid, 128, smem, st>>>(g, (const double2 *)r.phase, (const int4 *)r.kvec, recip_toff(r), nc,
+                                  (const double2 *)r.T, 4 * M_PI * scale, f, e, e0);
     }
   });
   return XK_LAUNCHED();
@@ -2810,7 +2828,7 @@ static cudaError_t recip_tables_of(const Geo &g, const Recip &r, cudaStream_t st
 static cudaError_t recip_force_from(const Geo &g, const Recip &own, const double *T_other, double scale, double *f,
                                     cudaStream_t st) {
   const int nc = own.ncol;
-  const size_t smem = sizeof(double2) * nc * (4 * own.nsum + 1);
+  const size_t smem = sizeof(double2) * own.tsz;
   dim3 grid((g.N + 127) / 128, g.P);
   DISPATCH_NS(own.nsum, {
     auto kf = k_recip_force<NS>;
@@ -2821,8 +2839,8 @@ static cudaError_t recip_force_from(const Geo &g, const Recip &own, const double
       opted = true;
     }
     XK_PROF("recip_force");
-    kf<<<grid, 128, smem, st>>>(g, (const double2 *)own.phase, (const int4 *)own.kvec, nc, (const double2 *)T_other,
-                                scale, f, nullptr, 0.0);
+    kf<<<grid, 128, smem, st>>>(g, (const double2 *)own.phase, (const int4 *)own.kvec, recip_toff(own), nc,
+                                (const double2 *)T_other, scale, f, nullptr, 0.0);
   });
   return XK_LAUNCHED();
 }

@@ -198,9 +198,11 @@ struct Recip {
   int nsum;
   int nk;              // half-space wave vectors of the cube
   int ncol;            // kept columns (set by recip_setup)
+  int tsz;             // entries of the kept columns' force tables (compact, set by recip_setup)
   double *coef;        // [nk] s * exp(-pi^2 G^2/alpha^2) / (pi V G^2), 0 for a dropped vector
   int *kvec;           // kept columns, longest first: int4 (nx | nzmax << 8, ny, first nz,
-                       // offset of its first k); recip_cols_ints(nsum) ints
+                       // offset of its first k), then compact table offsets;
+                       // recip_cols_ints(nsum) ints
   double *phase;       // [P][3][nsum+1][Ns] complex
   double *S;           // [P][nk] complex
   double *T;           // [P][columns][2 nsum + 1] complex force tables

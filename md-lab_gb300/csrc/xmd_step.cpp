@@ -375,6 +375,7 @@ int xmd::ewald_tables(md_pimd_t_x *pimd, SimDev *sd, PimdDev *pd) {
   r.S = pd->rc_S.as<double>();
   XMD_CUDA(xk::recip_setup(g, ns, a, qs, r, stream()));
   pd->rc_ncol = r.ncol;
+  pd->rc_tsz = r.tsz;
   pd->rc_nsum = ns;
   pd->rc_alpha = a;
   pd->rc_qs = qs;
@@ -393,6 +394,7 @@ xk::Recip xmd::recip_of(PimdDev *pd) {
   r.nsum = pd->rc_nsum;
   r.nk = pd->rc_nk;
   r.ncol = pd->rc_ncol;
+  r.tsz = pd->rc_tsz;
   r.coef = pd->rc_coef.as<double>();
   r.kvec = pd->rc_cols.as<int>();
   r.phase = pd->rc_phase.as<double>();
