@@ -660,25 +660,47 @@ def run_gb300(args, dist, rank, ws):
         forms["learned_fp32"] = lform
         headline = "learned_fp32"
     H = forms[headline]
-    # e2e through the C ABI, host structs authoritative every step: the state
-    # is uploaded from page-locked host memory and read back, plus the
-    # estimator, every step (the headline form, model attached and judging)
+    # e2e through the C ABI, host structs authoritative every step: each step
+    # the state goes back to page-locked host memory (md_simulation_sync_host_x
+    # with read_only = 0) and up again (the step's first call, the periodic
+    # wrap, uploads it), the step replays as a captured graph, and the
+    # primitive estimator is read back.  The learned headline judges as in its
+    # timed run: every JUDGE_EVERY-th step is the converged step plus the FP64
+    # judgement, so the e2e run covers JUDGE_EVERY steps.
+    wrap = lambda: lib.check(lib.md_periodic_boundary_x(s.sim))  # noqa: E731
     if model is not None:
-        model.attach(s, judge_every=JUDGE_EVERY, force_tol=args.force_tol, energy_tol=args.energy_tol)
-    ke = min(args.steps, args.e2e_steps)
+        model.detach(s)
+        g_conv, _ = R.capture(step)
+        model.attach(s, judge_every=0)
+        g_main, _ = R.capture(step)
+        ke = JUDGE_EVERY
+    else:
+        g_conv, g_main = None, R.capture(step)[0]
+        ke = min(args.steps, args.e2e_steps)
     h2d = C.sizeof(lib.Particle) * N * P + C.sizeof(lib.Nhc) * s.sim.contents.Nf
     lib.check(lib.md_gb300_synchronize_x())
     barrier(dist)
     t0 = time.perf_counter()
-    for _ in range(ke):
+    dropped = False
+    for i in range(ke):
         if not lib.md_simulation_sync_host_x(s.sim, 0):  # device -> host, host authoritative
             raise RuntimeError(lib.err())
-        step()  # first call uploads the host state
+        wrap()  # uploads the host state (positions are already inside the box)
+        if g_conv is not None and (dropped or i % JUDGE_EVERY == 0):
+            lib.check(lib.md_gb300_graph_launch_x(g_conv, 1))
+            if not dropped:
+                j = model.judge(s)
+                dropped = j["force_err"] > args.force_tol or j["energy_err"] > args.energy_tol
+        else:
+            lib.check(lib.md_gb300_graph_launch_x(g_main, 1))
         lib.check(lib.md_pimd_calc_VBN_energy_x(s.pimd, s.stats))
         s.take_energy()  # estimator read
     if not lib.md_simulation_sync_host_x(s.sim, 1):
         raise RuntimeError(lib.err())
     e2e_s = max_over_ranks(dist, (time.perf_counter() - t0) / ke)
+    for g in (g_conv, g_main):
+        if g is not None:
+            lib.md_gb300_graph_free_x(g)
     kps = H.get("kernels_per_learned_step", H.get("kernels_per_step"))
     result = {"metric": METRIC, "value": H["value"], "unit": "bead-steps/s", "n_gpus": ws,
               "steps": H.get("steps_timed", args.steps), "warmup": args.warmup, "ms_per_step": H["ms_per_step"],

@@ -2968,18 +2968,22 @@ __global__ void k_est_weights(int N, double beta, double vi, const double *__res
     const double t = __shfl_xor_sync(FULL, mloc, o);
     mloc = t < mloc ? t : mloc;
   }
+  // each weight's exponential once: kept in the output row, normalised below
   double s1 = 0.0;
-  for (int k = lane + 1; k <= n; k += 32)
-    s1 += exp((k - 1) * lnvi - beta * (row[k - 1] + VBN[n - k]) + mloc);
-  s1 = warp_sum(s1);
+  for (int k = lane + 1; k <= n; k += 32) {
+    const double w = exp((k - 1) * lnvi - beta * (row[k - 1] + VBN[n - k]) + mloc);
+    prow[n - k] = w;
+    s1 += w;
+  }
+  s1 = warp_sum_fx(s1);
   const double inv = 1.0 / s1;
   double cs = 0.0;
   for (int k = lane + 1; k <= n; k += 32) {
-    const double pk = exp((k - 1) * lnvi - beta * (row[k - 1] + VBN[n - k]) + mloc) * inv;
+    const double pk = prow[n - k] * inv;
     prow[n - k] = pk;
     cs = fma(-pk, row2[k - 1], cs);
   }
-  cs = warp_sum(cs);
+  cs = warp_sum_fx(cs);
   if (lane == 0) cvec[n] = cs;
 }
 
