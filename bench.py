@@ -592,6 +592,32 @@ def two_species_form(lib, R, args, fp64_peak):
     return out
 
 
+def recursion_form(lib, R, args):
+    """The exchange recursions alone (V_B forward and tmpV backward, weights,
+    diagonal-block inverses and the block solve: md_pimd_fill_VB_x) against
+    N: microseconds per call, graph-replayed, on electron-gas-like random
+    positions (P = 8 beads; the recursion's cost does not depend on P)."""
+    import numpy as np
+    import xmd_x
+    out = {}
+    for n in (64, 128, 256, 512, 1024, 2048):
+        box = (4 * math.pi * n / 3) ** (1 / 3)
+        s = xmd_x.PimdSystem(lib, n, 8, XI, 1.0, box=box)
+        rng = np.random.default_rng(n)
+        x = (rng.uniform(0, box, (n, 1, 3)) + 0.05 * rng.standard_normal((n, 8, 3))).ravel()
+        s.set_state(m=np.ones(n * 8), x=x, v=np.zeros(n * 8 * 3))
+        lib.check(lib.md_pimd_fast_fill_ENk_x(s.pimd, 1))
+        fill = lambda: lib.check(lib.md_pimd_fill_VB_x(s.pimd))  # noqa: E731
+        fill()
+        g, _ = R.capture(fill)
+        ms, _, _ = R.time([R.launcher(g)] * 10, [R.launcher(g)] * 3)
+        lib.md_gb300_graph_free_x(g)
+        out[str(n)] = round(ms * 1e3, 1)
+        s.free()
+    return {"us_per_fill_VB": out,
+            "what": "md_pimd_fill_VB_x: both recursions (weights, block inverses, block solve), graph-replayed"}
+
+
 def run_gb300(args, dist, rank, ws):
     import torch
     import xmd_x
@@ -626,6 +652,8 @@ def run_gb300(args, dist, rank, ws):
                                "kernel_ms_per_step": {k: v[0] for k, v in plain_prof.items()},
                                "roofline": roofline(plain_prof, fp64_peak, "fp64")}
     fp32_peak = lib.md_gb300_fp32_peak_x()
+    if "recursion" in want:
+        forms["recursion_vs_N"] = recursion_form(lib, R, args)
     if "two" in want:
         forms["two_species_fp64"] = two_species_form(lib, R, args, lib.md_gb300_fp64_peak_x())
         xmd_x.set_potentials(lib, coul_s=1.0, alpha=ALPHA_L / workload()[0], nsum=NSUM)
@@ -756,8 +784,8 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--cpu-budget", type=float, default=8.0, help="seconds of CPU sample")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--forms", default="plain,two,mixed,ensemble,learned",
-                    help="forms to run (comma list of plain, two, mixed, ensemble, learned)")
+    ap.add_argument("--forms", default="plain,two,recursion,mixed,ensemble,learned",
+                    help="forms to run (comma list of plain, two, recursion, mixed, ensemble, learned)")
     ap.add_argument("--learn-configs", type=int, default=3125,
                     help="configurations collected for training (x P bead slices)")
     ap.add_argument("--learn-steps", type=int, default=3000)
