@@ -11,6 +11,7 @@
 // reproducible run to run).
 //
 // Reference counterparts (MD-Lab file:line) are cited at each kernel.
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -1411,6 +1412,243 @@ __global__ void __launch_bounds__(TSB_WARPS * 32) k_tri_solve_b(int N, double be
   if (threadIdx.x == 0) out[backward ? N : 0] = 0.0;
 }
 
+// The block solve spread over a thread-block cluster: one cluster of TSC_CL
+// blocks per direction.  Block 0 solves the chunks in order, as above: (U)
+// each row of chunk c adds its terms over chunk c-1's unknowns to its sum
+// over everything before, (B) X = B R.  The other blocks own the later rows'
+// running sums (chunk k >= 1 belongs to block 1 + (k-1) mod (TSC_CL-1)): in
+// iteration c each adds chunk c-1's unknowns, which block 0 wrote into its
+// shared memory, to the rows of its chunks after c, and the owner of chunk
+// c+1 writes that chunk's completed sums into block 0's shared memory.  So
+// the long sums, which held most of the FP64 work and the L2 loads, run on
+// seven more SMs beside block 0's solve, one cluster barrier per chunk, and
+// block 0 loads only the next chunk's two 32 x 32 blocks (issued before the
+// chunk's solve, stored after it).
+constexpr int TSC_CL = 8;      // blocks per cluster (the portable cluster size)
+constexpr int TSC_WARPS = 16;  // warps per block; warp w takes rows w and w + 16 of a chunk
+constexpr int TSC_HB = 4;      // rows a summing warp loads before it reduces them
+
+__device__ inline int tsc_slots(int nch) { return (nch - 1 + TSC_CL - 2) / (TSC_CL - 1); }
+
+__global__ void __cluster_dims__(TSC_CL, 1, 1) __launch_bounds__(TSC_WARPS * 32)
+    k_tri_solve_c(int N, double beta, TriJob job, int first) {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cl = cg::this_cluster();
+  const int rank = (int)cl.block_rank();
+  const int backward = first + blockIdx.y;
+  const double *__restrict__ Mm = job.Mm[backward];
+  const int *__restrict__ Me = job.Me[backward];
+  const double *__restrict__ Bgm = job.Bm[backward];
+  const int *__restrict__ Bge = job.Be[backward];
+  const int nch = (N + TS_CHUNK - 1) / TS_CHUNK;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  constexpr int BLK = TS_CHUNK * TS_LD;
+  constexpr int CC = TS_CHUNK * TS_CHUNK;
+  extern __shared__ double sh[];
+  // block 0
+  double *Um = sh;                 // [2][TS_CHUNK][TS_LD] a chunk's weights against the chunk before it
+  double *Bsm = Um + 2 * BLK;      // [2][TS_CHUNK][TS_LD] a chunk's B block
+  double *Pm = Bsm + 2 * BLK;      // [2][TS_CHUNK] rows' sums over the unknowns before the previous chunk
+  double *Rm = Pm + 2 * TS_CHUNK;  // [TS_CHUNK] right-hand sides of the chunk being solved
+  double *Xm = Rm + TS_CHUNK;      // N+1
+  int *Ue = (int *)(Xm + N + 1);   // [2][TS_CHUNK][TS_LD]
+  int *Bse = Ue + 2 * BLK;         // [2][TS_CHUNK][TS_LD]
+  int *Pe = Bse + 2 * BLK;         // [2][TS_CHUNK]
+  int *Re = Pe + 2 * TS_CHUNK;     // [TS_CHUNK]
+  int *Xe = Re + TS_CHUNK;         // N+1
+  // blocks 1..TSC_CL-1
+  const int slots = tsc_slots(nch);
+  double *Hxm = sh;                  // [2][TS_CHUNK] the last solved chunk's unknowns
+  double *Hpm = Hxm + 2 * TS_CHUNK;  // [slots][TS_CHUNK] running sums of the owned chunks' rows
+  int *Hxe = (int *)(Hpm + slots * TS_CHUNK);
+  int *Hpe = Hxe + 2 * TS_CHUNK;
+  if (rank == 0) {
+    if (threadIdx.x == 0) {
+      Xm[0] = 0.5;
+      Xe[0] = 1;
+    }
+    // chunk 0: no chunk before it; its rows' sums over column 0 (X_0 = 1)
+    for (int q = threadIdx.x; q < CC; q += blockDim.x) {
+      const int r = q / TS_CHUNK, k = q % TS_CHUNK;
+      const size_t o = (size_t)r * TS_LD + k;
+      const bool in = 1 + r <= N;
+      Um[o] = 0.0;
+      Ue[o] = 0;
+      Bsm[o] = in ? Bgm[q] : 0.0;
+      Bse[o] = in ? Bge[q] : 0;
+    }
+    if (threadIdx.x < TS_CHUNK) {
+      const int i = 1 + threadIdx.x;
+      double pm = i <= N ? Mm[moff(i, 0)] : 0.0;
+      int pe = i <= N ? Me[moff(i, 0)] : 0;
+      norm2(pm, pe);
+      Pm[threadIdx.x] = pm;
+      Pe[threadIdx.x] = pe;
+    }
+  } else {
+    for (int q = threadIdx.x; q < slots * TS_CHUNK; q += blockDim.x) {
+      const int k = rank + (q / TS_CHUNK) * (TSC_CL - 1), i = 1 + k * TS_CHUNK + q % TS_CHUNK;
+      const bool in = k < nch && i <= N;
+      double pm = in ? Mm[moff(i, 0)] : 0.0;
+      int pe = in ? Me[moff(i, 0)] : 0;
+      norm2(pm, pe);
+      Hpm[q] = pm;
+      Hpe[q] = pe;
+    }
+  }
+  cl.sync();  // every block has started and holds its initial sums
+  for (int c = 0; c < nch; ++c) {
+    const int i0 = 1 + c * TS_CHUNK, buf = c & 1;
+    if (rank == 0) {
+      // chunk c+1's blocks: loads issued now, stored after this chunk's solve
+      const int n0 = i0 + TS_CHUNK;
+      double su[2], sb[2];
+      int seu[2], seb[2];
+#pragma unroll
+      for (int t = 0; t < 2; ++t) {
+        const int rs = threadIdx.x + t * TSC_WARPS * 32;
+        const int r = rs / TS_CHUNK, k = rs % TS_CHUNK, i = n0 + r;
+        const bool in = c + 1 < nch && i <= N;
+        su[t] = in ? Mm[moff(i, i0 + k)] : 0.0;
+        seu[t] = in ? Me[moff(i, i0 + k)] : 0;
+        sb[t] = in ? Bgm[(size_t)(c + 1) * CC + rs] : 0.0;
+        seb[t] = in ? Bge[(size_t)(c + 1) * CC + rs] : 0;
+      }
+      // U: right-hand sides
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int r = w + h * TSC_WARPS;
+        if (i0 + r > N) continue;  // warp-uniform
+        double pm = Pm[buf * TS_CHUNK + r];
+        int pe = Pe[buf * TS_CHUNK + r];
+        if (c > 0) {
+          const int col = i0 - TS_CHUNK + lane;
+          const size_t o = (size_t)buf * BLK + (size_t)r * TS_LD + lane;
+          const double mv = Um[o];
+          const bool nz = __double_as_longlong(mv) != 0 && __double_as_longlong(Xm[col]) != 0;
+          double sm;
+          int se;
+          ext_warp_sum(nz, mv * Xm[col], Ue[o] + Xe[col], sm, se);
+          if (lane == 0 && se != EXT_NONE) ext_acc(pm, pe, sm, se);
+        }
+        if (lane == 0) {
+          norm2(pm, pe);
+          Rm[r] = pm;
+          Re[r] = pe;
+        }
+      }
+      __syncthreads();
+      // B: the chunk's unknowns, also into every other block's shared memory
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int r = w + h * TSC_WARPS, i = i0 + r;
+        if (i > N) continue;  // warp-uniform
+        const size_t o = (size_t)buf * BLK + (size_t)r * TS_LD + lane;
+        const double bv = Bsm[o], rv = Rm[lane];
+        const bool nz = lane <= r && __double_as_longlong(bv) != 0 && __double_as_longlong(rv) != 0;
+        double sm;
+        int se;
+        ext_warp_sum(nz, bv * rv, Bse[o] + Re[lane], sm, se);  // (sm, se) reach every lane
+        double xm = se == EXT_NONE ? 0.0 : sm;
+        int xe = se == EXT_NONE ? 0 : se;
+        norm2(xm, xe);
+        if (lane == 0) {
+          Xm[i] = xm;
+          Xe[i] = xe;
+        } else if (lane < TSC_CL) {
+          *cl.map_shared_rank(Hxm + buf * TS_CHUNK + r, lane) = xm;
+          *cl.map_shared_rank(Hxe + buf * TS_CHUNK + r, lane) = xe;
+        }
+      }
+#pragma unroll
+      for (int t = 0; t < 2; ++t) {
+        const int rs = threadIdx.x + t * TSC_WARPS * 32;
+        const size_t o = (size_t)(buf ^ 1) * BLK + (size_t)(rs / TS_CHUNK) * TS_LD + rs % TS_CHUNK;
+        Um[o] = su[t];
+        Ue[o] = seu[t];
+        Bsm[o] = sb[t];
+        Bse[o] = seb[t];
+      }
+    } else {
+      if (c >= 1) {
+        // chunk c-1's unknowns into the rows of the owned chunks after c
+        const int j0 = i0 - TS_CHUNK, pb = (c - 1) & 1;
+        const double xv = Hxm[pb * TS_CHUNK + lane];
+        const int xe = Hxe[pb * TS_CHUNK + lane];
+        const int t0 = c + 1 > rank ? (c + 1 - rank + TSC_CL - 2) / (TSC_CL - 1) : 0;
+        const int nq = 2 * (slots - t0);
+        for (int qb = 0; qb < nq; qb += TSC_HB) {
+          double mv[TSC_HB];
+          int me[TSC_HB];
+#pragma unroll
+          for (int u = 0; u < TSC_HB; ++u) {
+            const int q = qb + u, t = t0 + q / 2, k = rank + t * (TSC_CL - 1);
+            const int i = 1 + k * TS_CHUNK + w + (q & 1) * TSC_WARPS;
+            const bool ok = q < nq && k < nch && i <= N;
+            mv[u] = ok ? Mm[moff(i, j0 + lane)] : 0.0;
+            me[u] = ok ? Me[moff(i, j0 + lane)] : 0;
+          }
+#pragma unroll
+          for (int u = 0; u < TSC_HB; ++u) {
+            const int q = qb + u, t = t0 + q / 2, k = rank + t * (TSC_CL - 1);
+            const int r = w + (q & 1) * TSC_WARPS, i = 1 + k * TS_CHUNK + r;
+            if (!(q < nq && k < nch && i <= N)) continue;  // warp-uniform
+            const bool nz = __double_as_longlong(mv[u]) != 0 && __double_as_longlong(xv) != 0;
+            double sm;
+            int se;
+            ext_warp_sum(nz, mv[u] * xv, me[u] + xe, sm, se);
+            if (lane == 0 && se != EXT_NONE) ext_acc(Hpm[t * TS_CHUNK + r], Hpe[t * TS_CHUNK + r], sm, se);
+          }
+        }
+      }
+      // the owner of chunk c+1 hands its rows' sums (now over the unknowns
+      // before chunk c) to block 0
+      const int kn = c + 1;
+      if (kn < nch && 1 + (kn - 1) % (TSC_CL - 1) == rank && lane == 0) {
+        const int t = (kn - 1) / (TSC_CL - 1);
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const int r = w + h * TSC_WARPS;
+          if (1 + kn * TS_CHUNK + r > N) continue;
+          *cl.map_shared_rank(Pm + (kn & 1) * TS_CHUNK + r, 0) = Hpm[t * TS_CHUNK + r];
+          *cl.map_shared_rank(Pe + (kn & 1) * TS_CHUNK + r, 0) = Hpe[t * TS_CHUNK + r];
+        }
+      }
+    }
+    cl.sync();
+  }
+  if (rank == 0) {
+    double *__restrict__ out = job.out[backward];
+    for (int i = threadIdx.x + 1; i <= N; i += blockDim.x) {
+      const double lnx = log(fabs(Xm[i])) + Xe[i] * LN2_HI + Xe[i] * LN2_LO;
+      out[backward ? N - i : i] = -lnx / beta;
+    }
+    if (threadIdx.x == 0) out[backward ? N : 0] = 0.0;
+  }
+}
+
+// whether a cluster of the block solve fits on this device with `smem`
+// bytes of shared memory per block (checked once per larger size)
+static bool cluster_solve_fits(size_t smem) {
+  static size_t checked = 0;
+  static bool fits = false;
+  if (smem <= checked) return fits;
+  if (cudaFuncSetAttribute(k_tri_solve_c, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(TSC_CL, 2);
+  cfg.blockDim = dim3(TSC_WARPS * 32);
+  cfg.dynamicSmemBytes = smem;
+  int n = 0;
+  const cudaError_t e = cudaOccupancyMaxActiveClusters(&n, (void *)k_tri_solve_c, &cfg);
+  if (e != cudaSuccess) cudaGetLastError();
+  fits = e == cudaSuccess && n >= 2;
+  checked = smem;
+  return fits;
+}
+
 static cudaError_t tri_solve(int N, double beta, const TriJob &job, int first, int count, cudaStream_t st) {
   if (!job.sign) {
     // unsigned weights: diagonal-block inverses, then the block solve
@@ -1421,6 +1659,14 @@ static cudaError_t tri_solve(int N, double beta, const TriJob &job, int first, i
     }
     cudaError_t e = XK_LAUNCHED();
     if (e != cudaSuccess) return e;
+    const size_t smem_c = (sizeof(double) + sizeof(int)) * (N + 1 + 3 * TS_CHUNK + 4 * TS_CHUNK * TS_LD) + 16;
+    if (cluster_solve_fits(smem_c)) {
+      {
+        XK_PROF(count == 2 ? "vb_tv_solve" : (first ? "tv_solve" : "vb_solve"));
+        k_tri_solve_c<<<dim3(TSC_CL, count), TSC_WARPS * 32, smem_c, st>>>(N, beta, job, first);
+      }
+      return XK_LAUNCHED();
+    }
     const size_t smem = (sizeof(double) + sizeof(int)) * (N + 1 + 2 * TS_CHUNK + 2 * TS_CHUNK * TS_LD) + 16;
     static bool opted_b = false;
     if (!opted_b) {
