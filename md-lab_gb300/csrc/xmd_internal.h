@@ -85,7 +85,7 @@ struct SimDev {
 struct PimdDev {
   bool valid = false;  // ENk / ENk2 / VBN / Eint on the device authoritative
   DevBuf ENk, ENk2, Eint, VBN, tmpV, G;
-  DevBuf linkt;  // N x N bead-P -> bead-1 springs (scratch of the ENk fill)
+  DevBuf linkt;  // 2N doubles: ENk increments and their prefix sums (scratch of the ENk fill)
   DevBuf lnn;    // ln l for l = 0..N, then 1/l for l = 0..N (entries 0 unused), host values
   DevBuf vsign;  // V_B and signs of md_pimd_calc_vi_sign_x
   DevBuf sk_buf; // wave vectors and results of md_pimd_calc_sphere_Sk_structure_x

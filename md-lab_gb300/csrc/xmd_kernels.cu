@@ -580,11 +580,22 @@ __device__ inline double spring2(Geo g, const double *x, int ja, int la, int jb,
   return s;
 }
 
+// spring between bead P of particle a and bead 1 of particle b (0-based),
+// weighted by the mass of the bead-P end as in the reference.
+template <int D>
+__device__ inline double link(Geo g, const double *x, const double *m, double w2, int a, int b,
+                              int image) {
+  const int jP = g.P - 1;
+  return 0.5 * m[(size_t)jP * g.Ns + a] * w2 * spring2<D>(g, x, jP, a, 0, b, image);
+}
+
 // interior ring springs of particle l and the closing spring P -> 1: one
-// warp per particle, lanes over the beads, fixed-order warp sum
+// warp per particle, lanes over the beads, fixed-order warp sum.  Also
+// gl[l] = Eint[l] + link(l, l+1) (l < N-1), the increments whose prefix
+// sums k_enk_direct needs.
 template <int D>
 __global__ void k_eint(Geo g, const double *__restrict__ x, const double *__restrict__ m,
-                       double w2, int image, double *Eint, double *ENk) {
+                       double w2, int image, double *Eint, double *ENk, double *gl) {
   const int l = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (l >= g.N) return;
@@ -596,76 +607,84 @@ __global__ void k_eint(Geo g, const double *__restrict__ x, const double *__rest
     Eint[l] = res;
     const int jP = g.P - 1;
     ENk[dtri(l + 1)] = res + 0.5 * m[(size_t)jP * g.Ns + l] * w2 * spring2<D>(g, x, jP, l, 0, l, image);
+  } else if (lane == 1 && l + 1 < g.N) {
+    gl[l] = res + link<D>(g, x, m, w2, l, l + 1, image);
   }
 }
 
-// spring between bead P of particle a and bead 1 of particle b (0-based),
-// weighted by the mass of the bead-P end as in the reference.
-template <int D>
-__device__ inline double link(Geo g, const double *x, const double *m, double w2, int a, int b,
-                              int image) {
-  const int jP = g.P - 1;
-  return 0.5 * m[(size_t)jP * g.Ns + a] * w2 * spring2<D>(g, x, jP, a, 0, b, image);
-}
 
-// every such spring: lt[a*N + b] = link(a, b), one thread per (a, b)
-template <int D>
-__global__ void k_link_table(Geo g, const double *__restrict__ x, const double *__restrict__ m, double w2,
-                             int image, double *__restrict__ lt) {
-  const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (size_t)g.N * g.N) return;
-  const int a = (int)(t / g.N), b = (int)(t % g.N);
-  lt[t] = link<D>(g, x, m, w2, a, b, image);
-}
-
-// one warp per particle l (1-based row l >= 2): E_l^(k) for k = 2..l as an
-// inclusive scan of the increments
-//   Eint[l-k+1] - link(l, l-k+2) + link(l-k+1, l-k+2) + link(l, l-k+1)
-// (links read from the table lt)
-__global__ void k_enk_rows(int N, const double *__restrict__ lt, const double *__restrict__ Eint,
-                           double *__restrict__ ENk) {
-  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  const int l = w + 2;  // 1-based
-  if (l > N) return;
-  double carry = ENk[dtri(l)];
-  const double *rl = lt + (size_t)(l - 1) * N;
-  for (int k0 = 2; k0 <= l; k0 += 32) {
-    const int k = k0 + lane;
-    double inc = 0;
-    if (k <= l) {
-      const int c = l - k + 1, b = l - k + 2;  // 1-based
-      inc = Eint[c - 1] - rl[b - 1] + lt[(size_t)(c - 1) * N + (b - 1)] + rl[c - 1];
-    }
+// exclusive prefix sums G[n] = gl[0] + ... + gl[n-1] (n = 0..N-1) into
+// gl[N + n]: one block, a fixed order (contiguous runs per thread, then the
+// run totals scanned over the block)
+__global__ void __launch_bounds__(1024) k_gscan(int N, double *__restrict__ gl) {
+  __shared__ double wsum[32];
+  const int n = N - 1;  // increments
+  const int per = (n + blockDim.x - 1) / blockDim.x;
+  const int a = min(n, (int)threadIdx.x * per), b = min(n, a + per);
+  double run = 0.0;
+  for (int c = a; c < b; ++c) run += gl[c];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  double inc = run;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const double t = __shfl_up_sync(FULL, inc, o);
+    if (lane >= o) inc += t;
+  }
+  if (lane == 31) wsum[w] = inc;
+  __syncthreads();
+  if (w == 0) {
+    double v = lane < (int)(blockDim.x >> 5) ? wsum[lane] : 0.0;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-      const double t = __shfl_up_sync(FULL, inc, o);
-      if (lane >= o) inc += t;
+      const double t = __shfl_up_sync(FULL, v, o);
+      if (lane >= o) v += t;
     }
-    const double e = carry + inc;
-    if (k <= l) ENk[dtri(l) + k - 1] = e;
-    carry = __shfl_sync(FULL, e, 31);
+    wsum[lane] = v;
   }
+  __syncthreads();
+  double pre = (w > 0 ? wsum[w - 1] : 0.0) + (inc - run);
+  for (int c = a; c < b; ++c) {
+    gl[N + c] = pre;
+    pre += gl[c];
+  }
+  if (threadIdx.x == blockDim.x - 1) gl[N + n] = pre;
+}
+
+// E_l^(k) for k = 2..l (1-based row l, one block per row) in closed form.
+// The reference's recursion adds, for k = 2..l with c = l-k+1,
+//   Eint[c] + link(c, c+1) + link(l, c) - link(l, c+1),
+// and the link(l, .) terms telescope, so
+//   E_l^(k) = Eint[l] + (G[l-1] - G[l-k]) + link(l, l-k+1),
+// G the prefix sums of Eint[c] + link(c, c+1): every entry independent, one
+// spring each (no N x N table of springs, no scan along the row).
+template <int D>
+__global__ void __launch_bounds__(256) k_enk_direct(Geo g, const double *__restrict__ x,
+                                                    const double *__restrict__ m, double w2, int image,
+                                                    const double *__restrict__ Eint,
+                                                    const double *__restrict__ gl, double *__restrict__ ENk) {
+  const int l = blockIdx.x + 2;  // 1-based row
+  const double el = Eint[l - 1], Gl = gl[g.N + l - 1];
+  for (int k = 2 + threadIdx.x; k <= l; k += blockDim.x)
+    ENk[dtri(l) + k - 1] = el + ((Gl - gl[g.N + l - k]) + link<D>(g, x, m, w2, l - 1, l - k, image));
 }
 
 cudaError_t fill_enk(const Geo &g, const double *x, const double *m, double w2, int image,
-                     double *Eint, double *ENk, double *lt, cudaStream_t st) {
+                     double *Eint, double *ENk, double *gl, cudaStream_t st) {
   {
     XK_PROF("eint");
-    DISPATCH_D(g.D, k_eint<D><<<cdiv((size_t)g.N * 32, 256), 256, 0, st>>>(g, x, m, w2, image, Eint, ENk));
+    DISPATCH_D(g.D, k_eint<D><<<cdiv((size_t)g.N * 32, 64), 64, 0, st>>>(g, x, m, w2, image, Eint, ENk, gl));
   }
   cudaError_t e = XK_LAUNCHED();
   if (e != cudaSuccess || g.N < 2) return e;
   {
-    XK_PROF("link_table");
-    DISPATCH_D(g.D, k_link_table<D><<<cdiv((size_t)g.N * g.N, 256), 256, 0, st>>>(g, x, m, w2, image, lt));
+    XK_PROF("gscan");
+    k_gscan<<<1, 1024, 0, st>>>(g.N, gl);
   }
   e = XK_LAUNCHED();
   if (e != cudaSuccess) return e;
-  const size_t thr = (size_t)(g.N - 1) * 32;
   {
-    XK_PROF("enk_rows");
-    k_enk_rows<<<cdiv(thr, 256), 256, 0, st>>>(g.N, lt, Eint, ENk);
+    XK_PROF("enk_direct");
+    DISPATCH_D(g.D, k_enk_direct<D><<<g.N - 1, 256, 0, st>>>(g, x, m, w2, image, Eint, gl, ENk));
   }
   return XK_LAUNCHED();
 }
@@ -1660,7 +1679,10 @@ static cudaError_t tri_solve(int N, double beta, const TriJob &job, int first, i
     cudaError_t e = XK_LAUNCHED();
     if (e != cudaSuccess) return e;
     const size_t smem_c = (sizeof(double) + sizeof(int)) * (N + 1 + 3 * TS_CHUNK + 4 * TS_CHUNK * TS_LD) + 16;
-    if (cluster_solve_fits(smem_c)) {
+    // the cluster pays off from five chunks on; below that (and in
+    // ensembles of small systems) one block per direction leaves the SMs to
+    // the other systems
+    if (nch > 4 && cluster_solve_fits(smem_c)) {
       {
         XK_PROF(count == 2 ? "vb_tv_solve" : (first ? "tv_solve" : "vb_solve"));
         k_tri_solve_c<<<dim3(TSC_CL, count), TSC_WARPS * 32, smem_c, st>>>(N, beta, job, first);

@@ -96,9 +96,9 @@ cudaError_t wrap_box(const Geo &g, double *x, cudaStream_t st);
 cudaError_t zero(double *p, size_t n, cudaStream_t st);
 
 // ---- exchange ----
-// lt: scratch of N*N doubles (the table of bead-P -> bead-1 springs)
+// gl: scratch of 2N doubles (the row increments and their prefix sums)
 cudaError_t fill_enk(const Geo &g, const double *x, const double *m, double w2, int image,
-                     double *Eint, double *ENk, double *lt, cudaStream_t st);
+                     double *Eint, double *ENk, double *gl, cudaStream_t st);
 cudaError_t fill_enk2(const Geo &g, const double *x, const double *m, double w2, int image,
                       double *ENk2, cudaStream_t st);
 // the cubic path's table (md_pimd_fill_ENk2_x), a different quantity

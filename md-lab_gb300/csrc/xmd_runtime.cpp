@@ -455,7 +455,7 @@ int pimd_device(md_pimd_t_x *pimd, SimDev **sd, PimdDev **pd) {
   XMD_TRY(reserve(d->VBN, (size_t)(N + 1) * 8));
   XMD_TRY(reserve(d->tmpV, (size_t)(N + 1) * 8));
   XMD_TRY(reserve(d->G, (size_t)N * N * 8));
-  XMD_TRY(reserve(d->linkt, (size_t)N * N * 8));
+  XMD_TRY(reserve(d->linkt, (size_t)2 * N * 8));
   {
     // ln l, then 1/l, for l = 0..N (entries 0 unused), host values
     std::vector<double> ln(2 * (size_t)(N + 1), 0.0);
