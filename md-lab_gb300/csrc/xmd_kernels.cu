@@ -353,6 +353,31 @@ cudaError_t inv_q(size_t n, const double *Q, double *iQ, cudaStream_t st) {
   return XK_LAUNCHED();
 }
 
+// exp(x) for the thermostat factors exp(-h v_eta / 4) and exp(-h v_eta / 2):
+// for |x| < 1/4, the usual case with a small step, its Taylor series through
+// x^12/12! by Horner's rule (the first omitted term is below 3e-18
+// relative, a fortieth of the FP64 rounding unit: twelve FMAs instead of a
+// general exponential's range reduction and longer polynomial), otherwise
+// exp().  The range test reads the bit pattern, off the FP64 pipe.
+__device__ inline double nhc_exp(double x) {
+  if ((__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFLL) < 0x3FD0000000000000LL) {  // |x| < 2^-2
+    double p = 1.0 / 479001600.0;
+    p = fma(p, x, 1.0 / 39916800.0);
+    p = fma(p, x, 1.0 / 3628800.0);
+    p = fma(p, x, 1.0 / 362880.0);
+    p = fma(p, x, 1.0 / 40320.0);
+    p = fma(p, x, 1.0 / 5040.0);
+    p = fma(p, x, 1.0 / 720.0);
+    p = fma(p, x, 1.0 / 120.0);
+    p = fma(p, x, 1.0 / 24.0);
+    p = fma(p, x, 1.0 / 6.0);
+    p = fma(p, x, 0.5);
+    p = fma(p, x, 1.0);
+    return fma(p, x, 1.0);
+  }
+  return exp(x);
+}
+
 template <int L>
 __device__ inline void chain_odd(ChainState<L> &c, double h, const double *nhf) {
   constexpr int M2 = L / 2;
@@ -363,7 +388,7 @@ __device__ inline void chain_odd(ChainState<L> &c, double h, const double *nhf) 
     if (j == M2) {
       c.vt[2 * j - 1] = c.vt[2 * j - 1] + 0.5 * h * nhf[2 * j - 1];
     } else {
-      const double e = exp(-0.25 * h * c.vt[2 * j]);
+      const double e = nhc_exp(-0.25 * h * c.vt[2 * j]);
       c.vt[2 * j - 1] = c.vt[2 * j - 1] * (e * e) + 0.5 * h * nhf[2 * j - 1] * e;
     }
   }
@@ -398,7 +423,7 @@ __global__ void __launch_bounds__(256) k_nhc_fast(Geo g, int half, double *__res
   double nhf[L];
   if (half == 1) chain_forces<L, true>(c, mass * vv * vv, 1.0, kT, nhf);
   // thermostatted half kick: md_simulation_x.c:674-678
-  const double ek = exp(-0.25 * h * c.vt[0]);
+  const double ek = nhc_exp(-0.25 * h * c.vt[0]);
   vv = vv * (ek * ek) + 0.5 * h * F * ek;
 #pragma unroll
   for (int k = 1; k <= M2; ++k) c.th[2 * k - 2] = c.th[2 * k - 2] + h * c.vt[2 * k - 2] / 2;
@@ -412,7 +437,7 @@ __global__ void __launch_bounds__(256) k_nhc_fast(Geo g, int half, double *__res
 #pragma unroll
     for (int k = 1; k <= M2; ++k)
       {
-        const double e = exp(-0.5 * h * c.vt[2 * k - 1]);
+        const double e = nhc_exp(-0.5 * h * c.vt[2 * k - 1]);
         c.vt[2 * k - 2] = c.vt[2 * k - 2] * (e * e) + h * nhf[2 * k - 2] * e;
       }
   }
@@ -463,7 +488,7 @@ __global__ void k_nhc_grouped(Geo g, int half, int nf, const int *__restrict__ c
   };
   double nhf[L];
   if (half == 1) chain_forces<L>(c, kinetic(), cfv, kT, nhf);
-  const double e2 = exp(-0.25 * h * c.vt[0]), e1 = e2 * e2;
+  const double e2 = nhc_exp(-0.25 * h * c.vt[0]), e1 = e2 * e2;
   for (int q = 0; q < f2; ++q) {
     const size_t s = slot(f0 + q);
     v[s] = v[s] * e1 + 0.5 * h * f[s] * e2;
@@ -483,7 +508,7 @@ __global__ void k_nhc_grouped(Geo g, int half, int nf, const int *__restrict__ c
 #pragma unroll
     for (int k = 1; k <= M2; ++k)
       {
-        const double e = exp(-0.5 * h * c.vt[2 * k - 1]);
+        const double e = nhc_exp(-0.5 * h * c.vt[2 * k - 1]);
         c.vt[2 * k - 2] = c.vt[2 * k - 2] * (e * e) + h * nhf[2 * k - 2] * e;
       }
   }
@@ -836,7 +861,23 @@ __device__ inline Ext ext_exp(double x) {
   const double q = rint(x * LOG2E);
   double r = fma(-q, LN2_HI, x);
   r = fma(-q, LN2_LO, r);
-  return {exp(r), (int)q};
+  // exp(r) for |r| <= ln2/2 by its Taylor series through r^13/13! (Horner):
+  // the first omitted term is below 5e-18 relative; thirteen FMAs, where a
+  // general exponential would reduce the argument a second time
+  double p = 1.0 / 6227020800.0;
+  p = fma(p, r, 1.0 / 479001600.0);
+  p = fma(p, r, 1.0 / 39916800.0);
+  p = fma(p, r, 1.0 / 3628800.0);
+  p = fma(p, r, 1.0 / 362880.0);
+  p = fma(p, r, 1.0 / 40320.0);
+  p = fma(p, r, 1.0 / 5040.0);
+  p = fma(p, r, 1.0 / 720.0);
+  p = fma(p, r, 1.0 / 120.0);
+  p = fma(p, r, 1.0 / 24.0);
+  p = fma(p, r, 1.0 / 6.0);
+  p = fma(p, r, 0.5);
+  p = fma(p, r, 1.0);
+  return {fma(p, r, 1.0), (int)q};
 }
 
 // m * 2^d for d <= 0 (0 once the result would drop below the subnormals)
@@ -877,10 +918,14 @@ __device__ inline size_t moff(int i, int j) { return (size_t)i * (i - 1) / 2 + j
 // lnn[l] = ln l come from the host.
 // sgn = -1 gives the weights of a negative xi' (|xi'| in vi and lnvi): the
 // mantissa of every term with odd k - 1 changes sign.
+// both = 1 (first = 0, both directions): the two triangles hold the same
+// numbers, M_{l,l-k} = M'_{N-l+k,N-l}, so block l takes row l of ENk and
+// writes each weight into both (one exponential per entry).
 __global__ void __launch_bounds__(128) k_weights(int N, double beta, double vi, double lnvi,
                                                  const double *__restrict__ ENk, const double *__restrict__ lnn,
                                                  double *__restrict__ Mf, int *__restrict__ Ef,
-                                                 double *__restrict__ Mb, int *__restrict__ Eb, int first, int sgn) {
+                                                 double *__restrict__ Mb, int *__restrict__ Eb, int first, int sgn,
+                                                 int both) {
   const int row = blockIdx.x + 1;
   const int dir = first + blockIdx.y;
   double *Mm = dir ? Mb : Mf;
@@ -893,17 +938,22 @@ __global__ void __launch_bounds__(128) k_weights(int N, double beta, double vi, 
     if (sgn < 0 && ((k - 1) & 1)) w.m = -w.m;
     Mm[moff(row, j)] = w.m;
     Me[moff(row, j)] = w.e;
+    if (both) {
+      Mb[moff(N - row + k, N - row)] = w.m;
+      Eb[moff(N - row + k, N - row)] = w.e;
+    }
   }
 }
 
 static cudaError_t weights(int N, double beta, double vi, const double *ENk, const double *lnn, double *rs_f,
                            double *rs_b, int first, int count, cudaStream_t st, int sgn = 1) {
   const double lnvi = vi != 0.0 ? log(vi) : 0.0;
-  dim3 grid(N, count);
+  const int both = count == 2 ? 1 : 0;  // first = 0
+  dim3 grid(N, both ? 1 : count);
   {
     XK_PROF("weights");
     k_weights<<<grid, 128, 0, st>>>(N, beta, vi, lnvi, ENk, lnn, rs_f, rs_f ? (int *)(rs_f + ntri(N)) : nullptr,
-                                    rs_b, rs_b ? (int *)(rs_b + ntri(N)) : nullptr, first, sgn);
+                                    rs_b, rs_b ? (int *)(rs_b + ntri(N)) : nullptr, first, sgn, both);
   }
   return XK_LAUNCHED();
 }
