@@ -921,13 +921,10 @@ __device__ inline size_t moff(int i, int j) { return (size_t)i * (i - 1) / 2 + j
 // both = 1 (first = 0, both directions): the two triangles hold the same
 // numbers, M_{l,l-k} = M'_{N-l+k,N-l}, so block l takes row l of ENk and
 // writes each weight into both (one exponential per entry).
-__global__ void __launch_bounds__(128) k_weights(int N, double beta, double vi, double lnvi,
-                                                 const double *__restrict__ ENk, const double *__restrict__ lnn,
-                                                 double *__restrict__ Mf, int *__restrict__ Ef,
-                                                 double *__restrict__ Mb, int *__restrict__ Eb, int first, int sgn,
-                                                 int both) {
-  const int row = blockIdx.x + 1;
-  const int dir = first + blockIdx.y;
+__device__ inline void weights_row(int N, double beta, double vi, double lnvi, const double *__restrict__ ENk,
+                                   const double *__restrict__ lnn, double *__restrict__ Mf, int *__restrict__ Ef,
+                                   double *__restrict__ Mb, int *__restrict__ Eb, int first, int sgn, int both,
+                                   int row, int dir) {
   double *Mm = dir ? Mb : Mf;
   int *Me = dir ? Eb : Ef;
   for (int j = threadIdx.x; j < row; j += blockDim.x) {
@@ -943,6 +940,14 @@ __global__ void __launch_bounds__(128) k_weights(int N, double beta, double vi, 
       Eb[moff(N - row + k, N - row)] = w.e;
     }
   }
+}
+
+__global__ void __launch_bounds__(128) k_weights(int N, double beta, double vi, double lnvi,
+                                                 const double *__restrict__ ENk, const double *__restrict__ lnn,
+                                                 double *__restrict__ Mf, int *__restrict__ Ef,
+                                                 double *__restrict__ Mb, int *__restrict__ Eb, int first, int sgn,
+                                                 int both) {
+  weights_row(N, beta, vi, lnvi, ENk, lnn, Mf, Ef, Mb, Eb, first, sgn, both, blockIdx.x + 1, first + blockIdx.y);
 }
 
 static cudaError_t weights(int N, double beta, double vi, const double *ENk, const double *lnn, double *rs_f,
@@ -1282,7 +1287,7 @@ size_t rec_scratch_doubles(int N) {
 // Within chunk c (rows i0 .. i0+31) the system reads X = R + A X with A the
 // strictly lower 32 x 32 block of the weights and R the rows' sums over all
 // earlier unknowns, so X = B R with B = (I - A)^-1 = I + A + A^2 + ...  B
-// depends only on the weights: k_block_inv computes it for every chunk at
+// depends only on the weights: k_weights_inv computes it for every chunk at
 // once (a warp per column, all chunks in parallel over the GPU), and the
 // solve then replaces the 32-step substitution by a 32-term product per row,
 // done by all warps.  With non-negative weights every term is non-negative,
@@ -1305,23 +1310,22 @@ __device__ inline void ext_warp_sum(bool nz, double pm, int pe, double &sum, int
 // B_c column s for every chunk c: grid (chunks x 4 column groups, directions),
 // 8 warps per block, warp w of group g takes column s = 8 g + w.  Lane t
 // holds B[t][s]; step r adds row r: B[r][s] = sum_{s<=t<r} A[r][t] B[t][s].
-__global__ void __launch_bounds__(256) k_block_inv(int N, TriJob job, int first) {
-  const int dir = first + blockIdx.y;
-  const double *__restrict__ Mm = job.Mm[dir];
-  const int *__restrict__ Me = job.Me[dir];
+// weight M_{i,j} of direction dir (0 forward, 1 backward) from ENk, the same
+// expression k_weights evaluates (so the same number)
+__device__ inline Ext weight_at(int N, double beta, double vi, double lnvi, const double *__restrict__ ENk,
+                                const double *__restrict__ lnn, int dir, int i, int j) {
+  const int k = i - j, l = dir ? N - j : i;
+  Ext w{0.0, 0};
+  if (vi != 0.0 || k == 1) w = ext_exp(-beta * ENk[dtri(l) + k - 1] + (k - 1) * lnvi - lnn[l]);
+  return w;
+}
+
+// Column s of B(c) for direction dir, one warp; the chunk's block
+// A[r][t] = M_{i0+r, i0+t} (t < r) is staged in Am/Ae.
+__device__ inline void block_inv_column(int N, const TriJob &job, int dir, int c, int s,
+                                        const double (*Am)[TS_LD], const int (*Ae)[TS_LD]) {
   const int lane = threadIdx.x & 31;
-  const int c = blockIdx.x >> 2, s = ((blockIdx.x & 3) << 3) + (threadIdx.x >> 5);
   const int i0 = 1 + c * TS_CHUNK;
-  // the chunk's block A[r][t] = M_{i0+r, i0+t} (t < r) staged once per block
-  __shared__ double Am[TS_CHUNK][TS_LD];
-  __shared__ int Ae[TS_CHUNK][TS_LD];
-  for (int q = threadIdx.x; q < TS_CHUNK * TS_CHUNK; q += blockDim.x) {
-    const int r = q / TS_CHUNK, t = q % TS_CHUNK;
-    const bool in = t < r && i0 + r <= N;
-    Am[r][t] = in ? Mm[moff(i0 + r, i0 + t)] : 0.0;
-    Ae[r][t] = in ? Me[moff(i0 + r, i0 + t)] : 0;
-  }
-  __syncthreads();
   double bm = lane == s ? 0.5 : 0.0;  // B[s][s] = 1 = 0.5 * 2^1
   int be = lane == s ? 1 : 0;
   for (int r = s + 1; r < TS_CHUNK && i0 + r <= N; ++r) {
@@ -1342,6 +1346,37 @@ __global__ void __launch_bounds__(256) k_block_inv(int N, TriJob job, int first)
   int *Be = job.Be[dir] + (size_t)c * TS_CHUNK * TS_CHUNK;
   Bm[lane * TS_CHUNK + s] = lane >= s ? bm : 0.0;
   Be[lane * TS_CHUNK + s] = lane >= s ? be : 0;
+}
+
+// Weights and the diagonal-block inverses in one launch, so that the
+// inverses (latency-bound: a chain of 31 warp sums per column) run beside
+// the weight rows instead of after them: blocks 0..N-1 are k_weights' rows,
+// the rest take four columns of one chunk's B each and evaluate the chunk's
+// diagonal block from ENk themselves.
+__global__ void __launch_bounds__(128) k_weights_inv(int N, double beta, double vi, double lnvi,
+                                                     const double *__restrict__ ENk,
+                                                     const double *__restrict__ lnn, TriJob job, int first,
+                                                     int both, int nblk) {
+  __shared__ double Am[TS_CHUNK][TS_LD];
+  __shared__ int Ae[TS_CHUNK][TS_LD];
+  if ((int)blockIdx.x < N) {
+    weights_row(N, beta, vi, lnvi, ENk, lnn, (double *)job.Mm[0], (int *)job.Me[0], (double *)job.Mm[1],
+                (int *)job.Me[1], first, 1, both, blockIdx.x + 1, first);
+    return;
+  }
+  const int b = blockIdx.x - N, dir = first + b / nblk, q = b % nblk;
+  const int c = q >> 3, s0 = (q & 7) << 2, s = s0 + (threadIdx.x >> 5);
+  const int i0 = 1 + c * TS_CHUNK;
+  // columns s0.. read the block's entries t >= s0 only
+  for (int e = threadIdx.x; e < TS_CHUNK * TS_CHUNK; e += blockDim.x) {
+    const int r = e / TS_CHUNK, t = e % TS_CHUNK;
+    Ext w{0.0, 0};
+    if (t < r && t >= s0 && i0 + r <= N) w = weight_at(N, beta, vi, lnvi, ENk, lnn, dir, i0 + r, i0 + t);
+    Am[r][t] = w.m;
+    Ae[r][t] = w.e;
+  }
+  __syncthreads();
+  block_inv_column(N, job, dir, c, s, Am, Ae);
 }
 
 // One block per direction, 16 warps, three phases per chunk c:
@@ -1720,14 +1755,9 @@ static bool cluster_solve_fits(size_t smem) {
 
 static cudaError_t tri_solve(int N, double beta, const TriJob &job, int first, int count, cudaStream_t st) {
   if (!job.sign) {
-    // unsigned weights: diagonal-block inverses, then the block solve
+    // unsigned weights: the block solve (the diagonal-block inverses came
+    // with the weights, k_weights_inv)
     const int nch = (N + TS_CHUNK - 1) / TS_CHUNK;
-    {
-      XK_PROF("block_inv");
-      k_block_inv<<<dim3(nch * 4, count), 256, 0, st>>>(N, job, first);
-    }
-    cudaError_t e = XK_LAUNCHED();
-    if (e != cudaSuccess) return e;
     const size_t smem_c = (sizeof(double) + sizeof(int)) * (N + 1 + 3 * TS_CHUNK + 4 * TS_CHUNK * TS_LD) + 16;
     // the cluster pays off from five chunks on; below that (and in
     // ensembles of small systems) one block per direction leaves the SMs to
@@ -1784,25 +1814,42 @@ static TriJob tri_job(int N, double *rs_f, double *rs_b, double *VBN, double *tm
   return j;
 }
 
+// unsigned weights of directions first .. first + count - 1 and their
+// diagonal-block inverses (count = 2: first = 0)
+static cudaError_t weights_inv(int N, double beta, double vi, const double *ENk, const double *lnn,
+                               const TriJob &job, int first, int count, cudaStream_t st) {
+  const double lnvi = vi != 0.0 ? log(vi) : 0.0;
+  const int nblk = (N + TS_CHUNK - 1) / TS_CHUNK * 8;  // four columns a block
+  {
+    XK_PROF("weights");
+    k_weights_inv<<<N + count * nblk, 128, 0, st>>>(N, beta, vi, lnvi, ENk, lnn, job, first, count == 2 ? 1 : 0,
+                                                      nblk);
+  }
+  return XK_LAUNCHED();
+}
+
 cudaError_t fill_vb(int N, double beta, double vi, const double *ENk, const double *lnn, double *VBN, double *rs,
                     cudaStream_t st) {
-  cudaError_t e = weights(N, beta, vi, ENk, lnn, rs, nullptr, 0, 1, st);
+  const TriJob j = tri_job(N, rs, nullptr, VBN, nullptr);
+  cudaError_t e = weights_inv(N, beta, vi, ENk, lnn, j, 0, 1, st);
   if (e != cudaSuccess) return e;
-  return tri_solve(N, beta, tri_job(N, rs, nullptr, VBN, nullptr), 0, 1, st);
+  return tri_solve(N, beta, j, 0, 1, st);
 }
 
 cudaError_t back_vb(int N, double beta, double vi, const double *ENk, const double *lnn, double *tmpV, double *rs,
                     cudaStream_t st) {
-  cudaError_t e = weights(N, beta, vi, ENk, lnn, nullptr, rs, 1, 1, st);
+  const TriJob j = tri_job(N, nullptr, rs, nullptr, tmpV);
+  cudaError_t e = weights_inv(N, beta, vi, ENk, lnn, j, 1, 1, st);
   if (e != cudaSuccess) return e;
-  return tri_solve(N, beta, tri_job(N, nullptr, rs, nullptr, tmpV), 1, 1, st);
+  return tri_solve(N, beta, j, 1, 1, st);
 }
 
 cudaError_t fill_vb_tv(int N, double beta, double vi, const double *ENk, const double *lnn, double *VBN,
                        double *tmpV, double *rs_f, double *rs_b, cudaStream_t st) {
-  cudaError_t e = weights(N, beta, vi, ENk, lnn, rs_f, rs_b, 0, 2, st);
+  const TriJob j = tri_job(N, rs_f, rs_b, VBN, tmpV);
+  cudaError_t e = weights_inv(N, beta, vi, ENk, lnn, j, 0, 2, st);
   if (e != cudaSuccess) return e;
-  return tri_solve(N, beta, tri_job(N, rs_f, rs_b, VBN, tmpV), 0, 2, st);
+  return tri_solve(N, beta, j, 0, 2, st);
 }
 
 cudaError_t fill_vb_signed(int N, double beta, double vi2, const double *ENk, const double *lnn, double *V2,
