@@ -93,17 +93,12 @@ cudaError_t launched() {
 
 __device__ inline size_t dtri(int n) { return (size_t)n * (n - 1) / 2; }
 
-// md_simulation_x.c:70-81 with md_periodic_image_count_x (:858-865): shift
-// a + L/2 into [0, L] by whole boxes, then subtract L/2 again.
-__device__ inline double min_image(double a, double L, double invL) {
-  a += L / 2;
-  int c = (int)(fabs(a) * invL);
-  if (a > L)
-    a += L * (double)(-c);
-  else if (a < 0)
-    a += L * (double)(c + 1);
-  return a - L / 2;
-}
+// Nearest image of a difference a in a box of side L: md_simulation_x.c:70-81
+// with md_periodic_image_count_x (:858-865) shift a + L/2 into [0, L] by
+// whole boxes and subtract L/2 again; a - L rint(a/L) is the same image in
+// three FP64 operations instead of eight (ties at exactly L/2 aside, the
+// results differ in the last bits only).
+__device__ inline double min_image(double a, double L, double invL) { return fma(-L, rint(a * invL), a); }
 
 __device__ inline double warp_sum(double v) {
 #pragma unroll
@@ -675,7 +670,7 @@ __global__ void __launch_bounds__(1024) k_gscan(int N, double *__restrict__ gl) 
   if (threadIdx.x == blockDim.x - 1) gl[N + n] = pre;
 }
 
-// E_l^(k) for k = 2..l (1-based row l, one block per row) in closed form.
+// E_l^(k) for k = 2..l (1-based row l) in closed form.
 // The reference's recursion adds, for k = 2..l with c = l-k+1,
 //   Eint[c] + link(c, c+1) + link(l, c) - link(l, c+1),
 // and the link(l, .) terms telescope, so
@@ -687,10 +682,14 @@ __global__ void __launch_bounds__(256) k_enk_direct(Geo g, const double *__restr
                                                     const double *__restrict__ m, double w2, int image,
                                                     const double *__restrict__ Eint,
                                                     const double *__restrict__ gl, double *__restrict__ ENk) {
-  const int l = blockIdx.x + 2;  // 1-based row
-  const double el = Eint[l - 1], Gl = gl[g.N + l - 1];
-  for (int k = 2 + threadIdx.x; k <= l; k += blockDim.x)
-    ENk[dtri(l) + k - 1] = el + ((Gl - gl[g.N + l - k]) + link<D>(g, x, m, w2, l - 1, l - k, image));
+  // rows l1 and N+2-l1 (l1-1 and N+1-l1 entries, N together) share a block
+  const int l1 = blockIdx.x + 2, l2 = g.N - blockIdx.x;
+  const int n1 = l1 - 1, n = n1 + (l2 > l1 ? l2 - 1 : 0);
+  for (int e = threadIdx.x; e < n; e += blockDim.x) {
+    const int l = e < n1 ? l1 : l2, k = 2 + (e < n1 ? e : e - n1);  // 1-based row, cycle length
+    ENk[dtri(l) + k - 1] =
+        Eint[l - 1] + ((gl[g.N + l - 1] - gl[g.N + l - k]) + link<D>(g, x, m, w2, l - 1, l - k, image));
+  }
 }
 
 cudaError_t fill_enk(const Geo &g, const double *x, const double *m, double w2, int image,
@@ -709,7 +708,7 @@ cudaError_t fill_enk(const Geo &g, const double *x, const double *m, double w2, 
   if (e != cudaSuccess) return e;
   {
     XK_PROF("enk_direct");
-    DISPATCH_D(g.D, k_enk_direct<D><<<g.N - 1, 256, 0, st>>>(g, x, m, w2, image, Eint, gl, ENk));
+    DISPATCH_D(g.D, k_enk_direct<D><<<g.N / 2, 256, 0, st>>>(g, x, m, w2, image, Eint, gl, ENk));
   }
   return XK_LAUNCHED();
 }
