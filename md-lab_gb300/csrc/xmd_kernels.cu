@@ -879,6 +879,15 @@ __device__ inline Ext ext_exp(double x) {
   return {fma(p, r, 1.0), (int)q};
 }
 
+// exp(x) through ext_exp, the power of two put into the exponent field by
+// integer arithmetic; results near or beyond the ends of the normal range
+// (|x| > 700) are left to exp()
+__device__ inline double exp_fast(double x) {
+  const Ext w = ext_exp(x);
+  if (w.e <= -1020 || w.e >= 1020) return exp(x);
+  return __longlong_as_double(__double_as_longlong(w.m) + ((long long)w.e << 52));
+}
+
 // m * 2^d for d <= 0 (0 once the result would drop below the subnormals)
 __device__ inline double scale_down(double m, int d) {
   if (d >= -1022) return m * __longlong_as_double((long long)(d + 1023) << 52);
@@ -1862,7 +1871,8 @@ cudaError_t fill_vb_signed(int N, double beta, double vi2, const double *ENk, co
 
 // connection probabilities G[l][j]: md_pimd_x.c:2660-2673
 // G[l][j] (md_pimd_x.c:2588-2620); ln xi comes from the host and 1/l from
-// a host table, so an element costs one exp on the FP64 pipe
+// a host table, so an element costs one exponential (exp_fast) on the FP64
+// pipe
 __global__ void k_fill_g(int N, double beta, double vi, double lnvi, const double *__restrict__ ENk,
                          const double *__restrict__ VBN, const double *__restrict__ tmpV,
                          const double *__restrict__ invl, double *__restrict__ G) {
@@ -1877,9 +1887,9 @@ __global__ void k_fill_g(int N, double beta, double vi, double lnvi, const doubl
     else if (vi == 0.0 && l - j != 0)
       gv = 0;
     else if (vi == 0.0)
-      gv = exp(-beta * (VBN[j - 1] + ENk[dtri(l) + l - j] + base)) * invl[l];
+      gv = exp_fast(-beta * (VBN[j - 1] + ENk[dtri(l) + l - j] + base)) * invl[l];
     else
-      gv = exp(-beta * (VBN[j - 1] + ENk[dtri(l) + l - j] + base) + (l - j) * lnvi) * invl[l];
+      gv = exp_fast(-beta * (VBN[j - 1] + ENk[dtri(l) + l - j] + base) + (l - j) * lnvi) * invl[l];
     G[(size_t)(l - 1) * N + (j - 1)] = gv;
   }
 }
@@ -1952,23 +1962,53 @@ __global__ void k_exch_ends(Geo g, const double *__restrict__ x, const double *_
   for (int d = 0; d < D; ++d) a1[d] = aP[d] = 0;
   if (l < N) {
     const double m1 = m[l], mP = m[(size_t)jP * g.Ns + l];
+    // The reference adds G-weighted gradients of both springs at the end
+    // bead for every partner q; the spring inside the ring (bead 1 -> 2,
+    // bead P -> P-1) does not depend on q, so it is weighted once by the sum
+    // of the weights and only the partner spring is evaluated per q (equal
+    // to rounding).
+    double x1[D], xP[D], s1 = 0.0, sP = 0.0;
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      x1[d] = x[sidx(0, d, l, D, g.Ns)];
+      xP[d] = x[sidx(jP, d, l, D, g.Ns)];
+    }
     // partner q runs over this block's part of 0..N-1
     for (int q = js * EX_TY + threadIdx.y; q < N; q += nsplit * EX_TY) {
-      double gr[D];
       // bead 1 of l, previous bead = bead P of q, weight G[q][l]
       const double g1 = G[(size_t)q * N + l];
       if (g1 != 0.0) {
-        grad2<D>(g, x, m1 * w2, 0, l, 1, l, jP, q, image, gr);
+        s1 += g1;
 #pragma unroll
-        for (int d = 0; d < D; ++d) a1[d] += g1 * gr[d];
+        for (int d = 0; d < D; ++d) {
+          double c = x1[d] - x[sidx(jP, d, q, D, g.Ns)];
+          if (image) c = min_image(c, g.box[d], g.inv_box[d]);
+          a1[d] = fma(g1, c, a1[d]);
+        }
       }
       // bead P of l, next bead = bead 1 of q, weight G[l][q]
       const double gP = G[(size_t)l * N + q];
       if (gP != 0.0) {
-        grad2<D>(g, x, mP * w2, jP, l, jP - 1, l, 0, q, image, gr);
+        sP += gP;
 #pragma unroll
-        for (int d = 0; d < D; ++d) aP[d] += gP * gr[d];
+        for (int d = 0; d < D; ++d) {
+          double c = xP[d] - x[sidx(0, d, q, D, g.Ns)];
+          if (image) c = min_image(c, g.box[d], g.inv_box[d]);
+          aP[d] = fma(gP, c, aP[d]);
+        }
       }
+    }
+    const double k1 = m1 * w2, kP = mP * w2;
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      double a = x1[d] - x[sidx(1, d, l, D, g.Ns)];
+      double b = xP[d] - x[sidx(jP - 1, d, l, D, g.Ns)];
+      if (image) {
+        a = min_image(a, g.box[d], g.inv_box[d]);
+        b = min_image(b, g.box[d], g.inv_box[d]);
+      }
+      a1[d] = k1 * (s1 * a + a1[d]);
+      aP[d] = kP * (sP * b + aP[d]);
     }
   }
 #pragma unroll
