@@ -94,6 +94,10 @@ struct PimdDev {
   // the current ENk with these beta and vi
   bool tmpv_fresh = false;
   double tmpv_beta = 0, tmpv_vi = 0;
+  // G (the cycle probabilities) belongs to the stored ENk, VBN and tmpV at
+  // g_beta, g_vi: the estimators then need no recursion of their own
+  bool g_fresh = false;
+  double g_beta = 0, g_vi = 0;
   // Ewald reciprocal tables, rebuilt when the parameters change
   DevBuf rc_coef, rc_cols, rc_phase, rc_S, rc_T;
   int rc_nsum = -1;

@@ -3473,8 +3473,50 @@ __global__ void __launch_bounds__(TS_WARPS * 32) k_lin_solve(int N, const double
 
 size_t vbn_scratch_doubles(int N) { return ntri(N) + N + 2; }
 
+// The same estimator from the cycle probabilities.  The recursion's res[N]
+// is the expectation of -sum over cycles of E2 when cycles are drawn as the
+// recursion draws them (last cycle of n particles has length k with
+// probability p_{n,k}); the probability that the cycle j..l occurs is
+// G[l][j] (j <= l), the connection probability of the exchange forces
+// (md_pimd_x.c:2588-2620).  So
+//   res[N] = -sum_l sum_{j<=l} G[l][j] E2[l][l-j+1],
+// every term independent: row sums (a block per row), then one block adds
+// the rows in order.
+__global__ void __launch_bounds__(256) k_est_rows(int N, const double *__restrict__ G, const double *__restrict__ E2,
+                                                  double *__restrict__ part) {
+  __shared__ double buf[33];
+  const int l = blockIdx.x + 1;
+  const double *grow = G + (size_t)(l - 1) * N, *erow = E2 + dtri(l);
+  double v = 0.0;
+  for (int j = threadIdx.x + 1; j <= l; j += blockDim.x) v = fma(grow[j - 1], erow[l - j], v);
+  v = block_sum(v, buf);
+  if (threadIdx.x == 0) part[l - 1] = v;
+}
+
+__global__ void __launch_bounds__(1024) k_est_total(int N, const double *__restrict__ part, double add,
+                                                    double *acc) {
+  __shared__ double buf[33];
+  double v = 0.0;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) v += part[i];
+  v = block_sum(v, buf);
+  if (threadIdx.x == 0) *acc += add - v;
+}
+
 cudaError_t vbn_energy(int N, double beta, double vi, double add, const double *ENk, const double *VBN,
-                       const double *ENk2, double *acc, double *scratch, cudaStream_t st) {
+                       const double *ENk2, double *acc, double *scratch, cudaStream_t st, const double *G) {
+  if (G) {
+    {
+      XK_PROF("est_rows");
+      k_est_rows<<<N, 256, 0, st>>>(N, G, ENk2 ? ENk2 : ENk, scratch);
+    }
+    cudaError_t e = XK_LAUNCHED();
+    if (e != cudaSuccess) return e;
+    {
+      XK_PROF("est_total");
+      k_est_total<<<1, 1024, 0, st>>>(N, scratch, add, acc);
+    }
+    return XK_LAUNCHED();
+  }
   double *Pw = scratch, *cvec = scratch + ntri(N) + 1;
   {
     XK_PROF("est_weights");

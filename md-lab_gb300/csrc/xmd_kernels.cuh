@@ -252,10 +252,13 @@ cudaError_t sk_structure(const Geo &g, const double *x, int ja, int jb, const do
 
 // ---- estimators ----
 // primitive (ENk2 == nullptr) or virial exchange estimator; res[N] + add is
-// added to *acc.  scratch: vbn_scratch_doubles(N) doubles.
+// added to *acc.  scratch: vbn_scratch_doubles(N) doubles.  G: the cycle
+// probabilities G[l][j] (fill_g) of the same ENk, VBN, beta and xi, or null
+// (then the reference's recursion is solved).
 size_t vbn_scratch_doubles(int N);
 cudaError_t vbn_energy(int N, double beta, double vi, double add, const double *ENk,
-                       const double *VBN, const double *ENk2, double *acc, double *scratch, cudaStream_t st);
+                       const double *VBN, const double *ENk2, double *acc, double *scratch, cudaStream_t st,
+                       const double *G = nullptr);
 cudaError_t force_virial(const Geo &g, const double *x, const double *f, const double *m,
                          int image, double *acc, double *scratch, cudaStream_t st);
 cudaError_t add_scalar(double *acc, double v, cudaStream_t st);

@@ -470,6 +470,7 @@ int pimd_device(md_pimd_t_x *pimd, SimDev **sd, PimdDev **pd) {
   XMD_TRY(reserve(d->rec, 2 * xk::rec_scratch_doubles(N) * 8));
   XMD_CUDA(cudaMemsetAsync(d->rec.p, 0, 2 * xk::rec_scratch_doubles(N) * 8, stream()));
   d->tmpv_fresh = false;
+  d->g_fresh = false;
   XMD_CUDA(cudaMemsetAsync(d->tmpV.p, 0, (size_t)(N + 1) * 8, stream()));
   cudaStream_t st = stream();
   XMD_CUDA(cudaMemcpyAsync(d->ENk.p, pimd->ENk[0], nt * 8, cudaMemcpyHostToDevice, st));

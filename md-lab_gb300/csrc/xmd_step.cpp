@@ -273,6 +273,7 @@ int md_pimd_fast_fill_ENk_x(md_pimd_t_x *pimd, int image) {
   XMD_CUDA(xk::fill_enk(sd->geo, sd->x.as<double>(), sd->m.as<double>(), pimd->omegaP * pimd->omegaP, image,
                         pd->Eint.as<double>(), pd->ENk.as<double>(), pd->linkt.as<double>(), stream()));
   pd->tmpv_fresh = false;
+  pd->g_fresh = false;
   return 0;
 }
 
@@ -298,6 +299,7 @@ int md_pimd_fill_VB_x(md_pimd_t_x *pimd) {
   pd->tmpv_fresh = true;
   pd->tmpv_beta = pimd->beta;
   pd->tmpv_vi = pimd->vi;
+  pd->g_fresh = false;
   return 0;
 }
 
@@ -331,6 +333,9 @@ int md_pimd_fast_fill_force_VB_x(md_pimd_t_x *pimd, int image) {
   XMD_CUDA(xk::exch_force(sd->geo, sd->x.as<double>(), sd->m.as<double>(), pimd->omegaP * pimd->omegaP, image,
                           pd->G.as<double>(), sd->fex.as<double>(), scr, st));
   XMD_TRY(side_end(sd));
+  pd->g_fresh = true;
+  pd->g_beta = pimd->beta;
+  pd->g_vi = pimd->vi;
   return 0;
 }
 
@@ -662,6 +667,13 @@ int md_gb300_pair_force_noalloc_x(md_pair_force_t_x pf, const double *x, const d
 // estimators: md_pimd_x.c:1111-1295, :1393-1525, :1679-1824,
 // :3989-4056, :4072-4348, :4423-4556
 // ------------------------------------------------------------------
+// G of the last exchange force call when it belongs to the stored ENk,
+// VBN and the current beta and xi, else null (the estimators then solve the
+// reference's recursion)
+static const double *cycle_probs(const md_pimd_t_x *pimd, PimdDev *pd) {
+  return pd->g_fresh && pd->g_beta == pimd->beta && pd->g_vi == pimd->vi ? pd->G.as<double>() : nullptr;
+}
+
 int md_pimd_calc_VBN_energy_x(md_pimd_t_x *pimd, md_stats_t_x *stats) {
   SimDev *sd;
   PimdDev *pd;
@@ -674,7 +686,7 @@ int md_pimd_calc_VBN_energy_x(md_pimd_t_x *pimd, md_stats_t_x *stats) {
   if (rc) return rc;
   const double add = D * pimd->N * pimd->P / (2 * pimd->beta);
   XMD_CUDA(xk::vbn_energy(pimd->N, pimd->beta, pimd->vi, add, pd->ENk.as<double>(), pd->VBN.as<double>(), nullptr,
-                          acc, scr, stream()));
+                          acc, scr, stream(), cycle_probs(pimd, pd)));
   return 0;
 }
 
@@ -718,7 +730,7 @@ int md_pimd_calc_vi_virial_energy_x(md_pimd_t_x *pimd, md_stats_t_x *stats, int 
   cudaStream_t st = stream();
   const double add = D * pimd->N / (2 * pimd->beta);
   XMD_CUDA(xk::vbn_energy(pimd->N, pimd->beta, pimd->vi, add, pd->ENk.as<double>(), pd->VBN.as<double>(),
-                          pd->ENk2.as<double>(), acc, scr, st));
+                          pd->ENk2.as<double>(), acc, scr, st, cycle_probs(pimd, pd)));
   XMD_CUDA(xk::force_virial(sd->geo, sd->x.as<double>(), sd->f.as<double>(), sd->m.as<double>(), image, acc, scr, st));
   return 0;
 }

@@ -70,14 +70,21 @@ def test_forces_and_estimators_vs_oracle(case):
     # estimators
     ck(lib.md_pimd_calc_VBN_energy_x(s.pimd, s.stats))
     e = L_.orc_vbn_energy(D, N, P, beta, vi, orc.ptr(ENk), orc.ptr(VBN))
-    assert_close([s.take_energy()], [e], PARITY, "primitive estimator")
+    assert_close([s.take_energy()], [e], PARITY, "primitive estimator (cycle probabilities)")
     ck(lib.md_pimd_fast_fill_ENk2_x(s.pimd, image))
     ENk2 = np.zeros(orc.ntri(N))
     L_.orc_fast_fill_ENk2(o.ref, N, P, omegaP, image, orc.ptr(ENk2))
     assert_close(s.exchange()["ENk2"], ENk2, PARITY, "ENk2")
     ck(lib.md_pimd_calc_vi_virial_energy_x(s.pimd, s.stats, image))
     ev = L_.orc_vi_virial_energy(o.ref, N, P, beta, vi, image, orc.ptr(ENk), orc.ptr(ENk2), orc.ptr(VBN))
-    assert_close([s.take_energy()], [ev], PARITY, "virial estimator")
+    assert_close([s.take_energy()], [ev], PARITY, "virial estimator (cycle probabilities)")
+    # a fresh V_B recursion leaves no cycle probabilities of a force call:
+    # both estimators then solve the recursion themselves
+    ck(lib.md_pimd_fill_VB_x(s.pimd))
+    ck(lib.md_pimd_calc_VBN_energy_x(s.pimd, s.stats))
+    assert_close([s.take_energy()], [e], PARITY, "primitive estimator (recursion)")
+    ck(lib.md_pimd_calc_vi_virial_energy_x(s.pimd, s.stats, image))
+    assert_close([s.take_energy()], [ev], PARITY, "virial estimator (recursion)")
     kind = orc.PAIR_EWALD if ueg else orc.PAIR_GAUSSIAN
     pe = lib.fn("md_coulomb_3d_ewald_energy_x" if ueg else "md_gaussian_energy_x")
     ck(lib.md_pimd_calc_pair_energy_x(s.pimd, pe, s.stats))
