@@ -65,6 +65,10 @@ void host_free(void *p);
 
 struct SimDev {
   bool valid = false;  // device copy authoritative
+  // the layout whose padding lanes were last zeroed (re-uploads of the same
+  // layout into the same buffers skip the memsets)
+  const void *zx = nullptr, *zth = nullptr;
+  int zN = -1, zNs = -1, zP = -1;
   xk::Geo geo{};
   int nf = 0, L = 0;
   bool fast_chains = true;

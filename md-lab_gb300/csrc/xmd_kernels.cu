@@ -226,7 +226,7 @@ cudaError_t soa_to_aos(const Geo &g, double *aos, const double *x, const double 
 // the chain order.
 template <int D>
 __global__ void k_chains(Geo g, int L, int nf, bool fast, bool to_dev, unsigned char *rec,
-                         size_t rb, double *th, double *vt, double *Q, const int *cf) {
+                         size_t rb, double *th, double *vt, double *Q, const int *cf, double *iQ, int all_iq) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= nf) return;
   size_t slot, stride;
@@ -250,7 +250,11 @@ __global__ void k_chains(Geo g, int L, int nf, bool fast, bool to_dev, unsigned 
     if (to_dev) {
       th[i * stride + slot] = r[i];
       vt[i * stride + slot] = r[L + i];
-      Q[i * stride + slot] = r[2 * L + i];
+      // 1/Q only where Q changed (a re-upload of the same chains divides
+      // nothing)
+      const double q = r[2 * L + i];
+      if (iQ && (all_iq || q != Q[i * stride + slot])) iQ[i * stride + slot] = q != 0.0 ? 1.0 / q : 0.0;
+      Q[i * stride + slot] = q;
     } else {
       r[i] = th[i * stride + slot];
       r[L + i] = vt[i * stride + slot];
@@ -286,11 +290,11 @@ cudaError_t upload_checks(const unsigned char *prec, int np, size_t pbytes, cons
 }
 
 cudaError_t chains_to_dev(const Geo &g, int L, int nf, bool fast, const unsigned char *rec,
-                          size_t rb, double *th, double *vt, double *Q, cudaStream_t st) {
+                          size_t rb, double *th, double *vt, double *Q, double *iQ, bool all_iq, cudaStream_t st) {
   {
     XK_PROF("chains");
-    DISPATCH_D(g.D, k_chains<D><<<cdiv(nf, 256), 256, 0, st>>>(g, L, nf, fast, true,
-                                                              (unsigned char *)rec, rb, th, vt, Q, nullptr));
+    DISPATCH_D(g.D, k_chains<D><<<cdiv(nf, 256), 256, 0, st>>>(g, L, nf, fast, true, (unsigned char *)rec, rb,
+                                                              th, vt, Q, nullptr, iQ, all_iq ? 1 : 0));
   }
   return XK_LAUNCHED();
 }
@@ -302,7 +306,7 @@ cudaError_t chains_to_host(const Geo &g, int L, int nf, bool fast, unsigned char
   {
     XK_PROF("chains");
     DISPATCH_D(g.D, k_chains<D><<<cdiv(nf, 256), 256, 0, st>>>(
-                        g, L, nf, fast, false, rec, rb, (double *)th, (double *)vt, (double *)Q, cf));
+                        g, L, nf, fast, false, rec, rb, (double *)th, (double *)vt, (double *)Q, cf, nullptr, 0));
   }
   return XK_LAUNCHED();
 }
@@ -334,19 +338,6 @@ __device__ inline void chain_forces(const ChainState<L> &c, double kin, double c
   }
 }
 
-// iQ[s] = 1/Q[s] for the n entries of the one-DOF chains' Q
-__global__ void k_inv_q(size_t n, const double *__restrict__ Q, double *__restrict__ iQ) {
-  const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < n) iQ[t] = Q[t] != 0.0 ? 1.0 / Q[t] : 0.0;
-}
-
-cudaError_t inv_q(size_t n, const double *Q, double *iQ, cudaStream_t st) {
-  {
-    XK_PROF("inv_q");
-    k_inv_q<<<cdiv(n, 256), 256, 0, st>>>(n, Q, iQ);
-  }
-  return XK_LAUNCHED();
-}
 
 // exp(x) for the thermostat factors exp(-h v_eta / 4) and exp(-h v_eta / 2):
 // for |x| < 1/4, the usual case with a small step, its Taylor series through

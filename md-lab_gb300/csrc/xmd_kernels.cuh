@@ -65,8 +65,10 @@ cudaError_t aos_to_soa(const Geo &g, const double *aos, double *x, double *v, do
 cudaError_t soa_to_aos(const Geo &g, double *aos, const double *x, const double *v,
                        const double *f, const double *m, cudaStream_t st);
 // chains: host records {int f; double theta[L], vtheta[L], Q[L]} of rec_bytes each
+// iQ (optional): 1/Q, updated where Q changes (everywhere with all_iq)
 cudaError_t chains_to_dev(const Geo &g, int L, int nf, bool fast, const unsigned char *rec,
-                          size_t rec_bytes, double *th, double *vt, double *Q, cudaStream_t st);
+                          size_t rec_bytes, double *th, double *vt, double *Q, double *iQ, bool all_iq,
+                          cudaStream_t st);
 // flags[0] := 0 unless every particle record (np of pbytes, mass first) has
 // the first one's mass; flags[1] := 0 unless every chain record (nc of
 // cbytes, int f first) has f == 1.  Flags start nonzero.
@@ -82,7 +84,7 @@ struct Chains {
   bool fast;            // one DOF per chain, chains in slot order
   int L, nf;            // chain length, number of chains
   double *th, *vt, *Q;  // [L][S] (fast) or [L][nf] (grouped)
-  const double *iQ;     // fast: 1/Q, same layout (inv_q)
+  const double *iQ;     // fast: 1/Q, same layout
   const int *cf;        // grouped: nhcs[i].f
   const int *c0;        // grouped: first DOF (reference numbering)
   const int *c2;        // grouped: number of DOFs updated
@@ -90,8 +92,6 @@ struct Chains {
 };
 cudaError_t nhc_vv3(const Geo &g, int half, const Chains &c, double *x, double *v,
                     const double *f, const double *m, double kT, double h, cudaStream_t st);
-// iQ[s] = 1/Q[s] (0 where Q = 0) for the n entries of the one-DOF chains
-cudaError_t inv_q(size_t n, const double *Q, double *iQ, cudaStream_t st);
 cudaError_t wrap_box(const Geo &g, double *x, cudaStream_t st);
 cudaError_t zero(double *p, size_t n, cudaStream_t st);
 

@@ -329,10 +329,15 @@ int sim_device(md_simulation_t_x *sim, SimDev **out) {
   XMD_TRY(reserve(d->f, S * 8));
   XMD_TRY(reserve(d->m, (size_t)g.P * g.Ns * 8));
   // padding lanes stay zero so that slice-wide kernels read defined values
-  XMD_CUDA(cudaMemsetAsync(d->x.p, 0, S * 8, st));
-  XMD_CUDA(cudaMemsetAsync(d->v.p, 0, S * 8, st));
-  XMD_CUDA(cudaMemsetAsync(d->f.p, 0, S * 8, st));
-  XMD_CUDA(cudaMemsetAsync(d->m.p, 0, (size_t)g.P * g.Ns * 8, st));
+  // (no kernel writes them: once per layout and allocation)
+  const bool same_layout = d->zx == d->x.p && d->zN == g.N && d->zNs == g.Ns && d->zP == g.P;
+  if (!same_layout) {
+    XMD_CUDA(cudaMemsetAsync(d->x.p, 0, S * 8, st));
+    XMD_CUDA(cudaMemsetAsync(d->v.p, 0, S * 8, st));
+    XMD_CUDA(cudaMemsetAsync(d->f.p, 0, S * 8, st));
+    XMD_CUDA(cudaMemsetAsync(d->m.p, 0, (size_t)g.P * g.Ns * 8, st));
+    d->zth = nullptr;
+  }
   // particle and chain records go up to their stages; whether all masses
   // are equal and all chains have one DOF is checked there on the device
   // (walking 13 MB of records on one host core took longer than the copies)
@@ -363,11 +368,16 @@ int sim_device(md_simulation_t_x *sim, SimDev **out) {
     XMD_TRY(reserve(d->th, cs * L * 8));
     XMD_TRY(reserve(d->vt, cs * L * 8));
     XMD_TRY(reserve(d->Q, cs * L * 8));
+    if (fast) XMD_TRY(reserve(d->iQ, S * L * 8));
+    const bool fresh_chains = !(fast && same_layout && d->zth == d->th.p);
     if (fast) {
-      // padding slots: Q = 1 so that no kernel ever divides by zero there
-      XMD_CUDA(cudaMemsetAsync(d->th.p, 0, cs * L * 8, st));
-      XMD_CUDA(cudaMemsetAsync(d->vt.p, 0, cs * L * 8, st));
-      XMD_CUDA(cudaMemsetAsync(d->Q.p, 0, cs * L * 8, st));
+      // padding slots stay zero (their 1/Q is 0, nothing divides by them)
+      if (fresh_chains) {
+        XMD_CUDA(cudaMemsetAsync(d->th.p, 0, cs * L * 8, st));
+        XMD_CUDA(cudaMemsetAsync(d->vt.p, 0, cs * L * 8, st));
+        XMD_CUDA(cudaMemsetAsync(d->Q.p, 0, cs * L * 8, st));
+        XMD_CUDA(cudaMemsetAsync(d->iQ.p, 0, cs * L * 8, st));
+      }
     } else {
       // grouped chains: first DOF and DOF count as the reference's loop
       // (md_simulation_x.c:664-668) computes them
@@ -390,12 +400,14 @@ int sim_device(md_simulation_t_x *sim, SimDev **out) {
       XMD_CUDA(cudaStreamSynchronize(st));  // the vectors above go out of scope
     }
     XMD_CUDA(xk::chains_to_dev(g, L, sim->Nf, fast, d->cstage.as<unsigned char>(), sizeof(md_nhc_t_x),
-                               d->th.as<double>(), d->vt.as<double>(), d->Q.as<double>(), st));
-    if (fast) {
-      XMD_TRY(reserve(d->iQ, S * L * 8));
-      XMD_CUDA(xk::inv_q(S * L, d->Q.as<double>(), d->iQ.as<double>(), st));
-    }
+                               d->th.as<double>(), d->vt.as<double>(), d->Q.as<double>(),
+                               fast ? d->iQ.as<double>() : nullptr, fresh_chains, st));
+    d->zth = fast ? d->th.p : nullptr;
   }
+  d->zx = d->x.p;
+  d->zN = g.N;
+  d->zNs = g.Ns;
+  d->zP = g.P;
   d->valid = true;
   return 0;
 }
