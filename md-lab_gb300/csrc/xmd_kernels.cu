@@ -167,13 +167,28 @@ static inline int cdiv(size_t a, int b) { return (int)((a + b - 1) / b); }
 // layout conversion
 // ===================================================================
 
+// The records are moved through shared memory a block at a time, so that
+// the reads (writes) of the record array are contiguous 8-byte words across
+// the block: the array may be the page-locked host array itself, read or
+// written by the kernel over the CPU-GPU link.
+constexpr int CONV_T = 256;  // particle records per block
+constexpr int CHAIN_T = 128;  // chain records per block (L <= 8: at most 25.6 KB staged)
+
 template <int D>
-__global__ void k_aos_to_soa(Geo g, const double *__restrict__ aos, double *x, double *v,
-                             double *f, double *m) {
-  const int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= g.N * g.P) return;
-  const int l = b / g.P, j = b % g.P;
-  const double *r = aos + (size_t)b * (1 + 3 * D);
+// mass_flag (optional) is cleared when a record's mass differs from the
+// first record's (bit pattern)
+__global__ void __launch_bounds__(CONV_T) k_aos_to_soa(Geo g, const double *__restrict__ aos, double *x, double *v,
+                                                       double *f, double *m, int *mass_flag) {
+  constexpr int RW = 1 + 3 * D;
+  __shared__ double sm[CONV_T * RW];
+  const int b0 = blockIdx.x * CONV_T, nb = min(CONV_T, g.N * g.P - b0);
+  const double *src = aos + (size_t)b0 * RW;
+  for (int q = threadIdx.x; q < nb * RW; q += CONV_T) sm[q] = src[q];
+  __syncthreads();
+  if ((int)threadIdx.x >= nb) return;
+  const int b = b0 + threadIdx.x, l = b / g.P, j = b % g.P;
+  const double *r = sm + threadIdx.x * RW;
+  if (mass_flag && __double_as_longlong(r[0]) != __double_as_longlong(aos[0])) atomicAnd(mass_flag, 0);
   m[(size_t)j * g.Ns + l] = r[0];
 #pragma unroll
   for (int d = 0; d < D; ++d) {
@@ -185,28 +200,34 @@ __global__ void k_aos_to_soa(Geo g, const double *__restrict__ aos, double *x, d
 }
 
 template <int D>
-__global__ void k_soa_to_aos(Geo g, double *__restrict__ aos, const double *x, const double *v,
-                             const double *f, const double *m) {
-  const int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= g.N * g.P) return;
-  const int l = b / g.P, j = b % g.P;
-  double *r = aos + (size_t)b * (1 + 3 * D);
-  r[0] = m[(size_t)j * g.Ns + l];
+__global__ void __launch_bounds__(CONV_T) k_soa_to_aos(Geo g, double *__restrict__ aos, const double *x,
+                                                       const double *v, const double *f, const double *m) {
+  constexpr int RW = 1 + 3 * D;
+  __shared__ double sm[CONV_T * RW];
+  const int b0 = blockIdx.x * CONV_T, nb = min(CONV_T, g.N * g.P - b0);
+  if ((int)threadIdx.x < nb) {
+    const int b = b0 + threadIdx.x, l = b / g.P, j = b % g.P;
+    double *r = sm + threadIdx.x * RW;
+    r[0] = m[(size_t)j * g.Ns + l];
 #pragma unroll
-  for (int d = 0; d < D; ++d) {
-    const size_t s = sidx(j, d, l, D, g.Ns);
-    r[1 + d] = x[s];
-    r[1 + D + d] = v[s];
-    r[1 + 2 * D + d] = f[s];
+    for (int d = 0; d < D; ++d) {
+      const size_t s = sidx(j, d, l, D, g.Ns);
+      r[1 + d] = x[s];
+      r[1 + D + d] = v[s];
+      r[1 + 2 * D + d] = f[s];
+    }
   }
+  __syncthreads();
+  double *dst = aos + (size_t)b0 * RW;
+  for (int q = threadIdx.x; q < nb * RW; q += CONV_T) dst[q] = sm[q];
 }
 
 cudaError_t aos_to_soa(const Geo &g, const double *aos, double *x, double *v, double *f,
-                       double *m, cudaStream_t st) {
+                       double *m, cudaStream_t st, int *mass_flag) {
   const int n = g.N * g.P;
   {
     XK_PROF("aos_to_soa");
-    DISPATCH_D(g.D, k_aos_to_soa<D><<<cdiv(n, 256), 256, 0, st>>>(g, aos, x, v, f, m));
+    DISPATCH_D(g.D, k_aos_to_soa<D><<<cdiv(n, CONV_T), CONV_T, 0, st>>>(g, aos, x, v, f, m, mass_flag));
   }
   return XK_LAUNCHED();
 }
@@ -216,7 +237,7 @@ cudaError_t soa_to_aos(const Geo &g, double *aos, const double *x, const double 
   const int n = g.N * g.P;
   {
     XK_PROF("soa_to_aos");
-    DISPATCH_D(g.D, k_soa_to_aos<D><<<cdiv(n, 256), 256, 0, st>>>(g, aos, x, v, f, m));
+    DISPATCH_D(g.D, k_soa_to_aos<D><<<cdiv(n, CONV_T), CONV_T, 0, st>>>(g, aos, x, v, f, m));
   }
   return XK_LAUNCHED();
 }
@@ -225,76 +246,69 @@ cudaError_t soa_to_aos(const Geo &g, double *aos, const double *x, const double 
 // starting at offset 8.  Fast chains go to slot order, grouped chains keep
 // the chain order.
 template <int D>
-__global__ void k_chains(Geo g, int L, int nf, bool fast, bool to_dev, unsigned char *rec,
-                         size_t rb, double *th, double *vt, double *Q, const int *cf, double *iQ, int all_iq) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= nf) return;
-  size_t slot, stride;
-  if (fast) {
-    const int b = c / D, d = c % D;
-    const int l = b / g.P, j = b % g.P;
-    slot = sidx(j, d, l, D, g.Ns);
-    stride = g.slots();
-  } else {
-    slot = c;
-    stride = nf;
+// f_flag (optional, upload) is cleared when a record's f differs from 1
+__global__ void __launch_bounds__(CHAIN_T) k_chains(Geo g, int L, int nf, bool fast, bool to_dev, unsigned char *rec,
+                                                   size_t rb, double *th, double *vt, double *Q, const int *cf,
+                                                   double *iQ, int all_iq, int *f_flag) {
+  // records staged as 8-byte words (rb is a multiple of 8), see k_aos_to_soa
+  extern __shared__ double csm[];
+  const int rw = (int)(rb / 8);
+  const int c0 = blockIdx.x * CHAIN_T, nb = min(CHAIN_T, nf - c0);
+  double *words = (double *)(rec + (size_t)c0 * rb);
+  if (to_dev) {
+    for (int q = threadIdx.x; q < nb * rw; q += CHAIN_T) csm[q] = words[q];
+    __syncthreads();
   }
-  double *r = (double *)(rec + (size_t)c * rb + 8);
-  if (!to_dev) {
-    // whole records go back: f (1 for one-DOF chains, else as uploaded), zero padding
-    int *fi = (int *)(rec + (size_t)c * rb);
-    fi[0] = fast ? 1 : cf[c];
-    fi[1] = 0;
-  }
-  for (int i = 0; i < L; ++i) {
-    if (to_dev) {
-      th[i * stride + slot] = r[i];
-      vt[i * stride + slot] = r[L + i];
-      // 1/Q only where Q changed (a re-upload of the same chains divides
-      // nothing)
-      const double q = r[2 * L + i];
-      if (iQ && (all_iq || q != Q[i * stride + slot])) iQ[i * stride + slot] = q != 0.0 ? 1.0 / q : 0.0;
-      Q[i * stride + slot] = q;
+  const int c = c0 + threadIdx.x;
+  if ((int)threadIdx.x < nb) {
+    size_t slot, stride;
+    if (fast) {
+      const int b = c / D, d = c % D;
+      const int l = b / g.P, j = b % g.P;
+      slot = sidx(j, d, l, D, g.Ns);
+      stride = g.slots();
     } else {
-      r[i] = th[i * stride + slot];
-      r[L + i] = vt[i * stride + slot];
-      r[2 * L + i] = Q[i * stride + slot];
+      slot = c;
+      stride = nf;
+    }
+    double *r = csm + threadIdx.x * rw + 1;
+    if (to_dev && f_flag && *(const int *)(csm + threadIdx.x * rw) != 1) atomicAnd(f_flag, 0);
+    if (!to_dev) {
+      // whole records go back: f (1 for one-DOF chains, else as uploaded), zero padding
+      int *fi = (int *)(csm + threadIdx.x * rw);
+      fi[0] = fast ? 1 : cf[c];
+      fi[1] = 0;
+    }
+    for (int i = 0; i < L; ++i) {
+      if (to_dev) {
+        th[i * stride + slot] = r[i];
+        vt[i * stride + slot] = r[L + i];
+        // 1/Q only where Q changed (a re-upload of the same chains divides
+        // nothing)
+        const double q = r[2 * L + i];
+        if (iQ && (all_iq || q != Q[i * stride + slot])) iQ[i * stride + slot] = q != 0.0 ? 1.0 / q : 0.0;
+        Q[i * stride + slot] = q;
+      } else {
+        r[i] = th[i * stride + slot];
+        r[L + i] = vt[i * stride + slot];
+        r[2 * L + i] = Q[i * stride + slot];
+      }
     }
   }
-}
-
-// Checks of freshly uploaded host records, so that the host need not walk
-// them: flags[0] stays nonzero when every particle has the first one's mass
-// (bit pattern), flags[1] when every chain record has f == 1.  The caller
-// sets both flags nonzero before the launch.
-__global__ void k_upload_checks(const unsigned char *__restrict__ prec, int np, size_t pbytes,
-                                const unsigned char *__restrict__ crec, int nc, size_t cbytes, int *flags) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  bool mass_ok = true, f_ok = true;
-  if (t < np)
-    mass_ok = *(const long long *)(prec + (size_t)t * pbytes) == *(const long long *)prec;
-  if (t < nc) f_ok = *(const int *)(crec + (size_t)t * cbytes) == 1;
-  if (!__all_sync(FULL, mass_ok) && (threadIdx.x & 31) == 0) atomicAnd(&flags[0], 0);
-  if (!__all_sync(FULL, f_ok) && (threadIdx.x & 31) == 0) atomicAnd(&flags[1], 0);
-}
-
-cudaError_t upload_checks(const unsigned char *prec, int np, size_t pbytes, const unsigned char *crec, int nc,
-                          size_t cbytes, int *flags, cudaStream_t st) {
-  const int n = np > nc ? np : nc;
-  if (n <= 0) return cudaSuccess;
-  {
-    XK_PROF("upload_checks");
-    k_upload_checks<<<cdiv(n, 256), 256, 0, st>>>(prec, np, pbytes, crec, nc, cbytes, flags);
+  if (!to_dev) {
+    __syncthreads();
+    for (int q = threadIdx.x; q < nb * rw; q += CHAIN_T) words[q] = csm[q];
   }
-  return XK_LAUNCHED();
 }
 
 cudaError_t chains_to_dev(const Geo &g, int L, int nf, bool fast, const unsigned char *rec,
-                          size_t rb, double *th, double *vt, double *Q, double *iQ, bool all_iq, cudaStream_t st) {
+                          size_t rb, double *th, double *vt, double *Q, double *iQ, bool all_iq, cudaStream_t st,
+                          int *f_flag) {
   {
     XK_PROF("chains");
-    DISPATCH_D(g.D, k_chains<D><<<cdiv(nf, 256), 256, 0, st>>>(g, L, nf, fast, true, (unsigned char *)rec, rb,
-                                                              th, vt, Q, nullptr, iQ, all_iq ? 1 : 0));
+    DISPATCH_D(g.D, k_chains<D><<<cdiv(nf, CHAIN_T), CHAIN_T, CHAIN_T * rb, st>>>(
+                        g, L, nf, fast, true, (unsigned char *)rec, rb, th, vt, Q, nullptr, iQ, all_iq ? 1 : 0,
+                        f_flag));
   }
   return XK_LAUNCHED();
 }
@@ -305,8 +319,9 @@ cudaError_t chains_to_host(const Geo &g, int L, int nf, bool fast, unsigned char
   if (!fast && !cf) return cudaErrorInvalidValue;
   {
     XK_PROF("chains");
-    DISPATCH_D(g.D, k_chains<D><<<cdiv(nf, 256), 256, 0, st>>>(
-                        g, L, nf, fast, false, rec, rb, (double *)th, (double *)vt, (double *)Q, cf, nullptr, 0));
+    DISPATCH_D(g.D, k_chains<D><<<cdiv(nf, CHAIN_T), CHAIN_T, CHAIN_T * rb, st>>>(
+                        g, L, nf, fast, false, rec, rb, (double *)th, (double *)vt, (double *)Q, cf, nullptr, 0,
+                        nullptr));
   }
   return XK_LAUNCHED();
 }

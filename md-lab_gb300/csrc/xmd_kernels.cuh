@@ -60,20 +60,17 @@ double fp64_peak_tflops(cudaStream_t st);
 double fp32_peak_tflops(cudaStream_t st);
 
 // ---- layout conversion (host AoS records <-> device SoA) ----
+// mass_flag (optional, nonzero before) := 0 unless every record has the
+// first one's mass (bit pattern)
 cudaError_t aos_to_soa(const Geo &g, const double *aos, double *x, double *v, double *f,
-                       double *m, cudaStream_t st);
+                       double *m, cudaStream_t st, int *mass_flag = nullptr);
 cudaError_t soa_to_aos(const Geo &g, double *aos, const double *x, const double *v,
                        const double *f, const double *m, cudaStream_t st);
 // chains: host records {int f; double theta[L], vtheta[L], Q[L]} of rec_bytes each
 // iQ (optional): 1/Q, updated where Q changes (everywhere with all_iq)
 cudaError_t chains_to_dev(const Geo &g, int L, int nf, bool fast, const unsigned char *rec,
                           size_t rec_bytes, double *th, double *vt, double *Q, double *iQ, bool all_iq,
-                          cudaStream_t st);
-// flags[0] := 0 unless every particle record (np of pbytes, mass first) has
-// the first one's mass; flags[1] := 0 unless every chain record (nc of
-// cbytes, int f first) has f == 1.  Flags start nonzero.
-cudaError_t upload_checks(const unsigned char *prec, int np, size_t pbytes, const unsigned char *crec, int nc,
-                          size_t cbytes, int *flags, cudaStream_t st);
+                          cudaStream_t st, int *f_flag = nullptr);  // f_flag := 0 unless every f is 1
 // whole records back, f included: 1 for one-DOF chains, cf[c] for grouped ones
 cudaError_t chains_to_host(const Geo &g, int L, int nf, bool fast, unsigned char *rec,
                            size_t rec_bytes, const double *th, const double *vt,

@@ -188,6 +188,13 @@ void host_free(void *p) {
   free(p);
 }
 
+// a page-locked array this library allocated (md_alloc_*): kernels read and
+// write it directly over the CPU-GPU link, with no staging copy
+static bool lib_pinned(const void *p) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  return g_pinned.count(const_cast<void *>(p)) != 0;
+}
+
 // ------------------------------------------------------------------
 // side tables
 // ------------------------------------------------------------------
@@ -338,72 +345,86 @@ int sim_device(md_simulation_t_x *sim, SimDev **out) {
     XMD_CUDA(cudaMemsetAsync(d->m.p, 0, (size_t)g.P * g.Ns * 8, st));
     d->zth = nullptr;
   }
-  // particle and chain records go up to their stages; whether all masses
-  // are equal and all chains have one DOF is checked there on the device
-  // (walking 13 MB of records on one host core took longer than the copies)
+  // Whether all masses are equal and all chains have one DOF is checked on
+  // the device while the records are converted (walking 13 MB of records on
+  // one host core took longer than the copies): the chain records are
+  // converted in the one-DOF layout when their count says so, and only if a
+  // record then shows f != 1 are they converted again in the grouped layout.
   d->nf = sim->Nf;
   d->L = L;
   const int nchain = sim->nhcs ? sim->Nf : 0;
   const size_t pbytes = sizeof(md_particle_t_x) * (size_t)sim->N;
   const size_t cbytes = sizeof(md_nhc_t_x) * (size_t)nchain;
-  XMD_TRY(reserve(d->stage, pbytes));
-  if (cbytes) XMD_TRY(reserve(d->cstage, cbytes));
   XMD_TRY(reserve(d->upflags, 2 * sizeof(int)));
   XMD_CUDA(cudaMemsetAsync(d->upflags.p, 0xff, 2 * sizeof(int), st));
-  XMD_CUDA(cudaMemcpyAsync(d->stage.p, sim->particles, pbytes, cudaMemcpyHostToDevice, st));
-  if (cbytes) XMD_CUDA(cudaMemcpyAsync(d->cstage.p, sim->nhcs, cbytes, cudaMemcpyHostToDevice, st));
-  XMD_CUDA(xk::upload_checks(d->stage.as<unsigned char>(), sim->N, sizeof(md_particle_t_x),
-                             d->cstage.as<unsigned char>(), nchain, sizeof(md_nhc_t_x), d->upflags.as<int>(), st));
-  XMD_CUDA(xk::aos_to_soa(g, d->stage.as<double>(), d->x.as<double>(), d->v.as<double>(),
-                          d->f.as<double>(), d->m.as<double>(), st));
+  // the library's own page-locked arrays are read in place; others go up
+  // to device stages first
+  const bool direct = lib_pinned(sim->particles) && (!cbytes || lib_pinned(sim->nhcs));
+  const unsigned char *prec = (const unsigned char *)sim->particles, *crec = (const unsigned char *)sim->nhcs;
+  if (!direct) {
+    XMD_TRY(reserve(d->stage, pbytes));
+    if (cbytes) XMD_TRY(reserve(d->cstage, cbytes));
+    XMD_CUDA(cudaMemcpyAsync(d->stage.p, sim->particles, pbytes, cudaMemcpyHostToDevice, st));
+    if (cbytes) XMD_CUDA(cudaMemcpyAsync(d->cstage.p, sim->nhcs, cbytes, cudaMemcpyHostToDevice, st));
+    prec = d->stage.as<unsigned char>();
+    crec = d->cstage.as<unsigned char>();
+  }
+  XMD_CUDA(xk::aos_to_soa(g, (const double *)prec, d->x.as<double>(), d->v.as<double>(), d->f.as<double>(),
+                          d->m.as<double>(), st, d->upflags.as<int>()));
+  const bool try_fast = nchain > 0 && sim->Nf == D * sim->N;
+  bool fresh_chains = true;
+  if (try_fast) {
+    XMD_TRY(reserve(d->th, S * L * 8));
+    XMD_TRY(reserve(d->vt, S * L * 8));
+    XMD_TRY(reserve(d->Q, S * L * 8));
+    XMD_TRY(reserve(d->iQ, S * L * 8));
+    fresh_chains = !(same_layout && d->zth == d->th.p);
+    if (fresh_chains) {
+      // padding slots stay zero (their 1/Q is 0, nothing divides by them)
+      XMD_CUDA(cudaMemsetAsync(d->th.p, 0, S * L * 8, st));
+      XMD_CUDA(cudaMemsetAsync(d->vt.p, 0, S * L * 8, st));
+      XMD_CUDA(cudaMemsetAsync(d->Q.p, 0, S * L * 8, st));
+      XMD_CUDA(cudaMemsetAsync(d->iQ.p, 0, S * L * 8, st));
+    }
+    XMD_CUDA(xk::chains_to_dev(g, L, sim->Nf, true, crec, sizeof(md_nhc_t_x), d->th.as<double>(),
+                               d->vt.as<double>(), d->Q.as<double>(), d->iQ.as<double>(), fresh_chains, st,
+                               d->upflags.as<int>() + 1));
+  }
   int flags[2] = {0, 0};
   XMD_CUDA(cudaMemcpyAsync(flags, d->upflags.p, sizeof flags, cudaMemcpyDeviceToHost, st));
   XMD_CUDA(cudaStreamSynchronize(st));
   d->uniform_mass = flags[0] != 0;
   d->mass0 = sim->particles[0].m;
-  const bool fast = nchain > 0 && sim->Nf == D * sim->N && flags[1] != 0;
+  const bool fast = try_fast && flags[1] != 0;
   d->fast_chains = fast;
-  if (sim->nhcs && sim->Nf > 0) {
-    const size_t cs = fast ? S : (size_t)sim->Nf;
+  if (sim->nhcs && sim->Nf > 0 && !fast) {
+    // grouped chains: first DOF and DOF count as the reference's loop
+    // (md_simulation_x.c:664-668) computes them
+    const size_t cs = (size_t)sim->Nf;
     XMD_TRY(reserve(d->th, cs * L * 8));
     XMD_TRY(reserve(d->vt, cs * L * 8));
     XMD_TRY(reserve(d->Q, cs * L * 8));
-    if (fast) XMD_TRY(reserve(d->iQ, S * L * 8));
-    const bool fresh_chains = !(fast && same_layout && d->zth == d->th.p);
-    if (fast) {
-      // padding slots stay zero (their 1/Q is 0, nothing divides by them)
-      if (fresh_chains) {
-        XMD_CUDA(cudaMemsetAsync(d->th.p, 0, cs * L * 8, st));
-        XMD_CUDA(cudaMemsetAsync(d->vt.p, 0, cs * L * 8, st));
-        XMD_CUDA(cudaMemsetAsync(d->Q.p, 0, cs * L * 8, st));
-        XMD_CUDA(cudaMemsetAsync(d->iQ.p, 0, cs * L * 8, st));
-      }
-    } else {
-      // grouped chains: first DOF and DOF count as the reference's loop
-      // (md_simulation_x.c:664-668) computes them
-      std::vector<int> cf(sim->Nf), c0(sim->Nf), c2(sim->Nf);
-      int f0 = 0;
-      for (int i = 0; i < sim->Nf; ++i) {
-        cf[i] = sim->nhcs[i].f;
-        c0[i] = f0;
-        c2[i] = (i == sim->Nf - 1) ? D * sim->N - f0 : cf[i];
-        if (f0 < 0 || c2[i] < 0 || f0 + c2[i] > D * sim->N)
-          return fail(MD_GB_ERR_ARG, "chain %d covers DOFs outside the simulation", i);
-        f0 += cf[i];
-      }
-      XMD_TRY(reserve(d->cf, sizeof(int) * sim->Nf));
-      XMD_TRY(reserve(d->c0, sizeof(int) * sim->Nf));
-      XMD_TRY(reserve(d->c2, sizeof(int) * sim->Nf));
-      XMD_CUDA(cudaMemcpyAsync(d->cf.p, cf.data(), sizeof(int) * sim->Nf, cudaMemcpyHostToDevice, st));
-      XMD_CUDA(cudaMemcpyAsync(d->c0.p, c0.data(), sizeof(int) * sim->Nf, cudaMemcpyHostToDevice, st));
-      XMD_CUDA(cudaMemcpyAsync(d->c2.p, c2.data(), sizeof(int) * sim->Nf, cudaMemcpyHostToDevice, st));
-      XMD_CUDA(cudaStreamSynchronize(st));  // the vectors above go out of scope
+    std::vector<int> cf(sim->Nf), c0(sim->Nf), c2(sim->Nf);
+    int f0 = 0;
+    for (int i = 0; i < sim->Nf; ++i) {
+      cf[i] = sim->nhcs[i].f;
+      c0[i] = f0;
+      c2[i] = (i == sim->Nf - 1) ? D * sim->N - f0 : cf[i];
+      if (f0 < 0 || c2[i] < 0 || f0 + c2[i] > D * sim->N)
+        return fail(MD_GB_ERR_ARG, "chain %d covers DOFs outside the simulation", i);
+      f0 += cf[i];
     }
-    XMD_CUDA(xk::chains_to_dev(g, L, sim->Nf, fast, d->cstage.as<unsigned char>(), sizeof(md_nhc_t_x),
-                               d->th.as<double>(), d->vt.as<double>(), d->Q.as<double>(),
-                               fast ? d->iQ.as<double>() : nullptr, fresh_chains, st));
-    d->zth = fast ? d->th.p : nullptr;
+    XMD_TRY(reserve(d->cf, sizeof(int) * sim->Nf));
+    XMD_TRY(reserve(d->c0, sizeof(int) * sim->Nf));
+    XMD_TRY(reserve(d->c2, sizeof(int) * sim->Nf));
+    XMD_CUDA(cudaMemcpyAsync(d->cf.p, cf.data(), sizeof(int) * sim->Nf, cudaMemcpyHostToDevice, st));
+    XMD_CUDA(cudaMemcpyAsync(d->c0.p, c0.data(), sizeof(int) * sim->Nf, cudaMemcpyHostToDevice, st));
+    XMD_CUDA(cudaMemcpyAsync(d->c2.p, c2.data(), sizeof(int) * sim->Nf, cudaMemcpyHostToDevice, st));
+    XMD_CUDA(xk::chains_to_dev(g, L, sim->Nf, false, crec, sizeof(md_nhc_t_x), d->th.as<double>(),
+                               d->vt.as<double>(), d->Q.as<double>(), nullptr, true, st));
+    XMD_CUDA(cudaStreamSynchronize(st));  // the vectors above go out of scope
   }
+  d->zth = fast ? d->th.p : nullptr;
   d->zx = d->x.p;
   d->zN = g.N;
   d->zNs = g.Ns;
@@ -421,18 +442,26 @@ int sim_to_host(md_simulation_t_x *sim, bool keep) {
   cudaStream_t st = stream();
   const xk::Geo &g = d->geo;
   const size_t pbytes = sizeof(md_particle_t_x) * (size_t)sim->N;
-  XMD_CUDA(xk::soa_to_aos(g, d->stage.as<double>(), d->x.as<double>(), d->v.as<double>(),
-                          d->f.as<double>(), d->m.as<double>(), st));
-  XMD_CUDA(cudaMemcpyAsync(sim->particles, d->stage.p, pbytes, cudaMemcpyDeviceToHost, st));
+  // the library's own page-locked arrays are written in place by the
+  // kernels; others come down through device stages
+  if (lib_pinned(sim->particles)) {
+    XMD_CUDA(xk::soa_to_aos(g, (double *)sim->particles, d->x.as<double>(), d->v.as<double>(), d->f.as<double>(),
+                            d->m.as<double>(), st));
+  } else {
+    XMD_TRY(reserve(d->stage, pbytes));
+    XMD_CUDA(xk::soa_to_aos(g, d->stage.as<double>(), d->x.as<double>(), d->v.as<double>(), d->f.as<double>(),
+                            d->m.as<double>(), st));
+    XMD_CUDA(cudaMemcpyAsync(sim->particles, d->stage.p, pbytes, cudaMemcpyDeviceToHost, st));
+  }
   if (sim->nhcs && sim->Nf > 0) {
-    // whole chain records (f as uploaded) through their own stage, straight
-    // into the page-locked host array
+    // whole chain records (f as uploaded)
     const size_t cbytes = sizeof(md_nhc_t_x) * (size_t)sim->Nf;
-    XMD_TRY(reserve(d->cstage, cbytes));
-    XMD_CUDA(xk::chains_to_host(g, d->L, sim->Nf, d->fast_chains, d->cstage.as<unsigned char>(),
-                                sizeof(md_nhc_t_x), d->th.as<double>(), d->vt.as<double>(),
-                                d->Q.as<double>(), d->cf.as<int>(), st));
-    XMD_CUDA(cudaMemcpyAsync(sim->nhcs, d->cstage.p, cbytes, cudaMemcpyDeviceToHost, st));
+    const bool direct = lib_pinned(sim->nhcs);
+    if (!direct) XMD_TRY(reserve(d->cstage, cbytes));
+    unsigned char *crec = direct ? (unsigned char *)sim->nhcs : d->cstage.as<unsigned char>();
+    XMD_CUDA(xk::chains_to_host(g, d->L, sim->Nf, d->fast_chains, crec, sizeof(md_nhc_t_x), d->th.as<double>(),
+                                d->vt.as<double>(), d->Q.as<double>(), d->cf.as<int>(), st));
+    if (!direct) XMD_CUDA(cudaMemcpyAsync(sim->nhcs, d->cstage.p, cbytes, cudaMemcpyDeviceToHost, st));
   }
   XMD_CUDA(cudaStreamSynchronize(st));
   if (!keep) d->valid = false;
