@@ -171,6 +171,18 @@ static inline int cdiv(size_t a, int b) { return (int)((a + b - 1) / b); }
 // the reads (writes) of the record array are contiguous 8-byte words across
 // the block: the array may be the page-locked host array itself, read or
 // written by the kernel over the CPU-GPU link.
+// n 8-byte words from src to dst, both 16-byte aligned, by the block's
+// threads in 16-byte pieces, several loads in flight a thread (the source or
+// destination may be host memory across the CPU-GPU link)
+__device__ inline void block_copy_words(double *__restrict__ dst, const double *__restrict__ src, int n, int nthr) {
+  const int n2 = n >> 1;
+  const double2 *s2 = (const double2 *)src;
+  double2 *d2 = (double2 *)dst;
+#pragma unroll 4
+  for (int q = threadIdx.x; q < n2; q += nthr) d2[q] = s2[q];
+  if ((n & 1) && threadIdx.x == 0) dst[n - 1] = src[n - 1];
+}
+
 constexpr int CONV_T = 256;  // particle records per block
 constexpr int CHAIN_T = 128;  // chain records per block (L <= 8: at most 25.6 KB staged)
 
@@ -180,10 +192,9 @@ template <int D>
 __global__ void __launch_bounds__(CONV_T) k_aos_to_soa(Geo g, const double *__restrict__ aos, double *x, double *v,
                                                        double *f, double *m, int *mass_flag) {
   constexpr int RW = 1 + 3 * D;
-  __shared__ double sm[CONV_T * RW];
+  __shared__ __align__(16) double sm[CONV_T * RW];
   const int b0 = blockIdx.x * CONV_T, nb = min(CONV_T, g.N * g.P - b0);
-  const double *src = aos + (size_t)b0 * RW;
-  for (int q = threadIdx.x; q < nb * RW; q += CONV_T) sm[q] = src[q];
+  block_copy_words(sm, aos + (size_t)b0 * RW, nb * RW, CONV_T);
   __syncthreads();
   if ((int)threadIdx.x >= nb) return;
   const int b = b0 + threadIdx.x, l = b / g.P, j = b % g.P;
@@ -203,7 +214,7 @@ template <int D>
 __global__ void __launch_bounds__(CONV_T) k_soa_to_aos(Geo g, double *__restrict__ aos, const double *x,
                                                        const double *v, const double *f, const double *m) {
   constexpr int RW = 1 + 3 * D;
-  __shared__ double sm[CONV_T * RW];
+  __shared__ __align__(16) double sm[CONV_T * RW];
   const int b0 = blockIdx.x * CONV_T, nb = min(CONV_T, g.N * g.P - b0);
   if ((int)threadIdx.x < nb) {
     const int b = b0 + threadIdx.x, l = b / g.P, j = b % g.P;
@@ -218,8 +229,7 @@ __global__ void __launch_bounds__(CONV_T) k_soa_to_aos(Geo g, double *__restrict
     }
   }
   __syncthreads();
-  double *dst = aos + (size_t)b0 * RW;
-  for (int q = threadIdx.x; q < nb * RW; q += CONV_T) dst[q] = sm[q];
+  block_copy_words(aos + (size_t)b0 * RW, sm, nb * RW, CONV_T);
 }
 
 cudaError_t aos_to_soa(const Geo &g, const double *aos, double *x, double *v, double *f,
@@ -250,13 +260,14 @@ template <int D>
 __global__ void __launch_bounds__(CHAIN_T) k_chains(Geo g, int L, int nf, bool fast, bool to_dev, unsigned char *rec,
                                                    size_t rb, double *th, double *vt, double *Q, const int *cf,
                                                    double *iQ, int all_iq, int *f_flag) {
-  // records staged as 8-byte words (rb is a multiple of 8), see k_aos_to_soa
-  extern __shared__ double csm[];
+  // records staged as 8-byte words (rb is a multiple of 8), see k_aos_to_soa;
+  // a block's records start 16-byte aligned (CHAIN_T rb is a multiple of 16)
+  extern __shared__ __align__(16) double csm[];
   const int rw = (int)(rb / 8);
   const int c0 = blockIdx.x * CHAIN_T, nb = min(CHAIN_T, nf - c0);
   double *words = (double *)(rec + (size_t)c0 * rb);
   if (to_dev) {
-    for (int q = threadIdx.x; q < nb * rw; q += CHAIN_T) csm[q] = words[q];
+    block_copy_words(csm, words, nb * rw, CHAIN_T);
     __syncthreads();
   }
   const int c = c0 + threadIdx.x;
@@ -297,7 +308,7 @@ __global__ void __launch_bounds__(CHAIN_T) k_chains(Geo g, int L, int nf, bool f
   }
   if (!to_dev) {
     __syncthreads();
-    for (int q = threadIdx.x; q < nb * rw; q += CHAIN_T) words[q] = csm[q];
+    block_copy_words(words, csm, nb * rw, CHAIN_T);
   }
 }
 
