@@ -4190,12 +4190,32 @@ cudaError_t pair_force32(const Geo &g, const PairPrm &p, const double *x, const 
 
 // ---- reciprocal space, mixed ----------------------------------------
 // FP32 copies of the FP64 phase factors: ph32[((j*3 + d)*(NS+1) + n)*Ns + l]
-__global__ void k_phase_to32(Geo g, int ns, const double2 *__restrict__ ph, float2 *__restrict__ ph32) {
+// FP32 phases straight from the positions (the layout of k_phase): the
+// fraction of x/L is taken in FP64 (exact), the sine and cosine of the
+// reduced angle in FP32, the harmonics by FP32 complex products; the
+// results match k_phase's rounded to FP32 to a few FP32 units, without the
+// FP64 sine and cosine.
+__global__ void k_phase32(Geo g, int ns, const double *__restrict__ x, float2 *__restrict__ ph32) {
   const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const size_t n = (size_t)g.P * 3 * (ns + 1) * g.Ns;
-  if (t >= n) return;
-  const double2 v = ph[t];
-  ph32[t] = make_float2((float)v.x, (float)v.y);
+  if (t >= (size_t)g.P * 3 * g.Ns) return;
+  const int l = (int)(t % g.Ns);
+  const int jd = (int)(t / g.Ns);  // j*3 + d
+  const int d = jd % 3;
+  float s1 = 0.f, c1 = 1.f;
+  if (l < g.N) {
+    double u = x[t] * g.inv_box[d];
+    u -= rint(u);  // in [-1/2, 1/2]
+    sincospif((float)(2.0 * u), &s1, &c1);
+  }
+  float re = 1.f, im = 0.f;
+  float2 *o = ph32 + (size_t)jd * (ns + 1) * g.Ns + l;
+  o[0] = make_float2(1.f, 0.f);
+  for (int n = 1; n <= ns; ++n) {
+    const float r2 = fmaf(re, c1, -im * s1), i2 = fmaf(re, s1, im * c1);
+    re = r2;
+    im = i2;
+    o[(size_t)n * g.Ns] = make_float2(re, im);
+  }
 }
 
 __device__ inline float2 cmulf(float2 a, float2 b) {
@@ -4355,20 +4375,13 @@ cudaError_t recip_force32(const Geo &g, const Recip &r, const double *x, double 
                           cudaStream_t st) {
   if (g.D != 3) return cudaErrorInvalidValue;
   const size_t n = (size_t)g.P * 3 * g.Ns;
-  {
-    XK_PROF("phase");
-    k_phase<<<cdiv(n, 256), 256, 0, st>>>(g, r.nsum, x, (double2 *)r.phase);
-  }
-  cudaError_t e = XK_LAUNCHED();
-  if (e != cudaSuccess) return e;
   // FP32 phases live behind the FP64 ones in the same buffer
   float2 *ph32 = (float2 *)(r.phase + recip_phase_doubles(g, r.nsum));
-  const size_t np = (size_t)g.P * 3 * (r.nsum + 1) * g.Ns;
   {
-    XK_PROF("phase_to32");
-    k_phase_to32<<<cdiv(np, 256), 256, 0, st>>>(g, r.nsum, (const double2 *)r.phase, ph32);
+    XK_PROF("phase32");
+    k_phase32<<<cdiv(n, 256), 256, 0, st>>>(g, r.nsum, x, ph32);
   }
-  e = XK_LAUNCHED();
+  cudaError_t e = XK_LAUNCHED();
   if (e != cudaSuccess) return e;
   const int nc = r.ncol;
   dim3 tgrid((nc + 7) / 8, g.P), tblk(r.nsum + 1, 8);
