@@ -600,6 +600,13 @@ cudaError_t zero(double *p, size_t n, cudaStream_t st) {
   return cudaMemsetAsync(p, 0, n * sizeof(double), st);
 }
 
+__global__ void k_set_value(double *p, double v) { *p = v; }
+
+cudaError_t set_value(double *p, double v, cudaStream_t st) {
+  k_set_value<<<1, 1, 0, st>>>(p, v);
+  return cudaGetLastError();
+}
+
 // ===================================================================
 // cycle spring energies E_l^(k): md_pimd_x.c:1969-2210 (CPU :2086-2207)
 // ===================================================================

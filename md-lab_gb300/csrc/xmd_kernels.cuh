@@ -91,6 +91,8 @@ cudaError_t nhc_vv3(const Geo &g, int half, const Chains &c, double *x, double *
                     const double *f, const double *m, double kT, double h, cudaStream_t st);
 cudaError_t wrap_box(const Geo &g, double *x, cudaStream_t st);
 cudaError_t zero(double *p, size_t n, cudaStream_t st);
+// *p = v in stream order (a value from the host without a host buffer)
+cudaError_t set_value(double *p, double v, cudaStream_t st);
 
 // ---- exchange ----
 // gl: scratch of 2N doubles (the row increments and their prefix sums)

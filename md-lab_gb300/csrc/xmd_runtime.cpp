@@ -551,8 +551,9 @@ int stats_device(md_stats_t_x *s, double **acc) {
   if (!d->valid) {
     if (capturing()) return fail(MD_GB_ERR_CAPTURE, "accumulator is not on the device yet");
     XMD_TRY(reserve(d->acc, 8));
-    XMD_CUDA(cudaMemcpyAsync(d->acc.p, &s->es[s->N - 1], 8, cudaMemcpyHostToDevice, stream()));
-    XMD_CUDA(cudaStreamSynchronize(stream()));
+    // the host value travels as a kernel argument: no copy from host memory
+    // in flight, so no synchronisation
+    XMD_CUDA(xk::set_value(d->acc.as<double>(), s->es[s->N - 1], stream()));
     d->valid = true;
   }
   *acc = d->acc.as<double>();
