@@ -371,8 +371,10 @@ def learned_form(lib, R, s, pair, step, args, ws):
     """Truncated Ewald (|n| <= NSUM_CHEAP) + the residual network, FP32 forces.
     Data from plain runs of this system (converged Ewald, mixed forces),
     training on the GPU, then the timed run with the converged sum as judge
-    every JUDGE_EVERY steps (the judge's converged step and its FP64
-    judgement are inside the timed region)."""
+    every JUDGE_EVERY steps: after every JUDGE_EVERY-th learned step the
+    configuration is judged (converged FP64 reciprocal sums, truncated sums
+    and network, compared; inside the timed region).  A failed judgement
+    sends the rest of the run to the converged step."""
     import xmd_x
     lib.check(lib.md_gb300_set_precision_x(1))
     box, _ = workload()
@@ -398,7 +400,9 @@ def learned_form(lib, R, s, pair, step, args, ws):
     judges = []
 
     def judge_step():
-        lib.check(lib.md_gb300_graph_launch_x(g_conv, 1))
+        lib.check(lib.md_gb300_graph_launch_x(g_conv if state["reverted"] else g_learn, 1))
+        if state["reverted"]:
+            return
         j = m.judge(s)
         judges.append(j)
         if j["force_err"] > args.force_tol or j["energy_err"] > args.energy_tol:
@@ -693,8 +697,8 @@ def run_gb300(args, dist, rank, ws):
     # with read_only = 0) and up again (the step's first call, the periodic
     # wrap, uploads it), the step replays as a captured graph, and the
     # primitive estimator is read back.  The learned headline judges as in its
-    # timed run: every JUDGE_EVERY-th step is the converged step plus the FP64
-    # judgement, so the e2e run covers JUDGE_EVERY steps.
+    # timed run: every JUDGE_EVERY-th step is followed by the FP64 judgement of
+    # its configuration, so the e2e run covers JUDGE_EVERY steps.
     wrap = lambda: lib.check(lib.md_periodic_boundary_x(s.sim))  # noqa: E731
     if model is not None:
         model.detach(s)
@@ -714,13 +718,10 @@ def run_gb300(args, dist, rank, ws):
         if not lib.md_simulation_sync_host_x(s.sim, 0):  # device -> host, host authoritative
             raise RuntimeError(lib.err())
         wrap()  # uploads the host state (positions are already inside the box)
-        if g_conv is not None and (dropped or i % JUDGE_EVERY == 0):
-            lib.check(lib.md_gb300_graph_launch_x(g_conv, 1))
-            if not dropped:
-                j = model.judge(s)
-                dropped = j["force_err"] > args.force_tol or j["energy_err"] > args.energy_tol
-        else:
-            lib.check(lib.md_gb300_graph_launch_x(g_main, 1))
+        lib.check(lib.md_gb300_graph_launch_x(g_conv if dropped else g_main, 1))
+        if g_conv is not None and not dropped and i % JUDGE_EVERY == 0:
+            j = model.judge(s)
+            dropped = j["force_err"] > args.force_tol or j["energy_err"] > args.energy_tol
         lib.check(lib.md_pimd_calc_VBN_energy_x(s.pimd, s.stats))
         s.take_energy()  # estimator read
     if not lib.md_simulation_sync_host_x(s.sim, 1):
