@@ -657,16 +657,15 @@ __global__ void k_eint(Geo g, const double *__restrict__ x, const double *__rest
 }
 
 
-// exclusive prefix sums G[n] = gl[0] + ... + gl[n-1] (n = 0..N-1) into
-// gl[N + n]: one block, a fixed order (contiguous runs per thread, then the
-// run totals scanned over the block)
-__global__ void __launch_bounds__(1024) k_gscan(int N, double *__restrict__ gl) {
+// exclusive prefix sums out[c] = in[0] + ... + in[c-1] (c = 0..n) by the
+// block, in a fixed order (contiguous runs per thread, then the run totals
+// scanned over the block): every block that calls it gets the same numbers
+__device__ inline void block_exclusive_prefix(const double *__restrict__ in, int n, double *out) {
   __shared__ double wsum[32];
-  const int n = N - 1;  // increments
   const int per = (n + blockDim.x - 1) / blockDim.x;
   const int a = min(n, (int)threadIdx.x * per), b = min(n, a + per);
   double run = 0.0;
-  for (int c = a; c < b; ++c) run += gl[c];
+  for (int c = a; c < b; ++c) run += in[c];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   double inc = run;
 #pragma unroll
@@ -688,10 +687,16 @@ __global__ void __launch_bounds__(1024) k_gscan(int N, double *__restrict__ gl) 
   __syncthreads();
   double pre = (w > 0 ? wsum[w - 1] : 0.0) + (inc - run);
   for (int c = a; c < b; ++c) {
-    gl[N + c] = pre;
-    pre += gl[c];
+    out[c] = pre;
+    pre += in[c];
   }
-  if (threadIdx.x == blockDim.x - 1) gl[N + n] = pre;
+  if (threadIdx.x == blockDim.x - 1) out[n] = pre;
+}
+
+// the prefix sums of the N-1 ENk increments into gl[N ..] (one block), for
+// systems too large to hold them in each k_enk_direct block
+__global__ void __launch_bounds__(1024) k_gscan(int N, double *__restrict__ gl) {
+  block_exclusive_prefix(gl, N - 1, gl + N);
 }
 
 // E_l^(k) for k = 2..l (1-based row l) in closed form.
@@ -701,18 +706,28 @@ __global__ void __launch_bounds__(1024) k_gscan(int N, double *__restrict__ gl) 
 //   E_l^(k) = Eint[l] + (G[l-1] - G[l-k]) + link(l, l-k+1),
 // G the prefix sums of Eint[c] + link(c, c+1): every entry independent, one
 // spring each (no N x N table of springs, no scan along the row).
+// With own_g, every block scans the increments itself into shared memory
+// (N doubles): a separate scan launch on the sequential path costs more than
+// the repeated scan.
 template <int D>
 __global__ void __launch_bounds__(256) k_enk_direct(Geo g, const double *__restrict__ x,
                                                     const double *__restrict__ m, double w2, int image,
                                                     const double *__restrict__ Eint,
-                                                    const double *__restrict__ gl, double *__restrict__ ENk) {
+                                                    const double *__restrict__ gl, double *__restrict__ ENk,
+                                                    int own_g) {
+  extern __shared__ double Gs[];
+  const double *G = gl + g.N;
+  if (own_g) {
+    block_exclusive_prefix(gl, g.N - 1, Gs);
+    __syncthreads();
+    G = Gs;
+  }
   // rows l1 and N+2-l1 (l1-1 and N+1-l1 entries, N together) share a block
   const int l1 = blockIdx.x + 2, l2 = g.N - blockIdx.x;
   const int n1 = l1 - 1, n = n1 + (l2 > l1 ? l2 - 1 : 0);
   for (int e = threadIdx.x; e < n; e += blockDim.x) {
     const int l = e < n1 ? l1 : l2, k = 2 + (e < n1 ? e : e - n1);  // 1-based row, cycle length
-    ENk[dtri(l) + k - 1] =
-        Eint[l - 1] + ((gl[g.N + l - 1] - gl[g.N + l - k]) + link<D>(g, x, m, w2, l - 1, l - k, image));
+    ENk[dtri(l) + k - 1] = Eint[l - 1] + ((G[l - 1] - G[l - k]) + link<D>(g, x, m, w2, l - 1, l - k, image));
   }
 }
 
@@ -724,15 +739,19 @@ cudaError_t fill_enk(const Geo &g, const double *x, const double *m, double w2, 
   }
   cudaError_t e = XK_LAUNCHED();
   if (e != cudaSuccess || g.N < 2) return e;
-  {
-    XK_PROF("gscan");
-    k_gscan<<<1, 1024, 0, st>>>(g.N, gl);
+  const bool own_g = g.N <= 6000;  // N doubles of shared memory a block (within 48 KB)
+  if (!own_g) {
+    {
+      XK_PROF("gscan");
+      k_gscan<<<1, 1024, 0, st>>>(g.N, gl);
+    }
+    e = XK_LAUNCHED();
+    if (e != cudaSuccess) return e;
   }
-  e = XK_LAUNCHED();
-  if (e != cudaSuccess) return e;
   {
     XK_PROF("enk_direct");
-    DISPATCH_D(g.D, k_enk_direct<D><<<g.N / 2, 256, 0, st>>>(g, x, m, w2, image, Eint, gl, ENk));
+    DISPATCH_D(g.D, k_enk_direct<D><<<g.N / 2, 256, own_g ? sizeof(double) * g.N : 0, st>>>(
+                        g, x, m, w2, image, Eint, gl, ENk, own_g ? 1 : 0));
   }
   return XK_LAUNCHED();
 }
