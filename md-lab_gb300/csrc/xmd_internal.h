@@ -123,6 +123,9 @@ void forget(const void *key);
 
 // device copies, created on demand
 int sim_device(md_simulation_t_x *sim, SimDev **out);
+// sim_device, with sim's pending exchange forces handed back in *fex (null
+// if none) instead of added to f: the caller's kernel adds them
+int sim_device_fex(md_simulation_t_x *sim, SimDev **out, const double **fex);
 int sim_to_host(md_simulation_t_x *sim, bool keep);
 int pimd_device(md_pimd_t_x *pimd, SimDev **sd, PimdDev **pd);
 int pimd_to_host(md_pimd_t_x *pimd, bool keep);

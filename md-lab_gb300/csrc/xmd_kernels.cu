@@ -409,7 +409,7 @@ __device__ inline void chain_odd(ChainState<L> &c, double h, const double *nhf) 
 template <int D, int L>
 __global__ void __launch_bounds__(256) k_nhc_fast(Geo g, int half, double *__restrict__ x,
                                                   double *__restrict__ v,
-                                                  const double *__restrict__ f,
+                                                  double *__restrict__ f, const double *__restrict__ fex,
                                                   const double *__restrict__ m,
                                                   double *__restrict__ th, double *__restrict__ vt,
                                                   const double *__restrict__ Q, const double *__restrict__ iQ,
@@ -431,7 +431,11 @@ __global__ void __launch_bounds__(256) k_nhc_fast(Geo g, int half, double *__res
   }
   const double mass = m[(size_t)j * g.Ns + l];
   double vv = v[s];
-  const double F = f[s];
+  double F = f[s];
+  if (fex) {  // the pending exchange forces, as add_into would add them
+    F += fex[s];
+    f[s] = F;
+  }
   double nhf[L];
   if (half == 1) chain_forces<L, true>(c, mass * vv * vv, 1.0, kT, nhf);
   // thermostatted half kick: md_simulation_x.c:674-678
@@ -554,15 +558,19 @@ __global__ void k_nhc_grouped(Geo g, int half, int nf, const int *__restrict__ c
   }
 
 cudaError_t nhc_vv3(const Geo &g, int half, const Chains &c, double *x, double *v,
-                    const double *f, const double *m, double kT, double h, cudaStream_t st) {
+                    double *f, const double *m, double kT, double h, cudaStream_t st, const double *fex) {
   if (c.fast) {
     const size_t S = g.slots();
     {
       XK_PROF("nhc_fast");
       DISPATCH_D(g.D, DISPATCH_L(c.L, k_nhc_fast<D, LL><<<cdiv(S, 256), 256, 0, st>>>(
-                                          g, half, x, v, f, m, c.th, c.vt, c.Q, c.iQ, kT, h)));
+                                          g, half, x, v, f, fex, m, c.th, c.vt, c.Q, c.iQ, kT, h)));
     }
   } else {
+    if (fex) {
+      cudaError_t e = add_into(f, fex, g.slots(), st);
+      if (e != cudaSuccess) return e;
+    }
     {
       XK_PROF("nhc_grouped");
       DISPATCH_D(g.D, DISPATCH_L(c.L, k_nhc_grouped<D, LL><<<cdiv(c.nf, 128), 128, 0, st>>>(

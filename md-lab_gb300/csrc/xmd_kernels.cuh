@@ -87,8 +87,11 @@ struct Chains {
   const int *c2;        // grouped: number of DOFs updated
   int ndof;             // D * beads
 };
+// fex (optional): exchange forces still to be added to f, added (and f
+// updated) by the half step itself
 cudaError_t nhc_vv3(const Geo &g, int half, const Chains &c, double *x, double *v,
-                    const double *f, const double *m, double kT, double h, cudaStream_t st);
+                    double *f, const double *m, double kT, double h, cudaStream_t st,
+                    const double *fex = nullptr);
 cudaError_t wrap_box(const Geo &g, double *x, cudaStream_t st);
 cudaError_t zero(double *p, size_t n, cudaStream_t st);
 // *p = v in stream order (a value from the host without a host buffer)

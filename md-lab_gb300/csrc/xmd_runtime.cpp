@@ -121,7 +121,9 @@ int side_end(SimDev *fex) {
   return 0;
 }
 
-int join_side() {
+// join; mine's exchange forces are not added but handed back in *fex (the
+// caller's next kernel adds them on its way)
+static int join_side_taking(SimDev *mine, const double **fex) {
   if (t_nojoin) return 0;
   auto it = g_side.find(stream());
   if (it == g_side.end() || !it->second.pending) return 0;
@@ -130,9 +132,15 @@ int join_side() {
   XMD_CUDA(cudaStreamWaitEvent(stream(), sd.done, 0));
   std::vector<SimDev *> add;
   add.swap(sd.fex);
-  for (SimDev *d : add) XMD_CUDA(xk::add_into(d->f.as<double>(), d->fex.as<double>(), d->geo.slots(), stream()));
+  for (SimDev *d : add) {
+    if (d == mine && fex)
+      *fex = d->fex.as<double>();
+    else
+      XMD_CUDA(xk::add_into(d->f.as<double>(), d->fex.as<double>(), d->geo.slots(), stream()));
+  }
   return 0;
 }
+int join_side() { return join_side_taking(nullptr, nullptr); }
 
 int reserve(DevBuf &b, size_t bytes) {
   if (bytes <= b.bytes && b.p) return 0;
@@ -431,6 +439,15 @@ int sim_device(md_simulation_t_x *sim, SimDev **out) {
   d->zP = g.P;
   d->valid = true;
   return 0;
+}
+
+int sim_device_fex(md_simulation_t_x *sim, SimDev **out, const double **fex) {
+  *fex = nullptr;
+  if (sim && device_present() && g_own) {
+    SimDev *d = lookup(g_sim, sim, false);
+    if (d && d->valid) XMD_TRY(join_side_taking(d, fex));
+  }
+  return sim_device(sim, out);
 }
 
 int sim_to_host(md_simulation_t_x *sim, bool keep) {

@@ -125,11 +125,15 @@ int md_reset_force_x(md_simulation_t_x *sim) {
 
 static int nhc(md_simulation_t_x *sim, md_num_t_x h, int half) {
   SimDev *sd;
-  XMD_TRY(sim_device(sim, &sd));
-  if (sd->nf < 1) return 0;
-  if (sd->L % 2 || sd->L > 8) return fail(MD_GB_ERR_UNSUPPORTED, "chain length %d (even, <= 8 supported)", sd->L);
+  const double *fex;  // exchange forces still to be added to f, if any
+  XMD_TRY(sim_device_fex(sim, &sd, &fex));
+  if (sd->nf < 1 || sd->L % 2 || sd->L > 8) {
+    if (fex) XMD_CUDA(xk::add_into(sd->f.as<double>(), fex, sd->geo.slots(), stream()));
+    if (sd->nf < 1) return 0;
+    return fail(MD_GB_ERR_UNSUPPORTED, "chain length %d (even, <= 8 supported)", sd->L);
+  }
   XMD_CUDA(xk::nhc_vv3(sd->geo, half, chains_of(sd), sd->x.as<double>(), sd->v.as<double>(),
-                       sd->f.as<double>(), sd->m.as<double>(), MD_kB_X * sim->T, h, stream()));
+                       sd->f.as<double>(), sd->m.as<double>(), MD_kB_X * sim->T, h, stream(), fex));
   return 0;
 }
 
