@@ -655,12 +655,17 @@ __global__ void k_eint(Geo g, const double *__restrict__ x, const double *__rest
   for (int j = lane; j + 1 < g.P; j += 32)
     res += 0.5 * m[(size_t)j * g.Ns + l] * w2 * spring2<D>(g, x, j, l, j + 1, l, image);
   res = warp_sum(res);
-  if (lane == 0) {
-    Eint[l] = res;
-    const int jP = g.P - 1;
-    ENk[dtri(l + 1)] = res + 0.5 * m[(size_t)jP * g.Ns + l] * w2 * spring2<D>(g, x, jP, l, 0, l, image);
-  } else if (lane == 1 && l + 1 < g.N) {
-    gl[l] = res + link<D>(g, x, m, w2, l, l + 1, image);
+  // lane 0: the closing spring of l (E_l^(1)); lane 1: the link to l+1 (the
+  // increment of the prefix sums), both in one pass
+  if (lane < 2) {
+    const int b = lane == 0 ? l : (l + 1 < g.N ? l + 1 : l);
+    const double lk = link<D>(g, x, m, w2, l, b, image);
+    if (lane == 0) {
+      Eint[l] = res;
+      ENk[dtri(l + 1)] = res + lk;
+    } else if (l + 1 < g.N) {
+      gl[l] = res + lk;
+    }
   }
 }
 
