@@ -212,8 +212,8 @@ def n_images(xcut=5.8):
 
 
 # algorithmic work per launch of each kernel (FMA = 2 flops); the same count
-# for the FP64 and FP32 versions of a kernel (the design doc section 4 derives
-# each from the kernel's arithmetic)
+# for the FP64 and FP32 versions of a kernel, each derived from the kernel's
+# arithmetic per pair, image or wave vector
 def kept_nz_pairs(nsum):
     """sum over the kept wave-vector columns (nx, ny) of their largest kept
     |nz|: the library leaves out vectors whose force weight |G| c(n) is
