@@ -4093,11 +4093,14 @@ __global__ void __launch_bounds__(256, 3) k_pair_tiles32(Geo g, P32 q, const flo
 }
 
 // FP32 copies of the positions and inverse masses for the FP32 pair kernel
+// FP32 positions and (im32 non-null: beads of different masses) inverse
+// masses; with one mass for all beads the tiles apply it to their sums and
+// no division is taken here
 __global__ void k_to32(Geo g, const double *__restrict__ x, const double *__restrict__ m, float *__restrict__ x32,
                        float *__restrict__ im32) {
   const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t < g.slots()) x32[t] = (float)x[t];
-  if (t < (size_t)g.P * g.Ns) im32[t] = (float)(1.0 / m[t]);
+  if (im32 && t < (size_t)g.P * g.Ns) im32[t] = (float)(1.0 / m[t]);
 }
 
 // f += scale * sum over the T partial slots, in double
@@ -4188,7 +4191,7 @@ cudaError_t pair_force32(const Geo &g, const PairPrm &p, const double *x, const 
   float *im32 = x32 + g.slots();
   {
     XK_PROF("to32");
-    k_to32<<<cdiv(g.slots(), 256), 256, 0, st>>>(g, x, m, x32, im32);
+    k_to32<<<cdiv(g.slots(), 256), 256, 0, st>>>(g, x, m, x32, q.uniform ? nullptr : im32);
   }
   cudaError_t le = XK_LAUNCHED();
   if (le != cudaSuccess) return le;
