@@ -105,20 +105,29 @@ double md_gb300_fp32_peak_x(void);
 
    Limit: ceil(N/32) * P * D * ld <= 524288 doubles (for example N = 256,
    P = 64 in 3D); larger configurations are refused with MD_GB_ERR_ARG.
+   The arithmetic is always FP64 (the MD_GB_PRECISION_FP64 kernel), whatever
+   md_gb300_set_precision_x selected for the other calls.
    The first call on each device looks up the array's device address with
    that device current.  All calls share the array, so calls that overlap
    on the GPU (different streams, or several host threads) race; nothing in
-   the array needs clearing between calls. */
+   the array needs clearing between calls.  A launch error left pending by
+   the caller's own earlier work is reported as MD_GB_ERR_CUDA before this
+   call launches anything. */
 int md_gb300_pair_force_noalloc_x(md_pair_force_t_x pf, const double *x, const double *m, double *f, int N, int P,
                                   int ld, const double *L, void *stream);
 
 /* Arithmetic of the pair forces (md_pimd_calc_pair_force_x), including
    both Ewald parts.  MD_GB_PRECISION_FP64 (default) reproduces MD-Lab to
    1e-10.  MD_GB_PRECISION_MIXED evaluates pair and real-space Ewald forces in
-   FP32 with compensated (Kahan) accumulation and the reciprocal sum with FP32
-   phase products accumulated in double-float; positions, the exchange
-   recursion, springs, the thermostat and every estimator stay FP64.  The
-   force error against the FP64 form is about 1e-6 of the force scale. */
+   FP32: each lane adds at most 32 FP32 pair terms (one 32 x 32 tile), and
+   the tile partials are added in FP64; the reciprocal sum uses FP32 phase
+   products accumulated in double-float (two-sum) structure factors.
+   Positions, the exchange recursion, springs, the thermostat and every
+   estimator stay FP64.  The force error against the FP64 form, measured as
+   max |f32 - f64| / max |f64| over all beads of the 512-electron, 64-bead
+   electron gas (Ewald |n| <= 10), is 2.1e-5 and set mainly by the FP32
+   rounding of the pair separations; the library's tests bound it by 5e-5
+   there and on the smaller systems they run. */
 /* Tile shape of the FP32 pair kernel (the mixed form) for pimd's system
    shape, chosen by timing: warps of 32 x 32 pair tiles per thread block, 1,
    2, 4 or 8 (small systems in an ensemble spread better over the SMs with
@@ -128,6 +137,29 @@ int md_gb300_pair_force_noalloc_x(md_pair_force_t_x pf, const double *x, const d
 int md_gb300_autotune_pair_x(md_pimd_t_x *pimd, md_pair_force_t_x pf, int repeats, int *warps, double *ms);
 /* set that choice directly (a tuning table kept by the caller) */
 int md_gb300_set_pair_tile_x(md_pair_force_t_x pf, int N, int P, int warps);
+
+/* Which kernel solves the exchange recursions (V_B and the backward tmpV,
+   md_pimd_fill_VB_x and the force call): MD_GB_SOLVE_BLOCK runs one thread
+   block per direction, MD_GB_SOLVE_CLUSTER one cluster of eight blocks per
+   direction (distributed shared memory), MD_GB_SOLVE_AUTO (default) picks
+   per N: a choice recorded by md_gb300_autotune_solve_x, else the cluster
+   from N = 129 on.  All paths give the same values to rounding.  Forcing
+   the cluster where none of its size fits makes the recursion calls fail
+   with MD_GB_ERR_CUDA.  md_gb300_get_solve_path_x(N) returns the path that
+   N uses (N < 1: the forced setting). */
+#define MD_GB_SOLVE_AUTO 0
+#define MD_GB_SOLVE_BLOCK 1
+#define MD_GB_SOLVE_CLUSTER 2
+int md_gb300_set_solve_path_x(int path);
+int md_gb300_get_solve_path_x(int N);
+/* Times both solve kernels on pimd's current cycle energies (scratch
+   outputs; pimd's V_B and tmpV are untouched) and records the faster one
+   for pimd's N; *path and *ms (may be NULL) receive it and its time. */
+int md_gb300_autotune_solve_x(md_pimd_t_x *pimd, int repeats, int *path, double *ms);
+/* Host copies of the backward recursion tmpV[0..N] and the connection
+   probabilities G[(l-1)*N + (j-1)] (md_pimd_x.c:2588-2673) left by the last
+   md_pimd_fast_fill_force_VB_x (either may be NULL); synchronises. */
+int md_gb300_exchange_tables_x(md_pimd_t_x *pimd, double *tmpV, double *G);
 
 #define MD_GB_PRECISION_FP64 0
 #define MD_GB_PRECISION_MIXED 1
@@ -191,6 +223,18 @@ int md_gb300_ewald_model_desc_info_x(md_gb300_ewald_model_t_x *model, double *rc
 /* tensor-core layout self-test: max errors of a 128 x 128 product for
    K-major operands and the two readings of MN-major descriptors */
 int md_gb300_tc_selftest_x(double err[5]);
+/* Bounded waits of the tensor-core kernels.  Every wait on an mbarrier
+   phase (bulk copies, MMA completion) gives up after `cycles` SM clock
+   cycles (default 2^32, about two seconds); the kernel then waits once more,
+   bounded the same way, for its own copies in flight, frees its tensor
+   memory, records an error status and returns, and the call that launched
+   it reports MD_GB_ERR_CUDA.  The self-test arms a barrier for 16 bytes that
+   nothing delivers (no copy is issued), waits with the limit `cycles` and
+   returns the recorded status in *status (4: the wait ran out) and the
+   cycles the wait took in *waited (may be NULL); the device stays usable. */
+int md_gb300_set_wait_limit_x(long long cycles);
+long long md_gb300_get_wait_limit_x(void);
+int md_gb300_wait_selftest_x(long long cycles, int *status, long long *waited);
 
 /* Text checkpoints (md_fprint_particle_pos_x / _vel_x / _force_x,
    md_fprint_nhcs_x, md_fprint_sim_box_x):

@@ -103,11 +103,16 @@ int md_pimd_fprint_ENk2_x(FILE *out, md_pimd_t_x *pimd);
 int md_pimd_calc_vi_virial_energy_x(md_pimd_t_x *pimd, md_stats_t_x *stats, int image);
 int md_pimd_fast_fill_ENk2_x(md_pimd_t_x *pimd, int image);
 
-/* accumulator arithmetic: md_pimd_x.h:163-169 */
+/* accumulator arithmetic: md_pimd_x.h:163-170, scalar (es) and
+   function-valued (fxs, the _f forms) */
 int md_reset_stats_x(md_stats_t_x *stats, md_num_t_x e);
+int md_reset_stats_f_x(md_stats_t_x *stats, md_num_t_x e);
 int md_stats_add_to_x(md_stats_t_x *stats, md_stats_t_x *stats2);
+int md_stats_add_to_f_x(md_stats_t_x *stats, md_stats_t_x *stats2);
 int md_stats_copy_to_x(md_stats_t_x *stats, md_stats_t_x *stats2);
+int md_stats_copy_to_f_x(md_stats_t_x *stats, md_stats_t_x *stats2);
 int md_stats_mult_to_x(md_stats_t_x *stats, md_stats_t_x *stats2);
+int md_stats_mult_to_f_x(md_stats_t_x *stats, md_stats_t_x *stats2);
 
 /* xi -> xi' reweighting with sign, e.g. bosons to fermions:
    md_pimd_x.h:171-172 (md_pimd_calc_vi_sign_x: the signed recursion runs on

@@ -769,4 +769,33 @@ int md_stats_mult_to_x(md_stats_t_x *s, md_stats_t_x *s2) {
   return 0;
 }
 
+// the same four on the function-valued accumulator fxs (S(k) and other
+// observables with `points` values): md_pimd_x.c:4566-4650.  add and copy
+// need equal point counts; mult scales by the scalar es[0] of the second
+int md_reset_stats_f_x(md_stats_t_x *s, md_num_t_x e) {
+  if (!(s = md_stats_sync_host_x(s))) return -1;
+  for (int i = 0; i < s->points; ++i) s->fxs[0][i] = e;
+  return 0;
+}
+
+int md_stats_add_to_f_x(md_stats_t_x *s, md_stats_t_x *s2) {
+  if (!s || !s2 || s->points != s2->points) return -1;
+  if (!(s = md_stats_sync_host_x(s)) || !(s2 = md_stats_sync_host_x(s2))) return -1;
+  for (int i = 0; i < s->points; ++i) s->fxs[s->N - 1][i] += s2->fxs[0][i];
+  return 0;
+}
+
+int md_stats_copy_to_f_x(md_stats_t_x *s, md_stats_t_x *s2) {
+  if (!s || !s2 || s->points != s2->points) return -1;
+  if (!(s = md_stats_sync_host_x(s)) || !(s2 = md_stats_sync_host_x(s2))) return -1;
+  for (int i = 0; i < s->points; ++i) s->fxs[0][i] = s2->fxs[0][i];
+  return 0;
+}
+
+int md_stats_mult_to_f_x(md_stats_t_x *s, md_stats_t_x *s2) {
+  if (!(s = md_stats_sync_host_x(s)) || !(s2 = md_stats_sync_host_x(s2))) return -1;
+  for (int i = 0; i < s->points; ++i) s->fxs[0][i] *= s2->es[0];
+  return 0;
+}
+
 }  // extern "C"

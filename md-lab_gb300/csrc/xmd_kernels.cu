@@ -1061,6 +1061,8 @@ struct TriJob {
   double *sign;  // optional: sign of X_i (signed weights), forward direction only
   double *Bm[2];  // inverses of the 32 x 32 diagonal blocks (unsigned weights):
   int *Be[2];     // [chunk][32][32] mantissas and exponents
+  double *Xm[2];  // optional: the unknowns X_0..X_N in extended range (unsigned
+  int *Xe[2];     // solves), kept for the connection probabilities
 };
 
 // Extended-range dot product of row i of the weights with the unknowns over
@@ -1341,9 +1343,12 @@ __global__ void __launch_bounds__(TS_WARPS * 32) k_tri_solve(int N, double beta,
 }
 
 // scratch: mantissas (ntri(N) doubles) then exponents (ntri(N) ints)
+// one direction's scratch: weights (mantissas, then exponents as ints), the
+// diagonal blocks' inverses (mantissas, exponents), the unknowns X_0..X_N
+// (mantissas, exponents)
 size_t rec_scratch_doubles(int N) {
   const size_t nch = (N + TS_CHUNK - 1) / TS_CHUNK;
-  return ntri(N) + (ntri(N) + 1) / 2 + 1 + nch * TS_CHUNK * TS_CHUNK * 3 / 2;
+  return ntri(N) + (ntri(N) + 1) / 2 + 1 + nch * TS_CHUNK * TS_CHUNK * 3 / 2 + (size_t)(N + 1) + (N + 2) / 2;
 }
 
 // directions first .. first + count - 1 of job
@@ -1578,6 +1583,11 @@ __global__ void __launch_bounds__(TSB_WARPS * 32) k_tri_solve_b(int N, double be
     out[backward ? N - i : i] = -lnx / beta;
   }
   if (threadIdx.x == 0) out[backward ? N : 0] = 0.0;
+  if (job.Xm[backward])
+    for (int i = threadIdx.x; i <= N; i += blockDim.x) {
+      job.Xm[backward][i] = Xm[i];
+      job.Xe[backward][i] = Xe[i];
+    }
 }
 
 // The block solve spread over a thread-block cluster: one cluster of TSC_CL
@@ -1792,6 +1802,11 @@ __global__ void __cluster_dims__(TSC_CL, 1, 1) __launch_bounds__(TSC_WARPS * 32)
       out[backward ? N - i : i] = -lnx / beta;
     }
     if (threadIdx.x == 0) out[backward ? N : 0] = 0.0;
+    if (job.Xm[backward])
+      for (int i = threadIdx.x; i <= N; i += blockDim.x) {
+        job.Xm[backward][i] = Xm[i];
+        job.Xe[backward][i] = Xe[i];
+      }
   }
 }
 
@@ -1817,16 +1832,48 @@ static bool cluster_solve_fits(size_t smem) {
   return fits;
 }
 
+// Which kernel solves the unsigned recursions: SOLVE_AUTO picks by size
+// (a choice recorded for this N by set_solve_choice, else the cluster from
+// five chunks on), SOLVE_BLOCK forces k_tri_solve_b, SOLVE_CLUSTER forces
+// k_tri_solve_c.  Both give the same unknowns to rounding.
+static std::atomic<int> g_solve_force{SOLVE_AUTO};
+static std::mutex g_solve_mu;
+static std::vector<std::pair<int, int>> g_solve_choice;  // (N, path)
+
+void set_solve_path(int path) { g_solve_force = path; }
+int solve_path() { return g_solve_force; }
+void set_solve_choice(int N, int path) {
+  std::lock_guard<std::mutex> lk(g_solve_mu);
+  for (auto &c : g_solve_choice)
+    if (c.first == N) {
+      c.second = path;
+      return;
+    }
+  g_solve_choice.emplace_back(N, path);
+}
+int solve_choice(int N) {
+  const int forced = g_solve_force;
+  if (forced != SOLVE_AUTO) return forced;
+  {
+    std::lock_guard<std::mutex> lk(g_solve_mu);
+    for (const auto &c : g_solve_choice)
+      if (c.first == N) return c.second;
+  }
+  // the cluster pays off from five chunks on; below that (and in ensembles
+  // of small systems) one block per direction leaves the SMs to the other
+  // systems
+  return (N + TS_CHUNK - 1) / TS_CHUNK > 4 ? SOLVE_CLUSTER : SOLVE_BLOCK;
+}
+
 static cudaError_t tri_solve(int N, double beta, const TriJob &job, int first, int count, cudaStream_t st) {
   if (!job.sign) {
     // unsigned weights: the block solve (the diagonal-block inverses came
     // with the weights, k_weights_inv)
-    const int nch = (N + TS_CHUNK - 1) / TS_CHUNK;
     const size_t smem_c = (sizeof(double) + sizeof(int)) * (N + 1 + 3 * TS_CHUNK + 4 * TS_CHUNK * TS_LD) + 16;
-    // the cluster pays off from five chunks on; below that (and in
-    // ensembles of small systems) one block per direction leaves the SMs to
-    // the other systems
-    if (nch > 4 && cluster_solve_fits(smem_c)) {
+    const int path = solve_choice(N);
+    if (path == SOLVE_CLUSTER && !cluster_solve_fits(smem_c) && g_solve_force == SOLVE_CLUSTER)
+      return cudaErrorInvalidConfiguration;  // forced, but no cluster of this size fits
+    if (path == SOLVE_CLUSTER && cluster_solve_fits(smem_c)) {
       {
         XK_PROF(count == 2 ? "vb_tv_solve" : (first ? "tv_solve" : "vb_solve"));
         k_tri_solve_c<<<dim3(TSC_CL, count), TSC_WARPS * 32, smem_c, st>>>(N, beta, job, first);
@@ -1868,6 +1915,8 @@ static TriJob tri_job(int N, double *rs_f, double *rs_b, double *VBN, double *tm
   for (int d = 0; d < 2; ++d) {
     j.Bm[d] = rs[d] ? rs[d] + boff : nullptr;
     j.Be[d] = rs[d] ? (int *)(rs[d] + boff + nb) : nullptr;
+    j.Xm[d] = rs[d] ? rs[d] + boff + nb + nb / 2 : nullptr;
+    j.Xe[d] = rs[d] ? (int *)(rs[d] + boff + nb + nb / 2 + N + 1) : nullptr;
   }
   j.Mm[0] = rs_f;
   j.Me[0] = (const int *)(rs_f + ntri(N));
@@ -1928,24 +1977,29 @@ cudaError_t fill_vb_signed(int N, double beta, double vi2, const double *ENk, co
 // connection probabilities G[l][j]: md_pimd_x.c:2660-2673
 // G[l][j] (md_pimd_x.c:2588-2620); ln xi comes from the host and 1/l from
 // a host table, so an element costs one exponential (exp_fast) on the FP64
-// pipe
+// pipe.  The exponent is a difference of numbers of size beta V_B^(N) (up to
+// ~1e5 at N = 512), so its rounding sets G's relative accuracy; it is summed
+// in the reference's order, ((V_B^(j-1) + E) + tmpV[l]) - V_B^(N), so that the
+// two round alike.
 __global__ void k_fill_g(int N, double beta, double vi, double lnvi, const double *__restrict__ ENk,
                          const double *__restrict__ VBN, const double *__restrict__ tmpV,
                          const double *__restrict__ invl, double *__restrict__ G) {
   const int l = blockIdx.y + 1;  // 1-based row
-  const double base = tmpV[l] - VBN[N];
+  const double tv = tmpV[l], vn = VBN[N];
   for (int j = blockIdx.x * blockDim.x + threadIdx.x + 1; j <= N; j += gridDim.x * blockDim.x) {
     double gv;
     if (j > l + 1)
       gv = 0;
     else if (j == l + 1)
-      gv = 1 - exp(-beta * (VBN[l] + base));
+      gv = 1 - exp(-beta * ((VBN[l] + tv) - vn));
     else if (vi == 0.0 && l - j != 0)
       gv = 0;
     else if (vi == 0.0)
-      gv = exp_fast(-beta * (VBN[j - 1] + ENk[dtri(l) + l - j] + base)) * invl[l];
+      gv = exp_fast(-beta * (((VBN[j - 1] + ENk[dtri(l) + l - j]) + tv) - vn)) * invl[l];
     else
-      gv = exp_fast(-beta * (VBN[j - 1] + ENk[dtri(l) + l - j] + base) + (l - j) * lnvi) * invl[l];
+      gv = exp_fast(__dadd_rn(__dmul_rn(-beta, ((VBN[j - 1] + ENk[dtri(l) + l - j]) + tv) - vn),
+                              __dmul_rn((double)(l - j), lnvi))) *
+           invl[l];
     G[(size_t)(l - 1) * N + (j - 1)] = gv;
   }
 }
@@ -1957,6 +2011,49 @@ cudaError_t fill_g(int N, double beta, double vi, const double *ENk, const doubl
   {
     XK_PROF("fill_g");
     k_fill_g<<<grid, 256, 0, st>>>(N, beta, vi, lnvi, ENk, VBN, tmpV, lnn + N + 1, G);
+  }
+  return XK_LAUNCHED();
+}
+
+// The same G from the extended-range numbers the recursions already hold.
+// With Z_n = exp(-beta V_B^(n)) = X_n of the forward solve, exp(-beta tmpV[l])
+// = X'_{N-l} of the backward one, and the weight M_{l,j-1} = xi^(l-j)/l
+// exp(-beta E_l^(l-j+1)) of the forward triangle,
+//   G[l][j] = M_{l,j-1} X_{j-1} X'_{N-l} / X_N        (j <= l)
+//   G[l][l+1] = 1 - X_l X'_{N-l} / X_N
+// a product of four numbers each held to a few ulps, where the reference's
+// exp(-beta(V_B^(j-1) + E + tmpV[l] - V_B^(N))) loses beta V_B^(N) ulps to the
+// cancellation inside the exponent (up to ~1e-10 relative at N = 512).
+__device__ inline double ext_val(double m, int e) { return m == 0.0 ? 0.0 : ldexp(m, e); }
+
+__global__ void k_fill_g_ext(int N, const double *__restrict__ Mm, const int *__restrict__ Me,
+                             const double *__restrict__ Xfm, const int *__restrict__ Xfe,
+                             const double *__restrict__ Xbm, const int *__restrict__ Xbe, double *__restrict__ G) {
+  const int l = blockIdx.y + 1;  // 1-based row
+  // X'_{N-l} / X_N, as a mantissa and an exponent
+  const double q = Xbm[N - l] / Xfm[N];
+  const int qe = Xbe[N - l] - Xfe[N];
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x + 1; j <= N; j += gridDim.x * blockDim.x) {
+    double gv;
+    if (j > l + 1) {
+      gv = 0;
+    } else if (j == l + 1) {
+      gv = 1 - ext_val(Xfm[l] * q, Xfe[l] + qe);
+    } else {
+      const size_t o = moff(l, j - 1);
+      const double w = Mm[o];
+      gv = w == 0.0 ? 0.0 : ext_val(w * Xfm[j - 1] * q, Me[o] + Xfe[j - 1] + qe);
+    }
+    G[(size_t)(l - 1) * N + (j - 1)] = gv;
+  }
+}
+
+cudaError_t fill_g_ext(int N, const double *rs_f, const double *rs_b, double *G, cudaStream_t st) {
+  const TriJob j = tri_job(N, (double *)rs_f, (double *)rs_b, nullptr, nullptr);
+  dim3 grid((N + 255) / 256, N);
+  {
+    XK_PROF("fill_g");
+    k_fill_g_ext<<<grid, 256, 0, st>>>(N, j.Mm[0], j.Me[0], j.Xm[0], j.Xe[0], j.Xm[1], j.Xe[1], G);
   }
   return XK_LAUNCHED();
 }
@@ -3819,12 +3916,16 @@ cudaError_t pair_force_noalloc(const Geo &g, const PairPrm &p, const double *x, 
 namespace xk {
 
 // ===================================================================
-// Mixed-precision form: pair and real-space Ewald forces in FP32 with
-// compensated (Kahan) accumulation of every force sum; reciprocal space
-// with FP32 phase products accumulated in double-float (an unevaluated sum
-// of two FP32 numbers, ~48 significant bits).  Positions, the phases
-// themselves and every estimator stay FP64; partial sums leave the FP32
-// kernels as doubles.
+// Mixed-precision form: pair and real-space Ewald forces in FP32, each
+// lane's sum over one 32 x 32 tile (at most 32 terms) in plain FP32 and the
+// tile partials added in FP64 (k_pair_finish32); reciprocal space with FP32
+// phase products accumulated in double-float structure factors (an
+// unevaluated sum of two FP32 numbers, ~48 significant bits) and each
+// particle's sum over the wave-vector columns compensated (Kahan).
+// Positions and every estimator stay FP64; partial sums leave the FP32
+// kernels as doubles.  Against the FP64 form the largest force error is
+// ~2e-5 of the largest force at 512 electrons, 64 beads, set by the FP32
+// rounding of the pair separations rather than by the sums.
 // ===================================================================
 
 struct Kahan {

@@ -121,11 +121,24 @@ cudaError_t fill_vb_tv(int N, double beta, double vi, const double *ENk, const d
                        double *tmpV, double *rs_f, double *rs_b, cudaStream_t st);
 // V_B for a signed xi' (md_pimd_calc_vi_sign_x): V2[n] = -ln|Z'_n|/beta and
 // sign[n] = sign of Z'_n, n = 0..N
+// which kernel solves the unsigned recursions (both give the same unknowns
+// to rounding): SOLVE_AUTO chooses by N (a recorded choice, else the cluster
+// from five 32-row chunks on); the others force one for every N
+enum SolvePath { SOLVE_AUTO = 0, SOLVE_BLOCK = 1, SOLVE_CLUSTER = 2 };
+void set_solve_path(int path);
+int solve_path();
+// record the path for one N (the solve autotuner) and read the path used for N
+void set_solve_choice(int N, int path);
+int solve_choice(int N);
 cudaError_t fill_vb_signed(int N, double beta, double vi2, const double *ENk, const double *lnn, double *V2,
                            double *sign, double *rs, cudaStream_t st);
 // lnn: the host table of ln l then 1/l (2 (N+1) doubles)
 cudaError_t fill_g(int N, double beta, double vi, const double *ENk, const double *VBN,
                    const double *tmpV, const double *lnn, double *G, cudaStream_t st);
+// G from the extended-range weights and unknowns that fill_vb_tv left in
+// its scratch (rs_f, rs_b): valid only while that call's ENk, beta and xi
+// are current; a few ulps where fill_g loses up to beta V_B^(N) ulps
+cudaError_t fill_g_ext(int N, const double *rs_f, const double *rs_b, double *G, cudaStream_t st);
 // scratch: at least exch_scratch_doubles(g) doubles
 size_t exch_scratch_doubles(const Geo &g);
 cudaError_t exch_force(const Geo &g, const double *x, const double *m, double w2, int image,

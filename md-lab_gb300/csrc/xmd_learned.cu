@@ -11,6 +11,7 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -122,12 +123,13 @@ __device__ __forceinline__ uint32_t mbar_try(uint32_t bar, uint32_t parity) {
       : "memory");
   return ok;
 }
-// bounded wait for the phase with the given parity: false after about two
-// seconds of SM clock
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+// bounded wait for the phase with the given parity: false once `limit` SM
+// clock cycles have passed (the library's default, 2^32, is about two
+// seconds)
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, long long limit) {
   const long long t0 = clock64();
   while (!mbar_try(bar, parity))
-    if (clock64() - t0 > (1ll << 32)) return false;
+    if (clock64() - t0 > limit) return false;
   return true;
 }
 // 1-D bulk copy global -> shared, completion counted on the mbarrier
@@ -176,6 +178,37 @@ __device__ __forceinline__ void tc_fail(int *err, int code) {
   if (threadIdx.x == 0) atomicCAS(err ? err : &g_tc_status, 0, code);
 }
 
+// Every thread of the block waits (bounded) for bar's phase `parity`.  On a
+// time-out the block waits once more, again bounded, so that its own bulk
+// copies or MMAs still in flight towards that barrier can land before the
+// caller records the error, frees its tensor memory and returns.
+__device__ __forceinline__ bool block_wait(uint32_t bar, uint32_t parity, long long limit) {
+  if (__syncthreads_and(tc::mbar_wait(bar, parity, limit))) return true;
+  tc::mbar_wait(bar, parity, limit);
+  __syncthreads();
+  return false;
+}
+
+// Wait-limit self-test: one block arms a barrier for 16 bytes that no copy
+// will deliver (no copy is issued, nothing is in flight) and waits for it
+// with the block_wait the tensor-core kernels use; the wait runs out after
+// `limit` cycles and the block records status 4.  out[0] receives the
+// cycles the block spent waiting.
+__global__ void k_wait_probe(long long limit, int *err, long long *out) {
+  __shared__ __align__(8) uint64_t bar;
+  const uint32_t b = tc::saddr(&bar);
+  if (threadIdx.x == 0) {
+    tc::mbar_init(b, 1);
+    tc::mbar_fence_init();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) tc::mbar_expect_tx(b, 16);  // the one arrival; 16 bytes stay pending
+  const long long t0 = clock64();
+  const bool ok = block_wait(b, 0, limit);
+  if (!ok) tc_fail(err, 4);
+  if (threadIdx.x == 0) out[0] = clock64() - t0;
+}
+
 // host RNE rounding to BF16 (the device uses __float2bfloat16_rn)
 static inline uint16_t host_bf16(float f) {
   uint32_t u;
@@ -203,7 +236,7 @@ constexpr int ST_CASES = 5;
 constexpr uint32_t ST_SMEM = 131072 + 64;
 
 __global__ void __launch_bounds__(128, 1) k_tc_selftest(const uint8_t *__restrict__ imgs, float *__restrict__ out,
-                                                      int *err) {
+                                                      int *err, long long wait) {
   extern __shared__ __align__(1024) uint8_t sm[];
   uint64_t *bar = (uint64_t *)(sm + 131072);
   uint32_t *slot = (uint32_t *)(sm + 131080);
@@ -247,7 +280,7 @@ __global__ void __launch_bounds__(128, 1) k_tc_selftest(const uint8_t *__restric
       }
       tc::commit(b);
     }
-    const bool ok = __syncthreads_and(tc::mbar_wait(b, ph));
+    const bool ok = block_wait(b, ph, wait);
     ph ^= 1;
     if (!ok) {
       tc_fail(err, 2);
@@ -304,7 +337,7 @@ cudaError_t tc_selftest(double err[5], cudaStream_t st) {
   if (e == cudaSuccess) e = cudaMemsetAsync(derr, 0, sizeof(int), st);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_tc_selftest, cudaFuncAttributeMaxDynamicSharedMemorySize, ST_SMEM);
   if (e == cudaSuccess) {
-    k_tc_selftest<<<1, 128, ST_SMEM, st>>>(dimg, dout, derr);
+    k_tc_selftest<<<1, 128, ST_SMEM, st>>>(dimg, dout, derr, wait_limit());
     e = XK_LAUNCHED();
   }
   std::vector<float> out((size_t)ST_CASES * 128 * 128);
@@ -381,7 +414,7 @@ __device__ __forceinline__ void issue_layer(uint32_t s0, int layer, uint32_t tm)
 }
 
 __global__ void __launch_bounds__(128, 1) k_mlp_fwd(MlpDev w, const uint8_t *__restrict__ ximg, int ntiles,
-                                                  float4 *__restrict__ Y, int *err) {
+                                                  float4 *__restrict__ Y, int *err, long long wait) {
   extern __shared__ __align__(1024) uint8_t sm[];
   float *sb1 = (float *)(sm + fw::B), *sb2 = sb1 + 128, *sb3 = sb2 + 128;
   uint64_t *bars = (uint64_t *)(sm + fw::BAR);
@@ -410,14 +443,14 @@ __global__ void __launch_bounds__(128, 1) k_mlp_fwd(MlpDev w, const uint8_t *__r
     tc::bulk_g2s(s0 + fw::W2, w.w2img, 32768, bar_w);
     tc::bulk_g2s(s0 + fw::W3, w.w3img, 4096, bar_w);
   }
-  bool ok = __syncthreads_and(tc::mbar_wait(bar_w, 0));
+  bool ok = block_wait(bar_w, 0, wait);
   uint32_t px = 0, pm = 0;
   for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
     if (tid == 0) {
       tc::mbar_expect_tx(bar_x, (uint32_t)MLP_TILE_BYTES);
       tc::bulk_g2s(s0 + fw::X, ximg + (size_t)tile * MLP_TILE_BYTES, (uint32_t)MLP_TILE_BYTES, bar_x);
     }
-    ok = __syncthreads_and(tc::mbar_wait(bar_x, px));
+    ok = block_wait(bar_x, px, wait);
     px ^= 1;
     for (int layer = 1; layer <= 3 && ok; ++layer) {
       if (tid == 0) {
@@ -425,7 +458,7 @@ __global__ void __launch_bounds__(128, 1) k_mlp_fwd(MlpDev w, const uint8_t *__r
         issue_layer(s0, layer, tm);
         tc::commit(bar_m);
       }
-      ok = __syncthreads_and(tc::mbar_wait(bar_m, pm));
+      ok = block_wait(bar_m, pm, wait);
       pm ^= 1;
       if (!ok) break;
       tc::fence_after();
@@ -491,7 +524,8 @@ template <int MNV>
 __global__ void __launch_bounds__(128, 1) k_mlp_train(MlpDev w, const uint8_t *__restrict__ ximg,
                                                     const float *__restrict__ V, const float4 *__restrict__ T,
                                                     int ntiles_data, int batch_tiles, uint32_t seed, MlpLoss loss,
-                                                    float *__restrict__ grad, float *__restrict__ lossacc, int *err) {
+                                                    float *__restrict__ grad, float *__restrict__ lossacc, int *err,
+                                                    long long wait) {
   extern __shared__ __align__(1024) uint8_t sm[];
   float *w3f = (float *)(sm + tr::W3F), *sb1 = (float *)(sm + tr::B1), *sb2 = (float *)(sm + tr::B2),
         *sb3 = (float *)(sm + tr::B3);
@@ -526,11 +560,11 @@ __global__ void __launch_bounds__(128, 1) k_mlp_train(MlpDev w, const uint8_t *_
     tc::bulk_g2s(s0 + tr::W2, w.w2img, 32768, bar_w);
     tc::bulk_g2s(s0 + tr::W3, w.w3img, 4096, bar_w);
   }
-  bool ok = __syncthreads_and(tc::mbar_wait(bar_w, 0));
+  bool ok = block_wait(bar_w, 0, wait);
   uint32_t px = 0, pm = 0;
   int done = 0;
   auto mma_wait = [&]() {
-    ok = __syncthreads_and(tc::mbar_wait(bar_m, pm));
+    ok = block_wait(bar_m, pm, wait);
     pm ^= 1;
     tc::fence_after();
   };
@@ -551,7 +585,7 @@ __global__ void __launch_bounds__(128, 1) k_mlp_train(MlpDev w, const uint8_t *_
 #pragma unroll
     for (int i = 0; i < 9; ++i) v[i] = V[grow * DESC_VSTRIDE + i];
     const float wr = V[grow * DESC_VSTRIDE + 9];
-    ok = __syncthreads_and(tc::mbar_wait(bar_x, px));
+    ok = block_wait(bar_x, px, wait);
     px ^= 1;
     if (!ok) break;
     // ---- forward ----
@@ -828,7 +862,7 @@ cudaError_t mlp_forward(const MlpDev &w, const uint8_t *ximg, int ntiles, float4
   const int grid = ntiles < sm_count() ? ntiles : sm_count();
   {
     XK_PROF("mlp_forward");
-    k_mlp_fwd<<<grid, 128, fw::SMEM, st>>>(w, ximg, ntiles, Y, err);
+    k_mlp_fwd<<<grid, 128, fw::SMEM, st>>>(w, ximg, ntiles, Y, err, wait_limit());
   }
   return XK_LAUNCHED();
 }
@@ -848,7 +882,8 @@ cudaError_t mlp_train_grad(const MlpDev &w, const uint8_t *ximg, const float *V,
   const int grid = batch_tiles < sm_count() ? batch_tiles : sm_count();
   {
     XK_PROF("mlp_train");
-    kf<<<grid, 128, tr::SMEM, st>>>(w, ximg, V, T, ntiles_data, batch_tiles, seed, loss, grad, lossacc, err);
+    kf<<<grid, 128, tr::SMEM, st>>>(w, ximg, V, T, ntiles_data, batch_tiles, seed, loss, grad, lossacc, err,
+                                    wait_limit());
   }
   return XK_LAUNCHED();
 }
@@ -1125,6 +1160,29 @@ __global__ void k_sum_particles(Geo g, const double *__restrict__ e, double w, d
 cudaError_t sum_particles(const Geo &g, const double *e, double w, double *acc, cudaStream_t st) {
   k_sum_particles<<<1, 256, 0, st>>>(g, e, w, acc);
   return XK_LAUNCHED();
+}
+
+static std::atomic<long long> g_wait_limit{1ll << 32};
+long long wait_limit() { return g_wait_limit; }
+void set_wait_limit(long long cycles) { g_wait_limit = cycles; }
+
+cudaError_t wait_probe(long long limit, int *status, long long *cycles, cudaStream_t st) {
+  int *derr = nullptr;
+  long long *dcyc = nullptr;
+  cudaError_t e = cudaMalloc(&derr, sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc(&dcyc, sizeof(long long));
+  if (e == cudaSuccess) e = cudaMemsetAsync(derr, 0, sizeof(int), st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(dcyc, 0, sizeof(long long), st);
+  if (e == cudaSuccess) {
+    k_wait_probe<<<1, 64, 0, st>>>(limit, derr, dcyc);
+    e = XK_LAUNCHED();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(status, derr, sizeof(int), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(cycles, dcyc, sizeof(long long), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (derr) cudaFree(derr);
+  if (dcyc) cudaFree(dcyc);
+  return e;
 }
 
 // status word of the tensor-core kernels that were given no error pointer

@@ -114,6 +114,14 @@ cudaError_t resid_judge(const Geo &g, const double *fp, const double *fa, const 
 cudaError_t sum_particles(const Geo &g, const double *e, double w, double *acc, cudaStream_t st);
 // status word of tensor-core kernels launched with err == nullptr
 cudaError_t tc_status(int *out, bool clear);
+// cycles a tensor-core kernel waits on one mbarrier phase before it gives up
+// and records an error (default 2^32, about two seconds at 2 GHz)
+long long wait_limit();
+void set_wait_limit(long long cycles);
+// the wait-limit self-test kernel: a barrier whose 16 bytes never arrive,
+// waited for with `limit`; *status = the recorded status (4 on a time-out),
+// *cycles = the cycles the wait took
+cudaError_t wait_probe(long long limit, int *status, long long *cycles, cudaStream_t st);
 
 // tensor-core layout self-test: D = A B^T on one CTA for K-major operands
 // and for MN-major A / B under both readings of the descriptor offsets.

@@ -337,6 +337,24 @@ int md_gb300_tc_selftest_x(double err[5]) {
   return 0;
 }
 
+int md_gb300_set_wait_limit_x(long long cycles) {
+  if (cycles < 1) return fail(MD_GB_ERR_ARG, "wait limit must be positive");
+  xk::set_wait_limit(cycles);
+  return 0;
+}
+
+long long md_gb300_get_wait_limit_x(void) { return xk::wait_limit(); }
+
+int md_gb300_wait_selftest_x(long long cycles, int *status, long long *waited) {
+  XMD_TRY(ensure_device());
+  if (!status || cycles < 1) return fail(MD_GB_ERR_ARG, "wait self-test: NULL status or non-positive limit");
+  if (capturing()) return fail(MD_GB_ERR_CAPTURE, "self-test while capturing");
+  long long w = 0;
+  XMD_CUDA(xk::wait_probe(cycles, status, &w, stream()));
+  if (waited) *waited = w;
+  return 0;
+}
+
 void md_gb300_ewald_model_free_x(md_gb300_ewald_model_t_x *M) {
   if (!M) return;
   for (auto it = g_attached.begin(); it != g_attached.end();)

@@ -328,11 +328,17 @@ int md_pimd_fast_fill_force_VB_x(md_pimd_t_x *pimd, int image) {
   cudaStream_t st;
   XMD_TRY(side_begin(&st));
   const int N = pimd->N;
-  if (!(pd->tmpv_fresh && pd->tmpv_beta == pimd->beta && pd->tmpv_vi == pimd->vi))
+  if (pd->tmpv_fresh && pd->tmpv_beta == pimd->beta && pd->tmpv_vi == pimd->vi) {
+    // both recursions of the current ENk are in pd->rec: G from their
+    // extended-range numbers
+    double *rs = pd->rec.as<double>();
+    XMD_CUDA(xk::fill_g_ext(N, rs, rs + xk::rec_scratch_doubles(N), pd->G.as<double>(), st));
+  } else {
     XMD_CUDA(xk::back_vb(N, pimd->beta, pimd->vi, pd->ENk.as<double>(), pd->lnn.as<double>(),
                          pd->tmpV.as<double>(), pd->rec.as<double>(), st));
-  XMD_CUDA(xk::fill_g(N, pimd->beta, pimd->vi, pd->ENk.as<double>(), pd->VBN.as<double>(), pd->tmpV.as<double>(),
-                      pd->lnn.as<double>(), pd->G.as<double>(), st));
+    XMD_CUDA(xk::fill_g(N, pimd->beta, pimd->vi, pd->ENk.as<double>(), pd->VBN.as<double>(),
+                        pd->tmpV.as<double>(), pd->lnn.as<double>(), pd->G.as<double>(), st));
+  }
   XMD_CUDA(cudaMemsetAsync(sd->fex.p, 0, sd->geo.slots() * sizeof(double), st));
   XMD_CUDA(xk::exch_force(sd->geo, sd->x.as<double>(), sd->m.as<double>(), pimd->omegaP * pimd->omegaP, image,
                           pd->G.as<double>(), sd->fex.as<double>(), scr, st));
@@ -630,6 +636,88 @@ int md_gb300_set_precision_x(int mode) {
 
 int md_gb300_get_precision_x(void) { return g_precision; }
 
+int md_gb300_set_solve_path_x(int path) {
+  if (path != MD_GB_SOLVE_AUTO && path != MD_GB_SOLVE_BLOCK && path != MD_GB_SOLVE_CLUSTER)
+    return fail(MD_GB_ERR_ARG, "unknown recursion solve path %d", path);
+  xk::set_solve_path(path);
+  return 0;
+}
+
+int md_gb300_get_solve_path_x(int N) { return N < 1 ? xk::solve_path() : xk::solve_choice(N); }
+
+// Solve autotuner (md_gb300_x.h): both recursions of pimd's current ENk,
+// timed with each solve kernel into scratch outputs; pimd's own V_B, tmpV
+// and weights are not touched.
+int md_gb300_autotune_solve_x(md_pimd_t_x *pimd, int repeats, int *path, double *ms) {
+  if (repeats < 1) return fail(MD_GB_ERR_ARG, "repeats must be positive");
+  if (capturing()) return fail(MD_GB_ERR_CAPTURE, "autotuning times kernels; not while capturing");
+  SimDev *sd;
+  PimdDev *pd;
+  XMD_TRY(pimd_device(pimd, &sd, &pd));
+  XMD_TRY(check_plain(pimd));
+  const int N = pimd->N;
+  const size_t nrs = xk::rec_scratch_doubles(N);
+  DevBuf tmp;
+  XMD_TRY(reserve(tmp, (2 * nrs + 2 * (size_t)(N + 1)) * sizeof(double)));
+  double *rs = tmp.as<double>(), *vb = rs + 2 * nrs, *tv = vb + N + 1;
+  cudaStream_t st = stream();
+  cudaEvent_t a = nullptr, b = nullptr;
+  cudaError_t e = cudaMemsetAsync(tmp.p, 0, tmp.bytes, st);
+  if (e == cudaSuccess) e = cudaEventCreate(&a);
+  if (e == cudaSuccess) e = cudaEventCreate(&b);
+  const int saved = xk::solve_path();
+  const int cand[2] = {MD_GB_SOLVE_BLOCK, MD_GB_SOLVE_CLUSTER};
+  int best_p = xk::solve_choice(N);
+  double best = INFINITY;
+  for (int ci = 0; ci < 2 && e == cudaSuccess; ++ci) {
+    xk::set_solve_path(cand[ci]);
+    e = xk::fill_vb_tv(N, pimd->beta, pimd->vi, pd->ENk.as<double>(), pd->lnn.as<double>(), vb, tv, rs, rs + nrs,
+                       st);
+    if (e == cudaErrorInvalidConfiguration) {  // no cluster of this size fits: not a candidate
+      cudaGetLastError();
+      e = cudaSuccess;
+      continue;
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(a, st);
+    for (int r = 0; r < repeats && e == cudaSuccess; ++r)
+      e = xk::fill_vb_tv(N, pimd->beta, pimd->vi, pd->ENk.as<double>(), pd->lnn.as<double>(), vb, tv, rs, rs + nrs,
+                         st);
+    if (e == cudaSuccess) e = cudaEventRecord(b, st);
+    if (e == cudaSuccess) e = cudaEventSynchronize(b);
+    float t = 0;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&t, a, b);
+    if (e == cudaSuccess && t / repeats < best) {
+      best = t / repeats;
+      best_p = cand[ci];
+    }
+  }
+  xk::set_solve_path(saved);
+  if (a) cudaEventDestroy(a);
+  if (b) cudaEventDestroy(b);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  release(tmp);
+  if (e != cudaSuccess) return cuda_fail(e, "recursion-solve autotuning");
+  xk::set_solve_choice(N, best_p);
+  if (path) *path = best_p;
+  if (ms) *ms = best;
+  return 0;
+}
+
+// tmpV (backward recursion, N+1) and G (connection probabilities, N x N,
+// G[(l-1)*N + (j-1)]) of the last exchange force call, copied to the host
+int md_gb300_exchange_tables_x(md_pimd_t_x *pimd, double *tmpV, double *G) {
+  if (capturing()) return fail(MD_GB_ERR_CAPTURE, "host copy while capturing a graph");
+  SimDev *sd;
+  PimdDev *pd;
+  XMD_TRY(pimd_device(pimd, &sd, &pd));
+  const int N = pimd->N;
+  cudaStream_t st = stream();
+  if (tmpV) XMD_CUDA(cudaMemcpyAsync(tmpV, pd->tmpV.p, (size_t)(N + 1) * 8, cudaMemcpyDeviceToHost, st));
+  if (G) XMD_CUDA(cudaMemcpyAsync(G, pd->G.p, (size_t)N * N * 8, cudaMemcpyDeviceToHost, st));
+  XMD_CUDA(cudaStreamSynchronize(st));
+  return 0;
+}
+
 // Pair forces for callers that cannot allocate device memory (md_gb300_x.h).
 // Everything here works on the caller's device pointers and stream; the
 // per-tile partial sums go to a fixed array inside the library.  This
@@ -663,6 +751,11 @@ int md_gb300_pair_force_noalloc_x(md_pair_force_t_x pf, const double *x, const d
                 "no-allocation pair forces: N=%d, P=%d, ld=%d needs %zu doubles of scratch, more than the fixed %zu "
                 "(ceil(N/32) * P * D * ld must not exceed it)",
                 N, P, ld, need, (size_t)xk::NOALLOC_SCRATCH_DOUBLES);
+  // a launch error left by the caller's earlier work is theirs: report it
+  // as such before this call launches anything (its own launch status is
+  // read with cudaGetLastError, which would otherwise return that error)
+  const cudaError_t pending = cudaGetLastError();
+  if (pending != cudaSuccess) return cuda_fail(pending, "error pending from earlier work, before the no-allocation call");
   XMD_CUDA(xk::pair_force_noalloc(g, pair_params(kind), x, m, f, (cudaStream_t)stream));
   return 0;
 }
@@ -910,11 +1003,17 @@ int md_pimd_calc_vi_sign_x(md_pimd_t_x *pimd, md_stats_t_x *e_s, md_stats_t_x *s
   XMD_TRY(pimd_device(pimd, &sd, &pd));
   XMD_TRY(check_plain(pimd));
   const int N = pimd->N;
-  XMD_TRY(reserve(pd->vsign, sizeof(double) * 2 * (N + 1)));
+  // its own weight scratch behind V2 and the signs: the recursions' scratch
+  // (pd->rec) holds the weights and unknowns the next force call reads
+  const size_t need = sizeof(double) * (2 * (size_t)(N + 1) + xk::rec_scratch_doubles(N));
   cudaStream_t st = stream();
+  if (pd->vsign.bytes < need) {
+    XMD_TRY(reserve(pd->vsign, need));
+    XMD_CUDA(cudaMemsetAsync(pd->vsign.p, 0, need, st));
+  }
   double *V2 = pd->vsign.as<double>(), *sg = V2 + (N + 1);
   XMD_CUDA(xk::fill_vb_signed(N, pimd->beta, vi2, pd->ENk.as<double>(), pd->lnn.as<double>(), V2, sg,
-                              pd->rec.as<double>(), st));
+                              V2 + 2 * (N + 1), st));
   double r[3];
   XMD_CUDA(cudaMemcpyAsync(&r[0], V2 + N, 8, cudaMemcpyDeviceToHost, st));
   XMD_CUDA(cudaMemcpyAsync(&r[1], sg + N, 8, cudaMemcpyDeviceToHost, st));

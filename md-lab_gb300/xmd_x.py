@@ -161,8 +161,15 @@ class XLib:
                 "md_gb300_get_precision_x": (_i, []),
                 "md_gb300_pair_force_noalloc_x": (_i, [_vp, _vp, _vp, _vp, _i, _i, _i, _dp, _vp]),
                 "md_gb300_tc_selftest_x": (_i, [_dp]),
+                "md_gb300_set_wait_limit_x": (_i, [C.c_longlong]),
+                "md_gb300_get_wait_limit_x": (C.c_longlong, []),
+                "md_gb300_wait_selftest_x": (_i, [C.c_longlong, C.POINTER(_i), C.POINTER(C.c_longlong)]),
                 "md_gb300_autotune_pair_x": (_i, [pp, _vp, _i, C.POINTER(_i), _dp]),
                 "md_gb300_set_pair_tile_x": (_i, [_vp, _i, _i, _i]),
+                "md_gb300_set_solve_path_x": (_i, [_i]),
+                "md_gb300_get_solve_path_x": (_i, [_i]),
+                "md_gb300_autotune_solve_x": (_i, [pp, _i, C.POINTER(_i), _dp]),
+                "md_gb300_exchange_tables_x": (_i, [pp, _dp, _dp]),
                 "md_gb300_capture_ensemble_x": (_i, [_i, _vp, _vp, C.POINTER(_vp)]),
                 "md_gb300_ewald_model_nparam_x": (_i, []),
                 "md_gb300_ewald_model_create_x": (_i, [C.POINTER(_vp), pp, _i, C.c_long, C.c_uint]),

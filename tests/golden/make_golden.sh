@@ -1,11 +1,16 @@
 #!/bin/sh
 # Regenerates the golden fixtures in tests/golden/ from MD-Lab's own _nocl
-# build.  Needs the MD-Lab source tree (REF_DIR, default /root/reference);
-# the fixtures it writes are committed, so the tests themselves never need it.
+# build.  Needs the MD-Lab source tree: REF_DIR or MDLAB_SRC, else this
+# container's read-only mount of it; the fixtures it writes are committed, so
+# the tests themselves never need it.
 set -e
 HERE=$(cd "$(dirname "$0")" && pwd)
 ROOT=$(cd "$HERE/../.." && pwd)
-REF_DIR=${REF_DIR:-/root/reference}
+REF_DIR=${REF_DIR:-${MDLAB_SRC:-/root/reference}}
+if [ ! -f "$REF_DIR/md_pimd_x.c" ]; then
+  echo "make_golden.sh: no MD-Lab source tree at '$REF_DIR' (set MDLAB_SRC)" >&2
+  exit 2
+fi
 make -s -C "$ROOT/oracle" ref REF_DIR="$REF_DIR"
 OUT=$ROOT/oracle/_ref
 for v in d3l8 d3l4 d2l4; do
