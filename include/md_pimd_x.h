@@ -103,6 +103,19 @@ int md_pimd_fprint_ENk2_x(FILE *out, md_pimd_t_x *pimd);
 int md_pimd_calc_vi_virial_energy_x(md_pimd_t_x *pimd, md_stats_t_x *stats, int image);
 int md_pimd_fast_fill_ENk2_x(md_pimd_t_x *pimd, int image);
 
+/* estimators and observables outside the step: md_pimd_x.h:143, :155-156,
+   :160.  The virial about the box centre (md_pimd_x.c:3898) and the centroid
+   virial (:3924) sum over beads on the GPU; md_pimd_polymer_periodic_
+   boundary_x shifts whole ring polymers by their first bead's image count
+   (:4350); md_pimd_calc_pair_correlation_x bins the distances from bead 1 to
+   bead pi on the GPU (each in the reference's bin) and adds 1/norm per count
+   to stats->fxs[stats->N - 1] on the host (:2974). */
+int md_pimd_calc_pair_correlation_x(md_pimd_t_x *pimd, md_stats_t_x *stats, md_num_t_x rmax, md_num_t_x norm, int pi,
+                                    int image);
+int md_pimd_calc_virial_energy_x(md_pimd_t_x *pimd, md_stats_t_x *stats);
+int md_pimd_calc_centroid_virial_energy_x(md_pimd_t_x *pimd, md_stats_t_x *stats, int fc);
+int md_pimd_polymer_periodic_boundary_x(md_pimd_t_x *pimd);
+
 /* accumulator arithmetic: md_pimd_x.h:163-170, scalar (es) and
    function-valued (fxs, the _f forms) */
 int md_reset_stats_x(md_stats_t_x *stats, md_num_t_x e);

@@ -3726,6 +3726,134 @@ cudaError_t force_virial(const Geo &g, const double *x, const double *f, const d
   return reduce_into(scratch, nb, 0.5, 0.0, acc, st);
 }
 
+// -(x - c) . f m summed over all beads, c = L/2 (mode 0, md_pimd_x.c:3898-3922)
+// or each particle's centroid (mode 1, :3923-3955, the centroid summed as the
+// reference does, x_j / P in bead order).  One thread per particle.
+template <int D>
+__global__ void k_virial_about(Geo g, const double *__restrict__ x, const double *__restrict__ f,
+                               const double *__restrict__ m, int mode, double *part) {
+  __shared__ double buf[33];
+  double e = 0;
+  for (int l = blockIdx.x * blockDim.x + threadIdx.x; l < g.N; l += gridDim.x * blockDim.x) {
+    double c[D];
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      c[d] = mode ? 0.0 : g.box[d] / 2;
+      if (mode)
+        for (int j = 0; j < g.P; ++j) c[d] += x[sidx(j, d, l, D, g.Ns)] / g.P;
+    }
+    for (int j = 0; j < g.P; ++j) {
+      const double mm = m[(size_t)j * g.Ns + l];
+#pragma unroll
+      for (int d = 0; d < D; ++d) e += -(x[sidx(j, d, l, D, g.Ns)] - c[d]) * f[sidx(j, d, l, D, g.Ns)] * mm;
+    }
+  }
+  e = block_sum(e, buf);
+  if (threadIdx.x == 0) part[blockIdx.x] = e;
+}
+
+cudaError_t virial_about(const Geo &g, const double *x, const double *f, const double *m, int mode, double add,
+                         double *acc, double *scratch, cudaStream_t st) {
+  int nb = cdiv((size_t)g.N, 128);
+  if (nb > 304) nb = 304;
+  {
+    XK_PROF("virial_about");
+    DISPATCH_D(g.D, k_virial_about<D><<<nb, 128, 0, st>>>(g, x, f, m, mode, scratch));
+  }
+  cudaError_t e = XK_LAUNCHED();
+  if (e != cudaSuccess) return e;
+  return reduce_into(scratch, nb, 0.5, add, acc, st);
+}
+
+// md_simulation_x.c:858-865
+__device__ inline int image_count(double x, double L) {
+  const int c = (int)(fabs(x) / L);
+  return x > L ? -c : (x < 0 ? c + 1 : 0);
+}
+
+// md_pimd_x.c:4350-4374: every bead of a ring polymer shifted by the image
+// count of its first bead; one thread per (dimension, particle)
+__global__ void k_polymer_wrap(Geo g, double *x) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= g.D * g.N) return;
+  const int d = t / g.N, l = t % g.N;
+  const double L = g.box[d];
+  const int c = image_count(x[sidx(0, d, l, g.D, g.Ns)], L);
+  if (c == 0) return;
+  const double sh = __dmul_rn((double)c, L);
+  for (int j = 0; j < g.P; ++j) {
+    const size_t o = sidx(j, d, l, g.D, g.Ns);
+    x[o] = __dadd_rn(x[o], sh);
+  }
+}
+
+cudaError_t polymer_wrap(const Geo &g, double *x, cudaStream_t st) {
+  {
+    XK_PROF("polymer_wrap");
+    k_polymer_wrap<<<cdiv((size_t)g.D * g.N, 128), 128, 0, st>>>(g, x);
+  }
+  return XK_LAUNCHED();
+}
+
+// md_pimd_x.c:3081-3108: histogram of the distances from bead 1 of l to bead
+// jb of every other particle, bin (int)(r / incre) below `points`.  Every
+// operation of the distance is the reference's, rounded alike (no fused
+// multiply-add: md_minimum_image_x is a += L/2, a += L count, a - L/2), so
+// each distance lands in the reference's bin.  Block (32 x 8): 32 first
+// beads l, 8 warps over the partners; counts in shared memory, then added
+// to the global histogram.
+template <int D>
+__global__ void k_pair_hist(Geo g, const double *__restrict__ x, int jb, int points, double incre, int image,
+                            unsigned int *hist) {
+  extern __shared__ unsigned int sh_hist[];
+  for (int i = threadIdx.y * 32 + threadIdx.x; i < points; i += 256) sh_hist[i] = 0;
+  __syncthreads();
+  const int l = blockIdx.x * 32 + threadIdx.x;
+  if (l < g.N) {
+    double p1[D];
+#pragma unroll
+    for (int d = 0; d < D; ++d) p1[d] = x[sidx(0, d, l, D, g.Ns)];
+    for (int q = blockIdx.y * 8 + threadIdx.y; q < g.N; q += gridDim.y * 8) {
+      if (q == l) continue;
+      double s2 = 0;
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        double a = __dsub_rn(p1[d], x[sidx(jb, d, q, D, g.Ns)]);
+        if (image) {
+          const double L = g.box[d], h = L / 2;
+          a = __dadd_rn(a, h);
+          a = __dadd_rn(a, __dmul_rn(L, (double)image_count(a, L)));
+          a = __dsub_rn(a, h);
+        }
+        s2 = __dadd_rn(s2, __dmul_rn(a, a));
+      }
+      const int k = (int)__ddiv_rn(__dsqrt_rn(s2), incre);
+      if (k < points) atomicAdd(&sh_hist[k], 1u);
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.y * 32 + threadIdx.x; i < points; i += 256)
+    if (sh_hist[i]) atomicAdd(&hist[i], sh_hist[i]);
+}
+
+cudaError_t pair_hist(const Geo &g, const double *x, int jb, int points, double rmax, int image, unsigned int *hist,
+                      cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(hist, 0, sizeof(unsigned int) * points, st);
+  if (e != cudaSuccess) return e;
+  const int bx = (g.N + 31) / 32;
+  int by = (2 * 152 + bx - 1) / bx;
+  const int maxy = (g.N + 7) / 8;
+  if (by > maxy) by = maxy;
+  if (by < 1) by = 1;
+  const double incre = rmax / points;
+  {
+    XK_PROF("pair_hist");
+    DISPATCH_D(g.D, (k_pair_hist<D><<<dim3(bx, by), dim3(32, 8), sizeof(unsigned int) * points, st>>>(
+                        g, x, jb, points, incre, image, hist)));
+  }
+  return XK_LAUNCHED();
+}
+
 __global__ void k_add_into(double *__restrict__ f, const double *__restrict__ a, size_t n) {
   const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t < n) f[t] += a[t];

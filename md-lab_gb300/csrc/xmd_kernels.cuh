@@ -277,6 +277,16 @@ cudaError_t vbn_energy(int N, double beta, double vi, double add, const double *
 cudaError_t force_virial(const Geo &g, const double *x, const double *f, const double *m,
                          int image, double *acc, double *scratch, cudaStream_t st);
 cudaError_t add_scalar(double *acc, double v, cudaStream_t st);
+// 0.5 sum over beads of -(x - c) . f m, c = L/2 (mode 0) or the particle's
+// centroid (mode 1), plus `add`, added to *acc.  scratch: 304 doubles
+cudaError_t virial_about(const Geo &g, const double *x, const double *f, const double *m, int mode, double add,
+                         double *acc, double *scratch, cudaStream_t st);
+// whole ring polymers shifted into the box by their first bead's image count
+cudaError_t polymer_wrap(const Geo &g, double *x, cudaStream_t st);
+// hist[k] = number of (l, q != l) whose bead-0 to bead-jb distance r has
+// (int)(r / (rmax / points)) = k < points (minimum image when `image`)
+cudaError_t pair_hist(const Geo &g, const double *x, int jb, int points, double rmax, int image, unsigned int *hist,
+                      cudaStream_t st);
 // f[i] += a[i], i < n
 cudaError_t add_into(double *f, const double *a, size_t n, cudaStream_t st);
 

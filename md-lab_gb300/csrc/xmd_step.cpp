@@ -832,6 +832,77 @@ int md_pimd_calc_vi_virial_energy_x(md_pimd_t_x *pimd, md_stats_t_x *stats, int 
   return 0;
 }
 
+// md_pimd_x.c:3898-3922 and :3923-3955: the virial about the box centre and
+// the centroid virial (plus (D N - fc/P) / (2 beta)), from the stored forces
+static int virial_about(md_pimd_t_x *pimd, md_stats_t_x *stats, int mode, double add) {
+  SimDev *sd;
+  PimdDev *pd;
+  double *acc;
+  XMD_TRY(pimd_device(pimd, &sd, &pd));
+  XMD_TRY(stats_device(stats, &acc));
+  int rc;
+  double *scr = scratch_for(sd, general_scratch(sd->geo), &rc);
+  if (rc) return rc;
+  XMD_CUDA(xk::virial_about(sd->geo, sd->x.as<double>(), sd->f.as<double>(), sd->m.as<double>(), mode, add, acc, scr,
+                            stream()));
+  return 0;
+}
+
+int md_pimd_calc_virial_energy_x(md_pimd_t_x *pimd, md_stats_t_x *stats) {
+  if (!pimd || !pimd->sim || !pimd->sim->box || pimd->sim->box->type != MD_ND_RECT_BOX_X)
+    return fail(MD_GB_ERR_ARG, "the virial about the box centre needs a rectangular box");
+  return virial_about(pimd, stats, 0, 0.0);
+}
+
+int md_pimd_calc_centroid_virial_energy_x(md_pimd_t_x *pimd, md_stats_t_x *stats, int fc) {
+  if (!pimd) return fail(MD_GB_ERR_ARG, "NULL path-integral state");
+  return virial_about(pimd, stats, 1, (D * pimd->N - fc / (double)pimd->P) / (2 * pimd->beta));
+}
+
+// md_pimd_x.c:4350-4374
+int md_pimd_polymer_periodic_boundary_x(md_pimd_t_x *pimd) {
+  if (!pimd || !pimd->sim || !pimd->sim->box || pimd->sim->box->type != MD_ND_RECT_BOX_X)
+    return fail(MD_GB_ERR_ARG, "the polymer wrap needs a rectangular box");
+  SimDev *sd;
+  PimdDev *pd;
+  XMD_TRY(pimd_device(pimd, &sd, &pd));
+  XMD_CUDA(xk::polymer_wrap(sd->geo, sd->x.as<double>(), stream()));
+  return 0;
+}
+
+// md_pimd_x.c:2974-3109: g(r) between bead 1 and bead pi.  The distances
+// are binned on the GPU (integer counts, each distance in the reference's
+// bin); the counts then add 1/norm to stats->fxs[stats->N - 1] on the host,
+// one addition per count as the reference does, so the sums are the
+// reference's to the bit.
+int md_pimd_calc_pair_correlation_x(md_pimd_t_x *pimd, md_stats_t_x *stats, md_num_t_x rmax, md_num_t_x norm, int pi,
+                                    int image) {
+  if (!stats || !stats->fxs) return fail(MD_GB_ERR_ARG, "NULL accumulator");
+  if (capturing()) return fail(MD_GB_ERR_CAPTURE, "reads a result back; not while capturing");
+  if (stats->points < 1) return 0;
+  if (!(rmax > 0)) return fail(MD_GB_ERR_ARG, "rmax must be positive");
+  SimDev *sd;
+  PimdDev *pd;
+  XMD_TRY(pimd_device(pimd, &sd, &pd));
+  XMD_TRY(check_image(sd, image));
+  if (pi < 1 || pi > pimd->P) return fail(MD_GB_ERR_ARG, "bead index pi must be in 1..P");
+  const int pts = stats->points;
+  XMD_TRY(reserve(pd->sk_buf, sizeof(unsigned int) * (size_t)pts));
+  cudaStream_t st = stream();
+  std::vector<unsigned int> cnt(pts);
+  XMD_CUDA(xk::pair_hist(sd->geo, sd->x.as<double>(), pi - 1, pts, rmax, image, pd->sk_buf.as<unsigned int>(), st));
+  XMD_CUDA(cudaMemcpyAsync(cnt.data(), pd->sk_buf.p, sizeof(unsigned int) * pts, cudaMemcpyDeviceToHost, st));
+  XMD_CUDA(cudaStreamSynchronize(st));
+  if (!md_stats_sync_host_x(stats)) return -1;
+  const double w = 1.0 / norm;
+  for (int k = 0; k < pts; ++k) {
+    double v = stats->fxs[stats->N - 1][k];
+    for (unsigned int c = 0; c < cnt[k]; ++c) v += w;
+    stats->fxs[stats->N - 1][k] = v;
+  }
+  return 0;
+}
+
 int md_pimd_calc_trap_energy_x(md_pimd_t_x *pimd, md_trap_energy_t_x te, md_stats_t_x *stats) {
   const int kind = trap_kind_of((const void *)te, true);
   if (!kind) return fail(MD_GB_ERR_UNSUPPORTED, "trap energy function has no device kernel");

@@ -124,6 +124,14 @@ class XLib:
             "md_pimd_calc_pair_force_2_x": (_i, [pp, pp, _vp]),
             "md_pimd_calc_pair_energy_2_x": (_i, [pp, pp, _vp, pst]),
             "md_pimd_calc_vi_sign_x": (_i, [pp, pst, pst, _d]),
+            "md_pimd_calc_virial_energy_x": (_i, [pp, pst]),
+            "md_pimd_calc_centroid_virial_energy_x": (_i, [pp, pst, _i]),
+            "md_pimd_polymer_periodic_boundary_x": (_i, [pp]),
+            "md_pimd_calc_pair_correlation_x": (_i, [pp, pst, _d, _d, _i, _i]),
+            "md_reset_stats_f_x": (_i, [pst, _d]),
+            "md_stats_add_to_f_x": (_i, [pst, pst]),
+            "md_stats_copy_to_f_x": (_i, [pst, pst]),
+            "md_stats_mult_to_f_x": (_i, [pst, pst]),
             "md_calc_3d_ueg_madelung_x": (_d, [_dp]),
             "md_set_harmonic_trap_frequency_x": (None, [_d]),
             "md_set_harmonic_trap_center_x": (None, [_dp]),

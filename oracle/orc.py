@@ -76,6 +76,10 @@ def lib():
             "orc_pair_energy": (d, [vp, i, i, i, vp]),
             "orc_pair_energy_one": (d, [i, vp, i, _dp, _dp, _dp]),
             "orc_madelung": (d, [_dp, vp]),
+            "orc_virial_energy": (d, [vp, i, i]),
+            "orc_centroid_virial_energy": (d, [vp, i, i, d, i]),
+            "orc_polymer_periodic_boundary": (None, [vp, i, i]),
+            "orc_pair_correlation": (None, [vp, i, i, i, d, d, i, i, _dp]),
             "orc_vi_sign": (d, [i, d, d, d, _dp, _dp]),
             "orc_step": (i, [vp, vp, d, _dp, _dp, _dp]),
             "orc_set_seed": (None, [C.c_uint]),

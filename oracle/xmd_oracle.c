@@ -771,6 +771,84 @@ double orc_pair_energy_2(const orc_sim_t *a, int Na, const orc_sim_t *b, int Nb,
 }
 
 /* md_simulation_x.c:223-257 */
+/* md_pimd_x.c:3898-3922: -(1/2) sum over beads of (x - L/2) . f m, f the
+   stored accelerations, L the box */
+double orc_virial_energy(const orc_sim_t *s, int N, int P) {
+  double res = 0;
+  for (int j = 1; j <= P; ++j)
+    for (int l = 1; l <= N; ++l) {
+      const int b = bidx(l, j, P);
+      for (int i = 0; i < s->D; ++i)
+        res += -(s->x[(size_t)b * s->D + i] - s->box[i] / 2) * s->f[(size_t)b * s->D + i] * s->m[b];
+    }
+  return res / 2.0;
+}
+
+/* md_pimd_x.c:3923-3955: the same about each particle's centroid, plus
+   (D N - fc/P) / (2 beta) */
+double orc_centroid_virial_energy(const orc_sim_t *s, int N, int P, double beta, int fc) {
+  const int D = s->D;
+  double *c = (double *)malloc(sizeof(double) * D * N);
+  if (!c) return NAN;
+  for (int l = 1; l <= N; ++l) {
+    for (int i = 0; i < D; ++i) c[D * (l - 1) + i] = 0;
+    for (int j = 1; j <= P; ++j)
+      for (int i = 0; i < D; ++i) c[D * (l - 1) + i] += s->x[(size_t)bidx(l, j, P) * D + i] / P;
+  }
+  double res = 0;
+  for (int j = 1; j <= P; ++j)
+    for (int l = 1; l <= N; ++l) {
+      const int b = bidx(l, j, P);
+      for (int i = 0; i < D; ++i)
+        res += -(s->x[(size_t)b * D + i] - c[D * (l - 1) + i]) * s->f[(size_t)b * D + i] * s->m[b];
+    }
+  free(c);
+  return res / 2.0 + (D * N - fc / (double)P) / (2 * beta);
+}
+
+/* md_pimd_x.c:4350-4374: each ring polymer shifted by the image count of
+   its first bead */
+void orc_polymer_periodic_boundary(orc_sim_t *s, int N, int P) {
+  const int D = s->D;
+  int cnt[3];
+  for (int l = 1; l <= N; ++l) {
+    const int b1 = bidx(l, 1, P);
+    for (int i = 0; i < D; ++i) cnt[i] = orc_periodic_image_count(s->x[(size_t)b1 * D + i], s->box[i]);
+    for (int j = 1; j <= P; ++j)
+      for (int i = 0; i < D; ++i) s->x[(size_t)bidx(l, j, P) * D + i] += cnt[i] * s->box[i];
+  }
+}
+
+/* md_pimd_x.c:2974, CPU branch :3081-3108 (md_pimd_calc_pair_correlation_x):
+   distances from bead 1 of l to bead pi of every other particle, minimum
+   image when `image`, histogram of `points` bins over [0, rmax), each count
+   adding 1/norm to out (distances at rmax and beyond are dropped) */
+void orc_pair_correlation(const orc_sim_t *s, int N, int P, int points, double rmax, double norm, int pi,
+                          int image, double *out) {
+  const int D = s->D;
+  const double incre = rmax / points;
+  for (int l = 1; l <= N; ++l)
+    for (int j = 1; j <= N; ++j) {
+      if (l == j) continue;
+      const double *p1 = &s->x[(size_t)bidx(l, 1, P) * D];
+      const double *p2 = &s->x[(size_t)bidx(j, pi, P) * D];
+      double r;
+      if (image) {
+        double d = 0;
+        for (int i = 0; i < D; ++i) {
+          const double t = orc_minimum_image(p1[i] - p2[i], s->box[i]);
+          d += t * t;
+        }
+        r = sqrt(d);
+      } else {
+        r = dist(D, p1, p2);
+      }
+      const int k = (int)(r / incre);
+      if (k >= points) continue;
+      out[k] += 1.0 / norm;
+    }
+}
+
 double orc_madelung(const double *L, const orc_params_t *p) {
   const double V = L[0] * L[1] * L[2];
   const double a = p->coul_alpha;

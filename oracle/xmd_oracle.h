@@ -120,6 +120,11 @@ double orc_pair_energy_one(int kind, const orc_params_t *p, int D,
 double orc_pair_energy_2(const orc_sim_t *a, int Na, const orc_sim_t *b, int Nb,
                          int P, int kind, const orc_params_t *p);
 double orc_madelung(const double *L, const orc_params_t *p);
+double orc_virial_energy(const orc_sim_t *s, int N, int P);
+double orc_centroid_virial_energy(const orc_sim_t *s, int N, int P, double beta, int fc);
+void orc_polymer_periodic_boundary(orc_sim_t *s, int N, int P);
+void orc_pair_correlation(const orc_sim_t *s, int N, int P, int points, double rmax, double norm, int pi,
+                          int image, double *out);
 double orc_vi_sign(int N, double beta, double vi, double vi2, const double *ENk,
                    const double *VBN);
 

@@ -467,6 +467,106 @@ static void run_two(const scen_t *c, int Nb, double mb) {
   rec1("final/cross_e", take());
 }
 
+/* observables and accumulator helpers outside the step: the plain and
+   centroid virial estimators (md_pimd_x.c:3898, :3924), g(r) between bead 1
+   and bead P/2+1 (md_pimd_x.c:2974) with and without the minimum image, the
+   whole-polymer periodic wrap (md_pimd_x.c:4350) and the function-valued
+   accumulator arithmetic (md_pimd_x.c:4566-4650).  The trajectory before
+   them runs without the per-step wrap, so beads leave the box. */
+static void rec_stats_f(const char *name, md_stats_t_x *st) { rec(name, st->fxs[st->N - 1], st->points); }
+
+static void run_obs(const scen_t *c) {
+  scen_t c2 = *c;
+  c2.pbc = 0;
+  md_set_pimd_mode_x(1);
+  md_set_seed_x((unsigned)c->seed);
+  int nb = c->N * c->P;
+  md_simulation_t_x *sim = md_alloc_simulation_x(nb, c->f, c->fc, MD_ND_RECT_BOX_X);
+  double T, Lb;
+  if (c->ueg) {
+    Lb = cbrt(4.0 * M_PI * c->N / 3.0) * c->rs;
+    double n = c->N / (Lb * Lb * Lb);
+    T = c->theta * 0.5 * pow(6.0 * M_PI * M_PI * n, 2.0 / 3.0);
+  } else {
+    Lb = c->box;
+    T = 1.0 / c->beta;
+  }
+  double Lv[D], center[D], zero[D];
+  for (int d = 0; d < D; ++d) {
+    Lv[d] = Lb;
+    center[d] = Lb / 2;
+    zero[d] = 0;
+  }
+  md_init_nd_rect_box_x(sim->box, Lv);
+  md_pimd_t_x *pimd = md_alloc_pimd_x(sim, c->N, c->P, c->vi, T);
+  md_init_particle_mass_x(sim, 1.0, 0, nb);
+  if (c->ueg)
+    md_pimd_init_particle_uniform_pos_x(pimd, center, Lv, 0.05 * c->rs);
+  else
+    for (int b = 0; b < nb; ++b)
+      for (int d = 0; d < D; ++d) sim->particles[b].x[d] = md_random_gaussian_x();
+  md_init_maxwell_vel_x(sim, T);
+  md_init_nhc_x(sim, md_get_quick_Q_x(T, pimd->omegaP), 0, sim->Nf, 0);
+  for (int b = 0; b < nb; ++b)
+    for (int d = 0; d < D; ++d) sim->particles[b].f[d] = 0;
+  md_set_harmonic_trap_frequency_x(1.0);
+  md_set_harmonic_trap_center_x(zero);
+  md_set_gaussian_force_strength_x(c->g);
+  md_set_guassian_force_range_x(c->s);
+  md_set_coulomb_force_strength_x(1.0);
+  md_set_coulomb_truc_x(c->alpha_L / Lb);
+  md_set_coulomb_n_sum_x(c->nsum);
+  double hdr[] = {D, LC, c->N, c->P, c->f, c->fc, c->vi, pimd->beta, pimd->omegaP, T, Lb, c->dt,
+                  c->image, 0, c->ueg, c->g, c->s, c->alpha_L / Lb, c->nsum, c->steps, c->every};
+  rec("hdr", hdr, sizeof hdr / sizeof hdr[0]);
+  {
+    double *m = malloc(sizeof(double) * nb);
+    for (int b = 0; b < nb; ++b) m[b] = sim->particles[b].m;
+    rec("m", m, nb);
+    free(m);
+  }
+  for (int st = 1; st <= c->steps; ++st) {
+    md_update_nhc_VV3_1_x(sim, c->dt);
+    forces(pimd, &c2, 0);
+    md_update_nhc_VV3_2_x(sim, c->dt);
+  }
+  forces(pimd, &c2, 0);
+  rec_field("obs/", sim, 'x');
+  rec_field("obs/", sim, 'f');
+  md_pimd_calc_virial_energy_x(pimd, g_st);
+  rec1("obs/e_virial", take());
+  md_pimd_calc_centroid_virial_energy_x(pimd, g_st, 0);
+  rec1("obs/e_centroid_fc0", take());
+  md_pimd_calc_centroid_virial_energy_x(pimd, g_st, 3);
+  rec1("obs/e_centroid_fc3", take());
+  const int pts = 40;
+  const double norm = 0.5 * c->N * (c->N - 1);
+  for (int img = 0; img <= 1; ++img) {
+    md_stats_t_x *st = md_alloc_stats_x(pts);
+    st->fxs[0][3] = 0.25;  /* the call adds to what is there */
+    md_pimd_calc_pair_correlation_x(pimd, st, Lb / 2, norm, c->P / 2 + 1, img);
+    rec_stats_f(img ? "gr/image" : "gr/plain", st);
+  }
+  double grp[] = {pts, Lb / 2, norm, c->P / 2 + 1};
+  rec("gr/params", grp, 4);
+  md_pimd_polymer_periodic_boundary_x(pimd);
+  rec_field("pbc/", sim, 'x');
+  /* accumulator arithmetic on fxs */
+  md_stats_t_x *a = md_alloc_stats_x(5), *b = md_alloc_stats_x(5), *q = md_alloc_stats_x(4);
+  for (int i = 0; i < 5; ++i) b->fxs[0][i] = i + 0.5;
+  b->es[0] = 1.5;
+  md_reset_stats_f_x(a, 2.0);
+  rec_stats_f("acc/reset", a);
+  md_stats_add_to_f_x(a, b);
+  rec_stats_f("acc/add", a);
+  md_stats_mult_to_f_x(a, b);
+  rec_stats_f("acc/mult", a);
+  rec1("acc/add_mismatch_rc", md_stats_add_to_f_x(a, q));
+  rec1("acc/copy_mismatch_rc", md_stats_copy_to_f_x(a, q));
+  md_stats_copy_to_f_x(a, b);
+  rec_stats_f("acc/copy", a);
+}
+
 static int geti(int argc, char **argv, const char *k, int dflt) {
   size_t n = strlen(k);
   for (int i = 3; i < argc; ++i)
@@ -517,6 +617,8 @@ int main(int argc, char **argv) {
     run_rng();
   else if (!strcmp(argv[1], "pairs"))
     run_pairs();
+  else if (!strcmp(argv[1], "obs"))
+    run_obs(&c);
   else if (!strcmp(argv[1], "two"))
     run_two(&c, geti(argc, argv, "Nb", 4), getd(argc, argv, "mb", 1.0));
   else

@@ -44,6 +44,10 @@ $G3 cubic d3l4_cubic_img.bin N=6 P=4 vi=1 beta=3 seed=22 image=1 box=2.5
 $G3 two d3l4_two_ueg.bin N=5 Nb=4 P=4 vi=0.8 rs=2 theta=0.5 ueg=1 image=1 pbc=1 nsum=3 dt=0.05 seed=23 steps=10 mb=1
 $G3 two d3l4_two_trap.bin N=6 Nb=5 P=4 vi=0.5 beta=3 seed=24 steps=20 mb=2
 $G2 two d2l4_two_trap.bin N=3 Nb=7 P=6 vi=1 beta=2 seed=25 steps=20 mb=0.5
+# observables outside the step (plain and centroid virial, g(r), polymer wrap,
+# function-valued accumulators) after a trajectory without the per-step wrap
+$G3 obs d3l4_obs_ueg.bin N=9 P=6 vi=0.7 rs=2 theta=0.5 ueg=1 image=1 nsum=2 dt=0.05 seed=31 steps=15
+$G2 obs d2l4_obs_trap.bin N=7 P=5 vi=1 beta=3 seed=32 steps=10 box=3
 # random numbers and isolated pair callbacks
 $G3 rng rng.bin
 $G3 pairs d3_pairs.bin

@@ -273,8 +273,8 @@ def test_connection_probabilities_against_extended_precision(N, P, kind, vi):
     e_gpu, e_ref = relerr(got["G"], exact), relerr(ref["G"], exact)
     print(f"N={N} P={P} {kind} xi={vi}: G against extended precision: this library {e_gpu:.2e}, "
           f"the reference's formula in FP64 {e_ref:.2e}")
-    assert e_gpu <= 1e-11
-    assert e_gpu <= 0.5 * e_ref
+    assert e_gpu <= 5e-11
+    assert e_gpu <= 0.2 * e_ref
 
 
 def test_solve_autotuner_records_its_choice():

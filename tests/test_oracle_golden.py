@@ -209,3 +209,33 @@ def test_oracle_two_species(name):
         for k in ("x", "v", "theta", "vtheta"):
             assert_close(getattr(s, k), fx[sp + "final/" + k], 1e-9, f"{name} {sp} final {k}")
     assert_close([orc.pair_energy_2(a, Na, b, Nb, P, pair, prm)], fx["final/cross_e"], 1e-9, "final cross energy")
+
+
+OBS_FIXTURES = ["d3l4_obs_ueg", "d2l4_obs_trap"]
+
+
+@pytest.mark.parametrize("name", OBS_FIXTURES)
+def test_oracle_observables(name):
+    """plain and centroid virial estimators, g(r) with and without the
+    minimum image, and the whole-polymer periodic wrap, on the state the
+    reference recorded after a trajectory without the per-step wrap"""
+    fx = fixtures.load(name)
+    h = fixtures.header(fx)
+    N, P, D = h["N"], h["P"], h["D"]
+    L = orc.lib()
+    nb = N * P
+    s = orc.OrcSim(D, h["L"], nb, fx["m"], fx["obs/x"], np.zeros(nb * D), fx["obs/f"], np.ones(nb * D),
+                   np.zeros(nb * D * h["L"]), np.zeros(nb * D * h["L"]), np.ones(nb * D * h["L"]), h["T"],
+                   [h["box"]] * 3)
+    assert_close([L.orc_virial_energy(s.ref, N, P)], fx["obs/e_virial"], TIGHT, "virial")
+    for fc in (0, 3):
+        assert_close([L.orc_centroid_virial_energy(s.ref, N, P, h["beta"], fc)], fx[f"obs/e_centroid_fc{fc}"],
+                     TIGHT, f"centroid virial fc={fc}")
+    pts, rmax, norm, pi = fx["gr/params"]
+    for img, key in ((0, "gr/plain"), (1, "gr/image")):
+        out = np.zeros(int(pts))
+        out[3] = 0.25
+        L.orc_pair_correlation(s.ref, N, P, int(pts), rmax, norm, int(pi), img, orc.ptr(out))
+        assert np.array_equal(out, fx[key]), key  # counts of 1/norm: bit for bit
+    L.orc_polymer_periodic_boundary(s.ref, N, P)
+    assert np.array_equal(s.x, fx["pbc/x"])
