@@ -236,6 +236,20 @@ def kept_nz_pairs(nsum):
     return sum(nzmax.values())
 
 
+def shell_vectors(count=32):
+    """half-space wave vectors of the `count` lowest shells |n|^2 (the
+    descriptors' structure-factor features)"""
+    shells, n2 = [], 0
+    while len(shells) < count:
+        n2 += 1
+        if any(a * a + b * b <= n2 and int(round(math.sqrt(n2 - a * a - b * b))) ** 2 == n2 - a * a - b * b
+               for a in range(int(math.sqrt(n2)) + 1) for b in range(int(math.sqrt(n2)) + 1)):
+            shells.append(n2)
+    m = int(math.sqrt(shells[-1]))
+    return sum(1 for a in range(m + 1) for b in range(-m, m + 1) for c in range(-m, m + 1)
+               if (a > 0 or (a == 0 and b > 0) or (a == 0 and b == 0 and c > 0)) and a * a + b * b + c * c in shells)
+
+
 def kernel_flops(name, nsum=NSUM):
     if name in ("recip_force", "recip_force32"):
         # 17.7 flop per +-nz pair of a kept column per particle and slice
@@ -249,11 +263,16 @@ def kernel_flops(name, nsum=NSUM):
         pairs = P * N * (N - 1) / 2
         return pairs * (47.0 * n_images(3.6) + 39.0)
     if name == "desc":
-        # per ordered pair: 12 flop for the minimum-image distance, and for the
-        # (4/3) pi (1/2)^3 = 52% inside rc = L/2 another 45 (cut-off weight,
-        # bins, two deposits, three vector features); per particle the
-        # 128 x 64 histogram-to-feature product
-        return N * N * P * (12.0 + 0.5236 * 45.0) + N * P * 2.0 * 128 * 64
+        # per ordered pair: 15 flop for the minimum-image distance and the
+        # cut-off test, and for the (4/3) pi (1/2)^3 = 52% inside rc = L/2
+        # another 45 (r, cut-off weight, bin weights, two deposits, three
+        # Gaussian-weighted vector features); per particle the 64 x 32
+        # histogram-to-feature product
+        return N * N * P * (15.0 + 0.5236 * 45.0) + N * P * 2.0 * 64 * 32
+    if name == "desc_shells":
+        # per slice, wave vector of the 32 lowest shells and particle: two
+        # complex products and the complex add (14 flop)
+        return P * shell_vectors() * N * 14.0
     if name == "mlp_forward":
         return 2.0 * N * P * (64 * 128 + 128 * 128 + 128 * 16)
     return None

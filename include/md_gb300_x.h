@@ -173,10 +173,11 @@ int md_gb300_get_precision_x(void);
    reciprocal sum (n_sum from md_set_coulomb_*) and a truncated one
    (n_sum_cheap): an energy and the coefficients of three vector features
    that give the force.  Inputs are 64 descriptors per particle: 32 Gaussian
-   radial functions and the spherical averages sin(kr)/(kr) of the 32 lowest
-   reciprocal-lattice shells, both summed over minimum-image neighbours
-   within half the box.  A model belongs to one system shape (N, P, box,
-   Ewald alpha and strength) and lives on the GPU. */
+   radial functions (centres 0.5 .. L/2) of the particle's minimum-image
+   neighbours within half the box, and |S(k)| of its bead slice on the 32
+   lowest reciprocal-lattice shells (the root mean square of |S(k)|/sqrt(N)
+   over each shell).  A model belongs to one system shape (N, P, box, Ewald
+   alpha and strength) and lives on the GPU. */
 typedef struct md_gb300_ewald_model md_gb300_ewald_model_t_x;
 int md_gb300_ewald_model_nparam_x(void);
 /* capacity: configurations (all bead slices of the system) kept for training */
@@ -216,7 +217,10 @@ int md_gb300_mlp_forward_x(md_gb300_ewald_model_t_x *model, const float *X, int 
 int md_gb300_mlp_grad_x(md_gb300_ewald_model_t_x *model, const float *X, const float *V, const float *T, int rows,
                         double we, double wf, float *grad, float *loss);
 /* raw descriptors F[N*P][64] and vector features V[N*P][12] of pimd's
-   current configuration (row j*N + l), and the descriptor definition */
+   current configuration (row j*N + l), and the descriptor definition: the
+   cut-off rc, the radial basis basis[64][32] (the 32 Gaussians at the
+   centres of 64 histogram bins on [0, rc)), and the centres and widths of
+   the vector features' radial bumps */
 int md_gb300_ewald_model_features_x(md_gb300_ewald_model_t_x *model, md_pimd_t_x *pimd, float *F, float *V);
 int md_gb300_ewald_model_desc_info_x(md_gb300_ewald_model_t_x *model, double *rc, float *basis, double vmu[3],
                                      double vsig[3]);

@@ -891,30 +891,109 @@ cudaError_t mlp_train_grad(const MlpDev &w, const uint8_t *ximg, const float *V,
 // ===================================================================
 // descriptors
 // ===================================================================
-// Block = 32 particles of one bead slice (the rows), 8 warps over the
-// slice's partners.  Lane t of every warp handles row t; warp w visits the
-// partners w, w+8, ...  For each minimum-image partner within rc the pair
-// deposits fc(r) = (1 - r^2/rc^2)^2 into a radial histogram of DESC_BINS bins
-// by linear ("cloud in cell") weights between bin centres, and adds
-// fc(r) q_m(r) (x_l - x_c)/r to three vector sums (q_m Gaussian bumps).  The
-// 64 features are then the histogram times a fixed basis (32 Gaussians in r
-// and the spherical average sin(k r)/(k r) of the 32 lowest reciprocal-lattice
-// shells), normalised and stored as BF16 tile images.
-constexpr int DS_ROWS = 32, DS_WARPS = 8;
+// 64 features per (slice, particle):
+//   0..31   radial: minimum-image neighbours within rc deposit fc(r) =
+//           (1 - r^2/rc^2)^2 into a DESC_BINS-bin histogram (linear weights
+//           between bin centres); the features are the histogram times 32
+//           Gaussians in r centred 0.5 .. rc (p.basis)
+//   32..63  the slice's structure factor: for each of the 32 lowest
+//           reciprocal-lattice shells, sqrt(mean over the shell of
+//           |S(k)|^2 / N) (k_sk_shells, the same for every particle of the
+//           slice)
+// and three vector features per particle, sum over the same neighbours of
+// fc(r) q_m(r) (x_l - x_c)/r with Gaussian bumps q_m (centres 0.25, 0.5,
+// 0.75 rc, width 0.15 rc).
+
+// |S(k)| shell features: blocks (slice, group of SH_K wave vectors), SH_G
+// threads per wave vector.  The particles' phase factors e^{2 pi i n x_d /
+// L_d}, n = 0..nmax, go to shared memory in chunks of SH_CHUNK particles;
+// thread (k, g) sums S(k) over the chunk's particles g, g + SH_G, ...; the
+// SH_G partial sums are added in shared memory, and |S(k)|^2 / (N count)
+// goes to k's shell (shell[] zeroed beforehand); the square roots are taken
+// where the features are read (k_desc).
+constexpr int SH_K = 128, SH_G = 4, SH_T = SH_K * SH_G, SH_CHUNK = 256, SH_LD = SH_CHUNK + 1;
+
+__device__ __forceinline__ float2 cmulf2(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+__global__ void __launch_bounds__(SH_T) k_sk_shells(Geo g, DescPrm p, const double *__restrict__ x) {
+  extern __shared__ float2 shp[];  // [3][nmax + 1][SH_LD]
+  __shared__ float2 part[SH_G][SH_K];
+  const int j = blockIdx.x, t = threadIdx.x, np1 = p.nmax + 1;
+  const int kl = t % SH_K, grp = t / SH_K;
+  const int k = blockIdx.y * SH_K + kl;
+  const int4 kv = k < p.nkvec ? p.kvec[k] : make_int4(0, 0, 0, -1);
+  const int ny = abs(kv.y), nz = abs(kv.z);
+  const float sy = kv.y < 0 ? -1.f : 1.f, sz = kv.z < 0 ? -1.f : 1.f;
+  float sr = 0.f, si = 0.f;
+  for (int c0 = 0; c0 < g.N; c0 += SH_CHUNK) {
+    __syncthreads();
+    for (int q = t; q < 3 * SH_CHUNK; q += SH_T) {
+      const int d = q / SH_CHUNK, i = q % SH_CHUNK, l = c0 + i;
+      float2 e = make_float2(0.f, 0.f), e1 = make_float2(0.f, 0.f);
+      if (l < g.N) {  // padding particles contribute nothing
+        double u = x[sidx(j, d, l, 3, g.Ns)] * g.inv_box[d];
+        u -= floor(u);
+        float sn, cs;
+        sincospif(2.f * (float)u, &sn, &cs);
+        e = make_float2(1.f, 0.f);
+        e1 = make_float2(cs, sn);
+      }
+      for (int n = 0; n < np1; ++n) {
+        shp[(d * np1 + n) * SH_LD + i] = e;
+        e = cmulf2(e, e1);
+      }
+    }
+    __syncthreads();
+    if (kv.w < 0) continue;
+    const int cn = min(SH_CHUNK, g.N - c0);
+    const float2 *px = shp + kv.x * SH_LD, *py = shp + (np1 + ny) * SH_LD, *pz = shp + (2 * np1 + nz) * SH_LD;
+#pragma unroll 4
+    for (int i = grp; i < cn; i += SH_G) {
+      float2 ey = py[i], ez = pz[i];
+      ey.y *= sy;
+      ez.y *= sz;
+      const float2 v = cmulf2(cmulf2(px[i], ey), ez);
+      sr += v.x;
+      si += v.y;
+    }
+  }
+  part[grp][kl] = make_float2(sr, si);
+  __syncthreads();
+  if (grp == 0 && kv.w >= 0) {
+#pragma unroll
+    for (int q = 1; q < SH_G; ++q) {
+      sr += part[q][kl].x;
+      si += part[q][kl].y;
+    }
+    atomicAdd(&p.shell[j * DESC_SHELLS + kv.w], (sr * sr + si * si) * p.shell_norm[kv.w]);
+  }
+}
+
+// Radial and vector features.  Block = 32 particles of one bead slice (the
+// rows) x 8 warps over the slice's partners: lane t of warp w handles row t
+// and the partners w, w + 8, ...  Every thread keeps its own histogram
+// column in shared memory (bin b of thread i at hist[b * 256 + i]: the
+// lanes of a warp always hit 32 distinct banks, and no two threads write the
+// same word, so there are no atomics); a pair outside the cut-off deposits
+// zero weight instead of branching.  The 8 columns of a row are then summed
+// into one before the basis product.
+constexpr int DS_ROWS = 32, DS_WARPS = 8, DS_T = DS_ROWS * DS_WARPS;
 
 template <bool RAW>
-__global__ void __launch_bounds__(DS_WARPS * 32) k_desc(Geo g, DescPrm p, const double *__restrict__ x,
-                                                        uint8_t *__restrict__ ximg, float *__restrict__ V,
-                                                        float *__restrict__ raw) {
-  // the 32 KB basis is read through L1 (shared by every block on the SM),
-  // so that shared memory holds only per-block data and more blocks fit
+__global__ void __launch_bounds__(DS_T, 2) k_desc(Geo g, DescPrm p, const double *__restrict__ x,
+                                                  uint8_t *__restrict__ ximg, float *__restrict__ V,
+                                                  float *__restrict__ raw) {
   extern __shared__ __align__(16) float dsm[];
-  float *hist = dsm;                                 // [DESC_BINS][DS_ROWS]: lane t owns column t
-  float *vacc = hist + DESC_BINS * DS_ROWS;          // DS_WARPS * DS_ROWS * 9
-  float4 *pos = (float4 *)(vacc + DS_WARPS * DS_ROWS * 9);  // N; 25600 bytes in: 16-byte aligned
+  float *hist = dsm;                                        // [DESC_BINS][DS_T]
+  float *vacc = hist + DESC_BINS * DS_T;                    // [DS_WARPS][DS_ROWS][9]
+  float4 *pos = (float4 *)(vacc + DS_WARPS * DS_ROWS * 9);  // N
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int j = blockIdx.y, l0 = blockIdx.x * DS_ROWS;
-  for (int q = tid; q < DS_ROWS * DESC_BINS; q += blockDim.x) hist[q] = 0.f;
+  float *hcol = hist + tid;
+#pragma unroll 8
+  for (int b = 0; b < DESC_BINS; ++b) hcol[b * DS_T] = 0.f;
   for (int q = tid; q < g.N; q += blockDim.x)
     pos[q] = make_float4((float)x[sidx(j, 0, q, 3, g.Ns)], (float)x[sidx(j, 1, q, 3, g.Ns)],
                          (float)x[sidx(j, 2, q, 3, g.Ns)], 0.f);
@@ -926,9 +1005,6 @@ __global__ void __launch_bounds__(DS_WARPS * 32) k_desc(Geo g, DescPrm p, const 
   float vs[9];
 #pragma unroll
   for (int i = 0; i < 9; ++i) vs[i] = 0.f;
-  // bin b of row t at hist[b*32 + t]: the lanes of a warp (rows) always hit
-  // distinct banks, whatever bins they deposit into
-  float *hrow = hist + lane;
   for (int c = warp; c < g.N; c += DS_WARPS) {
     const float4 xc = pos[c];
     float d0 = xr.x - xc.x, d1 = xr.y - xc.y, d2 = xr.z - xc.z;
@@ -936,28 +1012,23 @@ __global__ void __launch_bounds__(DS_WARPS * 32) k_desc(Geo g, DescPrm p, const 
     d1 -= p.box[1] * rintf(d1 * p.inv_box[1]);
     d2 -= p.box[2] * rintf(d2 * p.inv_box[2]);
     const float r2 = d0 * d0 + d1 * d1 + d2 * d2;
-    if (!live || c == l || !(r2 < rc2)) continue;
-    const float ir = rsqrtf(r2), r = r2 * ir, u = 1.f - r2 * inv_rc2, fc = u * u;
-    const float tb = r * p.inv_h - 0.5f;
-    int b0 = (int)floorf(tb);
-    float w1 = tb - (float)b0;
-    if (b0 < 0) {
-      b0 = 0;
-      w1 = 0.f;
-    }
-    if (b0 >= DESC_BINS - 1) {
-      b0 = DESC_BINS - 1;
-      w1 = 0.f;
-    }
-    atomicAdd(&hrow[b0 * DS_ROWS], fc * (1.f - w1));
-    if (w1 > 0.f) atomicAdd(&hrow[(b0 + 1) * DS_ROWS], fc * w1);
+    const bool in = live && c != l && r2 < rc2;
+    const float r2s = in ? r2 : rc2;  // fc = 0 there: every deposit below adds zero
+    const float ir = rsqrtf(r2s), r = r2s * ir, u = 1.f - r2s * inv_rc2, fc = in ? u * u : 0.f;
+    const float tb = fmaxf(r * p.inv_h - 0.5f, 0.f);  // below the first bin centre: all into bin 0
+    const int b0 = min((int)tb, DESC_BINS - 1);
+    const float w1 = b0 < DESC_BINS - 1 ? tb - (float)b0 : 0.f;
+    const int b1 = min(b0 + 1, DESC_BINS - 1);
+    hcol[b0 * DS_T] += fc * (1.f - w1);
+    hcol[b1 * DS_T] += fc * w1;
+    const float fir = fc * ir;
 #pragma unroll
     for (int m = 0; m < 3; ++m) {
       const float dr = r - p.vmu[m];
-      const float q = fc * __expf(-dr * dr * p.vinv2s2[m]) * ir;
-      vs[3 * m] += q * d0;
-      vs[3 * m + 1] += q * d1;
-      vs[3 * m + 2] += q * d2;
+      const float q = fir * __expf(-dr * dr * p.vinv2s2[m]);
+      vs[3 * m] = fmaf(q, d0, vs[3 * m]);
+      vs[3 * m + 1] = fmaf(q, d1, vs[3 * m + 1]);
+      vs[3 * m + 2] = fmaf(q, d2, vs[3 * m + 2]);
     }
   }
 #pragma unroll
@@ -965,7 +1036,7 @@ __global__ void __launch_bounds__(DS_WARPS * 32) k_desc(Geo g, DescPrm p, const 
   __syncthreads();
   if (warp == 0 && live) {
     const size_t grow = (size_t)j * g.N + l;
-    float* vo = V + grow * DESC_VSTRIDE;
+    float *vo = V + grow * DESC_VSTRIDE;
 #pragma unroll
     for (int i = 0; i < 9; ++i) {
       float s = 0.f;
@@ -976,61 +1047,99 @@ __global__ void __launch_bounds__(DS_WARPS * 32) k_desc(Geo g, DescPrm p, const 
     vo[10] = 0.f;
     vo[11] = 0.f;
   }
-  // features: 8 per thread, row = tid / 8
-  const int rr = tid >> 3, f0 = (tid & 7) * 8;
-  float acc[8];
+  // the 8 partner groups' columns of each row summed into the first
+  // (thread t: row t & 31, bins (t >> 5) + 8i; each (bin, row) has one thread)
+  {
+    const int row = tid & (DS_ROWS - 1);
+    for (int b = tid >> 5; b < DESC_BINS; b += DS_WARPS) {
+      float h = 0.f;
 #pragma unroll
-  for (int q = 0; q < 8; ++q) acc[q] = 0.f;
+      for (int w = 0; w < DS_WARPS; ++w) h += hist[b * DS_T + w * DS_ROWS + row];
+      hist[b * DS_T + row] = h;
+    }
+  }
+  __syncthreads();
+  // features: thread (row rr, group f0) takes radial features f0..f0+3 and
+  // shell features 32+f0..32+f0+3
+  const int rr = tid >> 3, f0 = (tid & 7) * 4;
+  float acc[4] = {0.f, 0.f, 0.f, 0.f};
   const float *hr = hist + rr;
   for (int b = 0; b < DESC_BINS; ++b) {
-    const float h = hr[b * DS_ROWS];
-    const float4 u0 = __ldg((const float4 *)(p.basis + b * 64 + f0));
-    const float4 u1 = __ldg((const float4 *)(p.basis + b * 64 + f0 + 4));
+    const float h = hr[b * DS_T];
+    const float4 u0 = __ldg((const float4 *)(p.basis + b * 32 + f0));
     acc[0] = fmaf(h, u0.x, acc[0]);
     acc[1] = fmaf(h, u0.y, acc[1]);
     acc[2] = fmaf(h, u0.z, acc[2]);
     acc[3] = fmaf(h, u0.w, acc[3]);
-    acc[4] = fmaf(h, u1.x, acc[4]);
-    acc[5] = fmaf(h, u1.y, acc[5]);
-    acc[6] = fmaf(h, u1.z, acc[6]);
-    acc[7] = fmaf(h, u1.w, acc[7]);
   }
   const int lr = l0 + rr;
   if (lr >= g.N) return;
+  const float4 sh = *(const float4 *)(p.shell + j * DESC_SHELLS + f0);
+  const float sv[4] = {sqrtf(sh.x), sqrtf(sh.y), sqrtf(sh.z), sqrtf(sh.w)};
   const size_t grow = (size_t)j * g.N + lr;
   if (RAW) {
 #pragma unroll
-    for (int q = 0; q < 8; ++q) raw[grow * 64 + f0 + q] = acc[q];
+    for (int q = 0; q < 4; ++q) {
+      raw[grow * 64 + f0 + q] = acc[q];
+      raw[grow * 64 + 32 + f0 + q] = sv[q];
+    }
   }
-  uint32_t pk[4];
+  uint8_t *tile = ximg + (grow / MLP_TILE) * MLP_TILE_BYTES;
+  const int row = (int)(grow % MLP_TILE);
+  uint32_t pk[2];
 #pragma unroll
-  for (int q = 0; q < 4; ++q)
+  for (int q = 0; q < 2; ++q)
     pk[q] = tc::pack_bf16((acc[2 * q] - p.fmean[f0 + 2 * q]) * p.fistd[f0 + 2 * q],
                           (acc[2 * q + 1] - p.fmean[f0 + 2 * q + 1]) * p.fistd[f0 + 2 * q + 1]);
-  *(uint4 *)(ximg + (grow / MLP_TILE) * MLP_TILE_BYTES + kmaj_off((int)(grow % MLP_TILE), f0, MLP_IN)) =
-      make_uint4(pk[0], pk[1], pk[2], pk[3]);
+  *(uint2 *)(tile + kmaj_off(row, f0, MLP_IN)) = make_uint2(pk[0], pk[1]);
+#pragma unroll
+  for (int q = 0; q < 2; ++q)
+    pk[q] = tc::pack_bf16((sv[2 * q] - p.fmean[32 + f0 + 2 * q]) * p.fistd[32 + f0 + 2 * q],
+                          (sv[2 * q + 1] - p.fmean[32 + f0 + 2 * q + 1]) * p.fistd[32 + f0 + 2 * q + 1]);
+  *(uint2 *)(tile + kmaj_off(row, 32 + f0, MLP_IN)) = make_uint2(pk[0], pk[1]);
 }
 
 static size_t desc_smem(int N) {
-  return sizeof(float) * ((size_t)DS_ROWS * DESC_BINS + DS_WARPS * DS_ROWS * 9) + sizeof(float4) * (size_t)N;
+  return sizeof(float) * ((size_t)DESC_BINS * DS_T + DS_WARPS * DS_ROWS * 9) + sizeof(float4) * (size_t)N;
 }
 
 cudaError_t desc_build(const Geo &g, const DescPrm &p, const double *x, uint8_t *ximg, float *V, float *raw,
                        cudaStream_t st) {
   if (g.D != 3) return cudaErrorInvalidValue;
-  const size_t smem = desc_smem(g.N);
-  if (smem > 227 * 1024) return cudaErrorInvalidValue;
-  static bool opted[2] = {false, false};
+  const size_t smem = desc_smem(g.N), smem_sh = sizeof(float2) * 3 * (p.nmax + 1) * SH_LD;
+  if (smem > 227 * 1024 || smem_sh > 200 * 1024) return cudaErrorInvalidValue;
+  // dynamic shared memory opted in up to what each launch needs (k_sk_shells
+  // also holds a static array, so it cannot take the whole 227 KB)
+  static size_t opted[3] = {0, 0, 0};
   auto kf = raw ? k_desc<true> : k_desc<false>;
-  if (!opted[raw ? 1 : 0]) {
-    cudaError_t e = cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-    if (e != cudaSuccess) return e;
-    opted[raw ? 1 : 0] = true;
+  if (opted[raw ? 1 : 0] < smem) {
+    cudaError_t e = cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return e;
+    }
+    opted[raw ? 1 : 0] = smem;
   }
+  if (opted[2] < smem_sh) {
+    cudaError_t e = cudaFuncSetAttribute(k_sk_shells, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_sh);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return e;
+    }
+    opted[2] = smem_sh;
+  }
+  cudaError_t e = cudaMemsetAsync(p.shell, 0, sizeof(float) * DESC_SHELLS * g.P, st);
+  if (e != cudaSuccess) return e;
+  {
+    XK_PROF("desc_shells");
+    k_sk_shells<<<dim3(g.P, (p.nkvec + SH_K - 1) / SH_K), SH_T, smem_sh, st>>>(g, p, x);
+  }
+  e = XK_LAUNCHED();
+  if (e != cudaSuccess) return e;
   dim3 grid((g.N + DS_ROWS - 1) / DS_ROWS, g.P);
   {
     XK_PROF("desc");
-    kf<<<grid, DS_WARPS * 32, smem, st>>>(g, p, x, ximg, V, raw);
+    kf<<<grid, DS_T, smem, st>>>(g, p, x, ximg, V, raw);
   }
   return XK_LAUNCHED();
 }

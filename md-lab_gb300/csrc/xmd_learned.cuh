@@ -19,7 +19,8 @@
 namespace xk {
 
 constexpr int MLP_IN = 64, MLP_H = 128, MLP_OUT = 4, MLP_TILE = 128;
-constexpr int DESC_BINS = 128;   // radial histogram bins on [0, rc)
+constexpr int DESC_BINS = 64;    // radial histogram bins on [0, rc)
+constexpr int DESC_SHELLS = 32;  // reciprocal-lattice shells of the |S(k)| features
 constexpr int DESC_VSTRIDE = 12; // floats per row of V: 3 vectors, weight, 2 pad
 constexpr size_t MLP_TILE_BYTES = (size_t)MLP_TILE * MLP_IN * 2;  // one X tile image
 
@@ -50,7 +51,11 @@ struct DescPrm {
   float box[3], inv_box[3];
   float vmu[3], vinv2s2[3];    // vector radial bases: centres, 1/(2 sigma^2)
   float vscale[3];             // scale of each vector feature in V
-  const float *basis;          // [DESC_BINS][64] histogram -> feature matrix
+  const float *basis;          // [DESC_BINS][32] histogram -> radial features (Gaussians in r)
+  const int4 *kvec;            // half-space wave vectors of the lowest shells: (nx >= 0, ny, nz, shell)
+  int nkvec, nmax;             // their count and largest |n_i|
+  const float *shell_norm;     // [DESC_SHELLS] 1 / (N x half-space vectors of the shell)
+  float *shell;                // [P][DESC_SHELLS] scratch: each slice's shell features (squared)
   const float *fmean, *fistd;  // feature normalisation
 };
 

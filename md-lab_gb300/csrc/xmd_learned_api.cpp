@@ -34,6 +34,7 @@ struct md_gb300_ewald_model {
   long cap_cfg = 0, ncollected = 0;
   DevBuf par, grad, m1, m2, w1, w2, w3, w3f, lossacc, err;
   DevBuf basis, fmean, fistd;
+  DevBuf dkv, dsn, dsh;  // descriptor wave vectors, shell normalisation, per-slice shell features
   DevBuf dsx, dsv, dst;
   DevBuf lx, lv, ly, raw;
   DevBuf fa, fb, ea, eb, fp, ep, jacc;
@@ -111,24 +112,40 @@ static std::vector<int> lowest_shells(int count) {
   return s;
 }
 
-// histogram -> feature basis: 32 Gaussians in r (centres 0.5 .. rc, width
-// their spacing) and sin(k r)/(k r) for the 32 lowest reciprocal shells,
-// evaluated at the bin centres
-static void make_basis(const double *box, double rc, std::vector<float> &B) {
-  B.assign((size_t)xk::DESC_BINS * 64, 0.f);
+// histogram -> radial features: 32 Gaussians in r (centres 0.5 .. rc,
+// width their spacing) evaluated at the bin centres
+static void make_basis(double rc, std::vector<float> &B) {
+  B.assign((size_t)xk::DESC_BINS * 32, 0.f);
   const double h = rc / xk::DESC_BINS, sp = (rc - 0.5) / 31.0;
-  const std::vector<int> sh = lowest_shells(32);
   for (int b = 0; b < xk::DESC_BINS; ++b) {
     const double r = (b + 0.5) * h;
     for (int f = 0; f < 32; ++f) {
       const double mu = 0.5 + f * sp;
-      B[(size_t)b * 64 + f] = (float)exp(-(r - mu) * (r - mu) / (2 * sp * sp));
-    }
-    for (int s = 0; s < 32; ++s) {
-      const double k = 2 * M_PI * sqrt((double)sh[s]) / box[0], kr = k * r;
-      B[(size_t)b * 64 + 32 + s] = (float)(sin(kr) / kr);
+      B[(size_t)b * 32 + f] = (float)exp(-(r - mu) * (r - mu) / (2 * sp * sp));
     }
   }
+}
+
+// half-space wave vectors n (nx > 0; or nx = 0, ny > 0; or nx = ny = 0,
+// nz > 0) of the DESC_SHELLS lowest shells |n|^2, as (nx, ny, nz, shell),
+// and the number of vectors per shell
+static void shell_vectors(std::vector<int> &kv, std::vector<int> &count, int &nmax) {
+  const std::vector<int> sh = lowest_shells(xk::DESC_SHELLS);
+  const int top = sh.back();
+  nmax = (int)floor(sqrt((double)top));
+  count.assign(xk::DESC_SHELLS, 0);
+  kv.clear();
+  for (int a = 0; a <= nmax; ++a)
+    for (int b = -nmax; b <= nmax; ++b)
+      for (int c = -nmax; c <= nmax; ++c) {
+        if (!(a > 0 || (a == 0 && b > 0) || (a == 0 && b == 0 && c > 0))) continue;
+        const int n2 = a * a + b * b + c * c;
+        for (int s2 = 0; s2 < xk::DESC_SHELLS; ++s2)
+          if (sh[s2] == n2) {
+            kv.insert(kv.end(), {a, b, c, s2});
+            count[s2]++;
+          }
+      }
 }
 
 static int geometry_matches(Model *M, SimDev *sd) {
@@ -362,7 +379,7 @@ void md_gb300_ewald_model_free_x(md_gb300_ewald_model_t_x *M) {
   DevBuf *bufs[] = {&M->par,  &M->grad, &M->m1,   &M->m2,    &M->w1,      &M->w2,   &M->w3,   &M->w3f,  &M->lossacc,
                     &M->err,  &M->basis, &M->fmean, &M->fistd, &M->dsx,   &M->dsv,  &M->dst,  &M->lx,   &M->lv,
                     &M->ly,   &M->raw,  &M->fa,   &M->fb,    &M->ea,      &M->eb,   &M->fp,   &M->ep,   &M->jacc,
-                    &M->rc_coef, &M->rc_cols, &M->rc_phase, &M->rc_S, &M->rc_T};
+                    &M->rc_coef, &M->rc_cols, &M->rc_phase, &M->rc_S, &M->rc_T, &M->dkv, &M->dsn, &M->dsh};
   for (DevBuf *b : bufs) release(*b);
   if (M->ms) {
     cudaStreamSynchronize(M->ms);
@@ -419,7 +436,13 @@ int md_gb300_ewald_model_create_x(md_gb300_ewald_model_t_x **out, md_pimd_t_x *p
   res(M->w3f, 4 * 512);
   res(M->lossacc, 16);
   res(M->err, 16);
-  res(M->basis, 4 * xk::DESC_BINS * 64);
+  res(M->basis, 4 * xk::DESC_BINS * 32);
+  std::vector<int> kvh, kcount;
+  int kmax = 0;
+  shell_vectors(kvh, kcount, kmax);
+  res(M->dkv, sizeof(int) * kvh.size());
+  res(M->dsn, 4 * xk::DESC_SHELLS);
+  res(M->dsh, 4 * (size_t)xk::DESC_SHELLS * g.P);
   res(M->fmean, 4 * 64);
   res(M->fistd, 4 * 64);
   res(M->dsx, (size_t)capacity_cfg * (rows / xk::MLP_TILE) * tile_bytes);
@@ -459,7 +482,14 @@ int md_gb300_ewald_model_create_x(md_gb300_ewald_model_t_x **out, md_pimd_t_x *p
   // descriptors
   const double rcut = 0.5 * fmin(g.box[0], fmin(g.box[1], g.box[2]));
   std::vector<float> B;
-  make_basis(g.box, rcut, B);
+  make_basis(rcut, B);
+  std::vector<float> sn(xk::DESC_SHELLS);
+  for (int i = 0; i < xk::DESC_SHELLS; ++i) sn[i] = (float)(1.0 / ((double)g.N * kcount[i]));
+  M->dp.kvec = M->dkv.as<int4>();
+  M->dp.nkvec = (int)(kvh.size() / 4);
+  M->dp.nmax = kmax;
+  M->dp.shell_norm = M->dsn.as<float>();
+  M->dp.shell = M->dsh.as<float>();
   M->dp.rc = (float)rcut;
   M->dp.inv_h = (float)(xk::DESC_BINS / rcut);
   for (int d = 0; d < 3; ++d) {
@@ -486,6 +516,9 @@ int md_gb300_ewald_model_create_x(md_gb300_ewald_model_t_x **out, md_pimd_t_x *p
   fill(xk::MLP_W3, 128, 4, 4 * 128, 0.1);
   cudaStream_t st = stream();
   if ((e = cudaMemcpyAsync(M->basis.p, B.data(), B.size() * 4, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
+      (e = cudaMemcpyAsync(M->dkv.p, kvh.data(), kvh.size() * sizeof(int), cudaMemcpyHostToDevice, st)) !=
+          cudaSuccess ||
+      (e = cudaMemcpyAsync(M->dsn.p, sn.data(), sn.size() * 4, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
       (e = cudaMemcpyAsync(M->par.p, p.data(), p.size() * 4, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
       (e = xk::mlp_pack(M->par.as<float>(), M->w1.as<uint8_t>(), M->w2.as<uint8_t>(), M->w3.as<uint8_t>(),
                         M->w3f.as<float>(), st)) != cudaSuccess ||
@@ -718,7 +751,7 @@ int md_gb300_ewald_model_desc_info_x(md_gb300_ewald_model_t_x *M, double *rc, fl
     if (vsig) vsig[d] = M->vsig[d];
   }
   if (basis) {
-    XMD_CUDA(cudaMemcpy(basis, M->basis.p, 4 * xk::DESC_BINS * 64, cudaMemcpyDeviceToHost));
+    XMD_CUDA(cudaMemcpy(basis, M->basis.p, 4 * xk::DESC_BINS * 32, cudaMemcpyDeviceToHost));
   }
   return 0;
 }

@@ -474,7 +474,7 @@ class EwaldModel:
     def desc_info(self):
         import numpy as np
         rc = C.c_double()
-        B = np.zeros((128, 64), np.float32)
+        B = np.zeros((64, 32), np.float32)
         mu, sg = (C.c_double * 3)(), (C.c_double * 3)()
         self.lib.check(self.lib.md_gb300_ewald_model_desc_info_x(self.h, C.byref(rc), B.ctypes.data_as(_fp), mu, sg))
         return rc.value, B, list(mu), list(sg)

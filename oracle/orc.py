@@ -241,7 +241,7 @@ def mlp_grad(X, V, T, p, we=1.0, wf=1.0, inv_rows=None, bf=0):
     return g, loss
 
 
-def desc_features(x, box, rc, basis, vmu, vsig, nb=128):
+def desc_features(x, box, rc, basis, vmu, vsig, nb=64):
     """x: positions [N][3] of one bead slice"""
     x = np.ascontiguousarray(x, np.float64)
     N = x.shape[0]

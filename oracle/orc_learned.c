@@ -41,16 +41,39 @@ double orc_bf16(double v) {
 static double rnd(double v, int on) { return on ? orc_bf16(v) : v; }
 
 /*
- * Descriptors of particle l among N (positions AoS x[l*3 + d], box L[3]):
- * every minimum-image partner c != l with r < rc deposits fc(r) =
- * (1 - r^2/rc^2)^2 into a histogram of nb bins of width h = rc/nb by linear
- * weights between bin centres (b + 1/2) h: t = r/h - 1/2, b0 = floor(t),
- * w = t - b0; bin b0 gets fc (1 - w), bin b0 + 1 gets fc w; below the first
- * centre (b0 < 0) or from the last centre on (b0 >= nb - 1) all of fc goes
- * to the end bin.  Features F[f] = sum_b hist[b] basis[b][f] (64 features).
+ * Descriptors of the N particles of one bead slice (positions AoS
+ * x[l*3 + d], box L[3]), 64 per particle:
+ *
+ * F[0..31]: every minimum-image partner c != l with r < rc deposits
+ *   fc(r) = (1 - r^2/rc^2)^2 into a histogram of nb bins of width h = rc/nb
+ *   by linear weights between bin centres (b + 1/2) h: t = r/h - 1/2,
+ *   b0 = floor(t), w = t - b0; bin b0 gets fc (1 - w), bin b0 + 1 gets fc w;
+ *   below the first centre (b0 < 0) or from the last centre on
+ *   (b0 >= nb - 1) all of fc goes to the end bin.  F[f] = sum_b hist[b]
+ *   basis[b][f] (basis[nb][32]: Gaussians in r).
+ * F[32..63]: for the 32 lowest shells |n|^2 of the reciprocal lattice
+ *   (k = 2 pi n / L), sqrt(sum over the shell's half-space vectors of
+ *   |S(k)|^2 / (N count)), S(k) = sum_l exp(i k . x_l); the same for every
+ *   particle of the slice.
  * Vector features Vv[3m + d] = sum_c fc(r) exp(-(r - mu_m)^2 / (2 s_m^2))
- * (x_l - x_c)_d / r.
+ *   (x_l - x_c)_d / r.
  */
+#define ORC_SHELLS 32
+
+/* the ORC_SHELLS lowest positive sums of three squares */
+static void lowest_shells(int *sh) {
+  int n = 0;
+  for (int n2 = 1; n < ORC_SHELLS; ++n2) {
+    int ok = 0;
+    for (int a = 0; a * a <= n2 && !ok; ++a)
+      for (int b = 0; a * a + b * b <= n2 && !ok; ++b) {
+        const int c2 = n2 - a * a - b * b, c = (int)lround(sqrt((double)c2));
+        if (c * c == c2) ok = 1;
+      }
+    if (ok) sh[n++] = n2;
+  }
+}
+
 void orc_desc_features(int N, const double *x, const double *L, double rc, int nb, const double *basis,
                        const double *vmu, const double *vsig, double *F, double *Vv) {
   const double h = rc / nb;
@@ -86,11 +109,40 @@ void orc_desc_features(int N, const double *x, const double *L, double rc, int n
         for (int k = 0; k < 3; ++k) Vv[l * 9 + 3 * m + k] += q * d[k];
       }
     }
-    for (int f = 0; f < ORC_IN; ++f) {
+    for (int f = 0; f < 32; ++f) {
       double s = 0;
-      for (int b = 0; b < nb; ++b) s += hist[b] * basis[b * ORC_IN + f];
+      for (int b = 0; b < nb; ++b) s += hist[b] * basis[b * 32 + f];
       F[l * ORC_IN + f] = s;
     }
+  }
+  /* structure-factor shells */
+  int sh[ORC_SHELLS];
+  lowest_shells(sh);
+  const int nmax = (int)floor(sqrt((double)sh[ORC_SHELLS - 1]));
+  double acc[ORC_SHELLS];
+  int cnt[ORC_SHELLS];
+  for (int i = 0; i < ORC_SHELLS; ++i) acc[i] = 0, cnt[i] = 0;
+  for (int a = 0; a <= nmax; ++a)
+    for (int b = -nmax; b <= nmax; ++b)
+      for (int c = -nmax; c <= nmax; ++c) {
+        if (!(a > 0 || (a == 0 && b > 0) || (a == 0 && b == 0 && c > 0))) continue;
+        const int n2 = a * a + b * b + c * c;
+        int s2 = -1;
+        for (int i = 0; i < ORC_SHELLS; ++i)
+          if (sh[i] == n2) s2 = i;
+        if (s2 < 0) continue;
+        double sr = 0, si = 0;
+        for (int l = 0; l < N; ++l) {
+          const double ph = 2 * M_PI * (a * x[l * 3] / L[0] + b * x[l * 3 + 1] / L[1] + c * x[l * 3 + 2] / L[2]);
+          sr += cos(ph);
+          si += sin(ph);
+        }
+        acc[s2] += sr * sr + si * si;
+        cnt[s2] += 1;
+      }
+  for (int i = 0; i < ORC_SHELLS; ++i) {
+    const double v = sqrt(acc[i] / ((double)N * cnt[i]));
+    for (int l = 0; l < N; ++l) F[l * ORC_IN + 32 + i] = v;
   }
 }
 

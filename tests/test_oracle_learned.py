@@ -79,9 +79,9 @@ def test_rounded_gradient_close_to_exact():
 
 def test_two_particle_descriptor():
     box = np.array([10.0, 10.0, 10.0])
-    rc, nb = 5.0, 128
+    rc, nb = 5.0, 64
     rng = np.random.default_rng(4)
-    B = rng.standard_normal((nb, 64))
+    B = rng.standard_normal((nb, 32))
     mu, sg = [1.25, 2.5, 3.75], [0.75, 0.75, 0.75]
     r = 2.3456
     x = np.array([[1.0, 1.0, 1.0], [1.0 + r, 1.0, 1.0]])
@@ -92,17 +92,32 @@ def test_two_particle_descriptor():
     w = t - b0
     fc = (1 - r * r / (rc * rc)) ** 2
     expect = fc * ((1 - w) * B[b0] + w * B[b0 + 1])
-    np.testing.assert_allclose(F[0], expect, rtol=1e-12, atol=1e-14)
-    np.testing.assert_allclose(F[1], expect, rtol=1e-12, atol=1e-14)
+    np.testing.assert_allclose(F[0, :32], expect, rtol=1e-12, atol=1e-14)
+    np.testing.assert_allclose(F[1, :32], expect, rtol=1e-12, atol=1e-14)
     q = [fc * math.exp(-(r - m) ** 2 / (2 * s * s)) / r for m, s in zip(mu, sg)]
     for m in range(3):
         assert math.isclose(Vv[0, 3 * m], -q[m] * r, rel_tol=1e-12)
         assert math.isclose(Vv[1, 3 * m], q[m] * r, rel_tol=1e-12)
+    # structure-factor shells: |S(k)|^2 = 2 + 2 cos(k . d) for two particles,
+    # averaged over each shell's half-space vectors, divided by N = 2
+    shells = [1, 2, 3, 4, 5, 6, 8, 9, 10, 11, 12, 13, 14, 16, 17, 18, 19, 20, 21, 22, 24, 25, 26, 27, 29, 30,
+              32, 33, 34, 35, 36, 37]
+    for i, n2 in enumerate(shells):
+        vals = []
+        for a in range(0, 7):
+            for b in range(-6, 7):
+                for c in range(-6, 7):
+                    if not (a > 0 or (a == 0 and b > 0) or (a == 0 and b == 0 and c > 0)):
+                        continue
+                    if a * a + b * b + c * c == n2:
+                        vals.append(2 + 2 * math.cos(2 * math.pi * a * r / box[0]))
+        assert math.isclose(F[0, 32 + i], math.sqrt(np.mean(vals) / 2), rel_tol=1e-12)
+        assert F[1, 32 + i] == F[0, 32 + i]
     # minimum image: the same pair across the boundary
     x2 = np.array([[0.5, 1.0, 1.0], [0.5 - r + 10.0, 1.0, 1.0]])
     F2, _ = orc.desc_features(x2, box, rc, B, mu, sg, nb)
-    np.testing.assert_allclose(F2[0], expect, rtol=1e-10, atol=1e-12)
+    np.testing.assert_allclose(F2[0], F[0], rtol=1e-10, atol=1e-12)
     # beyond the cut-off nothing is deposited
     x3 = np.array([[1.0, 1.0, 1.0], [1.0, 1.0 + 5.2, 1.0]])
     F3, V3 = orc.desc_features(x3, 2 * box, rc, B, mu, sg, nb)
-    assert not F3.any() and not V3.any()
+    assert not F3[:, :32].any() and not V3.any()
