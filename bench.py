@@ -204,9 +204,9 @@ def cpu_step_estimate(cores, budget_s):
 # ---------------------------------------------------------------------
 # GB300 arm
 # ---------------------------------------------------------------------
-def n_images(xcut=5.8):
+def n_images(xcut=5.2):
     """expected real-space images per pair inside the cut-off alpha R < xcut
-    (5.8 in the FP64 kernels, 3.6 in the FP32 ones)"""
+    (5.2 in the FP64 force kernels, 3.6 in the FP32 ones)"""
     box, _ = workload()
     rc = xcut / (ALPHA_L / box)
     return 4 / 3 * math.pi * rc ** 3 / box ** 3
@@ -293,10 +293,10 @@ def measured_peaks():
         return {}
 
 
-def make_system(lib):
+def make_system(lib, xi=XI):
     import xmd_x
     box, T = workload()
-    s = xmd_x.PimdSystem(lib, N, P, XI, T, box=box)
+    s = xmd_x.PimdSystem(lib, N, P, xi, T, box=box)
     lib.md_set_seed_x(2024)
     lib.md_init_particle_mass_x(s.sim, 1.0, 0, N * P)
     c = (C.c_double * 3)(box / 2, box / 2, box / 2)
@@ -394,6 +394,13 @@ def roofline(prof, peak, peak_name, unit_nsum=NSUM):
     return roof
 
 
+def judge_fails(j, args):
+    """the network is dropped when, on the judged configuration, its force
+    error exceeds the truncated sum's own (it would do harm) or its energy
+    error per particle exceeds the energy tolerance"""
+    return j["force_err"] > args.force_tol * j["force_err_truncated"] or j["energy_err"] > args.energy_tol
+
+
 def learned_form(lib, R, s, pair, step, args, ws):
     """Truncated Ewald (|n| <= NSUM_CHEAP) + the residual network, FP32 forces.
     Data from plain runs of this system (converged Ewald, mixed forces),
@@ -432,7 +439,7 @@ def learned_form(lib, R, s, pair, step, args, ws):
             return
         j = m.judge(s)
         judges.append(j)
-        if j["force_err"] > args.force_tol or j["energy_err"] > args.energy_tol:
+        if judge_fails(j, args):
             state["reverted"] = True
 
     def learned_step():
@@ -461,7 +468,8 @@ def learned_form(lib, R, s, pair, step, args, ws):
             "delta_E_per_particle_truncated_only_Ha": max(j["energy_err_truncated"] for j in all_j),
             "force_err_rms_rel": max(j["force_err"] for j in all_j),
             "force_err_rms_rel_truncated_only": max(j["force_err_truncated"] for j in all_j),
-            "tolerances": {"force": args.force_tol, "energy_per_particle_Ha": args.energy_tol},
+            "tolerances": {"force": f"{args.force_tol} x the truncated sum's force error on the same configuration",
+                           "energy_per_particle_Ha": args.energy_tol},
             "kernel_ms_per_step": {k: v[0] for k, v in prof.items()}}
     return m, form, prof, kps
 
@@ -708,11 +716,34 @@ def run_gb300(args, dist, rank, ws):
                                       "kernels_per_step": mixed_kps, "force_error_vs_fp64": ferr,
                                       "clocks": mixed_clocks,
                                       "kernel_ms_per_step": {k: v[0] for k, v in mixed_prof.items()}}
+    if "truncated" in want:
+        # FP32 forces with the reciprocal sum truncated to |n| <= NSUM_CHEAP
+        # and no network: what the learned form adds its residual to
+        lib.check(lib.md_gb300_set_precision_x(1))
+        xmd_x.set_potentials(lib, coul_s=1.0, alpha=ALPHA_L / workload()[0], nsum=NSUM_CHEAP)
+        tr_ms, tr_kps, _, tr_clocks = graph_form()
+        forms["truncated_fp32"] = {"value": ws * N * P / (tr_ms * 1e-3), "ms_per_step": tr_ms,
+                                   "kernels_per_step": tr_kps, "clocks": tr_clocks, "nsum": NSUM_CHEAP}
+        xmd_x.set_potentials(lib, coul_s=1.0, alpha=ALPHA_L / workload()[0], nsum=NSUM)
+        lib.check(lib.md_gb300_set_precision_x(0))
     if "ensemble" in want:
         forms["ensemble_64"] = ensemble_form(lib, R, args)
     headline = next((k for k in ("plain_fp64", "mixed_fp32_forces", "two_species_fp64", "ensemble_64")
                      if k in forms), None)
     model = None
+    if "learned_xi1" in want:
+        # the same workload at xi = 1 (bosons): its own system, data and network
+        s1 = make_system(lib, xi=1.0)
+        step1 = lambda: xmd_x.md_step(lib, s1, DT, image=1, pair=pair, pbc=True)  # noqa: E731
+        for _ in range(args.warmup):
+            step1()
+        m1, f1, p1, _ = learned_form(lib, R, s1, pair, step1, args, ws)
+        f1["roofline"] = roofline(p1, fp32_peak, "fp32")
+        f1["xi"] = 1.0
+        forms["learned_fp32_xi1"] = f1
+        m1.free()
+        s1.free()
+        lib.check(lib.md_gb300_set_precision_x(0))
     if "learned" in want:
         model, lform, lprof, lkps = learned_form(lib, R, s, pair, step, args, ws)
         lform["roofline"] = roofline(lprof, fp32_peak, "fp32")
@@ -749,8 +780,7 @@ def run_gb300(args, dist, rank, ws):
         wrap()  # uploads the host state (positions are already inside the box)
         lib.check(lib.md_gb300_graph_launch_x(g_conv if dropped else g_main, 1))
         if g_conv is not None and not dropped and i % JUDGE_EVERY == 0:
-            j = model.judge(s)
-            dropped = j["force_err"] > args.force_tol or j["energy_err"] > args.energy_tol
+            dropped = judge_fails(model.judge(s), args)
         lib.check(lib.md_pimd_calc_VBN_energy_x(s.pimd, s.stats))
         s.take_energy()  # estimator read
     if not lib.md_simulation_sync_host_x(s.sim, 1):
@@ -834,14 +864,17 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--cpu-budget", type=float, default=8.0, help="seconds of CPU sample")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--forms", default="plain,two,recursion,mixed,ensemble,learned",
-                    help="forms to run (comma list of plain, two, recursion, mixed, ensemble, learned)")
+    ap.add_argument("--forms", default="plain,two,recursion,mixed,truncated,ensemble,learned_xi1,learned",
+                    help="forms to run (comma list of plain, two, recursion, mixed, truncated, ensemble, "
+                         "learned_xi1, learned)")
     ap.add_argument("--learn-configs", type=int, default=3125,
                     help="configurations collected for training (x P bead slices)")
     ap.add_argument("--learn-steps", type=int, default=3000)
     ap.add_argument("--learn-batch", type=int, default=128, help="tiles of 128 rows per Adam step")
     ap.add_argument("--learn-lr", type=float, default=1e-3)
-    ap.add_argument("--force-tol", type=float, default=0.05)
+    ap.add_argument("--force-tol", type=float, default=1.0,
+                    help="the judge drops the network when its force error exceeds this multiple of the "
+                         "truncated sum's on the same configuration")
     ap.add_argument("--energy-tol", type=float, default=1e-4)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)

@@ -1,0 +1,50 @@
+"""The mixed, truncated and learned forms of the electron-gas step against
+the FP64 form (md-lab_gb300/xmd_forms.py), at the benchmark's system (512
+electrons, 64 beads, rs = 1, theta = 0.5, xi = 0.5) on short runs:
+
+  * on the same configurations: the mixed form's forces within 5e-5 of the
+    largest FP64 force, the learned form's pair energy within 1e-4 Ha per
+    particle and closer to FP64 than the truncated sum's, and the
+    primitive estimator (positions only) the same in every form;
+  * on each form's own trajectory: the block-averaged primitive and virial
+    total-energy estimators and the pair energy within 4 combined standard
+    errors of the FP64 run's; the learned run's judgements all within
+    1e-4 Ha per particle.
+
+The committed long runs (10^4 steps per form, xi = 0.5 and 1.0) are made by
+the same module's command line."""
+import pytest
+
+import xmd_forms
+import xmd_x
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def result():
+    lib = xmd_x.load(3, 4)
+    return xmd_forms.validate(lib, xi=0.5, steps=1500, every=10, blocks=10, equil=300, compare_steps=100,
+                              compare_every=25, configs=300, adam_steps=1500, sigmas=4.0)
+
+
+def test_same_configuration_errors(result):
+    same = result["same_configuration"]
+    print({f: {k: v["max"] for k, v in e.items()} for f, e in same.items()})
+    assert same["mixed"]["force_max"]["max"] <= 5e-5
+    assert same["learned"]["pair_energy_per_particle"]["max"] <= 1e-4
+    assert (same["learned"]["pair_energy_per_particle"]["mean"]
+            < same["truncated"]["pair_energy_per_particle"]["mean"])
+    for f in ("mixed", "truncated", "learned"):
+        assert same[f]["primitive_estimator_rel"]["max"] <= 1e-12
+
+
+def test_estimators_within_statistical_error(result):
+    traj = result["trajectories"]
+    for f in ("mixed", "truncated", "learned", "fp64_replica"):
+        for k, a in traj[f]["vs_fp64"].items():
+            print(f, k, a, traj[f]["estimators"][k], traj["fp64"]["estimators"][k])
+            assert a["within"], (f, k, a)
+    lj = traj["learned"]
+    assert lj["judged"] >= 1
+    assert lj["judgements"]["energy_err"]["max"] <= 1e-4
