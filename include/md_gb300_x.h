@@ -203,7 +203,10 @@ int md_gb300_ewald_model_attach_x(md_pimd_t_x *pimd, md_gb300_ewald_model_t_x *m
                                   double force_tol, double energy_tol);
 /* errors on pimd's current configuration: out[0] force error and out[1]
    energy error per particle (Ha) of truncated sum + network, out[2], out[3]
-   the same for the truncated sum alone */
+   the same for the truncated sum alone.  A judgement (this call, or the
+   attached model's own cadence) evaluates eight consecutive bead slices
+   (all of them when P <= 8), the next eight at the next judgement, so that
+   every slice is judged in turn at an eighth of the cost of all 64. */
 int md_gb300_ewald_model_judge_x(md_gb300_ewald_model_t_x *model, md_pimd_t_x *pimd, double out[4]);
 int md_gb300_ewald_model_status_x(md_gb300_ewald_model_t_x *model, long *configurations, int *judged,
                                   int *reverted, double last[4]);

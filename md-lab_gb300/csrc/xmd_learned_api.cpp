@@ -164,24 +164,28 @@ static int zero(DevBuf &b) {
 }
 
 // converged and truncated reciprocal forces (raw, FP64) and per-particle
-// energies of the current configuration into fa/ea and fb/eb
-static int both_sums(Model *M, md_pimd_t_x *pimd, SimDev *sd, PimdDev *pd) {
+// energies of the bead slices g covers (x: the first of them) into fa/ea
+// and fb/eb
+static int both_sums(Model *M, md_pimd_t_x *pimd, SimDev *sd, PimdDev *pd, const xk::Geo &g, const double *x) {
   XMD_TRY(ewald_tables(pimd, sd, pd));
   XMD_TRY(zero(M->fa));
   XMD_TRY(zero(M->fb));
-  const double *x = sd->x.as<double>();
-  XMD_CUDA(xk::recip_force_energy(sd->geo, recip_of(pd), x, 1.0, M->fa.as<double>(), M->ea.as<double>(), stream()));
-  XMD_CUDA(xk::recip_force_energy(sd->geo, M->cheap, x, 1.0, M->fb.as<double>(), M->eb.as<double>(), stream()));
+  XMD_CUDA(xk::recip_force_energy(g, recip_of(pd), x, 1.0, M->fa.as<double>(), M->ea.as<double>(), stream()));
+  XMD_CUDA(xk::recip_force_energy(g, M->cheap, x, 1.0, M->fb.as<double>(), M->eb.as<double>(), stream()));
   return 0;
 }
+static int both_sums(Model *M, md_pimd_t_x *pimd, SimDev *sd, PimdDev *pd) {
+  return both_sums(M, pimd, sd, pd, sd->geo, sd->x.as<double>());
+}
 
-// descriptors and network output of the current configuration (live buffers)
-static int predict(Model *M, SimDev *sd, cudaStream_t st) {
-  XMD_CUDA(xk::desc_build(sd->geo, M->dp, sd->x.as<double>(), M->lx.as<uint8_t>(), M->lv.as<float>(), nullptr, st));
-  XMD_CUDA(xk::mlp_forward(dev_view(M), M->lx.as<uint8_t>(), tiles_of(M->N * M->P), M->ly.as<float4>(),
+// descriptors and network output of the bead slices g covers (live buffers)
+static int predict(Model *M, const xk::Geo &g, const double *x, cudaStream_t st) {
+  XMD_CUDA(xk::desc_build(g, M->dp, x, M->lx.as<uint8_t>(), M->lv.as<float>(), nullptr, st));
+  XMD_CUDA(xk::mlp_forward(dev_view(M), M->lx.as<uint8_t>(), tiles_of(g.N * g.P), M->ly.as<float4>(),
                            M->err.as<int>(), st));
   return 0;
 }
+static int predict(Model *M, SimDev *sd, cudaStream_t st) { return predict(M, sd->geo, sd->x.as<double>(), st); }
 
 // normalisation of inputs and outputs from the first configuration
 static int normalise(Model *M, SimDev *sd) {
@@ -239,29 +243,41 @@ static int normalise(Model *M, SimDev *sd) {
   return 0;
 }
 
+// A judgement evaluates the converged and truncated FP64 reciprocal sums and
+// the network on JUDGE_SLICES consecutive bead slices, a different block each
+// time (every slice is judged in turn): the errors are averages over
+// N x JUDGE_SLICES particle-slices, at a fraction of the cost of all of them.
+constexpr int JUDGE_SLICES = 8;
+
 static int judge_now(Model *M, md_pimd_t_x *pimd, SimDev *sd, PimdDev *pd, double out[4]) {
   if (!M->normalized) return fail(MD_GB_ERR_ARG, "the model has no data yet");
   if (capturing()) return fail(MD_GB_ERR_CAPTURE, "judging reads results back; not while capturing");
   cudaStream_t st = stream();
-  XMD_TRY(both_sums(M, pimd, sd, pd));
-  XMD_TRY(predict(M, sd, stream()));
-  XMD_CUDA(xk::resid_apply(sd->geo, M->rp, M->ly.as<float4>(), M->lv.as<float>(), 1.0, nullptr, M->fp.as<double>(),
+  xk::Geo g = sd->geo;
+  const int pj = M->P < JUDGE_SLICES ? M->P : JUDGE_SLICES;
+  int j0 = (int)(((long)M->judged * pj) % M->P);
+  if (j0 + pj > M->P) j0 = M->P - pj;
+  g.P = pj;
+  const double *x = sd->x.as<double>() + (size_t)j0 * 3 * g.Ns;
+  XMD_TRY(both_sums(M, pimd, sd, pd, g, x));
+  XMD_TRY(predict(M, g, x, stream()));
+  XMD_CUDA(xk::resid_apply(g, M->rp, M->ly.as<float4>(), M->lv.as<float>(), 1.0, nullptr, M->fp.as<double>(),
                            M->ep.as<double>(), st));
   XMD_TRY(zero(M->jacc));
-  XMD_CUDA(xk::resid_judge(sd->geo, M->fp.as<double>(), M->fa.as<double>(), M->fb.as<double>(), M->ep.as<double>(),
+  XMD_CUDA(xk::resid_judge(g, M->fp.as<double>(), M->fa.as<double>(), M->fb.as<double>(), M->ep.as<double>(),
                            M->ea.as<double>(), M->eb.as<double>(), M->jacc.as<double>(), st));
-  std::vector<double> acc(3 + 2 * (size_t)M->P);
+  std::vector<double> acc(3 + 2 * (size_t)pj);
   int kerr = 0;
   XMD_CUDA(cudaMemcpyAsync(acc.data(), M->jacc.p, acc.size() * 8, cudaMemcpyDeviceToHost, st));
   XMD_CUDA(cudaMemcpyAsync(&kerr, M->err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
   XMD_CUDA(cudaStreamSynchronize(st));
   if (kerr) return fail(MD_GB_ERR_CUDA, "tensor-core kernel reported error %d (wait timed out)", kerr);
   double em = 0, et = 0;
-  for (int j = 0; j < M->P; ++j) {
+  for (int j = 0; j < pj; ++j) {
     em += acc[3 + j];
-    et += acc[3 + M->P + j];
+    et += acc[3 + pj + j];
   }
-  const double norm = acc[1] > 0 ? acc[1] : 1.0, np = (double)M->N * M->P;
+  const double norm = acc[1] > 0 ? acc[1] : 1.0, np = (double)M->N * pj;
   out[0] = sqrt(acc[0] / norm);
   out[1] = fabs(em) / np;
   out[2] = sqrt(acc[2] / norm);
