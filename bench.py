@@ -689,13 +689,19 @@ def run_gb300(args, dist, rank, ws):
     want = set(args.forms.split(","))
     forms = {}
     if "plain" in want:
-        # plain FP64: the form that reproduces MD-Lab to 1e-10
+        # plain FP64: the form that reproduces MD-Lab to 1e-10, with launch
+        # shapes chosen by the FP64 autotuner for this system
         lib.check(lib.md_gb300_set_precision_x(0))
+        bps, lay, tms = C.c_int(), C.c_int(), C.c_double()
+        lib.check(lib.md_gb300_autotune_fp64_x(s.pimd, pair, 3, C.byref(bps), C.byref(lay), C.byref(tms)),
+                  "FP64 autotuning")
+        step()
         plain_ms, plain_kps, plain_wall, plain_clocks = graph_form()
         plain_prof = R.profile(step)
         fp64_peak = lib.md_gb300_fp64_peak_x()
         forms["plain_fp64"] = {"value": ws * N * P / (plain_ms * 1e-3), "ms_per_step": plain_ms,
                                "kernels_per_step": plain_kps, "clocks": plain_clocks,
+                               "autotuned": {"tile_blocks_per_sm": bps.value, "sk_layout": lay.value},
                                "kernel_ms_per_step": {k: v[0] for k, v in plain_prof.items()},
                                "roofline": roofline(plain_prof, fp64_peak, "fp64")}
     fp32_peak = lib.md_gb300_fp32_peak_x()

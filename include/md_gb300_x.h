@@ -137,6 +137,16 @@ int md_gb300_pair_force_noalloc_x(md_pair_force_t_x pf, const double *x, const d
 int md_gb300_autotune_pair_x(md_pimd_t_x *pimd, md_pair_force_t_x pf, int repeats, int *warps, double *ms);
 /* set that choice directly (a tuning table kept by the caller) */
 int md_gb300_set_pair_tile_x(md_pair_force_t_x pf, int N, int P, int warps);
+/* The FP64 form's launch shapes for pimd's system shape, chosen by timing:
+   the tile kernels' thread blocks per SM (1 or 2, *blocks_per_sm) and, for
+   md_coulomb_3d_ewald_force_x, the structure-factor kernel's layout
+   (*sk_layout: 1 = 16 columns x 16 particle groups per block, 2 = 8 x 32,
+   3 = 64 columns, one thread each; 0 for the other potentials).  The choices
+   are kept for this potential kind, N, P (and n_sum) and used by the FP64
+   force calls; the forces agree to rounding whatever the choice.  *ms: the
+   time of one force call's tiles plus reciprocal sum with the choices. */
+int md_gb300_autotune_fp64_x(md_pimd_t_x *pimd, md_pair_force_t_x pf, int repeats, int *blocks_per_sm,
+                             int *sk_layout, double *ms);
 
 /* Which kernel solves the exchange recursions (V_B and the backward tmpV,
    md_pimd_fill_VB_x and the force call): MD_GB_SOLVE_BLOCK runs one thread

@@ -2761,11 +2761,37 @@ static int resident_grid(K kernel, size_t warps_needed, int &occ, int &sms, size
   return (int)(need < full ? need : full);
 }
 
+// choices of the FP64 autotuner per system shape (what, kind, D, N, P)
+static std::mutex g_tune64_mu;
+static std::vector<std::pair<std::array<int, 5>, int>> g_tune64;
+
+void set_tuning(int what, int kind, int D, int N, int P, int v) {
+  std::lock_guard<std::mutex> lk(g_tune64_mu);
+  for (auto &e : g_tune64)
+    if (e.first == std::array<int, 5>{what, kind, D, N, P}) {
+      e.second = v;
+      return;
+    }
+  g_tune64.push_back({{what, kind, D, N, P}, v});
+}
+
+int tuning(int what, int kind, int D, int N, int P) {
+  std::lock_guard<std::mutex> lk(g_tune64_mu);
+  for (auto &e : g_tune64)
+    if (e.first == std::array<int, 5>{what, kind, D, N, P}) return e.second;
+  return 0;
+}
+
+// the FP64 tile kernels' persistent grid: blocks per SM as tuned for this
+// shape (TUNE_PAIR64_BPS), else as many as stay resident
 template <int D, int KIND, bool ENERGY>
-static int pair_grid(size_t warps_needed) {
+static int pair_grid(size_t warps_needed, const Geo &g) {
   static int occ = 0, sms = 0;
-  return resident_grid(k_pair_tiles<D, KIND, ENERGY>, warps_needed, occ, sms,
-                       KIND == PAIR_EWALD_REAL ? EW_TAB_BYTES : 0);
+  const int full = resident_grid(k_pair_tiles<D, KIND, ENERGY>, warps_needed, occ, sms,
+                                 KIND == PAIR_EWALD_REAL ? EW_TAB_BYTES : 0);
+  const int bps = tuning(TUNE_PAIR64_BPS, KIND, D, g.N, g.P);
+  if (bps > 0 && bps < occ) return full < sms * bps ? full : sms * bps;
+  return full;
 }
 
 template <int D, bool ENERGY>
@@ -2776,32 +2802,32 @@ static cudaError_t pair_launch(const Geo &g, const PairPrm &p, const double *x, 
     case PAIR_GAUSSIAN:
       {
         XK_PROF("pair_tiles_gauss");
-        k_pair_tiles<D, PAIR_GAUSSIAN, ENERGY><<<pair_grid<D, PAIR_GAUSSIAN, ENERGY>(warps), 256, 0, st>>>(g, p, x, m, out, T, jobs);
+        k_pair_tiles<D, PAIR_GAUSSIAN, ENERGY><<<pair_grid<D, PAIR_GAUSSIAN, ENERGY>(warps, g), 256, 0, st>>>(g, p, x, m, out, T, jobs);
       }
       break;
     case PAIR_PERIODIC_GAUSSIAN:
       {
         XK_PROF("pair_tiles_pgauss");
-        k_pair_tiles<D, PAIR_PERIODIC_GAUSSIAN, ENERGY><<<pair_grid<D, PAIR_PERIODIC_GAUSSIAN, ENERGY>(warps), 256, 0, st>>>(g, p, x, m, out, T, jobs);
+        k_pair_tiles<D, PAIR_PERIODIC_GAUSSIAN, ENERGY><<<pair_grid<D, PAIR_PERIODIC_GAUSSIAN, ENERGY>(warps, g), 256, 0, st>>>(g, p, x, m, out, T, jobs);
       }
       break;
     case PAIR_COULOMB:
       {
         XK_PROF("pair_tiles_coul");
-        k_pair_tiles<D, PAIR_COULOMB, ENERGY><<<pair_grid<D, PAIR_COULOMB, ENERGY>(warps), 256, 0, st>>>(g, p, x, m, out, T, jobs);
+        k_pair_tiles<D, PAIR_COULOMB, ENERGY><<<pair_grid<D, PAIR_COULOMB, ENERGY>(warps, g), 256, 0, st>>>(g, p, x, m, out, T, jobs);
       }
       break;
     case PAIR_PERIODIC_COULOMB:
       {
         XK_PROF("pair_tiles_pcoul");
-        k_pair_tiles<D, PAIR_PERIODIC_COULOMB, ENERGY><<<pair_grid<D, PAIR_PERIODIC_COULOMB, ENERGY>(warps), 256, 0, st>>>(g, p, x, m, out, T, jobs);
+        k_pair_tiles<D, PAIR_PERIODIC_COULOMB, ENERGY><<<pair_grid<D, PAIR_PERIODIC_COULOMB, ENERGY>(warps, g), 256, 0, st>>>(g, p, x, m, out, T, jobs);
       }
       break;
     case PAIR_EWALD_REAL:
       if (D != 3) return cudaErrorInvalidValue;
       {
         XK_PROF("pair_tiles_ewald_real");
-        k_pair_tiles<D, PAIR_EWALD_REAL, ENERGY><<<pair_grid<D, PAIR_EWALD_REAL, ENERGY>(warps), 256, EW_TAB_BYTES, st>>>(g, p, x, m, out, T, jobs);
+        k_pair_tiles<D, PAIR_EWALD_REAL, ENERGY><<<pair_grid<D, PAIR_EWALD_REAL, ENERGY>(warps, g), 256, EW_TAB_BYTES, st>>>(g, p, x, m, out, T, jobs);
       }
       break;
     default:
@@ -3281,13 +3307,16 @@ static cudaError_t structure_factors(const Geo &g, const Recip &r, const double 
   const int nc = r.ncol;
   {
     XK_PROF("sk");
-    if (g.N >= SK_BIG_N && (size_t)((nc + 15) / 16) * g.P < 2 * 152) {
+    int lay = tuning(TUNE_SK_LAYOUT, r.nsum, 3, g.N, g.P);
+    if (lay == 0)
+      lay = g.N < SK_BIG_N ? SK_64x1 : ((size_t)((nc + 15) / 16) * g.P < 2 * 152 ? SK_8x32 : SK_16x16);
+    if (lay == SK_8x32) {
       // few slices (a judgement's): 8 columns of 32 lanes per block, twice
       // the blocks, each with half the work
       dim3 grid((nc + 7) / 8, g.P);
       DISPATCH_NS(r.nsum, (k_sk<NS, 8, 32><<<grid, 256, 0, st>>>(g, (const double2 *)r.phase,
                                                                  (const int4 *)r.kvec, nc, (double2 *)r.S, r.nk)));
-    } else if (g.N >= SK_BIG_N) {
+    } else if (lay == SK_16x16) {
       dim3 grid((nc + 15) / 16, g.P);
       DISPATCH_NS(r.nsum, (k_sk<NS, 16, 16><<<grid, 256, 0, st>>>(g, (const double2 *)r.phase,
                                                                   (const int4 *)r.kvec, nc, (double2 *)r.S, r.nk)));

@@ -178,6 +178,14 @@ struct PairPrm {
 size_t pair_scratch_doubles(const Geo &g);
 cudaError_t pair_force(const Geo &g, const PairPrm &p, const double *x, const double *m,
                        double *f, double *scratch, cudaStream_t st);
+// choices of the FP64 autotuner, per (what, kind, D, N, P); tuning() is 0
+// where none was recorded (the built-in rule applies).  TUNE_PAIR64_BPS: the
+// FP64 tile kernels' blocks per SM (kind = PairKind).  TUNE_SK_LAYOUT: the
+// structure-factor kernel's layout (kind = n_sum, D = 3).
+enum { TUNE_PAIR64_BPS = 0, TUNE_SK_LAYOUT = 1 };
+enum { SK_16x16 = 1, SK_8x32 = 2, SK_64x1 = 3 };
+void set_tuning(int what, int kind, int D, int N, int P, int v);
+int tuning(int what, int kind, int D, int N, int P);
 cudaError_t pair_energy(const Geo &g, const PairPrm &p, const double *x, double *acc,
                         double *scratch, cudaStream_t st);
 

@@ -635,6 +635,92 @@ int md_gb300_autotune_pair_x(md_pimd_t_x *pimd, md_pair_force_t_x pf, int repeat
   return 0;
 }
 
+// FP64 autotuner (md_gb300_x.h): the tile kernels' blocks per SM and, for
+// Ewald, the structure-factor layout, each timed on this system's positions
+// into a scratch force array; the choices are recorded for this shape.
+int md_gb300_autotune_fp64_x(md_pimd_t_x *pimd, md_pair_force_t_x pf, int repeats, int *blocks_per_sm,
+                             int *sk_layout, double *ms) {
+  const int kind = pair_kind_of((const void *)pf, false);
+  if (!kind) return fail(MD_GB_ERR_UNSUPPORTED, "pair force function has no device kernel");
+  if (repeats < 1) return fail(MD_GB_ERR_ARG, "repeats must be positive");
+  if (capturing()) return fail(MD_GB_ERR_CAPTURE, "autotuning times kernels; not while capturing");
+  SimDev *sd;
+  PimdDev *pd;
+  XMD_TRY(pimd_device(pimd, &sd, &pd));
+  const bool ewald = kind == xk::PAIR_EWALD_REAL;
+  if (ewald && D != 3) return fail(MD_GB_ERR_UNSUPPORTED, "Ewald is 3D only");
+  if (ewald && !sd->uniform_mass) return fail(MD_GB_ERR_UNSUPPORTED, "structure-factor Ewald needs equal bead masses");
+  int rc;
+  double *scr = scratch_for(sd, general_scratch(sd->geo), &rc);
+  if (rc) return rc;
+  xk::PairPrm prm = pair_params(kind);
+  ewald_shifts(prm, sd->geo);
+  if (ewald) {
+    if (prm.kmax[0] > 1 || prm.kmax[1] > 1 || prm.kmax[2] > 1)
+      return fail(MD_GB_ERR_UNSUPPORTED, "Ewald alpha*L below %.1f (images beyond the neighbouring boxes)",
+                  2 * EWALD_XCUT / 3);
+    prm.rcut = EWALD_XCUT_FORCE / prm.alpha;
+    XMD_TRY(ewald_tables(pimd, sd, pd));
+  }
+  const xk::Geo &g = sd->geo;
+  DevBuf ftmp;
+  XMD_TRY(reserve(ftmp, g.slots() * sizeof(double)));
+  cudaStream_t st = stream();
+  cudaEvent_t a = nullptr, b = nullptr;
+  cudaError_t e = cudaEventCreate(&a);
+  if (e == cudaSuccess) e = cudaEventCreate(&b);
+  // mean time of one call of fn after one untimed call
+  auto timeit = [&](auto fn, double &out) {
+    if (e == cudaSuccess) e = fn();
+    if (e == cudaSuccess) e = cudaEventRecord(a, st);
+    for (int r = 0; r < repeats && e == cudaSuccess; ++r) e = fn();
+    if (e == cudaSuccess) e = cudaEventRecord(b, st);
+    if (e == cudaSuccess) e = cudaEventSynchronize(b);
+    float t = 0;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&t, a, b);
+    out = t / repeats;
+  };
+  auto tiles = [&]() { return xk::pair_force(g, prm, sd->x.as<double>(), sd->m.as<double>(), ftmp.as<double>(), scr, st); };
+  int best_bps = 0;
+  double best_t = INFINITY, best_r = 0;
+  for (int bps = 1; bps <= 2 && e == cudaSuccess; ++bps) {
+    xk::set_tuning(xk::TUNE_PAIR64_BPS, kind, D, g.N, g.P, bps);
+    double t = 0;
+    timeit(tiles, t);
+    if (e == cudaSuccess && t < best_t) {
+      best_t = t;
+      best_bps = bps;
+    }
+  }
+  if (best_bps) xk::set_tuning(xk::TUNE_PAIR64_BPS, kind, D, g.N, g.P, best_bps);
+  int best_lay = 0;
+  if (ewald && e == cudaSuccess) {
+    const double inv_mP = 1.0 / (sd->mass0 * pimd->P);
+    auto recip = [&]() { return xk::recip_force(g, recip_of(pd), sd->x.as<double>(), inv_mP, ftmp.as<double>(), st); };
+    best_r = INFINITY;
+    const int lays[3] = {xk::SK_16x16, xk::SK_8x32, xk::SK_64x1};
+    for (int i = 0; i < 3 && e == cudaSuccess; ++i) {
+      xk::set_tuning(xk::TUNE_SK_LAYOUT, md_coulomb_n_sum_x, 3, g.N, g.P, lays[i]);
+      double t = 0;
+      timeit(recip, t);
+      if (e == cudaSuccess && t < best_r) {
+        best_r = t;
+        best_lay = lays[i];
+      }
+    }
+    if (best_lay) xk::set_tuning(xk::TUNE_SK_LAYOUT, md_coulomb_n_sum_x, 3, g.N, g.P, best_lay);
+  }
+  if (a) cudaEventDestroy(a);
+  if (b) cudaEventDestroy(b);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  release(ftmp);
+  if (e != cudaSuccess) return cuda_fail(e, "FP64 autotuning");
+  if (blocks_per_sm) *blocks_per_sm = best_bps;
+  if (sk_layout) *sk_layout = best_lay;
+  if (ms) *ms = best_t + best_r;
+  return 0;
+}
+
 int md_gb300_set_precision_x(int mode) {
   if (mode != MD_GB_PRECISION_FP64 && mode != MD_GB_PRECISION_MIXED)
     return fail(MD_GB_ERR_ARG, "unknown precision mode %d", mode);

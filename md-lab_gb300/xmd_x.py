@@ -175,6 +175,7 @@ class XLib:
                 "md_gb300_autotune_pair_x": (_i, [pp, _vp, _i, C.POINTER(_i), _dp]),
                 "md_gb300_set_pair_tile_x": (_i, [_vp, _i, _i, _i]),
                 "md_gb300_set_solve_path_x": (_i, [_i]),
+                "md_gb300_autotune_fp64_x": (_i, [pp, _vp, _i, C.POINTER(_i), C.POINTER(_i), _dp]),
                 "md_gb300_get_solve_path_x": (_i, [_i]),
                 "md_gb300_autotune_solve_x": (_i, [pp, _i, C.POINTER(_i), _dp]),
                 "md_gb300_exchange_tables_x": (_i, [pp, _dp, _dp]),

@@ -116,3 +116,42 @@ def test_autotuned_tile_shape_leaves_forces_unchanged(lib):
             s.free()
     finally:
         lib.check(lib.md_gb300_set_precision_x(0))
+
+
+def test_fp64_autotuner_keeps_parity(lib):
+    """The FP64 launch shapes (tile blocks per SM, structure-factor layout)
+    chosen by timing: the forces after tuning equal those before to rounding,
+    and every layout gives the same structure-factor sums to rounding."""
+    import orc
+    from gpu_common import random_state
+    from helpers import assert_close
+    lib.check(lib.md_gb300_set_precision_x(0))
+    for kind, N, P in (("ueg", 260, 2), ("trap", 96, 8)):
+        box = (4 * np.pi * N / 3) ** (1 / 3) if kind == "ueg" else 10.0
+        st = random_state(3, 4, N, P, 1.0, box, kind == "ueg", seed=N)
+        s = xmd_x.PimdSystem(lib, N, P, 0.5, 1.0, box=box)
+        s.set_state(**st)
+        xmd_x.set_potentials(lib, gauss_g=0.75 * np.pi, gauss_s=0.5, coul_s=1.0, alpha=5.6 / box, nsum=4)
+        pf = lib.fn("md_coulomb_3d_ewald_force_x" if kind == "ueg" else "md_gaussian_force_x")
+
+        def forces():
+            lib.check(lib.md_reset_force_x(s.sim))
+            lib.check(lib.md_pimd_calc_pair_force_x(s.pimd, pf))
+            return s.state()["f"]
+
+        before = forces()
+        bps, lay, ms = C.c_int(), C.c_int(), C.c_double()
+        lib.check(lib.md_gb300_autotune_fp64_x(s.pimd, pf, 3, C.byref(bps), C.byref(lay), C.byref(ms)), "autotune")
+        assert bps.value in (1, 2) and ms.value > 0
+        assert lay.value in ((1, 2, 3) if kind == "ueg" else (0,))
+        assert_close(forces(), before, 1e-13, "forces after FP64 autotuning")
+        if kind == "ueg":  # the untuned Ewald path is pinned by the parity tests
+            s.free()
+            continue
+        o = orc.OrcSim(3, 4, N * P, st["m"], st["x"], st["v"], np.zeros(N * P * 3), st["cf"], st["theta"],
+                       st["vtheta"], st["Q"], 1.0, [box] * 3)
+        prm = orc.params(gauss_g=0.75 * np.pi, gauss_s=0.5, coul_s=1.0, coul_alpha=5.6 / box, coul_nsum=4)
+        orc.lib().orc_pair_force(o.ref, N, P, orc.PAIR_EWALD if kind == "ueg" else orc.PAIR_GAUSSIAN,
+                                 orc.C.byref(prm))
+        assert_close(forces(), o.f, 1e-10, "tuned FP64 forces vs the oracle")
+        s.free()
