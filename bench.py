@@ -118,6 +118,18 @@ class Clocks:
         for ln in self.proc.stdout:
             self.rows.append([c.strip() for c in ln.split(",")])
 
+    def started(self, limit=5.0):
+        """wait (bounded) for nvidia-smi's first row, so that sampling covers
+        the region that follows; rows before it are not counted"""
+        t = time.perf_counter()
+        while self.proc and not self.rows and time.perf_counter() - t < limit:
+            time.sleep(0.005)
+        self.n0 = len(self.rows)
+        return self
+
+    def fresh(self):
+        return len(self.rows) - getattr(self, "n0", 0)
+
     def __exit__(self, *a):
         if self.proc:
             self.proc.terminate()
@@ -126,7 +138,7 @@ class Clocks:
     def summary(self):
         sm, reasons, mx = [], set(), None
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for r in self.rows:
+        for r in self.rows[getattr(self, "n0", 0):]:
             try:
                 sm.append(float(r[0]))
                 mx = float(r[1])
@@ -330,7 +342,7 @@ class Runner:
         lib = self.lib
         return lambda: lib.check(lib.md_gb300_graph_launch_x(g, 1))
 
-    def time(self, actions, warm):
+    def time(self, actions, warm, clocks=True):
         """Per-step CUDA events around each action (one step each); the L2 is
         flushed (256 MB write) before every step, outside the events."""
         torch, lib = self.torch, self.lib
@@ -341,6 +353,7 @@ class Runner:
         barrier(self.dist)
         torch.cuda.synchronize()
         with Clocks(self.dev) as clk:
+            clk.started()
             t0 = time.perf_counter()
             with torch.cuda.stream(self.stream):
                 for (e0, e1), act in zip(evs, actions):
@@ -351,10 +364,24 @@ class Runner:
             lib.check(lib.md_gb300_synchronize_x())
             torch.cuda.synchronize()
             wall = time.perf_counter() - t0
+            # a timed region of a few ms falls between nvidia-smi's 100 ms
+            # samples: the same step is replayed (untimed, same flush) until
+            # five samples under load exist, at most 3 s
+            pad, t1 = 0, time.perf_counter()
+            while clocks and clk.proc and clk.fresh() < 5 and time.perf_counter() - t1 < 3.0:
+                with torch.cuda.stream(self.stream):
+                    for _ in range(16):
+                        self.flush.zero_()
+                        warm[0]()
+                lib.check(lib.md_gb300_synchronize_x())
+                pad += 16
         barrier(self.dist)
         self.last_ms = [a.elapsed_time(b) for a, b in evs]
         ms = sum(self.last_ms) / len(evs)
-        return max_over_ranks(self.dist, ms), wall, clk.summary()
+        summ = clk.summary()
+        summ["window"] = (f"the {len(actions)} timed steps" if not pad else
+                          f"the {len(actions)} timed steps and {pad} untimed replays of the same step after them")
+        return max_over_ranks(self.dist, ms), wall, summ
 
     def profile(self, step, n=2):
         """live per-kernel times of n un-captured steps: {kernel: ms per step}"""
@@ -571,7 +598,7 @@ def ensemble_form(lib, R, args):
         for gi in singles:
             lib.check(lib.md_gb300_graph_launch_x(gi, 1))
 
-    ms_seq, _, _ = R.time([seq] * nst, [seq] * 3)
+    ms_seq, _, _ = R.time([seq] * nst, [seq] * 3, clocks=False)
     for gi in singles:
         lib.md_gb300_graph_free_x(gi)
     lib.md_gb300_graph_free_x(g)
@@ -657,7 +684,7 @@ def recursion_form(lib, R, args):
         fill = lambda: lib.check(lib.md_pimd_fill_VB_x(s.pimd))  # noqa: E731
         fill()
         g, _ = R.capture(fill)
-        ms, _, _ = R.time([R.launcher(g)] * 10, [R.launcher(g)] * 3)
+        ms, _, _ = R.time([R.launcher(g)] * 10, [R.launcher(g)] * 3, clocks=False)
         lib.md_gb300_graph_free_x(g)
         out[str(n)] = round(ms * 1e3, 1)
         s.free()
