@@ -602,6 +602,18 @@ def ensemble_form(lib, R, args):
     for gi in singles:
         lib.md_gb300_graph_free_x(gi)
     lib.md_gb300_graph_free_x(g)
+    # one persistent kernel per step: cluster size by the autotuner (which
+    # advances the systems by the steps it times), then captured
+    ms_br, kernels_br = ms, kernels
+    cl, tms = C.c_int(), C.c_double()
+    lib.check(lib.md_gb300_autotune_ensemble_x(len(systems), C.cast(fn, C.c_void_p), None, 3, C.byref(cl),
+                                               C.byref(tms)), "persistent ensemble autotuning")
+    gp = C.c_void_p()
+    lib.check(lib.md_gb300_capture_ensemble_persistent_x(len(systems), C.cast(fn, C.c_void_p), None, C.byref(gp)),
+              "persistent ensemble capture")
+    kernels = lib.md_gb300_graph_kernel_count_x(gp)
+    ms, wall, clocks = R.time([R.launcher(gp)] * nst, [R.launcher(gp)] * 3)
+    lib.md_gb300_graph_free_x(gp)
     for _, s, _ in systems:
         s.free()
     lib.check(lib.md_gb300_set_precision_x(0))
@@ -609,6 +621,9 @@ def ensemble_form(lib, R, args):
     xmd_x.set_potentials(lib, coul_s=1.0, alpha=ALPHA_L / box, nsum=NSUM)
     return {"value": beads / (ms * 1e-3), "unit": "bead-steps/s", "ms_per_step": ms, "systems": len(specs),
             "bead_slots": beads, "kernels_per_launch": kernels, "steps_timed": nst,
+            "persistent_cluster_blocks": cl.value,
+            "graph_branches_ms_per_step": ms_br, "graph_branches_kernels": kernels_br,
+            "gain_vs_graph_branches": ms_br / ms,
             "sequential_graphs_ms_per_step": ms_seq, "gain_vs_sequential": ms_seq / ms,
             "tile_warps_chosen": {f"{k[0]} N={k[1]} P={k[2]}": v for k, v in sorted(tuned.items())},
             "clocks": clocks,

@@ -64,6 +64,29 @@ int md_gb300_graph_launch_x(md_gb300_graph_t_x *graph, int count);
    state must exist already (one ordinary step first). */
 typedef int (*md_gb300_system_step_fn_x)(int system, void *ctx);
 int md_gb300_capture_ensemble_x(int n, md_gb300_system_step_fn_x step, void *ctx, md_gb300_graph_t_x **graph);
+/* The same ensemble step as ONE persistent kernel launch (captured into a
+   graph): thread-block clusters take the systems of a list balanced by
+   estimated cost and run each system's whole step, its stages separated by
+   cluster barriers.  While planning, step(i, ctx)'s calls do not launch;
+   each records its call and the md_set_* parameters of the moment.  Every
+   system's calls must be the reference driver's step, in this order:
+   md_update_nhc_VV3_1_x, md_reset_force_x, md_pimd_fast_fill_ENk_x,
+   md_pimd_fill_VB_x, md_pimd_fast_fill_force_VB_x, optionally
+   md_pimd_calc_trap_force_x and md_pimd_calc_pair_force_x,
+   md_update_nhc_VV3_2_x, optionally md_periodic_boundary_x; pair forces in
+   MD_GB_PRECISION_MIXED (FP32), one-DOF thermostat chains of length 4 or 8,
+   N <= 2048, no learned model attached.  Other calls are refused
+   (MD_GB_ERR_UNSUPPORTED).  The results equal those of the per-system calls
+   to rounding.  The cluster size is the one md_gb300_autotune_ensemble_x
+   chose for this ensemble's shapes, else 4 blocks. */
+int md_gb300_capture_ensemble_persistent_x(int n, md_gb300_system_step_fn_x step, void *ctx,
+                                           md_gb300_graph_t_x **graph);
+/* Times the persistent step at cluster sizes 1, 2, 4 and 8 blocks (each
+   `repeats` + 1 launches, so the systems advance by those steps) and
+   records the fastest for this ensemble's shapes; *cluster and *ms (may be
+   NULL) receive it and its time per step. */
+int md_gb300_autotune_ensemble_x(int n, md_gb300_system_step_fn_x step, void *ctx, int repeats, int *cluster,
+                                 double *ms);
 /* kernel nodes in a captured graph (kernels launched per replay) */
 int md_gb300_graph_kernel_count_x(md_gb300_graph_t_x *graph);
 void md_gb300_graph_free_x(md_gb300_graph_t_x *graph);

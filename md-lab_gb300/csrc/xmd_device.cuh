@@ -672,6 +672,9 @@ struct P32 {
   float im0;
 };
 
+// the FP32 pair kernel's constants for a system and potential (host)
+P32 make_p32(const Geo &g, const PairPrm &p);
+
 template <int D, int KIND>
 __device__ inline void pair_eval32(const P32 &q, const float *dx, float *F) {
   if (KIND == PAIR_GAUSSIAN || KIND == PAIR_PERIODIC_GAUSSIAN) {
@@ -779,6 +782,10 @@ __device__ inline float2 cmulf(float2 a, float2 b) {
   return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
 }
 
+
+// the solve's job for weight scratch rs_f / rs_b (rec_scratch_doubles(N)
+// each) and outputs VBN / tmpV (host)
+TriJob tri_job(int N, double *rs_f, double *rs_b, double *VBN, double *tmpV);
 
 // The block solve of direction `backward` by the calling thread block (any
 // whole number of warps; rows of a chunk go round-robin over the warps, each
@@ -913,6 +920,290 @@ __device__ inline void tri_solve_b_dev(int N, double beta, const TriJob &job, in
       job.Xm[backward][i] = Xm[i];
       job.Xe[backward][i] = Xe[i];
     }
+}
+
+
+// particle l's interior springs, E_l^(1) and the increment gl[l]: one warp
+template <int D>
+__device__ inline void eint_particle(const Geo &g, const double *__restrict__ x, const double *__restrict__ m,
+                                     double w2, int image, double *Eint, double *ENk, double *gl, int l, int lane) {
+  double res = 0;
+  for (int j = lane; j + 1 < g.P; j += 32)
+    res += 0.5 * m[(size_t)j * g.Ns + l] * w2 * spring2<D>(g, x, j, l, j + 1, l, image);
+  res = warp_sum(res);
+  // lane 0: the closing spring of l (E_l^(1)); lane 1: the link to l+1 (the
+  // increment of the prefix sums), both in one pass
+  if (lane < 2) {
+    const int b = lane == 0 ? l : (l + 1 < g.N ? l + 1 : l);
+    const double lk = link<D>(g, x, m, w2, l, b, image);
+    if (lane == 0) {
+      Eint[l] = res;
+      ENk[dtri(l + 1)] = res + lk;
+    } else if (l + 1 < g.N) {
+      gl[l] = res + lk;
+    }
+  }
+}
+
+// E_l^(k) (1-based row l, cycle length k >= 2) from the prefix sums G
+template <int D>
+__device__ inline void enk_entry(const Geo &g, const double *__restrict__ x, const double *__restrict__ m, double w2,
+                                 int image, const double *__restrict__ Eint, const double *G, double *__restrict__ ENk,
+                                 int l, int k) {
+  ENk[dtri(l) + k - 1] = Eint[l - 1] + ((G[l - 1] - G[l - k]) + link<D>(g, x, m, w2, l - 1, l - k, image));
+}
+
+// the ring springs' force on interior bead j (1..P-2) of particle l
+template <int D>
+__device__ inline void spring_interior_bead(const Geo &g, const double *__restrict__ x,
+                                            const double *__restrict__ m, double w2, int image,
+                                            double *__restrict__ f, int j, int l) {
+  const double mm = m[(size_t)j * g.Ns + l];
+  double gr[D];
+  grad2<D>(g, x, mm * w2, j, l, j + 1, l, j - 1, l, image, gr);
+#pragma unroll
+  for (int d = 0; d < D; ++d) f[sidx(j, d, l, D, g.Ns)] += -gr[d] / mm;
+}
+
+// G[l][j] (1-based) from the extended-range weights and unknowns
+__device__ inline void g_ext_elem(int N, const double *__restrict__ Mm, const int *__restrict__ Me,
+                                  const double *__restrict__ Xfm, const int *__restrict__ Xfe,
+                                  const double *__restrict__ Xbm, const int *__restrict__ Xbe, double *__restrict__ G,
+                                  int l, int j) {
+  // X'_{N-l} / X_N, as a mantissa and an exponent
+  const double q = Xbm[N - l] / Xfm[N];
+  const int qe = Xbe[N - l] - Xfe[N];
+  double gv;
+  if (j > l + 1) {
+    gv = 0;
+  } else if (j == l + 1) {
+    gv = 1 - ext_val(Xfm[l] * q, Xfe[l] + qe);
+  } else {
+    const size_t o = moff(l, j - 1);
+    const double w = Mm[o];
+    gv = w == 0.0 ? 0.0 : ext_val(w * Xfm[j - 1] * q, Me[o] + Xfe[j - 1] + qe);
+  }
+  G[(size_t)(l - 1) * N + (j - 1)] = gv;
+}
+
+// FP32 phase factors e^{2 pi i n x/L}, n = 0..ns, of slot t (D = 3 layout)
+__device__ inline void phase32_slot(const Geo &g, int ns, const double *__restrict__ x, float2 *__restrict__ ph32,
+                                    size_t t) {
+  const int l = (int)(t % g.Ns);
+  const int jd = (int)(t / g.Ns);  // j*3 + d
+  const int d = jd % 3;
+  float s1 = 0.f, c1 = 1.f;
+  if (l < g.N) {
+    double u = x[t] * g.inv_box[d];
+    u -= rint(u);  // in [-1/2, 1/2]
+    sincospif((float)(2.0 * u), &s1, &c1);
+  }
+  float re = 1.f, im = 0.f;
+  float2 *o = ph32 + (size_t)jd * (ns + 1) * g.Ns + l;
+  o[0] = make_float2(1.f, 0.f);
+  for (int n = 1; n <= ns; ++n) {
+    const float r2 = fmaf(re, c1, -im * s1), i2 = fmaf(re, s1, im * c1);
+    re = r2;
+    im = i2;
+    o[(size_t)n * g.Ns] = make_float2(re, im);
+  }
+}
+
+// entry n (0..ns) of column ci's FP32 force table of slice j
+__device__ inline void recip_table32_entry(const int4 *__restrict__ cols, int ncol, const double2 *__restrict__ S,
+                                           const double *__restrict__ coef, int nk, float2 *__restrict__ T, int ns,
+                                           int j, int ci, int n) {
+  const int NT = 4 * ns + 1;
+  const int4 c = cols[ci];
+  auto W = [&](int nz) {
+    if (nz < c.z) return make_double2(0.0, 0.0);
+    const int k = c.w + (nz - c.z);
+    const double2 s = S[(size_t)j * nk + k];
+    return make_double2(coef[k] * s.x, -coef[k] * s.y);
+  };
+  float2 *o = T + ((size_t)j * ncol + ci) * NT;
+  if (n == 0) {
+    const double2 w = W(0);
+    o[0] = make_float2((float)w.x, (float)w.y);
+  } else {
+    const double2 wp = W(n), wm = W(-n);
+    const double Ar = wp.x + wm.x, Ai = wp.y + wm.y, Br = wp.x - wm.x, Bi = wp.y - wm.y;
+    o[4 * n - 3] = make_float2((float)Ar, (float)Ai);
+    o[4 * n - 2] = make_float2((float)Br, (float)Bi);
+    o[4 * n - 1] = make_float2((float)(n * Ar), (float)(n * Ai));
+    o[4 * n] = make_float2((float)(n * Br), (float)(n * Bi));
+  }
+}
+
+// tile job wi (slice wi / jobs, tile pair I <= J) of the FP32 pair forces,
+// one warp: per-tile sums into out (see k_pair_tiles32)
+template <int D, int KIND>
+__device__ inline void pair_tile32_job(const Geo &g, const P32 &q, const float *__restrict__ x,
+                                       const float *__restrict__ im, float *__restrict__ out, int T, int jobs, int wi,
+                                       int lane) {
+  const int j = wi / jobs;
+  int job = wi % jobs, I = 0;
+  while (job >= T - I) {
+    job -= T - I;
+    ++I;
+  }
+  const int J = I + job;
+  const int a = I * 32 + lane, b0 = J * 32 + lane;
+  const bool va = a < g.N, vb = b0 < g.N;
+  float xa[D], xb[D], fa[D], fb[D];
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    xa[d] = va ? x[sidx(j, d, a, D, g.Ns)] : 0.f;
+    xb[d] = vb ? x[sidx(j, d, b0, D, g.Ns)] : 0.f;
+    fa[d] = fb[d] = 0.f;
+  }
+  const int src = (lane + 1) & 31;
+  if (q.uniform) {
+    for (int s = 0; s < 32; ++s) {
+      const int bi = J * 32 + ((lane + s) & 31);
+      if (va && bi < g.N && (I != J || a > bi)) {
+        float dx[D], F[D];
+#pragma unroll
+        for (int d = 0; d < D; ++d) dx[d] = xa[d] - xb[d];
+        pair_eval32<D, KIND>(q, dx, F);
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+          fa[d] += F[d];
+          fb[d] -= F[d];
+        }
+      }
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        xb[d] = __shfl_sync(FULL, xb[d], src);
+        fb[d] = __shfl_sync(FULL, fb[d], src);
+      }
+    }
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      fa[d] *= q.im0;
+      fb[d] *= q.im0;
+    }
+  } else {
+    const float ima = va ? im[(size_t)j * g.Ns + a] : 1.f;
+    float imb = vb ? im[(size_t)j * g.Ns + b0] : 1.f;
+    for (int s = 0; s < 32; ++s) {
+      const int bi = J * 32 + ((lane + s) & 31);
+      if (va && bi < g.N && (I != J || a > bi)) {
+        float dx[D], F[D];
+#pragma unroll
+        for (int d = 0; d < D; ++d) dx[d] = xa[d] - xb[d];
+        pair_eval32<D, KIND>(q, dx, F);
+        // the reference divides by the mass of the higher-index particle
+        const float inv = a > bi ? ima : imb;
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+          fa[d] = fmaf(F[d], inv, fa[d]);
+          fb[d] = fmaf(-F[d], inv, fb[d]);
+        }
+      }
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        xb[d] = __shfl_sync(FULL, xb[d], src);
+        fb[d] = __shfl_sync(FULL, fb[d], src);
+      }
+      imb = __shfl_sync(FULL, imb, src);
+    }
+  }
+  if (I == J) {
+    if (va) {
+#pragma unroll
+      for (int d = 0; d < D; ++d) out[(((size_t)I * g.P + j) * D + d) * g.Ns + a] = fa[d] + fb[d];
+    }
+  } else {
+    if (va) {
+#pragma unroll
+      for (int d = 0; d < D; ++d) out[(((size_t)J * g.P + j) * D + d) * g.Ns + a] = fa[d];
+    }
+    if (vb) {
+#pragma unroll
+      for (int d = 0; d < D; ++d) out[(((size_t)I * g.P + j) * D + d) * g.Ns + b0] = fb[d];
+    }
+  }
+}
+
+// the exchange spring forces on the end beads of particles bx*32 .. +31
+// from partners js*EX_TY + ty + k nsplit EX_TY: one 32 x EX_TY thread
+// block (tx, ty), red: EX_TY * 2D * 32 doubles of shared memory
+template <int D>
+__device__ inline void exch_ends_block(const Geo &g, const double *__restrict__ x, const double *__restrict__ m,
+                                       double w2, int image, const double *__restrict__ G,
+                                       double *__restrict__ scratch, int nsplit, int bx, int js, int tx, int ty,
+                                       double *red) {
+  const int l = bx * 32 + tx;
+  const int N = g.N, jP = g.P - 1;
+  double a1[D], aP[D];
+#pragma unroll
+  for (int d = 0; d < D; ++d) a1[d] = aP[d] = 0;
+  if (l < N) {
+    const double m1 = m[l], mP = m[(size_t)jP * g.Ns + l];
+    // The reference adds G-weighted gradients of both springs at the end
+    // bead for every partner q; the spring inside the ring (bead 1 -> 2,
+    // bead P -> P-1) does not depend on q, so it is weighted once by the sum
+    // of the weights and only the partner spring is evaluated per q (equal
+    // to rounding).
+    double x1[D], xP[D], s1 = 0.0, sP = 0.0;
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      x1[d] = x[sidx(0, d, l, D, g.Ns)];
+      xP[d] = x[sidx(jP, d, l, D, g.Ns)];
+    }
+    // partner q runs over this block's part of 0..N-1
+    for (int q = js * EX_TY + ty; q < N; q += nsplit * EX_TY) {
+      // bead 1 of l, previous bead = bead P of q, weight G[q][l]
+      const double g1 = G[(size_t)q * N + l];
+      if (g1 != 0.0) {
+        s1 += g1;
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+          double c = x1[d] - x[sidx(jP, d, q, D, g.Ns)];
+          if (image) c = min_image(c, g.box[d], g.inv_box[d]);
+          a1[d] = fma(g1, c, a1[d]);
+        }
+      }
+      // bead P of l, next bead = bead 1 of q, weight G[l][q]
+      const double gP = G[(size_t)l * N + q];
+      if (gP != 0.0) {
+        sP += gP;
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+          double c = xP[d] - x[sidx(0, d, q, D, g.Ns)];
+          if (image) c = min_image(c, g.box[d], g.inv_box[d]);
+          aP[d] = fma(gP, c, aP[d]);
+        }
+      }
+    }
+    const double k1 = m1 * w2, kP = mP * w2;
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      double a = x1[d] - x[sidx(1, d, l, D, g.Ns)];
+      double b = xP[d] - x[sidx(jP - 1, d, l, D, g.Ns)];
+      if (image) {
+        a = min_image(a, g.box[d], g.inv_box[d]);
+        b = min_image(b, g.box[d], g.inv_box[d]);
+      }
+      a1[d] = k1 * (s1 * a + a1[d]);
+      aP[d] = kP * (sP * b + aP[d]);
+    }
+  }
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    red[(ty * 2 * D + d) * 32 + tx] = a1[d];
+    red[(ty * 2 * D + D + d) * 32 + tx] = aP[d];
+  }
+  __syncthreads();
+  if (ty == 0 && l < N) {
+#pragma unroll
+    for (int q = 0; q < 2 * D; ++q) {
+      double s = 0;
+      for (int y = 0; y < EX_TY; ++y) s += red[(y * 2 * D + q) * 32 + tx];
+      scratch[((size_t)js * 2 * D + q) * g.Ns + l] = s;
+    }
+  }
 }
 
 }  // namespace xk

@@ -1,0 +1,340 @@
+// xmd_ensemble_api.cpp -- the persistent ensemble step behind the C ABI:
+// md_gb300_capture_ensemble_persistent_x and md_gb300_autotune_ensemble_x.
+//
+// The driver describes one step of every system the way it would run it,
+// through a callback that makes the reference's calls (md_update_nhc_VV3_1_x
+// ... md_periodic_boundary_x) after setting that system's md_set_*
+// parameters.  While planning, those entry points do not launch: each
+// records its call, with the potential parameters and Ewald tables of the
+// moment, for the current system.  Each system's record must be the
+// reference driver's step (the thermostat half steps around the force
+// calls); it becomes one descriptor of the persistent kernel (xmd_ensemble.cu),
+// and one launch of that kernel, captured into a graph, then advances all
+// systems.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <utility>
+#include <vector>
+
+#include "xmd_internal.h"
+
+using namespace xmd;
+
+static const int D = MD_DIMENSION_X;
+
+namespace {
+
+struct Rec {
+  int op = 0;
+  md_simulation_t_x *sim = nullptr;
+  md_pimd_t_x *pimd = nullptr;
+  double dt = 0;
+  int arg = 0;
+  int kind = 0;
+  xk::TrapPrm tp{};
+  xk::PairPrm pp{};
+  xk::Recip rc{};
+  double inv_mP = 0;
+};
+
+struct Recorder {
+  std::vector<Rec> calls;  // the current system's
+  bool allowed = false;    // the recorder's own device-state calls
+};
+
+thread_local Recorder *t_rec = nullptr;
+
+// the recorder's own calls into the device-state functions
+struct Allow {
+  Allow() { t_rec->allowed = true; }
+  ~Allow() { t_rec->allowed = false; }
+};
+
+}  // namespace
+
+bool xmd::ens_recording() { return t_rec != nullptr; }
+
+int xmd::ens_refuse() {
+  if (t_rec && !t_rec->allowed)
+    return fail(MD_GB_ERR_UNSUPPORTED,
+                "a persistent ensemble step is made of the step's calls only (thermostat half steps, force reset, "
+                "cycle energies, recursions, exchange, trap and pair forces, periodic boundary)");
+  return 0;
+}
+
+int xmd::ens_record(int op, md_simulation_t_x *sim, md_pimd_t_x *pimd, double dt, int arg, const void *fn) {
+  Rec r;
+  r.op = op;
+  r.sim = sim;
+  r.pimd = pimd;
+  r.dt = dt;
+  r.arg = arg;
+  if (op == ENS_TRAP) {
+    r.kind = trap_kind_of(fn, false);
+    if (!r.kind) return fail(MD_GB_ERR_UNSUPPORTED, "trap force function has no device kernel");
+    r.tp = trap_params(r.kind);
+  } else if (op == ENS_PAIR) {
+    r.kind = pair_kind_of(fn, false);
+    if (!r.kind) return fail(MD_GB_ERR_UNSUPPORTED, "pair force function has no device kernel");
+    if (md_gb300_get_precision_x() != MD_GB_PRECISION_MIXED)
+      return fail(MD_GB_ERR_UNSUPPORTED, "the persistent ensemble computes pair forces in FP32: set "
+                                         "MD_GB_PRECISION_MIXED before planning it");
+    Allow a;
+    SimDev *sd;
+    PimdDev *pd;
+    XMD_TRY(pimd_device(pimd, &sd, &pd));
+    if (learned_mode(pimd, false))
+      return fail(MD_GB_ERR_UNSUPPORTED, "a learned Ewald model is attached to a system of the ensemble");
+    if (r.kind == xk::PAIR_PERIODIC_GAUSSIAN || r.kind == xk::PAIR_PERIODIC_COULOMB || r.kind == xk::PAIR_EWALD_REAL)
+      XMD_TRY(check_image(sd, 1));
+    r.pp = force_params(r.kind, sd);
+    if (r.kind == xk::PAIR_EWALD_REAL) {
+      if (D != 3) return fail(MD_GB_ERR_UNSUPPORTED, "Ewald sums are three-dimensional");
+      if (r.pp.kmax[0] > 1 || r.pp.kmax[1] > 1 || r.pp.kmax[2] > 1)
+        return fail(MD_GB_ERR_UNSUPPORTED, "Ewald alpha*L too small (images beyond the neighbouring boxes)");
+      if (!sd->uniform_mass) return fail(MD_GB_ERR_UNSUPPORTED, "structure-factor Ewald needs equal bead masses");
+      XMD_TRY(ewald_tables(pimd, sd, pd));
+      r.rc = recip_of(pd);
+      r.inv_mP = 1.0 / (sd->mass0 * pimd->P);
+    }
+  }
+  t_rec->calls.push_back(r);
+  return 0;
+}
+
+// one system's record as a descriptor of the persistent kernel
+static int describe(const std::vector<Rec> &c, xk::EnsSysDesc &d, md_pimd_t_x **pimd_out) {
+  static const int order[] = {ENS_NHC1, ENS_RESET, ENS_ENK, ENS_VB, ENS_FVB, ENS_TRAP, ENS_PAIR, ENS_NHC2, ENS_WRAP};
+  const bool optional[] = {false, false, false, false, false, true, true, false, true};
+  size_t at = 0;
+  const Rec *by[ENS_WRAP + 1] = {};
+  for (int k = 0; k < 9; ++k) {
+    if (at < c.size() && c[at].op == order[k]) {
+      by[order[k]] = &c[at++];
+    } else if (!optional[k]) {
+      return fail(MD_GB_ERR_UNSUPPORTED, "a persistent ensemble step must be the reference driver's step: "
+                                         "VV3_1, reset, ENk, V_B, exchange forces, [trap], [pair], VV3_2, [wrap]");
+    }
+  }
+  if (at != c.size())
+    return fail(MD_GB_ERR_UNSUPPORTED, "a persistent ensemble step must be the reference driver's step: "
+                                       "VV3_1, reset, ENk, V_B, exchange forces, [trap], [pair], VV3_2, [wrap]");
+  md_pimd_t_x *pimd = by[ENS_ENK]->pimd;
+  md_simulation_t_x *sim = by[ENS_NHC1]->sim;
+  for (const Rec &r : c) {
+    if (r.pimd && r.pimd != pimd) return fail(MD_GB_ERR_UNSUPPORTED, "one system's step uses two md_pimd_t_x");
+    if (r.sim && r.sim != sim) return fail(MD_GB_ERR_UNSUPPORTED, "one system's step uses two simulations");
+  }
+  if (!pimd || pimd->sim != sim) return fail(MD_GB_ERR_UNSUPPORTED, "the exchange calls use another simulation");
+  if (by[ENS_NHC1]->dt != by[ENS_NHC2]->dt)
+    return fail(MD_GB_ERR_UNSUPPORTED, "the two thermostat half steps use different time steps");
+  if (by[ENS_ENK]->arg != by[ENS_FVB]->arg)
+    return fail(MD_GB_ERR_UNSUPPORTED, "the cycle energies and exchange forces use different image flags");
+  if (pimd->worm_index > 0 || pimd->cut_Pj != -1 || pimd->pbc)
+    return fail(MD_GB_ERR_UNSUPPORTED, "worm, cut-bead and winding bookkeeping are not supported");
+  if (pimd->P < 2) return fail(MD_GB_ERR_ARG, "the exchange spring force needs P >= 2 beads");
+  Allow a;
+  SimDev *sd;
+  PimdDev *pd;
+  XMD_TRY(pimd_device(pimd, &sd, &pd));
+  const int image = by[ENS_ENK]->arg;
+  XMD_TRY(check_image(sd, image));
+  if (sd->nf < 1 || !sd->fast_chains || (sd->L != 4 && sd->L != 8))
+    return fail(MD_GB_ERR_UNSUPPORTED, "the persistent ensemble needs one-DOF thermostat chains of length 4 or 8");
+  if (pimd->N > xk::ENS_MAX_N) return fail(MD_GB_ERR_UNSUPPORTED, "N above %d", xk::ENS_MAX_N);
+  const xk::Geo &g = sd->geo;
+  const size_t nx = xk::exch_scratch_doubles(g);
+  XMD_TRY(reserve(sd->fex, g.slots() * sizeof(double)));
+  XMD_TRY(reserve(sd->xscr, nx * sizeof(double)));
+  memset(&d, 0, sizeof(d));
+  d.g = g;
+  d.image = image;
+  d.wrap = by[ENS_WRAP] ? 1 : 0;
+  if (by[ENS_TRAP]) {
+    d.trap_kind = by[ENS_TRAP]->kind;
+    d.tp = by[ENS_TRAP]->tp;
+  }
+  if (by[ENS_PAIR]) {
+    if (!sd->uniform_mass)
+      return fail(MD_GB_ERR_UNSUPPORTED, "the persistent ensemble's pair forces need equal bead masses");
+    d.pair_kind = by[ENS_PAIR]->kind;
+    d.pp = by[ENS_PAIR]->pp;
+    d.rc = by[ENS_PAIR]->rc;
+    d.inv_mP = by[ENS_PAIR]->inv_mP;
+  }
+  d.kT = MD_kB_X * sim->T;
+  d.h = by[ENS_NHC1]->dt;
+  d.beta = pimd->beta;
+  d.vi = pimd->vi;
+  d.w2 = pimd->omegaP * pimd->omegaP;
+  d.x = sd->x.as<double>();
+  d.v = sd->v.as<double>();
+  d.f = sd->f.as<double>();
+  d.m = sd->m.as<double>();
+  d.th = sd->th.as<double>();
+  d.vt = sd->vt.as<double>();
+  d.Q = sd->Q.as<double>();
+  d.iQ = sd->iQ.as<double>();
+  d.fex = sd->fex.as<double>();
+  d.xscr = sd->xscr.as<double>();
+  d.Eint = pd->Eint.as<double>();
+  d.ENk = pd->ENk.as<double>();
+  d.gl = pd->linkt.as<double>();
+  d.lnn = pd->lnn.as<double>();
+  d.VBN = pd->VBN.as<double>();
+  d.tmpV = pd->tmpV.as<double>();
+  d.G = pd->G.as<double>();
+  d.rs_f = pd->rec.as<double>();
+  d.rs_b = d.rs_f + xk::rec_scratch_doubles(pimd->N);
+  *pimd_out = pimd;
+  return 0;
+}
+
+// every system's step recorded and described
+static int plan(int n, md_gb300_system_step_fn_x step, void *ctx, std::vector<xk::EnsSysDesc> &descs,
+                std::vector<md_pimd_t_x *> &pimds) {
+  if (n < 1 || !step) return fail(MD_GB_ERR_ARG, "invalid ensemble arguments");
+  XMD_TRY(ensure_device());
+  if (capturing()) return fail(MD_GB_ERR_CAPTURE, "already capturing");
+  XMD_TRY(join_side());
+  descs.assign(n, xk::EnsSysDesc{});
+  pimds.assign(n, nullptr);
+  Recorder rec;
+  for (int i = 0; i < n; ++i) {
+    rec.calls.clear();
+    t_rec = &rec;
+    int rc = step(i, ctx);
+    t_rec = nullptr;
+    if (rc) return rc;
+    t_rec = &rec;
+    rc = describe(rec.calls, descs[i], &pimds[i]);
+    t_rec = nullptr;
+    if (rc) return rc;
+  }
+  return 0;
+}
+
+// after the kernel has run, each system's recursions, G and cycle energies
+// belong to its current positions, beta and xi (what the per-system calls
+// would have left)
+static void mark_fresh(const std::vector<md_pimd_t_x *> &pimds) {
+  for (md_pimd_t_x *p : pimds) {
+    SimDev *sd;
+    PimdDev *pd;
+    if (pimd_device(p, &sd, &pd) != 0) continue;
+    pd->tmpv_fresh = true;
+    pd->tmpv_beta = p->beta;
+    pd->tmpv_vi = p->vi;
+    pd->g_fresh = true;
+    pd->g_beta = p->beta;
+    pd->g_vi = p->vi;
+  }
+}
+
+// cluster sizes chosen by the autotuner, per ensemble shape
+static std::mutex g_mu;
+static std::vector<std::pair<std::vector<long long>, int>> g_choice;
+
+static std::vector<long long> signature(const std::vector<xk::EnsSysDesc> &d) {
+  std::vector<long long> s;
+  for (const auto &e : d)
+    s.push_back(((long long)e.g.N << 40) | ((long long)e.g.P << 20) | ((long long)e.pair_kind << 8) | e.rc.nsum);
+  return s;
+}
+
+static int chosen_cluster(const std::vector<long long> &sig) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  for (const auto &c : g_choice)
+    if (c.first == sig) return c.second;
+  return 0;
+}
+
+static void release_launch(void *p) {
+  xk::EnsLaunch *e = (xk::EnsLaunch *)p;
+  xk::ensemble_free(*e);
+  delete e;
+}
+
+extern "C" {
+
+int md_gb300_capture_ensemble_persistent_x(int n, md_gb300_system_step_fn_x step, void *ctx,
+                                           md_gb300_graph_t_x **out) {
+  if (!out) return fail(MD_GB_ERR_ARG, "NULL graph pointer");
+  std::vector<xk::EnsSysDesc> descs;
+  std::vector<md_pimd_t_x *> pimds;
+  XMD_TRY(plan(n, step, ctx, descs, pimds));
+  int cl = chosen_cluster(signature(descs));
+  if (!cl) cl = xk::ensemble_resident_clusters(D, MD_NHC_LENGTH_X, 4) > 0 ? 4 : 1;
+  xk::EnsLaunch *e = new xk::EnsLaunch();
+  cudaError_t ce = xk::ensemble_prepare(descs.data(), n, D, MD_NHC_LENGTH_X, cl, *e);
+  if (ce != cudaSuccess) {
+    delete e;
+    return cuda_fail(ce, "persistent ensemble plan");
+  }
+  const int rc = capture_single(
+      [](void *p) { return xk::ensemble_launch(*(xk::EnsLaunch *)p, stream()); }, e, release_launch, out);
+  if (rc) return rc;
+  mark_fresh(pimds);
+  return 0;
+}
+
+int md_gb300_autotune_ensemble_x(int n, md_gb300_system_step_fn_x step, void *ctx, int repeats, int *cluster,
+                                 double *ms) {
+  if (repeats < 1) repeats = 1;
+  std::vector<xk::EnsSysDesc> descs;
+  std::vector<md_pimd_t_x *> pimds;
+  XMD_TRY(plan(n, step, ctx, descs, pimds));
+  cudaStream_t st = stream();
+  cudaEvent_t a, b;
+  XMD_CUDA(cudaEventCreate(&a));
+  XMD_CUDA(cudaEventCreate(&b));
+  int best = 0;
+  double best_ms = 0;
+  cudaError_t ce = cudaSuccess;
+  for (int cl : {1, 2, 4, 8}) {
+    if (xk::ensemble_resident_clusters(D, MD_NHC_LENGTH_X, cl) < 1) continue;
+    xk::EnsLaunch e;
+    ce = xk::ensemble_prepare(descs.data(), n, D, MD_NHC_LENGTH_X, cl, e);
+    if (ce != cudaSuccess) break;
+    ce = xk::ensemble_launch(e, st);  // warm-up
+    for (int r = 0; r < repeats && ce == cudaSuccess; ++r) {
+      if (r == 0) ce = cudaEventRecord(a, st);
+      if (ce == cudaSuccess) ce = xk::ensemble_launch(e, st);
+    }
+    if (ce == cudaSuccess) ce = cudaEventRecord(b, st);
+    if (ce == cudaSuccess) ce = cudaEventSynchronize(b);
+    float t = 0;
+    if (ce == cudaSuccess) ce = cudaEventElapsedTime(&t, a, b);
+    xk::ensemble_free(e);
+    if (ce != cudaSuccess) break;
+    const double per = t / repeats;
+    if (!best || per < best_ms) {
+      best = cl;
+      best_ms = per;
+    }
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  if (ce != cudaSuccess) return cuda_fail(ce, "ensemble autotuning");
+  if (!best) return fail(MD_GB_ERR_UNSUPPORTED, "no cluster size of the persistent ensemble kernel fits");
+  {
+    std::lock_guard<std::mutex> lk(g_mu);
+    const auto sig = signature(descs);
+    bool found = false;
+    for (auto &c : g_choice)
+      if (c.first == sig) {
+        c.second = best;
+        found = true;
+      }
+    if (!found) g_choice.push_back({sig, best});
+  }
+  mark_fresh(pimds);
+  if (cluster) *cluster = best;
+  if (ms) *ms = best_ms;
+  return 0;
+}
+
+}  // extern "C"

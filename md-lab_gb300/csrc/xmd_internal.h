@@ -140,6 +140,9 @@ size_t general_scratch(const xk::Geo &g);
 int ewald_tables(md_pimd_t_x *pimd, SimDev *sd, PimdDev *pd);
 xk::Recip recip_of(PimdDev *pd);
 xk::PairPrm pair_params(int kind);
+// the parameters md_pimd_calc_pair_force_x uses for kind on this system
+// (image shifts, inverse mass, the Ewald forces' cut-off)
+xk::PairPrm force_params(int kind, const SimDev *sd);
 void ewald_shifts(xk::PairPrm &p, const xk::Geo &g);
 
 // learned Ewald residual (xmd_learned_api.cpp).  learned_mode: 0 = plain
@@ -150,6 +153,18 @@ int learned_pair_force(md_pimd_t_x *pimd, SimDev *sd, PimdDev *pd, const xk::Pai
 int learned_judge_step(md_pimd_t_x *pimd, SimDev *sd, PimdDev *pd);
 // reciprocal part of the energy in learned mode (truncated sum + network), added to *acc
 int learned_recip_energy(md_pimd_t_x *pimd, SimDev *sd, double *acc, double *scr);
+
+// persistent ensemble planning (xmd_ensemble_api.cpp): while it runs, the
+// step's entry points record their call for the current system instead of
+// launching (ens_record returns their status), and the device state of any
+// other call is refused.
+enum EnsOp { ENS_NHC1 = 1, ENS_RESET, ENS_ENK, ENS_VB, ENS_FVB, ENS_TRAP, ENS_PAIR, ENS_NHC2, ENS_WRAP };
+bool ens_recording();
+int ens_record(int op, md_simulation_t_x *sim, md_pimd_t_x *pimd, double dt, int arg, const void *fn);
+int ens_refuse();  // the error of a device call that is not part of the step
+// a graph of the one launch that launch(ctx) queues on the library stream;
+// release(ctx) runs when the graph is freed (or the capture fails)
+int capture_single(cudaError_t (*launch)(void *), void *ctx, void (*release)(void *), md_gb300_graph_t_x **out);
 
 // read the current potential parameter globals
 xk::TrapPrm trap_params(int kind);

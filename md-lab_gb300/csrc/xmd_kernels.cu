@@ -467,24 +467,8 @@ template <int D>
 __global__ void k_eint(Geo g, const double *__restrict__ x, const double *__restrict__ m,
                        double w2, int image, double *Eint, double *ENk, double *gl) {
   const int l = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
   if (l >= g.N) return;
-  double res = 0;
-  for (int j = lane; j + 1 < g.P; j += 32)
-    res += 0.5 * m[(size_t)j * g.Ns + l] * w2 * spring2<D>(g, x, j, l, j + 1, l, image);
-  res = warp_sum(res);
-  // lane 0: the closing spring of l (E_l^(1)); lane 1: the link to l+1 (the
-  // increment of the prefix sums), both in one pass
-  if (lane < 2) {
-    const int b = lane == 0 ? l : (l + 1 < g.N ? l + 1 : l);
-    const double lk = link<D>(g, x, m, w2, l, b, image);
-    if (lane == 0) {
-      Eint[l] = res;
-      ENk[dtri(l + 1)] = res + lk;
-    } else if (l + 1 < g.N) {
-      gl[l] = res + lk;
-    }
-  }
+  eint_particle<D>(g, x, m, w2, image, Eint, ENk, gl, l, threadIdx.x & 31);
 }
 
 
@@ -522,7 +506,7 @@ __global__ void __launch_bounds__(256) k_enk_direct(Geo g, const double *__restr
   const int n1 = l1 - 1, n = n1 + (l2 > l1 ? l2 - 1 : 0);
   for (int e = threadIdx.x; e < n; e += blockDim.x) {
     const int l = e < n1 ? l1 : l2, k = 2 + (e < n1 ? e : e - n1);  // 1-based row, cycle length
-    ENk[dtri(l) + k - 1] = Eint[l - 1] + ((G[l - 1] - G[l - k]) + link<D>(g, x, m, w2, l - 1, l - k, image));
+    enk_entry<D>(g, x, m, w2, image, Eint, G, ENk, l, k);
   }
 }
 
@@ -1247,7 +1231,7 @@ static cudaError_t tri_solve(int N, double beta, const TriJob &job, int first, i
   return XK_LAUNCHED();
 }
 
-static TriJob tri_job(int N, double *rs_f, double *rs_b, double *VBN, double *tmpV) {
+TriJob tri_job(int N, double *rs_f, double *rs_b, double *VBN, double *tmpV) {
   TriJob j{};
   const size_t boff = ntri(N) + (ntri(N) + 1) / 2 + 1;
   const size_t nb = (size_t)((N + TS_CHUNK - 1) / TS_CHUNK) * TS_CHUNK * TS_CHUNK;
@@ -1369,22 +1353,8 @@ __global__ void k_fill_g_ext(int N, const double *__restrict__ Mm, const int *__
                              const double *__restrict__ Xfm, const int *__restrict__ Xfe,
                              const double *__restrict__ Xbm, const int *__restrict__ Xbe, double *__restrict__ G) {
   const int l = blockIdx.y + 1;  // 1-based row
-  // X'_{N-l} / X_N, as a mantissa and an exponent
-  const double q = Xbm[N - l] / Xfm[N];
-  const int qe = Xbe[N - l] - Xfe[N];
-  for (int j = blockIdx.x * blockDim.x + threadIdx.x + 1; j <= N; j += gridDim.x * blockDim.x) {
-    double gv;
-    if (j > l + 1) {
-      gv = 0;
-    } else if (j == l + 1) {
-      gv = 1 - ext_val(Xfm[l] * q, Xfe[l] + qe);
-    } else {
-      const size_t o = moff(l, j - 1);
-      const double w = Mm[o];
-      gv = w == 0.0 ? 0.0 : ext_val(w * Xfm[j - 1] * q, Me[o] + Xfe[j - 1] + qe);
-    }
-    G[(size_t)(l - 1) * N + (j - 1)] = gv;
-  }
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x + 1; j <= N; j += gridDim.x * blockDim.x)
+    g_ext_elem(N, Mm, Me, Xfm, Xfe, Xbm, Xbe, G, l, j);
 }
 
 cudaError_t fill_g_ext(int N, const double *rs_f, const double *rs_b, double *G, cudaStream_t st) {
@@ -1412,11 +1382,7 @@ __global__ void k_spring_interior(Geo g, const double *__restrict__ x,
   if (P2 <= 0 || t >= (size_t)P2 * g.Ns) return;
   const int l = (int)(t % g.Ns), j = (int)(t / g.Ns) + 1;  // 0-based bead index 1..P-2
   if (l >= g.N) return;
-  const double mm = m[(size_t)j * g.Ns + l];
-  double gr[D];
-  grad2<D>(g, x, mm * w2, j, l, j + 1, l, j - 1, l, image, gr);
-#pragma unroll
-  for (int d = 0; d < D; ++d) f[sidx(j, d, l, D, g.Ns)] += -gr[d] / mm;
+  spring_interior_bead<D>(g, x, m, w2, image, f, j, l);
 }
 
 // bead 1 and bead P of every particle, weighted by G.  Block (32 x 8)
@@ -1427,78 +1393,8 @@ template <int D>
 __global__ void k_exch_ends(Geo g, const double *__restrict__ x, const double *__restrict__ m,
                             double w2, int image, const double *__restrict__ G,
                             double *__restrict__ scratch, int nsplit) {
-  __shared__ double red[EX_TY][2 * D][32];
-  const int l = blockIdx.x * 32 + threadIdx.x;
-  const int js = blockIdx.y;
-  const int N = g.N, jP = g.P - 1;
-  double a1[D], aP[D];
-#pragma unroll
-  for (int d = 0; d < D; ++d) a1[d] = aP[d] = 0;
-  if (l < N) {
-    const double m1 = m[l], mP = m[(size_t)jP * g.Ns + l];
-    // The reference adds G-weighted gradients of both springs at the end
-    // bead for every partner q; the spring inside the ring (bead 1 -> 2,
-    // bead P -> P-1) does not depend on q, so it is weighted once by the sum
-    // of the weights and only the partner spring is evaluated per q (equal
-    // to rounding).
-    double x1[D], xP[D], s1 = 0.0, sP = 0.0;
-#pragma unroll
-    for (int d = 0; d < D; ++d) {
-      x1[d] = x[sidx(0, d, l, D, g.Ns)];
-      xP[d] = x[sidx(jP, d, l, D, g.Ns)];
-    }
-    // partner q runs over this block's part of 0..N-1
-    for (int q = js * EX_TY + threadIdx.y; q < N; q += nsplit * EX_TY) {
-      // bead 1 of l, previous bead = bead P of q, weight G[q][l]
-      const double g1 = G[(size_t)q * N + l];
-      if (g1 != 0.0) {
-        s1 += g1;
-#pragma unroll
-        for (int d = 0; d < D; ++d) {
-          double c = x1[d] - x[sidx(jP, d, q, D, g.Ns)];
-          if (image) c = min_image(c, g.box[d], g.inv_box[d]);
-          a1[d] = fma(g1, c, a1[d]);
-        }
-      }
-      // bead P of l, next bead = bead 1 of q, weight G[l][q]
-      const double gP = G[(size_t)l * N + q];
-      if (gP != 0.0) {
-        sP += gP;
-#pragma unroll
-        for (int d = 0; d < D; ++d) {
-          double c = xP[d] - x[sidx(0, d, q, D, g.Ns)];
-          if (image) c = min_image(c, g.box[d], g.inv_box[d]);
-          aP[d] = fma(gP, c, aP[d]);
-        }
-      }
-    }
-    const double k1 = m1 * w2, kP = mP * w2;
-#pragma unroll
-    for (int d = 0; d < D; ++d) {
-      double a = x1[d] - x[sidx(1, d, l, D, g.Ns)];
-      double b = xP[d] - x[sidx(jP - 1, d, l, D, g.Ns)];
-      if (image) {
-        a = min_image(a, g.box[d], g.inv_box[d]);
-        b = min_image(b, g.box[d], g.inv_box[d]);
-      }
-      a1[d] = k1 * (s1 * a + a1[d]);
-      aP[d] = kP * (sP * b + aP[d]);
-    }
-  }
-#pragma unroll
-  for (int d = 0; d < D; ++d) {
-    red[threadIdx.y][d][threadIdx.x] = a1[d];
-    red[threadIdx.y][D + d][threadIdx.x] = aP[d];
-  }
-  __syncthreads();
-  if (threadIdx.y == 0 && l < N) {
-#pragma unroll
-    for (int q = 0; q < 2 * D; ++q) {
-      double s = 0;
-      for (int y = 0; y < EX_TY; ++y) s += red[y][q][threadIdx.x];
-      scratch[((size_t)js * 2 * D + q) * g.Ns + l] = s;
-    }
-  }
+  __shared__ double red[EX_TY * 2 * D * 32];
+  exch_ends_block<D>(g, x, m, w2, image, G, scratch, nsplit, blockIdx.x, blockIdx.y, threadIdx.x, threadIdx.y, red);
 }
 
 template <int D>
@@ -3425,89 +3321,7 @@ __global__ void __launch_bounds__(256, 3) k_pair_tiles32(Geo g, P32 q, const flo
   // persistent warps: tile jobs (slice j, tile pair I <= J) in round-robin,
   // warps numbered across blocks first (the last round spreads over all SMs)
   for (int wi = (threadIdx.x >> 5) * gridDim.x + blockIdx.x; wi < jobs * g.P; wi += nwarps) {
-    const int j = wi / jobs;
-    int job = wi % jobs, I = 0;
-    while (job >= T - I) {
-      job -= T - I;
-      ++I;
-    }
-    const int J = I + job;
-    const int a = I * 32 + lane, b0 = J * 32 + lane;
-    const bool va = a < g.N, vb = b0 < g.N;
-    float xa[D], xb[D], fa[D], fb[D];
-#pragma unroll
-    for (int d = 0; d < D; ++d) {
-      xa[d] = va ? x[sidx(j, d, a, D, g.Ns)] : 0.f;
-      xb[d] = vb ? x[sidx(j, d, b0, D, g.Ns)] : 0.f;
-      fa[d] = fb[d] = 0.f;
-    }
-    const int src = (lane + 1) & 31;
-    if (q.uniform) {
-      for (int s = 0; s < 32; ++s) {
-        const int bi = J * 32 + ((lane + s) & 31);
-        if (va && bi < g.N && (I != J || a > bi)) {
-          float dx[D], F[D];
-#pragma unroll
-          for (int d = 0; d < D; ++d) dx[d] = xa[d] - xb[d];
-          pair_eval32<D, KIND>(q, dx, F);
-#pragma unroll
-          for (int d = 0; d < D; ++d) {
-            fa[d] += F[d];
-            fb[d] -= F[d];
-          }
-        }
-#pragma unroll
-        for (int d = 0; d < D; ++d) {
-          xb[d] = __shfl_sync(FULL, xb[d], src);
-          fb[d] = __shfl_sync(FULL, fb[d], src);
-        }
-      }
-#pragma unroll
-      for (int d = 0; d < D; ++d) {
-        fa[d] *= q.im0;
-        fb[d] *= q.im0;
-      }
-    } else {
-      const float ima = va ? im[(size_t)j * g.Ns + a] : 1.f;
-      float imb = vb ? im[(size_t)j * g.Ns + b0] : 1.f;
-      for (int s = 0; s < 32; ++s) {
-        const int bi = J * 32 + ((lane + s) & 31);
-        if (va && bi < g.N && (I != J || a > bi)) {
-          float dx[D], F[D];
-#pragma unroll
-          for (int d = 0; d < D; ++d) dx[d] = xa[d] - xb[d];
-          pair_eval32<D, KIND>(q, dx, F);
-          // the reference divides by the mass of the higher-index particle
-          const float inv = a > bi ? ima : imb;
-#pragma unroll
-          for (int d = 0; d < D; ++d) {
-            fa[d] = fmaf(F[d], inv, fa[d]);
-            fb[d] = fmaf(-F[d], inv, fb[d]);
-          }
-        }
-#pragma unroll
-        for (int d = 0; d < D; ++d) {
-          xb[d] = __shfl_sync(FULL, xb[d], src);
-          fb[d] = __shfl_sync(FULL, fb[d], src);
-        }
-        imb = __shfl_sync(FULL, imb, src);
-      }
-    }
-    if (I == J) {
-      if (va) {
-#pragma unroll
-        for (int d = 0; d < D; ++d) out[(((size_t)I * g.P + j) * D + d) * g.Ns + a] = fa[d] + fb[d];
-      }
-    } else {
-      if (va) {
-#pragma unroll
-        for (int d = 0; d < D; ++d) out[(((size_t)J * g.P + j) * D + d) * g.Ns + a] = fa[d];
-      }
-      if (vb) {
-#pragma unroll
-        for (int d = 0; d < D; ++d) out[(((size_t)I * g.P + j) * D + d) * g.Ns + b0] = fb[d];
-      }
-    }
+    pair_tile32_job<D, KIND>(g, q, x, im, out, T, jobs, wi, lane);
   }
 }
 
@@ -3580,12 +3394,8 @@ static cudaError_t launch_pair32(const Geo &g, const P32 &q, const float *x, con
   return cudaSuccess;
 }
 
-cudaError_t pair_force32(const Geo &g, const PairPrm &p, const double *x, const double *m, double *f,
-                         double *scratch, cudaStream_t st) {
-  const int T = (g.N + 31) / 32;
-  const int jobs = T * (T + 1) / 2;
-  int wpb = pair32_warps(p.kind, g.D, g.N, g.P);
-  if (wpb != 1 && wpb != 2 && wpb != 4 && wpb != 8) wpb = 8;
+// the FP32 pair kernel's constants for a system and potential
+P32 make_p32(const Geo &g, const PairPrm &p) {
   P32 q{};
   for (int d = 0; d < 3; ++d) {
     q.L[d] = (float)g.box[d];
@@ -3603,6 +3413,16 @@ cudaError_t pair_force32(const Geo &g, const PairPrm &p, const double *x, const 
   if (p.kind == PAIR_EWALD_REAL && rc32 <= fmin(g.box[0], fmin(g.box[1], g.box[2]))) q.kmax = 0;
   q.uniform = p.inv_mass > 0;
   q.im0 = (float)p.inv_mass;
+  return q;
+}
+
+cudaError_t pair_force32(const Geo &g, const PairPrm &p, const double *x, const double *m, double *f,
+                         double *scratch, cudaStream_t st) {
+  const int T = (g.N + 31) / 32;
+  const int jobs = T * (T + 1) / 2;
+  int wpb = pair32_warps(p.kind, g.D, g.N, g.P);
+  if (wpb != 1 && wpb != 2 && wpb != 4 && wpb != 8) wpb = 8;
+  const P32 q = make_p32(g, p);
   // scratch: T * slots float partials (room for twice that is reserved),
   // then the FP32 positions and inverse masses
   float *part = (float *)scratch;
@@ -3659,24 +3479,7 @@ cudaError_t pair_force32(const Geo &g, const PairPrm &p, const double *x, const 
 __global__ void k_phase32(Geo g, int ns, const double *__restrict__ x, float2 *__restrict__ ph32) {
   const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (size_t)g.P * 3 * g.Ns) return;
-  const int l = (int)(t % g.Ns);
-  const int jd = (int)(t / g.Ns);  // j*3 + d
-  const int d = jd % 3;
-  float s1 = 0.f, c1 = 1.f;
-  if (l < g.N) {
-    double u = x[t] * g.inv_box[d];
-    u -= rint(u);  // in [-1/2, 1/2]
-    sincospif((float)(2.0 * u), &s1, &c1);
-  }
-  float re = 1.f, im = 0.f;
-  float2 *o = ph32 + (size_t)jd * (ns + 1) * g.Ns + l;
-  o[0] = make_float2(1.f, 0.f);
-  for (int n = 1; n <= ns; ++n) {
-    const float r2 = fmaf(re, c1, -im * s1), i2 = fmaf(re, s1, im * c1);
-    re = r2;
-    im = i2;
-    o[(size_t)n * g.Ns] = make_float2(re, im);
-  }
+  phase32_slot(g, ns, x, ph32, t);
 }
 
 
@@ -3755,30 +3558,11 @@ __global__ void __launch_bounds__(COLS * GR) k_sk32(Geo g, const float2 *__restr
 template <int NS>
 __global__ void k_recip_tables32(const int4 *__restrict__ cols, int ncol, const double2 *__restrict__ S,
                                  const double *__restrict__ coef, int nk, float2 *__restrict__ T) {
-  constexpr int NT = 4 * NS + 1;
   const int j = blockIdx.y;
   const int ci = blockIdx.x * blockDim.y + threadIdx.y;
   const int n = threadIdx.x;
   if (ci >= ncol || n > NS) return;
-  const int4 c = cols[ci];
-  auto W = [&](int nz) {
-    if (nz < c.z) return make_double2(0.0, 0.0);
-    const int k = c.w + (nz - c.z);
-    const double2 s = S[(size_t)j * nk + k];
-    return make_double2(coef[k] * s.x, -coef[k] * s.y);
-  };
-  float2 *o = T + ((size_t)j * ncol + ci) * NT;
-  if (n == 0) {
-    const double2 w = W(0);
-    o[0] = make_float2((float)w.x, (float)w.y);
-  } else {
-    const double2 wp = W(n), wm = W(-n);
-    const double Ar = wp.x + wm.x, Ai = wp.y + wm.y, Br = wp.x - wm.x, Bi = wp.y - wm.y;
-    o[4 * n - 3] = make_float2((float)Ar, (float)Ai);
-    o[4 * n - 2] = make_float2((float)Br, (float)Bi);
-    o[4 * n - 1] = make_float2((float)(n * Ar), (float)(n * Ai));
-    o[4 * n] = make_float2((float)(n * Br), (float)(n * Bi));
-  }
+  recip_table32_entry(cols, ncol, S, coef, nk, T, NS, j, ci, n);
 }
 
 template <int NS>

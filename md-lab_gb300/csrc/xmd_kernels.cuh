@@ -298,4 +298,46 @@ cudaError_t pair_hist(const Geo &g, const double *x, int jb, int points, double 
 // f[i] += a[i], i < n
 cudaError_t add_into(double *f, const double *a, size_t n, cudaStream_t st);
 
+// ---- persistent ensemble step (xmd_ensemble.cu) ----
+// One system's step as the persistent kernel runs it: the reference driver's
+// sequence md_update_nhc_VV3_1_x, md_reset_force_x, md_pimd_fast_fill_ENk_x,
+// md_pimd_fill_VB_x, md_pimd_fast_fill_force_VB_x, [trap force], [pair
+// force, FP32 form], md_update_nhc_VV3_2_x, [md_periodic_boundary_x], with
+// the arithmetic of those calls.  Pointers are the system's device buffers.
+struct EnsSysDesc {
+  Geo g;
+  int image;      // minimum image in the springs (the ENk / force calls' flag)
+  int wrap;       // periodic boundary at the end of the step
+  int trap_kind;  // 0: no trap force
+  TrapPrm tp;
+  int pair_kind;  // 0: no pair force
+  PairPrm pp;     // cut-off, image shifts and inverse mass set as for the force call
+  double kT, h, beta, vi, w2;
+  double *x, *v, *f, *m, *th, *vt;
+  const double *Q, *iQ;
+  double *fex;    // exchange spring forces (slots)
+  double *xscr;   // partial sums of the end-bead forces (exch_scratch_doubles)
+  double *Eint, *ENk, *gl;
+  const double *lnn;
+  double *VBN, *tmpV, *G;
+  double *rs_f, *rs_b;  // recursion scratch, rec_scratch_doubles(N) each
+  Recip rc;             // Ewald tables (pair_kind == PAIR_EWALD_REAL, D = 3)
+  double inv_mP;        // 1 / (m P) of the reciprocal forces
+};
+struct EnsLaunch {
+  void *plan = nullptr;  // device descriptors and the clusters' system lists
+  int D = 0, L = 0, cluster = 0, clusters = 0, nsys = 0;
+  size_t smem = 0;
+};
+// thread blocks per cluster the kernel can run with (1, 2, 4, 8); the
+// number of clusters of that size that stay resident (0: none fits)
+int ensemble_resident_clusters(int D, int L, int cluster);
+// the systems spread over the resident clusters by estimated cost (longest
+// first, each to the least loaded cluster); descriptors uploaded to e.plan
+cudaError_t ensemble_prepare(const EnsSysDesc *sys, int n, int D, int L, int cluster, EnsLaunch &e);
+cudaError_t ensemble_launch(const EnsLaunch &e, cudaStream_t st);
+void ensemble_free(EnsLaunch &e);
+// the supported shapes: N <= ENS_MAX_N, L in {4, 8}, D in 1..3, n_sum <= 11
+constexpr int ENS_MAX_N = 2048;
+
 }  // namespace xk

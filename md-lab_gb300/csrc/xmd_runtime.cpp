@@ -320,6 +320,7 @@ static xk::Geo make_geo(md_simulation_t_x *sim) {
 // ------------------------------------------------------------------
 int sim_device(md_simulation_t_x *sim, SimDev **out) {
   if (!sim || !sim->particles || sim->N < 1) return fail(MD_GB_ERR_ARG, "invalid simulation");
+  if (ens_recording()) XMD_TRY(ens_refuse());
   XMD_TRY(ensure_device());
   XMD_TRY(join_side());
   SimDev *d = lookup(g_sim, sim, true);
@@ -496,6 +497,7 @@ int scratch(SimDev *sd, size_t doubles, double **out) {
 // ------------------------------------------------------------------
 int pimd_device(md_pimd_t_x *pimd, SimDev **sd, PimdDev **pd) {
   if (!pimd || !pimd->sim) return fail(MD_GB_ERR_ARG, "invalid path-integral state");
+  if (ens_recording()) XMD_TRY(ens_refuse());
   if (pimd->N < 1 || pimd->P < 1 || pimd->N * pimd->P != pimd->sim->N)
     return fail(MD_GB_ERR_ARG, "N*P (%d*%d) does not match the simulation's %d beads", pimd->N,
                 pimd->P, pimd->sim->N);
@@ -599,7 +601,44 @@ using namespace xmd;
 struct md_gb300_graph {
   cudaGraph_t g = nullptr;
   cudaGraphExec_t e = nullptr;
+  void (*release)(void *) = nullptr;  // frees what the graph's kernels read (owned)
+  void *owned = nullptr;
 };
+
+namespace xmd {
+
+int capture_single(cudaError_t (*launch)(void *), void *ctx, void (*release)(void *), md_gb300_graph_t_x **out) {
+  if (capturing()) {
+    release(ctx);
+    return fail(MD_GB_ERR_CAPTURE, "already capturing");
+  }
+  cudaError_t e = cudaStreamBeginCapture(stream(), cudaStreamCaptureModeThreadLocal);
+  cudaGraph_t g = nullptr;
+  if (e == cudaSuccess) {
+    e = launch(ctx);
+    const cudaError_t ee = cudaStreamEndCapture(stream(), &g);
+    if (e == cudaSuccess) e = ee;
+  }
+  md_gb300_graph *gr = nullptr;
+  if (e == cudaSuccess) {
+    gr = new md_gb300_graph();
+    gr->g = g;
+    e = cudaGraphInstantiate(&gr->e, g, 0);
+  }
+  if (e != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    delete gr;
+    release(ctx);
+    cudaGetLastError();
+    return cuda_fail(e, "single-launch capture");
+  }
+  gr->release = release;
+  gr->owned = ctx;
+  *out = gr;
+  return 0;
+}
+
+}  // namespace xmd
 
 extern "C" {
 
@@ -758,6 +797,7 @@ void md_gb300_graph_free_x(md_gb300_graph_t_x *gr) {
   if (!gr) return;
   if (gr->e) cudaGraphExecDestroy(gr->e);
   if (gr->g) cudaGraphDestroy(gr->g);
+  if (gr->release) gr->release(gr->owned);
   delete gr;
 }
 

@@ -123,6 +123,7 @@ extern "C" {
 // integrator: md_simulation_x.c:421-472, :615-792, :794-856
 // ------------------------------------------------------------------
 int md_reset_force_x(md_simulation_t_x *sim) {
+  if (ens_recording()) return ens_record(ENS_RESET, sim, nullptr, 0, 0, nullptr);
   SimDev *sd;
   XMD_TRY(sim_device(sim, &sd));
   XMD_CUDA(xk::zero(sd->f.as<double>(), sd->geo.slots(), stream()));
@@ -130,6 +131,7 @@ int md_reset_force_x(md_simulation_t_x *sim) {
 }
 
 static int nhc(md_simulation_t_x *sim, md_num_t_x h, int half) {
+  if (ens_recording()) return ens_record(half == 1 ? ENS_NHC1 : ENS_NHC2, sim, nullptr, h, 0, nullptr);
   SimDev *sd;
   const double *fex;  // exchange forces still to be added to f, if any
   XMD_TRY(sim_device_fex(sim, &sd, &fex));
@@ -148,6 +150,7 @@ int md_update_nhc_VV3_2_x(md_simulation_t_x *sim, md_num_t_x h) { return nhc(sim
 
 int md_periodic_boundary_x(md_simulation_t_x *sim) {
   if (!sim || !sim->box || sim->box->type != MD_ND_RECT_BOX_X) return 0;
+  if (ens_recording()) return ens_record(ENS_WRAP, sim, nullptr, 0, 0, nullptr);
   SimDev *sd;
   XMD_TRY(sim_device(sim, &sd));
   XMD_CUDA(xk::wrap_box(sd->geo, sd->x.as<double>(), stream()));
@@ -272,6 +275,7 @@ int md_pimd_init_particle_uniform_pos_x(md_pimd_t_x *p, md_num_t_x *center, md_n
 // exchange: md_pimd_x.c:593-665, :814-953, :997-1109, :1969-2210, :2369-2721
 // ------------------------------------------------------------------
 int md_pimd_fast_fill_ENk_x(md_pimd_t_x *pimd, int image) {
+  if (ens_recording()) return ens_record(ENS_ENK, nullptr, pimd, 0, image, nullptr);
   // on the library stream: on the side stream its many small blocks would
   // compete with the structure-factor kernels that start the pair forces,
   // which costs more than the overlap gains
@@ -290,6 +294,7 @@ int md_pimd_fast_fill_ENk_x(md_pimd_t_x *pimd, int image) {
 int md_pimd_fill_ENk_x(md_pimd_t_x *pimd, int image) { return md_pimd_fast_fill_ENk_x(pimd, image); }
 
 int md_pimd_fill_VB_x(md_pimd_t_x *pimd) {
+  if (ens_recording()) return ens_record(ENS_VB, nullptr, pimd, 0, 0, nullptr);
   NoJoin nj;  // the exchange chain starts on the side stream here
   SimDev *sd;
   PimdDev *pd;
@@ -314,6 +319,7 @@ int md_pimd_fill_VB_x(md_pimd_t_x *pimd) {
 }
 
 int md_pimd_fast_fill_force_VB_x(md_pimd_t_x *pimd, int image) {
+  if (ens_recording()) return ens_record(ENS_FVB, nullptr, pimd, 0, image, nullptr);
   // continues the side stream after md_pimd_fill_VB_x (no join): G and the
   // exchange spring forces are computed there, into sd->fex, which the next
   // join adds to f
@@ -361,6 +367,7 @@ int md_pimd_fill_force_VB_x(md_pimd_t_x *pimd, int image) { return md_pimd_fast_
 // external forces: md_pimd_x.c:1297-1391, :1527-1677
 // ------------------------------------------------------------------
 int md_pimd_calc_trap_force_x(md_pimd_t_x *pimd, md_trap_force_t_x tf) {
+  if (ens_recording()) return ens_record(ENS_TRAP, nullptr, pimd, 0, 0, (const void *)tf);
   NoJoin nj;  // adds to f only: may overlap the side stream's exchange work
   const int kind = trap_kind_of((const void *)tf, false);
   if (!kind) return fail(MD_GB_ERR_UNSUPPORTED, "trap force function has no device kernel");
@@ -447,9 +454,18 @@ void xmd::ewald_shifts(xk::PairPrm &p, const xk::Geo &g) {
   }
 }
 
+xk::PairPrm xmd::force_params(int kind, const SimDev *sd) {
+  xk::PairPrm prm = pair_params(kind);
+  ewald_shifts(prm, sd->geo);  // the alpha L limit is the energies' (the longer cut-off)
+  prm.inv_mass = sd->uniform_mass ? 1.0 / sd->mass0 : 0.0;
+  if (kind == xk::PAIR_EWALD_REAL && prm.alpha > 0) prm.rcut = EWALD_XCUT_FORCE / prm.alpha;
+  return prm;
+}
+
 extern "C" {
 
 int md_pimd_calc_pair_force_x(md_pimd_t_x *pimd, md_pair_force_t_x pf) {
+  if (ens_recording()) return ens_record(ENS_PAIR, nullptr, pimd, 0, 0, (const void *)pf);
   NoJoin nj;  // adds to f only: may overlap the side stream's exchange work
   const int kind = pair_kind_of((const void *)pf, false);
   if (!kind) return fail(MD_GB_ERR_UNSUPPORTED, "pair force function has no device kernel");
@@ -463,11 +479,8 @@ int md_pimd_calc_pair_force_x(md_pimd_t_x *pimd, md_pair_force_t_x pf) {
   double *scr = scratch_for(sd, general_scratch(sd->geo), &rc);
   if (rc) return rc;
   cudaStream_t st = stream();
-  xk::PairPrm prm = pair_params(kind);
-  ewald_shifts(prm, sd->geo);  // the alpha L limit is the energies' (the longer cut-off)
-  prm.inv_mass = sd->uniform_mass ? 1.0 / sd->mass0 : 0.0;
+  xk::PairPrm prm = force_params(kind, sd);
   const bool mixed = g_precision == MD_GB_PRECISION_MIXED;
-  if (kind == xk::PAIR_EWALD_REAL && prm.alpha > 0) prm.rcut = EWALD_XCUT_FORCE / prm.alpha;
   int learned = 0;
   if (kind == xk::PAIR_EWALD_REAL) {
     if (prm.kmax[0] > 1 || prm.kmax[1] > 1 || prm.kmax[2] > 1)

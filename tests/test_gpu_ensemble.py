@@ -1,6 +1,6 @@
 """Ensembles: several independent systems advanced by one CUDA graph (one
-launch per step, each system on its own branch), and the tile-shape
-autotuner of the FP32 pair kernel.  The ensemble must give bit-for-bit the
+launch per step, each system on its own branch, or one persistent kernel for
+all of them), and the tile-shape autotuners.  The ensemble must give bit-for-bit the
 states that stepping each system on its own gives; the autotuner's choice
 must not change any force."""
 import ctypes as C
@@ -11,6 +11,7 @@ import pytest
 
 import xmd_x
 from gpu_common import random_state
+from helpers import relerr
 
 pytestmark = pytest.mark.gpu
 
@@ -155,3 +156,128 @@ def test_fp64_autotuner_keeps_parity(lib):
                                  orc.C.byref(prm))
         assert_close(forces(), o.f, 1e-10, "tuned FP64 forces vs the oracle")
         s.free()
+
+
+# uneven systems for the persistent kernel: traps with Gaussian repulsion and
+# electron gases (Ewald |n| <= 4 and 8), N from 8 to 160 (more than one
+# staged chunk of 128 particles, five 32-row chunks of the recursion), P from
+# 2 to 32, xi from 0 to 1
+PERSISTENT = [("trap", 8, 16, 1.0, 2.0, 0), ("ueg", 16, 8, 0.5, 1.0, 4), ("trap", 12, 32, 0.25, 4.0, 0),
+              ("ueg", 24, 16, 0.75, 3.0, 8), ("ueg", 40, 4, 0.0, 2.0, 8), ("trap", 70, 8, 1.0, 5.0, 0),
+              ("ueg", 160, 2, 1.0, 1.5, 4), ("trap", 33, 3, 0.5, 8.0, 0)]
+
+
+def persistent_step(lib, spec, s, box):
+    kind, nsum = spec[0], spec[5]
+    if kind == "ueg":
+        xmd_x.set_potentials(lib, coul_s=1.0, alpha=5.6 / box, nsum=nsum)
+        xmd_x.md_step(lib, s, 0.05, image=1, pair=lib.fn("md_coulomb_3d_ewald_force_x"), pbc=True)
+    else:
+        xmd_x.set_potentials(lib, trap_w=1.0, gauss_g=0.75 * math.pi, gauss_s=0.5)
+        xmd_x.md_step(lib, s, 0.005, trap=lib.fn("md_harmonic_trap_force_x"), pair=lib.fn("md_gaussian_force_x"))
+
+
+def _persistent_pair(lib):
+    ens = [make(lib, sp[:5], 300 + i) for i, sp in enumerate(PERSISTENT)]
+    ref = [make(lib, sp[:5], 300 + i) for i, sp in enumerate(PERSISTENT)]
+    for (s, box), sp in zip(ens + ref, PERSISTENT + PERSISTENT):
+        persistent_step(lib, sp, s, box)  # device state and Ewald tables exist before planning
+
+    def cb(i, ctx):
+        try:
+            s, box = ens[i]
+            persistent_step(lib, PERSISTENT[i], s, box)
+            return 0
+        except Exception:
+            return -1
+
+    return ens, ref, STEP_FN(cb)
+
+
+def test_persistent_ensemble_matches_individual_steps(lib):
+    """One persistent launch per step against the same steps made by the
+    per-system calls: positions, velocities, thermostats, forces, V_B and the
+    primitive estimator after 3 steps."""
+    lib.check(lib.md_gb300_set_precision_x(1))
+    try:
+        ens, ref, fn = _persistent_pair(lib)
+        g = C.c_void_p()
+        lib.check(lib.md_gb300_capture_ensemble_persistent_x(len(PERSISTENT), C.cast(fn, C.c_void_p), None,
+                                                             C.byref(g)), "persistent capture")
+        assert lib.md_gb300_graph_kernel_count_x(g) == 1
+        lib.check(lib.md_gb300_graph_launch_x(g, 3))
+        lib.check(lib.md_gb300_synchronize_x())
+        for _ in range(3):
+            for (s, box), sp in zip(ref, PERSISTENT):
+                persistent_step(lib, sp, s, box)
+        worst = {}
+        for (a, _), (b, _), sp in zip(ens, ref, PERSISTENT):
+            sa, sb = a.state(), b.state()
+            for k in ("x", "v", "theta", "vtheta", "f"):
+                worst[k] = max(worst.get(k, 0.0), relerr(sa[k], sb[k]))
+            ea, eb = a.exchange(), b.exchange()
+            for k in ("ENk", "VBN"):
+                worst[k] = max(worst.get(k, 0.0), relerr(ea[k], eb[k]))
+            est = []
+            for s in (a, b):
+                lib.check(lib.md_pimd_calc_VBN_energy_x(s.pimd, s.stats))
+                est.append(s.take_energy())
+            worst["E_primitive"] = max(worst.get("E_primitive", 0.0), abs(est[0] - est[1]) / abs(est[1]))
+        print("persistent vs per-system, largest relative differences:", worst)
+        for k in ("x", "v", "theta", "vtheta", "ENk", "VBN", "E_primitive"):
+            assert worst[k] <= 1e-12, (k, worst[k])
+        assert worst["f"] <= 1e-9, worst["f"]
+        lib.md_gb300_graph_free_x(g)
+        for s, _ in ens + ref:
+            s.free()
+    finally:
+        lib.check(lib.md_gb300_set_precision_x(0))
+
+
+def test_persistent_ensemble_autotuner_and_refusals(lib):
+    """The cluster-size autotuner picks a size that runs; the capture then
+    uses it and still matches the per-system calls.  A step with a call that
+    is not part of the reference driver's step, or in FP64 mode, is refused."""
+    lib.check(lib.md_gb300_set_precision_x(1))
+    try:
+        ens, ref, fn = _persistent_pair(lib)
+        cl, ms = C.c_int(), C.c_double()
+        lib.check(lib.md_gb300_autotune_ensemble_x(len(PERSISTENT), C.cast(fn, C.c_void_p), None, 2, C.byref(cl),
+                                                   C.byref(ms)), "ensemble autotune")
+        assert cl.value in (1, 2, 4, 8) and ms.value > 0
+        # the autotuner advanced every system by 4 x (2 + 1) steps
+        for _ in range(4 * 3):
+            for (s, box), sp in zip(ref, PERSISTENT):
+                persistent_step(lib, sp, s, box)
+        g = C.c_void_p()
+        lib.check(lib.md_gb300_capture_ensemble_persistent_x(len(PERSISTENT), C.cast(fn, C.c_void_p), None,
+                                                             C.byref(g)), "persistent capture")
+        lib.check(lib.md_gb300_graph_launch_x(g, 2))
+        for _ in range(2):
+            for (s, box), sp in zip(ref, PERSISTENT):
+                persistent_step(lib, sp, s, box)
+        for (a, _), (b, _) in zip(ens, ref):
+            sa, sb = a.state(), b.state()
+            assert relerr(sa["x"], sb["x"]) <= 1e-12
+            assert relerr(sa["f"], sb["f"]) <= 1e-9
+        lib.md_gb300_graph_free_x(g)
+
+        def bad(i, ctx):
+            s, box = ens[i]
+            r = lib.md_update_nhc_VV3_1_x(s.sim, 0.01)
+            if r:
+                return r
+            return lib.md_pimd_calc_VBN_energy_x(s.pimd, s.stats)  # not a step call
+
+        bad_fn = STEP_FN(bad)
+        assert lib.md_gb300_capture_ensemble_persistent_x(1, C.cast(bad_fn, C.c_void_p), None, C.byref(g)) != 0
+        lib.check(lib.md_gb300_set_precision_x(0))
+        assert lib.md_gb300_capture_ensemble_persistent_x(len(PERSISTENT), C.cast(fn, C.c_void_p), None,
+                                                          C.byref(g)) != 0
+        # the refusals left no recording behind: ordinary calls work
+        for (s, box), sp in zip(ens, PERSISTENT):
+            persistent_step(lib, sp, s, box)
+        for s, _ in ens + ref:
+            s.free()
+    finally:
+        lib.check(lib.md_gb300_set_precision_x(0))
