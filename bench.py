@@ -590,7 +590,7 @@ def ensemble_form(lib, R, args):
     kernels = lib.md_gb300_graph_kernel_count_x(g)
     beads = sum(n * p for _, n, p, _, _ in specs)
     nst = max(args.steps, 10)
-    ms, wall, clocks = R.time([R.launcher(g)] * nst, [R.launcher(g)] * 3)
+    ms, wall_br, clocks = R.time([R.launcher(g)] * nst, [R.launcher(g)] * 3)
     # the same 64 steps as separate graphs, one after the other
     singles = [R.capture(lambda i=i: one(i))[0] for i in range(len(systems))]
 
@@ -602,7 +602,7 @@ def ensemble_form(lib, R, args):
     for gi in singles:
         lib.md_gb300_graph_free_x(gi)
     lib.md_gb300_graph_free_x(g)
-    # one persistent kernel per step: cluster size by the autotuner (which
+    # one persistent kernel per step: grid size by the autotuner (which
     # advances the systems by the steps it times), then captured
     ms_br, kernels_br = ms, kernels
     cl, tms = C.c_int(), C.c_double()
@@ -613,6 +613,12 @@ def ensemble_form(lib, R, args):
               "persistent ensemble capture")
     kernels = lib.md_gb300_graph_kernel_count_x(gp)
     ms, wall, clocks = R.time([R.launcher(gp)] * nst, [R.launcher(gp)] * 3)
+    lib.check(lib.md_gb300_ensemble_status_x(gp), "persistent ensemble status")
+    ph = (C.c_double * 9)()
+    lib.md_gb300_ensemble_phase_times_x(gp, ph, 9)
+    phase_us = {nm: round(v, 1) for nm, v in zip(
+        ("VV3_1", "springs_Eint_tiles_Sk", "prefix_tables", "ENk_recip", "weights_inverses_pairsum", "solves", "G",
+         "exch_ends", "VV3_2"), ph)}
     lib.md_gb300_graph_free_x(gp)
     for _, s, _ in systems:
         s.free()
@@ -621,7 +627,8 @@ def ensemble_form(lib, R, args):
     xmd_x.set_potentials(lib, coul_s=1.0, alpha=ALPHA_L / box, nsum=NSUM)
     return {"value": beads / (ms * 1e-3), "unit": "bead-steps/s", "ms_per_step": ms, "systems": len(specs),
             "bead_slots": beads, "kernels_per_launch": kernels, "steps_timed": nst,
-            "persistent_cluster_blocks": cl.value,
+            "persistent_blocks_per_sm": cl.value, "persistent_phase_us": phase_us, "autotuned_ms": tms.value, "wall_s_timed": wall,
+            "graph_branches_wall_s_timed": wall_br,
             "graph_branches_ms_per_step": ms_br, "graph_branches_kernels": kernels_br,
             "gain_vs_graph_branches": ms_br / ms,
             "sequential_graphs_ms_per_step": ms_seq, "gain_vs_sequential": ms_seq / ms,
@@ -845,7 +852,7 @@ def run_gb300(args, dist, rank, ws):
     for g in (g_conv, g_main):
         if g is not None:
             lib.md_gb300_graph_free_x(g)
-    kps = H.get("kernels_per_learned_step", H.get("kernels_per_step"))
+    kps = H.get("kernels_per_learned_step", H.get("kernels_per_step", H.get("kernels_per_launch", 0)))
     result = {"metric": METRIC, "value": H["value"], "unit": "bead-steps/s", "n_gpus": ws,
               "steps": H.get("steps_timed", args.steps), "warmup": args.warmup, "ms_per_step": H["ms_per_step"],
               "higher_is_better": True, "scaling": "weak", "vs_baseline": None,

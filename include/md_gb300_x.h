@@ -65,27 +65,41 @@ int md_gb300_graph_launch_x(md_gb300_graph_t_x *graph, int count);
 typedef int (*md_gb300_system_step_fn_x)(int system, void *ctx);
 int md_gb300_capture_ensemble_x(int n, md_gb300_system_step_fn_x step, void *ctx, md_gb300_graph_t_x **graph);
 /* The same ensemble step as ONE persistent kernel launch (captured into a
-   graph): thread-block clusters take the systems of a list balanced by
-   estimated cost and run each system's whole step, its stages separated by
-   cluster barriers.  While planning, step(i, ctx)'s calls do not launch;
-   each records its call and the md_set_* parameters of the moment.  Every
-   system's calls must be the reference driver's step, in this order:
-   md_update_nhc_VV3_1_x, md_reset_force_x, md_pimd_fast_fill_ENk_x,
-   md_pimd_fill_VB_x, md_pimd_fast_fill_force_VB_x, optionally
-   md_pimd_calc_trap_force_x and md_pimd_calc_pair_force_x,
+   graph): the step's stages are nine phases, each holding that stage's work
+   of every system spread over the whole GPU, separated by grid barriers
+   (a cooperative launch of exactly the blocks that fit; a barrier wait that
+   runs out, about a second, ends the kernel instead of hanging and is
+   reported by md_gb300_ensemble_status_x).  While planning, step(i, ctx)'s
+   calls do not launch; each records its call and the md_set_* parameters
+   of the moment.  Every system's calls must be the reference driver's step,
+   in this order: md_update_nhc_VV3_1_x, md_reset_force_x,
+   md_pimd_fast_fill_ENk_x, md_pimd_fill_VB_x, md_pimd_fast_fill_force_VB_x,
+   optionally md_pimd_calc_trap_force_x and md_pimd_calc_pair_force_x,
    md_update_nhc_VV3_2_x, optionally md_periodic_boundary_x; pair forces in
-   MD_GB_PRECISION_MIXED (FP32), one-DOF thermostat chains of length 4 or 8,
-   N <= 2048, no learned model attached.  Other calls are refused
-   (MD_GB_ERR_UNSUPPORTED).  The results equal those of the per-system calls
-   to rounding.  The cluster size is the one md_gb300_autotune_ensemble_x
-   chose for this ensemble's shapes, else 4 blocks. */
+   MD_GB_PRECISION_MIXED (FP32) with equal bead masses, one-DOF thermostat
+   chains of length 4 or 8, P >= 2, N <= 2048, no learned model attached.
+   Other calls are refused (MD_GB_ERR_UNSUPPORTED).  The results equal those
+   of the per-system calls.  The grid is the blocks per SM that
+   md_gb300_autotune_ensemble_x chose for this ensemble's shapes, else all
+   that fit. */
 int md_gb300_capture_ensemble_persistent_x(int n, md_gb300_system_step_fn_x step, void *ctx,
                                            md_gb300_graph_t_x **graph);
-/* Times the persistent step at cluster sizes 1, 2, 4 and 8 blocks (each
-   `repeats` + 1 launches, so the systems advance by those steps) and
-   records the fastest for this ensemble's shapes; *cluster and *ms (may be
-   NULL) receive it and its time per step. */
-int md_gb300_autotune_ensemble_x(int n, md_gb300_system_step_fn_x step, void *ctx, int repeats, int *cluster,
+/* 0 when every launch of a persistent ensemble graph so far completed its
+   barriers; MD_GB_ERR_CUDA when a barrier wait ran out.  Synchronises. */
+int md_gb300_ensemble_status_x(md_gb300_graph_t_x *graph);
+/* The last launch's phase durations in microseconds (up to n of them: the
+   thermostat's first half and force reset; springs, cycle-energy increments,
+   pair tiles and structure factors; prefix sums and force tables; cycle
+   energies and reciprocal forces; recursion weights, block inverses and the
+   pair sums; the two solves; G; the end-bead exchange forces; the second
+   half step), as one block saw them; returns the number of phases.
+   Synchronises. */
+int md_gb300_ensemble_phase_times_x(md_gb300_graph_t_x *graph, double *us, int n);
+/* Times the persistent step at each grid size that fits (1 or 2 blocks per
+   SM; `repeats` + 1 launches each, so the systems advance by those steps)
+   and records the fastest for this ensemble's shapes; *blocks_per_sm and *ms
+   (may be NULL) receive it and its time per step. */
+int md_gb300_autotune_ensemble_x(int n, md_gb300_system_step_fn_x step, void *ctx, int repeats, int *blocks_per_sm,
                                  double *ms);
 /* kernel nodes in a captured graph (kernels launched per replay) */
 int md_gb300_graph_kernel_count_x(md_gb300_graph_t_x *graph);

@@ -1206,4 +1206,116 @@ __device__ inline void exch_ends_block(const Geo &g, const double *__restrict__ 
   }
 }
 
+// ---- FP32 structure factors (mixed form) --------------------------------
+// An item is one kept wave-vector column (nx, ny) and SK_NG harmonics
+// nz = n0+1 .. n0+SK_NG (and nz = 0 when n0 = 0) of one bead slice.  The
+// particles' phase products are summed in FP32 over SK_PB particles at a
+// time, and each partial sum is added into double-float accumulators: the FP32
+// partial of at most 16 unit-size terms carries an error of ~1e-7 of a
+// term, the size of the FP32 phase factors' own rounding, at a sixth of
+// the arithmetic of a double-float addition per particle.
+constexpr int SK_NG = 4;   // harmonics per item
+constexpr int SK_PB = 16;  // particles per FP32 partial sum
+
+struct SkAcc {
+  DF s0r, s0i, P[SK_NG][2], Q[SK_NG][2];
+};
+
+// the item's sums over the staged particles 0 .. cnt-1 of a chunk (sp:
+// [3][ns+1][stride] phase factors; stride padded so that rows fall in
+// different banks): thread g of gr sharing the item takes particles
+// b + g, b + g + gr, ... (SK_PB of them) of each block b of SK_PB * gr
+// consecutive particles, blocks b0, b0 + SK_PB gr, ... (one thread: every
+// block of SK_PB particles in order)
+__device__ inline void sk_item_blocks(SkAcc &A, const float2 *__restrict__ sp, int stride, int ns, int ax, int ay,
+                                      bool cy, int n0, int cnt, int g, int gr) {
+  for (int b = 0; b < cnt; b += SK_PB * gr) {
+    float s0r = 0.f, s0i = 0.f, p[SK_NG][2], q[SK_NG][2];
+#pragma unroll
+    for (int u = 0; u < SK_NG; ++u) p[u][0] = p[u][1] = q[u][0] = q[u][1] = 0.f;
+    for (int k = 0; k < SK_PB; ++k) {
+      const int l = b + g + k * gr;
+      if (l >= cnt) break;
+      float2 ey = sp[((ns + 1) + ay) * stride + l];
+      if (cy) ey.y = -ey.y;
+      const float2 exy = cmulf(sp[ax * stride + l], ey);
+      s0r += exy.x;
+      s0i += exy.y;
+#pragma unroll
+      for (int u = 0; u < SK_NG; ++u) {
+        const int n = n0 + u + 1;
+        if (n > ns) break;
+        const float2 ez = sp[(2 * (ns + 1) + n) * stride + l];
+        p[u][0] = fmaf(exy.x, ez.x, p[u][0]);
+        p[u][1] = fmaf(exy.y, ez.x, p[u][1]);
+        q[u][0] = fmaf(exy.x, ez.y, q[u][0]);
+        q[u][1] = fmaf(exy.y, ez.y, q[u][1]);
+      }
+    }
+    if (n0 == 0) {
+      A.s0r.add(s0r);
+      A.s0i.add(s0i);
+    }
+#pragma unroll
+    for (int u = 0; u < SK_NG; ++u) {
+      if (n0 + u + 1 > ns) break;
+      A.P[u][0].add(p[u][0]);
+      A.P[u][1].add(p[u][1]);
+      A.Q[u][0].add(q[u][0]);
+      A.Q[u][1].add(q[u][1]);
+    }
+  }
+}
+
+// S(k) of the item's wave vectors: Sj is the slice's row S + j nk
+__device__ inline void sk_item_store(const SkAcc &A, double2 *Sj, int4 c, int ns, int n0) {
+  double2 *o = Sj + c.w - c.z;
+  if (n0 == 0 && c.z <= 0) o[0] = make_double2(A.s0r.value(), A.s0i.value());
+#pragma unroll
+  for (int u = 0; u < SK_NG; ++u) {
+    const int n = n0 + u + 1;
+    if (n > ns) break;
+    const double Pr = A.P[u][0].value(), Pi = A.P[u][1].value();
+    const double Qr = A.Q[u][0].value(), Qi = A.Q[u][1].value();
+    o[n] = make_double2(Pr - Qi, Pi + Qr);
+    if (c.z < 0) o[-n] = make_double2(Pr + Qi, Pi - Qr);
+  }
+}
+
+// One particle's reciprocal force sums over cc kept columns (k_recip_force32's
+// arithmetic): cols and the columns' FP32 force tables sT (4 ns + 1 entries
+// each) in shared memory, the particle's x and y phase factors at
+// pxy[(d (ns+1) + n) * stride + li] (shared), its z factors in ez[1..ns]
+template <int NSM>
+__device__ inline void recip_cols32(Kahan &Fx, Kahan &Fy, Kahan &Fz, const int4 *__restrict__ cols, int cc,
+                                    const float2 *__restrict__ sT, int ns, const float2 *__restrict__ pxy, int stride,
+                                    int li, const float2 *ez) {
+  const int NT = 4 * ns + 1;
+  for (int ci = 0; ci < cc; ++ci) {
+    const int4 c = cols[ci];
+    const int nzc = col_nz(c);
+    float2 ey = pxy[((ns + 1) + (c.y < 0 ? -c.y : c.y)) * stride + li];
+    if (c.y < 0) ey.y = -ey.y;
+    const float2 exy = cmulf(pxy[col_nx(c) * stride + li], ey);
+    const float2 *t = sT + ci * NT;
+    float Ur = t[0].x, Ui = t[0].y, Vr = 0.f, Vi = 0.f;
+#pragma unroll
+    for (int n = 1; n <= NSM; ++n) {
+      if (n > ns || n > nzc) break;
+      const float2 A = t[4 * n - 3], B = t[4 * n - 2], nA = t[4 * n - 1], nB = t[4 * n];
+      const float cz = ez[n].x, sz = ez[n].y;
+      Ur = fmaf(cz, A.x, fmaf(-sz, B.y, Ur));
+      Ui = fmaf(cz, A.y, fmaf(sz, B.x, Ui));
+      Vr = fmaf(cz, nB.x, fmaf(-sz, nA.y, Vr));
+      Vi = fmaf(cz, nB.y, fmaf(sz, nA.x, Vi));
+    }
+    const float Tm = fmaf(exy.x, Ui, exy.y * Ur);
+    const float Zm = fmaf(exy.x, Vi, exy.y * Vr);
+    Fx.add((float)col_nx(c) * Tm);
+    Fy.add((float)c.y * Tm);
+    Fz.add(Zm);
+  }
+}
+
 }  // namespace xk
+

@@ -4,14 +4,13 @@
 // The fictitious-particle method needs many (xi, beta) systems to
 // extrapolate to xi = -1; each is small (N <= 128 beads per slice in the
 // benchmark ensemble) and one system's step is a chain of a dozen dependent
-// stages, so as separate kernels the systems leave most of the GPU idle
-// between launches.  Here one launch runs every stage of every system:
-// clusters of thread blocks take the systems of a list the host balanced
-// by estimated cost (longest first, each to the least loaded cluster), and
-// a cluster runs its systems one after the other.  Inside a system the
-// stages are separated by cluster barriers (barrier.cluster, with the
-// release / acquire ordering of the cluster's memory operations); there is
-// no wait on another cluster, so no spin loop exists anywhere.
+// stages, so as separate kernels the systems keep the GPU's launch path
+// busy with about a thousand small kernels a step.  Here one launch runs
+// every stage of every system: the step is nine phases, each phase holds the
+// work of ALL systems for that stage (spread over every thread, warp or
+// block of the grid, round-robin over the systems' tasks), and the phases
+// are separated by grid barriers.  The grid is exactly the blocks that fit
+// (a cooperative launch), and each barrier wait is bounded.
 //
 // Every stage uses the arithmetic of the per-system kernels through the same
 // device functions (xmd_device.cuh), in the same summation orders: the
@@ -37,15 +36,14 @@
 
 namespace xk {
 
-namespace cg = cooperative_groups;
-
 constexpr int ENS_T = 256;                // threads per block
 constexpr int ENS_W = ENS_T / 32;         // warps per block (the EX_TY rows of the end-bead block)
 constexpr size_t ENS_SMEM = 64 * 1024;    // dynamic shared memory per block
 constexpr int ENS_SKC = 128;              // particles per staged chunk of phase factors
-constexpr int ENS_NG = 4;                 // harmonics n per structure-factor item
 constexpr int ENS_NSMAX = 11;             // largest Ewald n_sum
+constexpr long long ENS_WAIT_LIMIT = 1LL << 31;  // clock cycles a grid-barrier wait may take (~1 s)
 static_assert(ENS_W == EX_TY, "the end-bead block is 32 x EX_TY threads");
+static_assert(ENS_SKC % SK_PB == 0, "staged chunks hold whole particle blocks");
 
 struct EnsSys {
   EnsSysDesc d;
@@ -60,7 +58,30 @@ struct EnsSys {
   double2 *S;
   float *part, *x32;
   double lnvi, rscale, pscale;
+  int rot[16];  // per task kind: (the kind's tasks before this system) mod (workers of that kind)
 };
+
+// task kinds of the step's phases (threads, warps or blocks, as noted)
+enum {
+  R_A,       // thread: first half step per slot
+  R_B_SPR,   // thread: interior springs
+  R_B_EINT,  // warp: E_l^(1) per particle (the pair tiles continue its numbering)
+  R_B_PAIR,  // warp: FP32 pair tile jobs
+  R_B_SK,    // block: structure factors per slice
+  R_C_PRE,   // block: prefix sums per system
+  R_C_TAB,   // thread: force-table entries
+  R_D_ENK,   // thread: cycle energies E_l^(k), k >= 2
+  R_D_REC,   // block: reciprocal forces per slice
+  R_E_W,     // warp: weight rows
+  R_E_PS,    // thread: pair sums per slot
+  R_E_INV,   // block: diagonal-block inverses
+  R_F,       // block: solves
+  R_G,       // thread: G entries
+  R_H,       // block: end-bead exchange forces
+  R_I,       // thread: second half step per slot
+  ENS_NROT
+};
+static_assert(ENS_NROT == 16, "EnsSys::rot holds every task kind");
 
 // one FP32 pair tile job of the system's potential kind
 template <int D>
@@ -85,118 +106,74 @@ __device__ inline void ens_pair_job(const EnsSys &E, int wi, int lane) {
   }
 }
 
-// Structure factors of bead slice j by the calling block.  Items are (kept
-// column, group of ENS_NG harmonics); each thread sums its item over the
-// slice's particles in order, as k_sk32 does per column, with the particles'
-// phase factors staged in shared memory ENS_SKC at a time.
+// Structure factors of bead slice j by the calling block: one thread per
+// item (kept column, SK_NG harmonics), every particle block in order, as
+// k_sk32 with one thread per item computes them; the particles' phase
+// factors staged in shared memory ENS_SKC at a time.
 __device__ inline void ens_sk_slice(const EnsSys &E, int j, float2 *sp) {
   const Geo &g = E.d.g;
   const int ns = E.ns, N = g.N, tid = threadIdx.x;
-  const int ngr = (ns + ENS_NG - 1) / ENS_NG;
+  const int ngr = (ns + SK_NG - 1) / SK_NG;
   const int items = E.ncol * ngr;
   const float2 *base = E.ph32 + (size_t)j * 3 * (ns + 1) * g.Ns;
   const int rows = 3 * (ns + 1);
   for (int b0 = 0; b0 < items; b0 += ENS_T) {
     const int item = b0 + tid;
     const bool live = item < items;
-    const int ci = live ? item / ngr : 0, gi = live ? item % ngr : 0;
+    const int ci = live ? item / ngr : 0, n0 = live ? (item % ngr) * SK_NG : 0;
     const int4 c = live ? E.cols[ci] : make_int4(0, 0, 1, 0);
     const int ax = col_nx(c), ay = c.y < 0 ? -c.y : c.y;
     const bool cy = c.y < 0;
-    const int n0 = gi * ENS_NG;
-    DF s0r, s0i, Pa[ENS_NG][2], Qa[ENS_NG][2];
+    SkAcc A;
     for (int l0 = 0; l0 < N; l0 += ENS_SKC) {
       const int cnt = N - l0 < ENS_SKC ? N - l0 : ENS_SKC;
       __syncthreads();
       for (int q = tid; q < rows * ENS_SKC; q += ENS_T) {
         const int l = q % ENS_SKC, row = q / ENS_SKC;
-        sp[q] = l < cnt ? base[(size_t)row * g.Ns + l0 + l] : make_float2(0.f, 0.f);
+        sp[row * (ENS_SKC + 1) + l] = l < cnt ? base[(size_t)row * g.Ns + l0 + l] : make_float2(0.f, 0.f);
       }
       __syncthreads();
-      if (!live) continue;
-      for (int l = 0; l < cnt; ++l) {
-        float2 ey = sp[((ns + 1) + ay) * ENS_SKC + l];
-        if (cy) ey.y = -ey.y;
-        const float2 exy = cmulf(sp[ax * ENS_SKC + l], ey);
-        if (gi == 0) {
-          s0r.add(exy.x);
-          s0i.add(exy.y);
-        }
-#pragma unroll
-        for (int u = 0; u < ENS_NG; ++u) {
-          const int n = n0 + u + 1;
-          if (n > ns) break;
-          const float2 ez = sp[(2 * (ns + 1) + n) * ENS_SKC + l];
-          Pa[u][0].add(exy.x * ez.x);
-          Pa[u][1].add(exy.y * ez.x);
-          Qa[u][0].add(exy.x * ez.y);
-          Qa[u][1].add(exy.y * ez.y);
-        }
-      }
+      if (live) sk_item_blocks(A, sp, ENS_SKC + 1, ns, ax, ay, cy, n0, cnt, 0, 1);
     }
-    if (!live) continue;
-    double2 *o = E.S + (size_t)j * E.nk + c.w - c.z;
-    if (gi == 0 && c.z <= 0) o[0] = make_double2(s0r.value(), s0i.value());
-#pragma unroll
-    for (int u = 0; u < ENS_NG; ++u) {
-      const int n = n0 + u + 1;
-      if (n > ns) break;
-      const double Pr = Pa[u][0].value(), Pi = Pa[u][1].value();
-      const double Qr = Qa[u][0].value(), Qi = Qa[u][1].value();
-      o[n] = make_double2(Pr - Qi, Pi + Qr);
-      if (c.z < 0) o[-n] = make_double2(Pr + Qi, Pi - Qr);
-    }
+    if (live) sk_item_store(A, E.S + (size_t)j * E.nk, c, ns, n0);
   }
 }
 
 // Reciprocal forces on the particles of bead slice j by the calling block,
-// as k_recip_force32 computes them (the same column order and compensated
-// sums), the slice's force tables staged in shared memory as many columns
-// at a time as fit.
-__device__ inline void ens_recip_slice(const EnsSys &E, int j, float2 *sT) {
+// as k_recip_force32 computes them (recip_cols32: the same column order and
+// compensated sums), 128 particles at a time; the columns, the particles' x
+// and y phase factors and as many columns' force tables as fit are staged
+// in shared memory.
+__device__ inline void ens_recip_slice(const EnsSys &E, int j, unsigned char *sh) {
   const Geo &g = E.d.g;
   const int ns = E.ns, NT = 4 * ns + 1, ncol = E.ncol, N = g.N, tid = threadIdx.x;
-  const int ccap = (int)(ENS_SMEM / (sizeof(float2) * NT));
+  int4 *sc = (int4 *)sh;
+  float2 *pxy = (float2 *)(sc + ncol);
+  float2 *sT = pxy + 2 * (ns + 1) * 128;
+  const int ccap = (int)((ENS_SMEM - sizeof(int4) * ncol - sizeof(float2) * 2 * (ns + 1) * 128) / (sizeof(float2) * NT));
   const float2 *Tj = E.T32 + (size_t)j * ncol * NT;
-  for (int lb = 0; lb < N; lb += ENS_T) {
+  const float2 *pj = E.ph32 + (size_t)j * 3 * (ns + 1) * g.Ns;
+  __syncthreads();
+  for (int q = tid; q < ncol; q += ENS_T) sc[q] = E.cols[q];
+  for (int lb = 0; lb < N; lb += 128) {
     const int l = lb + tid;
-    const bool live = l < N;
-    const float2 *pj = E.ph32 + (size_t)j * 3 * (ns + 1) * g.Ns + (live ? l : 0);
+    const bool live = tid < 128 && l < N;
+    __syncthreads();
+    for (int q = tid; q < 2 * (ns + 1) * 128; q += ENS_T) {
+      const int r = q / 128, li = q % 128;
+      pxy[q] = lb + li < N ? pj[(size_t)r * g.Ns + lb + li] : make_float2(0.f, 0.f);
+    }
     float2 ez[ENS_NSMAX + 1];
 #pragma unroll
     for (int n = 1; n <= ENS_NSMAX; ++n)
-      ez[n] = (live && n <= ns) ? pj[((size_t)2 * (ns + 1) + n) * g.Ns] : make_float2(0.f, 0.f);
+      ez[n] = (live && n <= ns) ? pj[((size_t)2 * (ns + 1) + n) * g.Ns + l] : make_float2(0.f, 0.f);
     Kahan Fx, Fy, Fz;
     for (int c0 = 0; c0 < ncol; c0 += ccap) {
       const int cc = ncol - c0 < ccap ? ncol - c0 : ccap;
       __syncthreads();
       for (int q = tid; q < cc * NT; q += ENS_T) sT[q] = Tj[(size_t)c0 * NT + q];
       __syncthreads();
-      if (!live) continue;
-      for (int ci = 0; ci < cc; ++ci) {
-        const int4 c = E.cols[c0 + ci];
-        const int nzc = col_nz(c);
-        float2 ey = pj[((size_t)(ns + 1) + (c.y < 0 ? -c.y : c.y)) * g.Ns];
-        if (c.y < 0) ey.y = -ey.y;
-        const float2 exy = cmulf(pj[(size_t)col_nx(c) * g.Ns], ey);
-        const float2 *t = sT + ci * NT;
-        float Ur = t[0].x, Ui = t[0].y, Vr = 0.f, Vi = 0.f;
-#pragma unroll
-        for (int n = 1; n <= ENS_NSMAX; ++n) {
-          if (n > ns || n > nzc) break;
-          const float2 A = t[4 * n - 3], B = t[4 * n - 2], nA = t[4 * n - 1], nB = t[4 * n];
-          const float cz = ez[n].x, sz = ez[n].y;
-          Ur = fmaf(cz, A.x, fmaf(-sz, B.y, Ur));
-          Ui = fmaf(cz, A.y, fmaf(sz, B.x, Ui));
-          Vr = fmaf(cz, nB.x, fmaf(-sz, nA.y, Vr));
-          Vi = fmaf(cz, nB.y, fmaf(sz, nA.x, Vi));
-        }
-        const float Tm = fmaf(exy.x, Ui, exy.y * Ur);
-        const float Zm = fmaf(exy.x, Vi, exy.y * Vr);
-        Fx.add((float)col_nx(c) * Tm);
-        Fy.add((float)c.y * Tm);
-        Fz.add(Zm);
-      }
+      if (live) recip_cols32<ENS_NSMAX>(Fx, Fy, Fz, sc + c0, cc, sT, ns, pxy, 128, tid, ez);
     }
     if (live) {
       double *f = E.d.f;
@@ -207,104 +184,232 @@ __device__ inline void ens_recip_slice(const EnsSys &E, int j, float2 *sT) {
   }
 }
 
-// The step of every system in the clusters' lists.  Grid: clusters of CL
-// blocks of ENS_T threads; cluster k runs systems list[off[k] .. off[k+1]).
-template <int D, int L>
-__global__ void __launch_bounds__(ENS_T, 2) k_ensemble_step(const EnsSys *__restrict__ sys,
-                                                            const int *__restrict__ list,
-                                                            const int *__restrict__ off) {
-  cg::cluster_group cl = cg::this_cluster();
-  const int CL = (int)cl.num_blocks();
-  const int cr = (int)cl.block_rank();
-  const int cid = blockIdx.x / CL;
-  extern __shared__ __align__(16) unsigned char ens_sh[];
-  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-  const int gt = cr * ENS_T + tid, GT = CL * ENS_T;
-  const int gw = cr * ENS_W + w, GW = CL * ENS_W;
-  for (int it = off[cid]; it < off[cid + 1]; ++it) {
-    const EnsSys &E = sys[list[it]];
-    const EnsSysDesc &d = E.d;
-    const Geo g = d.g;
-    const size_t Sn = g.slots();
-    const int N = g.N, P = g.P;
+// ---- grid barrier ----------------------------------------------------------
+// The phases of the step are separated by a barrier over the whole grid
+// (every block is resident: the grid is the number of blocks that fit, and
+// the launch is cooperative).  Block b's thread 0 arrives with an atomic
+// increment; the last arrival resets the count and advances the generation
+// the others wait on.  A wait gives up after `limit` clock cycles: it sets
+// err, and every later barrier of any launch returns at once, so a broken
+// grid ends instead of hanging; the host reads err as the step's status.
+struct EnsBar {
+  unsigned int count, gen;
+  int err;
+  int pad;
+  unsigned long long stamp[ENS_PHASES + 1];  // block 0's %globaltimer at the start and after each phase
+};
 
-    // A: first half step (md_update_nhc_VV3_1_x); the forces restart from
-    // the trap's (md_reset_force_x, md_pimd_calc_trap_force_x); FP32
-    // positions and phase factors of the new positions
-    for (size_t s = gt; s < Sn; s += GT) {
-      const int l = (int)(s % g.Ns);
-      if (l >= N) continue;
-      nhc_slot<D, L>(g, 1, s, l, d.x, d.v, d.f, nullptr, d.m, d.th, d.vt, d.Q, d.iQ, d.kT, d.h);
-      const double xn = d.x[s];
-      double f0 = 0.0;
-      if (d.trap_kind) f0 += trap_f(d.tp, (int)((s / g.Ns) % D), xn) / P;
-      d.f[s] = f0;
-      d.fex[s] = 0.0;
-      if (d.pair_kind) E.x32[s] = (float)xn;
-      if constexpr (D == 3)
-        if (E.ewald) phase32_slot(g, E.ns, d.x, E.ph32, s);
-    }
-    cl.sync();
+__device__ inline void ens_stamp(EnsBar *b, int k) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    b->stamp[k] = t;
+  }
+}
 
-    // B: E_l^(1) and the prefix-sum increments (md_pimd_fast_fill_ENk_x),
-    // interior ring springs into fex, FP32 pair tiles, structure factors
-    for (int l = gw; l < N; l += GW) eint_particle<D>(g, d.x, d.m, d.w2, d.image, d.Eint, d.ENk, d.gl, l, lane);
-    if (P > 2) {
-      const size_t n2 = (size_t)(P - 2) * g.Ns;
-      for (size_t t = gt; t < n2; t += GT) {
-        const int l = (int)(t % g.Ns), j = (int)(t / g.Ns) + 1;
-        if (l < N) spring_interior_bead<D>(g, d.x, d.m, d.w2, d.image, d.fex, j, l);
+__device__ inline void ens_grid_sync(EnsBar *b, unsigned int nblocks, long long limit) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned int *genp = &b->gen;
+    volatile int *errp = &b->err;
+    const unsigned int my = *genp;
+    __threadfence();
+    if (atomicAdd(&b->count, 1u) + 1u == nblocks) {
+      atomicExch(&b->count, 0u);
+      __threadfence();
+      atomicAdd(&b->gen, 1u);
+    } else {
+      const long long t0 = clock64();
+      while (*genp == my && !*errp) {
+        if (clock64() - t0 > limit) {
+          atomicExch(&b->err, 1);
+          break;
+        }
+        __nanosleep(32);
       }
     }
-    if (d.pair_kind) {
-      const int nj = E.jobs * P;
-      for (int wi = gw; wi < nj; wi += GW) ens_pair_job<D>(E, wi, lane);
-    }
-    if constexpr (D == 3)
-      if (E.ewald)
-        for (int j = cr; j < P; j += CL) ens_sk_slice(E, j, (float2 *)ens_sh);
-    cl.sync();
+    __threadfence();
+  }
+  __syncthreads();
+}
 
-    // C: the remaining cycle energies E_l^(k), k >= 2, from each block's own
-    // prefix sums; the FP32 force tables of the reciprocal sum
-    if (N >= 2) {
-      double *Gs = (double *)ens_sh;
-      block_exclusive_prefix(d.gl, N - 1, Gs);
-      __syncthreads();
-      const size_t ne = (size_t)N * (N - 1) / 2;
-      for (size_t q = gt; q < ne; q += GT) {
+// the first of a system's tasks that worker `me` (of `stride`) takes, the
+// tasks of all systems numbered in turn and dealt round-robin; rot is the
+// number of the kind's tasks before this system, modulo stride
+__device__ inline long long ens_first(long long me, int rot, long long stride) {
+  return me >= rot ? me - rot : me - rot + stride;
+}
+
+// One step of every system.  Each phase's work of ALL systems is spread over
+// the whole grid (threads, warps or blocks, round-robin over the tasks of the
+// systems in turn); the phases are separated by grid barriers.
+template <int D, int L>
+__global__ void __launch_bounds__(ENS_T, 2) k_ensemble_step(const EnsSys *__restrict__ sys, int nsys, EnsBar *bar,
+                                                            long long limit) {
+  extern __shared__ __align__(16) unsigned char ens_sh[];
+  if (*(volatile int *)&bar->err) return;  // an earlier step's barrier gave up
+  const unsigned int G = gridDim.x;
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  const long long GT = (long long)G * ENS_T, GW = (long long)G * ENS_W;
+  const long long gt = (long long)blockIdx.x * ENS_T + tid, gw = (long long)blockIdx.x * ENS_W + w;
+  const long long gb = blockIdx.x;
+  ens_stamp(bar, 0);
+
+  // A: first half step (md_update_nhc_VV3_1_x); the forces restart from the
+  // trap's (md_reset_force_x, md_pimd_calc_trap_force_x); FP32 positions and
+  // phase factors of the new positions
+  {
+    for (int i = 0; i < nsys; ++i) {
+      const EnsSys &E = sys[i];
+      const EnsSysDesc &d = E.d;
+      const Geo g = d.g;
+      const long long n = (long long)g.slots();
+      for (long long q = ens_first(gt, sys[i].rot[R_A], GT); q < n; q += GT) {
+        const size_t s = (size_t)q;
+        const int l = (int)(s % g.Ns);
+        if (l >= g.N) continue;
+        nhc_slot<D, L>(g, 1, s, l, d.x, d.v, d.f, nullptr, d.m, d.th, d.vt, d.Q, d.iQ, d.kT, d.h);
+        const double xn = d.x[s];
+        double f0 = 0.0;
+        if (d.trap_kind) f0 += trap_f(d.tp, (int)((s / g.Ns) % D), xn) / g.P;
+        d.f[s] = f0;
+        d.fex[s] = 0.0;
+        if (d.pair_kind) E.x32[s] = (float)xn;
+        if constexpr (D == 3)
+          if (E.ewald) phase32_slot(g, E.ns, d.x, E.ph32, s);
+      }
+    }
+  }
+  ens_grid_sync(bar, G, limit);
+  ens_stamp(bar, 1);
+
+  // B: interior ring springs into fex; E_l^(1) and the prefix-sum increments
+  // (md_pimd_fast_fill_ENk_x); FP32 pair tiles; structure factors
+  {
+    for (int i = 0; i < nsys; ++i) {
+      const EnsSysDesc &d = sys[i].d;
+      const Geo g = d.g;
+      const long long n = g.P > 2 ? (long long)(g.P - 2) * g.Ns : 0;
+      for (long long t = ens_first(gt, sys[i].rot[R_B_SPR], GT); t < n; t += GT) {
+        const int l = (int)(t % g.Ns), j = (int)(t / g.Ns) + 1;
+        if (l < g.N) spring_interior_bead<D>(g, d.x, d.m, d.w2, d.image, d.fex, j, l);
+      }
+    }
+  }
+  {
+    for (int i = 0; i < nsys; ++i) {
+      const EnsSysDesc &d = sys[i].d;
+      const Geo g = d.g;
+      for (long long l = ens_first(gw, sys[i].rot[R_B_EINT], GW); l < g.N; l += GW)
+        eint_particle<D>(g, d.x, d.m, d.w2, d.image, d.Eint, d.ENk, d.gl, (int)l, lane);
+    }
+    for (int i = 0; i < nsys; ++i) {
+      const EnsSys &E = sys[i];
+      if (!E.d.pair_kind) continue;
+      const long long n = (long long)E.jobs * E.d.g.P;
+      for (long long wi = ens_first(gw, sys[i].rot[R_B_PAIR], GW); wi < n; wi += GW) ens_pair_job<D>(E, (int)wi, lane);
+    }
+  }
+  if constexpr (D == 3) {
+    for (int i = 0; i < nsys; ++i) {
+      const EnsSys &E = sys[i];
+      if (!E.ewald) continue;
+      for (long long j = ens_first(gb, sys[i].rot[R_B_SK], G); j < E.d.g.P; j += G) ens_sk_slice(E, (int)j, (float2 *)ens_sh);
+    }
+  }
+  ens_grid_sync(bar, G, limit);
+  ens_stamp(bar, 2);
+
+  // C: prefix sums of the increments (a block per system, the block size of
+  // k_enk_direct's own scan, into gl[N ..]); the FP32 force tables
+  {
+    for (int i = 0; i < nsys; ++i) {
+      const EnsSysDesc &d = sys[i].d;
+      if (d.g.N < 2) continue;
+      if (ens_first(gb, sys[i].rot[R_C_PRE], G) == 0) {
+        block_exclusive_prefix(d.gl, d.g.N - 1, d.gl + d.g.N);
+        __syncthreads();  // its scratch is reused by the block's next system
+      }
+    }
+  }
+  if constexpr (D == 3) {
+    for (int i = 0; i < nsys; ++i) {
+      const EnsSys &E = sys[i];
+      if (!E.ewald) continue;
+      const int per = E.ns + 1;
+      const long long n = (long long)E.d.g.P * E.ncol * per;
+      for (long long q = ens_first(gt, sys[i].rot[R_C_TAB], GT); q < n; q += GT) {
+        const long long r = q / per;
+        recip_table32_entry(E.cols, E.ncol, E.S, E.coef, E.nk, E.T32, E.ns, (int)(r / E.ncol), (int)(r % E.ncol),
+                            (int)(q % per));
+      }
+    }
+  }
+  ens_grid_sync(bar, G, limit);
+  ens_stamp(bar, 3);
+
+  // D: the cycle energies E_l^(k), k >= 2; reciprocal forces
+  {
+    for (int i = 0; i < nsys; ++i) {
+      const EnsSysDesc &d = sys[i].d;
+      const Geo g = d.g;
+      const long long n = (long long)g.N * (g.N - 1) / 2;
+      for (long long q = ens_first(gt, sys[i].rot[R_D_ENK], GT); q < n; q += GT) {
         // rows r = l - 1 = 1 .. N-1 hold r entries each, r (r - 1) / 2 before row r
         int r = (int)((1.f + sqrtf(1.f + 8.f * (float)q)) * 0.5f);
-        while ((size_t)r * (r - 1) / 2 > q) --r;
-        while ((size_t)r * (r + 1) / 2 <= q) ++r;
-        const int k = 2 + (int)(q - (size_t)r * (r - 1) / 2);
-        enk_entry<D>(g, d.x, d.m, d.w2, d.image, d.Eint, Gs, d.ENk, r + 1, k);
+        while ((long long)r * (r - 1) / 2 > q) --r;
+        while ((long long)r * (r + 1) / 2 <= q) ++r;
+        const int k = 2 + (int)(q - (long long)r * (r - 1) / 2);
+        enk_entry<D>(g, d.x, d.m, d.w2, d.image, d.Eint, d.gl + g.N, d.ENk, r + 1, k);
       }
     }
-    if constexpr (D == 3)
-      if (E.ewald) {
-        const int per = E.ns + 1;
-        const size_t nt = (size_t)P * E.ncol * per;
-        for (size_t q = gt; q < nt; q += GT) {
-          const int n = (int)(q % per);
-          const size_t r = q / per;
-          recip_table32_entry(E.cols, E.ncol, E.S, E.coef, E.nk, E.T32, E.ns, (int)(r / E.ncol), (int)(r % E.ncol),
-                              n);
-        }
-      }
-    cl.sync();
+  }
+  if constexpr (D == 3) {
+    for (int i = 0; i < nsys; ++i) {
+      const EnsSys &E = sys[i];
+      if (!E.ewald) continue;
+      for (long long j = ens_first(gb, sys[i].rot[R_D_REC], G); j < E.d.g.P; j += G) ens_recip_slice(E, (int)j, ens_sh);
+    }
+  }
+  ens_grid_sync(bar, G, limit);
+  ens_stamp(bar, 4);
 
-    // D: weight rows of both recursions and the diagonal-block inverses
-    // (md_pimd_fill_VB_x); reciprocal forces
-    for (int row = gw + 1; row <= N; row += GW)
-      weights_row(N, d.beta, d.vi, E.lnvi, d.ENk, d.lnn, (double *)E.job.Mm[0], (int *)E.job.Me[0],
-                  (double *)E.job.Mm[1], (int *)E.job.Me[1], 0, 1, 1, row, 0, lane, 32);
-    {
-      const int nch = (N + TS_CHUNK - 1) / TS_CHUNK;
-      double(*Am)[TS_LD] = (double(*)[TS_LD])ens_sh;
-      int(*Ae)[TS_LD] = (int(*)[TS_LD])(ens_sh + sizeof(double) * TS_CHUNK * TS_LD);
-      for (int tk = cr; tk < 2 * nch; tk += CL) {
-        const int dir = tk / nch, c = tk % nch, i0 = 1 + c * TS_CHUNK;
+  // E: weight rows of both recursions and the diagonal-block inverses
+  // (md_pimd_fill_VB_x); the pair tiles' partial sums into f
+  {
+    for (int i = 0; i < nsys; ++i) {
+      const EnsSys &E = sys[i];
+      const EnsSysDesc &d = E.d;
+      const int N = d.g.N;
+      for (long long r = ens_first(gw, sys[i].rot[R_E_W], GW); r < N; r += GW)
+        weights_row(N, d.beta, d.vi, E.lnvi, d.ENk, d.lnn, (double *)E.job.Mm[0], (int *)E.job.Me[0],
+                    (double *)E.job.Mm[1], (int *)E.job.Me[1], 0, 1, 1, (int)r + 1, 0, lane, 32);
+    }
+  }
+  {
+    for (int i = 0; i < nsys; ++i) {
+      const EnsSys &E = sys[i];
+      if (!E.d.pair_kind) continue;
+      const Geo g = E.d.g;
+      const long long n = (long long)g.slots();
+      for (long long q = ens_first(gt, sys[i].rot[R_E_PS], GT); q < n; q += GT) {
+        const size_t s = (size_t)q;
+        if ((int)(s % g.Ns) >= g.N) continue;
+        double acc = 0;
+        for (int t = 0; t < E.T; ++t) acc += (double)E.part[(size_t)t * n + s];
+        E.d.f[s] += acc * E.pscale;
+      }
+    }
+  }
+  {
+    double(*Am)[TS_LD] = (double(*)[TS_LD])ens_sh;
+    int(*Ae)[TS_LD] = (int(*)[TS_LD])(ens_sh + sizeof(double) * TS_CHUNK * TS_LD);
+    for (int i = 0; i < nsys; ++i) {
+      const EnsSys &E = sys[i];
+      const EnsSysDesc &d = E.d;
+      const int N = d.g.N, nch = (N + TS_CHUNK - 1) / TS_CHUNK;
+      for (long long tk = ens_first(gb, sys[i].rot[R_E_INV], G); tk < 2 * nch; tk += G) {
+        const int dir = (int)tk / nch, c = (int)tk % nch, i0 = 1 + c * TS_CHUNK;
         __syncthreads();
         for (int e = tid; e < TS_CHUNK * TS_CHUNK; e += ENS_T) {
           const int r = e / TS_CHUNK, t = e % TS_CHUNK;
@@ -317,78 +422,95 @@ __global__ void __launch_bounds__(ENS_T, 2) k_ensemble_step(const EnsSys *__rest
         for (int sc = w; sc < TS_CHUNK; sc += ENS_W) block_inv_column(N, E.job, dir, c, sc, Am, Ae);
       }
     }
-    if constexpr (D == 3)
-      if (E.ewald)
-        for (int j = cr; j < P; j += CL) ens_recip_slice(E, j, (float2 *)ens_sh);
-    cl.sync();
+  }
+  ens_grid_sync(bar, G, limit);
+  ens_stamp(bar, 5);
 
-    // E: the forward (V_B) and backward (tmpV) solves on blocks 0 and 1 (block
-    // 0 alone: one after the other); the pair tiles' partial sums into f on
-    // the other blocks
-    if (cr == 0) tri_solve_b_dev(N, d.beta, E.job, 0, (double *)ens_sh);
-    if (cr == (CL > 1 ? 1 : 0)) {
-      if (CL == 1) __syncthreads();
-      tri_solve_b_dev(N, d.beta, E.job, 1, (double *)ens_sh);
-    }
-    if (d.pair_kind) {
-      const int b0 = CL > 2 ? 2 : 0, nb = CL > 2 ? CL - 2 : CL;
-      if (cr >= b0)
-        for (size_t s = (size_t)(cr - b0) * ENS_T + tid; s < Sn; s += (size_t)nb * ENS_T) {
-          if ((int)(s % g.Ns) >= N) continue;
-          double acc = 0;
-          for (int t = 0; t < E.T; ++t) acc += (double)E.part[(size_t)t * Sn + s];
-          d.f[s] += acc * E.pscale;
-        }
-    }
-    cl.sync();
-
-    // F: cycle probabilities G from the extended-range numbers
-    // (md_pimd_fast_fill_force_VB_x)
-    for (size_t q = gt; q < (size_t)N * N; q += GT)
-      g_ext_elem(N, E.job.Mm[0], E.job.Me[0], E.job.Xm[0], E.job.Xe[0], E.job.Xm[1], E.job.Xe[1], d.G,
-                 (int)(q / N) + 1, (int)(q % N) + 1);
-    cl.sync();
-
-    // G: G-weighted springs of the end beads, partial sums per partner split
-    {
-      const int tiles = (N + 31) / 32, ntask = tiles * E.nsplit;
-      for (int tk = cr; tk < ntask; tk += CL) {
-        exch_ends_block<D>(g, d.x, d.m, d.w2, d.image, d.G, d.xscr, E.nsplit, tk % tiles, tk / tiles, lane, w,
-                           (double *)ens_sh);
+  // F: the forward (V_B) and backward (tmpV) block solves, a block each
+  {
+    for (int i = 0; i < nsys; ++i) {
+      const EnsSys &E = sys[i];
+      for (long long dir = ens_first(gb, sys[i].rot[R_F], G); dir < 2; dir += G) {
         __syncthreads();
-      }
-    }
-    cl.sync();
-
-    // H: the end beads' exchange forces into fex, the second half step with
-    // f + fex (md_update_nhc_VV3_2_x), the periodic wrap
-    for (size_t s = gt; s < Sn; s += GT) {
-      const int l = (int)(s % g.Ns);
-      if (l >= N) continue;
-      const int jd = (int)(s / g.Ns), j = jd / D, dd = jd % D;
-      if (j == 0 || j == P - 1) {
-        const int qq = (j == P - 1 ? D : 0) + dd;
-        double sum = 0;
-        for (int js = 0; js < E.nsplit; ++js) sum += d.xscr[((size_t)js * 2 * D + qq) * g.Ns + l];
-        d.fex[s] += -sum / d.m[(size_t)j * g.Ns + l];
-      }
-      nhc_slot<D, L>(g, 2, s, l, d.x, d.v, d.f, d.fex, d.m, d.th, d.vt, d.Q, d.iQ, d.kT, d.h);
-      if (d.wrap) {
-        const double Lb = g.box[dd];
-        double a = d.x[s];
-        if (a < 0)
-          a += Lb;
-        else if (a > Lb)
-          a -= Lb;
-        d.x[s] = a;
+        tri_solve_b_dev(E.d.g.N, E.d.beta, E.job, (int)dir, (double *)ens_sh);
       }
     }
   }
+  ens_grid_sync(bar, G, limit);
+  ens_stamp(bar, 6);
+
+  // G: cycle probabilities G from the extended-range numbers
+  // (md_pimd_fast_fill_force_VB_x)
+  {
+    for (int i = 0; i < nsys; ++i) {
+      const EnsSys &E = sys[i];
+      const int N = E.d.g.N;
+      const long long n = (long long)N * N;
+      for (long long q = ens_first(gt, sys[i].rot[R_G], GT); q < n; q += GT)
+        g_ext_elem(N, E.job.Mm[0], E.job.Me[0], E.job.Xm[0], E.job.Xe[0], E.job.Xm[1], E.job.Xe[1], E.d.G,
+                   (int)(q / N) + 1, (int)(q % N) + 1);
+    }
+  }
+  ens_grid_sync(bar, G, limit);
+  ens_stamp(bar, 7);
+
+  // H: G-weighted springs of the end beads, partial sums per partner split
+  {
+    for (int i = 0; i < nsys; ++i) {
+      const EnsSys &E = sys[i];
+      const EnsSysDesc &d = E.d;
+      const Geo g = d.g;
+      const int tiles = (g.N + 31) / 32;
+      const long long n = (long long)tiles * E.nsplit;
+      for (long long tk = ens_first(gb, sys[i].rot[R_H], G); tk < n; tk += G) {
+        exch_ends_block<D>(g, d.x, d.m, d.w2, d.image, d.G, d.xscr, E.nsplit, (int)(tk % tiles), (int)(tk / tiles),
+                           lane, w, (double *)ens_sh);
+        __syncthreads();
+      }
+    }
+  }
+  ens_grid_sync(bar, G, limit);
+  ens_stamp(bar, 8);
+
+  // I: the end beads' exchange forces into fex, the second half step with
+  // f + fex (md_update_nhc_VV3_2_x), the periodic wrap
+  {
+    for (int i = 0; i < nsys; ++i) {
+      const EnsSys &E = sys[i];
+      const EnsSysDesc &d = E.d;
+      const Geo g = d.g;
+      const long long n = (long long)g.slots();
+      for (long long q = ens_first(gt, sys[i].rot[R_I], GT); q < n; q += GT) {
+        const size_t s = (size_t)q;
+        const int l = (int)(s % g.Ns);
+        if (l >= g.N) continue;
+        const int jd = (int)(s / g.Ns), j = jd / D, dd = jd % D;
+        if (j == 0 || j == g.P - 1) {
+          const int qq = (j == g.P - 1 ? D : 0) + dd;
+          double sum = 0;
+          for (int js = 0; js < E.nsplit; ++js) sum += d.xscr[((size_t)js * 2 * D + qq) * g.Ns + l];
+          d.fex[s] += -sum / d.m[(size_t)j * g.Ns + l];
+        }
+        nhc_slot<D, L>(g, 2, s, l, d.x, d.v, d.f, d.fex, d.m, d.th, d.vt, d.Q, d.iQ, d.kT, d.h);
+        if (d.wrap) {
+          const double Lb = g.box[dd];
+          double a = d.x[s];
+          if (a < 0)
+            a += Lb;
+          else if (a > Lb)
+            a -= Lb;
+          d.x[s] = a;
+        }
+      }
+    }
+  }
+  __syncthreads();
+  ens_stamp(bar, ENS_PHASES);
 }
 
 // ---- host side ----------------------------------------------------------
 
-using EnsFn = void (*)(const EnsSys *, const int *, const int *);
+using EnsFn = void (*)(const EnsSys *, int, EnsBar *, long long);
 
 static EnsFn ens_kernel(int D, int L) {
   switch (D * 16 + L) {
@@ -413,54 +535,32 @@ static cudaError_t ens_opt_in(EnsFn fn) {
   return cudaSuccess;
 }
 
-static void ens_config(int cluster, int clusters, cudaStream_t st, cudaLaunchConfig_t &cfg,
-                       cudaLaunchAttribute &attr) {
-  memset(&cfg, 0, sizeof(cfg));
-  memset(&attr, 0, sizeof(attr));
-  cfg.gridDim = dim3((unsigned)(cluster * clusters), 1, 1);
-  cfg.blockDim = dim3(ENS_T, 1, 1);
-  cfg.dynamicSmemBytes = ENS_SMEM;
-  cfg.stream = st;
-  attr.id = cudaLaunchAttributeClusterDimension;
-  attr.val.clusterDim.x = (unsigned)cluster;
-  attr.val.clusterDim.y = 1;
-  attr.val.clusterDim.z = 1;
-  cfg.attrs = &attr;
-  cfg.numAttrs = 1;
-}
-
-int ensemble_resident_clusters(int D, int L, int cluster) {
-  if (cluster != 1 && cluster != 2 && cluster != 4 && cluster != 8) return 0;
+int ensemble_max_blocks_per_sm(int D, int L) {
   EnsFn fn = ens_kernel(D, L);
   if (!fn || ens_opt_in(fn) != cudaSuccess) {
     cudaGetLastError();
     return 0;
   }
-  cudaLaunchConfig_t cfg;
-  cudaLaunchAttribute attr;
-  ens_config(cluster, 1, nullptr, cfg, attr);
   int n = 0;
-  if (cudaOccupancyMaxActiveClusters(&n, fn, &cfg) != cudaSuccess) {
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, ENS_T, ENS_SMEM) != cudaSuccess) {
     cudaGetLastError();
     return 0;
   }
   return n;
 }
 
-// estimated cost of one system's step (arbitrary units: pair-image
-// evaluations, structure-factor products, recursion entries, barriers)
-static double ens_cost(const EnsSys &E) {
-  const Geo &g = E.d.g;
-  double c = 2.0e4 + 40.0 * (double)g.N * g.N + 60.0 * (double)g.P * g.N;
-  if (E.d.pair_kind) c += (double)E.jobs * 1024.0 * g.P * (E.d.pair_kind == PAIR_EWALD_REAL ? 3.0 : 1.0);
-  if (E.ewald) c += 1.2 * (double)g.P * g.N * E.ncol * (E.ns + 1);
-  return c;
+static int sm_count() {
+  int dev = 0, n = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+  return n > 0 ? n : 1;
 }
 
-cudaError_t ensemble_prepare(const EnsSysDesc *sd, int n, int D, int L, int cluster, EnsLaunch &out) {
+cudaError_t ensemble_prepare(const EnsSysDesc *sd, int n, int D, int L, int blocks_per_sm, EnsLaunch &out) {
   if (n < 1 || !ens_kernel(D, L)) return cudaErrorInvalidValue;
-  const int resident = ensemble_resident_clusters(D, L, cluster);
-  if (resident < 1) return cudaErrorInvalidConfiguration;
+  const int fit = ensemble_max_blocks_per_sm(D, L);
+  if (fit < 1 || blocks_per_sm < 1) return cudaErrorInvalidConfiguration;
+  if (blocks_per_sm > fit) blocks_per_sm = fit;
   std::vector<EnsSys> sys(n);
   for (int i = 0; i < n; ++i) {
     EnsSys &E = sys[i];
@@ -490,28 +590,52 @@ cudaError_t ensemble_prepare(const EnsSysDesc *sd, int n, int D, int L, int clus
     E.lnvi = E.d.vi != 0.0 ? log(E.d.vi) : 0.0;
     E.pscale = 1.0 / g.P;
   }
-  // longest first, each to the least loaded of the resident clusters
-  const int K = n < resident ? n : resident;
-  std::vector<int> order(n);
-  for (int i = 0; i < n; ++i) order[i] = i;
-  std::vector<double> cost(n);
-  for (int i = 0; i < n; ++i) cost[i] = ens_cost(sys[i]);
-  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost[a] > cost[b]; });
-  std::vector<std::vector<int>> lists(K);
-  std::vector<double> load(K, 0.0);
-  for (int i : order) {
-    const int k = (int)(std::min_element(load.begin(), load.end()) - load.begin());
-    lists[k].push_back(i);
-    load[k] += cost[i];
+  // the systems (largest first, so that the round-robin of each phase
+  // starts with the longest tasks), the grid barrier, then the FP32 pair
+  // scratch of every system (tile partials, FP32 positions), kept in the
+  // plan so that no later call can move it
+  std::stable_sort(sys.begin(), sys.end(), [](const EnsSys &a, const EnsSys &b) {
+    return (double)a.d.g.N * a.d.g.N * a.d.g.P > (double)b.d.g.N * b.d.g.N * b.d.g.P;
+  });
+  // each kind's tasks numbered over the systems in this order (as the
+  // kernel's loops number them); rot = tasks before the system, mod workers
+  {
+    const long long G = (long long)blocks_per_sm * sm_count();
+    const long long stride[ENS_NROT] = {G * ENS_T, G * ENS_T, G * ENS_W, G * ENS_W, G, G, G * ENS_T, G * ENS_T,
+                                        G, G * ENS_W, G * ENS_T, G, G, G * ENS_T, G, G * ENS_T};
+    long long base[ENS_NROT] = {};
+    for (int pass = 0; pass < 2; ++pass)  // the pair tiles continue E_l^(1)'s numbering
+      for (int i = 0; i < n; ++i) {
+        EnsSys &E = sys[i];
+        const Geo &g = E.d.g;
+        const long long slots = (long long)g.slots(), N = g.N, P = g.P;
+        long long cnt[ENS_NROT] = {};
+        cnt[R_A] = slots;
+        cnt[R_B_SPR] = P > 2 ? (P - 2) * g.Ns : 0;
+        cnt[R_B_EINT] = N;
+        cnt[R_B_PAIR] = E.d.pair_kind ? (long long)E.jobs * P : 0;
+        cnt[R_B_SK] = E.ewald ? P : 0;
+        cnt[R_C_PRE] = N >= 2 ? 1 : 0;
+        cnt[R_C_TAB] = E.ewald ? P * E.ncol * (E.ns + 1) : 0;
+        cnt[R_D_ENK] = N * (N - 1) / 2;
+        cnt[R_D_REC] = E.ewald ? P : 0;
+        cnt[R_E_W] = N;
+        cnt[R_E_PS] = E.d.pair_kind ? slots : 0;
+        cnt[R_E_INV] = 2 * ((N + TS_CHUNK - 1) / TS_CHUNK);
+        cnt[R_F] = 2;
+        cnt[R_G] = N * N;
+        cnt[R_H] = (long long)((g.N + 31) / 32) * E.nsplit;
+        cnt[R_I] = slots;
+        for (int k = 0; k < ENS_NROT; ++k) {
+          if ((k == R_B_PAIR) != (pass == 1)) continue;
+          if (pass == 1 && i == 0) base[R_B_PAIR] = base[R_B_EINT];
+          E.rot[k] = (int)(base[k] % stride[k]);
+          base[k] += cnt[k];
+        }
+      }
   }
-  std::vector<int> flat, off(K + 1, 0);
-  for (int k = 0; k < K; ++k) {
-    flat.insert(flat.end(), lists[k].begin(), lists[k].end());
-    off[k + 1] = (int)flat.size();
-  }
-  // the FP32 pair scratch (tile partials, then the FP32 positions) of every
-  // system lives in the plan itself, so that no later call can move it
-  const size_t head = (sizeof(EnsSys) * n + sizeof(int) * (flat.size() + off.size()) + 255) & ~(size_t)255;
+  const size_t bar_at = (sizeof(EnsSys) * n + 255) & ~(size_t)255;
+  const size_t head = bar_at + 256;
   std::vector<size_t> at(n, 0);
   size_t bytes = head;
   for (int i = 0; i < n; ++i) {
@@ -527,10 +651,8 @@ cudaError_t ensemble_prepare(const EnsSysDesc *sd, int n, int D, int L, int clus
     sys[i].part = (float *)((unsigned char *)plan + at[i]);
     sys[i].x32 = sys[i].part + (size_t)sys[i].T * sys[i].d.g.slots();
   }
-  std::vector<unsigned char> host(head);
+  std::vector<unsigned char> host(head, 0);
   memcpy(host.data(), sys.data(), sizeof(EnsSys) * n);
-  memcpy(host.data() + sizeof(EnsSys) * n, flat.data(), sizeof(int) * flat.size());
-  memcpy(host.data() + sizeof(EnsSys) * n + sizeof(int) * flat.size(), off.data(), sizeof(int) * off.size());
   e = cudaMemcpy(plan, host.data(), head, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) {
     cudaFree(plan);
@@ -538,10 +660,10 @@ cudaError_t ensemble_prepare(const EnsSysDesc *sd, int n, int D, int L, int clus
   }
   ensemble_free(out);
   out.plan = plan;
+  out.bar = (unsigned char *)plan + bar_at;
   out.D = D;
   out.L = L;
-  out.cluster = cluster;
-  out.clusters = K;
+  out.blocks = blocks_per_sm * sm_count();
   out.nsys = n;
   out.smem = ENS_SMEM;
   return cudaSuccess;
@@ -552,18 +674,34 @@ cudaError_t ensemble_launch(const EnsLaunch &e, cudaStream_t st) {
   if (!fn || !e.plan) return cudaErrorInvalidValue;
   cudaError_t oe = ens_opt_in(fn);
   if (oe != cudaSuccess) return oe;
-  const EnsSys *sys = (const EnsSys *)e.plan;
-  const int *list = (const int *)(sys + e.nsys);
-  const int *off = list + e.nsys;
   cudaLaunchConfig_t cfg;
   cudaLaunchAttribute attr;
-  ens_config(e.cluster, e.clusters, st, cfg, attr);
+  memset(&cfg, 0, sizeof(cfg));
+  memset(&attr, 0, sizeof(attr));
+  cfg.gridDim = dim3((unsigned)e.blocks, 1, 1);
+  cfg.blockDim = dim3(ENS_T, 1, 1);
+  cfg.dynamicSmemBytes = ENS_SMEM;
+  cfg.stream = st;
+  attr.id = cudaLaunchAttributeCooperative;  // every block resident: the grid barrier needs it
+  attr.val.cooperative = 1;
+  cfg.attrs = &attr;
+  cfg.numAttrs = 1;
   {
     XK_PROF("ensemble_step");
-    oe = cudaLaunchKernelEx(&cfg, fn, sys, list, off);
+    oe = cudaLaunchKernelEx(&cfg, fn, (const EnsSys *)e.plan, e.nsys, (EnsBar *)e.bar, ENS_WAIT_LIMIT);
   }
   if (oe != cudaSuccess) return oe;
   return XK_LAUNCHED();
+}
+
+cudaError_t ensemble_status(const EnsLaunch &e, int *failed, double *phase_us) {
+  EnsBar b{};
+  cudaError_t r = cudaMemcpy(&b, e.bar, sizeof(b), cudaMemcpyDeviceToHost);
+  if (r != cudaSuccess) return r;
+  *failed = b.err;
+  if (phase_us)
+    for (int k = 0; k < ENS_PHASES; ++k) phase_us[k] = (double)(b.stamp[k + 1] - b.stamp[k]) * 1e-3;
+  return r;
 }
 
 void ensemble_free(EnsLaunch &e) {

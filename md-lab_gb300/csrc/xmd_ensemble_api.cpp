@@ -234,7 +234,7 @@ static void mark_fresh(const std::vector<md_pimd_t_x *> &pimds) {
   }
 }
 
-// cluster sizes chosen by the autotuner, per ensemble shape
+// grid sizes (blocks per SM) chosen by the autotuner, per ensemble shape
 static std::mutex g_mu;
 static std::vector<std::pair<std::vector<long long>, int>> g_choice;
 
@@ -245,7 +245,7 @@ static std::vector<long long> signature(const std::vector<xk::EnsSysDesc> &d) {
   return s;
 }
 
-static int chosen_cluster(const std::vector<long long> &sig) {
+static int chosen_blocks(const std::vector<long long> &sig) {
   std::lock_guard<std::mutex> lk(g_mu);
   for (const auto &c : g_choice)
     if (c.first == sig) return c.second;
@@ -258,6 +258,15 @@ static void release_launch(void *p) {
   delete e;
 }
 
+static int check_status(const xk::EnsLaunch &e) {
+  int failed = 0;
+  XMD_CUDA(xk::ensemble_status(e, &failed));
+  if (failed)
+    return fail(MD_GB_ERR_CUDA, "a grid-barrier wait of the persistent ensemble step ran out (not every block was "
+                                "resident); the systems' state is not valid");
+  return 0;
+}
+
 extern "C" {
 
 int md_gb300_capture_ensemble_persistent_x(int n, md_gb300_system_step_fn_x step, void *ctx,
@@ -266,22 +275,44 @@ int md_gb300_capture_ensemble_persistent_x(int n, md_gb300_system_step_fn_x step
   std::vector<xk::EnsSysDesc> descs;
   std::vector<md_pimd_t_x *> pimds;
   XMD_TRY(plan(n, step, ctx, descs, pimds));
-  int cl = chosen_cluster(signature(descs));
-  if (!cl) cl = xk::ensemble_resident_clusters(D, MD_NHC_LENGTH_X, 4) > 0 ? 4 : 1;
+  int bps = chosen_blocks(signature(descs));
+  if (!bps) bps = xk::ensemble_max_blocks_per_sm(D, MD_NHC_LENGTH_X);
+  if (bps < 1) return fail(MD_GB_ERR_UNSUPPORTED, "the persistent ensemble kernel does not fit on an SM");
   xk::EnsLaunch *e = new xk::EnsLaunch();
-  cudaError_t ce = xk::ensemble_prepare(descs.data(), n, D, MD_NHC_LENGTH_X, cl, *e);
+  cudaError_t ce = xk::ensemble_prepare(descs.data(), n, D, MD_NHC_LENGTH_X, bps, *e);
   if (ce != cudaSuccess) {
     delete e;
     return cuda_fail(ce, "persistent ensemble plan");
   }
   const int rc = capture_single(
-      [](void *p) { return xk::ensemble_launch(*(xk::EnsLaunch *)p, stream()); }, e, release_launch, out);
+      [](void *p) { return xk::ensemble_launch(*(xk::EnsLaunch *)p, stream()); }, e, release_launch,
+      GRAPH_ENSEMBLE, out);
   if (rc) return rc;
   mark_fresh(pimds);
   return 0;
 }
 
-int md_gb300_autotune_ensemble_x(int n, md_gb300_system_step_fn_x step, void *ctx, int repeats, int *cluster,
+int md_gb300_ensemble_status_x(md_gb300_graph_t_x *graph) {
+  xk::EnsLaunch *e = (xk::EnsLaunch *)graph_owned(graph, GRAPH_ENSEMBLE);
+  if (!e) return fail(MD_GB_ERR_ARG, "not a persistent ensemble graph");
+  XMD_TRY(join_side());
+  XMD_CUDA(cudaStreamSynchronize(stream()));
+  return check_status(*e);
+}
+
+int md_gb300_ensemble_phase_times_x(md_gb300_graph_t_x *graph, double *us, int n) {
+  xk::EnsLaunch *e = (xk::EnsLaunch *)graph_owned(graph, GRAPH_ENSEMBLE);
+  if (!e || !us || n < 1) return fail(MD_GB_ERR_ARG, "not a persistent ensemble graph, or no room");
+  XMD_TRY(join_side());
+  XMD_CUDA(cudaStreamSynchronize(stream()));
+  int failed = 0;
+  double t[xk::ENS_PHASES];
+  XMD_CUDA(xk::ensemble_status(*e, &failed, t));
+  for (int k = 0; k < n && k < xk::ENS_PHASES; ++k) us[k] = t[k];
+  return xk::ENS_PHASES;
+}
+
+int md_gb300_autotune_ensemble_x(int n, md_gb300_system_step_fn_x step, void *ctx, int repeats, int *blocks_per_sm,
                                  double *ms) {
   if (repeats < 1) repeats = 1;
   std::vector<xk::EnsSysDesc> descs;
@@ -293,33 +324,32 @@ int md_gb300_autotune_ensemble_x(int n, md_gb300_system_step_fn_x step, void *ct
   XMD_CUDA(cudaEventCreate(&b));
   int best = 0;
   double best_ms = 0;
-  cudaError_t ce = cudaSuccess;
-  for (int cl : {1, 2, 4, 8}) {
-    if (xk::ensemble_resident_clusters(D, MD_NHC_LENGTH_X, cl) < 1) continue;
+  int rc = 0;
+  const int fit = xk::ensemble_max_blocks_per_sm(D, MD_NHC_LENGTH_X);
+  for (int bps = 1; bps <= fit && !rc; ++bps) {
     xk::EnsLaunch e;
-    ce = xk::ensemble_prepare(descs.data(), n, D, MD_NHC_LENGTH_X, cl, e);
-    if (ce != cudaSuccess) break;
-    ce = xk::ensemble_launch(e, st);  // warm-up
-    for (int r = 0; r < repeats && ce == cudaSuccess; ++r) {
-      if (r == 0) ce = cudaEventRecord(a, st);
-      if (ce == cudaSuccess) ce = xk::ensemble_launch(e, st);
-    }
+    cudaError_t ce = xk::ensemble_prepare(descs.data(), n, D, MD_NHC_LENGTH_X, bps, e);
+    if (ce == cudaSuccess) ce = xk::ensemble_launch(e, st);  // warm-up
+    if (ce == cudaSuccess) ce = cudaEventRecord(a, st);
+    for (int r = 0; r < repeats && ce == cudaSuccess; ++r) ce = xk::ensemble_launch(e, st);
     if (ce == cudaSuccess) ce = cudaEventRecord(b, st);
     if (ce == cudaSuccess) ce = cudaEventSynchronize(b);
     float t = 0;
     if (ce == cudaSuccess) ce = cudaEventElapsedTime(&t, a, b);
+    if (ce != cudaSuccess) rc = cuda_fail(ce, "ensemble autotuning");
+    if (!rc) rc = check_status(e);
     xk::ensemble_free(e);
-    if (ce != cudaSuccess) break;
+    if (rc) break;
     const double per = t / repeats;
     if (!best || per < best_ms) {
-      best = cl;
+      best = bps;
       best_ms = per;
     }
   }
   cudaEventDestroy(a);
   cudaEventDestroy(b);
-  if (ce != cudaSuccess) return cuda_fail(ce, "ensemble autotuning");
-  if (!best) return fail(MD_GB_ERR_UNSUPPORTED, "no cluster size of the persistent ensemble kernel fits");
+  if (rc) return rc;
+  if (!best) return fail(MD_GB_ERR_UNSUPPORTED, "the persistent ensemble kernel does not fit on an SM");
   {
     std::lock_guard<std::mutex> lk(g_mu);
     const auto sig = signature(descs);
@@ -332,7 +362,7 @@ int md_gb300_autotune_ensemble_x(int n, md_gb300_system_step_fn_x step, void *ct
     if (!found) g_choice.push_back({sig, best});
   }
   mark_fresh(pimds);
-  if (cluster) *cluster = best;
+  if (blocks_per_sm) *blocks_per_sm = best;
   if (ms) *ms = best_ms;
   return 0;
 }

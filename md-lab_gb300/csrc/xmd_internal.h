@@ -164,7 +164,11 @@ int ens_record(int op, md_simulation_t_x *sim, md_pimd_t_x *pimd, double dt, int
 int ens_refuse();  // the error of a device call that is not part of the step
 // a graph of the one launch that launch(ctx) queues on the library stream;
 // release(ctx) runs when the graph is freed (or the capture fails)
-int capture_single(cudaError_t (*launch)(void *), void *ctx, void (*release)(void *), md_gb300_graph_t_x **out);
+int capture_single(cudaError_t (*launch)(void *), void *ctx, void (*release)(void *), int kind,
+                   md_gb300_graph_t_x **out);
+// what a graph from capture_single owns, if it was made with this kind
+void *graph_owned(md_gb300_graph_t_x *g, int kind);
+constexpr int GRAPH_ENSEMBLE = 1;
 
 // read the current potential parameter globals
 xk::TrapPrm trap_params(int kind);

@@ -3483,75 +3483,61 @@ __global__ void k_phase32(Geo g, int ns, const double *__restrict__ x, float2 *_
 }
 
 
-// structure factors as k_sk, FP32 products accumulated in double-float
-template <int NS, int COLS, int GR>
-__global__ void __launch_bounds__(COLS * GR) k_sk32(Geo g, const float2 *__restrict__ ph,
-                                                   const int4 *__restrict__ cols, int ncol,
-                                                   double2 *__restrict__ S, int nk) {
-  constexpr int SK_THREADS = COLS * GR, SK_GROUPS = GR;
-  __shared__ float2 sp[3][NS + 1][SK_CHUNK];
+// structure factors of the mixed form: block (items, slice j) of 256
+// threads, GR threads per item (GR = 1: each item's particles in order,
+// the persistent ensemble's arithmetic; GR = 4 or 16 for large slices with
+// few items: the GR threads take interleaved particles and their
+// accumulators are combined pairwise in a fixed order).  The staged rows
+// are padded by one entry so that the lanes' different rows fall in
+// different banks.
+template <int NS, int GR>
+__global__ void __launch_bounds__(256) k_sk32(Geo g, const float2 *__restrict__ ph, const int4 *__restrict__ cols,
+                                              int ncol, double2 *__restrict__ S, int nk) {
+  constexpr int NGR = (NS + SK_NG - 1) / SK_NG;
+  constexpr int CH = GR == 16 ? 256 : 64, LD = CH + 1;  // particles per staged chunk (whole blocks of SK_PB GR)
+  static_assert(CH % (SK_PB * GR) == 0, "staged chunks hold whole particle blocks");
+  __shared__ float2 sp[3 * (NS + 1) * LD];
   const int j = blockIdx.y;
-  const int gq = threadIdx.x & (SK_GROUPS - 1);
-  const int ci = blockIdx.x * COLS + threadIdx.x / SK_GROUPS;
-  const bool live = ci < ncol;
+  const int gq = threadIdx.x % GR;
+  const int item = blockIdx.x * (256 / GR) + threadIdx.x / GR;
+  const bool live = item < ncol * NGR;
+  const int ci = live ? item / NGR : 0, n0 = live ? (item % NGR) * SK_NG : 0;
   const int4 c = live ? cols[ci] : make_int4(0, 0, 1, 0);
   const int ax = col_nx(c), ay = c.y < 0 ? -c.y : c.y;
   const bool cy = c.y < 0;
-  DF s0r, s0i, P[NS][2], Q[NS][2];
+  SkAcc A;
   const float2 *base = ph + (size_t)j * 3 * (NS + 1) * g.Ns;
-  for (int l0 = 0; l0 < g.N; l0 += SK_CHUNK) {
-    const int cnt = g.N - l0 < SK_CHUNK ? g.N - l0 : SK_CHUNK;
+  for (int l0 = 0; l0 < g.N; l0 += CH) {
+    const int cnt = g.N - l0 < CH ? g.N - l0 : CH;
     __syncthreads();
-    for (int q = threadIdx.x; q < 3 * (NS + 1) * SK_CHUNK; q += SK_THREADS) {
-      const int l = q % SK_CHUNK, row = q / SK_CHUNK;
-      (&sp[0][0][0])[q] = l < cnt ? base[(size_t)row * g.Ns + l0 + l] : make_float2(0.f, 0.f);
+    for (int q = threadIdx.x; q < 3 * (NS + 1) * CH; q += 256) {
+      const int l = q % CH, row = q / CH;
+      sp[row * LD + l] = l < cnt ? base[(size_t)row * g.Ns + l0 + l] : make_float2(0.f, 0.f);
     }
     __syncthreads();
-    if (!live) continue;
-    for (int l = gq; l < cnt; l += SK_GROUPS) {
-      float2 ey = sp[1][ay][l];
-      if (cy) ey.y = -ey.y;
-      const float2 exy = cmulf(sp[0][ax][l], ey);
-      s0r.add(exy.x);
-      s0i.add(exy.y);
+    if (live) sk_item_blocks(A, sp, LD, NS, ax, ay, cy, n0, cnt, gq, GR);
+  }
+  if (GR > 1) {
+    auto comb = [](DF &v, int o) {
+      const float h = __shfl_xor_sync(FULL, v.hi, o), lo = __shfl_xor_sync(FULL, v.lo, o);
+      v.add(h);
+      v.lo += lo;
+    };
 #pragma unroll
-      for (int n = 1; n <= NS; ++n) {
-        const float2 ez = sp[2][n][l];
-        P[n - 1][0].add(exy.x * ez.x);
-        P[n - 1][1].add(exy.y * ez.x);
-        Q[n - 1][0].add(exy.x * ez.y);
-        Q[n - 1][1].add(exy.y * ez.y);
+    for (int o = 1; o < GR; o <<= 1) {
+      comb(A.s0r, o);
+      comb(A.s0i, o);
+#pragma unroll
+      for (int u = 0; u < SK_NG; ++u) {
+        comb(A.P[u][0], o);
+        comb(A.P[u][1], o);
+        comb(A.Q[u][0], o);
+        comb(A.Q[u][1], o);
       }
     }
   }
-  // the column's lanes, pairwise in a fixed order (both parts of each sum)
-  auto comb = [](DF &v, int o) {
-    const float h = __shfl_xor_sync(FULL, v.hi, o), lo = __shfl_xor_sync(FULL, v.lo, o);
-    v.add(h);
-    v.lo += lo;
-  };
-#pragma unroll
-  for (int o = 1; o < SK_GROUPS; o <<= 1) {
-    comb(s0r, o);
-    comb(s0i, o);
-#pragma unroll
-    for (int n = 0; n < NS; ++n) {
-      comb(P[n][0], o);
-      comb(P[n][1], o);
-      comb(Q[n][0], o);
-      comb(Q[n][1], o);
-    }
-  }
   if (!live || gq != 0) return;
-  double2 *o = S + (size_t)j * nk + c.w - c.z;
-  if (c.z <= 0) o[0] = make_double2(s0r.value(), s0i.value());
-#pragma unroll
-  for (int n = 1; n <= NS; ++n) {
-    const double Pr = P[n - 1][0].value(), Pi = P[n - 1][1].value();
-    const double Qr = Q[n - 1][0].value(), Qi = Q[n - 1][1].value();
-    o[n] = make_double2(Pr - Qi, Pi + Qr);
-    if (c.z < 0) o[-n] = make_double2(Pr + Qi, Pi - Qr);
-  }
+  sk_item_store(A, S + (size_t)j * nk, c, NS, n0);
 }
 
 // force tables as k_recip_tables, stored in FP32
@@ -3571,43 +3557,27 @@ __global__ void __launch_bounds__(128) k_recip_force32(Geo g, const float2 *__re
                                                        const float2 *__restrict__ T, double scale,
                                                        double *__restrict__ f) {
   constexpr int NT = 4 * NS + 1;
-  extern __shared__ float smf[];
-  float2 *sT = (float2 *)smf;
+  extern __shared__ __align__(16) float smf[];
+  // the columns (16-byte records first, so that they stay aligned), the x
+  // and y phase factors of the block's 128 particles, and the slice's force
+  // tables, all staged
+  int4 *sc = (int4 *)smf;
+  float2 *pxy = (float2 *)(sc + ncol);
+  float2 *sT = pxy + 2 * (NS + 1) * 128;
   const int j = blockIdx.y;
   const float2 *Tj = T + (size_t)j * ncol * NT;
   for (int q = threadIdx.x; q < ncol * NT; q += blockDim.x) sT[q] = Tj[q];
+  for (int q = threadIdx.x; q < ncol; q += blockDim.x) sc[q] = cols[q];
+  const int l0 = blockIdx.x * 128, li = threadIdx.x, l = l0 + li;
+  const float2 *pj = ph + (size_t)j * 3 * (NS + 1) * g.Ns;
+  for (int r = 0; r < 2 * (NS + 1); ++r) pxy[r * 128 + li] = l < g.N ? pj[(size_t)r * g.Ns + l] : make_float2(0.f, 0.f);
   __syncthreads();
-  const int l = blockIdx.x * blockDim.x + threadIdx.x;
   if (l >= g.N) return;
-  const float2 *pj = ph + (size_t)j * 3 * (NS + 1) * g.Ns + l;
   float2 ez[NS + 1];
 #pragma unroll
-  for (int n = 1; n <= NS; ++n) ez[n] = pj[((size_t)2 * (NS + 1) + n) * g.Ns];
+  for (int n = 1; n <= NS; ++n) ez[n] = pj[((size_t)2 * (NS + 1) + n) * g.Ns + l];
   Kahan Fx, Fy, Fz;
-  for (int ci = 0; ci < ncol; ++ci) {
-    const int4 c = cols[ci];
-    const int nzc = col_nz(c);
-    float2 ey = pj[((size_t)(NS + 1) + (c.y < 0 ? -c.y : c.y)) * g.Ns];
-    if (c.y < 0) ey.y = -ey.y;
-    const float2 exy = cmulf(pj[(size_t)col_nx(c) * g.Ns], ey);
-    const float2 *t = sT + ci * NT;
-    float Ur = t[0].x, Ui = t[0].y, Vr = 0.f, Vi = 0.f;
-#pragma unroll
-    for (int n = 1; n <= NS; ++n) {
-      if (n > nzc) break;  // uniform across the block
-      const float2 A = t[4 * n - 3], B = t[4 * n - 2], nA = t[4 * n - 1], nB = t[4 * n];
-      const float cz = ez[n].x, sz = ez[n].y;
-      Ur = fmaf(cz, A.x, fmaf(-sz, B.y, Ur));
-      Ui = fmaf(cz, A.y, fmaf(sz, B.x, Ui));
-      Vr = fmaf(cz, nB.x, fmaf(-sz, nA.y, Vr));
-      Vi = fmaf(cz, nB.y, fmaf(sz, nA.x, Vi));
-    }
-    const float Tm = fmaf(exy.x, Ui, exy.y * Ur);
-    const float Zm = fmaf(exy.x, Vi, exy.y * Vr);
-    Fx.add((float)col_nx(c) * Tm);
-    Fy.add((float)c.y * Tm);
-    Fz.add(Zm);
-  }
+  recip_cols32<NS>(Fx, Fy, Fz, sc, ncol, sT, NS, pxy, 128, li, ez);
   f[sidx(j, 0, l, 3, g.Ns)] += scale * Fx.value() * g.inv_box[0];
   f[sidx(j, 1, l, 3, g.Ns)] += scale * Fy.value() * g.inv_box[1];
   f[sidx(j, 2, l, 3, g.Ns)] += scale * Fz.value() * g.inv_box[2];
@@ -3628,19 +3598,24 @@ cudaError_t recip_force32(const Geo &g, const Recip &r, const double *x, double 
   const int nc = r.ncol;
   dim3 tgrid((nc + 7) / 8, g.P), tblk(r.nsum + 1, 8);
   dim3 grid((g.N + 127) / 128, g.P);
-  const size_t smem = sizeof(float2) * nc * (4 * r.nsum + 1);
+  const size_t smem =
+      sizeof(float2) * nc * (4 * r.nsum + 1) + sizeof(int4) * nc + sizeof(float2) * 2 * (r.nsum + 1) * 128;
   float2 *T32 = (float2 *)r.T;
   DISPATCH_NS(r.nsum, {
     {
-      // 16 groups per column for large slices at small |n| (registers stay
-      // low); one thread per column otherwise
+      // one thread per item for slices below SK_BIG_N particles; above,
+      // 4 or (few items) 16 threads share an item's particle blocks
       XK_PROF("sk32");
-      if (g.N >= SK_BIG_N && NS <= 6)
-        k_sk32<NS, 16, 16><<<dim3((nc + 15) / 16, g.P), 256, 0, st>>>(g, ph32, (const int4 *)r.kvec, nc,
+      const int items = nc * ((NS + SK_NG - 1) / SK_NG);
+      if (g.N < SK_BIG_N)
+        k_sk32<NS, 1><<<dim3((items + 255) / 256, g.P), 256, 0, st>>>(g, ph32, (const int4 *)r.kvec, nc,
                                                                      (double2 *)r.S, r.nk);
-      else
-        k_sk32<NS, 64, 1><<<dim3((nc + 63) / 64, g.P), 64, 0, st>>>(g, ph32, (const int4 *)r.kvec, nc,
+      else if (items > 64 || NS > 6)
+        k_sk32<NS, 4><<<dim3((items + 63) / 64, g.P), 256, 0, st>>>(g, ph32, (const int4 *)r.kvec, nc,
                                                                    (double2 *)r.S, r.nk);
+      else
+        k_sk32<(NS <= 6 ? NS : 6), 16><<<dim3((items + 15) / 16, g.P), 256, 0, st>>>(
+            g, ph32, (const int4 *)r.kvec, nc, (double2 *)r.S, r.nk);
     }
     {
       XK_PROF("recip_tables32");

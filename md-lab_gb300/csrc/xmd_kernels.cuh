@@ -325,17 +325,24 @@ struct EnsSysDesc {
   double inv_mP;        // 1 / (m P) of the reciprocal forces
 };
 struct EnsLaunch {
-  void *plan = nullptr;  // device descriptors and the clusters' system lists
-  int D = 0, L = 0, cluster = 0, clusters = 0, nsys = 0;
+  void *plan = nullptr;  // device descriptors, grid barrier, FP32 pair scratch
+  void *bar = nullptr;
+  int D = 0, L = 0, blocks = 0, nsys = 0;
   size_t smem = 0;
 };
-// thread blocks per cluster the kernel can run with (1, 2, 4, 8); the
-// number of clusters of that size that stay resident (0: none fits)
-int ensemble_resident_clusters(int D, int L, int cluster);
-// the systems spread over the resident clusters by estimated cost (longest
-// first, each to the least loaded cluster); descriptors uploaded to e.plan
-cudaError_t ensemble_prepare(const EnsSysDesc *sys, int n, int D, int L, int cluster, EnsLaunch &e);
+// thread blocks of the persistent kernel that fit on one SM (0: none)
+int ensemble_max_blocks_per_sm(int D, int L);
+// descriptors uploaded (largest systems first) for a grid of
+// blocks_per_sm x SMs blocks (capped at what fits)
+cudaError_t ensemble_prepare(const EnsSysDesc *sys, int n, int D, int L, int blocks_per_sm, EnsLaunch &e);
 cudaError_t ensemble_launch(const EnsLaunch &e, cudaStream_t st);
+// *failed = 1 when a grid-barrier wait of an earlier launch gave up (its
+// step and every later one did not run to completion); phase_us (optional,
+// ENS_PHASES values): the last launch's phase durations as block 0 saw them
+// (the phases end at the grid barriers; the last one at block 0's own end).
+// Synchronous.
+constexpr int ENS_PHASES = 9;
+cudaError_t ensemble_status(const EnsLaunch &e, int *failed, double *phase_us = nullptr);
 void ensemble_free(EnsLaunch &e);
 // the supported shapes: N <= ENS_MAX_N, L in {4, 8}, D in 1..3, n_sum <= 11
 constexpr int ENS_MAX_N = 2048;

@@ -603,11 +603,15 @@ struct md_gb300_graph {
   cudaGraphExec_t e = nullptr;
   void (*release)(void *) = nullptr;  // frees what the graph's kernels read (owned)
   void *owned = nullptr;
+  int kind = 0;  // what owned is (capture_single's caller)
 };
 
 namespace xmd {
 
-int capture_single(cudaError_t (*launch)(void *), void *ctx, void (*release)(void *), md_gb300_graph_t_x **out) {
+void *graph_owned(md_gb300_graph_t_x *g, int kind) { return g && g->kind == kind ? g->owned : nullptr; }
+
+int capture_single(cudaError_t (*launch)(void *), void *ctx, void (*release)(void *), int kind,
+                   md_gb300_graph_t_x **out) {
   if (capturing()) {
     release(ctx);
     return fail(MD_GB_ERR_CAPTURE, "already capturing");
@@ -634,6 +638,7 @@ int capture_single(cudaError_t (*launch)(void *), void *ctx, void (*release)(voi
   }
   gr->release = release;
   gr->owned = ctx;
+  gr->kind = kind;
   *out = gr;
   return 0;
 }

@@ -182,6 +182,8 @@ class XLib:
                 "md_gb300_capture_ensemble_x": (_i, [_i, _vp, _vp, C.POINTER(_vp)]),
                 "md_gb300_capture_ensemble_persistent_x": (_i, [_i, _vp, _vp, C.POINTER(_vp)]),
                 "md_gb300_autotune_ensemble_x": (_i, [_i, _vp, _vp, _i, C.POINTER(_i), _dp]),
+                "md_gb300_ensemble_status_x": (_i, [_vp]),
+                "md_gb300_ensemble_phase_times_x": (_i, [_vp, _dp, _i]),
                 "md_gb300_ewald_model_nparam_x": (_i, []),
                 "md_gb300_ewald_model_create_x": (_i, [C.POINTER(_vp), pp, _i, C.c_long, C.c_uint]),
                 "md_gb300_ewald_model_free_x": (None, [_vp]),

@@ -206,7 +206,7 @@ def test_persistent_ensemble_matches_individual_steps(lib):
                                                              C.byref(g)), "persistent capture")
         assert lib.md_gb300_graph_kernel_count_x(g) == 1
         lib.check(lib.md_gb300_graph_launch_x(g, 3))
-        lib.check(lib.md_gb300_synchronize_x())
+        lib.check(lib.md_gb300_ensemble_status_x(g), "persistent step status")
         for _ in range(3):
             for (s, box), sp in zip(ref, PERSISTENT):
                 persistent_step(lib, sp, s, box)
@@ -235,24 +235,26 @@ def test_persistent_ensemble_matches_individual_steps(lib):
 
 
 def test_persistent_ensemble_autotuner_and_refusals(lib):
-    """The cluster-size autotuner picks a size that runs; the capture then
-    uses it and still matches the per-system calls.  A step with a call that
-    is not part of the reference driver's step, or in FP64 mode, is refused."""
+    """The grid-size autotuner picks a size that runs; the capture then uses
+    it and still matches the per-system calls.  A step with a call that is
+    not part of the reference driver's step, or in FP64 mode, is refused."""
     lib.check(lib.md_gb300_set_precision_x(1))
     try:
         ens, ref, fn = _persistent_pair(lib)
-        cl, ms = C.c_int(), C.c_double()
-        lib.check(lib.md_gb300_autotune_ensemble_x(len(PERSISTENT), C.cast(fn, C.c_void_p), None, 2, C.byref(cl),
+        bps, ms = C.c_int(), C.c_double()
+        lib.check(lib.md_gb300_autotune_ensemble_x(len(PERSISTENT), C.cast(fn, C.c_void_p), None, 2, C.byref(bps),
                                                    C.byref(ms)), "ensemble autotune")
-        assert cl.value in (1, 2, 4, 8) and ms.value > 0
-        # the autotuner advanced every system by 4 x (2 + 1) steps
-        for _ in range(4 * 3):
-            for (s, box), sp in zip(ref, PERSISTENT):
-                persistent_step(lib, sp, s, box)
+        assert bps.value in (1, 2) and ms.value > 0
+        # the autotuner advanced the systems: the per-system copies restart
+        # from their state
+        for (a, _), (b, _) in zip(ens, ref):
+            st = a.state()
+            b.set_state(**st)
         g = C.c_void_p()
         lib.check(lib.md_gb300_capture_ensemble_persistent_x(len(PERSISTENT), C.cast(fn, C.c_void_p), None,
                                                              C.byref(g)), "persistent capture")
         lib.check(lib.md_gb300_graph_launch_x(g, 2))
+        lib.check(lib.md_gb300_ensemble_status_x(g), "persistent step status")
         for _ in range(2):
             for (s, box), sp in zip(ref, PERSISTENT):
                 persistent_step(lib, sp, s, box)
