@@ -605,9 +605,9 @@ def ensemble_form(lib, R, args):
     # one persistent kernel per step: grid size by the autotuner (which
     # advances the systems by the steps it times), then captured
     ms_br, kernels_br = ms, kernels
-    cl, tms = C.c_int(), C.c_double()
+    cl, grp, tms = C.c_int(), C.c_int(), C.c_double()
     lib.check(lib.md_gb300_autotune_ensemble_x(len(systems), C.cast(fn, C.c_void_p), None, 3, C.byref(cl),
-                                               C.byref(tms)), "persistent ensemble autotuning")
+                                               C.byref(grp), C.byref(tms)), "persistent ensemble autotuning")
     gp = C.c_void_p()
     lib.check(lib.md_gb300_capture_ensemble_persistent_x(len(systems), C.cast(fn, C.c_void_p), None, C.byref(gp)),
               "persistent ensemble capture")
@@ -627,7 +627,8 @@ def ensemble_form(lib, R, args):
     xmd_x.set_potentials(lib, coul_s=1.0, alpha=ALPHA_L / box, nsum=NSUM)
     return {"value": beads / (ms * 1e-3), "unit": "bead-steps/s", "ms_per_step": ms, "systems": len(specs),
             "bead_slots": beads, "kernels_per_launch": kernels, "steps_timed": nst,
-            "persistent_blocks_per_sm": cl.value, "persistent_phase_us": phase_us, "autotuned_ms": tms.value, "wall_s_timed": wall,
+            "persistent_blocks_per_sm": cl.value, "persistent_groups": grp.value,
+            "persistent_phase_us_group0": phase_us, "autotuned_ms": tms.value, "wall_s_timed": wall,
             "graph_branches_wall_s_timed": wall_br,
             "graph_branches_ms_per_step": ms_br, "graph_branches_kernels": kernels_br,
             "gain_vs_graph_branches": ms_br / ms,

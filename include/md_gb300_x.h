@@ -66,7 +66,8 @@ typedef int (*md_gb300_system_step_fn_x)(int system, void *ctx);
 int md_gb300_capture_ensemble_x(int n, md_gb300_system_step_fn_x step, void *ctx, md_gb300_graph_t_x **graph);
 /* The same ensemble step as ONE persistent kernel launch (captured into a
    graph): the step's stages are nine phases, each holding that stage's work
-   of every system spread over the whole GPU, separated by grid barriers
+   of every system of a group of blocks spread over the group, separated by
+   the group's barriers
    (a cooperative launch of exactly the blocks that fit; a barrier wait that
    runs out, about a second, ends the kernel instead of hanging and is
    reported by md_gb300_ensemble_status_x).  While planning, step(i, ctx)'s
@@ -79,9 +80,9 @@ int md_gb300_capture_ensemble_x(int n, md_gb300_system_step_fn_x step, void *ctx
    MD_GB_PRECISION_MIXED (FP32) with equal bead masses, one-DOF thermostat
    chains of length 4 or 8, P >= 2, N <= 2048, no learned model attached.
    Other calls are refused (MD_GB_ERR_UNSUPPORTED).  The results equal those
-   of the per-system calls.  The grid is the blocks per SM that
-   md_gb300_autotune_ensemble_x chose for this ensemble's shapes, else all
-   that fit. */
+   of the per-system calls.  The grid is the shape that
+   md_gb300_autotune_ensemble_x chose for this ensemble's shapes, else 2
+   blocks per SM in 4 groups. */
 int md_gb300_capture_ensemble_persistent_x(int n, md_gb300_system_step_fn_x step, void *ctx,
                                            md_gb300_graph_t_x **graph);
 /* 0 when every launch of a persistent ensemble graph so far completed its
@@ -95,12 +96,16 @@ int md_gb300_ensemble_status_x(md_gb300_graph_t_x *graph);
    half step), as one block saw them; returns the number of phases.
    Synchronises. */
 int md_gb300_ensemble_phase_times_x(md_gb300_graph_t_x *graph, double *us, int n);
-/* Times the persistent step at each grid size that fits (1 or 2 blocks per
-   SM; `repeats` + 1 launches each, so the systems advance by those steps)
-   and records the fastest for this ensemble's shapes; *blocks_per_sm and *ms
-   (may be NULL) receive it and its time per step. */
+/* Times the persistent step at each grid shape: 2 or 3 blocks per SM (the
+   latter with the kernel compiled for three) and the blocks split into 1,
+   2, 4, 8, 16 or 32 groups, each stepping its share of the systems (spread by
+   estimated cost) with its own barriers, so that the groups' phases drift
+   apart and one group's FP64 thermostat overlaps another's FP32 sums.
+   Each shape runs `repeats` + 1 launches, so the systems advance by those
+   steps.  The fastest is recorded for this ensemble's shapes; *blocks_per_sm,
+   *groups and *ms (may be NULL) receive it and its time per step. */
 int md_gb300_autotune_ensemble_x(int n, md_gb300_system_step_fn_x step, void *ctx, int repeats, int *blocks_per_sm,
-                                 double *ms);
+                                 int *groups, double *ms);
 /* kernel nodes in a captured graph (kernels launched per replay) */
 int md_gb300_graph_kernel_count_x(md_gb300_graph_t_x *graph);
 void md_gb300_graph_free_x(md_gb300_graph_t_x *graph);

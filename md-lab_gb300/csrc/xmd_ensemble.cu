@@ -243,23 +243,32 @@ __device__ inline long long ens_first(long long me, int rot, long long stride) {
 // One step of every system.  Each phase's work of ALL systems is spread over
 // the whole grid (threads, warps or blocks, round-robin over the tasks of the
 // systems in turn); the phases are separated by grid barriers.
-template <int D, int L>
-__global__ void __launch_bounds__(ENS_T, 2) k_ensemble_step(const EnsSys *__restrict__ sys, int nsys, EnsBar *bar,
-                                                            long long limit) {
+template <int D, int L, int MINB>
+__global__ void __launch_bounds__(ENS_T, MINB) k_ensemble_step(const EnsSys *__restrict__ sys,
+                                                               const int *__restrict__ goff, int K, EnsBar *bars,
+                                                               long long limit) {
   extern __shared__ __align__(16) unsigned char ens_sh[];
+  // K groups of blocks (block b in group b mod K), each stepping its own
+  // systems sys[goff[k] .. goff[k+1]) with its own barriers: the groups'
+  // phases drift apart, so one group's FP64 thermostat runs beside another
+  // group's FP32 sums on the same SMs
+  const int grp = blockIdx.x % K;
+  EnsBar *bar = bars + grp;
   if (*(volatile int *)&bar->err) return;  // an earlier step's barrier gave up
-  const unsigned int G = gridDim.x;
+  const unsigned int G = gridDim.x / K;
+  const int i0 = goff[grp], i1 = goff[grp + 1];
   const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  const long long rank = blockIdx.x / K;
   const long long GT = (long long)G * ENS_T, GW = (long long)G * ENS_W;
-  const long long gt = (long long)blockIdx.x * ENS_T + tid, gw = (long long)blockIdx.x * ENS_W + w;
-  const long long gb = blockIdx.x;
+  const long long gt = rank * ENS_T + tid, gw = rank * ENS_W + w;
+  const long long gb = rank;
   ens_stamp(bar, 0);
 
   // A: first half step (md_update_nhc_VV3_1_x); the forces restart from the
   // trap's (md_reset_force_x, md_pimd_calc_trap_force_x); FP32 positions and
   // phase factors of the new positions
   {
-    for (int i = 0; i < nsys; ++i) {
+    for (int i = i0; i < i1; ++i) {
       const EnsSys &E = sys[i];
       const EnsSysDesc &d = E.d;
       const Geo g = d.g;
@@ -286,7 +295,7 @@ __global__ void __launch_bounds__(ENS_T, 2) k_ensemble_step(const EnsSys *__rest
   // B: interior ring springs into fex; E_l^(1) and the prefix-sum increments
   // (md_pimd_fast_fill_ENk_x); FP32 pair tiles; structure factors
   {
-    for (int i = 0; i < nsys; ++i) {
+    for (int i = i0; i < i1; ++i) {
       const EnsSysDesc &d = sys[i].d;
       const Geo g = d.g;
       const long long n = g.P > 2 ? (long long)(g.P - 2) * g.Ns : 0;
@@ -297,13 +306,13 @@ __global__ void __launch_bounds__(ENS_T, 2) k_ensemble_step(const EnsSys *__rest
     }
   }
   {
-    for (int i = 0; i < nsys; ++i) {
+    for (int i = i0; i < i1; ++i) {
       const EnsSysDesc &d = sys[i].d;
       const Geo g = d.g;
       for (long long l = ens_first(gw, sys[i].rot[R_B_EINT], GW); l < g.N; l += GW)
         eint_particle<D>(g, d.x, d.m, d.w2, d.image, d.Eint, d.ENk, d.gl, (int)l, lane);
     }
-    for (int i = 0; i < nsys; ++i) {
+    for (int i = i0; i < i1; ++i) {
       const EnsSys &E = sys[i];
       if (!E.d.pair_kind) continue;
       const long long n = (long long)E.jobs * E.d.g.P;
@@ -311,7 +320,7 @@ __global__ void __launch_bounds__(ENS_T, 2) k_ensemble_step(const EnsSys *__rest
     }
   }
   if constexpr (D == 3) {
-    for (int i = 0; i < nsys; ++i) {
+    for (int i = i0; i < i1; ++i) {
       const EnsSys &E = sys[i];
       if (!E.ewald) continue;
       for (long long j = ens_first(gb, sys[i].rot[R_B_SK], G); j < E.d.g.P; j += G) ens_sk_slice(E, (int)j, (float2 *)ens_sh);
@@ -323,7 +332,7 @@ __global__ void __launch_bounds__(ENS_T, 2) k_ensemble_step(const EnsSys *__rest
   // C: prefix sums of the increments (a block per system, the block size of
   // k_enk_direct's own scan, into gl[N ..]); the FP32 force tables
   {
-    for (int i = 0; i < nsys; ++i) {
+    for (int i = i0; i < i1; ++i) {
       const EnsSysDesc &d = sys[i].d;
       if (d.g.N < 2) continue;
       if (ens_first(gb, sys[i].rot[R_C_PRE], G) == 0) {
@@ -333,7 +342,7 @@ __global__ void __launch_bounds__(ENS_T, 2) k_ensemble_step(const EnsSys *__rest
     }
   }
   if constexpr (D == 3) {
-    for (int i = 0; i < nsys; ++i) {
+    for (int i = i0; i < i1; ++i) {
       const EnsSys &E = sys[i];
       if (!E.ewald) continue;
       const int per = E.ns + 1;
@@ -350,7 +359,7 @@ __global__ void __launch_bounds__(ENS_T, 2) k_ensemble_step(const EnsSys *__rest
 
   // D: the cycle energies E_l^(k), k >= 2; reciprocal forces
   {
-    for (int i = 0; i < nsys; ++i) {
+    for (int i = i0; i < i1; ++i) {
       const EnsSysDesc &d = sys[i].d;
       const Geo g = d.g;
       const long long n = (long long)g.N * (g.N - 1) / 2;
@@ -365,7 +374,7 @@ __global__ void __launch_bounds__(ENS_T, 2) k_ensemble_step(const EnsSys *__rest
     }
   }
   if constexpr (D == 3) {
-    for (int i = 0; i < nsys; ++i) {
+    for (int i = i0; i < i1; ++i) {
       const EnsSys &E = sys[i];
       if (!E.ewald) continue;
       for (long long j = ens_first(gb, sys[i].rot[R_D_REC], G); j < E.d.g.P; j += G) ens_recip_slice(E, (int)j, ens_sh);
@@ -377,7 +386,7 @@ __global__ void __launch_bounds__(ENS_T, 2) k_ensemble_step(const EnsSys *__rest
   // E: weight rows of both recursions and the diagonal-block inverses
   // (md_pimd_fill_VB_x); the pair tiles' partial sums into f
   {
-    for (int i = 0; i < nsys; ++i) {
+    for (int i = i0; i < i1; ++i) {
       const EnsSys &E = sys[i];
       const EnsSysDesc &d = E.d;
       const int N = d.g.N;
@@ -387,7 +396,7 @@ __global__ void __launch_bounds__(ENS_T, 2) k_ensemble_step(const EnsSys *__rest
     }
   }
   {
-    for (int i = 0; i < nsys; ++i) {
+    for (int i = i0; i < i1; ++i) {
       const EnsSys &E = sys[i];
       if (!E.d.pair_kind) continue;
       const Geo g = E.d.g;
@@ -404,7 +413,7 @@ __global__ void __launch_bounds__(ENS_T, 2) k_ensemble_step(const EnsSys *__rest
   {
     double(*Am)[TS_LD] = (double(*)[TS_LD])ens_sh;
     int(*Ae)[TS_LD] = (int(*)[TS_LD])(ens_sh + sizeof(double) * TS_CHUNK * TS_LD);
-    for (int i = 0; i < nsys; ++i) {
+    for (int i = i0; i < i1; ++i) {
       const EnsSys &E = sys[i];
       const EnsSysDesc &d = E.d;
       const int N = d.g.N, nch = (N + TS_CHUNK - 1) / TS_CHUNK;
@@ -428,7 +437,7 @@ __global__ void __launch_bounds__(ENS_T, 2) k_ensemble_step(const EnsSys *__rest
 
   // F: the forward (V_B) and backward (tmpV) block solves, a block each
   {
-    for (int i = 0; i < nsys; ++i) {
+    for (int i = i0; i < i1; ++i) {
       const EnsSys &E = sys[i];
       for (long long dir = ens_first(gb, sys[i].rot[R_F], G); dir < 2; dir += G) {
         __syncthreads();
@@ -442,7 +451,7 @@ __global__ void __launch_bounds__(ENS_T, 2) k_ensemble_step(const EnsSys *__rest
   // G: cycle probabilities G from the extended-range numbers
   // (md_pimd_fast_fill_force_VB_x)
   {
-    for (int i = 0; i < nsys; ++i) {
+    for (int i = i0; i < i1; ++i) {
       const EnsSys &E = sys[i];
       const int N = E.d.g.N;
       const long long n = (long long)N * N;
@@ -456,7 +465,7 @@ __global__ void __launch_bounds__(ENS_T, 2) k_ensemble_step(const EnsSys *__rest
 
   // H: G-weighted springs of the end beads, partial sums per partner split
   {
-    for (int i = 0; i < nsys; ++i) {
+    for (int i = i0; i < i1; ++i) {
       const EnsSys &E = sys[i];
       const EnsSysDesc &d = E.d;
       const Geo g = d.g;
@@ -475,7 +484,7 @@ __global__ void __launch_bounds__(ENS_T, 2) k_ensemble_step(const EnsSys *__rest
   // I: the end beads' exchange forces into fex, the second half step with
   // f + fex (md_update_nhc_VV3_2_x), the periodic wrap
   {
-    for (int i = 0; i < nsys; ++i) {
+    for (int i = i0; i < i1; ++i) {
       const EnsSys &E = sys[i];
       const EnsSysDesc &d = E.d;
       const Geo g = d.g;
@@ -510,16 +519,19 @@ __global__ void __launch_bounds__(ENS_T, 2) k_ensemble_step(const EnsSys *__rest
 
 // ---- host side ----------------------------------------------------------
 
-using EnsFn = void (*)(const EnsSys *, int, EnsBar *, long long);
+using EnsFn = void (*)(const EnsSys *, const int *, int, EnsBar *, long long);
 
-static EnsFn ens_kernel(int D, int L) {
+// the kernel compiled for 2 blocks per SM (128 registers) or 3 (80
+// registers, some spilled to local memory)
+static EnsFn ens_kernel(int D, int L, int bps) {
+  const bool three = bps >= 3;
   switch (D * 16 + L) {
-    case 1 * 16 + 4: return k_ensemble_step<1, 4>;
-    case 1 * 16 + 8: return k_ensemble_step<1, 8>;
-    case 2 * 16 + 4: return k_ensemble_step<2, 4>;
-    case 2 * 16 + 8: return k_ensemble_step<2, 8>;
-    case 3 * 16 + 4: return k_ensemble_step<3, 4>;
-    case 3 * 16 + 8: return k_ensemble_step<3, 8>;
+    case 1 * 16 + 4: return three ? k_ensemble_step<1, 4, 3> : k_ensemble_step<1, 4, 2>;
+    case 1 * 16 + 8: return three ? k_ensemble_step<1, 8, 3> : k_ensemble_step<1, 8, 2>;
+    case 2 * 16 + 4: return three ? k_ensemble_step<2, 4, 3> : k_ensemble_step<2, 4, 2>;
+    case 2 * 16 + 8: return three ? k_ensemble_step<2, 8, 3> : k_ensemble_step<2, 8, 2>;
+    case 3 * 16 + 4: return three ? k_ensemble_step<3, 4, 3> : k_ensemble_step<3, 4, 2>;
+    case 3 * 16 + 8: return three ? k_ensemble_step<3, 8, 3> : k_ensemble_step<3, 8, 2>;
     default: return nullptr;
   }
 }
@@ -536,17 +548,21 @@ static cudaError_t ens_opt_in(EnsFn fn) {
 }
 
 int ensemble_max_blocks_per_sm(int D, int L) {
-  EnsFn fn = ens_kernel(D, L);
-  if (!fn || ens_opt_in(fn) != cudaSuccess) {
-    cudaGetLastError();
-    return 0;
+  int best = 0;
+  for (int bps : {2, 3}) {
+    EnsFn fn = ens_kernel(D, L, bps);
+    if (!fn || ens_opt_in(fn) != cudaSuccess) {
+      cudaGetLastError();
+      continue;
+    }
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, ENS_T, ENS_SMEM) != cudaSuccess) {
+      cudaGetLastError();
+      continue;
+    }
+    if (n > best) best = n > 3 ? 3 : n;
   }
-  int n = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, ENS_T, ENS_SMEM) != cudaSuccess) {
-    cudaGetLastError();
-    return 0;
-  }
-  return n;
+  return best;
 }
 
 static int sm_count() {
@@ -556,14 +572,32 @@ static int sm_count() {
   return n > 0 ? n : 1;
 }
 
-cudaError_t ensemble_prepare(const EnsSysDesc *sd, int n, int D, int L, int blocks_per_sm, EnsLaunch &out) {
-  if (n < 1 || !ens_kernel(D, L)) return cudaErrorInvalidValue;
+// estimated cost of a system's step, for spreading the systems over the
+// groups (FP64 operations, with the FP32 work counted at a sixteenth)
+static double ens_cost(const EnsSys &E) {
+  const Geo &g = E.d.g;
+  const double slots = (double)g.slots(), N = g.N, P = g.P;
+  double c = 2.0e4 + 220.0 * slots + 60.0 * N * N;
+  if (E.d.pair_kind) c += (double)E.jobs * P * 1024.0 * 60.0 / 16.0;
+  if (E.ewald) {
+    const double ngr = (E.ns + SK_NG - 1) / SK_NG;
+    c += P * E.ncol * (E.ns + 1) * 24.0 + P * N * E.ncol * (ngr * 34.0 + 45.0) / 16.0;
+  }
+  return c;
+}
+
+cudaError_t ensemble_prepare(const EnsSysDesc *sd, int n, int D, int L, int blocks_per_sm, int groups,
+                             EnsLaunch &out) {
+  if (n < 1 || !ens_kernel(D, L, 2) || groups < 1 || groups > ENS_MAX_GROUPS) return cudaErrorInvalidValue;
   const int fit = ensemble_max_blocks_per_sm(D, L);
   if (fit < 1 || blocks_per_sm < 1) return cudaErrorInvalidConfiguration;
   if (blocks_per_sm > fit) blocks_per_sm = fit;
-  std::vector<EnsSys> sys(n);
+  const int K = groups < n ? groups : n;
+  const int blocks = (blocks_per_sm * sm_count()) / K * K;
+  const long long Gk = blocks / K;
+  std::vector<EnsSys> all(n);
   for (int i = 0; i < n; ++i) {
-    EnsSys &E = sys[i];
+    EnsSys &E = all[i];
     memset(&E, 0, sizeof(E));
     E.d = sd[i];
     const Geo &g = E.d.g;
@@ -590,22 +624,38 @@ cudaError_t ensemble_prepare(const EnsSysDesc *sd, int n, int D, int L, int bloc
     E.lnvi = E.d.vi != 0.0 ? log(E.d.vi) : 0.0;
     E.pscale = 1.0 / g.P;
   }
-  // the systems (largest first, so that the round-robin of each phase
-  // starts with the longest tasks), the grid barrier, then the FP32 pair
-  // scratch of every system (tile partials, FP32 positions), kept in the
-  // plan so that no later call can move it
-  std::stable_sort(sys.begin(), sys.end(), [](const EnsSys &a, const EnsSys &b) {
-    return (double)a.d.g.N * a.d.g.N * a.d.g.P > (double)b.d.g.N * b.d.g.N * b.d.g.P;
-  });
-  // each kind's tasks numbered over the systems in this order (as the
-  // kernel's loops number them); rot = tasks before the system, mod workers
-  {
-    const long long G = (long long)blocks_per_sm * sm_count();
-    const long long stride[ENS_NROT] = {G * ENS_T, G * ENS_T, G * ENS_W, G * ENS_W, G, G, G * ENS_T, G * ENS_T,
-                                        G, G * ENS_W, G * ENS_T, G, G, G * ENS_T, G, G * ENS_T};
+  // longest first, each to the least loaded group; each group's systems
+  // contiguous, its largest first (the round-robin of each phase then starts
+  // with the longest tasks)
+  std::vector<int> order(n);
+  std::vector<double> cost(n);
+  for (int i = 0; i < n; ++i) {
+    order[i] = i;
+    cost[i] = ens_cost(all[i]);
+  }
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return cost[x] > cost[y]; });
+  std::vector<std::vector<int>> lists(K);
+  std::vector<double> load(K, 0.0);
+  for (int i : order) {
+    const int k = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+    lists[k].push_back(i);
+    load[k] += cost[i];
+  }
+  std::vector<EnsSys> sys;
+  std::vector<int> goff(K + 1, 0);
+  for (int k = 0; k < K; ++k) {
+    for (int i : lists[k]) sys.push_back(all[i]);
+    goff[k + 1] = (int)sys.size();
+  }
+  // each kind's tasks numbered over the group's systems in this order (as
+  // the kernel's loops number them); rot = tasks before the system, mod the
+  // group's workers of that kind
+  for (int k = 0; k < K; ++k) {
+    const long long stride[ENS_NROT] = {Gk * ENS_T, Gk * ENS_T, Gk * ENS_W, Gk * ENS_W, Gk, Gk, Gk * ENS_T, Gk * ENS_T,
+                                        Gk, Gk * ENS_W, Gk * ENS_T, Gk, Gk, Gk * ENS_T, Gk, Gk * ENS_T};
     long long base[ENS_NROT] = {};
     for (int pass = 0; pass < 2; ++pass)  // the pair tiles continue E_l^(1)'s numbering
-      for (int i = 0; i < n; ++i) {
+      for (int i = goff[k]; i < goff[k + 1]; ++i) {
         EnsSys &E = sys[i];
         const Geo &g = E.d.g;
         const long long slots = (long long)g.slots(), N = g.N, P = g.P;
@@ -626,16 +676,20 @@ cudaError_t ensemble_prepare(const EnsSysDesc *sd, int n, int D, int L, int bloc
         cnt[R_G] = N * N;
         cnt[R_H] = (long long)((g.N + 31) / 32) * E.nsplit;
         cnt[R_I] = slots;
-        for (int k = 0; k < ENS_NROT; ++k) {
-          if ((k == R_B_PAIR) != (pass == 1)) continue;
-          if (pass == 1 && i == 0) base[R_B_PAIR] = base[R_B_EINT];
-          E.rot[k] = (int)(base[k] % stride[k]);
-          base[k] += cnt[k];
+        for (int q = 0; q < ENS_NROT; ++q) {
+          if ((q == R_B_PAIR) != (pass == 1)) continue;
+          if (pass == 1 && i == goff[k]) base[R_B_PAIR] = base[R_B_EINT];
+          E.rot[q] = (int)(base[q] % stride[q]);
+          base[q] += cnt[q];
         }
       }
   }
-  const size_t bar_at = (sizeof(EnsSys) * n + 255) & ~(size_t)255;
-  const size_t head = bar_at + 256;
+  // the systems, the group offsets, the groups' barriers, then the FP32 pair
+  // scratch of every system (tile partials, FP32 positions), kept in the
+  // plan so that no later call can move it
+  const size_t goff_at = (sizeof(EnsSys) * n + 255) & ~(size_t)255;
+  const size_t bar_at = (goff_at + sizeof(int) * (K + 1) + 255) & ~(size_t)255;
+  const size_t head = bar_at + ((sizeof(EnsBar) * K + 255) & ~(size_t)255);
   std::vector<size_t> at(n, 0);
   size_t bytes = head;
   for (int i = 0; i < n; ++i) {
@@ -653,6 +707,7 @@ cudaError_t ensemble_prepare(const EnsSysDesc *sd, int n, int D, int L, int bloc
   }
   std::vector<unsigned char> host(head, 0);
   memcpy(host.data(), sys.data(), sizeof(EnsSys) * n);
+  memcpy(host.data() + goff_at, goff.data(), sizeof(int) * (K + 1));
   e = cudaMemcpy(plan, host.data(), head, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) {
     cudaFree(plan);
@@ -660,17 +715,20 @@ cudaError_t ensemble_prepare(const EnsSysDesc *sd, int n, int D, int L, int bloc
   }
   ensemble_free(out);
   out.plan = plan;
+  out.goff = (unsigned char *)plan + goff_at;
   out.bar = (unsigned char *)plan + bar_at;
   out.D = D;
   out.L = L;
-  out.blocks = blocks_per_sm * sm_count();
+  out.blocks = blocks;
+  out.bps = blocks_per_sm;
+  out.groups = K;
   out.nsys = n;
   out.smem = ENS_SMEM;
   return cudaSuccess;
 }
 
 cudaError_t ensemble_launch(const EnsLaunch &e, cudaStream_t st) {
-  EnsFn fn = ens_kernel(e.D, e.L);
+  EnsFn fn = ens_kernel(e.D, e.L, e.bps);
   if (!fn || !e.plan) return cudaErrorInvalidValue;
   cudaError_t oe = ens_opt_in(fn);
   if (oe != cudaSuccess) return oe;
@@ -688,19 +746,21 @@ cudaError_t ensemble_launch(const EnsLaunch &e, cudaStream_t st) {
   cfg.numAttrs = 1;
   {
     XK_PROF("ensemble_step");
-    oe = cudaLaunchKernelEx(&cfg, fn, (const EnsSys *)e.plan, e.nsys, (EnsBar *)e.bar, ENS_WAIT_LIMIT);
+    oe = cudaLaunchKernelEx(&cfg, fn, (const EnsSys *)e.plan, (const int *)e.goff, e.groups, (EnsBar *)e.bar,
+                            ENS_WAIT_LIMIT);
   }
   if (oe != cudaSuccess) return oe;
   return XK_LAUNCHED();
 }
 
 cudaError_t ensemble_status(const EnsLaunch &e, int *failed, double *phase_us) {
-  EnsBar b{};
-  cudaError_t r = cudaMemcpy(&b, e.bar, sizeof(b), cudaMemcpyDeviceToHost);
+  std::vector<EnsBar> b(e.groups);
+  cudaError_t r = cudaMemcpy(b.data(), e.bar, sizeof(EnsBar) * e.groups, cudaMemcpyDeviceToHost);
   if (r != cudaSuccess) return r;
-  *failed = b.err;
+  *failed = 0;
+  for (const EnsBar &x : b) *failed |= x.err;
   if (phase_us)
-    for (int k = 0; k < ENS_PHASES; ++k) phase_us[k] = (double)(b.stamp[k + 1] - b.stamp[k]) * 1e-3;
+    for (int k = 0; k < ENS_PHASES; ++k) phase_us[k] = (double)(b[0].stamp[k + 1] - b[0].stamp[k]) * 1e-3;
   return r;
 }
 

@@ -13,6 +13,7 @@
 // systems.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -234,9 +235,9 @@ static void mark_fresh(const std::vector<md_pimd_t_x *> &pimds) {
   }
 }
 
-// grid sizes (blocks per SM) chosen by the autotuner, per ensemble shape
+// grid shapes (blocks per SM, groups) chosen by the autotuner, per ensemble shape
 static std::mutex g_mu;
-static std::vector<std::pair<std::vector<long long>, int>> g_choice;
+static std::vector<std::pair<std::vector<long long>, std::pair<int, int>>> g_choice;
 
 static std::vector<long long> signature(const std::vector<xk::EnsSysDesc> &d) {
   std::vector<long long> s;
@@ -245,11 +246,11 @@ static std::vector<long long> signature(const std::vector<xk::EnsSysDesc> &d) {
   return s;
 }
 
-static int chosen_blocks(const std::vector<long long> &sig) {
+static std::pair<int, int> chosen_shape(const std::vector<long long> &sig) {
   std::lock_guard<std::mutex> lk(g_mu);
   for (const auto &c : g_choice)
     if (c.first == sig) return c.second;
-  return 0;
+  return {0, 0};
 }
 
 static void release_launch(void *p) {
@@ -275,11 +276,11 @@ int md_gb300_capture_ensemble_persistent_x(int n, md_gb300_system_step_fn_x step
   std::vector<xk::EnsSysDesc> descs;
   std::vector<md_pimd_t_x *> pimds;
   XMD_TRY(plan(n, step, ctx, descs, pimds));
-  int bps = chosen_blocks(signature(descs));
-  if (!bps) bps = xk::ensemble_max_blocks_per_sm(D, MD_NHC_LENGTH_X);
-  if (bps < 1) return fail(MD_GB_ERR_UNSUPPORTED, "the persistent ensemble kernel does not fit on an SM");
+  std::pair<int, int> shape = chosen_shape(signature(descs));
+  if (!shape.first) shape = {std::min(2, xk::ensemble_max_blocks_per_sm(D, MD_NHC_LENGTH_X)), 4};
+  if (shape.first < 1) return fail(MD_GB_ERR_UNSUPPORTED, "the persistent ensemble kernel does not fit on an SM");
   xk::EnsLaunch *e = new xk::EnsLaunch();
-  cudaError_t ce = xk::ensemble_prepare(descs.data(), n, D, MD_NHC_LENGTH_X, bps, *e);
+  cudaError_t ce = xk::ensemble_prepare(descs.data(), n, D, MD_NHC_LENGTH_X, shape.first, shape.second, *e);
   if (ce != cudaSuccess) {
     delete e;
     return cuda_fail(ce, "persistent ensemble plan");
@@ -313,7 +314,7 @@ int md_gb300_ensemble_phase_times_x(md_gb300_graph_t_x *graph, double *us, int n
 }
 
 int md_gb300_autotune_ensemble_x(int n, md_gb300_system_step_fn_x step, void *ctx, int repeats, int *blocks_per_sm,
-                                 double *ms) {
+                                 int *groups, double *ms) {
   if (repeats < 1) repeats = 1;
   std::vector<xk::EnsSysDesc> descs;
   std::vector<md_pimd_t_x *> pimds;
@@ -322,34 +323,36 @@ int md_gb300_autotune_ensemble_x(int n, md_gb300_system_step_fn_x step, void *ct
   cudaEvent_t a, b;
   XMD_CUDA(cudaEventCreate(&a));
   XMD_CUDA(cudaEventCreate(&b));
-  int best = 0;
+  std::pair<int, int> best{0, 0};
   double best_ms = 0;
   int rc = 0;
   const int fit = xk::ensemble_max_blocks_per_sm(D, MD_NHC_LENGTH_X);
-  for (int bps = 1; bps <= fit && !rc; ++bps) {
-    xk::EnsLaunch e;
-    cudaError_t ce = xk::ensemble_prepare(descs.data(), n, D, MD_NHC_LENGTH_X, bps, e);
-    if (ce == cudaSuccess) ce = xk::ensemble_launch(e, st);  // warm-up
-    if (ce == cudaSuccess) ce = cudaEventRecord(a, st);
-    for (int r = 0; r < repeats && ce == cudaSuccess; ++r) ce = xk::ensemble_launch(e, st);
-    if (ce == cudaSuccess) ce = cudaEventRecord(b, st);
-    if (ce == cudaSuccess) ce = cudaEventSynchronize(b);
-    float t = 0;
-    if (ce == cudaSuccess) ce = cudaEventElapsedTime(&t, a, b);
-    if (ce != cudaSuccess) rc = cuda_fail(ce, "ensemble autotuning");
-    if (!rc) rc = check_status(e);
-    xk::ensemble_free(e);
-    if (rc) break;
-    const double per = t / repeats;
-    if (!best || per < best_ms) {
-      best = bps;
-      best_ms = per;
+  for (int bps = fit >= 2 ? 2 : 1; bps <= fit && !rc; ++bps)
+    for (int K : {1, 2, 4, 8, 16, 32}) {
+      if (K > n) break;
+      xk::EnsLaunch e;
+      cudaError_t ce = xk::ensemble_prepare(descs.data(), n, D, MD_NHC_LENGTH_X, bps, K, e);
+      if (ce == cudaSuccess) ce = xk::ensemble_launch(e, st);  // warm-up
+      if (ce == cudaSuccess) ce = cudaEventRecord(a, st);
+      for (int r = 0; r < repeats && ce == cudaSuccess; ++r) ce = xk::ensemble_launch(e, st);
+      if (ce == cudaSuccess) ce = cudaEventRecord(b, st);
+      if (ce == cudaSuccess) ce = cudaEventSynchronize(b);
+      float t = 0;
+      if (ce == cudaSuccess) ce = cudaEventElapsedTime(&t, a, b);
+      if (ce != cudaSuccess) rc = cuda_fail(ce, "ensemble autotuning");
+      if (!rc) rc = check_status(e);
+      xk::ensemble_free(e);
+      if (rc) break;
+      const double per = t / repeats;
+      if (!best.first || per < best_ms) {
+        best = {bps, K};
+        best_ms = per;
+      }
     }
-  }
   cudaEventDestroy(a);
   cudaEventDestroy(b);
   if (rc) return rc;
-  if (!best) return fail(MD_GB_ERR_UNSUPPORTED, "the persistent ensemble kernel does not fit on an SM");
+  if (!best.first) return fail(MD_GB_ERR_UNSUPPORTED, "the persistent ensemble kernel does not fit on an SM");
   {
     std::lock_guard<std::mutex> lk(g_mu);
     const auto sig = signature(descs);
@@ -362,7 +365,8 @@ int md_gb300_autotune_ensemble_x(int n, md_gb300_system_step_fn_x step, void *ct
     if (!found) g_choice.push_back({sig, best});
   }
   mark_fresh(pimds);
-  if (blocks_per_sm) *blocks_per_sm = best;
+  if (blocks_per_sm) *blocks_per_sm = best.first;
+  if (groups) *groups = best.second;
   if (ms) *ms = best_ms;
   return 0;
 }

@@ -325,16 +325,19 @@ struct EnsSysDesc {
   double inv_mP;        // 1 / (m P) of the reciprocal forces
 };
 struct EnsLaunch {
-  void *plan = nullptr;  // device descriptors, grid barrier, FP32 pair scratch
-  void *bar = nullptr;
-  int D = 0, L = 0, blocks = 0, nsys = 0;
+  void *plan = nullptr;  // device descriptors, group offsets, barriers, FP32 pair scratch
+  void *goff = nullptr, *bar = nullptr;
+  int D = 0, L = 0, blocks = 0, bps = 0, groups = 0, nsys = 0;
   size_t smem = 0;
 };
+constexpr int ENS_MAX_GROUPS = 32;
 // thread blocks of the persistent kernel that fit on one SM (0: none)
 int ensemble_max_blocks_per_sm(int D, int L);
-// descriptors uploaded (largest systems first) for a grid of
-// blocks_per_sm x SMs blocks (capped at what fits)
-cudaError_t ensemble_prepare(const EnsSysDesc *sys, int n, int D, int L, int blocks_per_sm, EnsLaunch &e);
+// descriptors uploaded for a grid of blocks_per_sm x SMs blocks (capped at
+// what fits) in `groups` groups with their own barriers, the systems spread
+// over the groups by estimated cost
+cudaError_t ensemble_prepare(const EnsSysDesc *sys, int n, int D, int L, int blocks_per_sm, int groups,
+                             EnsLaunch &e);
 cudaError_t ensemble_launch(const EnsLaunch &e, cudaStream_t st);
 // *failed = 1 when a grid-barrier wait of an earlier launch gave up (its
 // step and every later one did not run to completion); phase_us (optional,

@@ -181,7 +181,7 @@ class XLib:
                 "md_gb300_exchange_tables_x": (_i, [pp, _dp, _dp]),
                 "md_gb300_capture_ensemble_x": (_i, [_i, _vp, _vp, C.POINTER(_vp)]),
                 "md_gb300_capture_ensemble_persistent_x": (_i, [_i, _vp, _vp, C.POINTER(_vp)]),
-                "md_gb300_autotune_ensemble_x": (_i, [_i, _vp, _vp, _i, C.POINTER(_i), _dp]),
+                "md_gb300_autotune_ensemble_x": (_i, [_i, _vp, _vp, _i, C.POINTER(_i), C.POINTER(_i), _dp]),
                 "md_gb300_ensemble_status_x": (_i, [_vp]),
                 "md_gb300_ensemble_phase_times_x": (_i, [_vp, _dp, _i]),
                 "md_gb300_ewald_model_nparam_x": (_i, []),

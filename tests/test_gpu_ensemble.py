@@ -143,7 +143,7 @@ def test_fp64_autotuner_keeps_parity(lib):
         before = forces()
         bps, lay, ms = C.c_int(), C.c_int(), C.c_double()
         lib.check(lib.md_gb300_autotune_fp64_x(s.pimd, pf, 3, C.byref(bps), C.byref(lay), C.byref(ms)), "autotune")
-        assert bps.value in (1, 2) and ms.value > 0
+        assert bps.value in (1, 2, 3) and ms.value > 0
         assert lay.value in ((1, 2, 3) if kind == "ueg" else (0,))
         assert_close(forces(), before, 1e-13, "forces after FP64 autotuning")
         if kind == "ueg":  # the untuned Ewald path is pinned by the parity tests
@@ -235,16 +235,16 @@ def test_persistent_ensemble_matches_individual_steps(lib):
 
 
 def test_persistent_ensemble_autotuner_and_refusals(lib):
-    """The grid-size autotuner picks a size that runs; the capture then uses
-    it and still matches the per-system calls.  A step with a call that is
+    """The grid-shape autotuner (blocks per SM, groups) picks a shape that
+    runs; the capture then uses it and still matches the per-system calls.  A step with a call that is
     not part of the reference driver's step, or in FP64 mode, is refused."""
     lib.check(lib.md_gb300_set_precision_x(1))
     try:
         ens, ref, fn = _persistent_pair(lib)
-        bps, ms = C.c_int(), C.c_double()
+        bps, grp, ms = C.c_int(), C.c_int(), C.c_double()
         lib.check(lib.md_gb300_autotune_ensemble_x(len(PERSISTENT), C.cast(fn, C.c_void_p), None, 2, C.byref(bps),
-                                                   C.byref(ms)), "ensemble autotune")
-        assert bps.value in (1, 2) and ms.value > 0
+                                                   C.byref(grp), C.byref(ms)), "ensemble autotune")
+        assert bps.value in (1, 2, 3) and grp.value in (1, 2, 4, 8, 16, 32) and ms.value > 0
         # the autotuner advanced the systems: the per-system copies restart
         # from their state
         for (a, _), (b, _) in zip(ens, ref):
