@@ -614,11 +614,12 @@ def ensemble_form(lib, R, args):
     kernels = lib.md_gb300_graph_kernel_count_x(gp)
     ms, wall, clocks = R.time([R.launcher(gp)] * nst, [R.launcher(gp)] * 3)
     lib.check(lib.md_gb300_ensemble_status_x(gp), "persistent ensemble status")
-    ph = (C.c_double * 9)()
-    lib.md_gb300_ensemble_phase_times_x(gp, ph, 9)
+    ph = (C.c_double * 45)()
+    nph = lib.md_gb300_ensemble_phase_times_x(gp, ph, 45)
+    group_us = [round(v, 1) for v in ph[13:nph]]
     phase_us = {nm: round(v, 1) for nm, v in zip(
         ("VV3_1", "springs_Eint_tiles_Sk", "prefix_tables", "ENk_recip", "weights_inverses_pairsum", "solves", "G",
-         "exch_ends", "VV3_2"), ph)}
+         "exch_ends", "VV3_2", "block0_springs", "block0_Eint", "block0_tiles", "block0_Sk"), ph)}
     lib.md_gb300_graph_free_x(gp)
     for _, s, _ in systems:
         s.free()
@@ -628,7 +629,7 @@ def ensemble_form(lib, R, args):
     return {"value": beads / (ms * 1e-3), "unit": "bead-steps/s", "ms_per_step": ms, "systems": len(specs),
             "bead_slots": beads, "kernels_per_launch": kernels, "steps_timed": nst,
             "persistent_blocks_per_sm": cl.value, "persistent_groups": grp.value,
-            "persistent_phase_us_group0": phase_us, "autotuned_ms": tms.value, "wall_s_timed": wall,
+            "persistent_phase_us_group0": phase_us, "persistent_group_us": group_us, "autotuned_ms": tms.value, "wall_s_timed": wall,
             "graph_branches_wall_s_timed": wall_br,
             "graph_branches_ms_per_step": ms_br, "graph_branches_kernels": kernels_br,
             "gain_vs_graph_branches": ms_br / ms,

@@ -93,8 +93,10 @@ int md_gb300_ensemble_status_x(md_gb300_graph_t_x *graph);
    pair tiles and structure factors; prefix sums and force tables; cycle
    energies and reciprocal forces; recursion weights, block inverses and the
    pair sums; the two solves; G; the end-bead exchange forces; the second
-   half step), as one block saw them; returns the number of phases.
-   Synchronises. */
+   half step), as one block saw them, then that block's own time in the
+   second phase for its springs, cycle-energy increments, pair tiles and
+   structure factors, then each group's step time; returns the number of
+   values (13 + groups).  Synchronises. */
 int md_gb300_ensemble_phase_times_x(md_gb300_graph_t_x *graph, double *us, int n);
 /* Times the persistent step at each grid shape: 2 or 3 blocks per SM (the
    latter with the kernel compiled for three) and the blocks split into 1,

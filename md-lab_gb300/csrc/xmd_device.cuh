@@ -1009,29 +1009,30 @@ __device__ inline void phase32_slot(const Geo &g, int ns, const double *__restri
   }
 }
 
-// entry n (0..ns) of column ci's FP32 force table of slice j
-__device__ inline void recip_table32_entry(const int4 *__restrict__ cols, int ncol, const double2 *__restrict__ S,
-                                           const double *__restrict__ coef, int nk, float2 *__restrict__ T, int ns,
+// entry n (0..ns) of column ci's FP32 force table of slice j, in FP32
+// from the FP32 structure factors S and coefficients coef32
+__device__ inline void recip_table32_entry(const int4 *__restrict__ cols, int ncol, const float2 *__restrict__ S,
+                                           const float *__restrict__ coef32, int nk, float2 *__restrict__ T, int ns,
                                            int j, int ci, int n) {
   const int NT = 4 * ns + 1;
   const int4 c = cols[ci];
   auto W = [&](int nz) {
-    if (nz < c.z) return make_double2(0.0, 0.0);
+    if (nz < c.z) return make_float2(0.f, 0.f);
     const int k = c.w + (nz - c.z);
-    const double2 s = S[(size_t)j * nk + k];
-    return make_double2(coef[k] * s.x, -coef[k] * s.y);
+    const float2 s = S[(size_t)j * nk + k];
+    return make_float2(coef32[k] * s.x, -coef32[k] * s.y);
   };
   float2 *o = T + ((size_t)j * ncol + ci) * NT;
   if (n == 0) {
-    const double2 w = W(0);
-    o[0] = make_float2((float)w.x, (float)w.y);
+    o[0] = W(0);
   } else {
-    const double2 wp = W(n), wm = W(-n);
-    const double Ar = wp.x + wm.x, Ai = wp.y + wm.y, Br = wp.x - wm.x, Bi = wp.y - wm.y;
-    o[4 * n - 3] = make_float2((float)Ar, (float)Ai);
-    o[4 * n - 2] = make_float2((float)Br, (float)Bi);
-    o[4 * n - 1] = make_float2((float)(n * Ar), (float)(n * Ai));
-    o[4 * n] = make_float2((float)(n * Br), (float)(n * Bi));
+    const float2 wp = W(n), wm = W(-n);
+    const float Ar = wp.x + wm.x, Ai = wp.y + wm.y, Br = wp.x - wm.x, Bi = wp.y - wm.y;
+    const float fn = (float)n;
+    o[4 * n - 3] = make_float2(Ar, Ai);
+    o[4 * n - 2] = make_float2(Br, Bi);
+    o[4 * n - 1] = make_float2(fn * Ar, fn * Ai);
+    o[4 * n] = make_float2(fn * Br, fn * Bi);
   }
 }
 
@@ -1267,18 +1268,31 @@ __device__ inline void sk_item_blocks(SkAcc &A, const float2 *__restrict__ sp, i
   }
 }
 
-// S(k) of the item's wave vectors: Sj is the slice's row S + j nk
-__device__ inline void sk_item_store(const SkAcc &A, double2 *Sj, int4 c, int ns, int n0) {
-  double2 *o = Sj + c.w - c.z;
-  if (n0 == 0 && c.z <= 0) o[0] = make_double2(A.s0r.value(), A.s0i.value());
+// a + b and a - b of two double-float values, rounded to FP32 (TwoSum of
+// the high parts, the low parts added to its error)
+__device__ inline float df_sum(const DF &a, const DF &b) {
+  const float s = a.hi + b.hi, bp = s - a.hi;
+  const float e = (a.hi - (s - bp)) + (b.hi - bp);
+  return s + ((e + a.lo) + b.lo);
+}
+__device__ inline float df_diff(const DF &a, const DF &b) {
+  const float s = a.hi - b.hi, bp = s - a.hi;
+  const float e = (a.hi - (s - bp)) + (-b.hi - bp);
+  return s + ((e + a.lo) - b.lo);
+}
+
+// S(k) of the item's wave vectors in FP32 (the FP32 force tables are all
+// that reads it): Sj is the slice's row S + j nk
+__device__ inline void sk_item_store(const SkAcc &A, float2 *Sj, int4 c, int ns, int n0) {
+  float2 *o = Sj + c.w - c.z;
+  if (n0 == 0 && c.z <= 0) o[0] = make_float2(A.s0r.hi + A.s0r.lo, A.s0i.hi + A.s0i.lo);
 #pragma unroll
   for (int u = 0; u < SK_NG; ++u) {
     const int n = n0 + u + 1;
     if (n > ns) break;
-    const double Pr = A.P[u][0].value(), Pi = A.P[u][1].value();
-    const double Qr = A.Q[u][0].value(), Qi = A.Q[u][1].value();
-    o[n] = make_double2(Pr - Qi, Pi + Qr);
-    if (c.z < 0) o[-n] = make_double2(Pr + Qi, Pi - Qr);
+    const DF &Pr = A.P[u][0], &Pi = A.P[u][1], &Qr = A.Q[u][0], &Qi = A.Q[u][1];
+    o[n] = make_float2(df_diff(Pr, Qi), df_sum(Pi, Qr));
+    if (c.z < 0) o[-n] = make_float2(df_sum(Pr, Qi), df_diff(Pi, Qr));
   }
 }
 

@@ -53,9 +53,9 @@ struct EnsSys {
   int ewald;  // reciprocal sums present (D = 3)
   int ns, ncol, nk;
   const int4 *cols;
-  const double *coef;
+  const float *coef32;
   float2 *ph32, *T32;
-  double2 *S;
+  float2 *S;
   float *part, *x32;
   double lnvi, rscale, pscale;
   int rot[16];  // per task kind: (the kind's tasks before this system) mod (workers of that kind)
@@ -197,7 +197,21 @@ struct EnsBar {
   int err;
   int pad;
   unsigned long long stamp[ENS_PHASES + 1];  // block 0's %globaltimer at the start and after each phase
+  unsigned long long sub[4];  // block 0 inside phase B: after its springs, E_l^(1), pair tiles, structure factors
+  unsigned long long t0, t1;  // the group's first block: start and end of the step
 };
+
+// block 0's own time inside a phase (its threads synchronised first)
+__device__ inline void ens_sub(EnsBar *b, int k) {
+  if (blockIdx.x == 0) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      unsigned long long t;
+      asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+      b->sub[k] = t;
+    }
+  }
+}
 
 __device__ inline void ens_stamp(EnsBar *b, int k) {
   if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -263,6 +277,11 @@ __global__ void __launch_bounds__(ENS_T, MINB) k_ensemble_step(const EnsSys *__r
   const long long gt = rank * ENS_T + tid, gw = rank * ENS_W + w;
   const long long gb = rank;
   ens_stamp(bar, 0);
+  if (rank == 0 && tid == 0) {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    bar->t0 = t;
+  }
 
   // A: first half step (md_update_nhc_VV3_1_x); the forces restart from the
   // trap's (md_reset_force_x, md_pimd_calc_trap_force_x); FP32 positions and
@@ -305,6 +324,7 @@ __global__ void __launch_bounds__(ENS_T, MINB) k_ensemble_step(const EnsSys *__r
       }
     }
   }
+  ens_sub(bar, 0);
   {
     for (int i = i0; i < i1; ++i) {
       const EnsSysDesc &d = sys[i].d;
@@ -312,6 +332,7 @@ __global__ void __launch_bounds__(ENS_T, MINB) k_ensemble_step(const EnsSys *__r
       for (long long l = ens_first(gw, sys[i].rot[R_B_EINT], GW); l < g.N; l += GW)
         eint_particle<D>(g, d.x, d.m, d.w2, d.image, d.Eint, d.ENk, d.gl, (int)l, lane);
     }
+    ens_sub(bar, 1);
     for (int i = i0; i < i1; ++i) {
       const EnsSys &E = sys[i];
       if (!E.d.pair_kind) continue;
@@ -319,6 +340,7 @@ __global__ void __launch_bounds__(ENS_T, MINB) k_ensemble_step(const EnsSys *__r
       for (long long wi = ens_first(gw, sys[i].rot[R_B_PAIR], GW); wi < n; wi += GW) ens_pair_job<D>(E, (int)wi, lane);
     }
   }
+  ens_sub(bar, 2);
   if constexpr (D == 3) {
     for (int i = i0; i < i1; ++i) {
       const EnsSys &E = sys[i];
@@ -326,6 +348,7 @@ __global__ void __launch_bounds__(ENS_T, MINB) k_ensemble_step(const EnsSys *__r
       for (long long j = ens_first(gb, sys[i].rot[R_B_SK], G); j < E.d.g.P; j += G) ens_sk_slice(E, (int)j, (float2 *)ens_sh);
     }
   }
+  ens_sub(bar, 3);
   ens_grid_sync(bar, G, limit);
   ens_stamp(bar, 2);
 
@@ -349,7 +372,7 @@ __global__ void __launch_bounds__(ENS_T, MINB) k_ensemble_step(const EnsSys *__r
       const long long n = (long long)E.d.g.P * E.ncol * per;
       for (long long q = ens_first(gt, sys[i].rot[R_C_TAB], GT); q < n; q += GT) {
         const long long r = q / per;
-        recip_table32_entry(E.cols, E.ncol, E.S, E.coef, E.nk, E.T32, E.ns, (int)(r / E.ncol), (int)(r % E.ncol),
+        recip_table32_entry(E.cols, E.ncol, E.S, E.coef32, E.nk, E.T32, E.ns, (int)(r / E.ncol), (int)(r % E.ncol),
                             (int)(q % per));
       }
     }
@@ -515,6 +538,11 @@ __global__ void __launch_bounds__(ENS_T, MINB) k_ensemble_step(const EnsSys *__r
   }
   __syncthreads();
   ens_stamp(bar, ENS_PHASES);
+  if (rank == 0 && tid == 0) {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    bar->t1 = t;
+  }
 }
 
 // ---- host side ----------------------------------------------------------
@@ -572,17 +600,17 @@ static int sm_count() {
   return n > 0 ? n : 1;
 }
 
-// estimated cost of a system's step, for spreading the systems over the
-// groups (FP64 operations, with the FP32 work counted at a sixteenth)
+// estimated cost of a system's step in microseconds of one group of the
+// benchmark's grid, for spreading the systems over the groups: a fixed part
+// per system (its latency-bound tasks: prefix scan, solves, barriers' share)
+// and the work that grows with the system (fitted to measured group times of
+// the 64-system ensemble: the Ewald sums dominate, then the pair tiles)
 static double ens_cost(const EnsSys &E) {
   const Geo &g = E.d.g;
-  const double slots = (double)g.slots(), N = g.N, P = g.P;
-  double c = 2.0e4 + 220.0 * slots + 60.0 * N * N;
-  if (E.d.pair_kind) c += (double)E.jobs * P * 1024.0 * 60.0 / 16.0;
-  if (E.ewald) {
-    const double ngr = (E.ns + SK_NG - 1) / SK_NG;
-    c += P * E.ncol * (E.ns + 1) * 24.0 + P * N * E.ncol * (ngr * 34.0 + 45.0) / 16.0;
-  }
+  const double N = g.N, P = g.P, slots = (double)g.slots();
+  double c = 30.0 + 1.0e-3 * slots + 1.0e-3 * N * N;
+  if (E.d.pair_kind && !E.ewald) c += 1.2e-4 * (double)E.jobs * P * 1024.0;
+  if (E.ewald) c += 4.0e-5 * P * N * E.ncol * (E.ns + 1);
   return c;
 }
 
@@ -615,10 +643,10 @@ cudaError_t ensemble_prepare(const EnsSysDesc *sd, int n, int D, int L, int bloc
       E.ncol = r.ncol;
       E.nk = r.nk;
       E.cols = (const int4 *)r.kvec;
-      E.coef = r.coef;
+      E.coef32 = (const float *)(r.coef + r.nk);
       E.ph32 = (float2 *)(r.phase + recip_phase_doubles(g, r.nsum));
       E.T32 = (float2 *)r.T;
-      E.S = (double2 *)r.S;
+      E.S = (float2 *)r.S;
       E.rscale = 4 * M_PI * E.d.inv_mP;
     }
     E.lnvi = E.d.vi != 0.0 ? log(E.d.vi) : 0.0;
@@ -759,8 +787,16 @@ cudaError_t ensemble_status(const EnsLaunch &e, int *failed, double *phase_us) {
   if (r != cudaSuccess) return r;
   *failed = 0;
   for (const EnsBar &x : b) *failed |= x.err;
-  if (phase_us)
+  if (phase_us) {
     for (int k = 0; k < ENS_PHASES; ++k) phase_us[k] = (double)(b[0].stamp[k + 1] - b[0].stamp[k]) * 1e-3;
+    unsigned long long prev = b[0].stamp[1];
+    for (int k = 0; k < 4; ++k) {
+      phase_us[ENS_PHASES + k] = (double)(b[0].sub[k] - prev) * 1e-3;
+      prev = b[0].sub[k];
+    }
+    for (int k = 0; k < ENS_MAX_GROUPS; ++k)
+      phase_us[ENS_PHASES + 4 + k] = k < e.groups ? (double)(b[k].t1 - b[k].t0) * 1e-3 : 0.0;
+  }
   return r;
 }
 

@@ -307,10 +307,11 @@ int md_gb300_ensemble_phase_times_x(md_gb300_graph_t_x *graph, double *us, int n
   XMD_TRY(join_side());
   XMD_CUDA(cudaStreamSynchronize(stream()));
   int failed = 0;
-  double t[xk::ENS_PHASES];
+  double t[xk::ENS_PHASES + 4 + xk::ENS_MAX_GROUPS];
   XMD_CUDA(xk::ensemble_status(*e, &failed, t));
-  for (int k = 0; k < n && k < xk::ENS_PHASES; ++k) us[k] = t[k];
-  return xk::ENS_PHASES;
+  const int m = xk::ENS_PHASES + 4 + e->groups;
+  for (int k = 0; k < n && k < m; ++k) us[k] = t[k];
+  return m;
 }
 
 int md_gb300_autotune_ensemble_x(int n, md_gb300_system_step_fn_x step, void *ctx, int repeats, int *blocks_per_sm,

@@ -2453,6 +2453,10 @@ cudaError_t recip_setup(const Geo &g, int ns, double alpha, double qs, Recip &r,
   for (double c : coef) r.csum += c;
   cudaError_t e = cudaMemcpyAsync(r.coef, coef.data(), sizeof(double) * nk, cudaMemcpyHostToDevice, st);
   if (e != cudaSuccess) return e;
+  // an FP32 copy behind them for the mixed form's force tables
+  std::vector<float> coef32(coef.begin(), coef.end());
+  e = cudaMemcpyAsync(r.coef + nk, coef32.data(), sizeof(float) * nk, cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return e;
   if (!cd.empty()) {
     e = cudaMemcpyAsync(r.kvec, cd.data(), sizeof(int4) * cd.size(), cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) return e;
@@ -3492,7 +3496,7 @@ __global__ void k_phase32(Geo g, int ns, const double *__restrict__ x, float2 *_
 // different banks.
 template <int NS, int GR>
 __global__ void __launch_bounds__(256) k_sk32(Geo g, const float2 *__restrict__ ph, const int4 *__restrict__ cols,
-                                              int ncol, double2 *__restrict__ S, int nk) {
+                                              int ncol, float2 *__restrict__ S, int nk) {
   constexpr int NGR = (NS + SK_NG - 1) / SK_NG;
   constexpr int CH = GR == 16 ? 256 : 64, LD = CH + 1;  // particles per staged chunk (whole blocks of SK_PB GR)
   static_assert(CH % (SK_PB * GR) == 0, "staged chunks hold whole particle blocks");
@@ -3542,13 +3546,13 @@ __global__ void __launch_bounds__(256) k_sk32(Geo g, const float2 *__restrict__ 
 
 // force tables as k_recip_tables, stored in FP32
 template <int NS>
-__global__ void k_recip_tables32(const int4 *__restrict__ cols, int ncol, const double2 *__restrict__ S,
-                                 const double *__restrict__ coef, int nk, float2 *__restrict__ T) {
+__global__ void k_recip_tables32(const int4 *__restrict__ cols, int ncol, const float2 *__restrict__ S,
+                                 const float *__restrict__ coef32, int nk, float2 *__restrict__ T) {
   const int j = blockIdx.y;
   const int ci = blockIdx.x * blockDim.y + threadIdx.y;
   const int n = threadIdx.x;
   if (ci >= ncol || n > NS) return;
-  recip_table32_entry(cols, ncol, S, coef, nk, T, NS, j, ci, n);
+  recip_table32_entry(cols, ncol, S, coef32, nk, T, NS, j, ci, n);
 }
 
 template <int NS>
@@ -3601,6 +3605,7 @@ cudaError_t recip_force32(const Geo &g, const Recip &r, const double *x, double 
   const size_t smem =
       sizeof(float2) * nc * (4 * r.nsum + 1) + sizeof(int4) * nc + sizeof(float2) * 2 * (r.nsum + 1) * 128;
   float2 *T32 = (float2 *)r.T;
+  float2 *S32 = (float2 *)r.S;  // the FP32 structure factors (the FP64 form's buffer, first half)
   DISPATCH_NS(r.nsum, {
     {
       // one thread per item for slices below SK_BIG_N particles; above,
@@ -3609,17 +3614,17 @@ cudaError_t recip_force32(const Geo &g, const Recip &r, const double *x, double 
       const int items = nc * ((NS + SK_NG - 1) / SK_NG);
       if (g.N < SK_BIG_N)
         k_sk32<NS, 1><<<dim3((items + 255) / 256, g.P), 256, 0, st>>>(g, ph32, (const int4 *)r.kvec, nc,
-                                                                     (double2 *)r.S, r.nk);
+                                                                     S32, r.nk);
       else if (items > 64 || NS > 6)
-        k_sk32<NS, 4><<<dim3((items + 63) / 64, g.P), 256, 0, st>>>(g, ph32, (const int4 *)r.kvec, nc,
-                                                                   (double2 *)r.S, r.nk);
+        k_sk32<NS, 4><<<dim3((items + 63) / 64, g.P), 256, 0, st>>>(g, ph32, (const int4 *)r.kvec, nc, S32, r.nk);
       else
         k_sk32<(NS <= 6 ? NS : 6), 16><<<dim3((items + 15) / 16, g.P), 256, 0, st>>>(
-            g, ph32, (const int4 *)r.kvec, nc, (double2 *)r.S, r.nk);
+            g, ph32, (const int4 *)r.kvec, nc, S32, r.nk);
     }
     {
       XK_PROF("recip_tables32");
-      k_recip_tables32<NS><<<tgrid, tblk, 0, st>>>((const int4 *)r.kvec, nc, (const double2 *)r.S, r.coef, r.nk, T32);
+      k_recip_tables32<NS><<<tgrid, tblk, 0, st>>>((const int4 *)r.kvec, nc, S32, (const float *)(r.coef + r.nk),
+                                                  r.nk, T32);
     }
     auto kf = k_recip_force32<NS>;
     static bool opted = false;

@@ -222,7 +222,8 @@ struct Recip {
   int nk;              // half-space wave vectors of the cube
   int ncol;            // kept columns (set by recip_setup)
   int tsz;             // entries of the kept columns' force tables (compact, set by recip_setup)
-  double *coef;        // [nk] s * exp(-pi^2 G^2/alpha^2) / (pi V G^2), 0 for a dropped vector
+  double *coef;        // [nk] s * exp(-pi^2 G^2/alpha^2) / (pi V G^2), 0 for a dropped vector;
+                       // then the same nk values in FP32 (recip_coef_bytes(nk) bytes in all)
   int *kvec;           // kept columns, longest first: int4 (nx | nzmax << 8, ny, first nz,
                        // offset of its first k), then compact table offsets;
                        // recip_cols_ints(nsum) ints
@@ -232,6 +233,7 @@ struct Recip {
   double csum;         // sum of coef (host value, set by recip_setup)
 };
 size_t recip_phase_doubles(const Geo &g, int nsum);
+inline size_t recip_coef_bytes(int nk) { return (sizeof(double) + sizeof(float)) * (size_t)nk; }
 int recip_count(int nsum);
 size_t recip_cols_ints(int nsum);
 size_t recip_table_doubles(const Geo &g, int nsum);
@@ -341,9 +343,11 @@ cudaError_t ensemble_prepare(const EnsSysDesc *sys, int n, int D, int L, int blo
 cudaError_t ensemble_launch(const EnsLaunch &e, cudaStream_t st);
 // *failed = 1 when a grid-barrier wait of an earlier launch gave up (its
 // step and every later one did not run to completion); phase_us (optional,
-// ENS_PHASES values): the last launch's phase durations as block 0 saw them
-// (the phases end at the grid barriers; the last one at block 0's own end).
-// Synchronous.
+// ENS_PHASES + 4 + ENS_MAX_GROUPS values): the last launch's phase
+// durations as block 0 saw them (the phases end at the group's barriers;
+// the last one at block 0's own end), block 0's own time in phase B for its
+// springs, E_l^(1), pair tiles and structure factors, then each group's
+// step time (its first block's start to end).  Synchronous.
 constexpr int ENS_PHASES = 9;
 cudaError_t ensemble_status(const EnsLaunch &e, int *failed, double *phase_us = nullptr);
 void ensemble_free(EnsLaunch &e);

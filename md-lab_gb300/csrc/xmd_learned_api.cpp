@@ -476,7 +476,7 @@ int md_gb300_ewald_model_create_x(md_gb300_ewald_model_t_x **out, md_pimd_t_x *p
   res(M->ep, ne * 8);
   res(M->jacc, (3 + 2 * (size_t)g.P) * 8);
   const int nk = xk::recip_count(nsum_cheap);
-  res(M->rc_coef, 8 * (size_t)nk);
+  res(M->rc_coef, xk::recip_coef_bytes(nk));
   res(M->rc_cols, sizeof(int) * xk::recip_cols_ints(nsum_cheap));
   res(M->rc_phase, 8 * xk::recip_phase_doubles(g, nsum_cheap) * 3 / 2);
   res(M->rc_S, 16 * (size_t)nk * g.P);

@@ -391,7 +391,7 @@ int xmd::ewald_tables(md_pimd_t_x *pimd, SimDev *sd, PimdDev *pd) {
     return 0;
   if (capturing()) return fail(MD_GB_ERR_CAPTURE, "Ewald tables change while capturing a graph");
   const int nk = xk::recip_count(ns);
-  XMD_TRY(reserve(pd->rc_coef, sizeof(double) * nk));
+  XMD_TRY(reserve(pd->rc_coef, xk::recip_coef_bytes(nk)));
   XMD_TRY(reserve(pd->rc_cols, sizeof(int) * xk::recip_cols_ints(ns)));
   // FP64 phases, then their FP32 copy for the mixed form
   XMD_TRY(reserve(pd->rc_phase, sizeof(double) * xk::recip_phase_doubles(g, ns) * 3 / 2));
