@@ -293,7 +293,7 @@ def kernel_flops(name, nsum=NSUM):
 # DRAM traffic per launch (dram__bytes_read.sum + dram__bytes_write.sum) of
 # each kernel with a FLOP model, from one ncu capture on this workload
 # (summaries in profiles/, named for the kernel)
-TRAFFIC = {"desc": 833024, "pair_tiles32_ewald_real": 424192, "pair_tiles_ewald_real": 1125632,
+TRAFFIC = {"desc": 822272, "pair_tiles32_ewald_real": 424192, "pair_tiles_ewald_real": 1125632,
            "sk": 17358592, "recip_force": 23965184, "mlp_forward": 4273408}
 
 

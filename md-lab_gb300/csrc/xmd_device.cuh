@@ -965,14 +965,19 @@ __device__ inline void spring_interior_bead(const Geo &g, const double *__restri
   for (int d = 0; d < D; ++d) f[sidx(j, d, l, D, g.Ns)] += -gr[d] / mm;
 }
 
-// G[l][j] (1-based) from the extended-range weights and unknowns
+// X'_{N-l} / X_N of row l (1-based) of G, as a mantissa q and an exponent qe
+__device__ inline void g_ext_row(int N, const double *__restrict__ Xfm, const int *__restrict__ Xfe,
+                                 const double *__restrict__ Xbm, const int *__restrict__ Xbe, int l, double &q,
+                                 int &qe) {
+  q = Xbm[N - l] / Xfm[N];
+  qe = Xbe[N - l] - Xfe[N];
+}
+
+// G[l][j] (1-based) from the extended-range weights and unknowns, the row's
+// factor (q, qe) from g_ext_row
 __device__ inline void g_ext_elem(int N, const double *__restrict__ Mm, const int *__restrict__ Me,
-                                  const double *__restrict__ Xfm, const int *__restrict__ Xfe,
-                                  const double *__restrict__ Xbm, const int *__restrict__ Xbe, double *__restrict__ G,
-                                  int l, int j) {
-  // X'_{N-l} / X_N, as a mantissa and an exponent
-  const double q = Xbm[N - l] / Xfm[N];
-  const int qe = Xbe[N - l] - Xfe[N];
+                                  const double *__restrict__ Xfm, const int *__restrict__ Xfe, double q, int qe,
+                                  double *__restrict__ G, int l, int j) {
   double gv;
   if (j > l + 1) {
     gv = 0;

@@ -478,9 +478,13 @@ __global__ void __launch_bounds__(ENS_T, MINB) k_ensemble_step(const EnsSys *__r
       const EnsSys &E = sys[i];
       const int N = E.d.g.N;
       const long long n = (long long)N * N;
-      for (long long q = ens_first(gt, sys[i].rot[R_G], GT); q < n; q += GT)
-        g_ext_elem(N, E.job.Mm[0], E.job.Me[0], E.job.Xm[0], E.job.Xe[0], E.job.Xm[1], E.job.Xe[1], E.d.G,
-                   (int)(q / N) + 1, (int)(q % N) + 1);
+      for (long long q = ens_first(gt, sys[i].rot[R_G], GT); q < n; q += GT) {
+        const int l = (int)(q / N) + 1;
+        double qf;
+        int qe;
+        g_ext_row(N, E.job.Xm[0], E.job.Xe[0], E.job.Xm[1], E.job.Xe[1], l, qf, qe);
+        g_ext_elem(N, E.job.Mm[0], E.job.Me[0], E.job.Xm[0], E.job.Xe[0], qf, qe, E.d.G, l, (int)(q % N) + 1);
+      }
     }
   }
   ens_grid_sync(bar, G, limit);

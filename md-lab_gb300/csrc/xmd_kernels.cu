@@ -1353,8 +1353,11 @@ __global__ void k_fill_g_ext(int N, const double *__restrict__ Mm, const int *__
                              const double *__restrict__ Xfm, const int *__restrict__ Xfe,
                              const double *__restrict__ Xbm, const int *__restrict__ Xbe, double *__restrict__ G) {
   const int l = blockIdx.y + 1;  // 1-based row
+  double q;
+  int qe;
+  g_ext_row(N, Xfm, Xfe, Xbm, Xbe, l, q, qe);
   for (int j = blockIdx.x * blockDim.x + threadIdx.x + 1; j <= N; j += gridDim.x * blockDim.x)
-    g_ext_elem(N, Mm, Me, Xfm, Xfe, Xbm, Xbe, G, l, j);
+    g_ext_elem(N, Mm, Me, Xfm, Xfe, q, qe, G, l, j);
 }
 
 cudaError_t fill_g_ext(int N, const double *rs_f, const double *rs_b, double *G, cudaStream_t st) {
