@@ -164,12 +164,14 @@ int md_gb300_pair_force_noalloc_x(md_pair_force_t_x pf, const double *x, const d
    both Ewald parts.  MD_GB_PRECISION_FP64 (default) reproduces MD-Lab to
    1e-10.  MD_GB_PRECISION_MIXED evaluates pair and real-space Ewald forces in
    FP32: each lane adds at most 32 FP32 pair terms (one 32 x 32 tile), and
-   the tile partials are added in FP64; the reciprocal sum uses FP32 phase
-   products accumulated in double-float (two-sum) structure factors.
+   the tile partials are added in FP64; the reciprocal sum builds its
+   structure factors from FP32 phase products, summed in FP32 over 16
+   particles at a time and those partial sums in double-float (two-sum),
+   then FP32 force tables and compensated (Kahan) column sums per particle.
    Positions, the exchange recursion, springs, the thermostat and every
    estimator stay FP64.  The force error against the FP64 form, measured as
    max |f32 - f64| / max |f64| over all beads of the 512-electron, 64-bead
-   electron gas (Ewald |n| <= 10), is 2.1e-5 and set mainly by the FP32
+   electron gas (Ewald |n| <= 10), is 1.1e-5 and set mainly by the FP32
    rounding of the pair separations; the library's tests bound it by 5e-5
    there and on the smaller systems they run. */
 /* Tile shape of the FP32 pair kernel (the mixed form) for pimd's system

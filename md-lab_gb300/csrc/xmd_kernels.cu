@@ -3303,13 +3303,14 @@ namespace xk {
 // Mixed-precision form: pair and real-space Ewald forces in FP32, each
 // lane's sum over one 32 x 32 tile (at most 32 terms) in plain FP32 and the
 // tile partials added in FP64 (k_pair_finish32); reciprocal space with FP32
-// phase products accumulated in double-float structure factors (an
-// unevaluated sum of two FP32 numbers, ~48 significant bits) and each
-// particle's sum over the wave-vector columns compensated (Kahan).
-// Positions and every estimator stay FP64; partial sums leave the FP32
-// kernels as doubles.  Against the FP64 form the largest force error is
-// ~2e-5 of the largest force at 512 electrons, 64 beads, set by the FP32
-// rounding of the pair separations rather than by the sums.
+// phase products summed in FP32 over 16 particles and those partial sums
+// in double-float (an unevaluated sum of two FP32 numbers, ~48 significant
+// bits), S(k) and the force tables in FP32, and each particle's sum over
+// the wave-vector columns compensated (Kahan).  Positions and every
+// estimator stay FP64; partial sums leave the FP32 kernels as doubles.
+// Against the FP64 form the largest force error is ~1e-5 of the largest
+// force at 512 electrons, 64 beads, set by the FP32 rounding of the pair
+// separations rather than by the sums.
 // ===================================================================
 
 
