@@ -283,3 +283,70 @@ def test_persistent_ensemble_autotuner_and_refusals(lib):
             s.free()
     finally:
         lib.check(lib.md_gb300_set_precision_x(0))
+
+
+@pytest.mark.parametrize("variant", [(2, 4), (3, 8)], ids=["d2l4", "d3l8"])
+def test_persistent_ensemble_other_variants(variant):
+    """The persistent kernel's other instantiations: D = 2 (traps with the
+    periodic Gaussian pair force, minimum image) and chains of length 8
+    (traps and an electron gas), against the per-system calls."""
+    D, L = variant
+    vl = xmd_x.load(D, L)
+    vl.check(vl.md_gb300_set_precision_x(1))
+    try:
+        specs = [("trap", 10, 8, 1.0, 2.0), ("trap", 40, 4, 0.5, 3.0), ("trap", 70, 16, 0.0, 1.0)]
+        if D == 3:
+            specs.append(("ueg", 24, 8, 0.75, 2.0))
+
+        def make_v(spec, seed):
+            kind, N, P, vi, beta = spec
+            T = 1.0 / beta
+            box = (4 * math.pi * N / 3) ** (1 / 3) * 2.0 if kind == "ueg" else 6.0
+            st = random_state(D, L, N, P, T, box, kind == "ueg", seed)
+            s = xmd_x.PimdSystem(vl, N, P, vi, T, box=box)
+            s.set_state(**st)
+            return s, box
+
+        def stepv(spec, s, box):
+            if spec[0] == "ueg":
+                xmd_x.set_potentials(vl, coul_s=1.0, alpha=5.6 / box, nsum=4)
+                xmd_x.md_step(vl, s, 0.05, image=1, pair=vl.fn("md_coulomb_3d_ewald_force_x"), pbc=True)
+            elif D == 2:
+                xmd_x.set_potentials(vl, trap_w=1.0, gauss_g=0.75 * math.pi, gauss_s=0.5)
+                xmd_x.md_step(vl, s, 0.005, image=1, trap=vl.fn("md_harmonic_trap_force_x"),
+                              pair=vl.fn("md_periodic_gaussian_force_x"))
+            else:
+                xmd_x.set_potentials(vl, trap_w=1.0, gauss_g=0.75 * math.pi, gauss_s=0.5)
+                xmd_x.md_step(vl, s, 0.005, trap=vl.fn("md_harmonic_trap_force_x"), pair=vl.fn("md_gaussian_force_x"))
+
+        ens = [make_v(sp, 500 + i) for i, sp in enumerate(specs)]
+        ref = [make_v(sp, 500 + i) for i, sp in enumerate(specs)]
+        for (s, box), sp in zip(ens + ref, specs + specs):
+            stepv(sp, s, box)
+
+        def cb(i, ctx):
+            try:
+                s, box = ens[i]
+                stepv(specs[i], s, box)
+                return 0
+            except Exception:
+                return -1
+
+        fn = STEP_FN(cb)
+        g = C.c_void_p()
+        vl.check(vl.md_gb300_capture_ensemble_persistent_x(len(specs), C.cast(fn, C.c_void_p), None, C.byref(g)),
+                 "persistent capture")
+        vl.check(vl.md_gb300_graph_launch_x(g, 3))
+        vl.check(vl.md_gb300_ensemble_status_x(g), "persistent step status")
+        for _ in range(3):
+            for (s, box), sp in zip(ref, specs):
+                stepv(sp, s, box)
+        for (a, _), (b, _) in zip(ens, ref):
+            sa, sb = a.state(), b.state()
+            for k in ("x", "v", "theta", "vtheta", "f"):
+                assert relerr(sa[k], sb[k]) <= (1e-9 if k == "f" else 1e-12), k
+        vl.md_gb300_graph_free_x(g)
+        for s, _ in ens + ref:
+            s.free()
+    finally:
+        vl.check(vl.md_gb300_set_precision_x(0))
