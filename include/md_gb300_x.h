@@ -103,9 +103,12 @@ int md_gb300_ensemble_phase_times_x(md_gb300_graph_t_x *graph, double *us, int n
    2, 4, 8, 16 or 32 groups, each stepping its share of the systems (spread by
    estimated cost) with its own barriers, so that the groups' phases drift
    apart and one group's FP64 thermostat overlaps another's FP32 sums.
-   Each shape runs `repeats` + 1 launches, so the systems advance by those
-   steps.  The fastest is recorded for this ensemble's shapes; *blocks_per_sm,
-   *groups and *ms (may be NULL) receive it and its time per step. */
+   The fastest shape is then rebalanced up to three times: each system's
+   estimated cost is scaled by its group's measured time over the group's
+   estimate, and the systems are spread again.  Each trial runs `repeats` + 1
+   launches, so the systems advance by those steps.  The fastest shape and
+   balance are recorded for this ensemble's shapes; *blocks_per_sm, *groups
+   and *ms (may be NULL) receive the shape and its time per step. */
 int md_gb300_autotune_ensemble_x(int n, md_gb300_system_step_fn_x step, void *ctx, int repeats, int *blocks_per_sm,
                                  int *groups, double *ms);
 /* kernel nodes in a captured graph (kernels launched per replay) */

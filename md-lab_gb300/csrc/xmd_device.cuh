@@ -953,16 +953,20 @@ __device__ inline void enk_entry(const Geo &g, const double *__restrict__ x, con
   ENk[dtri(l) + k - 1] = Eint[l - 1] + ((G[l - 1] - G[l - k]) + link<D>(g, x, m, w2, l - 1, l - k, image));
 }
 
-// the ring springs' force on interior bead j (1..P-2) of particle l
+// the ring springs' force on interior bead j (1..P-2) of particle l, as the
+// acceleration the step stores in f: the reference divides the gradient
+// m w2 (2x - x_n - x_p) (md_pimd_x.c:2344-2367) by the bead's mass m, which
+// cancels, so w2 (x - x_n) + w2 (x - x_p) is taken directly (equal to
+// rounding; no FP64 division, the GPU's slowest FP64 operation)
 template <int D>
 __device__ inline void spring_interior_bead(const Geo &g, const double *__restrict__ x,
                                             const double *__restrict__ m, double w2, int image,
                                             double *__restrict__ f, int j, int l) {
-  const double mm = m[(size_t)j * g.Ns + l];
+  (void)m;
   double gr[D];
-  grad2<D>(g, x, mm * w2, j, l, j + 1, l, j - 1, l, image, gr);
+  grad2<D>(g, x, w2, j, l, j + 1, l, j - 1, l, image, gr);
 #pragma unroll
-  for (int d = 0; d < D; ++d) f[sidx(j, d, l, D, g.Ns)] += -gr[d] / mm;
+  for (int d = 0; d < D; ++d) f[sidx(j, d, l, D, g.Ns)] += -gr[d];
 }
 
 // X'_{N-l} / X_N of row l (1-based) of G, as a mantissa q and an exponent qe

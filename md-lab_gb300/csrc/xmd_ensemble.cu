@@ -299,7 +299,7 @@ __global__ void __launch_bounds__(ENS_T, MINB) k_ensemble_step(const EnsSys *__r
         nhc_slot<D, L>(g, 1, s, l, d.x, d.v, d.f, nullptr, d.m, d.th, d.vt, d.Q, d.iQ, d.kT, d.h);
         const double xn = d.x[s];
         double f0 = 0.0;
-        if (d.trap_kind) f0 += trap_f(d.tp, (int)((s / g.Ns) % D), xn) / g.P;
+        if (d.trap_kind) f0 += trap_f(d.tp, (int)((s / g.Ns) % D), xn) * E.pscale;
         d.f[s] = f0;
         d.fex[s] = 0.0;
         if (d.pair_kind) E.x32[s] = (float)xn;
@@ -619,7 +619,7 @@ static double ens_cost(const EnsSys &E) {
 }
 
 cudaError_t ensemble_prepare(const EnsSysDesc *sd, int n, int D, int L, int blocks_per_sm, int groups,
-                             EnsLaunch &out) {
+                             EnsLaunch &out, const double *costs) {
   if (n < 1 || !ens_kernel(D, L, 2) || groups < 1 || groups > ENS_MAX_GROUPS) return cudaErrorInvalidValue;
   const int fit = ensemble_max_blocks_per_sm(D, L);
   if (fit < 1 || blocks_per_sm < 1) return cudaErrorInvalidConfiguration;
@@ -663,7 +663,7 @@ cudaError_t ensemble_prepare(const EnsSysDesc *sd, int n, int D, int L, int bloc
   std::vector<double> cost(n);
   for (int i = 0; i < n; ++i) {
     order[i] = i;
-    cost[i] = ens_cost(all[i]);
+    cost[i] = costs ? costs[i] : ens_cost(all[i]);
   }
   std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return cost[x] > cost[y]; });
   std::vector<std::vector<int>> lists(K);
@@ -746,6 +746,11 @@ cudaError_t ensemble_prepare(const EnsSysDesc *sd, int n, int D, int L, int bloc
     return e;
   }
   ensemble_free(out);
+  out.cost = cost;
+  out.group_of.assign(n, 0);
+  for (int k = 0; k < K; ++k)
+    for (int i : lists[k]) out.group_of[i] = k;
+  out.load = load;
   out.plan = plan;
   out.goff = (unsigned char *)plan + goff_at;
   out.bar = (unsigned char *)plan + bar_at;
@@ -806,7 +811,9 @@ cudaError_t ensemble_status(const EnsLaunch &e, int *failed, double *phase_us) {
 
 void ensemble_free(EnsLaunch &e) {
   if (e.plan) cudaFree(e.plan);
-  e = EnsLaunch{};
+  e.plan = e.goff = e.bar = nullptr;
+  e.D = e.L = e.blocks = e.bps = e.groups = e.nsys = 0;
+  e.smem = 0;
 }
 
 }  // namespace xk

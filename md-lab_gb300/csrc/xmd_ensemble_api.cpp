@@ -235,9 +235,14 @@ static void mark_fresh(const std::vector<md_pimd_t_x *> &pimds) {
   }
 }
 
-// grid shapes (blocks per SM, groups) chosen by the autotuner, per ensemble shape
+// grid shapes (blocks per SM, groups) and the systems' costs chosen by the
+// autotuner, per ensemble shape
+struct EnsChoice {
+  int bps = 0, groups = 0;
+  std::vector<double> cost;
+};
 static std::mutex g_mu;
-static std::vector<std::pair<std::vector<long long>, std::pair<int, int>>> g_choice;
+static std::vector<std::pair<std::vector<long long>, EnsChoice>> g_choice;
 
 static std::vector<long long> signature(const std::vector<xk::EnsSysDesc> &d) {
   std::vector<long long> s;
@@ -246,11 +251,11 @@ static std::vector<long long> signature(const std::vector<xk::EnsSysDesc> &d) {
   return s;
 }
 
-static std::pair<int, int> chosen_shape(const std::vector<long long> &sig) {
+static EnsChoice chosen_shape(const std::vector<long long> &sig) {
   std::lock_guard<std::mutex> lk(g_mu);
   for (const auto &c : g_choice)
     if (c.first == sig) return c.second;
-  return {0, 0};
+  return EnsChoice{};
 }
 
 static void release_launch(void *p) {
@@ -276,11 +281,15 @@ int md_gb300_capture_ensemble_persistent_x(int n, md_gb300_system_step_fn_x step
   std::vector<xk::EnsSysDesc> descs;
   std::vector<md_pimd_t_x *> pimds;
   XMD_TRY(plan(n, step, ctx, descs, pimds));
-  std::pair<int, int> shape = chosen_shape(signature(descs));
-  if (!shape.first) shape = {std::min(2, xk::ensemble_max_blocks_per_sm(D, MD_NHC_LENGTH_X)), 4};
-  if (shape.first < 1) return fail(MD_GB_ERR_UNSUPPORTED, "the persistent ensemble kernel does not fit on an SM");
+  EnsChoice shape = chosen_shape(signature(descs));
+  if (!shape.bps) {
+    shape.bps = std::min(2, xk::ensemble_max_blocks_per_sm(D, MD_NHC_LENGTH_X));
+    shape.groups = 4;
+  }
+  if (shape.bps < 1) return fail(MD_GB_ERR_UNSUPPORTED, "the persistent ensemble kernel does not fit on an SM");
   xk::EnsLaunch *e = new xk::EnsLaunch();
-  cudaError_t ce = xk::ensemble_prepare(descs.data(), n, D, MD_NHC_LENGTH_X, shape.first, shape.second, *e);
+  cudaError_t ce = xk::ensemble_prepare(descs.data(), n, D, MD_NHC_LENGTH_X, shape.bps, shape.groups, *e,
+                                        (int)shape.cost.size() == n ? shape.cost.data() : nullptr);
   if (ce != cudaSuccess) {
     delete e;
     return cuda_fail(ce, "persistent ensemble plan");
@@ -324,7 +333,30 @@ int md_gb300_autotune_ensemble_x(int n, md_gb300_system_step_fn_x step, void *ct
   cudaEvent_t a, b;
   XMD_CUDA(cudaEventCreate(&a));
   XMD_CUDA(cudaEventCreate(&b));
-  std::pair<int, int> best{0, 0};
+  // one shape's time per step (repeats launches after one warm-up) and, in
+  // *group_us, each group's time in the last launch
+  auto time_shape = [&](int bps, int K, const double *costs, double *per, std::vector<double> *group_us,
+                        xk::EnsLaunch &e) -> int {
+    cudaError_t ce = xk::ensemble_prepare(descs.data(), n, D, MD_NHC_LENGTH_X, bps, K, e, costs);
+    if (ce == cudaSuccess) ce = xk::ensemble_launch(e, st);  // warm-up
+    if (ce == cudaSuccess) ce = cudaEventRecord(a, st);
+    for (int r = 0; r < repeats && ce == cudaSuccess; ++r) ce = xk::ensemble_launch(e, st);
+    if (ce == cudaSuccess) ce = cudaEventRecord(b, st);
+    if (ce == cudaSuccess) ce = cudaEventSynchronize(b);
+    float t = 0;
+    if (ce == cudaSuccess) ce = cudaEventElapsedTime(&t, a, b);
+    if (ce != cudaSuccess) return cuda_fail(ce, "ensemble autotuning");
+    XMD_TRY(check_status(e));
+    *per = t / repeats;
+    if (group_us) {
+      int failed = 0;
+      std::vector<double> tt(xk::ENS_PHASES + 4 + xk::ENS_MAX_GROUPS);
+      XMD_CUDA(xk::ensemble_status(e, &failed, tt.data()));
+      group_us->assign(tt.begin() + xk::ENS_PHASES + 4, tt.begin() + xk::ENS_PHASES + 4 + e.groups);
+    }
+    return 0;
+  };
+  EnsChoice best;
   double best_ms = 0;
   int rc = 0;
   const int fit = xk::ensemble_max_blocks_per_sm(D, MD_NHC_LENGTH_X);
@@ -332,28 +364,46 @@ int md_gb300_autotune_ensemble_x(int n, md_gb300_system_step_fn_x step, void *ct
     for (int K : {1, 2, 4, 8, 16, 32}) {
       if (K > n) break;
       xk::EnsLaunch e;
-      cudaError_t ce = xk::ensemble_prepare(descs.data(), n, D, MD_NHC_LENGTH_X, bps, K, e);
-      if (ce == cudaSuccess) ce = xk::ensemble_launch(e, st);  // warm-up
-      if (ce == cudaSuccess) ce = cudaEventRecord(a, st);
-      for (int r = 0; r < repeats && ce == cudaSuccess; ++r) ce = xk::ensemble_launch(e, st);
-      if (ce == cudaSuccess) ce = cudaEventRecord(b, st);
-      if (ce == cudaSuccess) ce = cudaEventSynchronize(b);
-      float t = 0;
-      if (ce == cudaSuccess) ce = cudaEventElapsedTime(&t, a, b);
-      if (ce != cudaSuccess) rc = cuda_fail(ce, "ensemble autotuning");
-      if (!rc) rc = check_status(e);
-      xk::ensemble_free(e);
-      if (rc) break;
-      const double per = t / repeats;
-      if (!best.first || per < best_ms) {
-        best = {bps, K};
+      double per = 0;
+      rc = time_shape(bps, K, nullptr, &per, nullptr, e);
+      if (!rc && (!best.bps || per < best_ms)) {
+        best.bps = bps;
+        best.groups = K;
+        best.cost = e.cost;
         best_ms = per;
       }
+      xk::ensemble_free(e);
+      if (rc) break;
     }
+  // the best shape rebalanced on measured group times: each system's cost
+  // scaled by its group's measured time over the group's estimated load
+  for (int round = 0; round < 3 && !rc && best.groups > 1; ++round) {
+    xk::EnsLaunch e;
+    double per = 0;
+    std::vector<double> gt;
+    rc = time_shape(best.bps, best.groups, best.cost.data(), &per, &gt, e);
+    if (!rc) {
+      if (per < best_ms) best_ms = per;
+      std::vector<double> cost = e.cost;
+      for (int i = 0; i < n; ++i) {
+        const int k = e.group_of[i];
+        if (e.load[k] > 0 && gt[k] > 0) cost[i] *= gt[k] / e.load[k];
+      }
+      xk::EnsLaunch e2;
+      double per2 = 0;
+      rc = time_shape(best.bps, best.groups, cost.data(), &per2, nullptr, e2);
+      if (!rc && per2 < best_ms) {
+        best_ms = per2;
+        best.cost = cost;
+      }
+      xk::ensemble_free(e2);
+    }
+    xk::ensemble_free(e);
+  }
   cudaEventDestroy(a);
   cudaEventDestroy(b);
   if (rc) return rc;
-  if (!best.first) return fail(MD_GB_ERR_UNSUPPORTED, "the persistent ensemble kernel does not fit on an SM");
+  if (!best.bps) return fail(MD_GB_ERR_UNSUPPORTED, "the persistent ensemble kernel does not fit on an SM");
   {
     std::lock_guard<std::mutex> lk(g_mu);
     const auto sig = signature(descs);
@@ -366,8 +416,8 @@ int md_gb300_autotune_ensemble_x(int n, md_gb300_system_step_fn_x step, void *ct
     if (!found) g_choice.push_back({sig, best});
   }
   mark_fresh(pimds);
-  if (blocks_per_sm) *blocks_per_sm = best.first;
-  if (groups) *groups = best.second;
+  if (blocks_per_sm) *blocks_per_sm = best.bps;
+  if (groups) *groups = best.groups;
   if (ms) *ms = best_ms;
   return 0;
 }

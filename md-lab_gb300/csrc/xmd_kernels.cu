@@ -1457,19 +1457,21 @@ cudaError_t exch_force(const Geo &g, const double *x, const double *m, double w2
 // ===================================================================
 
 
+// f += V'(x) / P, the 1/P from the host (a product instead of an FP64
+// division per DOF; equal to rounding)
 __global__ void k_trap_force(Geo g, TrapPrm p, const double *__restrict__ x,
-                             double *__restrict__ f) {
+                             double *__restrict__ f, double invP) {
   const size_t s = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= g.slots() || (int)(s % g.Ns) >= g.N) return;
   const int d = (int)((s / g.Ns) % g.D);
-  f[s] += trap_f(p, d, x[s]) / g.P;
+  f[s] += trap_f(p, d, x[s]) * invP;
 }
 
 cudaError_t trap_force(const Geo &g, const TrapPrm &p, const double *x, double *f,
                        cudaStream_t st) {
   {
     XK_PROF("trap_force");
-    k_trap_force<<<cdiv(g.slots(), 256), 256, 0, st>>>(g, p, x, f);
+    k_trap_force<<<cdiv(g.slots(), 256), 256, 0, st>>>(g, p, x, f, 1.0 / g.P);
   }
   return XK_LAUNCHED();
 }

@@ -14,6 +14,7 @@
 #include <cstddef>
 #include <cstdint>
 #include <string>
+#include <vector>
 
 #ifdef __CUDACC__
 #define XK_HD __host__ __device__
@@ -331,15 +332,18 @@ struct EnsLaunch {
   void *goff = nullptr, *bar = nullptr;
   int D = 0, L = 0, blocks = 0, bps = 0, groups = 0, nsys = 0;
   size_t smem = 0;
+  std::vector<double> cost;    // the estimated cost of each system (caller's order) the plan balanced
+  std::vector<int> group_of;   // each system's group
+  std::vector<double> load;    // each group's estimated total
 };
 constexpr int ENS_MAX_GROUPS = 32;
 // thread blocks of the persistent kernel that fit on one SM (0: none)
 int ensemble_max_blocks_per_sm(int D, int L);
 // descriptors uploaded for a grid of blocks_per_sm x SMs blocks (capped at
 // what fits) in `groups` groups with their own barriers, the systems spread
-// over the groups by estimated cost
+// over the groups by estimated cost (the built-in model, or `costs`)
 cudaError_t ensemble_prepare(const EnsSysDesc *sys, int n, int D, int L, int blocks_per_sm, int groups,
-                             EnsLaunch &e);
+                             EnsLaunch &e, const double *costs = nullptr);
 cudaError_t ensemble_launch(const EnsLaunch &e, cudaStream_t st);
 // *failed = 1 when a grid-barrier wait of an earlier launch gave up (its
 // step and every later one did not run to completion); phase_us (optional,
