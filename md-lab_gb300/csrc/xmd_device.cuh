@@ -1305,6 +1305,8 @@ __device__ inline void sk_item_store(const SkAcc &A, float2 *Sj, int4 c, int ns,
   }
 }
 
+constexpr int RF_PB = 128;  // particles per block of the FP32 reciprocal forces (two threads each)
+
 // One particle's reciprocal force sums over cc kept columns (k_recip_force32's
 // arithmetic): cols and the columns' FP32 force tables sT (4 ns + 1 entries
 // each) in shared memory, the particle's x and y phase factors at

@@ -140,10 +140,11 @@ __device__ inline void ens_sk_slice(const EnsSys &E, int j, float2 *sp) {
 }
 
 // Reciprocal forces on the particles of bead slice j by the calling block,
-// as k_recip_force32 computes them (recip_cols32: the same column order and
-// compensated sums), 128 particles at a time; the columns, the particles' x
-// and y phase factors and as many columns' force tables as fit are staged
-// in shared memory.
+// as k_recip_force32 computes them (two threads per particle, each summing
+// its half of the columns in order with recip_cols32, the halves added in
+// double), 128 particles at a time; the columns, the particles' x and y
+// phase factors and as many columns' force tables as fit are staged in
+// shared memory.
 __device__ inline void ens_recip_slice(const EnsSys &E, int j, unsigned char *sh) {
   const Geo &g = E.d.g;
   const int ns = E.ns, NT = 4 * ns + 1, ncol = E.ncol, N = g.N, tid = threadIdx.x;
@@ -153,15 +154,17 @@ __device__ inline void ens_recip_slice(const EnsSys &E, int j, unsigned char *sh
   const int ccap = (int)((ENS_SMEM - sizeof(int4) * ncol - sizeof(float2) * 2 * (ns + 1) * 128) / (sizeof(float2) * NT));
   const float2 *Tj = E.T32 + (size_t)j * ncol * NT;
   const float2 *pj = E.ph32 + (size_t)j * 3 * (ns + 1) * g.Ns;
+  const int li = tid >> 1, h = tid & 1;
+  const int half = (ncol + 1) / 2, ca = h ? half : 0, cb = h ? ncol : half;
   __syncthreads();
   for (int q = tid; q < ncol; q += ENS_T) sc[q] = E.cols[q];
   for (int lb = 0; lb < N; lb += 128) {
-    const int l = lb + tid;
-    const bool live = tid < 128 && l < N;
+    const int l = lb + li;
+    const bool live = l < N;
     __syncthreads();
     for (int q = tid; q < 2 * (ns + 1) * 128; q += ENS_T) {
-      const int r = q / 128, li = q % 128;
-      pxy[q] = lb + li < N ? pj[(size_t)r * g.Ns + lb + li] : make_float2(0.f, 0.f);
+      const int r = q / 128, lq = q % 128;
+      pxy[q] = lb + lq < N ? pj[(size_t)r * g.Ns + lb + lq] : make_float2(0.f, 0.f);
     }
     float2 ez[ENS_NSMAX + 1];
 #pragma unroll
@@ -173,13 +176,18 @@ __device__ inline void ens_recip_slice(const EnsSys &E, int j, unsigned char *sh
       __syncthreads();
       for (int q = tid; q < cc * NT; q += ENS_T) sT[q] = Tj[(size_t)c0 * NT + q];
       __syncthreads();
-      if (live) recip_cols32<ENS_NSMAX>(Fx, Fy, Fz, sc + c0, cc, sT, ns, pxy, 128, tid, ez);
+      const int a = ca > c0 ? ca : c0, b = cb < c0 + cc ? cb : c0 + cc;
+      if (live && a < b) recip_cols32<ENS_NSMAX>(Fx, Fy, Fz, sc + a, b - a, sT + (size_t)(a - c0) * NT, ns, pxy, 128, li, ez);
     }
-    if (live) {
+    double fx = Fx.value(), fy = Fy.value(), fz = Fz.value();
+    fx += __shfl_xor_sync(FULL, fx, 1);
+    fy += __shfl_xor_sync(FULL, fy, 1);
+    fz += __shfl_xor_sync(FULL, fz, 1);
+    if (live && !h) {
       double *f = E.d.f;
-      f[sidx(j, 0, l, 3, g.Ns)] += E.rscale * Fx.value() * g.inv_box[0];
-      f[sidx(j, 1, l, 3, g.Ns)] += E.rscale * Fy.value() * g.inv_box[1];
-      f[sidx(j, 2, l, 3, g.Ns)] += E.rscale * Fz.value() * g.inv_box[2];
+      f[sidx(j, 0, l, 3, g.Ns)] += E.rscale * fx * g.inv_box[0];
+      f[sidx(j, 1, l, 3, g.Ns)] += E.rscale * fy * g.inv_box[1];
+      f[sidx(j, 2, l, 3, g.Ns)] += E.rscale * fz * g.inv_box[2];
     }
   }
 }

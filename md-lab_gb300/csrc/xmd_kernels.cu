@@ -3561,36 +3561,48 @@ __global__ void k_recip_tables32(const int4 *__restrict__ cols, int ncol, const 
   recip_table32_entry(cols, ncol, S, coef32, nk, T, NS, j, ci, n);
 }
 
+// Two threads per particle, RF_PB particles a block: thread h of a pair
+// sums the columns of its half (recip_cols32, the columns in order), and the
+// two compensated sums are added in double.
 template <int NS>
-__global__ void __launch_bounds__(128) k_recip_force32(Geo g, const float2 *__restrict__ ph,
+__global__ void __launch_bounds__(2 * RF_PB) k_recip_force32(Geo g, const float2 *__restrict__ ph,
                                                        const int4 *__restrict__ cols, int ncol,
                                                        const float2 *__restrict__ T, double scale,
                                                        double *__restrict__ f) {
   constexpr int NT = 4 * NS + 1;
   extern __shared__ __align__(16) float smf[];
   // the columns (16-byte records first, so that they stay aligned), the x
-  // and y phase factors of the block's 128 particles, and the slice's force
+  // and y phase factors of the block's 64 particles, and the slice's force
   // tables, all staged
   int4 *sc = (int4 *)smf;
   float2 *pxy = (float2 *)(sc + ncol);
-  float2 *sT = pxy + 2 * (NS + 1) * 128;
+  float2 *sT = pxy + 2 * (NS + 1) * RF_PB;
   const int j = blockIdx.y;
   const float2 *Tj = T + (size_t)j * ncol * NT;
   for (int q = threadIdx.x; q < ncol * NT; q += blockDim.x) sT[q] = Tj[q];
   for (int q = threadIdx.x; q < ncol; q += blockDim.x) sc[q] = cols[q];
-  const int l0 = blockIdx.x * 128, li = threadIdx.x, l = l0 + li;
+  const int l0 = blockIdx.x * RF_PB, li = threadIdx.x >> 1, h = threadIdx.x & 1, l = l0 + li;
   const float2 *pj = ph + (size_t)j * 3 * (NS + 1) * g.Ns;
-  for (int r = 0; r < 2 * (NS + 1); ++r) pxy[r * 128 + li] = l < g.N ? pj[(size_t)r * g.Ns + l] : make_float2(0.f, 0.f);
+  for (int q = threadIdx.x; q < 2 * (NS + 1) * RF_PB; q += blockDim.x) {
+    const int r = q / RF_PB, lq = l0 + q % RF_PB;
+    pxy[q] = lq < g.N ? pj[(size_t)r * g.Ns + lq] : make_float2(0.f, 0.f);
+  }
   __syncthreads();
-  if (l >= g.N) return;
+  const bool live = l < g.N;
   float2 ez[NS + 1];
 #pragma unroll
-  for (int n = 1; n <= NS; ++n) ez[n] = pj[((size_t)2 * (NS + 1) + n) * g.Ns + l];
+  for (int n = 1; n <= NS; ++n) ez[n] = live ? pj[((size_t)2 * (NS + 1) + n) * g.Ns + l] : make_float2(0.f, 0.f);
+  const int half = (ncol + 1) / 2, ca = h ? half : 0, cb = h ? ncol : half;
   Kahan Fx, Fy, Fz;
-  recip_cols32<NS>(Fx, Fy, Fz, sc, ncol, sT, NS, pxy, 128, li, ez);
-  f[sidx(j, 0, l, 3, g.Ns)] += scale * Fx.value() * g.inv_box[0];
-  f[sidx(j, 1, l, 3, g.Ns)] += scale * Fy.value() * g.inv_box[1];
-  f[sidx(j, 2, l, 3, g.Ns)] += scale * Fz.value() * g.inv_box[2];
+  if (live) recip_cols32<NS>(Fx, Fy, Fz, sc + ca, cb - ca, sT + (size_t)ca * NT, NS, pxy, RF_PB, li, ez);
+  double fx = Fx.value(), fy = Fy.value(), fz = Fz.value();
+  fx += __shfl_xor_sync(FULL, fx, 1);
+  fy += __shfl_xor_sync(FULL, fy, 1);
+  fz += __shfl_xor_sync(FULL, fz, 1);
+  if (!live || h) return;
+  f[sidx(j, 0, l, 3, g.Ns)] += scale * fx * g.inv_box[0];
+  f[sidx(j, 1, l, 3, g.Ns)] += scale * fy * g.inv_box[1];
+  f[sidx(j, 2, l, 3, g.Ns)] += scale * fz * g.inv_box[2];
 }
 
 cudaError_t recip_force32(const Geo &g, const Recip &r, const double *x, double inv_mP, double *f,
@@ -3607,9 +3619,9 @@ cudaError_t recip_force32(const Geo &g, const Recip &r, const double *x, double 
   if (e != cudaSuccess) return e;
   const int nc = r.ncol;
   dim3 tgrid((nc + 7) / 8, g.P), tblk(r.nsum + 1, 8);
-  dim3 grid((g.N + 127) / 128, g.P);
+  dim3 grid((g.N + RF_PB - 1) / RF_PB, g.P);
   const size_t smem =
-      sizeof(float2) * nc * (4 * r.nsum + 1) + sizeof(int4) * nc + sizeof(float2) * 2 * (r.nsum + 1) * 128;
+      sizeof(float2) * nc * (4 * r.nsum + 1) + sizeof(int4) * nc + sizeof(float2) * 2 * (r.nsum + 1) * RF_PB;
   float2 *T32 = (float2 *)r.T;
   float2 *S32 = (float2 *)r.S;  // the FP32 structure factors (the FP64 form's buffer, first half)
   DISPATCH_NS(r.nsum, {
@@ -3641,7 +3653,7 @@ cudaError_t recip_force32(const Geo &g, const Recip &r, const double *x, double 
     }
     {
       XK_PROF("recip_force32");
-      kf<<<grid, 128, smem, st>>>(g, ph32, (const int4 *)r.kvec, nc, T32, 4 * M_PI * inv_mP, f);
+      kf<<<grid, 2 * RF_PB, smem, st>>>(g, ph32, (const int4 *)r.kvec, nc, T32, 4 * M_PI * inv_mP, f);
     }
   });
   return XK_LAUNCHED();
