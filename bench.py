@@ -227,11 +227,14 @@ def n_images(xcut=5.2):
 # algorithmic work per launch of each kernel (FMA = 2 flops); the same count
 # for the FP64 and FP32 versions of a kernel, each derived from the kernel's
 # arithmetic per pair, image or wave vector
-def kept_nz_pairs(nsum):
+def kept_nz_pairs(nsum, part=None):
     """sum over the kept wave-vector columns (nx, ny) of their largest kept
     |nz|: the library leaves out vectors whose force weight |G| c(n) is
     below 1e-17 of the largest (RECIP_KEEP), so the column kernels run
-    this many +-nz pairs instead of ncol * nsum (cubic box, alpha L = ALPHA_L)"""
+    this many +-nz pairs instead of ncol * nsum (cubic box, alpha L = ALPHA_L).
+    part "fp64" / "fp32": only the columns the FP64 form's split keeps in
+    FP64 / sends to the FP32 kernels (largest weight in the column at or
+    above / below 1e-7 of the largest, RECIP_SPLIT)"""
     w = {}
     for nx in range(nsum + 1):
         for ny in range(-nsum, nsum + 1):
@@ -241,10 +244,15 @@ def kept_nz_pairs(nsum):
                 g2 = nx * nx + ny * ny + nz * nz
                 w[(nx, ny, nz)] = math.exp(-math.pi ** 2 * g2 / ALPHA_L ** 2) / math.sqrt(g2)
     wmax = max(w.values())
-    nzmax = {}
+    nzmax, wcol = {}, {}
     for (nx, ny, nz), v in w.items():
         if v >= 1e-17 * wmax:
             nzmax[(nx, ny)] = max(nzmax.get((nx, ny), 0), abs(nz))
+            wcol[(nx, ny)] = max(wcol.get((nx, ny), 0.0), v)
+    if part == "fp64":
+        return sum(z for c, z in nzmax.items() if wcol[c] >= 1e-7 * wmax)
+    if part == "fp32":
+        return sum(z for c, z in nzmax.items() if wcol[c] < 1e-7 * wmax)
     return sum(nzmax.values())
 
 
@@ -262,15 +270,19 @@ def shell_vectors(count=32):
                if (a > 0 or (a == 0 and b > 0) or (a == 0 and b == 0 and c > 0)) and a * a + b * b + c * c in shells)
 
 
-def kernel_flops(name, nsum=NSUM):
+def kernel_flops(name, nsum=NSUM, split=False):
+    """split: the FP64 form's kernels with their FP32 parts split off (real-
+    space images at alpha R >= 4 and the small-weight wave-vector columns
+    on the FP32 pipe): the FP64 work of the FP64 kernels"""
+    part = "fp64" if split else None
     if name in ("recip_force", "recip_force32"):
         # 17.7 flop per +-nz pair of a kept column per particle and slice
-        return 17.7 * kept_nz_pairs(nsum) * N * P
+        return 17.7 * kept_nz_pairs(nsum, part if name == "recip_force" else None) * N * P
     if name in ("sk", "sk32"):
-        return 8.8 * kept_nz_pairs(nsum) * N * P
+        return 8.8 * kept_nz_pairs(nsum, part if name == "sk" else None) * N * P
     if name == "pair_tiles_ewald_real":
         pairs = P * N * (N - 1) / 2
-        return pairs * (47.0 * n_images() + 39.0)
+        return pairs * (47.0 * n_images(4.0 if split else 5.2) + 39.0)
     if name == "pair_tiles32_ewald_real":
         pairs = P * N * (N - 1) / 2
         return pairs * (47.0 * n_images(3.6) + 39.0)
@@ -396,21 +408,21 @@ class Runner:
         return {k: (v[0] / n, v[1] // n) for k, v in prof.items()}
 
 
-def roofline(prof, peak, peak_name, unit_nsum=NSUM):
+def roofline(prof, peak, peak_name, unit_nsum=NSUM, split=False):
     """FLOP roofline of the step's dominant arithmetic kernel (the largest
     with a FLOP model) from its live per-launch time; the overall largest
     kernel is named beside it (the exchange recursion is latency-bound: N
     dependent steps, no FLOP or byte roofline applies)"""
     total = sum(v[0] for v in prof.values())
     top_name, (top_ms, _) = max(prof.items(), key=lambda kv: kv[1][0])
-    modelled = {k: v for k, v in prof.items() if kernel_flops(k, unit_nsum)}
+    modelled = {k: v for k, v in prof.items() if kernel_flops(k, unit_nsum, split)}
     name, (ms, launches) = max(modelled.items(), key=lambda kv: kv[1][0])
     per_launch_ms = ms / max(launches, 1)
     roof = {"kernel": name, "bound": "fp64" if peak_name == "fp64" else "fp32", "unit": "TFLOP/s",
             "share": ms / total if total else None, "launch_ms": per_launch_ms, "peak": peak,
             "peak_source": f"live {peak_name.upper()} FMA probe on this GPU (md_gb300_{peak_name}_peak_x)",
             "traffic": TRAFFIC.get(name)}
-    flops = kernel_flops(name, unit_nsum)
+    flops = kernel_flops(name, unit_nsum, split)
     if flops:
         roof["algorithmic_flop_per_launch"] = flops
         roof["achieved"] = flops / (per_launch_ms * 1e-3) / 1e12
@@ -750,11 +762,23 @@ def run_gb300(args, dist, rank, ws):
         plain_ms, plain_kps, plain_wall, plain_clocks = graph_form()
         plain_prof = R.profile(step)
         fp64_peak = lib.md_gb300_fp64_peak_x()
+        # every term in FP64 (MD_GB_PRECISION_FP64_STRICT), for comparison
+        lib.check(lib.md_gb300_set_precision_x(2))
+        step()
+        strict_ms, _, _, strict_clocks = graph_form()
+        strict_prof = R.profile(step)
+        lib.check(lib.md_gb300_set_precision_x(0))
+        step()
         forms["plain_fp64"] = {"value": ws * N * P / (plain_ms * 1e-3), "ms_per_step": plain_ms,
                                "kernels_per_step": plain_kps, "clocks": plain_clocks,
                                "autotuned": {"tile_blocks_per_sm": bps.value, "sk_layout": lay.value},
                                "kernel_ms_per_step": {k: v[0] for k, v in plain_prof.items()},
-                               "roofline": roofline(plain_prof, fp64_peak, "fp64")}
+                               "roofline": roofline(plain_prof, fp64_peak, "fp64", split=True),
+                               "arithmetic": "FP64, with the real-space images at alpha R >= 4 and the "
+                                             "wave-vector columns of force weight below 1e-7 on the FP32 pipe",
+                               "strict_fp64": {"ms_per_step": strict_ms, "clocks": strict_clocks,
+                                               "kernel_ms_per_step": {k: v[0] for k, v in strict_prof.items()},
+                                               "roofline": roofline(strict_prof, fp64_peak, "fp64")}}
     fp32_peak = lib.md_gb300_fp32_peak_x()
     if "recursion" in want:
         forms["recursion_vs_N"] = recursion_form(lib, R, args)

@@ -165,7 +165,16 @@ int md_gb300_pair_force_noalloc_x(md_pair_force_t_x pf, const double *x, const d
 
 /* Arithmetic of the pair forces (md_pimd_calc_pair_force_x), including
    both Ewald parts.  MD_GB_PRECISION_FP64 (default) reproduces MD-Lab to
-   1e-10.  MD_GB_PRECISION_MIXED evaluates pair and real-space Ewald forces in
+   1e-10: every term is FP64 except two groups of small ones, evaluated on
+   the FP32 pipe: the real-space Ewald images at alpha R >= 4 (each below
+   5.2e-7 of the pair strength over R^2; added to the FP64 sum per pair),
+   and the reciprocal wave-vector columns (nx, ny) whose every vector has a
+   force weight |G| c(n) below 1e-7 of the largest (FP32 structure factors,
+   tables and compensated column sums).  Against
+   MD_GB_PRECISION_FP64_STRICT, which evaluates those in FP64 too, the
+   forces of the 512-electron, 64-bead electron gas (Ewald |n| <= 10) differ
+   by 2.4e-16 of the largest and by at most 6.8e-12 of any bead's own.
+   MD_GB_PRECISION_MIXED evaluates pair and real-space Ewald forces in
    FP32: each lane adds at most 32 FP32 pair terms (one 32 x 32 tile), and
    the tile partials are added in FP64; the reciprocal sum builds its
    structure factors from FP32 phase products, summed in FP32 over 16
@@ -222,6 +231,7 @@ int md_gb300_exchange_tables_x(md_pimd_t_x *pimd, double *tmpV, double *G);
 
 #define MD_GB_PRECISION_FP64 0
 #define MD_GB_PRECISION_MIXED 1
+#define MD_GB_PRECISION_FP64_STRICT 2
 int md_gb300_set_precision_x(int mode);
 int md_gb300_get_precision_x(void);
 

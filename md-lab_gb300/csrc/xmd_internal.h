@@ -109,6 +109,8 @@ struct PimdDev {
   int rc_nk = 0;
   int rc_ncol = 0;  // kept wave-vector columns
   int rc_tsz = 0;   // entries of their compact force tables
+  int rc_ncol_in = 0, rc_ncol_out = 0, rc_tsz_in = 0;  // the FP64 forces' split (xk::Recip)
+  size_t rc_s32_off = 0;  // doubles of rc_S before the split's FP32 structure factors
   double rc_csum = 0;
 };
 

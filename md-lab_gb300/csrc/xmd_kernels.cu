@@ -15,6 +15,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cfloat>
 #include <array>
 #include <atomic>
 #include <cmath>
@@ -1613,13 +1614,20 @@ __device__ inline void pair_eval(const PairPrm &p, const Geo &g, const double *d
     // from rsqrt.  On this GPU FP64 comparisons and int <-> double
     // conversions share the slow FP64 pipe, so rounding to integers uses
     // the 1.5 * 2^52 addition and the cut-off test compares bit patterns.
+    // Forces only: images at alpha R >= p.xsplit (two thirds of those inside
+    // rcut at alpha rcut = 5.2, xsplit = 4) go to the FP32 pipe instead,
+    // through ew_h32, and their sum joins the FP64 one per pair.
     constexpr double MAGIC = 6755399441055744.0;  // 1.5 * 2^52
     const double *tab = ENERGY_TAB ? tabs + EW_NINT * (EW_DEG + 1) : tabs;
     const double rc2 = p.rcut * p.rcut;
     const long long rc2_bits = __double_as_longlong(rc2);
     double mm[3];
     int sh[3];
-    unsigned mask = 0u;
+    unsigned mask = 0u, far = 0u;
+    // FP32 copies of the box and of the minimum image (from the FP32
+    // positions): the culling, and the far images' evaluation
+    const float L0 = (float)g.box[0], L1 = (float)g.box[1], L2 = (float)g.box[2];
+    float m0 = 0.f, m1 = 0.f, m2 = 0.f;
     if (active) {
 #pragma unroll
       for (int d = 0; d < 3; ++d) {
@@ -1628,17 +1636,39 @@ __device__ inline void pair_eval(const PairPrm &p, const Geo &g, const double *d
         mm[d] = fma(-(tq - MAGIC), g.box[d], dx[d]);
       }
       const float rc2f = (float)(rc2 * 1.0001);
-      const float L0 = (float)g.box[0], L1 = (float)g.box[1], L2 = (float)g.box[2];
-      const float m0 = fmaf(-(float)sh[0], L0, dxf[0]);
-      const float m1 = fmaf(-(float)sh[1], L1, dxf[1]);
-      const float m2 = fmaf(-(float)sh[2], L2, dxf[2]);
+      m0 = fmaf(-(float)sh[0], L0, dxf[0]);
+      m1 = fmaf(-(float)sh[1], L1, dxf[1]);
+      m2 = fmaf(-(float)sh[2], L2, dxf[2]);
 #pragma unroll
       for (int c = 0; c < 27; ++c) {
         const int k0 = c / 9 - 1, k1 = (c / 3) % 3 - 1, k2 = c % 3 - 1;
         const float t0 = fmaf(-(float)k0, L0, m0), t1 = fmaf(-(float)k1, L1, m1), t2 = fmaf(-(float)k2, L2, m2);
         const float r2 = fmaf(t2, t2, fmaf(t1, t1, t0 * t0));
         const bool in_cube = abs(sh[0] + k0) <= p.nsum && abs(sh[1] + k1) <= p.nsum && abs(sh[2] + k2) <= p.nsum;
-        if (r2 < rc2f && in_cube) mask |= 1u << c;
+        if (!ENERGY_TAB && r2 >= p.xs2f) {
+          // a far image (alpha R >= xsplit): FP32, cut at rcut in FP32
+          if (r2 < p.rcf2 && in_cube) far |= 1u << c;
+        } else if (r2 < rc2f && in_cube) {
+          mask |= 1u << c;
+        }
+      }
+    }
+    // far images on the FP32 pipe, each lane its own (their h(alpha R) is
+    // below 5.2e-7, so FP32's relative error of a few 1e-6 leaves a few
+    // 1e-13 of the force in all)
+    float G0 = 0.f, G1 = 0.f, G2 = 0.f;
+    if (!ENERGY_TAB) {
+      unsigned fr = far;
+      while (fr) {
+        const int c = __ffs(fr) - 1;
+        fr &= fr - 1;
+        const float t0 = fmaf(-(float)(c / 9 - 1), L0, m0);
+        const float t1 = fmaf(-(float)((c / 3) % 3 - 1), L1, m1);
+        const float t2 = fmaf(-(float)(c % 3 - 1), L2, m2);
+        const float v = ew_h32(fmaf(t2, t2, fmaf(t1, t1, t0 * t0)), p.alphaf);
+        G0 = fmaf(t0, v, G0);
+        G1 = fmaf(t1, v, G1);
+        G2 = fmaf(t2, v, G2);
       }
     }
     double F0 = 0, F1 = 0, F2 = 0, e = 0;
@@ -1724,6 +1754,11 @@ __device__ inline void pair_eval(const PairPrm &p, const Geo &g, const double *d
         }
       }
       __syncwarp();
+    }
+    if (!ENERGY_TAB && __any_sync(FULL, far != 0u)) {
+      F0 += (double)G0;
+      F1 += (double)G1;
+      F2 += (double)G2;
     }
     F[0] = p.qs * F0;
     if (D > 1) F[1] = p.qs * F1;
@@ -2001,9 +2036,20 @@ static int pair_grid(size_t warps_needed, const Geo &g) {
   return full;
 }
 
+// the FP32 constants of the Ewald far images (PairPrm::alphaf, xs2f, rcf2)
+PairPrm with_far_images(const PairPrm &p) {
+  PairPrm q = p;
+  q.alphaf = (float)p.alpha;
+  q.rcf2 = (float)(p.rcut * p.rcut);
+  q.xs2f = FLT_MAX;
+  if (p.xsplit > 0 && p.alpha > 0) q.xs2f = (float)((p.xsplit / p.alpha) * (p.xsplit / p.alpha));
+  return q;
+}
+
 template <int D, bool ENERGY>
-static cudaError_t pair_launch(const Geo &g, const PairPrm &p, const double *x, const double *m,
+static cudaError_t pair_launch(const Geo &g, const PairPrm &p_in, const double *x, const double *m,
                                double *out, int T, int jobs, cudaStream_t st) {
+  const PairPrm p = with_far_images(p_in);
   const size_t warps = (size_t)jobs * g.P;
   switch (p.kind) {
     case PAIR_GAUSSIAN:
@@ -2088,7 +2134,8 @@ static cudaError_t cross_launch(const Geo &ga, const Geo &gb, const PairPrm &p, 
   const size_t dyn = KIND == PAIR_EWALD_REAL ? EW_TAB_BYTES : 0;
   const int grid = resident_grid(k_pair_cross<D, KIND, ENERGY>, (size_t)TA * TB * ga.P, occ, sms, dyn);
   XK_PROF("pair_cross");
-  k_pair_cross<D, KIND, ENERGY><<<grid, 256, dyn, st>>>(ga, gb, p, xa, ma, xb, mb, outa, outb, TA, TB);
+  k_pair_cross<D, KIND, ENERGY><<<grid, 256, dyn, st>>>(ga, gb, with_far_images(p), xa, ma, xb, mb, outa, outb, TA,
+                                                        TB);
   return XK_LAUNCHED();
 }
 
@@ -2409,6 +2456,9 @@ __global__ void k_recip_energy(Geo g, const double2 *__restrict__ S, const doubl
   if (threadIdx.x == 0) part[j] = e;
 }
 
+static int ncols(int ns) { return ns * (2 * ns + 1) + ns + 1; }
+static size_t recip_split_at(int ns) { return (5 * (size_t)ncols(ns) + 1 + 3) & ~(size_t)3; }
+
 cudaError_t recip_setup(const Geo &g, int ns, double alpha, double qs, Recip &r,
                         cudaStream_t st) {
   // host-side tables: c(n) in the full column order, then the kept columns
@@ -2450,6 +2500,29 @@ cudaError_t recip_setup(const Geo &g, int ns, double alpha, double qs, Recip &r,
   // compact table offsets of the kept columns (4 nzmax + 1 entries each)
   std::vector<int> toff(kept.size() + 1, 0);
   for (size_t i = 0; i < kept.size(); ++i) toff[i + 1] = toff[i] + 4 * kept[i].first + 1;
+  // the split for the FP64 forces: the columns whose largest force weight
+  // is below RECIP_SPLIT of the largest go to the FP32 kernels (after the
+  // FP64 ones in the split list, both parts longest first)
+  std::vector<int4> split_in, split_out;
+  std::vector<int> toff_in(1, 0);
+  for (size_t i = 0; i < kept.size(); ++i) {
+    const int4 c = kept[i].second;
+    const int nzmax = kept[i].first;
+    double wc = 0;
+    for (int nz = c.z; nz <= nzmax; ++nz) {
+      const int k = c.w + nz - c.z;
+      wc = wgt[k] > wc ? wgt[k] : wc;
+    }
+    if (wc < RECIP_SPLIT * wmax) {
+      split_out.push_back(c);
+    } else {
+      split_in.push_back(c);
+      toff_in.push_back(toff_in.back() + 4 * nzmax + 1);
+    }
+  }
+  r.ncol_in = (int)split_in.size();
+  r.ncol_out = (int)split_out.size();
+  r.tsz_in = toff_in.back();
   r.nsum = ns;
   r.nk = nk;
   r.ncol = (int)cd.size();
@@ -2469,22 +2542,40 @@ cudaError_t recip_setup(const Geo &g, int ns, double alpha, double qs, Recip &r,
   e = cudaMemcpyAsync(r.kvec + 4 * (size_t)(ns * (2 * ns + 1) + ns + 1), toff.data(), sizeof(int) * toff.size(),
                       cudaMemcpyHostToDevice, st);
   if (e != cudaSuccess) return e;
+  split_in.insert(split_in.end(), split_out.begin(), split_out.end());
+  if (!split_in.empty()) {
+    e = cudaMemcpyAsync(r.kvec + recip_split_at(ns), split_in.data(), sizeof(int4) * split_in.size(),
+                        cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return e;
+  }
+  e = cudaMemcpyAsync(r.kvec + recip_split_at(ns) + 4 * (size_t)ncols(ns), toff_in.data(),
+                      sizeof(int) * toff_in.size(), cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return e;
   // dropped vectors keep S = 0 (their c(n) = 0 multiplies them in the energies)
   if (r.S) {
     e = cudaMemsetAsync(r.S, 0, sizeof(double2) * (size_t)nk * g.P, st);
     if (e != cudaSuccess) return e;
   }
+  if (r.S32) {
+    e = cudaMemsetAsync(r.S32, 0, sizeof(float2) * (size_t)nk * g.P, st);
+    if (e != cudaSuccess) return e;
+  }
   return cudaStreamSynchronize(st);
 }
 
-size_t recip_cols_ints(int ns) { return 5 * (size_t)(ns * (2 * ns + 1) + ns + 1) + 1; }
+// kvec: the kept columns (int4, longest first) and their compact table
+// offsets, then, from recip_split_at (16-byte aligned), the split list (the
+// FP64 columns, then the FP32 ones) and the FP64 columns' table offsets
+size_t recip_cols_ints(int ns) { return recip_split_at(ns) + 5 * (size_t)ncols(ns) + 1; }
 
 // compact table offsets behind the column table in the same buffer
 static const int *recip_toff(const Recip &r) {
   return r.kvec + 4 * (size_t)(r.nsum * (2 * r.nsum + 1) + r.nsum + 1);
 }
-
-static int ncols(int ns) { return ns * (2 * ns + 1) + ns + 1; }
+static const int4 *recip_split_cols(const Recip &r) { return (const int4 *)(r.kvec + recip_split_at(r.nsum)); }
+static const int *recip_split_toff(const Recip &r) {
+  return r.kvec + recip_split_at(r.nsum) + 4 * (size_t)ncols(r.nsum);
+}
 
 #define DISPATCH_NS(nsv, ...)                                         \
   switch (nsv) {                                                      \
@@ -2503,8 +2594,10 @@ static int ncols(int ns) { return ns * (2 * ns + 1) + ns + 1; }
     default: return cudaErrorInvalidValue;                            \
   }
 
+// FP64 structure factors of the columns cols[0, nc) (all kept columns by default)
 static cudaError_t structure_factors(const Geo &g, const Recip &r, const double *x,
-                                     cudaStream_t st) {
+                                     cudaStream_t st, const int4 *cols = nullptr, int nc = -1) {
+  if (!cols) cols = (const int4 *)r.kvec, nc = r.ncol;
   const size_t n = (size_t)g.P * 3 * g.Ns;
   {
     XK_PROF("phase");
@@ -2512,7 +2605,7 @@ static cudaError_t structure_factors(const Geo &g, const Recip &r, const double 
   }
   cudaError_t e = XK_LAUNCHED();
   if (e != cudaSuccess) return e;
-  const int nc = r.ncol;
+  if (nc <= 0) return cudaSuccess;
   {
     XK_PROF("sk");
     int lay = tuning(TUNE_SK_LAYOUT, r.nsum, 3, g.N, g.P);
@@ -2523,15 +2616,15 @@ static cudaError_t structure_factors(const Geo &g, const Recip &r, const double 
       // the blocks, each with half the work
       dim3 grid((nc + 7) / 8, g.P);
       DISPATCH_NS(r.nsum, (k_sk<NS, 8, 32><<<grid, 256, 0, st>>>(g, (const double2 *)r.phase,
-                                                                 (const int4 *)r.kvec, nc, (double2 *)r.S, r.nk)));
+                                                                 cols, nc, (double2 *)r.S, r.nk)));
     } else if (lay == SK_16x16) {
       dim3 grid((nc + 15) / 16, g.P);
       DISPATCH_NS(r.nsum, (k_sk<NS, 16, 16><<<grid, 256, 0, st>>>(g, (const double2 *)r.phase,
-                                                                  (const int4 *)r.kvec, nc, (double2 *)r.S, r.nk)));
+                                                                  cols, nc, (double2 *)r.S, r.nk)));
     } else {
       dim3 grid((nc + 63) / 64, g.P);
       DISPATCH_NS(r.nsum, (k_sk<NS, 64, 1><<<grid, 64, 0, st>>>(g, (const double2 *)r.phase,
-                                                                (const int4 *)r.kvec, nc, (double2 *)r.S, r.nk)));
+                                                                cols, nc, (double2 *)r.S, r.nk)));
     }
   }
   return XK_LAUNCHED();
@@ -2539,36 +2632,49 @@ static cudaError_t structure_factors(const Geo &g, const Recip &r, const double 
 
 size_t recip_table_doubles(const Geo &g, int ns) { return (size_t)g.P * ncols(ns) * (4 * ns + 1) * 2; }
 
+static cudaError_t recip_cols32(const Geo &g, const Recip &r, const double *x, double inv_mP, double *f,
+                                cudaStream_t st, const int4 *cols, int nc, float2 *S32, float2 *T32);
+
 cudaError_t recip_force(const Geo &g, const Recip &r, const double *x, double inv_mP, double *f,
-                        cudaStream_t st) {
+                        cudaStream_t st, bool fp32_outer) {
   if (g.D != 3) return cudaErrorInvalidValue;
-  cudaError_t e = structure_factors(g, r, x, st);
+  // the split: the FP64 columns here, the small-weight ones by the FP32 kernels
+  const bool split = fp32_outer && r.S32 && r.ncol_out > 0;
+  const int4 *cols = split ? recip_split_cols(r) : (const int4 *)r.kvec;
+  const int *toff = split ? recip_split_toff(r) : recip_toff(r);
+  const int nc = split ? r.ncol_in : r.ncol;
+  cudaError_t e = structure_factors(g, r, x, st, cols, nc);
   if (e != cudaSuccess) return e;
-  const int nc = r.ncol;
-  const size_t smem = sizeof(double2) * r.tsz;
+  const size_t smem = sizeof(double2) * (split ? r.tsz_in : r.tsz);
   dim3 tgrid((nc + 7) / 8, g.P), tblk(r.nsum + 1, 8);
   dim3 grid((g.N + 127) / 128, g.P);
-  DISPATCH_NS(r.nsum, {
-    {
-      XK_PROF("recip_tables");
-      k_recip_tables<NS><<<tgrid, tblk, 0, st>>>((const int4 *)r.kvec, nc, (const double2 *)r.S, r.coef,
-                                                 r.nk, (double2 *)r.T);
-    }
-    auto kf = k_recip_force<NS>;
-    // opt in to the largest dynamic shared memory once per instantiation
-    static bool opted = false;
-    if (!opted) {
-      cudaError_t ea = cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-      if (ea != cudaSuccess) return ea;
-      opted = true;
-    }
-    {
-      XK_PROF("recip_force");
-      kf<<<grid, 128, smem, st>>>(g, (const double2 *)r.phase, (const int4 *)r.kvec, recip_toff(r), nc,
-                                  (const double2 *)r.T, 4 * M_PI * inv_mP, f, nullptr, 0.0);
-    }
-  });
-  return XK_LAUNCHED();
+  if (nc > 0) {
+    DISPATCH_NS(r.nsum, {
+      {
+        XK_PROF("recip_tables");
+        k_recip_tables<NS><<<tgrid, tblk, 0, st>>>(cols, nc, (const double2 *)r.S, r.coef, r.nk, (double2 *)r.T);
+      }
+      auto kf = k_recip_force<NS>;
+      // opt in to the largest dynamic shared memory once per instantiation
+      static bool opted = false;
+      if (!opted) {
+        cudaError_t ea = cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+        if (ea != cudaSuccess) return ea;
+        opted = true;
+      }
+      {
+        XK_PROF("recip_force");
+        kf<<<grid, 128, smem, st>>>(g, (const double2 *)r.phase, cols, toff, nc, (const double2 *)r.T,
+                                    4 * M_PI * inv_mP, f, nullptr, 0.0);
+      }
+    });
+    e = XK_LAUNCHED();
+    if (e != cudaSuccess) return e;
+  }
+  if (!split) return cudaSuccess;
+  // the FP32 columns' tables go behind the FP64 columns' ones
+  float2 *T32 = (float2 *)(r.T + 2 * (size_t)g.P * r.ncol_in * (4 * r.nsum + 1));
+  return recip_cols32(g, r, x, inv_mP, f, st, cols + r.ncol_in, r.ncol_out, (float2 *)r.S32, T32);
 }
 
 cudaError_t recip_force_energy(const Geo &g, const Recip &r, const double *x, double scale, double *f,
@@ -3608,6 +3714,14 @@ __global__ void __launch_bounds__(2 * RF_PB) k_recip_force32(Geo g, const float2
 cudaError_t recip_force32(const Geo &g, const Recip &r, const double *x, double inv_mP, double *f,
                           cudaStream_t st) {
   if (g.D != 3) return cudaErrorInvalidValue;
+  // the FP32 structure factors and tables use the FP64 form's buffers
+  return recip_cols32(g, r, x, inv_mP, f, st, (const int4 *)r.kvec, r.ncol, (float2 *)r.S, (float2 *)r.T);
+}
+
+// phases, structure factors, tables and forces in FP32 for the columns
+// cols[0, nc): all kept columns (the mixed form) or the FP64 form's split
+static cudaError_t recip_cols32(const Geo &g, const Recip &r, const double *x, double inv_mP, double *f,
+                                cudaStream_t st, const int4 *cols, int nc, float2 *S32, float2 *T32) {
   const size_t n = (size_t)g.P * 3 * g.Ns;
   // FP32 phases live behind the FP64 ones in the same buffer
   float2 *ph32 = (float2 *)(r.phase + recip_phase_doubles(g, r.nsum));
@@ -3617,13 +3731,11 @@ cudaError_t recip_force32(const Geo &g, const Recip &r, const double *x, double 
   }
   cudaError_t e = XK_LAUNCHED();
   if (e != cudaSuccess) return e;
-  const int nc = r.ncol;
+  if (nc <= 0) return cudaSuccess;
   dim3 tgrid((nc + 7) / 8, g.P), tblk(r.nsum + 1, 8);
   dim3 grid((g.N + RF_PB - 1) / RF_PB, g.P);
   const size_t smem =
       sizeof(float2) * nc * (4 * r.nsum + 1) + sizeof(int4) * nc + sizeof(float2) * 2 * (r.nsum + 1) * RF_PB;
-  float2 *T32 = (float2 *)r.T;
-  float2 *S32 = (float2 *)r.S;  // the FP32 structure factors (the FP64 form's buffer, first half)
   DISPATCH_NS(r.nsum, {
     {
       // one thread per item for slices below SK_BIG_N particles; above,
@@ -3631,17 +3743,17 @@ cudaError_t recip_force32(const Geo &g, const Recip &r, const double *x, double 
       XK_PROF("sk32");
       const int items = nc * ((NS + SK_NG - 1) / SK_NG);
       if (g.N < SK_BIG_N)
-        k_sk32<NS, 1><<<dim3((items + 255) / 256, g.P), 256, 0, st>>>(g, ph32, (const int4 *)r.kvec, nc,
+        k_sk32<NS, 1><<<dim3((items + 255) / 256, g.P), 256, 0, st>>>(g, ph32, cols, nc,
                                                                      S32, r.nk);
       else if (items > 64 || NS > 6)
-        k_sk32<NS, 4><<<dim3((items + 63) / 64, g.P), 256, 0, st>>>(g, ph32, (const int4 *)r.kvec, nc, S32, r.nk);
+        k_sk32<NS, 4><<<dim3((items + 63) / 64, g.P), 256, 0, st>>>(g, ph32, cols, nc, S32, r.nk);
       else
         k_sk32<(NS <= 6 ? NS : 6), 16><<<dim3((items + 15) / 16, g.P), 256, 0, st>>>(
-            g, ph32, (const int4 *)r.kvec, nc, S32, r.nk);
+            g, ph32, cols, nc, S32, r.nk);
     }
     {
       XK_PROF("recip_tables32");
-      k_recip_tables32<NS><<<tgrid, tblk, 0, st>>>((const int4 *)r.kvec, nc, S32, (const float *)(r.coef + r.nk),
+      k_recip_tables32<NS><<<tgrid, tblk, 0, st>>>(cols, nc, S32, (const float *)(r.coef + r.nk),
                                                   r.nk, T32);
     }
     auto kf = k_recip_force32<NS>;
@@ -3653,7 +3765,7 @@ cudaError_t recip_force32(const Geo &g, const Recip &r, const double *x, double 
     }
     {
       XK_PROF("recip_force32");
-      kf<<<grid, 2 * RF_PB, smem, st>>>(g, ph32, (const int4 *)r.kvec, nc, T32, 4 * M_PI * inv_mP, f);
+      kf<<<grid, 2 * RF_PB, smem, st>>>(g, ph32, cols, nc, T32, 4 * M_PI * inv_mP, f);
     }
   });
   return XK_LAUNCHED();

@@ -175,7 +175,19 @@ struct PairPrm {
   double rcut;          // Ewald real-space cut-off radius
   int kmax[3];          // Ewald: image shifts |k| <= kmax around the minimum image
   double inv_mass;      // > 0: every bead has this inverse mass (FP32 kernel shortcut)
+  double xsplit;        // Ewald forces of the FP64 kernels: images with alpha R >= xsplit are
+                        // evaluated on the FP32 pipe (0: every image in FP64)
+  // set by the FP64 force launchers from the fields above
+  float alphaf;         // alpha
+  float xs2f;           // (xsplit / alpha)^2, or FLT_MAX with xsplit = 0
+  float rcf2;           // rcut^2
 };
+// alpha R at and beyond which the FP64 kernels evaluate real-space Ewald
+// images on the FP32 pipe (every image there has h(alpha R) < 5.2e-7, and
+// the sum of their sizes over all partners is 4 pi rho / alpha times the
+// integral of h from 4 on, 6.3e-8 pi rho / alpha; the FP32 evaluation's own
+// relative error is below 1e-5 there)
+constexpr double EWALD_XSPLIT = 4.0;
 size_t pair_scratch_doubles(const Geo &g);
 cudaError_t pair_force(const Geo &g, const PairPrm &p, const double *x, const double *m,
                        double *f, double *scratch, cudaStream_t st);
@@ -218,11 +230,20 @@ cudaError_t pair_energy_2(const Geo &ga, const Geo &gb, const PairPrm &p, const 
 // only because it is a cube (at alpha L = 5.6, nsum = 10 the kept ones are
 // the 52% inside |n|^2 <= 111).
 constexpr double RECIP_KEEP = 1e-17;
+// The FP64 forces (recip_force with fp32_outer) take the columns whose
+// every vector has a force weight below RECIP_SPLIT of the largest through
+// the FP32 kernels (at alpha L = 5.6 the columns with nx^2 + ny^2 >= 49: 45%
+// of the vectors); their FP32 rounding of a few 1e-7 then leaves below
+// 1e-13 of the reciprocal force.
+constexpr double RECIP_SPLIT = 1e-7;
 struct Recip {
   int nsum;
   int nk;              // half-space wave vectors of the cube
   int ncol;            // kept columns (set by recip_setup)
   int tsz;             // entries of the kept columns' force tables (compact, set by recip_setup)
+  int ncol_in, ncol_out;  // of those, the FP64 and the FP32 columns of the split (set by recip_setup)
+  int tsz_in;          // entries of the FP64 columns' compact force tables (set by recip_setup)
+  double *S32;         // [P][nk] FP32 complex structure factors of the split's FP32 columns, or NULL
   double *coef;        // [nk] s * exp(-pi^2 G^2/alpha^2) / (pi V G^2), 0 for a dropped vector;
                        // then the same nk values in FP32 (recip_coef_bytes(nk) bytes in all)
   int *kvec;           // kept columns, longest first: int4 (nx | nzmax << 8, ny, first nz,
@@ -240,8 +261,9 @@ size_t recip_cols_ints(int nsum);
 size_t recip_table_doubles(const Geo &g, int nsum);
 cudaError_t recip_setup(const Geo &g, int nsum, double alpha, double qs, Recip &r,
                         cudaStream_t st);
+// fp32_outer (with r.S32 set): the split columns through the FP32 kernels
 cudaError_t recip_force(const Geo &g, const Recip &r, const double *x, double inv_mP,
-                        double *f, cudaStream_t st);
+                        double *f, cudaStream_t st, bool fp32_outer = false);
 cudaError_t recip_energy(const Geo &g, const Recip &r, const double *x, double *acc,
                          double *scratch, cudaStream_t st);
 

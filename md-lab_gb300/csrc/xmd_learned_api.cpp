@@ -490,6 +490,7 @@ int md_gb300_ewald_model_create_x(md_gb300_ewald_model_t_x **out, md_pimd_t_x *p
   M->cheap.phase = M->rc_phase.as<double>();
   M->cheap.S = M->rc_S.as<double>();
   M->cheap.T = M->rc_T.as<double>();
+  M->cheap.S32 = nullptr;  // no split: the truncated sums are all FP64 or all FP32
   cudaError_t e = xk::recip_setup(g, nsum_cheap, M->alpha, M->qs, M->cheap, stream());
   if (e != cudaSuccess) {
     md_gb300_ewald_model_free_x(M);

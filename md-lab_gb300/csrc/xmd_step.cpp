@@ -395,15 +395,21 @@ int xmd::ewald_tables(md_pimd_t_x *pimd, SimDev *sd, PimdDev *pd) {
   XMD_TRY(reserve(pd->rc_cols, sizeof(int) * xk::recip_cols_ints(ns)));
   // FP64 phases, then their FP32 copy for the mixed form
   XMD_TRY(reserve(pd->rc_phase, sizeof(double) * xk::recip_phase_doubles(g, ns) * 3 / 2));
-  XMD_TRY(reserve(pd->rc_S, sizeof(double) * 2 * (size_t)nk * g.P));
+  // FP64 structure factors, then the FP32 ones of the FP64 form's split
+  XMD_TRY(reserve(pd->rc_S, sizeof(double) * 3 * (size_t)nk * g.P));
   XMD_TRY(reserve(pd->rc_T, sizeof(double) * xk::recip_table_doubles(g, ns)));
   xk::Recip r{};
   r.coef = pd->rc_coef.as<double>();
   r.kvec = pd->rc_cols.as<int>();
   r.S = pd->rc_S.as<double>();
+  r.S32 = r.S + 2 * (size_t)nk * g.P;
   XMD_CUDA(xk::recip_setup(g, ns, a, qs, r, stream()));
   pd->rc_ncol = r.ncol;
   pd->rc_tsz = r.tsz;
+  pd->rc_ncol_in = r.ncol_in;
+  pd->rc_ncol_out = r.ncol_out;
+  pd->rc_tsz_in = r.tsz_in;
+  pd->rc_s32_off = 2 * (size_t)nk * g.P;
   pd->rc_nsum = ns;
   pd->rc_alpha = a;
   pd->rc_qs = qs;
@@ -423,6 +429,10 @@ xk::Recip xmd::recip_of(PimdDev *pd) {
   r.nk = pd->rc_nk;
   r.ncol = pd->rc_ncol;
   r.tsz = pd->rc_tsz;
+  r.ncol_in = pd->rc_ncol_in;
+  r.ncol_out = pd->rc_ncol_out;
+  r.tsz_in = pd->rc_tsz_in;
+  r.S32 = pd->rc_S.as<double>() + pd->rc_s32_off;
   r.coef = pd->rc_coef.as<double>();
   r.kvec = pd->rc_cols.as<int>();
   r.phase = pd->rc_phase.as<double>();
@@ -441,6 +451,7 @@ xk::PairPrm xmd::pair_params(int kind) {
   p.alpha = md_coulomb_truc_x;
   p.nsum = md_coulomb_n_sum_x;
   p.rcut = p.alpha > 0 ? EWALD_XCUT / p.alpha : 0;
+  p.xsplit = g_precision == MD_GB_PRECISION_FP64_STRICT ? 0.0 : xk::EWALD_XSPLIT;
   return p;
 }
 
@@ -494,7 +505,8 @@ int md_pimd_calc_pair_force_x(md_pimd_t_x *pimd, md_pair_force_t_x pf) {
     if (mixed)
       XMD_CUDA(xk::recip_force32(sd->geo, recip_of(pd), sd->x.as<double>(), inv_mP, sd->f.as<double>(), st));
     else
-      XMD_CUDA(xk::recip_force(sd->geo, recip_of(pd), sd->x.as<double>(), inv_mP, sd->f.as<double>(), st));
+      XMD_CUDA(xk::recip_force(sd->geo, recip_of(pd), sd->x.as<double>(), inv_mP, sd->f.as<double>(), st,
+                               g_precision != MD_GB_PRECISION_FP64_STRICT));
   }
   if (mixed)
     XMD_CUDA(xk::pair_force32(sd->geo, prm, sd->x.as<double>(), sd->m.as<double>(), sd->f.as<double>(), scr, st));
@@ -709,7 +721,10 @@ int md_gb300_autotune_fp64_x(md_pimd_t_x *pimd, md_pair_force_t_x pf, int repeat
   int best_lay = 0;
   if (ewald && e == cudaSuccess) {
     const double inv_mP = 1.0 / (sd->mass0 * pimd->P);
-    auto recip = [&]() { return xk::recip_force(g, recip_of(pd), sd->x.as<double>(), inv_mP, ftmp.as<double>(), st); };
+    auto recip = [&]() {
+    return xk::recip_force(g, recip_of(pd), sd->x.as<double>(), inv_mP, ftmp.as<double>(), st,
+                           g_precision != MD_GB_PRECISION_FP64_STRICT);
+  };
     best_r = INFINITY;
     const int lays[3] = {xk::SK_16x16, xk::SK_8x32, xk::SK_64x1};
     for (int i = 0; i < 3 && e == cudaSuccess; ++i) {
@@ -735,7 +750,7 @@ int md_gb300_autotune_fp64_x(md_pimd_t_x *pimd, md_pair_force_t_x pf, int repeat
 }
 
 int md_gb300_set_precision_x(int mode) {
-  if (mode != MD_GB_PRECISION_FP64 && mode != MD_GB_PRECISION_MIXED)
+  if (mode != MD_GB_PRECISION_FP64 && mode != MD_GB_PRECISION_MIXED && mode != MD_GB_PRECISION_FP64_STRICT)
     return fail(MD_GB_ERR_ARG, "unknown precision mode %d", mode);
   g_precision = mode;
   return 0;

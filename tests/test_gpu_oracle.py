@@ -196,3 +196,30 @@ def test_full_size_properties(big_ueg):
         s.set_state(x=st["x"])
         deriv = (es[0] - es[1]) / (2 * h)
         assert abs(deriv + f[a, j, d]) <= 1e-5 * max(1.0, abs(f[a, j, d])), (deriv, f[a, j, d])
+
+
+def test_full_size_far_images_fp32_vs_strict_fp64(big_ueg):
+    """The default FP64 form evaluates the real-space Ewald images at
+    alpha R >= 4 and the wave-vector columns whose force weight is below
+    1e-7 of the largest on the FP32 pipe; against
+    MD_GB_PRECISION_FP64_STRICT (every term in FP64) every bead's pair force
+    agrees within 1e-10 of its own size, and the whole array within 1e-12
+    of its largest component."""
+    lib, s, st, box, T = big_ueg
+    N, P, D = 512, 64, 3
+    out = {}
+    try:
+        for mode in (2, 0):
+            lib.check(lib.md_gb300_set_precision_x(mode))
+            lib.check(lib.md_reset_force_x(s.sim))
+            lib.check(lib.md_pimd_calc_pair_force_x(s.pimd, lib.fn("md_coulomb_3d_ewald_force_x")))
+            out[mode] = s.state()["f"].reshape(N, P, D).copy()
+    finally:
+        lib.check(lib.md_gb300_set_precision_x(0))
+    d = np.abs(out[0] - out[2])
+    scale = np.abs(out[2]).max()
+    per_bead = d.max(axis=2) / np.maximum(np.abs(out[2]).max(axis=2), 1e-300)
+    print("largest difference / largest force", d.max() / scale, "largest per-bead relative", per_bead.max())
+    assert d.max() <= 1e-12 * scale
+    assert per_bead.max() <= 1e-10
+    assert d.max() > 0  # the FP32 path ran
