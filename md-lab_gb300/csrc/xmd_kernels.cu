@@ -1571,10 +1571,13 @@ struct EwWarp {
   int base[32];              // first queue item of each lane
 };
 
+// Ewald forces (not energies) come back without the strength p.qs, which
+// the kernels fold into the inverse masses: F the FP64 images' sum, G the
+// FP32 sum of the far images (alpha R >= p.xsplit).
 template <int D, int KIND, bool ENERGY_TAB>
 __device__ inline void pair_eval(const PairPrm &p, const Geo &g, const double *dx, const float *dxf,
                                  double *F, double &E, bool want_e, const double *tabs, bool active,
-                                 EwWarp *ws, int lane) {
+                                 EwWarp *ws, int lane, float *G = nullptr) {
   if (KIND == PAIR_GAUSSIAN || KIND == PAIR_PERIODIC_GAUSSIAN) {
     double t[D], r2 = 0;
 #pragma unroll
@@ -1619,23 +1622,41 @@ __device__ inline void pair_eval(const PairPrm &p, const Geo &g, const double *d
     // through ew_h32, and their sum joins the FP64 one per pair.
     constexpr double MAGIC = 6755399441055744.0;  // 1.5 * 2^52
     const double *tab = ENERGY_TAB ? tabs + EW_NINT * (EW_DEG + 1) : tabs;
-    const double rc2 = p.rcut * p.rcut;
-    const long long rc2_bits = __double_as_longlong(rc2);
+    const long long rc2_bits = __double_as_longlong(p.rc2);
     double mm[3];
     int sh[3];
     unsigned mask = 0u, far = 0u;
-    // FP32 copies of the box and of the minimum image (from the FP32
-    // positions): the culling, and the far images' evaluation
-    const float L0 = (float)g.box[0], L1 = (float)g.box[1], L2 = (float)g.box[2];
+    // FP32 minimum image (from the FP32 positions): the culling, and the far
+    // images' evaluation
+    const float L0 = p.boxf[0], L1 = p.boxf[1], L2 = p.boxf[2];
     float m0 = 0.f, m1 = 0.f, m2 = 0.f;
     if (active) {
+      if (ENERGY_TAB) {
 #pragma unroll
-      for (int d = 0; d < 3; ++d) {
-        const double tq = fma(dx[d], g.inv_box[d], MAGIC);  // MAGIC + rint(dx/L)
-        sh[d] = __double2loint(tq);
-        mm[d] = fma(-(tq - MAGIC), g.box[d], dx[d]);
+        for (int d = 0; d < 3; ++d) {
+          const double tq = fma(dx[d], g.inv_box[d], MAGIC);  // MAGIC + rint(dx/L)
+          sh[d] = __double2loint(tq);
+          mm[d] = fma(-(tq - MAGIC), g.box[d], dx[d]);
+        }
+      } else {
+        // forces: the shift from the FP32 separation (near a half box either
+        // image is a valid centre: the candidates reach one box further
+        // either way, and alpha rcut <= 5.2 keeps rcut below 1.35 L), and
+        // m = dx - s L by one FP64 addition of -L, 0 or L
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          sh[d] = __float2int_rn(dxf[d] * p.iboxf[d]);
+          double sel = 0.0;
+          if (sh[d] == 1) {
+            sel = -g.box[d];
+          } else if (sh[d] == -1) {
+            sel = g.box[d];
+          } else if (sh[d] != 0) {
+            sel = -(double)sh[d] * g.box[d];
+          }
+          mm[d] = dx[d] + sel;
+        }
       }
-      const float rc2f = (float)(rc2 * 1.0001);
       m0 = fmaf(-(float)sh[0], L0, dxf[0]);
       m1 = fmaf(-(float)sh[1], L1, dxf[1]);
       m2 = fmaf(-(float)sh[2], L2, dxf[2]);
@@ -1648,7 +1669,7 @@ __device__ inline void pair_eval(const PairPrm &p, const Geo &g, const double *d
         if (!ENERGY_TAB && r2 >= p.xs2f) {
           // a far image (alpha R >= xsplit): FP32, cut at rcut in FP32
           if (r2 < p.rcf2 && in_cube) far |= 1u << c;
-        } else if (r2 < rc2f && in_cube) {
+        } else if (r2 < p.rcf2_cull && in_cube) {
           mask |= 1u << c;
         }
       }
@@ -1656,8 +1677,8 @@ __device__ inline void pair_eval(const PairPrm &p, const Geo &g, const double *d
     // far images on the FP32 pipe, each lane its own (their h(alpha R) is
     // below 5.2e-7, so FP32's relative error of a few 1e-6 leaves a few
     // 1e-13 of the force in all)
-    float G0 = 0.f, G1 = 0.f, G2 = 0.f;
     if (!ENERGY_TAB) {
+      float G0 = 0.f, G1 = 0.f, G2 = 0.f;
       unsigned fr = far;
       while (fr) {
         const int c = __ffs(fr) - 1;
@@ -1670,6 +1691,7 @@ __device__ inline void pair_eval(const PairPrm &p, const Geo &g, const double *d
         G1 = fmaf(t1, v, G1);
         G2 = fmaf(t2, v, G2);
       }
+      G[0] = G0, G[1] = G1, G[2] = G2;
     }
     double F0 = 0, F1 = 0, F2 = 0, e = 0;
     // the three candidate components per axis, m - k L for k = -1, 0, 1
@@ -1755,14 +1777,9 @@ __device__ inline void pair_eval(const PairPrm &p, const Geo &g, const double *d
       }
       __syncwarp();
     }
-    if (!ENERGY_TAB && __any_sync(FULL, far != 0u)) {
-      F0 += (double)G0;
-      F1 += (double)G1;
-      F2 += (double)G2;
-    }
-    F[0] = p.qs * F0;
-    if (D > 1) F[1] = p.qs * F1;
-    if (D > 2) F[2] = p.qs * F2;
+    F[0] = F0;
+    if (D > 1) F[1] = F1;
+    if (D > 2) F[2] = F2;
     if (want_e) E = p.qs * e;
   }
 }
@@ -1808,21 +1825,26 @@ __global__ void __launch_bounds__(256, 2) k_pair_tiles(Geo g, PairPrm p,
       fa[d] = fb[d] = 0.0;
     }
     // inverse masses, so that each pair multiplies instead of dividing
-    const double ima = (!ENERGY && va) ? 1.0 / m[(size_t)j * g.Ns + a] : 1.0;
-    double imb = (!ENERGY && vb) ? 1.0 / m[(size_t)j * g.Ns + b0] : 1.0;
+    // (Ewald forces: times the strength, and FP32 copies for the far images)
+    constexpr bool EWF = KIND == PAIR_EWALD_REAL && !ENERGY;
+    const double ima = (!ENERGY && va) ? (EWF ? p.qs : 1.0) / m[(size_t)j * g.Ns + a] : 1.0;
+    double imb = (!ENERGY && vb) ? (EWF ? p.qs : 1.0) / m[(size_t)j * g.Ns + b0] : 1.0;
+    const float ima32 = EWF ? (float)ima : 0.f;
+    float imb32 = EWF ? (float)imb : 0.f;
+    float ga[3] = {0.f, 0.f, 0.f}, gb[3] = {0.f, 0.f, 0.f};  // far images' forces (FP32)
     double ea = 0;
     for (int s = 0; s < 32; ++s) {
       const int bi = J * 32 + ((lane + s) & 31);
       const bool act = va && bi < g.N && (I != J || a > bi);
       double dx[D], F[D], E = 0;
-      float dxf[D];
+      float dxf[D], G[3] = {0.f, 0.f, 0.f};
 #pragma unroll
       for (int d = 0; d < D; ++d) {
         dx[d] = xa[d] - xb[d];
         dxf[d] = xaf[d] - xbf[d];
         F[d] = 0;
       }
-      if (KIND == PAIR_EWALD_REAL) pair_eval<D, KIND, ENERGY>(p, g, dx, dxf, F, E, ENERGY, stab, act, ews, lane);
+      if (KIND == PAIR_EWALD_REAL) pair_eval<D, KIND, ENERGY>(p, g, dx, dxf, F, E, ENERGY, stab, act, ews, lane, G);
       if (act) {
         if (KIND != PAIR_EWALD_REAL)
           pair_eval<D, KIND, ENERGY>(p, g, dx, dxf, F, E, ENERGY, stab, true, nullptr, lane);
@@ -1836,6 +1858,14 @@ __global__ void __launch_bounds__(256, 2) k_pair_tiles(Geo g, PairPrm p,
             fa[d] += F[d] * inv;
             fb[d] -= F[d] * inv;
           }
+          if (EWF) {
+            const float inv32 = a > bi ? ima32 : imb32;
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+              ga[d] = fmaf(G[d], inv32, ga[d]);
+              gb[d] = fmaf(-G[d], inv32, gb[d]);
+            }
+          }
         }
       }
       const int src = (lane + 1) & 31;
@@ -1844,13 +1874,22 @@ __global__ void __launch_bounds__(256, 2) k_pair_tiles(Geo g, PairPrm p,
         xb[d] = __shfl_sync(FULL, xb[d], src);
         if (KIND == PAIR_EWALD_REAL) xbf[d] = __shfl_sync(FULL, xbf[d], src);
         if (!ENERGY) fb[d] = __shfl_sync(FULL, fb[d], src);
+        if (EWF) gb[d] = __shfl_sync(FULL, gb[d], src);
       }
       if (!ENERGY) imb = __shfl_sync(FULL, imb, src);
+      if (EWF) imb32 = __shfl_sync(FULL, imb32, src);
     }
     if (ENERGY) {
       ea = warp_sum(ea);
       if (lane == 0) out[warp] = ea;
       continue;
+    }
+    if (EWF) {
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        fa[d] += (double)ga[d];
+        fb[d] += (double)gb[d];
+      }
     }
     // slot layout: out[((t*P + j)*D + d)*Ns + l]
     if (I == J) {
@@ -1923,21 +1962,26 @@ __global__ void __launch_bounds__(256, 2) k_pair_cross(Geo ga, Geo gb, PairPrm p
       xbf[d] = (float)xb_[d];
       fa[d] = fb[d] = 0.0;
     }
-    const double ima = (!ENERGY && va) ? 1.0 / ma[(size_t)j * ga.Ns + a] : 1.0;
-    double imb = (!ENERGY && vb) ? 1.0 / mb[(size_t)j * gb.Ns + b0] : 1.0;
+    // inverse masses (Ewald forces: times the strength, and FP32 copies)
+    constexpr bool EWF = KIND == PAIR_EWALD_REAL && !ENERGY;
+    const double ima = (!ENERGY && va) ? (EWF ? p.qs : 1.0) / ma[(size_t)j * ga.Ns + a] : 1.0;
+    double imb = (!ENERGY && vb) ? (EWF ? p.qs : 1.0) / mb[(size_t)j * gb.Ns + b0] : 1.0;
+    const float ima32 = EWF ? (float)ima : 0.f;
+    float imb32 = EWF ? (float)imb : 0.f;
+    float gfa[3] = {0.f, 0.f, 0.f}, gfb[3] = {0.f, 0.f, 0.f};  // far images' forces (FP32)
     double ea = 0;
     for (int s = 0; s < 32; ++s) {
       const int bi = J * 32 + ((lane + s) & 31);
       const bool act = va && bi < gb.N;
       double dx[D], F[D], E = 0;
-      float dxf[D];
+      float dxf[D], G[3] = {0.f, 0.f, 0.f};
 #pragma unroll
       for (int d = 0; d < D; ++d) {
         dx[d] = xa_[d] - xb_[d];
         dxf[d] = xaf[d] - xbf[d];
         F[d] = 0;
       }
-      if (KIND == PAIR_EWALD_REAL) pair_eval<D, KIND, ENERGY>(p, ga, dx, dxf, F, E, ENERGY, stab, act, ews, lane);
+      if (KIND == PAIR_EWALD_REAL) pair_eval<D, KIND, ENERGY>(p, ga, dx, dxf, F, E, ENERGY, stab, act, ews, lane, G);
       if (act) {
         if (KIND != PAIR_EWALD_REAL)
           pair_eval<D, KIND, ENERGY>(p, ga, dx, dxf, F, E, ENERGY, stab, true, nullptr, lane);
@@ -1949,6 +1993,13 @@ __global__ void __launch_bounds__(256, 2) k_pair_cross(Geo ga, Geo gb, PairPrm p
             fa[d] += F[d] * ima;
             fb[d] -= F[d] * imb;
           }
+          if (EWF) {
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+              gfa[d] = fmaf(G[d], ima32, gfa[d]);
+              gfb[d] = fmaf(-G[d], imb32, gfb[d]);
+            }
+          }
         }
       }
       const int src = (lane + 1) & 31;
@@ -1957,13 +2008,22 @@ __global__ void __launch_bounds__(256, 2) k_pair_cross(Geo ga, Geo gb, PairPrm p
         xb_[d] = __shfl_sync(FULL, xb_[d], src);
         if (KIND == PAIR_EWALD_REAL) xbf[d] = __shfl_sync(FULL, xbf[d], src);
         if (!ENERGY) fb[d] = __shfl_sync(FULL, fb[d], src);
+        if (EWF) gfb[d] = __shfl_sync(FULL, gfb[d], src);
       }
       if (!ENERGY) imb = __shfl_sync(FULL, imb, src);
+      if (EWF) imb32 = __shfl_sync(FULL, imb32, src);
     }
     if (ENERGY) {
       ea = warp_sum(ea);
       if (lane == 0) outa[warp] = ea;
       continue;
+    }
+    if (EWF) {
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        fa[d] += (double)gfa[d];
+        fb[d] += (double)gfb[d];
+      }
     }
     if (va) {
 #pragma unroll
@@ -2036,20 +2096,27 @@ static int pair_grid(size_t warps_needed, const Geo &g) {
   return full;
 }
 
-// the FP32 constants of the Ewald far images (PairPrm::alphaf, xs2f, rcf2)
-PairPrm with_far_images(const PairPrm &p) {
+// the Ewald kernels' derived constants (PairPrm::rc2 ... iboxf), computed
+// once per launch instead of per pair
+PairPrm with_far_images(const PairPrm &p, const Geo &g) {
   PairPrm q = p;
+  q.rc2 = p.rcut * p.rcut;
   q.alphaf = (float)p.alpha;
-  q.rcf2 = (float)(p.rcut * p.rcut);
+  q.rcf2 = (float)q.rc2;
+  q.rcf2_cull = (float)(q.rc2 * 1.0001);
   q.xs2f = FLT_MAX;
   if (p.xsplit > 0 && p.alpha > 0) q.xs2f = (float)((p.xsplit / p.alpha) * (p.xsplit / p.alpha));
+  for (int d = 0; d < 3; ++d) {
+    q.boxf[d] = (float)g.box[d];
+    q.iboxf[d] = (float)g.inv_box[d];
+  }
   return q;
 }
 
 template <int D, bool ENERGY>
 static cudaError_t pair_launch(const Geo &g, const PairPrm &p_in, const double *x, const double *m,
                                double *out, int T, int jobs, cudaStream_t st) {
-  const PairPrm p = with_far_images(p_in);
+  const PairPrm p = with_far_images(p_in, g);
   const size_t warps = (size_t)jobs * g.P;
   switch (p.kind) {
     case PAIR_GAUSSIAN:
@@ -2134,7 +2201,7 @@ static cudaError_t cross_launch(const Geo &ga, const Geo &gb, const PairPrm &p, 
   const size_t dyn = KIND == PAIR_EWALD_REAL ? EW_TAB_BYTES : 0;
   const int grid = resident_grid(k_pair_cross<D, KIND, ENERGY>, (size_t)TA * TB * ga.P, occ, sms, dyn);
   XK_PROF("pair_cross");
-  k_pair_cross<D, KIND, ENERGY><<<grid, 256, dyn, st>>>(ga, gb, with_far_images(p), xa, ma, xb, mb, outa, outb, TA,
+  k_pair_cross<D, KIND, ENERGY><<<grid, 256, dyn, st>>>(ga, gb, with_far_images(p, ga), xa, ma, xb, mb, outa, outb, TA,
                                                         TB);
   return XK_LAUNCHED();
 }

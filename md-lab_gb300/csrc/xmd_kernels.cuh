@@ -177,10 +177,13 @@ struct PairPrm {
   double inv_mass;      // > 0: every bead has this inverse mass (FP32 kernel shortcut)
   double xsplit;        // Ewald forces of the FP64 kernels: images with alpha R >= xsplit are
                         // evaluated on the FP32 pipe (0: every image in FP64)
-  // set by the FP64 force launchers from the fields above
+  // set by the FP64 force launchers from the fields above and the box
+  double rc2;           // rcut^2
   float alphaf;         // alpha
   float xs2f;           // (xsplit / alpha)^2, or FLT_MAX with xsplit = 0
   float rcf2;           // rcut^2
+  float rcf2_cull;      // rcut^2 (1 + 1e-4): the FP32 culling's margin
+  float boxf[3], iboxf[3];  // box lengths and their inverses
 };
 // alpha R at and beyond which the FP64 kernels evaluate real-space Ewald
 // images on the FP32 pipe (every image there has h(alpha R) < 5.2e-7, and
