@@ -981,6 +981,14 @@ __global__ void __launch_bounds__(SH_T) k_sk_shells(Geo g, DescPrm p, const doub
 // into one before the basis product.
 constexpr int DS_ROWS = 32, DS_WARPS = 8, DS_T = DS_ROWS * DS_WARPS;
 
+// 2^x by the MUFU instruction (relative error about 2^-22; x below -126
+// gives 0, the limit the bumps approach far from their centres)
+__device__ __forceinline__ float ex2_approx(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
 template <bool RAW>
 __global__ void __launch_bounds__(DS_T, 2) k_desc(Geo g, DescPrm p, const double *__restrict__ x,
                                                   uint8_t *__restrict__ ximg, float *__restrict__ V,
@@ -1005,31 +1013,55 @@ __global__ void __launch_bounds__(DS_T, 2) k_desc(Geo g, DescPrm p, const double
   float vs[9];
 #pragma unroll
   for (int i = 0; i < 9; ++i) vs[i] = 0.f;
-  for (int c = warp; c < g.N; c += DS_WARPS) {
-    const float4 xc = pos[c];
-    float d0 = xr.x - xc.x, d1 = xr.y - xc.y, d2 = xr.z - xc.z;
-    d0 -= p.box[0] * rintf(d0 * p.inv_box[0]);
-    d1 -= p.box[1] * rintf(d1 * p.inv_box[1]);
-    d2 -= p.box[2] * rintf(d2 * p.inv_box[2]);
-    const float r2 = d0 * d0 + d1 * d1 + d2 * d2;
-    const bool in = live && c != l && r2 < rc2;
-    const float r2s = in ? r2 : rc2;  // fc = 0 there: every deposit below adds zero
-    const float ir = rsqrtf(r2s), r = r2s * ir, u = 1.f - r2s * inv_rc2, fc = in ? u * u : 0.f;
-    const float tb = fmaxf(r * p.inv_h - 0.5f, 0.f);  // below the first bin centre: all into bin 0
-    const int b0 = min((int)tb, DESC_BINS - 1);
-    const float w1 = b0 < DESC_BINS - 1 ? tb - (float)b0 : 0.f;
-    const int b1 = min(b0 + 1, DESC_BINS - 1);
-    hcol[b0 * DS_T] += fc * (1.f - w1);
-    hcol[b1 * DS_T] += fc * w1;
-    const float fir = fc * ir;
+  // per partner: the minimum image; the bin by the 1.5 * 2^23 rounding
+  // (no float <-> int conversions, which share the slow MUFU pipe; at an
+  // exact bin centre rounding to even picks the lower bin with weight 1 on
+  // the upper, the same deposits); the three vector bumps from two
+  // exponentials (q_1 = q_0 rho, q_2 = q_1 rho qk)
+  constexpr float RND = 12582912.f;  // 1.5 * 2^23
+  // two partners per iteration (c and c + DS_WARPS), their arithmetic
+  // interleaved, the deposits in partner order
+  for (int c = warp; c < g.N; c += 2 * DS_WARPS) {
+    const int cb = c + DS_WARPS;
+    const bool hb = cb < g.N;
+    const float4 xa4 = pos[c], xb4 = pos[hb ? cb : c];
+    float da[3] = {xr.x - xa4.x, xr.y - xa4.y, xr.z - xa4.z};
+    float db[3] = {xr.x - xb4.x, xr.y - xb4.y, xr.z - xb4.z};
 #pragma unroll
-    for (int m = 0; m < 3; ++m) {
-      const float dr = r - p.vmu[m];
-      const float q = fir * __expf(-dr * dr * p.vinv2s2[m]);
-      vs[3 * m] = fmaf(q, d0, vs[3 * m]);
-      vs[3 * m + 1] = fmaf(q, d1, vs[3 * m + 1]);
-      vs[3 * m + 2] = fmaf(q, d2, vs[3 * m + 2]);
+    for (int d = 0; d < 3; ++d) {
+      da[d] -= p.box[d] * rintf(da[d] * p.inv_box[d]);
+      db[d] -= p.box[d] * rintf(db[d] * p.inv_box[d]);
     }
+    const float r2a = da[0] * da[0] + da[1] * da[1] + da[2] * da[2];
+    const float r2b = db[0] * db[0] + db[1] * db[1] + db[2] * db[2];
+    const bool ina = live && c != l && r2a < rc2, inb = live && hb && cb != l && r2b < rc2;
+    const float r2sa = ina ? r2a : rc2, r2sb = inb ? r2b : rc2;  // fc = 0 there: the deposits add zero
+    const float ira = rsqrtf(r2sa), irb = rsqrtf(r2sb);
+    const float ra = r2sa * ira, rb = r2sb * irb;
+    const float ua = 1.f - r2sa * inv_rc2, ub = 1.f - r2sb * inv_rc2;
+    const float fca = ina ? ua * ua : 0.f, fcb = inb ? ub * ub : 0.f;
+    const float tba = fmaxf(ra * p.inv_h - 0.5f, 0.f), tbb = fmaxf(rb * p.inv_h - 0.5f, 0.f);
+    const float tqa = (tba - 0.5f) + RND, tqb = (tbb - 0.5f) + RND;
+    int b0a = __float_as_int(tqa) - __float_as_int(RND), b0b = __float_as_int(tqb) - __float_as_int(RND);
+    float w1a = tba - (tqa - RND), w1b = tbb - (tqb - RND);
+    if (b0a >= DESC_BINS - 1) b0a = DESC_BINS - 1, w1a = 0.f;
+    if (b0b >= DESC_BINS - 1) b0b = DESC_BINS - 1, w1b = 0.f;
+    const float ta = ra - p.vmu[0], tb = rb - p.vmu[0];
+    const float q0a = fca * ira * ex2_approx(-p.qa * ta * ta), q0b = fcb * irb * ex2_approx(-p.qa * tb * tb);
+    const float rhoa = ex2_approx(fmaf(p.qc1, ta, p.qc0)), rhob = ex2_approx(fmaf(p.qc1, tb, p.qc0));
+    const float q1a = q0a * rhoa, q1b = q0b * rhob;
+    const float q2a = q1a * (rhoa * p.qk), q2b = q1b * (rhob * p.qk);
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      vs[d] = fmaf(q0b, db[d], fmaf(q0a, da[d], vs[d]));
+      vs[3 + d] = fmaf(q1b, db[d], fmaf(q1a, da[d], vs[3 + d]));
+      vs[6 + d] = fmaf(q2b, db[d], fmaf(q2a, da[d], vs[6 + d]));
+    }
+    const float wa = fca * w1a, wb = fcb * w1b;
+    hcol[b0a * DS_T] += fca - wa;
+    hcol[min(b0a + 1, DESC_BINS - 1) * DS_T] += wa;
+    hcol[b0b * DS_T] += fcb - wb;
+    hcol[min(b0b + 1, DESC_BINS - 1) * DS_T] += wb;
   }
 #pragma unroll
   for (int i = 0; i < 9; ++i) vacc[(warp * DS_ROWS + lane) * 9 + i] = vs[i];

@@ -50,6 +50,10 @@ struct DescPrm {
   float rc, inv_h;             // cut-off radius (half the smallest box length), bins per unit
   float box[3], inv_box[3];
   float vmu[3], vinv2s2[3];    // vector radial bases: centres, 1/(2 sigma^2)
+  // the same bases, equally spaced with one width (centres mu_m = mu_0 + m D,
+  // a = 1/(2 sigma^2)), for the kernel: with t = r - mu_0, q_0 = 2^(-qa t^2),
+  // rho = 2^(qc1 t + qc0), q_1 = q_0 rho, q_2 = q_1 rho qk (log2 e folded in)
+  float qa, qc1, qc0, qk;
   float vscale[3];             // scale of each vector feature in V
   const float *basis;          // [DESC_BINS][32] histogram -> radial features (Gaussians in r)
   const int4 *kvec;            // half-space wave vectors of the lowest shells: (nx >= 0, ny, nz, shell)

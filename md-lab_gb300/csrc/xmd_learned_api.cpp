@@ -517,6 +517,13 @@ int md_gb300_ewald_model_create_x(md_gb300_ewald_model_t_x **out, md_pimd_t_x *p
     M->dp.vinv2s2[d] = (float)(1.0 / (2 * M->vsig[d] * M->vsig[d]));
     M->dp.vscale[d] = 1.f;
   }
+  {
+    const double a = 1.0 / (2 * M->vsig[0] * M->vsig[0]), D = 0.25 * rcut, L2E = 1.4426950408889634;
+    M->dp.qa = (float)(a * L2E);
+    M->dp.qc1 = (float)(2 * a * D * L2E);
+    M->dp.qc0 = (float)(-a * D * D * L2E);
+    M->dp.qk = (float)exp(-2 * a * D * D);
+  }
   M->dp.basis = M->basis.as<float>();
   M->dp.fmean = M->fmean.as<float>();
   M->dp.fistd = M->fistd.as<float>();
