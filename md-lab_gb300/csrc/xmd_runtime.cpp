@@ -62,8 +62,12 @@ int ensure_device() {
   if (!device_present()) return fail(MD_GB_ERR_NO_DEVICE, "no CUDA device is available");
   std::lock_guard<std::mutex> lk(g_mu);
   if (!g_own) {
-    cudaError_t e = cudaStreamCreateWithFlags(&g_own, cudaStreamNonBlocking);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamCreateWithFlags");
+    // a middle priority: above the learned model's descriptor stream (the
+    // default, lowest), below the exchange chain's side stream (highest)
+    int lo = 0, hi = 0;
+    cudaError_t e = cudaDeviceGetStreamPriorityRange(&lo, &hi);
+    if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&g_own, cudaStreamNonBlocking, (lo + hi) / 2);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamCreateWithPriority");
   }
   return 0;
 }
@@ -627,7 +631,7 @@ int capture_single(cudaError_t (*launch)(void *), void *ctx, void (*release)(voi
   if (e == cudaSuccess) {
     gr = new md_gb300_graph();
     gr->g = g;
-    e = cudaGraphInstantiate(&gr->e, g, 0);
+    e = cudaGraphInstantiate(&gr->e, g, cudaGraphInstantiateFlagUseNodePriority);
   }
   if (e != cudaSuccess) {
     if (g) cudaGraphDestroy(g);
@@ -709,7 +713,7 @@ int md_gb300_capture_end_x(md_gb300_graph_t_x **out) {
     delete gr;
     return cuda_fail(e, "cudaStreamEndCapture");
   }
-  e = cudaGraphInstantiate(&gr->e, gr->g, 0);
+  e = cudaGraphInstantiate(&gr->e, gr->g, cudaGraphInstantiateFlagUseNodePriority);
   if (e != cudaSuccess) {
     cudaGraphDestroy(gr->g);
     delete gr;
@@ -767,7 +771,7 @@ int md_gb300_capture_ensemble_x(int n, md_gb300_system_step_fn_x step, void *ctx
   }
   md_gb300_graph *gr = new md_gb300_graph();
   gr->g = g;
-  const cudaError_t ie = cudaGraphInstantiate(&gr->e, gr->g, 0);
+  const cudaError_t ie = cudaGraphInstantiate(&gr->e, gr->g, cudaGraphInstantiateFlagUseNodePriority);
   if (ie != cudaSuccess) {
     cudaGraphDestroy(gr->g);
     delete gr;
