@@ -2454,7 +2454,10 @@ __global__ void k_recip_tables(const int4 *__restrict__ cols, int ncol, const do
 // WITH_E also writes the particle's share of the slice energy,
 //   e[j*Ns + l] = sum_n c(n) Re(e^{i theta} conj S(n)) - e0 = Re(sum_col e_xy U) - e0,
 // with e0 = sum_n c(n), so that sum_l e = sum_n c(n) (|S(n)|^2 - N).
-template <int NS, bool WITH_E = false>
+// TPP > 1 (a few bead slices, as in the learned model's judgements): TPP
+// consecutive threads share a particle, thread h taking columns h, h + TPP,
+// ..., and their sums are added by a butterfly over the TPP lanes.
+template <int NS, bool WITH_E = false, int TPP = 1>
 __global__ void __launch_bounds__(128) k_recip_force(Geo g, const double2 *__restrict__ ph,
                                                      const int4 *__restrict__ cols, const int *__restrict__ toff,
                                                      int ncol, const double2 *__restrict__ T, double scale,
@@ -2472,14 +2475,14 @@ __global__ void __launch_bounds__(128) k_recip_force(Geo g, const double2 *__res
     for (int q = threadIdx.x & 31; q < n; q += 32) sT[toff[ci] + q] = Tj[(size_t)ci * NT + q];
   }
   __syncthreads();
-  const int l = blockIdx.x * blockDim.x + threadIdx.x;
-  if (l >= g.N) return;
+  const int l = blockIdx.x * (blockDim.x / TPP) + threadIdx.x / TPP, h = threadIdx.x % TPP;
+  if (l >= g.N) return;  // (a particle's TPP lanes leave together)
   double2 ez[NS + 1];
   const double2 *pz = ph + (((size_t)j * 3 + 2) * (NS + 1)) * g.Ns + l;
 #pragma unroll
   for (int n = 1; n <= NS; ++n) ez[n] = pz[(size_t)n * g.Ns];
   double Fx = 0, Fy = 0, Fz = 0, Er = 0;
-  for (int ci = 0; ci < ncol; ++ci) {
+  for (int ci = h; ci < ncol; ci += TPP) {
     const int4 c = cols[ci];
     const int nzc = col_nz(c);
     const double2 exy = cmul(phase_at(ph, g, NS, j, 0, col_nx(c), l), phase_at(ph, g, NS, j, 1, c.y, l));
@@ -2501,6 +2504,17 @@ __global__ void __launch_bounds__(128) k_recip_force(Geo g, const double2 *__res
     Fy = fma((double)c.y, Tm, Fy);
     Fz += Zm;
     if (WITH_E) Er += fma(exy.x, Ur, -exy.y * Ui);  // Re(e_xy U)
+  }
+  if (TPP > 1) {
+    const unsigned gm = ((1u << TPP) - 1u) << ((threadIdx.x & 31) & ~(TPP - 1));
+#pragma unroll
+    for (int o = 1; o < TPP; o <<= 1) {
+      Fx += __shfl_xor_sync(gm, Fx, o);
+      Fy += __shfl_xor_sync(gm, Fy, o);
+      Fz += __shfl_xor_sync(gm, Fz, o);
+      if (WITH_E) Er += __shfl_xor_sync(gm, Er, o);
+    }
+    if (h != 0) return;
   }
   if (WITH_E) e[(size_t)j * g.Ns + l] = Er - e0;
   f[sidx(j, 0, l, 3, g.Ns)] += scale * Fx * g.inv_box[0];
@@ -2753,28 +2767,33 @@ cudaError_t recip_force_energy(const Geo &g, const Recip &r, const double *x, do
   const double e0 = r.csum;
   const size_t smem = sizeof(double2) * r.tsz;
   dim3 tgrid((nc + 7) / 8, g.P), tblk(r.nsum + 1, 8);
-  // blocks of 128 particles, or fewer when that leaves most SMs idle (a few
-  // bead slices, as in the learned model's judgements): a block's time is
-  // set by its particles' column sums, whatever the grid
-  int tpb = 128;
-  while (tpb > 32 && (size_t)((g.N + tpb - 1) / tpb) * g.P < 2 * 152) tpb >>= 1;
-  dim3 grid((g.N + tpb - 1) / tpb, g.P);
+  // blocks of 128 threads; with few bead slices (the learned model's
+  // judgements) 4 or 16 threads share a particle's columns, so that the
+  // grid still covers every SM twice
+  int dev = 0, sms = 152;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const size_t parts = (size_t)g.N * g.P;
+  const int tpp = parts * 1 >= (size_t)256 * sms ? 1 : (parts * 4 >= (size_t)256 * sms ? 4 : 16);
+  const int ppb = 128 / tpp;
+  dim3 grid((g.N + ppb - 1) / ppb, g.P);
   DISPATCH_NS(r.nsum, {
     {
       XK_PROF("recip_tables");
       k_recip_tables<NS><<<tgrid, tblk, 0, st>>>((const int4 *)r.kvec, nc, (const double2 *)r.S, r.coef,
                                                  r.nk, (double2 *)r.T);
     }
-    auto kf = k_recip_force<NS, true>;
-    static bool opted = false;
-    if (!opted) {
+    auto kf = tpp == 1 ? k_recip_force<NS, true, 1> : (tpp == 4 ? k_recip_force<NS, true, 4> : k_recip_force<NS, true, 16>);
+    static bool opted[3] = {false, false, false};
+    const int oi = tpp == 1 ? 0 : (tpp == 4 ? 1 : 2);
+    if (!opted[oi]) {
       cudaError_t ea = cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
       if (ea != cudaSuccess) return ea;
-      opted = true;
+      opted[oi] = true;
     }
     {
       XK_PROF("recip_force_energy");
-      kf<<<grid, tpb, smem, st>>>(g, (const double2 *)r.phase, (const int4 *)r.kvec, recip_toff(r), nc,
+      kf<<<grid, 128, smem, st>>>(g, (const double2 *)r.phase, (const int4 *)r.kvec, recip_toff(r), nc,
                                   (const double2 *)r.T, 4 * M_PI * scale, f, e, e0);
     }
   });
