@@ -42,6 +42,7 @@ struct ProfRec {
 static std::vector<ProfRec> g_prof_recs;
 
 void profile_enable(bool on) { g_prof = on; }
+bool profiling() { return g_prof; }
 
 // sums the recorded launches per kernel name: returns "name ms launches;..."
 std::string profile_report() {

@@ -55,6 +55,9 @@ struct Prof {
 
 // live per-kernel timing with CUDA events; report is "name total_ms launches;..."
 void profile_enable(bool on);
+// whether the live per-kernel timing is on (the library then joins its
+// forked streams at once, so that each kernel is timed alone)
+bool profiling();
 std::string profile_report();
 // measured FP64 FMA throughput of this GPU in TFLOP/s (-1 on failure)
 double fp64_peak_tflops(cudaStream_t st);

@@ -321,6 +321,8 @@ int learned_pair_force(md_pimd_t_x *pimd, SimDev *sd, PimdDev *pd, const xk::Pai
   XMD_CUDA(cudaStreamWaitEvent(M->ms, M->mfork, 0));
   XMD_TRY(predict(M, sd, M->ms));
   XMD_CUDA(cudaEventRecord(M->mdone, M->ms));
+  // timing each kernel alone: the network's branch is joined at once
+  if (xk::profiling() && !capturing()) XMD_CUDA(cudaStreamWaitEvent(st, M->mdone, 0));
   if (md_gb300_get_precision_x() == MD_GB_PRECISION_MIXED) {
     XMD_CUDA(xk::recip_force32(sd->geo, M->cheap, x, inv_mP, f, st));
     XMD_CUDA(xk::pair_force32(sd->geo, prm, x, sd->m.as<double>(), f, scr, st));

@@ -120,6 +120,8 @@ int side_begin(cudaStream_t *out) {
 int side_end(SimDev *fex) {
   Side &sd = g_side[stream()];
   XMD_CUDA(cudaEventRecord(sd.done, sd.s));
+  // timing each kernel alone: the library stream waits for the side chain now
+  if (xk::profiling() && !capturing()) XMD_CUDA(cudaStreamWaitEvent(stream(), sd.done, 0));
   sd.pending = true;
   if (fex && std::find(sd.fex.begin(), sd.fex.end(), fex) == sd.fex.end()) sd.fex.push_back(fex);
   return 0;
