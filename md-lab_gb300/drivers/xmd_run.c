@@ -21,7 +21,8 @@
  *            Ewald alpha = alphaL [5.6] / L, reciprocal cube nsum [8];
  *            T from theta [0.5] x the spin-polarised Fermi temperature
  *            when the input gives no T
- *   precision [0]: 1 = FP32 pair forces (md_gb300_set_precision_x)
+ *   precision [0]: 1 = FP32 pair forces, 2 = every term in FP64
+ *            (md_gb300_set_precision_x)
  * Output: "param key value" lines, then "sample step E_primitive
  * E_virial" every `every` steps after equilibration, and one line
  * "result E_primitive mean err E_virial mean err samples n blocks b
