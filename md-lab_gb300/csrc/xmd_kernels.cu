@@ -1618,8 +1618,8 @@ __device__ inline void pair_eval(const PairPrm &p, const Geo &g, const double *d
     // from rsqrt.  On this GPU FP64 comparisons and int <-> double
     // conversions share the slow FP64 pipe, so rounding to integers uses
     // the 1.5 * 2^52 addition and the cut-off test compares bit patterns.
-    // Forces only: images at alpha R >= p.xsplit (two thirds of those inside
-    // rcut at alpha rcut = 5.2, xsplit = 4) go to the FP32 pipe instead,
+    // Forces only: images at alpha R >= p.xsplit (55% of those inside rcut
+    // at alpha rcut = 5.2, xsplit = 4) go to the FP32 pipe instead,
     // through ew_h32, and their sum joins the FP64 one per pair.
     constexpr double MAGIC = 6755399441055744.0;  // 1.5 * 2^52
     const double *tab = ENERGY_TAB ? tabs + EW_NINT * (EW_DEG + 1) : tabs;
