@@ -25,7 +25,8 @@ def test_real_space_split_moves_more_than_half_of_the_images():
     # images at alpha R >= 4 of those inside 5.2: 1 - (4 / 5.2)^3 = 54.5%
     assert math.isclose(1 - n_fp64 / n_all, 1 - (4 / 5.2) ** 3, rel_tol=1e-12)
     strict, split = bench.kernel_flops("pair_tiles_ewald_real"), bench.kernel_flops("pair_tiles_ewald_real", split=True)
-    assert split < 0.5 * strict
+    # 47 flop x 1.53 images + 39 a pair against 47 x 3.35 + 39: 56%
+    assert 0.5 * strict < split < 0.6 * strict
     # the FP32 kernels' models do not depend on the split
     assert bench.kernel_flops("recip_force32", split=True) == bench.kernel_flops("recip_force32")
     assert bench.kernel_flops("recip_force", split=True) < bench.kernel_flops("recip_force")
